@@ -1,0 +1,138 @@
+/*
+ * ORACLE (test infrastructure only): CPU restatement of vcfpop's Bayesian
+ * STRUCTURE MCMC (src/structure.cpp:405-2166) for REAL = float with
+ * -g_fastsingle=yes, one thread and the scalar math path (-g_simd=none).
+ * Parity pinned against the reference program built from its own sources
+ * (oracle/Makefile -> oracle/_ref/vcfpop) through tests/golden/.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+ * this library; the product never links it.
+ */
+#ifndef STRUCTURE_ORACLE_H
+#define STRUCTURE_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A dataset after the reference's locus sort (structure.cpp:2349-2381) and
+ * grouping of individuals by population (filter.cpp:300-345). */
+typedef struct {
+    int32_t N;            /* individuals */
+    int64_t L;            /* loci */
+    int32_t S;            /* populations (sampling locations) */
+    int32_t vmax;         /* max copies stored per call (>= maxploidy) */
+    int32_t maxploidy;    /* max ploidy of a typed call (function.cpp:4906-4912) */
+    int32_t maxK;         /* max alleles at a locus */
+    int64_t KT;           /* total alleles */
+    const int32_t* k;     /* [L] alleles per locus */
+    const int64_t* off;   /* [L] allele_freq_offset */
+    const uint8_t* gcopies; /* [L*N] typed copies of each call, 0 = missing */
+    const uint8_t* galleles;/* [L*N*vmax] allele index per copy, ascending */
+    const int64_t* vt;    /* [N] typed allele copies per individual */
+    const int32_t* popid; /* [N] population of each individual */
+    const int32_t* pop_ind0; /* [S] first individual of each population */
+    const int32_t* pop_nind; /* [S] individuals per population */
+    const float* totfreq; /* [KT] total-population allele frequency (F-model init) */
+    const int32_t* nhaplo;/* [L] typed copies per locus (F-model init) */
+    int64_t coprime;      /* structure_loc_coprime (structure.cpp:2384-2386) */
+} orc_data;
+
+/* Mirrors BAYESIAN<REAL>::ReadPar (structure.cpp:405-464). */
+typedef struct {
+    int32_t K;
+    int32_t admix, locpriori, fmodel;
+    int32_t nburnin, nreps, nthinning, nadmburnin;   /* nadmburnin: flag value */
+    int32_t writelnl;
+    double lambda, stdlambda, maxlambda;
+    int32_t inferlambda, difflambda;
+    double alpha, stdalpha, maxalpha, alphapriora, alphapriorb;
+    int32_t metrofreq, inferalpha, diffalpha, uniformalpha;
+    double r, maxr, epsr, epseta, epsgamma;
+    double pmeanf, pstdf, stdf;
+    int32_t fsame;
+    uint64_t seed;        /* HashULong(g_seed + run id) */
+} orc_params;
+
+typedef struct orc_chain orc_chain;
+
+/* Chain state, field by field as BAYESIAN<float> (structure.h:50-170). */
+struct orc_chain {
+    orc_params P;
+    const orc_data* D;
+    int32_t K, N, S, nburnin, nreps, nadmburnin, nthinning;
+    int64_t L, KT;
+    float *Freq, *FreqM, *FreqA;
+    double* Lambda;
+    int64_t* MiSum;     /* becomes double after arrange (UnifyInt64ToDouble) */
+    uint16_t* Z;
+    int64_t* Mi;
+    float* Q;
+    int32_t* Ni;
+    double* Alpha;
+    double *f, *F;
+    double *Eta, *Gamma;
+    float* Di;
+    double *AlphaLocal, *SumAlpha;
+    float *fbuf1, *fbuf2;
+    double *bufNK1, *bufNK2, *bufN1, *bufN2;
+    float* bufK;
+    double r;
+    int32_t m, nr, nlnL, rlen;
+    double* lnL;
+    double* rout;
+    int64_t* kdis;
+    int32_t binaryq, singlez;
+};
+
+/* ---- datasets ---- */
+typedef struct orc_owned_data orc_owned_data;
+/* Build from per-copy allele arrays in INPUT locus order:
+ *   G[l*N*vmax + i*vmax + c] allele index, or -1 when missing / absent copy
+ *   ploidy[i] copies in each individual's calls (missing calls keep it)
+ *   k[l] alleles per locus. Individuals must already be grouped by pop.
+ * Applies the reference's genotype-id counting, locus sort and offsets. */
+orc_owned_data* orc_data_build(int32_t N, int64_t L, int32_t vmax, const int8_t* G,
+                               const int32_t* ploidy, const int32_t* k,
+                               const int32_t* popid, int32_t S);
+const orc_data* orc_data_view(const orc_owned_data* d);
+const int64_t* orc_data_order(const orc_owned_data* d); /* sorted -> input locus */
+void orc_data_free(orc_owned_data* d);
+
+/* ---- chains ---- */
+orc_chain* orc_chain_new(const orc_data* D, const orc_params* P);
+void orc_chain_free(orc_chain* c);
+void orc_init(orc_chain* c);            /* InitFix, InitAdmix, InitLocPriori, InitFmodel */
+void orc_sweep(orc_chain* c);           /* one iteration m (structure.cpp:2124-2153), m++ */
+void orc_arrange(orc_chain* c);         /* structure.cpp:1860-1869 */
+void orc_run(orc_chain* c);             /* init + all sweeps + arrange */
+
+/* individual steps at the chain's current m */
+void orc_update_p(orc_chain* c);
+void orc_update_q(orc_chain* c);
+void orc_update_q_noadmix(orc_chain* c);
+void orc_update_q_admix(orc_chain* c);
+void orc_update_q_metro(orc_chain* c);
+void orc_update_locpriori(orc_chain* c);
+void orc_update_z(orc_chain* c);
+void orc_update_z_noadmix(orc_chain* c);
+void orc_update_z_admix(orc_chain* c);
+void orc_update_alpha(orc_chain* c);
+void orc_update_a(orc_chain* c);
+void orc_update_f(orc_chain* c);
+void orc_record(orc_chain* c);
+double orc_record_lnl(orc_chain* c);    /* RecordCPU likelihood only, no side effects */
+/* LL[i*K+k] = sum log p of UpdateQNoAdmix before PolyLog (no side effects
+ * on the chain except scratch). out must hold N*K doubles. */
+void orc_loglik_noadmix(orc_chain* c, double* out);
+
+/* Output files in the reference's format (structure.cpp:86-401). */
+int orc_write_structure(orc_chain* c, const char* out_prefix, int rep, int id,
+                        const char* const* ind_names, const char* const* pop_names,
+                        const char* const* loc_names, int decimal, int diversity);
+uint32_t orc_hash_ulong_c(uint64_t v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
