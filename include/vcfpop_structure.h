@@ -1,0 +1,177 @@
+/*
+ * vcfpop STRUCTURE sweep on one GB300 -- the drop-in C ABI.
+ *
+ * The reference (vcfpop v1.08b) has no library boundary for this path; it is
+ * reached through the -structure flag block and the BAYESIAN<REAL> step
+ * methods, with the device crossing inside BAYESIAN<REAL>::*CUDA() and the
+ * extern "C" helpers of src/structureCUDA.h:6-52. Each entry point below names
+ * the reference interface it replaces.
+ *
+ * Every call returns 0 on success or a negative VP_E* code; vp_last_error()
+ * gives the message of the calling thread's last failure. No call exits the
+ * process (the reference's checkErrors exits, src/structureCUDA.cpp:183-196).
+ * A context is thread-compatible, not thread-safe: one host thread drives it.
+ */
+#ifndef VCFPOP_STRUCTURE_H
+#define VCFPOP_STRUCTURE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VP_OK 0
+#define VP_E_ARG (-1)      /* invalid argument or size */
+#define VP_E_CUDA (-2)     /* CUDA runtime failure (message has the CUDA error) */
+#define VP_E_MEM (-3)      /* device or host allocation failed */
+#define VP_E_STATE (-4)    /* call not valid in the object's current state */
+#define VP_E_NODEV (-5)    /* no CUDA device / extension not usable */
+
+/* random-number streams */
+#define VP_RNG_REFERENCE 0 /* the reference's xorshift streams, draw for draw */
+#define VP_RNG_COUNTER 1   /* Philox counter streams: every step fully parallel */
+
+/* likelihood form for no-admixture chains */
+#define VP_FORM_PLAIN 0    /* FP32 per-individual stream over loci */
+#define VP_FORM_TC 1       /* tensor-core contraction, split-BF16 log-frequencies */
+
+/* ---- input genotypes ---------------------------------------------------- */
+/* Replaces the loader's genotype store (src/function.h:53-330, GENO_READER
+ * src/function.cpp:3499-3568) as the input of CalcBayesian: per call, the
+ * allele index of each copy in ascending order (unphased), -1 for missing. */
+typedef struct {
+    int32_t n_ind;          /* N */
+    int64_t n_loc;          /* L, input order (before filtering and sorting) */
+    int32_t vmax;           /* copies stored per call */
+    const int8_t* alleles;  /* [L][N][vmax] allele per copy, -1 = missing/absent;
+                               may be NULL when packed2 is given */
+    const uint32_t* packed2;/* optional biallelic-diploid form: [L][ceil(N/16)] words,
+                               2 bits per call = count of allele 1, 3 = missing */
+    const int32_t* ploidy;  /* [N] copies per call of each individual */
+    const int32_t* n_alleles; /* [L] alleles per locus (REF + ALTs) */
+    const int32_t* popid;   /* [N] population index, individuals grouped by population */
+    int32_t n_pop;          /* S */
+} vp_input;
+
+typedef struct vp_dataset vp_dataset;
+
+/* Filter, sort and index the loci as CalcBayesian does before its runs:
+ * monomorphic loci removed (src/filter.cpp:102-131), loci sorted by genotype-id
+ * bit width (src/structure.cpp:2202-2295), allele offsets (2374-2381).
+ * Host-only; no GPU needed. */
+int vp_dataset_prepare(const vp_input* in, vp_dataset** out);
+
+typedef struct {
+    int32_t n_ind, n_pop, maxploidy, max_alleles, packed2;
+    int64_t n_loc, n_alleles_total;  /* L after filtering, KT */
+    int64_t coprime;
+} vp_dataset_info;
+int vp_dataset_info_get(const vp_dataset* ds, vp_dataset_info* info);
+/* sorted position -> input locus index, L entries */
+int vp_dataset_order(const vp_dataset* ds, int64_t* order);
+void vp_dataset_free(vp_dataset* ds);
+
+/* ---- device context ------------------------------------------------------ */
+typedef struct vp_ctx vp_ctx;
+/* Upload the packed genotype matrix once (replaces CopyStructureMemory,
+ * src/structureCUDA.cpp:969-1094, and its per-device replicas). */
+int vp_open(const vp_dataset* ds, int device, vp_ctx** out);
+int vp_close(vp_ctx* ctx);
+int vp_sync(vp_ctx* ctx);
+
+/* ---- chains ---------------------------------------------------------------- */
+/* One (K, replicate) run: the fields of BAYESIAN<REAL>::ReadPar
+ * (src/structure.cpp:405-464). Flags use 1 = yes, 0 = no. */
+typedef struct {
+    int32_t K;
+    int32_t admix, locpriori, fmodel;
+    int32_t nburnin, nreps, nthinning, nadmburnin;
+    int32_t writelnl;
+    double lambda, stdlambda, maxlambda;
+    int32_t inferlambda, difflambda;
+    double alpha, stdalpha, maxalpha, alphapriora, alphapriorb;
+    int32_t metrofreq, inferalpha, diffalpha, uniformalpha;
+    double r, maxr, epsr, epseta, epsgamma;
+    double pmeanf, pstdf, stdf;
+    int32_t fsame;
+    uint64_t seed;          /* HashULong(g_seed + run id), see vp_run_seed() */
+    int32_t rng;            /* VP_RNG_* */
+    int32_t form;           /* VP_FORM_* */
+} vp_params;
+
+/* Defaults of the -structure_* block (src/parameters.cpp:584-627). */
+void vp_params_default(vp_params* p);
+/* The reference's per-run seed HashULong(g_seed + id) (src/structure.cpp:463). */
+uint64_t vp_run_seed(int64_t g_seed, int32_t run_id);
+
+typedef struct vp_chain vp_chain;
+/* Allocate a run's device state and initialise it (InitFix, InitAdmix,
+ * InitLocPriori, InitFmodel: src/structure.cpp:466-708). */
+int vp_chain_create(vp_ctx* ctx, const vp_params* p, vp_chain** out);
+int vp_chain_destroy(vp_chain* c);
+
+/* Advance chains by nsweeps MCMC iterations each (the loop body of
+ * BAYESIAN<REAL>::MCMC, src/structure.cpp:2124-2153). Chains that share a
+ * context run their sweeps as shared launches. Asynchronous on the context's
+ * stream; vp_sync waits. */
+int vp_run(vp_chain** chains, int32_t nchains, int32_t nsweeps);
+
+/* Run every remaining sweep of every chain, then Arrange()
+ * (src/structure.cpp:1860-1869). */
+int vp_finish(vp_chain** chains, int32_t nchains);
+
+typedef struct {
+    int32_t K, N, S, nburnin, nreps, nthinning, nr, nlnl, rlen;
+    int64_t KT;
+    uint64_t seed;
+    double* rout;      /* [rlen] mean lnL, E[lnL^2], var, lnP(D), parameter means */
+    double* lnl;       /* [nlnl] recorded likelihoods (writelnl) */
+    float* Q;          /* [N*K] final admixture proportions */
+    double* ancestry;  /* [N*K] normalised MiSum */
+    float* freqm;      /* [K*KT] mean allele frequencies */
+} vp_result;
+/* Copy a finished chain's results into caller-owned buffers (any pointer
+ * may be NULL to skip it). Sizes come from vp_chain_sizes. */
+int vp_chain_sizes(vp_chain* c, vp_result* sizes);
+int vp_chain_result(vp_chain* c, vp_result* out);
+
+/* ---- single steps and state access (parity tests, debugging) ------------- */
+#define VP_STEP_UPDATEP 1
+#define VP_STEP_UPDATEQ 2
+#define VP_STEP_LOCPRIORI 3
+#define VP_STEP_UPDATEZ 4
+#define VP_STEP_ALPHA 5
+#define VP_STEP_UPDATEA 6
+#define VP_STEP_UPDATEF 7
+#define VP_STEP_RECORD 8
+#define VP_STEP_NEXT 9      /* m += 1 */
+#define VP_STEP_LOGLIK 10   /* no-admix log-likelihood LL[N*K] only (no draws) */
+
+#define VP_F_FREQ 1     /* float [K*KT] */
+#define VP_F_Q 2        /* float [N*K] */
+#define VP_F_Z 3        /* uint16 [N] */
+#define VP_F_NI 4       /* int32 [K*KT] */
+#define VP_F_MI 5       /* int32 [N*K] */
+#define VP_F_LL 6       /* double [N*K] last log-likelihood */
+#define VP_F_ALPHA 7    /* double [K] */
+#define VP_F_M 8        /* int32 [1] sweep index */
+#define VP_F_LNL 9      /* double [1] last sweep's likelihood */
+#define VP_F_FREQA 10   /* float [3*KT] */
+#define VP_F_FF 11      /* double [2*K]: f then F */
+#define VP_F_LOCP 12    /* double: r, Eta[K], Gamma[S*K], AlphaLocal[S*K], SumAlpha[S] */
+#define VP_F_DI 13      /* float [S*K] */
+#define VP_F_METRO 14   /* double [N] last Metropolis log ratio */
+int vp_chain_step(vp_chain* c, int32_t step);
+int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes);
+int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t bytes);
+
+/* Kernel launches issued by this library since the context was opened. */
+int64_t vp_launch_count(vp_ctx* ctx);
+
+const char* vp_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1038,3 +1038,46 @@ int orc_write_structure(orc_chain* c, const char* prefix, int rep, int id,
     fclose(f);
     return 0;
 }
+
+/* ================= test access ================= */
+void* orc_field(orc_chain* c, int f, int64_t* n) {
+    int64_t K = c->K, N = c->N, KT = c->KT, S = c->S;
+    switch (f) {
+        case 1: *n = K * KT; return c->Freq;
+        case 2: *n = N * K; return c->Q;
+        case 3: *n = N; return c->Z;
+        case 4: *n = K * KT; return c->Ni;
+        case 5: *n = N * K; return c->Mi;
+        case 6: *n = N * K; return c->bufNK1;
+        case 7: *n = K; return c->Alpha;
+        case 10: *n = KT; return c->FreqA;
+        case 11: *n = c->f ? K : 0; return c->f;
+        case 12: *n = c->F ? K : 0; return c->F;
+        case 13: *n = c->Di ? S * K : 0; return c->Di;
+        case 14: *n = N; return c->bufN1;
+        case 15: *n = c->Eta ? K : 0; return c->Eta;
+        case 16: *n = c->Gamma ? S * K : 0; return c->Gamma;
+        case 17: *n = c->AlphaLocal ? S * K : 0; return c->AlphaLocal;
+        case 18: *n = c->SumAlpha ? S : 0; return c->SumAlpha;
+        case 19: *n = c->rlen; return c->rout;
+        case 20: *n = c->nlnL; return c->lnL;
+        case 21: *n = N * K; return c->MiSum;
+        case 22: *n = K * KT; return c->FreqM;
+    }
+    *n = 0;
+    return NULL;
+}
+int32_t* orc_m(orc_chain* c) { return &c->m; }
+double* orc_r(orc_chain* c) { return &c->r; }
+int32_t* orc_binaryq(orc_chain* c) { return &c->binaryq; }
+const void* orc_data_field(const orc_data* d, int f, int64_t* n) {
+    switch (f) {
+        case 1: *n = d->L; return d->k;
+        case 2: *n = d->L; return d->off;
+        case 3: *n = d->N; return d->vt;
+        case 4: *n = d->L * d->N; return d->gcopies;
+        case 5: *n = d->L * d->N * d->vmax; return d->galleles;
+    }
+    *n = 0;
+    return 0;
+}

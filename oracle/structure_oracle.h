@@ -132,6 +132,18 @@ int orc_write_structure(orc_chain* c, const char* out_prefix, int rep, int id,
                         const char* const* loc_names, int decimal, int diversity);
 uint32_t orc_hash_ulong_c(uint64_t v);
 
+/* Raw access to chain state for tests; field ids follow include/vcfpop_structure.h
+ * (1 Freq f32, 2 Q f32, 3 Z u16, 4 Ni i32, 5 Mi i64, 6 LL f64 (bufNK1), 7 Alpha f64,
+ *  10 FreqA f32, 11 f f64, 12 F f64, 13 Di f32, 14 Metropolis ratio f64 (bufN1),
+ *  15 Eta f64, 16 Gamma f64, 17 AlphaLocal f64, 18 SumAlpha f64, 19 rout f64,
+ *  20 lnL trace f64, 21 MiSum i64, 22 FreqM f32). *n receives the element count. */
+void* orc_field(orc_chain* c, int field, int64_t* n);
+int32_t* orc_m(orc_chain* c);
+double* orc_r(orc_chain* c);
+int32_t* orc_binaryq(orc_chain* c);
+/* dataset arrays: 1 k, 2 off(i64), 3 vt(i64), 4 gcopies(u8), 5 galleles(u8) */
+const void* orc_data_field(const orc_data* d, int field, int64_t* n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,174 @@
+"""ctypes handle on the oracle (oracle/_build/liborc.so): test infrastructure.
+
+The oracle is the CPU restatement of the reference's STRUCTURE path, pinned
+byte-for-byte to the reference program by tests/test_oracle_golden.py. Tests use
+it as the checker for the GPU library, never the other way round.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIBPATH = os.path.join(ROOT, "oracle", "_build", "liborc.so")
+_lib = None
+
+
+class OrcParams(C.Structure):
+    _fields_ = [("K", C.c_int32), ("admix", C.c_int32), ("locpriori", C.c_int32), ("fmodel", C.c_int32),
+                ("nburnin", C.c_int32), ("nreps", C.c_int32), ("nthinning", C.c_int32), ("nadmburnin", C.c_int32),
+                ("writelnl", C.c_int32),
+                ("lambda_", C.c_double), ("stdlambda", C.c_double), ("maxlambda", C.c_double),
+                ("inferlambda", C.c_int32), ("difflambda", C.c_int32),
+                ("alpha", C.c_double), ("stdalpha", C.c_double), ("maxalpha", C.c_double),
+                ("alphapriora", C.c_double), ("alphapriorb", C.c_double),
+                ("metrofreq", C.c_int32), ("inferalpha", C.c_int32), ("diffalpha", C.c_int32),
+                ("uniformalpha", C.c_int32),
+                ("r", C.c_double), ("maxr", C.c_double), ("epsr", C.c_double), ("epseta", C.c_double),
+                ("epsgamma", C.c_double), ("pmeanf", C.c_double), ("pstdf", C.c_double), ("stdf", C.c_double),
+                ("fsame", C.c_int32), ("seed", C.c_uint64)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all"])
+        L = C.CDLL(LIBPATH)
+        P = C.c_void_p
+        L.orc_data_build.restype = P
+        L.orc_data_build.argtypes = [C.c_int32, C.c_int64, C.c_int32, P, P, P, P, C.c_int32]
+        L.orc_data_view.restype = P
+        L.orc_data_view.argtypes = [P]
+        L.orc_data_order.restype = C.POINTER(C.c_int64)
+        L.orc_data_order.argtypes = [P]
+        L.orc_data_free.argtypes = [P]
+        L.orc_chain_new.restype = P
+        L.orc_chain_new.argtypes = [P, C.POINTER(OrcParams)]
+        L.orc_chain_free.argtypes = [P]
+        for f in ["orc_init", "orc_sweep", "orc_arrange", "orc_run", "orc_update_p", "orc_update_q",
+                  "orc_update_q_noadmix", "orc_update_q_admix", "orc_update_q_metro", "orc_update_locpriori",
+                  "orc_update_z", "orc_update_z_noadmix", "orc_update_z_admix", "orc_update_alpha", "orc_update_a",
+                  "orc_update_f", "orc_record"]:
+            getattr(L, f).argtypes = [P]
+            getattr(L, f).restype = None
+        L.orc_record_lnl.argtypes = [P]
+        L.orc_record_lnl.restype = C.c_double
+        L.orc_loglik_noadmix.argtypes = [P, P]
+        L.orc_field.restype = P
+        L.orc_field.argtypes = [P, C.c_int, C.POINTER(C.c_int64)]
+        L.orc_data_field.restype = P
+        L.orc_data_field.argtypes = [P, C.c_int, C.POINTER(C.c_int64)]
+        L.orc_m.restype = C.POINTER(C.c_int32)
+        L.orc_m.argtypes = [P]
+        L.orc_r.restype = C.POINTER(C.c_double)
+        L.orc_r.argtypes = [P]
+        L.orc_binaryq.restype = C.POINTER(C.c_int32)
+        L.orc_binaryq.argtypes = [P]
+        L.orc_hash_ulong_c.restype = C.c_uint32
+        L.orc_hash_ulong_c.argtypes = [C.c_uint64]
+        _lib = L
+    return _lib
+
+
+FIELD_DT = {1: np.float32, 2: np.float32, 3: np.uint16, 4: np.int32, 5: np.int64, 6: np.float64, 7: np.float64,
+            10: np.float32, 11: np.float64, 12: np.float64, 13: np.float32, 14: np.float64, 15: np.float64,
+            16: np.float64, 17: np.float64, 18: np.float64, 19: np.float64, 20: np.float64, 21: np.int64,
+            22: np.float32}
+NAMES = dict(FREQ=1, Q=2, Z=3, NI=4, MI=5, LL=6, ALPHA=7, FREQA=10, f=11, F=12, DI=13, METRO=14, ETA=15,
+             GAMMA=16, ALPHALOCAL=17, SUMALPHA=18, ROUT=19, LNL=20, MISUM=21, FREQM=22)
+
+
+class Data:
+    def __init__(self, d: dict, n_pop=None):
+        G = np.ascontiguousarray(d["G"], dtype=np.int8)
+        self.G = G
+        self.ploidy = np.ascontiguousarray(d["ploidy"], dtype=np.int32)
+        self.k = np.ascontiguousarray(d["k"], dtype=np.int32)
+        self.pop = np.ascontiguousarray(d["pop"], dtype=np.int32)
+        self.S = int(n_pop if n_pop is not None else self.pop.max() + 1)
+        L, N, vmax = G.shape
+        self.h = lib().orc_data_build(N, L, vmax, G.ctypes.data, self.ploidy.ctypes.data, self.k.ctypes.data,
+                                      self.pop.ctypes.data, self.S)
+        self.view = lib().orc_data_view(self.h)
+        self.N = N
+
+    def order(self, L):
+        return np.ctypeslib.as_array(lib().orc_data_order(self.h), shape=(L,)).copy()
+
+    def field(self, f, dt):
+        n = C.c_int64()
+        p = lib().orc_data_field(self.view, f, C.byref(n))
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), shape=(n.value,)).copy()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_data_free(self.h)
+            self.h = None
+
+
+def params(K, seed, **kw):
+    p = OrcParams()
+    p.K = K
+    p.nburnin, p.nreps, p.nthinning, p.nadmburnin = 1000, 10000, 10, 500
+    p.lambda_, p.stdlambda, p.maxlambda = 1, 0.3, 10
+    p.alpha, p.stdalpha, p.maxalpha, p.alphapriora, p.alphapriorb = 1, 0.025, 10, 0.05, 0.001
+    p.metrofreq, p.inferalpha, p.diffalpha, p.uniformalpha = 10, 1, 0, 1
+    p.r, p.maxr, p.epsr, p.epseta, p.epsgamma = 1, 20, 0.1, 0.025, 0.025
+    p.pmeanf, p.pstdf, p.stdf, p.fsame = 0.01, 0.05, 0.05, 0
+    p.seed = seed
+    alias = dict(f="fmodel", singlef="fsame", stdr="epsr", **{"lambda": "lambda_"})
+    for k, v in kw.items():
+        setattr(p, alias.get(k, k), int(v) if isinstance(v, bool) else v)
+    return p
+
+
+class Chain:
+    def __init__(self, data: Data, p: OrcParams):
+        self.data = data
+        self.p = p
+        self.h = lib().orc_chain_new(data.view, C.byref(p))
+
+    def init(self):
+        lib().orc_init(self.h)
+
+    def field(self, name):
+        f = NAMES[name]
+        n = C.c_int64()
+        ptr = lib().orc_field(self.h, f, C.byref(n))
+        if not ptr or n.value == 0:
+            return np.zeros(0, FIELD_DT[f])
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(FIELD_DT[f]))),
+                                     shape=(n.value,))
+
+    def get(self, name):
+        return self.field(name).copy()
+
+    def set(self, name, v):
+        a = self.field(name)
+        a[:] = np.asarray(v, dtype=a.dtype).reshape(-1)
+
+    @property
+    def m(self):
+        return lib().orc_m(self.h)[0]
+
+    @m.setter
+    def m(self, v):
+        lib().orc_m(self.h)[0] = v
+
+    @property
+    def r(self):
+        return lib().orc_r(self.h)[0]
+
+    def step(self, name):
+        getattr(lib(), "orc_" + name)(self.h)
+
+    def loglik(self):
+        out = np.zeros(self.data.N * self.p.K)
+        lib().orc_loglik_noadmix(self.h, out.ctypes.data)
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_chain_free(self.h)
+            self.h = None

@@ -1,0 +1,89 @@
+"""CPU checks of the C ABI and the host logic (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from vcfpop_gb300 import _lib as B
+from vcfpop_gb300 import structure as S
+from vcfpop_gb300 import synth
+
+from . import orc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    hdr = open(os.path.join(ROOT, "include", "vcfpop_structure.h")).read()
+    declared = sorted(set(re.findall(r"\b(vp_[a-z0-9_]+)\s*\(", hdr)))
+    assert declared, "no declarations found"
+    L = B.lib()
+    for name in declared:
+        assert hasattr(L, name), f"{name} declared but not exported"
+    assert set(declared) == set(B.EXPORTS)
+
+
+def test_run_seed_matches_reference_hash():
+    for g, i in [(1, 1), (7, 3), (0, 1), (123456, 42)]:
+        assert S.run_seed(g, i) == orc.lib().orc_hash_ulong_c(g + i)
+    assert S.run_seed(1, 1) == 4273950213  # Seed= line of the reference's c1 run file
+
+
+def _compare_dataset(d, packed):
+    ds = S.Dataset.from_synth(d, packed=packed)
+    od = orc.Data(d)
+    L = ds.L
+    assert np.array_equal(ds.order(), od.order(L))
+    k_or = od.field(1, np.int32)
+    assert len(k_or) == L
+    return ds, od
+
+
+@pytest.mark.parametrize("packed", [True, False])
+def test_dataset_prepare_matches_oracle_biallelic(packed):
+    d = synth.fmodel(11, 150, 900, 3, 0.1, 0.05)
+    _compare_dataset(d, packed)
+
+
+def test_dataset_prepare_matches_oracle_polyploid():
+    rng = np.random.default_rng(1)
+    d = synth.fmodel(12, 90, 400, 3, 0.08, 0.03, ploidy=np.array([2, 4, 6] * 30),
+                     n_alleles=rng.integers(2, 9, 400), anc_alpha=1.0, loc_ids=np.repeat(np.arange(3), 30),
+                     loc_alpha=1.0)
+    ds, od = _compare_dataset(d, False)
+    assert ds.maxploidy == 6
+    assert ds.KT == int(od.field(1, np.int32).sum())
+
+
+def test_dataset_rejects_bad_input():
+    with pytest.raises(B.VpError):
+        S.Dataset(np.array([2, 2], np.int32), np.array([2], np.int32), np.array([1, 0], np.int32), 2,
+                  G=np.zeros((1, 2, 2), np.int8))  # populations not grouped
+
+
+def test_all_monomorphic_rejected():
+    G = np.zeros((5, 10, 2), np.int8)
+    with pytest.raises(B.VpError, match="monomorphic"):
+        S.Dataset(np.full(10, 2, np.int32), np.full(5, 2, np.int32), np.zeros(10, np.int32), 1, G=G)
+
+
+def test_open_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    d = synth.fmodel(3, 40, 100, 2, 0.1, 0.0)
+    ds = S.Dataset.from_synth(d)
+    with pytest.raises(B.VpError, match="no CUDA device"):
+        S.Context(ds)
+
+
+def test_pack2_roundtrip():
+    d = synth.fmodel(5, 37, 50, 2, 0.1, 0.2)
+    P = S.pack2(d["G"])
+    for l in range(50):
+        for i in range(37):
+            code = (int(P[l, i // 16]) >> (2 * (i % 16))) & 3
+            g = d["G"][l, i]
+            assert code == (3 if g[0] < 0 else int(g[0]) + int(g[1]))

@@ -1,0 +1,110 @@
+"""ctypes binding of libvcfpop_structure.so (declared in include/vcfpop_structure.h).
+
+This is the same binding a Python caller of the reference's STRUCTURE path would
+add: plain pointers and sizes, integer status codes turned into exceptions.
+The library is the product path; there is no Python or CPU fallback, so a
+missing or unloadable library raises.
+"""
+import ctypes as C
+import os
+
+from .build import LIB
+
+VP_RNG_REFERENCE, VP_RNG_COUNTER = 0, 1
+VP_FORM_PLAIN, VP_FORM_TC = 0, 1
+
+STEP = dict(UPDATEP=1, UPDATEQ=2, LOCPRIORI=3, UPDATEZ=4, ALPHA=5, UPDATEA=6, UPDATEF=7, RECORD=8, NEXT=9,
+            LOGLIK=10)
+FIELD = dict(FREQ=1, Q=2, Z=3, NI=4, MI=5, LL=6, ALPHA=7, M=8, LNL=9, FREQA=10, FF=11, LOCP=12, DI=13, METRO=14)
+
+
+class VpInput(C.Structure):
+    _fields_ = [("n_ind", C.c_int32), ("n_loc", C.c_int64), ("vmax", C.c_int32),
+                ("alleles", C.c_void_p), ("packed2", C.c_void_p), ("ploidy", C.c_void_p),
+                ("n_alleles", C.c_void_p), ("popid", C.c_void_p), ("n_pop", C.c_int32)]
+
+
+class VpDatasetInfo(C.Structure):
+    _fields_ = [("n_ind", C.c_int32), ("n_pop", C.c_int32), ("maxploidy", C.c_int32), ("max_alleles", C.c_int32),
+                ("packed2", C.c_int32), ("n_loc", C.c_int64), ("n_alleles_total", C.c_int64), ("coprime", C.c_int64)]
+
+
+class VpParams(C.Structure):
+    _fields_ = [("K", C.c_int32), ("admix", C.c_int32), ("locpriori", C.c_int32), ("fmodel", C.c_int32),
+                ("nburnin", C.c_int32), ("nreps", C.c_int32), ("nthinning", C.c_int32), ("nadmburnin", C.c_int32),
+                ("writelnl", C.c_int32),
+                ("lambda_", C.c_double), ("stdlambda", C.c_double), ("maxlambda", C.c_double),
+                ("inferlambda", C.c_int32), ("difflambda", C.c_int32),
+                ("alpha", C.c_double), ("stdalpha", C.c_double), ("maxalpha", C.c_double),
+                ("alphapriora", C.c_double), ("alphapriorb", C.c_double),
+                ("metrofreq", C.c_int32), ("inferalpha", C.c_int32), ("diffalpha", C.c_int32),
+                ("uniformalpha", C.c_int32),
+                ("r", C.c_double), ("maxr", C.c_double), ("epsr", C.c_double), ("epseta", C.c_double),
+                ("epsgamma", C.c_double),
+                ("pmeanf", C.c_double), ("pstdf", C.c_double), ("stdf", C.c_double),
+                ("fsame", C.c_int32), ("seed", C.c_uint64), ("rng", C.c_int32), ("form", C.c_int32)]
+
+
+class VpResult(C.Structure):
+    _fields_ = [("K", C.c_int32), ("N", C.c_int32), ("S", C.c_int32), ("nburnin", C.c_int32), ("nreps", C.c_int32),
+                ("nthinning", C.c_int32), ("nr", C.c_int32), ("nlnl", C.c_int32), ("rlen", C.c_int32),
+                ("KT", C.c_int64), ("seed", C.c_uint64),
+                ("rout", C.c_void_p), ("lnl", C.c_void_p), ("Q", C.c_void_p), ("ancestry", C.c_void_p),
+                ("freqm", C.c_void_p)]
+
+
+class VpError(RuntimeError):
+    pass
+
+
+_lib = None
+
+# every exported symbol of include/vcfpop_structure.h
+EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_dataset_free", "vp_open",
+           "vp_close", "vp_sync", "vp_params_default", "vp_run_seed", "vp_chain_create", "vp_chain_destroy",
+           "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_step", "vp_chain_get",
+           "vp_chain_set", "vp_launch_count", "vp_last_error"]
+
+
+def lib():
+    """Load the library (building it first if this tree has not)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        from .build import build
+        build()
+    L = C.CDLL(LIB)
+    P = C.c_void_p
+    L.vp_dataset_prepare.argtypes = [C.POINTER(VpInput), C.POINTER(P)]
+    L.vp_dataset_info_get.argtypes = [P, C.POINTER(VpDatasetInfo)]
+    L.vp_dataset_order.argtypes = [P, P]
+    L.vp_dataset_free.argtypes = [P]
+    L.vp_dataset_free.restype = None
+    L.vp_open.argtypes = [P, C.c_int, C.POINTER(P)]
+    L.vp_close.argtypes = [P]
+    L.vp_sync.argtypes = [P]
+    L.vp_params_default.argtypes = [C.POINTER(VpParams)]
+    L.vp_params_default.restype = None
+    L.vp_run_seed.argtypes = [C.c_int64, C.c_int32]
+    L.vp_run_seed.restype = C.c_uint64
+    L.vp_chain_create.argtypes = [P, C.POINTER(VpParams), C.POINTER(P)]
+    L.vp_chain_destroy.argtypes = [P]
+    L.vp_run.argtypes = [C.POINTER(P), C.c_int32, C.c_int32]
+    L.vp_finish.argtypes = [C.POINTER(P), C.c_int32]
+    L.vp_chain_sizes.argtypes = [P, C.POINTER(VpResult)]
+    L.vp_chain_result.argtypes = [P, C.POINTER(VpResult)]
+    L.vp_chain_step.argtypes = [P, C.c_int32]
+    L.vp_chain_get.argtypes = [P, C.c_int32, P, C.c_size_t]
+    L.vp_chain_set.argtypes = [P, C.c_int32, P, C.c_size_t]
+    L.vp_launch_count.argtypes = [P]
+    L.vp_launch_count.restype = C.c_int64
+    L.vp_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        raise VpError(f"vcfpop_structure error {rc}: {lib().vp_last_error().decode()}")
+    return rc

@@ -1,0 +1,1169 @@
+// Kernels of one STRUCTURE sweep. Every kernel takes the chain descriptor from
+// device memory (chains[blockIdx.z] for batched launches) and reads the sweep
+// index m from the chain's control block, so the kernel sequence of a sweep is
+// fixed and can be captured once in a CUDA graph and replayed: steps that do
+// not apply at this m (Metropolis vs Gibbs Q, the no-admixture burn-in switch,
+// thinning) return early on the device.
+#pragma once
+#include "vp_device.cuh"
+
+namespace vp {
+
+constexpr int KG = 16;          // clusters per thread in the likelihood kernels
+constexpr int LL_BLOCK = 128;   // individuals per likelihood CTA
+constexpr int SUB = 32;         // loci per FP32 sub-sum before folding into FP64
+
+struct DevData {
+    int32_t N, S, vmax, maxploidy, maxK, Nw, packed2;
+    int64_t L, KT, coprime;
+    const uint32_t* g2;   // [L][Nw]
+    const uint8_t* gb;    // [L][N][vmax]
+    const int32_t* k;
+    const int64_t* off;
+    const int64_t* vt;
+    const int32_t* popid;
+    const int32_t* pop_ind0;
+    const int32_t* pop_nind;
+    const float* totfreq;
+    const int32_t* nhaplo;
+};
+
+struct Ctl {
+    int32_t m, nr, nlnl, pad;
+    double r;
+    double lnl;           // likelihood of the last sampled labels (no-admixture form)
+};
+
+struct DevChain {
+    DevData D;
+    int32_t K, admix, locpriori, fmodel, nburnin, nreps, nthinning, nadmburnin, writelnl;
+    int32_t metrofreq, inferalpha, diffalpha, uniformalpha, fsame, difflambda, rlen, rng, nchunk, lchunk;
+    int32_t zadm_tn, nlnlp;
+    double lambda, alpha, stdalpha, maxalpha, alphapriora, alphapriorb, maxr, epsr, epseta, epsgamma;
+    double pmeanf, pstdf, stdf;
+    uint64_t seed;
+    Ctl* ctl;
+    float *Freq, *FreqM, *FreqA, *Q, *Qprop, *Di, *lt, *fbuf;
+    uint16_t* Z;
+    int32_t *Mi, *Ni;
+    int64_t* MiSum;
+    double *LLp, *LL, *metro, *metrop, *Alpha, *Lambda, *f, *F, *Eta, *Gamma, *AlphaLocal, *SumAlpha;
+    double *rout, *lnlTrace, *red, *lnlp;
+    Rng64* rstate;
+};
+
+// step ids folded into Philox counters
+enum : uint32_t { ST_INITZ = 1, ST_P = 2, ST_Q = 3, ST_METRO_P = 4, ST_METRO_A = 5, ST_Z = 6, ST_A = 7, ST_INITADM = 8 };
+
+__device__ __forceinline__ bool binaryq_at(const DevChain& c, int m) { return !c.admix && m >= c.nadmburnin; }
+__device__ __forceinline__ bool metro_turn(const DevChain& c, int m) { return c.admix && c.metrofreq > 0 && m % c.metrofreq == 0; }
+__device__ __forceinline__ bool record_at(const DevChain& c, int m) {
+    return (c.writelnl && m < c.nburnin && m % c.nthinning == 0) || (m >= c.nburnin && (m - c.nburnin) % c.nthinning == 0);
+}
+
+// ---------------------------------------------------------------------------
+// block reductions
+template <typename T>
+__device__ T block_sum(T v, T* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh[w] = v;
+    __syncthreads();
+    T r = 0;
+    if (threadIdx.x == 0)
+        for (int j = 0; j < nw; ++j) r += sh[j];
+    __syncthreads();
+    return r;  // valid in thread 0
+}
+
+// ---------------------------------------------------------------------------
+// initialisation: InitFix (src/structure.cpp:466-553), InitLocPriori (651-675),
+// InitFmodel (677-708)
+__global__ void k_init_state(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K;
+    int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t l = tid; l < D.L; l += nt) {
+        int k2 = D.k[l];
+        float v = k2 == 2 ? 0.5f : (float)(1.0 / k2);
+        for (int k = 0; k < K; ++k)
+            for (int a = 0; a < k2; ++a) {
+                int64_t j = k * D.KT + D.off[l] + a;
+                c.Freq[j] = c.fmodel ? (float)c.lambda : v;
+                c.FreqM[j] = 0.f;
+                c.Ni[j] = 0;
+            }
+        if (c.fmodel) {
+            // the total-population frequencies are laid out in pre-sort order but
+            // read with this (sorted) locus' offset and index, as in the reference
+            const float* p2 = D.totfreq + D.off[l];
+            int nh = D.nhaplo[l];
+            for (int a = 0; a < k2; ++a)
+                c.FreqA[D.off[l] + a] = (float)((c.lambda + p2[a] * nh) / (k2 * c.lambda + nh));
+        }
+    }
+    for (int64_t j = tid; j < (int64_t)D.N * K; j += nt) {
+        c.Q[j] = (float)(1.0 / K);
+        c.Mi[j] = 0;
+        c.MiSum[j] = 0;
+    }
+    for (int64_t i = tid; i < D.N; i += nt) c.Z[i] = 0;
+    if (tid < K) {
+        c.Alpha[tid] = c.alpha;
+        c.Lambda[tid] = c.lambda;
+        if (c.fmodel) { c.F[tid] = c.pmeanf; c.f[tid] = (1 - c.pmeanf) / c.pmeanf; }
+        if (c.locpriori && !c.admix) c.Eta[tid] = (double)(1.0 / K);
+    }
+    if (c.locpriori)
+        for (int64_t j = tid; j < (int64_t)D.S * K; j += nt) {
+            c.AlphaLocal[j] = c.alpha;
+            if (!c.admix) { c.Gamma[j] = (double)(1.0 / K); c.Di[j] = 0.f; }
+        }
+    if (c.locpriori)
+        for (int64_t s = tid; s < D.S; s += nt) c.SumAlpha[s] = 0;
+    for (int64_t j = tid; j < c.rlen; j += nt) c.rout[j] = 0;
+    if (tid == 0) { c.ctl->m = 0; c.ctl->nr = 0; c.ctl->nlnl = 0; c.ctl->r = 1; c.ctl->lnl = 0; }
+}
+
+// InitAdmix, single-label form (no admixture, no admixture burn-in):
+// Z_i ~ U{0..K-1} from RNG(seed-1, SALT_INITADM), Mi[i, Z_i] = vt_i
+// (src/structure.cpp:564-573)
+__global__ void k_init_z_single(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const int K = c.K, N = c.D.N;
+    if (c.rng == 0) {
+        if (blockIdx.x || threadIdx.x) return;
+        Rng64 r; r.init(c.seed - 1, VP_SALT_INITADM);
+        for (int i = 0; i < N; ++i) {
+            int z = (int)r.nextn(K);
+            c.Z[i] = (uint16_t)z;
+            c.Mi[i * K + z] = (int32_t)c.D.vt[i];
+        }
+    } else {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+            Philox p; p.init(c.seed, ST_INITZ, (uint32_t)i, 0);
+            int z = (int)(p.next() % (uint32_t)K);
+            c.Z[i] = (uint16_t)z;
+            c.Mi[i * K + z] = (int32_t)c.D.vt[i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// genotype access
+struct Copies {
+    int n;
+    uint8_t a[10];
+};
+__device__ __forceinline__ void load_copies(const DevData& D, int64_t l, int i, Copies& cp) {
+    if (D.packed2) {
+        int code = (D.g2[l * D.Nw + (i >> 4)] >> ((i & 15) * 2)) & 3;
+        if (code == 3) { cp.n = 0; return; }
+        cp.n = 2;
+        cp.a[0] = code == 2 ? 1 : 0;
+        cp.a[1] = code == 0 ? 0 : 1;
+        return;
+    }
+    const uint8_t* g = D.gb + ((size_t)l * D.N + i) * D.vmax;
+    int n = 0;
+    if (g[0] != 0xFF)
+        for (; n < D.vmax && g[n] != 0xFF; ++n) cp.a[n] = g[n];
+    cp.n = n;
+}
+
+// InitAdmix, per-copy form: per locus RNG(seed + l, SALT_INITADM), one draw per
+// typed copy (src/structure.cpp:617-645)
+__global__ void k_init_admix(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K;
+    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (l >= D.L) return;
+    Rng64 r;
+    if (c.rng == 0) r.init(c.seed + l, VP_SALT_INITADM);
+    int64_t o = D.off[l];
+    for (int i = 0; i < D.N; ++i) {
+        Copies cp;
+        load_copies(D, l, i, cp);
+        if (!cp.n) continue;
+        Philox ph;
+        if (c.rng) ph.init(c.seed, ST_INITADM, (uint32_t)l, (uint32_t)i);
+        for (int a = 0; a < cp.n; ++a) {
+            int k2 = c.rng == 0 ? (int)r.nextn(K) : (int)(ph.next() % (uint32_t)K);
+            atomicAdd(&c.Mi[i * K + k2], 1);
+            atomicAdd(&c.Ni[k2 * D.KT + o + cp.a[a]], 1);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// UpdateP (src/structure.cpp:810-862): p_{k,l,.} ~ Dirichlet(prior + Ni).
+// Also writes the lookup table the likelihood kernels read:
+//   packed2: lt[(l*K + k)*4 + code] = code's log-probability (code 3 -> 0)
+//   general: lt[k*KT + off_l + a]   = ln p
+__device__ __forceinline__ float prior_of(const DevChain& c, int k, int64_t j) {
+    if (!c.fmodel) return (float)c.Lambda[k];
+    return c.FreqA[j] * (float)c.f[c.fsame ? 0 : k];
+}
+__device__ __forceinline__ void write_lt(const DevChain& c, int k, int64_t l, const float* p, int k2) {
+    const DevData& D = c.D;
+    if (D.packed2) {
+        float l0 = ln_freq(p[0]), l1 = ln_freq(p[1]);
+        float4 t = make_float4(l0 + l0, l0 + l1, l1 + l1, 0.f);
+        reinterpret_cast<float4*>(c.lt)[l * c.K + k] = t;
+    } else {
+        for (int a = 0; a < k2; ++a) c.lt[k * D.KT + D.off[l] + a] = ln_freq(p[a]);
+    }
+}
+
+// rebuild the lookup table from Freq (after a host-side state import)
+__global__ void k_refresh_lt(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    int64_t kl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (kl >= (int64_t)c.K * D.L) return;
+    int k = (int)(kl / D.L);
+    int64_t l = kl % D.L;
+    write_lt(c, k, l, c.Freq + k * D.KT + D.off[l], D.k[l]);
+}
+
+// reference streams: 128 block streams RNG(seed + m*128 + b, SALT_UPDATEP),
+// each serial over its share of the K*L range
+__global__ void k_update_p_ref(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    int b = threadIdx.x;
+    if (b >= 128) return;
+    int64_t kl0 = (int64_t)(b * K) * D.L / 128, kl1 = (int64_t)((b + 1) * K) * D.L / 128;
+    Rng64 r;
+    r.init(c.seed + (uint64_t)(m * 128 + b), VP_SALT_UPDATEP);
+    float p[64];
+    for (int64_t kl = kl0; kl < kl1; ++kl) {
+        int k = (int)(kl / D.L);
+        int64_t l = kl % D.L;
+        int k2 = D.k[l];
+        int64_t j = k * D.KT + D.off[l];
+        double s = 0;
+        for (int a = 0; a < k2; ++a) {
+            double v = r.gamma((double)prior_of(c, k, D.off[l] + a) + (double)c.Ni[j + a]);
+            p[a] = (float)v;
+            s += v;
+        }
+        float inv = (float)(1.0 / s);
+        for (int a = 0; a < k2; ++a) { p[a] *= inv; c.Freq[j + a] = p[a]; }
+        write_lt(c, k, l, p, k2);
+    }
+}
+
+// counter streams: one thread per (k, l)
+__global__ void k_update_p_ctr(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    int64_t kl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (kl >= (int64_t)K * D.L) return;
+    int k = (int)(kl / D.L);
+    int64_t l = kl % D.L;
+    int k2 = D.k[l];
+    int64_t j = k * D.KT + D.off[l];
+    Philox ph;
+    ph.init(c.seed, ST_P | ((uint32_t)m << 4), (uint32_t)kl, (uint32_t)(kl >> 32));
+    float p[64];
+    float s = 0;
+    for (int a = 0; a < k2; ++a) {
+        float v = ph.gammaf(prior_of(c, k, D.off[l] + a) + (float)c.Ni[j + a]);
+        p[a] = v;
+        s += v;
+    }
+    float inv = 1.f / s;
+    for (int a = 0; a < k2; ++a) { p[a] *= inv; c.Freq[j + a] = p[a]; }
+    write_lt(c, k, l, p, k2);
+}
+
+// ---------------------------------------------------------------------------
+// Log-likelihood of every individual under every cluster (the locus loop of
+// UpdateQNoAdmix, src/structure.cpp:902-932): LL[i,k] = sum over loci and
+// copies of ln p_{k,l,allele}. One thread per individual; grid.y splits the
+// loci into chunks whose FP64 partials are summed in a fixed order later.
+// FP32 sums over SUB loci are folded into FP64 accumulators.
+template <int KC>
+__global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int kgroups, int force) {
+    const DevChain& c = chains[blockIdx.z / kgroups];
+    const int kg0 = (blockIdx.z % kgroups) * KC;
+    const DevData& D = c.D;
+    const int K = c.K;
+    if (!force && !binaryq_at(c, c.ctl->m)) return;
+    const int i = blockIdx.x * LL_BLOCK + threadIdx.x;
+    const int64_t l0 = (int64_t)blockIdx.y * c.lchunk;
+    const int64_t l1 = min(D.L, l0 + c.lchunk);
+    if (l0 >= D.L) return;
+    double accd[KC];
+    float acc[KC];
+#pragma unroll
+    for (int k = 0; k < KC; ++k) { accd[k] = 0; acc[k] = 0.f; }
+    const bool live = i < D.N;
+    int cnt = 0;
+    if (D.packed2) {
+        const float4* T = reinterpret_cast<const float4*>(c.lt);
+        const uint32_t* g = D.g2 + (i >> 4);
+        const int sh = (i & 15) * 2;
+        for (int64_t l = l0; l < l1; ++l) {
+            uint32_t w = live ? __ldg(g + l * D.Nw) : 0xFFFFFFFFu;
+            int code = (w >> sh) & 3;
+            const float* t = reinterpret_cast<const float*>(T + l * K + kg0) + code;
+#pragma unroll
+            for (int k = 0; k < KC; ++k)
+                if (kg0 + k < K) acc[k] += __ldg(t + 4 * k);
+            if (++cnt == SUB) {
+                cnt = 0;
+#pragma unroll
+                for (int k = 0; k < KC; ++k) { accd[k] += acc[k]; acc[k] = 0.f; }
+            }
+        }
+    } else {
+        for (int64_t l = l0; l < l1; ++l) {
+            Copies cp;
+            if (live) load_copies(D, l, i, cp); else cp.n = 0;
+            const float* t = c.lt + D.off[l];
+            for (int a = 0; a < cp.n; ++a) {
+#pragma unroll
+                for (int k = 0; k < KC; ++k)
+                    if (kg0 + k < K) acc[k] += __ldg(t + (int64_t)(kg0 + k) * D.KT + cp.a[a]);
+            }
+            if (++cnt == SUB) {
+                cnt = 0;
+#pragma unroll
+                for (int k = 0; k < KC; ++k) { accd[k] += acc[k]; acc[k] = 0.f; }
+            }
+        }
+    }
+    if (!live) return;
+    double* out = c.LLp + ((int64_t)blockIdx.y * D.N + i) * K;
+#pragma unroll
+    for (int k = 0; k < KC; ++k)
+        if (kg0 + k < K) out[kg0 + k] = accd[k] + (double)acc[k];
+}
+
+// PolyLog (src/statistics.cpp:116-155): draw k with probability proportional
+// to exp(LL_k - max); overwrites ll with the weights.
+__device__ __forceinline__ int polylog(double* ll, int K, double u01, bool ref, Rng64* r) {
+    double mx = -1.79769313486231570e+308, s = VP_MIN_FREQ * K;
+    for (int k = 0; k < K; ++k) if (!(ll[k] < mx)) mx = ll[k];
+    for (int k = 0; k < K; ++k) {
+        double d = ll[k] - mx;
+        ll[k] = d < -23 ? VP_MIN_FREQ : exp(d);
+        s += ll[k];
+    }
+    double t = ref ? r->uniform(0, s) : u01 * s;
+    for (int k = 0; k < K; ++k) {
+        if (t < ll[k]) return k;
+        t -= ll[k];
+    }
+    return K - 1;
+}
+
+// UpdateQNoAdmix label draw (src/structure.cpp:891-900) plus the state the
+// reference rebuilds afterwards: Q one-hot, Mi[i, Z_i] = vt_i
+// (src/structure.cpp:1305-1310), Di for the location prior (1151-1158) and the
+// likelihood of the new labels, sum_i LL[i, Z_i], which is exactly what Record
+// computes for a no-admixture sweep (src/structure.cpp:1902-1938).
+constexpr int SAMPLE_BLOCK = 256;
+__global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain* chains, int force) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, N = D.N, m = c.ctl->m;
+    if (!force && !binaryq_at(c, m)) return;
+    __shared__ double sh[32];
+    double lnl = 0;
+    double ll[64];
+    const bool ref = c.rng == 0;
+    Rng64 r;
+    if (ref) r.init(c.seed + (uint64_t)m, VP_SALT_UPDATEQ);
+    // reference streams are serial over individuals: one thread walks them all
+    for (int i = ref ? 0 : threadIdx.x; i < N; i += ref ? 1 : blockDim.x) {
+        if (ref && threadIdx.x) break;
+        for (int k = 0; k < K; ++k) ll[k] = 0;
+        for (int ch = 0; ch < c.nchunk; ++ch) {
+            const double* p = c.LLp + ((int64_t)ch * N + i) * K;
+            for (int k = 0; k < K; ++k) ll[k] += p[k];
+        }
+        for (int k = 0; k < K; ++k) c.LL[(int64_t)i * K + k] = ll[k];
+        if (force) continue;
+        for (int k = 0; k < K; ++k) c.Q[(int64_t)i * K + k] = 0.f;
+        for (int k = 0; k < K; ++k) c.Mi[(int64_t)i * K + k] = 0;
+        if (D.vt[i] == 0) continue;
+        double lln[64];
+        for (int k = 0; k < K; ++k) lln[k] = ll[k];
+        if (c.locpriori) {
+            const double* g = c.Gamma + D.popid[i] * K;
+            for (int k = 0; k < K; ++k) ll[k] += log(g[k]);
+        }
+        double u = 0;
+        if (!ref) { Philox ph; ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0); u = ph.uniformd(); }
+        int z = polylog(ll, K, u, ref, &r);
+        c.Q[(int64_t)i * K + z] = 1.f;
+        c.Z[i] = (uint16_t)z;
+        c.Mi[(int64_t)i * K + z] = (int32_t)D.vt[i];
+        lnl += lln[z];
+    }
+    if (force) return;
+    double tot = ref ? lnl : block_sum(lnl, sh);
+    if (threadIdx.x == 0) c.ctl->lnl = tot;
+    if (c.locpriori) {
+        __syncthreads();
+        for (int j = threadIdx.x; j < D.S * K; j += blockDim.x) c.Di[j] = 0.f;
+        __syncthreads();
+        // Q is one-hot, so these float sums are exact small integers
+        for (int i = threadIdx.x; i < N; i += blockDim.x)
+            if (D.vt[i]) atomicAdd(&c.Di[D.popid[i] * K + c.Z[i]], 1.f);
+    }
+}
+
+// UpdateZNoAdmix (src/structure.cpp:1257-1301): Ni[k,l,a] = copies of allele a
+// at locus l among individuals labelled k. One warp per locus; per-warp shared
+// histograms take the per-call increments, then the warp writes its row.
+constexpr int COUNT_WARPS = 8;
+__global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevChain* chains, int force) {
+    extern __shared__ int32_t hist[];
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K;
+    if (!force && !binaryq_at(c, c.ctl->m)) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t l = (int64_t)blockIdx.x * COUNT_WARPS + warp;
+    const int hsz = K * D.maxK;
+    int32_t* h = hist + warp * hsz;
+    for (int j = lane; j < hsz; j += 32) h[j] = 0;
+    __syncwarp();
+    if (l < D.L) {
+        if (D.packed2) {
+            const uint32_t* row = D.g2 + l * D.Nw;
+            for (int w = lane; w < D.Nw; w += 32) {
+                uint32_t word = row[w];
+                int i0 = w * 16;
+                for (int j = 0; j < 16 && i0 + j < D.N; ++j) {
+                    int code = (word >> (2 * j)) & 3;
+                    if (code == 3) continue;
+                    int z = c.Z[i0 + j];
+                    if (code != 2) atomicAdd(&h[z * 2 + 0], 2 - code);
+                    if (code != 0) atomicAdd(&h[z * 2 + 1], code);
+                }
+            }
+        } else {
+            int k2 = D.k[l];
+            for (int i = lane; i < D.N; i += 32) {
+                Copies cp;
+                load_copies(D, l, i, cp);
+                int z = c.Z[i];
+                for (int a = 0; a < cp.n; ++a) atomicAdd(&h[z * k2 + cp.a[a]], 1);
+            }
+        }
+    }
+    __syncwarp();
+    if (l < D.L) {
+        int k2 = D.k[l];
+        for (int j = lane; j < K * k2; j += 32) {
+            int k = j / k2, a = j % k2;
+            c.Ni[k * D.KT + D.off[l] + a] = h[k * k2 + a];
+        }
+    }
+}
+
+// Dirichlet draw of one individual's admixture proportions from alpha + counts
+__device__ __forceinline__ void dirichlet_ref(Rng64& r, float* q, const double* a, const int32_t* b, int K) {
+    double s = 0;
+    for (int k = 0; k < K; ++k) {
+        double v = r.gamma(a[k] + (b ? (double)b[k] : 0.0));
+        q[k] = (float)v;
+        s += v;
+    }
+    float inv = (float)(1.0 / s);
+    for (int k = 0; k < K; ++k) q[k] *= inv;
+}
+__device__ __forceinline__ void dirichlet_ctr(Philox& p, float* q, const double* a, const int32_t* b, int K) {
+    float s = 0;
+    for (int k = 0; k < K; ++k) {
+        float v = p.gammaf((float)(a[k] + (b ? (double)b[k] : 0.0)));
+        q[k] = v;
+        s += v;
+    }
+    float inv = 1.f / s;
+    for (int k = 0; k < K; ++k) q[k] *= inv;
+}
+
+// UpdateQAdmix (src/structure.cpp:984-1004): Q_i ~ Dirichlet(alpha + Mi_i),
+// used by the admixture model and the no-admixture burn-in
+__global__ void k_update_q_admix(const DevChain* chains, int force) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    if (!force) {
+        if (c.admix && metro_turn(c, m)) return;
+        if (!c.admix && m >= c.nadmburnin) return;
+    }
+    if (c.rng == 0) {
+        if (blockIdx.x || threadIdx.x) return;
+        Rng64 r; r.init(c.seed + (uint64_t)m, VP_SALT_UPDATEQ);
+        for (int i = 0; i < D.N; ++i)
+            if (D.vt[i])
+                dirichlet_ref(r, c.Q + (int64_t)i * K, c.locpriori ? c.AlphaLocal + D.popid[i] * K : c.Alpha,
+                              c.Mi + (int64_t)i * K, K);
+        return;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
+        if (!D.vt[i]) continue;
+        Philox p; p.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 1);
+        dirichlet_ctr(p, c.Q + (int64_t)i * K, c.locpriori ? c.AlphaLocal + D.popid[i] * K : c.Alpha,
+                      c.Mi + (int64_t)i * K, K);
+    }
+}
+
+// UpdateQMetro (src/structure.cpp:1006-1086): proposals Q'_i ~ Dirichlet(alpha)
+__global__ void k_metro_propose(const DevChain* chains, int force) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    if (!force && !metro_turn(c, m)) return;
+    if (c.rng == 0) {
+        if (blockIdx.x || threadIdx.x) return;
+        Rng64 r; r.init(c.seed + (uint64_t)m, VP_SALT_UPDATEQ);
+        for (int i = 0; i < D.N; ++i)
+            if (D.vt[i])
+                dirichlet_ref(r, c.Qprop + (int64_t)i * K, c.locpriori ? c.AlphaLocal + D.popid[i] * K : c.Alpha,
+                              nullptr, K);
+        *c.rstate = r;  // the acceptance draws continue this stream
+        return;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
+        if (!D.vt[i]) continue;
+        Philox p; p.init(c.seed, ST_METRO_P | ((uint32_t)m << 4), (uint32_t)i, 0);
+        dirichlet_ctr(p, c.Qprop + (int64_t)i * K, c.locpriori ? c.AlphaLocal + D.popid[i] * K : c.Alpha,
+                      nullptr, K);
+    }
+}
+
+// log likelihood ratio of the proposals: sum over loci and copies of
+// ln( sum_k q'_k p / sum_k q_k p ), one thread per individual
+__global__ void __launch_bounds__(LL_BLOCK) k_metro_ratio(const DevChain* chains, int force) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    if (!force && !metro_turn(c, m)) return;
+    const int i = blockIdx.x * LL_BLOCK + threadIdx.x;
+    const int64_t l0 = (int64_t)blockIdx.y * c.lchunk, l1 = min(D.L, l0 + c.lchunk);
+    if (i >= D.N || l0 >= D.L) return;
+    float q1[64], q0[64];
+    for (int k = 0; k < K; ++k) { q1[k] = c.Qprop[(int64_t)i * K + k]; q0[k] = c.Q[(int64_t)i * K + k]; }
+    double accd = 0;
+    float acc = 0.f;
+    int cnt = 0;
+    for (int64_t l = l0; l < l1; ++l) {
+        Copies cp;
+        load_copies(D, l, i, cp);
+        const float* p = c.Freq + D.off[l];
+        for (int a = 0; a < cp.n; ++a) {
+            float s1 = 0.f, s2 = 0.f;
+            for (int k = 0; k < K; ++k) {
+                float pk = p[(int64_t)k * D.KT + cp.a[a]];
+                s1 += q1[k] * pk;
+                s2 += q0[k] * pk;
+            }
+            acc += logf(s1 / s2);
+        }
+        if (++cnt == SUB) { cnt = 0; accd += acc; acc = 0.f; }
+    }
+    c.metrop[(int64_t)blockIdx.y * D.N + i] = accd + (double)acc;
+}
+
+__global__ void k_metro_accept(const DevChain* chains, int force) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    if (!force && !metro_turn(c, m)) return;
+    const bool ref = c.rng == 0;
+    if (ref && (blockIdx.x || threadIdx.x)) return;
+    Rng64 r;
+    if (ref) r = *c.rstate;
+    for (int i = ref ? 0 : blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += ref ? 1 : gridDim.x * blockDim.x) {
+        double d = 0;
+        for (int ch = 0; ch < c.nchunk; ++ch) d += c.metrop[(int64_t)ch * D.N + i];
+        c.metro[i] = d;
+        if (D.vt[i] == 0) continue;
+        double u;
+        bool acc = d >= VP_NZERO;
+        if (!acc) {
+            if (ref) u = r.uniform();
+            else { Philox p; p.init(c.seed, ST_METRO_A | ((uint32_t)m << 4), (uint32_t)i, 0); u = p.uniformd(); }
+            acc = u < exp(d);
+        }
+        if (acc)
+            for (int k = 0; k < K; ++k) c.Q[(int64_t)i * K + k] = c.Qprop[(int64_t)i * K + k];
+    }
+}
+
+// Zero Mi and Ni ahead of the per-copy label draws
+__global__ void k_zero_counts(const DevChain* chains, int force) {
+    const DevChain& c = chains[blockIdx.z];
+    if (!force && binaryq_at(c, c.ctl->m)) return;
+    int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = tid; j < (int64_t)c.D.N * c.K; j += nt) c.Mi[j] = 0;
+    for (int64_t j = tid; j < (int64_t)c.K * c.D.KT; j += nt) c.Ni[j] = 0;
+    for (int64_t j = tid; j < c.nlnlp; j += nt) c.lnlp[j] = 0;
+}
+
+// Poly over float weights (src/statistics.cpp:357-385) with the reference's
+// float/double promotions
+__device__ __forceinline__ int poly_f(const float* w, int K, float u01_or_neg, Rng32* r) {
+    float sx = 0.f;
+    for (int k = 0; k < K; ++k) sx += w[k];
+    float s = sx + VP_MIN_FREQ * K;
+    float t = r ? r->uniform(0.f, s) : u01_or_neg * s;
+    for (int k = 0; k < K; ++k) {
+        if (t < w[k] + VP_MIN_FREQ) return k;
+        t -= w[k] + VP_MIN_FREQ;
+    }
+    return K - 1;
+}
+
+// UpdateZAdmix with reference streams (src/structure.cpp:1350-1438): one
+// thread per locus walks all individuals with RNG<float>(seed + m*L + l,
+// SALT_UPDATEZ), drawing maxploidy numbers per individual whether or not the
+// copies are typed. Also sums ln(sum_k q_k p) over copies: the admixture
+// likelihood Record needs (src/structure.cpp:1917-1925).
+__global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    if (!force && binaryq_at(c, m)) return;
+    __shared__ double sh[32];
+    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double lnl = 0;
+    if (l < D.L) {
+        Rng32 r;
+        r.init(c.seed + (uint64_t)((int64_t)m * D.L + l), VP_SALT_UPDATEZ);
+        int64_t o = D.off[l];
+        float w[64];
+        for (int i = 0; i < D.N; ++i) {
+            Copies cp;
+            load_copies(D, l, i, cp);
+            const float* q = c.Q + (int64_t)i * K;
+            for (int a = 0; a < D.maxploidy; ++a) {
+                if (a >= cp.n) { r.next(); continue; }
+                float sx = 0.f;
+                for (int k = 0; k < K; ++k) { w[k] = q[k] * c.Freq[k * D.KT + o + cp.a[a]]; sx += w[k]; }
+                lnl += (double)logf(sx);
+                int k2 = poly_f(w, K, 0.f, &r);
+                atomicAdd(&c.Mi[i * K + k2], 1);
+                c.Ni[k2 * D.KT + o + cp.a[a]]++;
+            }
+        }
+    }
+    double t = block_sum(lnl, sh);
+    if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
+}
+
+// UpdateZAdmix with counter streams: the CTA takes 32 loci (one per lane) and
+// an individual tile split across its warps; Q of the tile, Mi of the tile and
+// Ni of the 32 loci are staged in shared memory and flushed once.
+constexpr int ZA_WARPS = 8;
+__global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevChain* chains, int force) {
+    extern __shared__ unsigned char smraw[];
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    if (!force && binaryq_at(c, m)) return;
+    const int TN = c.zadm_tn;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int i0 = blockIdx.y * TN;
+    const int nin = min(TN, D.N - i0);
+    float* qs = reinterpret_cast<float*>(smraw);                 // [TN][K]
+    int32_t* mis = reinterpret_cast<int32_t*>(qs + TN * K);      // [TN][K]
+    int32_t* nis = mis + TN * K;                                  // [32][K][maxK]
+    __shared__ double sh[32];
+    for (int j = threadIdx.x; j < nin * K; j += blockDim.x) { qs[j] = c.Q[(int64_t)i0 * K + j]; mis[j] = 0; }
+    for (int j = threadIdx.x; j < 32 * K * D.maxK; j += blockDim.x) nis[j] = 0;
+    __syncthreads();
+    const int64_t l = (int64_t)blockIdx.x * 32 + lane;
+    double lnl = 0;
+    if (l < D.L) {
+        const int64_t o = D.off[l];
+        const int k2n = D.k[l];
+        float w[64];
+        for (int ii = warp; ii < nin; ii += ZA_WARPS) {
+            const int i = i0 + ii;
+            Copies cp;
+            load_copies(D, l, i, cp);
+            if (!cp.n) continue;
+            Philox ph;
+            ph.init(c.seed, ST_Z | ((uint32_t)m << 4), (uint32_t)l, (uint32_t)i);
+            const float* q = qs + ii * K;
+            float lacc = 0.f;
+            for (int a = 0; a < cp.n; ++a) {
+                float sx = 0.f;
+                for (int k = 0; k < K; ++k) { w[k] = q[k] * __ldg(c.Freq + k * D.KT + o + cp.a[a]); sx += w[k]; }
+                lacc += logf(sx);
+                int k2 = poly_f(w, K, ph.uniformf(), nullptr);
+                atomicAdd(&mis[ii * K + k2], 1);
+                atomicAdd(&nis[(lane * K + k2) * D.maxK + cp.a[a]], 1);
+            }
+            lnl += lacc;
+        }
+        (void)k2n;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nin * K; j += blockDim.x)
+        if (mis[j]) atomicAdd(&c.Mi[(int64_t)i0 * K + j], mis[j]);
+    for (int j = threadIdx.x; j < 32 * K * D.maxK; j += blockDim.x) {
+        int v = nis[j];
+        if (!v) continue;
+        int a = j % D.maxK, k = (j / D.maxK) % K, ln = j / (D.maxK * K);
+        int64_t ll = (int64_t)blockIdx.x * 32 + ln;
+        atomicAdd(&c.Ni[k * D.KT + D.off[ll] + a], v);
+    }
+    double t = block_sum(lnl, sh);
+    if (threadIdx.x == 0) c.lnlp[blockIdx.y * gridDim.x + blockIdx.x] = t;
+}
+
+// ---------------------------------------------------------------------------
+// exponent-split log product (src/math2.h:738-894, src/math2.cpp:1030-1116),
+// serial, for the reference-stream Metropolis-Hastings steps
+__device__ __forceinline__ void chargelog_f(int64_t& slog, double& prod, float v) {
+    prod *= (double)v;
+    if (prod < 1e-100 || prod > 1e100) {
+        long long b = __double_as_longlong(prod);
+        slog += ((b & 0x7FF0000000000000ll) >> 52) - 1023;
+        prod = __longlong_as_double((b & (long long)0x800FFFFFFFFFFFFFull) | 0x3FF0000000000000ll);
+    }
+}
+__device__ __forceinline__ void chargelog_d(int64_t& slog, double& prod, double v) {
+    if (v < 1e-100 || v > 1e100) {
+        long long b = __double_as_longlong(v);
+        slog += ((b & 0x7FF0000000000000ll) >> 52) - 1023;
+        v = __longlong_as_double((b & (long long)0x800FFFFFFFFFFFFFull) | 0x3FF0000000000000ll);
+    }
+    prod *= v;
+    if (prod < 1e-100 || prod > 1e100) {
+        long long b = __double_as_longlong(prod);
+        slog += ((b & 0x7FF0000000000000ll) >> 52) - 1023;
+        prod = __longlong_as_double((b & (long long)0x800FFFFFFFFFFFFFull) | 0x3FF0000000000000ll);
+    }
+}
+__device__ __forceinline__ double closelog(int64_t slog, double prod) { return ((double)slog + log2(prod)) * 0.693147180559945; }
+__device__ double logprod_f_serial(const float* a, int64_t n, int64_t sep) {
+    int64_t s = 0; double p = 1;
+    for (int64_t i = 0; i < n; ++i) chargelog_f(s, p, a[i * sep]);
+    return closelog(s, p);
+}
+__device__ double logprod_d_serial(const double* a, int64_t n, int64_t sep) {
+    int64_t s = 0; double p = 1;
+    for (int64_t i = 0; i < n; ++i) chargelog_d(s, p, a[i * sep]);
+    return closelog(s, p);
+}
+
+// Sums of ln Q that UpdateAlpha needs: one sequence per output
+//   inferalpha, one alpha: ln prod Q over all N*K (1 output)
+//   diffalpha:             ln prod Q[., k] (K outputs)
+//   location prior+admix:  ln prod Q[i in s, k] (S*K outputs)
+// Reference streams use the serial exponent-split product (a zero resets its
+// running mantissa, as in the reference); counter streams a parallel sum.
+__global__ void k_logprod_q(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    __shared__ double sh[32];
+    int nseq;
+    if (c.locpriori && c.admix) nseq = D.S * K;
+    else if (c.inferalpha && (c.admix || m < c.nadmburnin)) nseq = c.diffalpha ? K : 1;
+    else return;
+    for (int s = blockIdx.x; s < nseq; s += gridDim.x) {
+        const float* base; int64_t n, sep;
+        if (c.locpriori && c.admix) { int sp = s / K, k = s % K; base = c.Q + (int64_t)D.pop_ind0[sp] * K + k; n = D.pop_nind[sp]; sep = K; }
+        else if (c.diffalpha) { base = c.Q + s; n = D.N; sep = K; }
+        else { base = c.Q; n = (int64_t)D.N * K; sep = 1; }
+        if (c.rng == 0) {
+            if (threadIdx.x == 0) c.red[s] = logprod_f_serial(base, n, sep);
+        } else {
+            double v = 0;
+            for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+                float q = base[j * sep];
+                v += q > 0.f ? log((double)q) : -709.0895657128241;
+            }
+            v = block_sum(v, sh);
+            if (threadIdx.x == 0) c.red[s] = v;
+        }
+    }
+}
+
+// UpdateAlpha (src/structure.cpp:1499-1594), reference stream
+// RNG(seed + m, SALT_UPDATEALPHA), on one thread
+__global__ void k_update_alpha(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    if (threadIdx.x || blockIdx.x) return;
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m, S = D.S, N = D.N;
+    Rng64 rng; rng.init(c.seed + (uint64_t)m, VP_SALT_UPDATEALPHA);
+    if (c.locpriori && c.admix) {
+        double r = c.ctl->r;
+        for (int k = 0; k < K; ++k) {
+            double am = rng.normal(c.Alpha[k], c.stdalpha);
+            if (am > 0 && am < c.maxalpha) {
+                double d = am - c.Alpha[k];
+                double dlnL = S * (d * r * ref_mylog(r) + lgamma(r * c.Alpha[k]) - lgamma(r * am));
+                dlnL += r * d * logprod_d_serial(c.AlphaLocal + k, S, K);
+                if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL)) c.Alpha[k] = am;
+            }
+        }
+        if (m % 10 == 0)
+            for (int s = 0; s < S; ++s) {
+                double t = 0;
+                for (int k = 0; k < K; ++k) t += c.AlphaLocal[s * K + k];
+                c.SumAlpha[s] = t;
+            }
+        for (int s = 0; s < S; ++s) {
+            int snind = D.pop_nind[s];
+            for (int k = 0; k < K; ++k) {
+                double ao = c.AlphaLocal[s * K + k], am = rng.normal(ao, c.stdalpha);
+                if (am > 0 && am < c.maxalpha) {
+                    double d = am - ao;
+                    double dlnL = (r * c.Alpha[k] - 1) * ref_mylog(am / ao) - d * r +
+                        snind * (lgamma(c.SumAlpha[s] + d) - lgamma(am) - lgamma(c.SumAlpha[s]) + lgamma(ao));
+                    dlnL += d * c.red[s * K + k];
+                    if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL)) {
+                        c.AlphaLocal[s * K + k] = am;
+                        c.SumAlpha[s] += d;
+                    }
+                }
+            }
+        }
+        return;
+    }
+    if (!c.inferalpha) return;
+    if (!c.admix && m >= c.nadmburnin) return;
+    if (c.diffalpha) {
+        double sumalpha = 0;
+        for (int k = 0; k < K; ++k) sumalpha += c.Alpha[k];
+        for (int k = 0; k < K; ++k) {
+            double am = rng.normal(c.Alpha[k], c.stdalpha);
+            if (am <= 0 || (am >= c.maxalpha && c.uniformalpha)) continue;
+            double ao = c.Alpha[k], d = am - ao;
+            double dlnL = c.uniformalpha ? 0 : ((c.alphapriora - 1) * ref_mylog(am / ao) + (ao - am) / c.alphapriorb);
+            dlnL += (am - ao) * c.red[k] + (lgamma(sumalpha + d) - lgamma(sumalpha) - lgamma(am) + lgamma(ao)) * N;
+            if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL)) c.Alpha[k] = am;
+        }
+    } else {
+        double am = rng.normal(c.Alpha[0], c.stdalpha);
+        if (am <= 0 || (am >= c.maxalpha && c.uniformalpha)) return;
+        double ao = c.Alpha[0];
+        double dlnL = c.uniformalpha ? 0 : ((c.alphapriora - 1) * ref_mylog(am / ao) + (ao - am) / c.alphapriorb);
+        dlnL += (am - ao) * c.red[0] + (lgamma(K * am) - lgamma(K * ao) - K * lgamma(am) + K * lgamma(ao)) * N;
+        if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL))
+            for (int k = 0; k < K; ++k) c.Alpha[k] = am;
+    }
+}
+
+// UpdateLocPriori (src/structure.cpp:1168-1255), one thread
+__global__ void k_update_locpriori(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    if (threadIdx.x || blockIdx.x || !c.locpriori) return;
+    const DevData& D = c.D;
+    const int K = c.K, S = D.S, m = c.ctl->m;
+    Rng64 rng; rng.init(c.seed + (uint64_t)m, VP_SALT_UPDATELOC);
+    double r = c.ctl->r, epsr = c.epsr;
+    if (c.admix) {
+        double rm = rng.uniform(r - epsr, r + epsr);
+        if (rm > 0 && rm < c.maxr) {
+            double dlnL = 0, d = rm - r, dt1 = rm * ref_mylog(rm) - r * ref_mylog(r);
+            for (int k = 0; k < K; ++k) {
+                dlnL += S * (c.Alpha[k] * dt1 - lgamma(rm * c.Alpha[k]) + lgamma(r * c.Alpha[k]));
+                double sa = 0;
+                for (int s = 0; s < S; ++s) sa += c.AlphaLocal[s * K + k];
+                dlnL += c.Alpha[k] * d * logprod_d_serial(c.AlphaLocal + k, S, K) - sa * d;
+            }
+            if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL)) c.ctl->r = rm;
+        }
+        return;
+    }
+    double rm = rng.uniform(r - epsr, r + epsr);
+    if (rm > 0 && rm < c.maxr) {
+        double dlnL = lgamma(rm) - lgamma(r);
+        for (int k = 0; k < K; ++k) dlnL += lgamma(r * c.Eta[k]) - lgamma(rm * c.Eta[k]);
+        dlnL *= S;
+        for (int k = 0; k < K; ++k) dlnL += (rm - r) * c.Eta[k] * logprod_d_serial(c.Gamma + k, S, K);
+        if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL)) c.ctl->r = rm;
+    }
+    r = c.ctl->r;
+    if (K >= 2) {
+        int i1 = (int)rng.nextn(K), j1 = (int)rng.next_avoid(K, i1);
+        double delta = rng.uniform(0, c.epseta);
+        double e1 = c.Eta[i1] + delta, e2 = c.Eta[j1] - delta;
+        if (e1 < 1 && e2 > 0) {
+            double dlnL = S * (lgamma(r * c.Eta[i1]) + lgamma(r * c.Eta[j1]) - lgamma(r * e1) - lgamma(r * e2));
+            dlnL += r * delta * (logprod_d_serial(c.Gamma + i1, S, K) - logprod_d_serial(c.Gamma + j1, S, K));
+            if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL)) { c.Eta[i1] += delta; c.Eta[j1] -= delta; }
+        }
+        for (int s = 0; s < S; ++s) {
+            int a = (int)rng.nextn(K), b = (int)rng.next_avoid(K, a);
+            double dl = rng.uniform(0, c.epsgamma);
+            double* G = c.Gamma + s * K;
+            if (G[a] + dl < 1 && G[b] - dl > 0) {
+                double dlnL = (r * c.Eta[a] - 1.0 + c.Di[s * K + a]) * ref_mylog(1 + dl / G[a]) +
+                              (r * c.Eta[b] - 1.0 + c.Di[s * K + b]) * ref_mylog(1 - dl / G[b]);
+                if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL)) { G[a] += dl; G[b] -= dl; }
+            }
+        }
+    }
+    if (m % 10 == 0) {
+        // Unify (src/math2.cpp:2268-2285)
+        double s = 0;
+        for (int k = 0; k < K; ++k) s += c.Eta[k];
+        double inv = 1.0 / (s + K * VP_MIN_FREQ);
+        for (int k = 0; k < K; ++k) c.Eta[k] = (c.Eta[k] + VP_MIN_FREQ) * inv;
+        for (int sp = 0; sp < S; ++sp) {
+            double* G = c.Gamma + sp * K;
+            double t = 0;
+            for (int k = 0; k < K; ++k) t += G[k];
+            double iv = 1.0 / (t + K * VP_MIN_FREQ);
+            for (int k = 0; k < K; ++k) G[k] = (G[k] + VP_MIN_FREQ) * iv;
+        }
+    }
+}
+
+// UpdateA1 (src/structure.cpp:1646-1695): independent Dirichlet proposal of the
+// ancestral frequencies at each locus. Reference streams: 32 block streams.
+__device__ void update_a1_locus(const DevChain& c, int64_t l, Rng64* r, Philox* ph, float* pb, float* pc) {
+    const DevData& D = c.D;
+    const int K = c.K;
+    int k2 = D.k[l];
+    float* pa = c.FreqA + D.off[l];
+    double lam = c.Lambda[0];
+    for (int a = 0; a < k2; ++a) pb[a] = (float)lam;
+    for (int k = 0; k < K; ++k) {
+        const float* pk = c.Freq + k * D.KT + D.off[l];
+        float fk = (float)c.f[k];
+        for (int a = 0; a < k2; ++a) pb[a] += pk[a] * fk;
+    }
+    double s = 0;
+    for (int a = 0; a < k2; ++a) {
+        double v = r ? r->gamma((double)pb[a] * 1.0) : (double)ph->gammaf(pb[a]);
+        pc[a] = (float)v;
+        s += v;
+    }
+    float inv = (float)(1.0 / s);
+    for (int a = 0; a < k2; ++a) pc[a] *= inv;
+    double dlnL = 0;
+    for (int a = 0; a < k2; ++a) dlnL += (pb[a] - lam) * (ref_mylog(pa[a] / pc[a]));
+    for (int k = 0; k < K; ++k) {
+        const float* pk = c.Freq + k * D.KT + D.off[l];
+        double fr = c.f[k];
+        for (int a = 0; a < k2; ++a)
+            dlnL += lgamma(fr * pa[a]) - lgamma(fr * pc[a]) + fr * (pc[a] - pa[a]) * ref_mylog(pk[a]);
+    }
+    double u = dlnL >= VP_NZERO ? 0 : (r ? r->uniform() : ph->uniformd());
+    if (dlnL >= VP_NZERO || u < exp(dlnL))
+        for (int a = 0; a < k2; ++a) pa[a] = pc[a];
+}
+
+// UpdateA2 (src/structure.cpp:1745-1804): move mass delta between two alleles.
+// The reference does not advance its frequency pointer on a rejected-bounds
+// locus, so later loci of the same block read shifted frequencies; `pshift`
+// carries that offset for the reference-stream form.
+__device__ void update_a2_locus(const DevChain& c, int64_t l, int64_t pshift, Rng64* r, Philox* ph, bool* skipped) {
+    const DevData& D = c.D;
+    const int K = c.K;
+    int k2 = D.k[l];
+    float* pa = c.FreqA + D.off[l];
+    const float* p = c.Freq + D.off[l] - pshift;
+    double lam = c.Lambda[0];
+    int m1, n1;
+    double delta;
+    if (r) {
+        m1 = (int)r->nextn(k2); n1 = (int)r->next_avoid(k2, m1);
+        delta = r->uniform(0, pow((double)D.N, -0.5));
+    } else {
+        m1 = (int)(ph->next() % (uint32_t)k2);
+        n1 = (int)(ph->next() % (uint32_t)(k2 - 1)); if (n1 >= m1) n1++;
+        delta = ph->uniformd() * pow((double)D.N, -0.5);
+    }
+    double pm0 = pa[m1], pm1 = pm0 + delta, pn0 = pa[n1], pn1 = pn0 - delta;
+    *skipped = pm1 >= 1 || pn1 <= 0;
+    if (*skipped) return;
+    double dlnL = (lam - 1) * ref_mylog(pm1 * pn1 / pm0 / pn0);
+    for (int k = 0; k < K; ++k) {
+        double fr = c.f[k];
+        dlnL += lgamma(fr * pm0) + lgamma(fr * pn0) - lgamma(fr * pm1) - lgamma(fr * pn1) +
+                (fr * delta) * ref_mylog(p[k * D.KT + m1] / p[k * D.KT + n1]);
+    }
+    double u = dlnL >= VP_NZERO ? 0 : (r ? r->uniform() : ph->uniformd());
+    if (dlnL >= VP_NZERO || u < exp(dlnL)) { pa[m1] = (float)pm1; pa[n1] = (float)pn1; }
+}
+
+__global__ void k_update_a(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    if (!c.fmodel) return;
+    const DevData& D = c.D;
+    const int m = c.ctl->m;
+    const bool one = hash_ulong(c.seed + (uint64_t)m) & 1;
+    if (c.rng == 0) {
+        int b = blockIdx.x * blockDim.x + threadIdx.x;
+        if (b >= 32) return;
+        int64_t l0 = b * D.L / 32, l1 = (b + 1) * D.L / 32;
+        Rng64 r; r.init(c.seed + (uint64_t)(m * 32 + b), VP_SALT_UPDATEA);
+        float* pb = c.fbuf + (D.maxK + 16) * b * 2;
+        float* pc = pb + D.maxK + 16;
+        int64_t pshift = 0;
+        for (int64_t l = l0; l < l1; ++l) {
+            if (one) update_a1_locus(c, l, &r, nullptr, pb, pc);
+            else {
+                bool sk;
+                update_a2_locus(c, l, pshift, &r, nullptr, &sk);
+                if (sk) pshift += D.k[l];
+            }
+        }
+        return;
+    }
+    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (l >= D.L) return;
+    Philox ph; ph.init(c.seed, ST_A | ((uint32_t)m << 4), (uint32_t)l, 0);
+    float pb[64], pc[64];
+    if (one) update_a1_locus(c, l, nullptr, &ph, pb, pc);
+    else { bool sk; update_a2_locus(c, l, 0, nullptr, &ph, &sk); }
+}
+
+// UpdateF (src/structure.cpp:1806-1858): per-cluster F with a Normal random
+// walk. One block per chain: thread 0 owns the stream, the block reduces the
+// sum over all alleles for each proposal.
+__global__ void k_update_f(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    if (!c.fmodel) return;
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    __shared__ double sh[32];
+    __shared__ double s_fm, s_fo, s_Fm;
+    __shared__ int s_go;
+    Rng64 rng;
+    if (threadIdx.x == 0) rng.init(c.seed + (uint64_t)m, VP_SALT_UPDATEF);
+    for (int k = 0; k < K; ++k) {
+        if (threadIdx.x == 0) {
+            double Fo = c.F[k];
+            double Fm = rng.normal(Fo, c.stdf);
+            s_go = !(Fm < 0 || Fm > 1);
+            s_Fm = Fm; s_fo = c.f[k]; s_fm = (1 - Fm) / Fm;
+        }
+        __syncthreads();
+        if (!s_go) {
+            if (c.fsame) return;
+            __syncthreads();
+            continue;
+        }
+        double fm = s_fm, fo = s_fo;
+        double part = 0;
+        for (int k2 = k; k2 < K; ++k2) {
+            const float* p = c.Freq + k2 * D.KT;
+            for (int64_t a = threadIdx.x; a < D.KT; a += blockDim.x) {
+                float pa2 = c.FreqA[a];
+                part += pa2 * (fm - fo) * ref_mylog(p[a]) + lgamma(fo * pa2) - lgamma(fm * pa2);
+            }
+            if (!c.fsame) break;
+        }
+        double tot = block_sum(part, sh);
+        if (threadIdx.x == 0) {
+            double Fo = c.F[k], Fm = s_Fm;
+            double dlnL = c.pmeanf * (Fo - Fm) / (c.pstdf * c.pstdf) +
+                          (c.pmeanf * c.pmeanf / (c.pstdf * c.pstdf) - 1) * ref_mylog(Fm / Fo) +
+                          (c.fsame ? K : 1) * D.L * (lgamma(fm) - lgamma(fo));
+            dlnL += tot;
+            if (dlnL >= VP_NZERO || rng.uniform() < exp(dlnL)) {
+                if (c.fsame) for (int j = 0; j < K; ++j) { c.F[j] = Fm; c.f[j] = fm; }
+                else { c.F[k] = Fm; c.f[k] = fm; }
+            }
+        }
+        __syncthreads();
+        if (c.fsame) return;
+    }
+}
+
+// Record (src/structure.cpp:1941-2045): likelihood trace, running sums of the
+// likelihood and parameters, then m += 1. One block per chain.
+__global__ void k_record(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K, m = c.ctl->m;
+    __shared__ double sh[32];
+    if (record_at(c, m)) {
+        double like;
+        if (binaryq_at(c, m)) like = c.ctl->lnl;
+        else {
+            double v = 0;
+            for (int j = threadIdx.x; j < c.nlnlp; j += blockDim.x) v += c.lnlp[j];
+            like = block_sum(v, sh);
+        }
+        if (threadIdx.x == 0) {
+            if (c.writelnl) c.lnlTrace[c.ctl->nlnl++] = like;
+            if (m >= c.nburnin) {
+                c.ctl->nr++;
+                c.rout[0] += like;
+                c.rout[1] += like * like;
+                int nf = c.fmodel ? (c.fsame ? 1 : K) : 0;
+                int na = c.admix ? (c.diffalpha ? K : 1) : 0;
+                int nl = c.difflambda ? K : 1;
+                for (int j = 0; j < nl; ++j) c.rout[4 + j] += c.Lambda[j];
+                if (c.locpriori) {
+                    c.rout[4 + nl] += c.ctl->r;
+                    const double* g = c.admix ? c.Alpha : c.Eta;
+                    for (int j = 0; j < K; ++j) c.rout[4 + nl + 1 + j] += g[j];
+                    const double* gl = c.admix ? c.AlphaLocal : c.Gamma;
+                    for (int j = 0; j < K * D.S; ++j) c.rout[4 + nl + 1 + K + j] += gl[j];
+                } else if (c.admix)
+                    for (int j = 0; j < na; ++j) c.rout[4 + nl + j] += c.Alpha[j];
+                for (int j = 0; j < nf; ++j) c.rout[c.rlen - nf + j] += c.F[j];
+            }
+        }
+    }
+}
+
+// the element-wise part of Record: MiSum += Mi on every recorded sweep,
+// FreqM += Freq after burn-in; the last kernel of a sweep also advances m
+__global__ void k_accumulate(const DevChain* chains, int advance) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int m = c.ctl->m;
+    if (record_at(c, m)) {
+        int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t j = tid; j < (int64_t)D.N * c.K; j += nt) c.MiSum[j] += c.Mi[j];
+        if (m >= c.nburnin)
+            for (int64_t j = tid; j < (int64_t)c.K * D.KT; j += nt) c.FreqM[j] += c.Freq[j];
+    }
+}
+
+__global__ void k_advance(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    if (threadIdx.x == 0 && blockIdx.x == 0) c.ctl->m++;
+}
+
+// Arrange (src/structure.cpp:1860-1869)
+__global__ void k_arrange(const DevChain* chains, double* ancestry) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = c.K;
+    int nr = c.ctl->nr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
+        double s = 0;
+        for (int k = 0; k < K; ++k) s += (double)c.MiSum[(int64_t)i * K + k];
+        double inv = 1.0 / (s + K * VP_MIN_FREQ);
+        for (int k = 0; k < K; ++k) ancestry[(int64_t)i * K + k] = ((double)c.MiSum[(int64_t)i * K + k] + VP_MIN_FREQ) * inv;
+    }
+    float finv = (float)(1.0 / nr);
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < (int64_t)K * D.KT; j += (int64_t)gridDim.x * blockDim.x)
+        c.FreqM[j] *= finv;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double inv = 1.0 / nr;
+        for (int j = 0; j < c.rlen; ++j) c.rout[j] *= inv;
+        c.rout[2] = c.rout[1] - c.rout[0] * c.rout[0];
+        c.rout[3] = c.rout[0] - c.rout[2] / 2;
+    }
+}
+
+}  // namespace vp

@@ -1,0 +1,578 @@
+// Host side of the device STRUCTURE sweep: contexts, chain state, the launch
+// sequence of one sweep, CUDA-graph replay, and the C ABI.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "vp_internal.h"
+#include "vp_kernels.cuh"
+
+using namespace vp;
+
+struct vp_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevData D{};
+    std::vector<void*> allocs;
+    int64_t launches = 0;
+    int32_t N = 0, S = 0, maxK = 0, maxploidy = 0, packed2 = 0;
+    int64_t L = 0, KT = 0;
+    int nsm = 132;
+};
+
+struct vp_chain {
+    vp_ctx* ctx = nullptr;
+    vp_params P{};
+    DevChain h{};
+    DevChain* d = nullptr;
+    void* mem = nullptr;
+    int total = 0;        // sweeps of the run: nburnin (+ admixture burn-in) + nreps
+    int issued = 0;       // sweeps launched so far
+    int kc = 16, kgroups = 1;
+    bool arranged = false;
+    double* ancestry = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_nodes = 0;
+};
+
+namespace {
+
+#define CK(call)                                                                  \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            vp_set_error("%s failed: %s", #call, cudaGetErrorString(e_));         \
+            return VP_E_CUDA;                                                     \
+        }                                                                         \
+    } while (0)
+
+int check_launch(vp_ctx* ctx, const char* what) {
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        vp_set_error("launch of %s failed: %s", what, cudaGetErrorString(e));
+        return VP_E_CUDA;
+    }
+    return VP_OK;
+}
+#define VP_UNPACK(...) __VA_ARGS__
+#define LAUNCH(ctx, name, cfg, args)            \
+    do {                                        \
+        name<<<VP_UNPACK cfg>>> args;           \
+        int rc_ = check_launch(ctx, #name);     \
+        if (rc_) return rc_;                    \
+    } while (0)
+
+template <typename T>
+int upload(vp_ctx* ctx, const T* host, size_t n, const T** dev) {
+    if (n == 0) { *dev = nullptr; return VP_OK; }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) { vp_set_error("cudaMalloc(%zu) failed: %s", n * sizeof(T), cudaGetErrorString(e)); return VP_E_MEM; }
+    ctx->allocs.push_back(p);
+    CK(cudaMemcpyAsync(p, host, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    *dev = (const T*)p;
+    return VP_OK;
+}
+
+inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// bump allocator over one device allocation
+struct Carve {
+    char* base;
+    size_t off = 0;
+    template <typename T>
+    T* take(int64_t n) {
+        off = (off + 255) & ~(size_t)255;
+        T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+        off += (size_t)std::max<int64_t>(n, 1) * sizeof(T);
+        return p;
+    }
+};
+
+int kc_for(int K) { return K <= 4 ? 4 : K <= 8 ? 8 : 16; }
+
+int launch_loglik(vp_chain* c, int force) {
+    vp_ctx* x = c->ctx;
+    dim3 g(cdiv(x->N, LL_BLOCK), c->h.nchunk, c->kgroups);
+    switch (c->kc) {
+        case 4: LAUNCH(x, k_loglik<4>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
+        case 8: LAUNCH(x, k_loglik<8>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
+        default: LAUNCH(x, k_loglik<16>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
+    }
+    return VP_OK;
+}
+
+size_t count_smem(const vp_chain* c) { return (size_t)COUNT_WARPS * c->P.K * c->ctx->maxK * sizeof(int32_t); }
+size_t zadm_smem(const vp_chain* c) {
+    return (size_t)c->h.zadm_tn * c->P.K * 8 + (size_t)32 * c->P.K * c->ctx->maxK * 4;
+}
+
+int launch_step(vp_chain* c, int step, int force) {
+    vp_ctx* x = c->ctx;
+    cudaStream_t s = x->stream;
+    const vp_params& P = c->P;
+    const int K = P.K;
+    const bool ref = P.rng == VP_RNG_REFERENCE;
+    switch (step) {
+        case VP_STEP_UPDATEP:
+            if (ref) LAUNCH(x, k_update_p_ref, (dim3(1, 1, 1), 128, 0, s), (c->d));
+            else LAUNCH(x, k_update_p_ctr, (dim3(cdiv((int64_t)K * x->L, 256), 1, 1), 256, 0, s), (c->d));
+            return VP_OK;
+        case VP_STEP_LOGLIK: {
+            int rc = launch_loglik(c, 1);
+            if (rc) return rc;
+            LAUNCH(x, k_sample_noadmix, (dim3(1, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 1));
+            return VP_OK;
+        }
+        case VP_STEP_UPDATEQ: {
+            const unsigned gi = cdiv(x->N, 256);
+            if (!P.admix) {
+                if (!force || true) {
+                    int rc = launch_loglik(c, force);
+                    if (rc) return rc;
+                    LAUNCH(x, k_sample_noadmix, (dim3(1, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 0));
+                }
+                if (c->h.nadmburnin > 0) LAUNCH(x, k_update_q_admix, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
+            } else {
+                LAUNCH(x, k_update_q_admix, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
+                if (P.metrofreq > 0) {
+                    LAUNCH(x, k_metro_propose, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
+                    LAUNCH(x, k_metro_ratio, (dim3(cdiv(x->N, LL_BLOCK), c->h.nchunk, 1), LL_BLOCK, 0, s), (c->d, 0));
+                    LAUNCH(x, k_metro_accept, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
+                }
+            }
+            return VP_OK;
+        }
+        case VP_STEP_LOCPRIORI:
+            if (P.locpriori) LAUNCH(x, k_update_locpriori, (dim3(1, 1, 1), 32, 0, s), (c->d));
+            return VP_OK;
+        case VP_STEP_UPDATEZ:
+            if (!P.admix)
+                LAUNCH(x, k_count_noadmix, (dim3(cdiv(x->L, COUNT_WARPS), 1, 1), COUNT_WARPS * 32, count_smem(c), s), (c->d, 0));
+            if (P.admix || c->h.nadmburnin > 0) {
+                LAUNCH(x, k_zero_counts, (dim3(std::min<unsigned>(1024, cdiv((int64_t)K * x->KT, 256)), 1, 1), 256, 0, s), (c->d, 0));
+                if (ref)
+                    LAUNCH(x, k_update_z_admix_ref, (dim3(cdiv(x->L, 128), 1, 1), 128, 0, s), (c->d, 0));
+                else
+                    LAUNCH(x, k_update_z_admix_ctr, (dim3(cdiv(x->L, 32), cdiv(x->N, c->h.zadm_tn), 1), ZA_WARPS * 32,
+                           zadm_smem(c), s), (c->d, 0));
+            }
+            return VP_OK;
+        case VP_STEP_ALPHA:
+            if ((P.inferalpha && (P.admix || c->h.nadmburnin > 0)) || (P.locpriori && P.admix)) {
+                LAUNCH(x, k_logprod_q, (dim3(std::max(1, std::min(x->S * K, 256)), 1, 1), 256, 0, s), (c->d));
+                LAUNCH(x, k_update_alpha, (dim3(1, 1, 1), 32, 0, s), (c->d));
+            }
+            return VP_OK;
+        case VP_STEP_UPDATEA:
+            if (P.fmodel) {
+                if (ref) LAUNCH(x, k_update_a, (dim3(1, 1, 1), 32, 0, s), (c->d));
+                else LAUNCH(x, k_update_a, (dim3(cdiv(x->L, 128), 1, 1), 128, 0, s), (c->d));
+            }
+            return VP_OK;
+        case VP_STEP_UPDATEF:
+            if (P.fmodel) LAUNCH(x, k_update_f, (dim3(1, 1, 1), 256, 0, s), (c->d));
+            return VP_OK;
+        case VP_STEP_RECORD:
+            LAUNCH(x, k_record, (dim3(1, 1, 1), 256, 0, s), (c->d));
+            LAUNCH(x, k_accumulate, (dim3(std::min<unsigned>(1024, cdiv((int64_t)K * x->KT, 256)), 1, 1), 256, 0, s), (c->d, 0));
+            return VP_OK;
+        case VP_STEP_NEXT:
+            LAUNCH(x, k_advance, (dim3(1, 1, 1), 32, 0, s), (c->d));
+            return VP_OK;
+    }
+    vp_set_error("unknown step %d", step);
+    return VP_E_ARG;
+}
+
+int launch_sweep(vp_chain* c) {
+    static const int seq[] = {VP_STEP_UPDATEP, VP_STEP_UPDATEQ, VP_STEP_LOCPRIORI, VP_STEP_UPDATEZ, VP_STEP_ALPHA,
+                              VP_STEP_UPDATEA, VP_STEP_UPDATEF, VP_STEP_RECORD, VP_STEP_NEXT};
+    for (int st : seq) {
+        int rc = launch_step(c, st, 0);
+        if (rc) return rc;
+    }
+    return VP_OK;
+}
+
+}  // namespace
+
+extern "C" int vp_open(const vp_dataset* ds, int device, vp_ctx** out) {
+    if (!ds || !out) { vp_set_error("null argument"); return VP_E_ARG; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
+    if (device < 0 || device >= ndev) { vp_set_error("device %d out of range", device); return VP_E_ARG; }
+    if (ds->maxK > 64) { vp_set_error("loci with more than 64 alleles are not supported"); return VP_E_ARG; }
+    auto* x = new vp_ctx();
+    x->device = device;
+    cudaSetDevice(device);
+    cudaDeviceGetAttribute(&x->nsm, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        vp_set_error("cudaStreamCreate failed");
+        delete x;
+        return VP_E_CUDA;
+    }
+    x->N = ds->N; x->S = ds->S; x->L = ds->L; x->KT = ds->KT; x->maxK = ds->maxK; x->maxploidy = ds->maxploidy;
+    x->packed2 = ds->packed2;
+    DevData& D = x->D;
+    D.N = ds->N; D.S = ds->S; D.vmax = ds->vmax; D.maxploidy = ds->maxploidy; D.maxK = ds->maxK; D.Nw = ds->Nw;
+    D.packed2 = ds->packed2; D.L = ds->L; D.KT = ds->KT; D.coprime = ds->coprime;
+    int rc = 0;
+    if (ds->packed2) rc |= upload(x, ds->g2.data(), ds->g2.size(), &D.g2);
+    else rc |= upload(x, ds->gb.data(), ds->gb.size(), &D.gb);
+    rc |= upload(x, ds->k.data(), ds->k.size(), &D.k);
+    rc |= upload(x, ds->off.data(), ds->off.size(), &D.off);
+    rc |= upload(x, ds->vt.data(), ds->vt.size(), &D.vt);
+    rc |= upload(x, ds->popid.data(), ds->popid.size(), &D.popid);
+    rc |= upload(x, ds->pop_ind0.data(), ds->pop_ind0.size(), &D.pop_ind0);
+    rc |= upload(x, ds->pop_nind.data(), ds->pop_nind.size(), &D.pop_nind);
+    rc |= upload(x, ds->totfreq.data(), ds->totfreq.size(), &D.totfreq);
+    rc |= upload(x, ds->nhaplo.data(), ds->nhaplo.size(), &D.nhaplo);
+    if (rc) { vp_close(x); return rc < 0 ? rc : VP_E_CUDA; }
+    if (cudaStreamSynchronize(x->stream) != cudaSuccess) { vp_set_error("upload failed"); vp_close(x); return VP_E_CUDA; }
+    *out = x;
+    return VP_OK;
+}
+
+extern "C" int vp_close(vp_ctx* x) {
+    if (!x) return VP_OK;
+    cudaSetDevice(x->device);
+    if (x->stream) cudaStreamSynchronize(x->stream);
+    for (void* p : x->allocs) cudaFree(p);
+    if (x->stream) cudaStreamDestroy(x->stream);
+    delete x;
+    return VP_OK;
+}
+
+extern "C" int vp_sync(vp_ctx* x) {
+    if (!x) { vp_set_error("null context"); return VP_E_ARG; }
+    CK(cudaStreamSynchronize(x->stream));
+    return VP_OK;
+}
+
+extern "C" int64_t vp_launch_count(vp_ctx* x) { return x ? x->launches : -1; }
+
+extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
+    if (!x || !P || !out) { vp_set_error("null argument"); return VP_E_ARG; }
+    if (P->K < 1 || P->K > 64) { vp_set_error("K must be in 1..64"); return VP_E_ARG; }
+    if (P->nthinning < 1 || P->nburnin < 0 || P->nreps < 0) { vp_set_error("bad MCMC lengths"); return VP_E_ARG; }
+    if ((int64_t)P->K * x->maxK > 3072) { vp_set_error("K * max alleles must be <= 3072"); return VP_E_ARG; }
+    cudaSetDevice(x->device);
+    auto* c = new vp_chain();
+    c->ctx = x;
+    c->P = *P;
+    const int K = P->K, N = x->N, S = x->S;
+    const int64_t L = x->L, KT = x->KT;
+    DevChain& h = c->h;
+    h.D = x->D;
+    h.K = K; h.admix = P->admix; h.locpriori = P->locpriori; h.fmodel = P->fmodel;
+    // ReadPar (src/structure.cpp:459-463): the no-admixture burn-in only exists
+    // without admixture and without the location prior, and lengthens burn-in
+    h.nadmburnin = (!P->locpriori && !P->admix) ? P->nadmburnin : 0;
+    h.nburnin = P->nburnin + h.nadmburnin;
+    h.nreps = P->nreps; h.nthinning = P->nthinning; h.writelnl = P->writelnl;
+    h.metrofreq = P->metrofreq; h.inferalpha = P->inferalpha; h.diffalpha = P->diffalpha;
+    h.uniformalpha = P->uniformalpha; h.fsame = P->fsame; h.difflambda = P->difflambda; h.rng = P->rng;
+    h.lambda = P->lambda; h.alpha = P->alpha; h.stdalpha = P->stdalpha; h.maxalpha = P->maxalpha;
+    h.alphapriora = P->alphapriora; h.alphapriorb = P->alphapriorb; h.maxr = P->maxr; h.epsr = P->epsr;
+    h.epseta = P->epseta; h.epsgamma = P->epsgamma; h.pmeanf = P->pmeanf; h.pstdf = P->pstdf; h.stdf = P->stdf;
+    h.seed = P->seed;
+    int nf = P->fmodel ? (P->fsame ? 1 : K) : 0;
+    int na = P->admix ? (P->diffalpha ? K : 1) : 0;
+    int nl = P->difflambda ? K : 1;
+    h.rlen = P->locpriori ? 4 + nl + 1 + K + K * S + nf : 4 + nl + na + nf;
+    c->kc = kc_for(K);
+    c->kgroups = (K + c->kc - 1) / c->kc;
+    // locus chunks for the likelihood passes: enough CTAs to fill the SMs
+    {
+        int64_t nbi = cdiv(N, LL_BLOCK) * (int64_t)c->kgroups;
+        int64_t want = std::max<int64_t>(1, (int64_t)x->nsm * 4 / std::max<int64_t>(nbi, 1));
+        int64_t maxc = std::max<int64_t>(1, L / 64);
+        int64_t nch = std::min(want, maxc);
+        h.lchunk = (int32_t)((L + nch - 1) / nch);
+        h.nchunk = (int32_t)((L + h.lchunk - 1) / h.lchunk);
+    }
+    h.zadm_tn = 256;
+    while (h.zadm_tn > 32 && zadm_smem(c) > 96 * 1024) h.zadm_tn /= 2;
+    h.nlnlp = (int32_t)std::max<int64_t>(cdiv(L, 128), (int64_t)cdiv(L, 32) * cdiv(N, h.zadm_tn));
+    const int64_t ntrace = h.nburnin / h.nthinning + h.nreps / h.nthinning + 2;
+    const int64_t ltn = x->packed2 ? L * K * 4 : (int64_t)K * KT;
+    auto layout = [&](Carve& cv) {
+        h.ctl = cv.take<Ctl>(1);
+        h.rstate = cv.take<Rng64>(1);
+        h.Freq = cv.take<float>(K * KT);
+        h.FreqM = cv.take<float>(K * KT);
+        h.FreqA = cv.take<float>(P->fmodel ? KT : 1);
+        h.lt = cv.take<float>(ltn);
+        h.Q = cv.take<float>((int64_t)N * K);
+        h.Qprop = cv.take<float>((int64_t)N * K);
+        h.Di = cv.take<float>((int64_t)S * K);
+        h.fbuf = cv.take<float>(64 * (x->maxK + 16));
+        h.Z = cv.take<uint16_t>(N + 32);
+        h.Mi = cv.take<int32_t>((int64_t)N * K);
+        h.Ni = cv.take<int32_t>(K * KT);
+        h.MiSum = cv.take<int64_t>((int64_t)N * K);
+        h.LLp = cv.take<double>((int64_t)h.nchunk * N * K);
+        h.LL = cv.take<double>((int64_t)N * K);
+        h.metro = cv.take<double>(N);
+        h.metrop = cv.take<double>((int64_t)h.nchunk * N);
+        h.Alpha = cv.take<double>(K);
+        h.Lambda = cv.take<double>(K);
+        h.f = cv.take<double>(K);
+        h.F = cv.take<double>(K);
+        h.Eta = cv.take<double>(K);
+        h.Gamma = cv.take<double>((int64_t)S * K);
+        h.AlphaLocal = cv.take<double>((int64_t)S * K);
+        h.SumAlpha = cv.take<double>(S);
+        h.rout = cv.take<double>(h.rlen);
+        h.lnlTrace = cv.take<double>(ntrace);
+        h.red = cv.take<double>((int64_t)S * K + K + 1);
+        h.lnlp = cv.take<double>(h.nlnlp);
+        c->ancestry = cv.take<double>((int64_t)N * K);
+        c->d = cv.take<DevChain>(1);
+    };
+    Carve probe{nullptr};
+    layout(probe);
+    cudaError_t e = cudaMalloc(&c->mem, probe.off);
+    if (e != cudaSuccess) {
+        vp_set_error("cudaMalloc of %zu bytes for chain state failed: %s", probe.off, cudaGetErrorString(e));
+        delete c;
+        return VP_E_MEM;
+    }
+    Carve cv{(char*)c->mem};
+    layout(cv);
+    CK(cudaMemsetAsync(c->mem, 0, probe.off, x->stream));
+    CK(cudaMemcpyAsync(c->d, &h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
+    c->total = h.nburnin + h.nreps;
+    // InitFix / InitAdmix / InitLocPriori / InitFmodel
+    cudaStream_t s = x->stream;
+    int rc = VP_OK;
+    do {
+        k_init_state<<<dim3(std::min<unsigned>(1024, cdiv(std::max<int64_t>(L, (int64_t)N * K), 256)), 1, 1), 256, 0, s>>>(c->d);
+        if ((rc = check_launch(x, "k_init_state"))) break;
+        const bool singlez = h.nadmburnin == 0 && !P->admix;
+        if (singlez) {
+            k_init_z_single<<<P->rng ? cdiv(N, 256) : 1, P->rng ? 256 : 32, 0, s>>>(c->d);
+            if ((rc = check_launch(x, "k_init_z_single"))) break;
+            k_count_noadmix<<<cdiv(L, COUNT_WARPS), COUNT_WARPS * 32, count_smem(c), s>>>(c->d, 1);
+            if ((rc = check_launch(x, "k_count_noadmix"))) break;
+        } else {
+            k_init_admix<<<cdiv(L, 128), 128, 0, s>>>(c->d);
+            if ((rc = check_launch(x, "k_init_admix"))) break;
+        }
+    } while (0);
+    if (rc) { cudaFree(c->mem); delete c; return rc; }
+    *out = c;
+    return VP_OK;
+}
+
+extern "C" int vp_chain_destroy(vp_chain* c) {
+    if (!c) return VP_OK;
+    cudaSetDevice(c->ctx->device);
+    cudaStreamSynchronize(c->ctx->stream);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    cudaFree(c->mem);
+    delete c;
+    return VP_OK;
+}
+
+// Capture one sweep of the given chains into a graph (kernels read m from
+// device memory, so the same graph serves every sweep).
+static int capture_sweep(vp_chain** cs, int n, cudaGraphExec_t* exec, int* nodes) {
+    vp_ctx* x = cs[0]->ctx;
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal));
+    int64_t before = x->launches;
+    int rc = VP_OK;
+    for (int i = 0; i < n && !rc; ++i) rc = launch_sweep(cs[i]);
+    cudaError_t e = cudaStreamEndCapture(x->stream, &g);
+    if (rc) { if (e == cudaSuccess) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) { vp_set_error("graph capture failed: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+    *nodes = (int)(x->launches - before);
+    x->launches = before;
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { vp_set_error("graph instantiate failed: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+    return VP_OK;
+}
+
+extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
+    if (!cs || n <= 0 || nsweeps < 0) { vp_set_error("bad arguments"); return VP_E_ARG; }
+    vp_ctx* x = cs[0]->ctx;
+    for (int i = 0; i < n; ++i)
+        if (!cs[i] || cs[i]->ctx != x) { vp_set_error("all chains of one vp_run must share a context"); return VP_E_ARG; }
+    cudaSetDevice(x->device);
+    // chains with sweeps left; equal remaining counts share one graph
+    int left = nsweeps;
+    while (left > 0) {
+        std::vector<vp_chain*> act;
+        int step = left;
+        for (int i = 0; i < n; ++i) {
+            int rem = cs[i]->total - cs[i]->issued;
+            if (rem > 0) { act.push_back(cs[i]); step = std::min(step, rem); }
+        }
+        if (act.empty()) break;
+        if (step >= 4 && act.size() == 1) {
+            vp_chain* c = act[0];
+            if (!c->graph) {
+                int rc = capture_sweep(&c, 1, &c->graph, &c->graph_nodes);
+                if (rc) return rc;
+            }
+            for (int s = 0; s < step; ++s) {
+                CK(cudaGraphLaunch(c->graph, x->stream));
+                x->launches += c->graph_nodes;
+            }
+        } else if (step >= 4) {
+            cudaGraphExec_t ex;
+            int nodes = 0;
+            int rc = capture_sweep(act.data(), (int)act.size(), &ex, &nodes);
+            if (rc) return rc;
+            for (int s = 0; s < step; ++s) {
+                cudaError_t e = cudaGraphLaunch(ex, x->stream);
+                if (e != cudaSuccess) { cudaGraphExecDestroy(ex); vp_set_error("graph launch: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+                x->launches += nodes;
+            }
+            cudaGraphExecDestroy(ex);
+        } else {
+            for (int s = 0; s < step; ++s)
+                for (vp_chain* c : act) {
+                    int rc = launch_sweep(c);
+                    if (rc) return rc;
+                }
+        }
+        for (vp_chain* c : act) c->issued += step;
+        left -= step;
+    }
+    return VP_OK;
+}
+
+extern "C" int vp_finish(vp_chain** cs, int32_t n) {
+    if (!cs || n <= 0) { vp_set_error("bad arguments"); return VP_E_ARG; }
+    int mx = 0;
+    for (int i = 0; i < n; ++i) mx = std::max(mx, cs[i]->total - cs[i]->issued);
+    int rc = vp_run(cs, n, mx);
+    if (rc) return rc;
+    vp_ctx* x = cs[0]->ctx;
+    for (int i = 0; i < n; ++i) {
+        vp_chain* c = cs[i];
+        if (c->arranged) continue;
+        k_arrange<<<std::min<unsigned>(1024, cdiv((int64_t)c->P.K * x->KT, 256)), 256, 0, x->stream>>>(c->d, c->ancestry);
+        rc = check_launch(x, "k_arrange");
+        if (rc) return rc;
+        c->arranged = true;
+    }
+    return vp_sync(x);
+}
+
+extern "C" int vp_chain_sizes(vp_chain* c, vp_result* r) {
+    if (!c || !r) { vp_set_error("null argument"); return VP_E_ARG; }
+    memset(r, 0, sizeof *r);
+    r->K = c->P.K; r->N = c->ctx->N; r->S = c->ctx->S; r->KT = c->ctx->KT;
+    r->nburnin = c->h.nburnin; r->nreps = c->h.nreps; r->nthinning = c->h.nthinning; r->rlen = c->h.rlen;
+    r->seed = c->P.seed;
+    Ctl ctl;
+    CK(cudaMemcpy(&ctl, c->h.ctl, sizeof ctl, cudaMemcpyDeviceToHost));
+    r->nr = ctl.nr; r->nlnl = ctl.nlnl;
+    return VP_OK;
+}
+
+extern "C" int vp_chain_result(vp_chain* c, vp_result* out) {
+    if (!c || !out) { vp_set_error("null argument"); return VP_E_ARG; }
+    vp_result sz;
+    int rc = vp_chain_sizes(c, &sz);
+    if (rc) return rc;
+    const int64_t NK = (int64_t)sz.N * sz.K;
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    if (out->rout) CK(cudaMemcpy(out->rout, c->h.rout, sz.rlen * sizeof(double), cudaMemcpyDeviceToHost));
+    if (out->lnl) CK(cudaMemcpy(out->lnl, c->h.lnlTrace, sz.nlnl * sizeof(double), cudaMemcpyDeviceToHost));
+    if (out->Q) CK(cudaMemcpy(out->Q, c->h.Q, NK * sizeof(float), cudaMemcpyDeviceToHost));
+    if (out->ancestry) {
+        if (!c->arranged) { vp_set_error("ancestry is available after vp_finish"); return VP_E_STATE; }
+        CK(cudaMemcpy(out->ancestry, c->ancestry, NK * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    if (out->freqm) CK(cudaMemcpy(out->freqm, c->h.FreqM, sz.K * sz.KT * sizeof(float), cudaMemcpyDeviceToHost));
+    double *ro = out->rout, *ln = out->lnl;
+    float *q = out->Q, *fm = out->freqm;
+    double* an = out->ancestry;
+    *out = sz;
+    out->rout = ro; out->lnl = ln; out->Q = q; out->freqm = fm; out->ancestry = an;
+    return VP_OK;
+}
+
+static int field_ptr(vp_chain* c, int f, void** p, size_t* bytes) {
+    const DevChain& h = c->h;
+    const size_t K = c->P.K, N = c->ctx->N, KT = c->ctx->KT, S = c->ctx->S;
+    switch (f) {
+        case VP_F_FREQ: *p = h.Freq; *bytes = K * KT * 4; return VP_OK;
+        case VP_F_Q: *p = h.Q; *bytes = N * K * 4; return VP_OK;
+        case VP_F_Z: *p = h.Z; *bytes = N * 2; return VP_OK;
+        case VP_F_NI: *p = h.Ni; *bytes = K * KT * 4; return VP_OK;
+        case VP_F_MI: *p = h.Mi; *bytes = N * K * 4; return VP_OK;
+        case VP_F_LL: *p = h.LL; *bytes = N * K * 8; return VP_OK;
+        case VP_F_ALPHA: *p = h.Alpha; *bytes = K * 8; return VP_OK;
+        case VP_F_M: *p = &h.ctl->m; *bytes = 4; return VP_OK;
+        case VP_F_LNL: *p = &h.ctl->lnl; *bytes = 8; return VP_OK;
+        case VP_F_FREQA: *p = h.FreqA; *bytes = c->P.fmodel ? KT * 4 : 0; return VP_OK;
+        case VP_F_FF: *p = h.f; *bytes = 2 * K * 8; return VP_OK;  // f and F are adjacent 256-aligned? no
+        case VP_F_DI: *p = h.Di; *bytes = S * K * 4; return VP_OK;
+        case VP_F_METRO: *p = h.metro; *bytes = N * 8; return VP_OK;
+    }
+    vp_set_error("unknown field %d", f);
+    return VP_E_ARG;
+}
+
+extern "C" int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes) {
+    if (!c || !host) { vp_set_error("null argument"); return VP_E_ARG; }
+    cudaSetDevice(c->ctx->device);
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    if (field == VP_F_FF) {
+        size_t K = c->P.K;
+        if (bytes != 2 * K * 8) { vp_set_error("field %d holds %zu bytes", field, 2 * K * 8); return VP_E_ARG; }
+        CK(cudaMemcpy(host, c->h.f, K * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy((char*)host + K * 8, c->h.F, K * 8, cudaMemcpyDeviceToHost));
+        return VP_OK;
+    }
+    void* p; size_t n;
+    int rc = field_ptr(c, field, &p, &n);
+    if (rc) return rc;
+    if (bytes != n) { vp_set_error("field %d holds %zu bytes, not %zu", field, n, bytes); return VP_E_ARG; }
+    CK(cudaMemcpy(host, p, n, cudaMemcpyDeviceToHost));
+    return VP_OK;
+}
+
+extern "C" int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t bytes) {
+    if (!c || !host) { vp_set_error("null argument"); return VP_E_ARG; }
+    cudaSetDevice(c->ctx->device);
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    if (field == VP_F_FF) {
+        size_t K = c->P.K;
+        if (bytes != 2 * K * 8) { vp_set_error("field %d holds %zu bytes", field, 2 * K * 8); return VP_E_ARG; }
+        CK(cudaMemcpy(c->h.f, host, K * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(c->h.F, (const char*)host + K * 8, K * 8, cudaMemcpyHostToDevice));
+        return VP_OK;
+    }
+    void* p; size_t n;
+    int rc = field_ptr(c, field, &p, &n);
+    if (rc) return rc;
+    if (bytes != n) { vp_set_error("field %d holds %zu bytes, not %zu", field, n, bytes); return VP_E_ARG; }
+    CK(cudaMemcpy(p, host, n, cudaMemcpyHostToDevice));
+    if (field == VP_F_FREQ) {
+        // keep the likelihood lookup table in step with the frequencies
+        vp_ctx* x = c->ctx;
+        k_refresh_lt<<<cdiv((int64_t)c->P.K * x->L, 256), 256, 0, x->stream>>>(c->d);
+        rc = check_launch(x, "k_refresh_lt");
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(x->stream));
+    }
+    return VP_OK;
+}
+
+extern "C" int vp_chain_step(vp_chain* c, int32_t step) {
+    if (!c) { vp_set_error("null chain"); return VP_E_ARG; }
+    cudaSetDevice(c->ctx->device);
+    int rc = launch_step(c, step, 0);
+    if (rc) return rc;
+    return vp_sync(c->ctx);
+}

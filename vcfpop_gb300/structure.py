@@ -1,0 +1,220 @@
+"""Python front end of the GB300 STRUCTURE sweep, over the C ABI.
+
+Mirrors the reference's run structure (vcfpop src/structure.cpp): a dataset is
+prepared once (CalcBayesian's locus filter/sort), uploaded once, and each
+(K, replicate) run is a chain whose MCMC state stays on the GPU. Parameter
+names and defaults are those of the -structure_* flags.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as B
+
+PARAM_FLAGS = {
+    # -structure_* flag -> (field, kind)
+    "admix": ("admix", "yn"), "locpriori": ("locpriori", "yn"), "f": ("fmodel", "yn"),
+    "nburnin": ("nburnin", int), "nreps": ("nreps", int), "nthinning": ("nthinning", int),
+    "nadmburnin": ("nadmburnin", int), "writelnl": ("writelnl", "yn"),
+    "lambda": ("lambda_", float), "stdlambda": ("stdlambda", float), "maxlambda": ("maxlambda", float),
+    "alpha": ("alpha", float), "inferalpha": ("inferalpha", "yn"), "diffalpha": ("diffalpha", "yn"),
+    "uniformalpha": ("uniformalpha", "yn"), "stdalpha": ("stdalpha", float), "maxalpha": ("maxalpha", float),
+    "alphapriora": ("alphapriora", float), "alphapriorb": ("alphapriorb", float),
+    "metrofreq": ("metrofreq", int), "r": ("r", float), "maxr": ("maxr", float), "stdr": ("epsr", float),
+    "epseta": ("epseta", float), "epsgamma": ("epsgamma", float), "pmeanf": ("pmeanf", float),
+    "pstdf": ("pstdf", float), "stdf": ("stdf", float), "singlef": ("fsame", "yn"),
+}
+
+
+def params(K: int, seed: int, rng: int = B.VP_RNG_COUNTER, form: int = B.VP_FORM_PLAIN, **kw) -> B.VpParams:
+    """Build a run's parameters; keyword names are the -structure_* flag names
+    (yes/no may be given as bool, "yes"/"no" or 1/0)."""
+    p = B.VpParams()
+    B.lib().vp_params_default(C.byref(p))
+    p.K = K
+    p.seed = seed
+    p.rng = rng
+    p.form = form
+    for k, v in kw.items():
+        field, kind = PARAM_FLAGS[k]
+        if kind == "yn":
+            v = 1 if v in (True, 1, "yes") else 0
+        setattr(p, field, kind(v) if kind not in ("yn",) else v)
+    return p
+
+
+def run_seed(g_seed: int, run_id: int) -> int:
+    """HashULong(g_seed + run id), the reference's per-run seed."""
+    return int(B.lib().vp_run_seed(g_seed, run_id))
+
+
+def pack2(G: np.ndarray) -> np.ndarray:
+    """Pack biallelic diploid calls G[L, N, 2] (allele index, -1 missing) into
+    2-bit codes (count of allele 1; 3 = missing), 16 calls per uint32."""
+    L, N, _ = G.shape
+    code = np.where(G[:, :, 0] < 0, 3, G[:, :, 0].astype(np.int64) + G[:, :, 1].astype(np.int64)).astype(np.uint32)
+    Nw = (N + 15) // 16
+    pad = np.full((L, Nw * 16), 3, dtype=np.uint32)
+    pad[:, :N] = code
+    pad = pad.reshape(L, Nw, 16)
+    shifts = (np.arange(16, dtype=np.uint32) * 2)[None, None, :]
+    return np.bitwise_or.reduce(pad << shifts, axis=2).astype(np.uint32)
+
+
+class Dataset:
+    """A prepared dataset (host side): loci filtered and sorted as the reference does."""
+
+    def __init__(self, ploidy, n_alleles, popid, n_pop, G=None, packed2=None, n_ind=None):
+        self._keep = []
+        ploidy = np.ascontiguousarray(ploidy, dtype=np.int32)
+        n_alleles = np.ascontiguousarray(n_alleles, dtype=np.int32)
+        popid = np.ascontiguousarray(popid, dtype=np.int32)
+        inp = B.VpInput()
+        inp.n_ind = len(ploidy)
+        inp.n_loc = len(n_alleles)
+        if G is not None:
+            G = np.ascontiguousarray(G, dtype=np.int8)
+            inp.vmax = G.shape[2]
+            inp.alleles = G.ctypes.data
+            self._keep.append(G)
+        if packed2 is not None:
+            packed2 = np.ascontiguousarray(packed2, dtype=np.uint32)
+            inp.packed2 = packed2.ctypes.data
+            inp.vmax = 2
+            self._keep.append(packed2)
+        inp.ploidy = ploidy.ctypes.data
+        inp.n_alleles = n_alleles.ctypes.data
+        inp.popid = popid.ctypes.data
+        inp.n_pop = n_pop
+        self._keep += [ploidy, n_alleles, popid]
+        h = C.c_void_p()
+        B.check(B.lib().vp_dataset_prepare(C.byref(inp), C.byref(h)))
+        self.h = h
+        self._keep = []  # the library copied what it needs
+        info = B.VpDatasetInfo()
+        B.check(B.lib().vp_dataset_info_get(h, C.byref(info)))
+        self.N, self.L, self.KT, self.S = info.n_ind, info.n_loc, info.n_alleles_total, info.n_pop
+        self.maxploidy, self.maxK, self.packed2, self.coprime = info.maxploidy, info.max_alleles, info.packed2, info.coprime
+
+    @classmethod
+    def from_synth(cls, d: dict, n_pop: int | None = None, packed: bool | None = None):
+        G, ploidy, k, pop = d["G"], d["ploidy"], d["k"], d["pop"]
+        S = int(n_pop if n_pop is not None else pop.max() + 1)
+        if packed is None:
+            packed = bool((ploidy == 2).all() and (k == 2).all())
+        if packed:
+            return cls(ploidy, k, pop, S, packed2=pack2(G))
+        return cls(ploidy, k, pop, S, G=G)
+
+    def order(self) -> np.ndarray:
+        o = np.zeros(self.L, dtype=np.int64)
+        B.check(B.lib().vp_dataset_order(self.h, o.ctypes.data))
+        return o
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            B.lib().vp_dataset_free(self.h)
+            self.h = None
+
+
+class Context:
+    """The genotype matrix resident on one GPU."""
+
+    def __init__(self, ds: Dataset, device: int = 0):
+        h = C.c_void_p()
+        B.check(B.lib().vp_open(ds.h, device, C.byref(h)))
+        self.h = h
+        self.ds = ds
+
+    def sync(self):
+        B.check(B.lib().vp_sync(self.h))
+
+    def launches(self) -> int:
+        return int(B.lib().vp_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            B.lib().vp_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+_DT = {1: np.float32, 2: np.float32, 3: np.uint16, 4: np.int32, 5: np.int32, 6: np.float64, 7: np.float64,
+       8: np.int32, 9: np.float64, 10: np.float32, 11: np.float64, 13: np.float32, 14: np.float64}
+
+
+class Chain:
+    """One (K, replicate) run with device-resident state."""
+
+    def __init__(self, ctx: Context, p: B.VpParams):
+        h = C.c_void_p()
+        B.check(B.lib().vp_chain_create(ctx.h, C.byref(p), C.byref(h)))
+        self.h = h
+        self.ctx = ctx
+        self.p = p
+
+    def _size(self, field):
+        ds = self.ctx.ds
+        K = self.p.K
+        return {1: K * ds.KT, 2: ds.N * K, 3: ds.N, 4: K * ds.KT, 5: ds.N * K, 6: ds.N * K, 7: K, 8: 1, 9: 1,
+                10: ds.KT, 11: 2 * K, 13: ds.S * K, 14: ds.N}[field]
+
+    def get(self, name: str) -> np.ndarray:
+        f = B.FIELD[name]
+        a = np.zeros(self._size(f), dtype=_DT[f])
+        B.check(B.lib().vp_chain_get(self.h, f, a.ctypes.data, a.nbytes))
+        return a
+
+    def set(self, name: str, value) -> None:
+        f = B.FIELD[name]
+        a = np.ascontiguousarray(value, dtype=_DT[f]).reshape(-1)
+        B.check(B.lib().vp_chain_set(self.h, f, a.ctypes.data, a.nbytes))
+
+    def step(self, name: str) -> None:
+        B.check(B.lib().vp_chain_step(self.h, B.STEP[name]))
+
+    def run(self, nsweeps: int) -> None:
+        arr = (C.c_void_p * 1)(self.h)
+        B.check(B.lib().vp_run(arr, 1, nsweeps))
+
+    def result(self, final: bool = False) -> dict:
+        """Results; `final` (after vp_finish) adds the normalised ancestry."""
+        r = B.VpResult()
+        B.check(B.lib().vp_chain_sizes(self.h, C.byref(r)))
+        out = dict(rout=np.zeros(r.rlen), lnl=np.zeros(max(r.nlnl, 0)), Q=np.zeros(r.N * r.K, np.float32),
+                   ancestry=np.zeros(r.N * r.K), freqm=np.zeros(r.K * r.KT, np.float32))
+        r.rout, r.lnl, r.Q = out["rout"].ctypes.data, out["lnl"].ctypes.data, out["Q"].ctypes.data
+        r.ancestry = out["ancestry"].ctypes.data if final else None
+        r.freqm = out["freqm"].ctypes.data
+        if not final:
+            del out["ancestry"]
+        B.check(B.lib().vp_chain_result(self.h, C.byref(r)))
+        out.update(K=r.K, N=r.N, nr=r.nr, nburnin=r.nburnin, nreps=r.nreps, nthinning=r.nthinning, seed=r.seed)
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            B.lib().vp_chain_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def finish(chains: list[Chain]) -> None:
+    """Run every remaining sweep and Arrange() the results."""
+    arr = (C.c_void_p * len(chains))(*[c.h for c in chains])
+    B.check(B.lib().vp_finish(arr, len(chains)))
+
+
+def run_chains(chains: list[Chain], nsweeps: int | None = None) -> None:
+    """Advance chains that share a context together (shared launches, one graph)."""
+    arr = (C.c_void_p * len(chains))(*[c.h for c in chains])
+    if nsweeps is None:
+        B.check(B.lib().vp_finish(arr, len(chains)))
+    else:
+        B.check(B.lib().vp_run(arr, len(chains), nsweeps))
