@@ -6,6 +6,7 @@ it as the checker for the GPU library, never the other way round.
 """
 import ctypes as C
 import os
+import sys
 import subprocess
 
 import numpy as np
@@ -102,7 +103,7 @@ class Data:
         return np.ctypeslib.as_array(C.cast(p, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), shape=(n.value,)).copy()
 
     def __del__(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not sys.is_finalizing():
             lib().orc_data_free(self.h)
             self.h = None
 
@@ -169,6 +170,6 @@ class Chain:
         return out
 
     def __del__(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not sys.is_finalizing():
             lib().orc_chain_free(self.h)
             self.h = None

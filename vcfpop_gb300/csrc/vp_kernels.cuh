@@ -29,7 +29,7 @@ struct DevData {
 };
 
 struct Ctl {
-    int32_t m, nr, nlnl, pad;
+    int32_t m, nr, nlnl, done;     // done: blocks finished, for last-block reductions
     double r;
     double lnl;           // likelihood of the last sampled labels (no-admixture form)
 };
@@ -38,7 +38,7 @@ struct DevChain {
     DevData D;
     int32_t K, admix, locpriori, fmodel, nburnin, nreps, nthinning, nadmburnin, writelnl;
     int32_t metrofreq, inferalpha, diffalpha, uniformalpha, fsame, difflambda, rlen, rng, nchunk, lchunk;
-    int32_t zadm_tn, nlnlp;
+    int32_t zadm_tn, nlnlp, kp, nsampblk, zadm_lc;
     double lambda, alpha, stdalpha, maxalpha, alphapriora, alphapriorb, maxr, epsr, epseta, epsgamma;
     double pmeanf, pstdf, stdf;
     uint64_t seed;
@@ -124,7 +124,7 @@ __global__ void k_init_state(const DevChain* chains) {
     if (c.locpriori)
         for (int64_t s = tid; s < D.S; s += nt) c.SumAlpha[s] = 0;
     for (int64_t j = tid; j < c.rlen; j += nt) c.rout[j] = 0;
-    if (tid == 0) { c.ctl->m = 0; c.ctl->nr = 0; c.ctl->nlnl = 0; c.ctl->r = 1; c.ctl->lnl = 0; }
+    if (tid == 0) { c.ctl->m = 0; c.ctl->nr = 0; c.ctl->nlnl = 0; c.ctl->done = 0; c.ctl->r = 1; c.ctl->lnl = 0; }
 }
 
 // InitAdmix, single-label form (no admixture, no admixture burn-in):
@@ -211,8 +211,11 @@ __device__ __forceinline__ void write_lt(const DevChain& c, int k, int64_t l, co
     const DevData& D = c.D;
     if (D.packed2) {
         float l0 = ln_freq(p[0]), l1 = ln_freq(p[1]);
-        float4 t = make_float4(l0 + l0, l0 + l1, l1 + l1, 0.f);
-        reinterpret_cast<float4*>(c.lt)[l * c.K + k] = t;
+        float* t = c.lt + l * 4 * c.kp + k;
+        t[0] = l0 + l0;
+        t[c.kp] = l0 + l1;
+        t[2 * c.kp] = l1 + l1;
+        t[3 * c.kp] = 0.f;
     } else {
         for (int a = 0; a < k2; ++a) c.lt[k * D.KT + D.off[l] + a] = ln_freq(p[a]);
     }
@@ -286,44 +289,75 @@ __global__ void k_update_p_ctr(const DevChain* chains) {
 // ---------------------------------------------------------------------------
 // Log-likelihood of every individual under every cluster (the locus loop of
 // UpdateQNoAdmix, src/structure.cpp:902-932): LL[i,k] = sum over loci and
-// copies of ln p_{k,l,allele}. One thread per individual; grid.y splits the
-// loci into chunks whose FP64 partials are summed in a fixed order later.
-// FP32 sums over SUB loci are folded into FP64 accumulators.
+// copies of ln p_{k,l,allele}. One thread per individual, 128 per CTA; grid.y
+// splits the loci into chunks whose FP64 partials are summed in a fixed order
+// by the sampling kernel. Biallelic diploid data: each 32-locus slice of the
+// genotype words and of the per-genotype log-probability table is staged in
+// shared memory, and a thread adds table[code][k] for its individual; FP32
+// sums over a slice are folded into Kahan-compensated FP32 totals (FP64 adds
+// are slow on this part), converted to FP64 once per chunk.
+constexpr int LL_SL = 32;
+template <int KC>
+__device__ __forceinline__ void kahan_fold(float* acc, float* s, float* cmp) {
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+        float y = acc[k] - cmp[k];
+        float t = s[k] + y;
+        cmp[k] = (t - s[k]) - y;
+        s[k] = t;
+        acc[k] = 0.f;
+    }
+}
 template <int KC>
 __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int kgroups, int force) {
+    constexpr int TS = KC + 4;  // padded stride of one genotype row of the table
+    __shared__ __align__(16) float sT[LL_SL][4][TS];
+    __shared__ uint32_t sG[LL_SL][LL_BLOCK / 16];
     const DevChain& c = chains[blockIdx.z / kgroups];
     const int kg0 = (blockIdx.z % kgroups) * KC;
     const DevData& D = c.D;
     const int K = c.K;
     if (!force && !binaryq_at(c, c.ctl->m)) return;
-    const int i = blockIdx.x * LL_BLOCK + threadIdx.x;
+    const int i0 = blockIdx.x * LL_BLOCK;
+    const int i = i0 + threadIdx.x;
     const int64_t l0 = (int64_t)blockIdx.y * c.lchunk;
     const int64_t l1 = min(D.L, l0 + c.lchunk);
     if (l0 >= D.L) return;
-    double accd[KC];
-    float acc[KC];
+    float acc[KC], s[KC], cmp[KC];
 #pragma unroll
-    for (int k = 0; k < KC; ++k) { accd[k] = 0; acc[k] = 0.f; }
+    for (int k = 0; k < KC; ++k) { acc[k] = 0.f; s[k] = 0.f; cmp[k] = 0.f; }
     const bool live = i < D.N;
-    int cnt = 0;
     if (D.packed2) {
-        const float4* T = reinterpret_cast<const float4*>(c.lt);
-        const uint32_t* g = D.g2 + (i >> 4);
-        const int sh = (i & 15) * 2;
-        for (int64_t l = l0; l < l1; ++l) {
-            uint32_t w = live ? __ldg(g + l * D.Nw) : 0xFFFFFFFFu;
-            int code = (w >> sh) & 3;
-            const float* t = reinterpret_cast<const float*>(T + l * K + kg0) + code;
-#pragma unroll
-            for (int k = 0; k < KC; ++k)
-                if (kg0 + k < K) acc[k] += __ldg(t + 4 * k);
-            if (++cnt == SUB) {
-                cnt = 0;
-#pragma unroll
-                for (int k = 0; k < KC; ++k) { accd[k] += acc[k]; acc[k] = 0.f; }
+        const int w0 = i0 >> 4;
+        for (int64_t ls = l0; ls < l1; ls += LL_SL) {
+            const int nl = (int)min((int64_t)LL_SL, l1 - ls);
+            __syncthreads();
+            for (int j = threadIdx.x; j < LL_SL * 4 * KC; j += LL_BLOCK) {
+                int kk = j % KC, code = (j / KC) & 3, ll = j / (4 * KC);
+                float v = 0.f;
+                if (ll < nl && kg0 + kk < K) v = __ldg(c.lt + ((ls + ll) * 4 + code) * c.kp + kg0 + kk);
+                sT[ll][code][kk] = v;
             }
+            for (int j = threadIdx.x; j < LL_SL * (LL_BLOCK / 16); j += LL_BLOCK) {
+                int w = j % (LL_BLOCK / 16), ll = j / (LL_BLOCK / 16);
+                sG[ll][w] = (ll < nl && w0 + w < D.Nw) ? __ldg(D.g2 + (ls + ll) * D.Nw + w0 + w) : 0xFFFFFFFFu;
+            }
+            __syncthreads();
+            const int wsel = threadIdx.x >> 4, sh = (threadIdx.x & 15) * 2;
+#pragma unroll 4
+            for (int ll = 0; ll < nl; ++ll) {
+                const int code = (sG[ll][wsel] >> sh) & 3;
+                const float4* t = reinterpret_cast<const float4*>(&sT[ll][code][0]);
+#pragma unroll
+                for (int q = 0; q < KC / 4; ++q) {
+                    float4 v = t[q];
+                    acc[4 * q] += v.x; acc[4 * q + 1] += v.y; acc[4 * q + 2] += v.z; acc[4 * q + 3] += v.w;
+                }
+            }
+            kahan_fold<KC>(acc, s, cmp);
         }
     } else {
+        int cnt = 0;
         for (int64_t l = l0; l < l1; ++l) {
             Copies cp;
             if (live) load_copies(D, l, i, cp); else cp.n = 0;
@@ -333,18 +367,15 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
                 for (int k = 0; k < KC; ++k)
                     if (kg0 + k < K) acc[k] += __ldg(t + (int64_t)(kg0 + k) * D.KT + cp.a[a]);
             }
-            if (++cnt == SUB) {
-                cnt = 0;
-#pragma unroll
-                for (int k = 0; k < KC; ++k) { accd[k] += acc[k]; acc[k] = 0.f; }
-            }
+            if (++cnt == SUB) { cnt = 0; kahan_fold<KC>(acc, s, cmp); }
         }
+        kahan_fold<KC>(acc, s, cmp);
     }
     if (!live) return;
     double* out = c.LLp + ((int64_t)blockIdx.y * D.N + i) * K;
 #pragma unroll
     for (int k = 0; k < KC; ++k)
-        if (kg0 + k < K) out[kg0 + k] = accd[k] + (double)acc[k];
+        if (kg0 + k < K) out[kg0 + k] = (double)s[k] - (double)cmp[k];
 }
 
 // PolyLog (src/statistics.cpp:116-155): draw k with probability proportional
@@ -370,48 +401,84 @@ __device__ __forceinline__ int polylog(double* ll, int K, double u01, bool ref, 
 // (src/structure.cpp:1305-1310), Di for the location prior (1151-1158) and the
 // likelihood of the new labels, sum_i LL[i, Z_i], which is exactly what Record
 // computes for a no-admixture sweep (src/structure.cpp:1902-1938).
+// Reference streams are serial over individuals (one thread walks them all);
+// counter streams use one thread per individual, and the last block to finish
+// reduces the per-block likelihoods in a fixed order and rebuilds Di.
 constexpr int SAMPLE_BLOCK = 256;
+__device__ __forceinline__ bool last_block_done(Ctl* ctl, int nblocks) {
+    __shared__ int is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = atomicAdd(&ctl->done, 1) == nblocks - 1;
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+__device__ void sample_one(const DevChain& c, int i, int m, bool ref, Rng64* r, double* lnl) {
+    const DevData& D = c.D;
+    const int K = c.K, N = D.N;
+    double ll[64];
+    for (int k = 0; k < K; ++k) ll[k] = 0;
+    for (int ch = 0; ch < c.nchunk; ++ch) {
+        const double* p = c.LLp + ((int64_t)ch * N + i) * K;
+        for (int k = 0; k < K; ++k) ll[k] += p[k];
+    }
+    for (int k = 0; k < K; ++k) c.LL[(int64_t)i * K + k] = ll[k];
+    for (int k = 0; k < K; ++k) { c.Q[(int64_t)i * K + k] = 0.f; c.Mi[(int64_t)i * K + k] = 0; }
+    if (D.vt[i] == 0) return;
+    if (c.locpriori) {
+        const double* g = c.Gamma + D.popid[i] * K;
+        for (int k = 0; k < K; ++k) ll[k] += log(g[k]);
+    }
+    double u = 0;
+    if (!ref) { Philox ph; ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0); u = ph.uniformd(); }
+    double keep[64];
+    for (int k = 0; k < K; ++k) keep[k] = c.LL[(int64_t)i * K + k];
+    int z = polylog(ll, K, u, ref, r);
+    c.Q[(int64_t)i * K + z] = 1.f;
+    c.Z[i] = (uint16_t)z;
+    c.Mi[(int64_t)i * K + z] = (int32_t)D.vt[i];
+    *lnl += keep[z];
+}
 __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain* chains, int force) {
     const DevChain& c = chains[blockIdx.z];
     const DevData& D = c.D;
     const int K = c.K, N = D.N, m = c.ctl->m;
     if (!force && !binaryq_at(c, m)) return;
     __shared__ double sh[32];
-    double lnl = 0;
-    double ll[64];
     const bool ref = c.rng == 0;
-    Rng64 r;
-    if (ref) r.init(c.seed + (uint64_t)m, VP_SALT_UPDATEQ);
-    // reference streams are serial over individuals: one thread walks them all
-    for (int i = ref ? 0 : threadIdx.x; i < N; i += ref ? 1 : blockDim.x) {
-        if (ref && threadIdx.x) break;
-        for (int k = 0; k < K; ++k) ll[k] = 0;
-        for (int ch = 0; ch < c.nchunk; ++ch) {
-            const double* p = c.LLp + ((int64_t)ch * N + i) * K;
-            for (int k = 0; k < K; ++k) ll[k] += p[k];
-        }
-        for (int k = 0; k < K; ++k) c.LL[(int64_t)i * K + k] = ll[k];
-        if (force) continue;
-        for (int k = 0; k < K; ++k) c.Q[(int64_t)i * K + k] = 0.f;
-        for (int k = 0; k < K; ++k) c.Mi[(int64_t)i * K + k] = 0;
-        if (D.vt[i] == 0) continue;
-        double lln[64];
-        for (int k = 0; k < K; ++k) lln[k] = ll[k];
-        if (c.locpriori) {
-            const double* g = c.Gamma + D.popid[i] * K;
-            for (int k = 0; k < K; ++k) ll[k] += log(g[k]);
-        }
-        double u = 0;
-        if (!ref) { Philox ph; ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0); u = ph.uniformd(); }
-        int z = polylog(ll, K, u, ref, &r);
-        c.Q[(int64_t)i * K + z] = 1.f;
-        c.Z[i] = (uint16_t)z;
-        c.Mi[(int64_t)i * K + z] = (int32_t)D.vt[i];
-        lnl += lln[z];
+    if (force) {
+        // likelihood only (parity tests): sum the chunk partials
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+            for (int k = 0; k < K; ++k) {
+                double v = 0;
+                for (int ch = 0; ch < c.nchunk; ++ch) v += c.LLp[((int64_t)ch * N + i) * K + k];
+                c.LL[(int64_t)i * K + k] = v;
+            }
+        return;
     }
-    if (force) return;
-    double tot = ref ? lnl : block_sum(lnl, sh);
-    if (threadIdx.x == 0) c.ctl->lnl = tot;
+    if (ref) {
+        if (blockIdx.x) return;
+        if (threadIdx.x == 0) {
+            Rng64 r; r.init(c.seed + (uint64_t)m, VP_SALT_UPDATEQ);
+            double lnl = 0;
+            for (int i = 0; i < N; ++i) sample_one(c, i, m, true, &r, &lnl);
+            c.ctl->lnl = lnl;
+        }
+    } else {
+        double lnl = 0;
+        int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < N) sample_one(c, i, m, false, nullptr, &lnl);
+        double t = block_sum(lnl, sh);
+        if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
+        if (!last_block_done(c.ctl, gridDim.x)) return;
+        if (threadIdx.x == 0) {
+            double tot = 0;
+            for (int b = 0; b < (int)gridDim.x; ++b) tot += c.lnlp[b];
+            c.ctl->lnl = tot;
+            c.ctl->done = 0;
+        }
+    }
     if (c.locpriori) {
         __syncthreads();
         for (int j = threadIdx.x; j < D.S * K; j += blockDim.x) c.Di[j] = 0.f;
@@ -423,9 +490,11 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain*
 }
 
 // UpdateZNoAdmix (src/structure.cpp:1257-1301): Ni[k,l,a] = copies of allele a
-// at locus l among individuals labelled k. One warp per locus; per-warp shared
-// histograms take the per-call increments, then the warp writes its row.
-constexpr int COUNT_WARPS = 8;
+// at locus l among individuals labelled k. One warp per locus. Biallelic
+// diploid data: lane j takes individuals j, j+32, ... (coalesced codes and
+// labels) into a lane-private shared histogram (no atomics, no conflicts), and
+// the warp reduces it. General data: per-warp shared histogram with atomics.
+constexpr int COUNT_WARPS = 4;
 __global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevChain* chains, int force) {
     extern __shared__ int32_t hist[];
     const DevChain& c = chains[blockIdx.z];
@@ -434,32 +503,38 @@ __global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevCha
     if (!force && !binaryq_at(c, c.ctl->m)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t l = (int64_t)blockIdx.x * COUNT_WARPS + warp;
+    if (D.packed2) {
+        int32_t* h = hist + warp * (2 * K * 32);
+        for (int j = 0; j < 2 * K; ++j) h[j * 32 + lane] = 0;
+        if (l < D.L) {
+            const uint32_t* row = D.g2 + l * D.Nw;
+            for (int i = lane; i < D.N; i += 32) {
+                int code = (__ldg(row + (i >> 4)) >> ((i & 15) * 2)) & 3;
+                if (code == 3) continue;
+                int z = c.Z[i];
+                h[(z * 2) * 32 + lane] += 2 - code;
+                h[(z * 2 + 1) * 32 + lane] += code;
+            }
+            const int64_t o = D.off[l];
+            for (int j = 0; j < 2 * K; ++j) {
+                int v = h[j * 32 + lane];
+                for (int sft = 16; sft > 0; sft >>= 1) v += __shfl_xor_sync(0xffffffffu, v, sft);
+                if (lane == 0) c.Ni[(j >> 1) * D.KT + o + (j & 1)] = v;
+            }
+        }
+        return;
+    }
     const int hsz = K * D.maxK;
     int32_t* h = hist + warp * hsz;
     for (int j = lane; j < hsz; j += 32) h[j] = 0;
     __syncwarp();
     if (l < D.L) {
-        if (D.packed2) {
-            const uint32_t* row = D.g2 + l * D.Nw;
-            for (int w = lane; w < D.Nw; w += 32) {
-                uint32_t word = row[w];
-                int i0 = w * 16;
-                for (int j = 0; j < 16 && i0 + j < D.N; ++j) {
-                    int code = (word >> (2 * j)) & 3;
-                    if (code == 3) continue;
-                    int z = c.Z[i0 + j];
-                    if (code != 2) atomicAdd(&h[z * 2 + 0], 2 - code);
-                    if (code != 0) atomicAdd(&h[z * 2 + 1], code);
-                }
-            }
-        } else {
-            int k2 = D.k[l];
-            for (int i = lane; i < D.N; i += 32) {
-                Copies cp;
-                load_copies(D, l, i, cp);
-                int z = c.Z[i];
-                for (int a = 0; a < cp.n; ++a) atomicAdd(&h[z * k2 + cp.a[a]], 1);
-            }
+        int k2 = D.k[l];
+        for (int i = lane; i < D.N; i += 32) {
+            Copies cp;
+            load_copies(D, l, i, cp);
+            int z = c.Z[i];
+            for (int a = 0; a < cp.n; ++a) atomicAdd(&h[z * k2 + cp.a[a]], 1);
         }
     }
     __syncwarp();
@@ -665,65 +740,99 @@ __global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
     if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
 }
 
-// UpdateZAdmix with counter streams: the CTA takes 32 loci (one per lane) and
-// an individual tile split across its warps; Q of the tile, Mi of the tile and
-// Ni of the 32 loci are staged in shared memory and flushed once.
+// UpdateZAdmix with counter streams. Warp = 32 individuals (one per lane),
+// CTA = 8 warps = 256 individuals; grid.y splits the loci into ranges that a
+// CTA walks in slices of ZA_LC loci. A lane keeps its individual's Q row and
+// its Mi counts in registers; the slice's frequencies are staged in shared
+// memory; the per-copy increments of Ni are aggregated across the warp
+// (lanes with equal cluster and allele) before one shared-memory add, and the
+// slice histogram is flushed to Ni with one global atomic per entry.
 constexpr int ZA_WARPS = 8;
+constexpr int ZA_LC = 16;
+template <int KM>
 __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevChain* chains, int force) {
     extern __shared__ unsigned char smraw[];
     const DevChain& c = chains[blockIdx.z];
     const DevData& D = c.D;
-    const int K = c.K, m = c.ctl->m;
+    const int K = c.K, m = c.ctl->m, MK = D.maxK;
     if (!force && binaryq_at(c, m)) return;
-    const int TN = c.zadm_tn;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i0 = blockIdx.y * TN;
-    const int nin = min(TN, D.N - i0);
-    float* qs = reinterpret_cast<float*>(smraw);                 // [TN][K]
-    int32_t* mis = reinterpret_cast<int32_t*>(qs + TN * K);      // [TN][K]
-    int32_t* nis = mis + TN * K;                                  // [32][K][maxK]
     __shared__ double sh[32];
-    for (int j = threadIdx.x; j < nin * K; j += blockDim.x) { qs[j] = c.Q[(int64_t)i0 * K + j]; mis[j] = 0; }
-    for (int j = threadIdx.x; j < 32 * K * D.maxK; j += blockDim.x) nis[j] = 0;
-    __syncthreads();
-    const int64_t l = (int64_t)blockIdx.x * 32 + lane;
-    double lnl = 0;
-    if (l < D.L) {
-        const int64_t o = D.off[l];
-        const int k2n = D.k[l];
-        float w[64];
-        for (int ii = warp; ii < nin; ii += ZA_WARPS) {
-            const int i = i0 + ii;
+    const int KPAD = K | 1;                                       // odd stride: no bank conflicts
+    float* sF = reinterpret_cast<float*>(smraw);                  // [ZA_LC][MK][KPAD]
+    int32_t* hs = reinterpret_cast<int32_t*>(sF + ZA_LC * MK * KPAD);  // [ZA_LC][K][MK]
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (ZA_WARPS * 32) + threadIdx.x;
+    const bool live = i < D.N;
+    float q[KM];
+    int32_t mi[KM];
+#pragma unroll
+    for (int k = 0; k < KM; ++k) { q[k] = (live && k < K) ? c.Q[(int64_t)i * K + k] : 0.f; mi[k] = 0; }
+    const int64_t lb0 = (int64_t)blockIdx.y * c.zadm_lc, lb1 = min(D.L, lb0 + c.zadm_lc);
+    float ls = 0.f, lc = 0.f;  // Kahan sum of ln(sum_k q_k p)
+    for (int64_t l0 = lb0; l0 < lb1; l0 += ZA_LC) {
+        const int nl = (int)min((int64_t)ZA_LC, lb1 - l0);
+        __syncthreads();
+        for (int j = threadIdx.x; j < ZA_LC * MK * KPAD; j += blockDim.x) {
+            int k = j % KPAD, a = (j / KPAD) % MK, ll = j / (KPAD * MK);
+            float v = 0.f;
+            if (ll < nl && k < K && a < D.k[l0 + ll]) v = __ldg(c.Freq + (int64_t)k * D.KT + D.off[l0 + ll] + a);
+            sF[j] = v;
+        }
+        for (int j = threadIdx.x; j < ZA_LC * K * MK; j += blockDim.x) hs[j] = 0;
+        __syncthreads();
+        for (int ll = 0; ll < nl; ++ll) {
+            const int64_t l = l0 + ll;
             Copies cp;
-            load_copies(D, l, i, cp);
-            if (!cp.n) continue;
+            if (live) load_copies(D, l, i, cp); else cp.n = 0;
             Philox ph;
             ph.init(c.seed, ST_Z | ((uint32_t)m << 4), (uint32_t)l, (uint32_t)i);
-            const float* q = qs + ii * K;
             float lacc = 0.f;
-            for (int a = 0; a < cp.n; ++a) {
+            for (int a = 0; a < D.vmax; ++a) {
+                const bool act = a < cp.n;
+                const unsigned am = __ballot_sync(0xffffffffu, act);
+                if (!act) continue;
+                const int al = cp.a[a];
+                const float* f = sF + (ll * MK + al) * KPAD;
                 float sx = 0.f;
-                for (int k = 0; k < K; ++k) { w[k] = q[k] * __ldg(c.Freq + k * D.KT + o + cp.a[a]); sx += w[k]; }
+#pragma unroll
+                for (int k = 0; k < KM; ++k)
+                    if (k < K) sx += q[k] * f[k];
                 lacc += logf(sx);
-                int k2 = poly_f(w, K, ph.uniformf(), nullptr);
-                atomicAdd(&mis[ii * K + k2], 1);
-                atomicAdd(&nis[(lane * K + k2) * D.maxK + cp.a[a]], 1);
+                // Poly (src/statistics.cpp:357-385) on the same float weights
+                float t = ph.uniformf() * (sx + (float)(VP_MIN_FREQ * K));
+                int k2 = K - 1;
+                bool found = false;
+#pragma unroll
+                for (int k = 0; k < KM; ++k) {
+                    if (k < K && !found) {
+                        const float w = q[k] * f[k] + (float)VP_MIN_FREQ;
+                        if (t < w) { k2 = k; found = true; }
+                        else t -= w;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < KM; ++k) mi[k] += (k == k2);
+                const int key = k2 * MK + al;
+                const unsigned grp = __match_any_sync(am, key);
+                if (lane == __ffs(grp) - 1) atomicAdd(&hs[(ll * K + k2) * MK + al], __popc(grp));
             }
-            lnl += lacc;
+            float y = lacc - lc, tt = ls + y;
+            lc = (tt - ls) - y;
+            ls = tt;
         }
-        (void)k2n;
+        __syncthreads();
+        for (int j = threadIdx.x; j < ZA_LC * K * MK; j += blockDim.x) {
+            int v = hs[j];
+            if (!v) continue;
+            int a = j % MK, k = (j / MK) % K, ll = j / (MK * K);
+            atomicAdd(&c.Ni[(int64_t)k * D.KT + D.off[l0 + ll] + a], v);
+        }
     }
-    __syncthreads();
-    for (int j = threadIdx.x; j < nin * K; j += blockDim.x)
-        if (mis[j]) atomicAdd(&c.Mi[(int64_t)i0 * K + j], mis[j]);
-    for (int j = threadIdx.x; j < 32 * K * D.maxK; j += blockDim.x) {
-        int v = nis[j];
-        if (!v) continue;
-        int a = j % D.maxK, k = (j / D.maxK) % K, ln = j / (D.maxK * K);
-        int64_t ll = (int64_t)blockIdx.x * 32 + ln;
-        atomicAdd(&c.Ni[k * D.KT + D.off[ll] + a], v);
-    }
-    double t = block_sum(lnl, sh);
+    if (live)
+#pragma unroll
+        for (int k = 0; k < KM; ++k)
+            if (k < K && mi[k]) atomicAdd(&c.Mi[(int64_t)i * K + k], mi[k]);
+    double t = block_sum((double)ls - (double)lc, sh);
     if (threadIdx.x == 0) c.lnlp[blockIdx.y * gridDim.x + blockIdx.x] = t;
 }
 
@@ -769,32 +878,52 @@ __device__ double logprod_d_serial(const double* a, int64_t n, int64_t sep) {
 //   location prior+admix:  ln prod Q[i in s, k] (S*K outputs)
 // Reference streams use the serial exponent-split product (a zero resets its
 // running mantissa, as in the reference); counter streams a parallel sum.
+constexpr int LPQ_BLOCKS = 64;
 __global__ void k_logprod_q(const DevChain* chains) {
     const DevChain& c = chains[blockIdx.z];
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
     __shared__ double sh[32];
-    int nseq;
-    if (c.locpriori && c.admix) nseq = D.S * K;
-    else if (c.inferalpha && (c.admix || m < c.nadmburnin)) nseq = c.diffalpha ? K : 1;
+    int nseq, mode;
+    if (c.locpriori && c.admix) { nseq = D.S * K; mode = 2; }
+    else if (c.inferalpha && (c.admix || m < c.nadmburnin)) { nseq = c.diffalpha ? K : 1; mode = c.diffalpha; }
     else return;
-    for (int s = blockIdx.x; s < nseq; s += gridDim.x) {
-        const float* base; int64_t n, sep;
-        if (c.locpriori && c.admix) { int sp = s / K, k = s % K; base = c.Q + (int64_t)D.pop_ind0[sp] * K + k; n = D.pop_nind[sp]; sep = K; }
-        else if (c.diffalpha) { base = c.Q + s; n = D.N; sep = K; }
-        else { base = c.Q; n = (int64_t)D.N * K; sep = 1; }
-        if (c.rng == 0) {
-            if (threadIdx.x == 0) c.red[s] = logprod_f_serial(base, n, sep);
-        } else {
-            double v = 0;
-            for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-                float q = base[j * sep];
-                v += q > 0.f ? log((double)q) : -709.0895657128241;
-            }
-            v = block_sum(v, sh);
-            if (threadIdx.x == 0) c.red[s] = v;
+    if (c.rng == 0) {
+        // reference streams: the serial exponent-split product, one thread per sequence
+        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseq; s += gridDim.x * blockDim.x) {
+            const float* base; int64_t n, sep;
+            if (mode == 2) { int sp = s / K, k = s % K; base = c.Q + (int64_t)D.pop_ind0[sp] * K + k; n = D.pop_nind[sp]; sep = K; }
+            else if (mode == 1) { base = c.Q + s; n = D.N; sep = K; }
+            else { base = c.Q; n = (int64_t)D.N * K; sep = 1; }
+            c.red[s] = logprod_f_serial(base, n, sep);
         }
+        return;
     }
+    // counter streams: sum of ln Q per sequence, per-block partials reduced by
+    // the last block in a fixed order
+    double* part = c.red + (D.S * K + K + 1);   // [LPQ_BLOCKS][nseq]
+    const int64_t NK = (int64_t)D.N * K;
+    for (int s = 0; s < nseq; ++s) {
+        double v = 0;
+        const int64_t per = (NK + gridDim.x - 1) / gridDim.x;
+        const int64_t j0 = blockIdx.x * per, j1 = min(NK, j0 + per);
+        for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+            const int i = (int)(j / K), k = (int)(j % K);
+            const int sq = mode == 2 ? D.popid[i] * K + k : mode == 1 ? k : 0;
+            if (sq != s) continue;
+            const float q = c.Q[j];
+            v += q > 0.f ? (double)logf(q) : -709.0895657128241;
+        }
+        v = block_sum(v, sh);
+        if (threadIdx.x == 0) part[blockIdx.x * nseq + s] = v;
+    }
+    if (!last_block_done(c.ctl, gridDim.x)) return;
+    for (int s = threadIdx.x; s < nseq; s += blockDim.x) {
+        double t = 0;
+        for (int b2 = 0; b2 < (int)gridDim.x; ++b2) t += part[b2 * nseq + s];
+        c.red[s] = t;
+    }
+    if (threadIdx.x == 0) c.ctl->done = 0;
 }
 
 // UpdateAlpha (src/structure.cpp:1499-1594), reference stream

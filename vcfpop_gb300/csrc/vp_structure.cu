@@ -104,9 +104,39 @@ int launch_loglik(vp_chain* c, int force) {
     return VP_OK;
 }
 
-size_t count_smem(const vp_chain* c) { return (size_t)COUNT_WARPS * c->P.K * c->ctx->maxK * sizeof(int32_t); }
+size_t count_smem(const vp_chain* c) {
+    if (c->ctx->packed2) return (size_t)COUNT_WARPS * 2 * c->P.K * 32 * sizeof(int32_t);
+    return (size_t)COUNT_WARPS * c->P.K * c->ctx->maxK * sizeof(int32_t);
+}
 size_t zadm_smem(const vp_chain* c) {
-    return (size_t)c->h.zadm_tn * c->P.K * 8 + (size_t)32 * c->P.K * c->ctx->maxK * 4;
+    const int K = c->P.K, MK = c->ctx->maxK;
+    return (size_t)ZA_LC * MK * (K | 1) * 4 + (size_t)ZA_LC * K * MK * 4;
+}
+int km_for(int K) { return K <= 8 ? 8 : K <= 16 ? 16 : K <= 32 ? 32 : 64; }
+
+int launch_zadm_ctr(vp_chain* c, int force) {
+    vp_ctx* x = c->ctx;
+    dim3 g(cdiv(x->N, ZA_WARPS * 32), cdiv(x->L, c->h.zadm_lc), 1);
+    size_t sm = zadm_smem(c);
+    switch (km_for(c->P.K)) {
+        case 8: LAUNCH(x, k_update_z_admix_ctr<8>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
+        case 16: LAUNCH(x, k_update_z_admix_ctr<16>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
+        case 32: LAUNCH(x, k_update_z_admix_ctr<32>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
+        default: LAUNCH(x, k_update_z_admix_ctr<64>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
+    }
+    return VP_OK;
+}
+
+void set_smem_limits() {
+    static bool done = false;
+    if (done) return;
+    done = true;
+    const int big = 200 * 1024;
+    cudaFuncSetAttribute(k_count_noadmix, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_update_z_admix_ctr<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_update_z_admix_ctr<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_update_z_admix_ctr<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_update_z_admix_ctr<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 }
 
 int launch_step(vp_chain* c, int step, int force) {
@@ -123,7 +153,7 @@ int launch_step(vp_chain* c, int step, int force) {
         case VP_STEP_LOGLIK: {
             int rc = launch_loglik(c, 1);
             if (rc) return rc;
-            LAUNCH(x, k_sample_noadmix, (dim3(1, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 1));
+            LAUNCH(x, k_sample_noadmix, (dim3(c->h.nsampblk, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 1));
             return VP_OK;
         }
         case VP_STEP_UPDATEQ: {
@@ -132,7 +162,7 @@ int launch_step(vp_chain* c, int step, int force) {
                 if (!force || true) {
                     int rc = launch_loglik(c, force);
                     if (rc) return rc;
-                    LAUNCH(x, k_sample_noadmix, (dim3(1, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 0));
+                    LAUNCH(x, k_sample_noadmix, (dim3(ref ? 1 : c->h.nsampblk, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 0));
                 }
                 if (c->h.nadmburnin > 0) LAUNCH(x, k_update_q_admix, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
             } else {
@@ -155,14 +185,15 @@ int launch_step(vp_chain* c, int step, int force) {
                 LAUNCH(x, k_zero_counts, (dim3(std::min<unsigned>(1024, cdiv((int64_t)K * x->KT, 256)), 1, 1), 256, 0, s), (c->d, 0));
                 if (ref)
                     LAUNCH(x, k_update_z_admix_ref, (dim3(cdiv(x->L, 128), 1, 1), 128, 0, s), (c->d, 0));
-                else
-                    LAUNCH(x, k_update_z_admix_ctr, (dim3(cdiv(x->L, 32), cdiv(x->N, c->h.zadm_tn), 1), ZA_WARPS * 32,
-                           zadm_smem(c), s), (c->d, 0));
+                else {
+                    int rc = launch_zadm_ctr(c, 0);
+                    if (rc) return rc;
+                }
             }
             return VP_OK;
         case VP_STEP_ALPHA:
             if ((P.inferalpha && (P.admix || c->h.nadmburnin > 0)) || (P.locpriori && P.admix)) {
-                LAUNCH(x, k_logprod_q, (dim3(std::max(1, std::min(x->S * K, 256)), 1, 1), 256, 0, s), (c->d));
+                LAUNCH(x, k_logprod_q, (dim3(ref ? std::max(1, (x->S * K + 255) / 256) : LPQ_BLOCKS, 1, 1), 256, 0, s), (c->d));
                 LAUNCH(x, k_update_alpha, (dim3(1, 1, 1), 32, 0, s), (c->d));
             }
             return VP_OK;
@@ -258,7 +289,6 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
     if (!x || !P || !out) { vp_set_error("null argument"); return VP_E_ARG; }
     if (P->K < 1 || P->K > 64) { vp_set_error("K must be in 1..64"); return VP_E_ARG; }
     if (P->nthinning < 1 || P->nburnin < 0 || P->nreps < 0) { vp_set_error("bad MCMC lengths"); return VP_E_ARG; }
-    if ((int64_t)P->K * x->maxK > 3072) { vp_set_error("K * max alleles must be <= 3072"); return VP_E_ARG; }
     cudaSetDevice(x->device);
     auto* c = new vp_chain();
     c->ctx = x;
@@ -294,11 +324,22 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
         h.lchunk = (int32_t)((L + nch - 1) / nch);
         h.nchunk = (int32_t)((L + h.lchunk - 1) / h.lchunk);
     }
-    h.zadm_tn = 256;
-    while (h.zadm_tn > 32 && zadm_smem(c) > 96 * 1024) h.zadm_tn /= 2;
-    h.nlnlp = (int32_t)std::max<int64_t>(cdiv(L, 128), (int64_t)cdiv(L, 32) * cdiv(N, h.zadm_tn));
+    set_smem_limits();
+    h.kp = (K + 3) & ~3;
+    h.nsampblk = (int32_t)cdiv(N, SAMPLE_BLOCK);
+    {
+        // loci per CTA of the per-copy label kernel: about 4 CTAs per SM
+        int64_t nx = cdiv(N, ZA_WARPS * 32);
+        int64_t ny = std::max<int64_t>(1, (int64_t)x->nsm * 4 / nx);
+        int64_t lc = (L + ny - 1) / ny;
+        lc = (lc + ZA_LC - 1) / ZA_LC * ZA_LC;
+        h.zadm_lc = (int32_t)std::max<int64_t>(lc, ZA_LC);
+    }
+    if (zadm_smem(c) > 200 * 1024) { vp_set_error("K * max alleles too large for the admixture kernel"); delete c; return VP_E_ARG; }
+    h.nlnlp = (int32_t)std::max<int64_t>(std::max<int64_t>(cdiv(L, 128), (int64_t)cdiv(N, ZA_WARPS * 32) * cdiv(L, h.zadm_lc)),
+                                         h.nsampblk);
     const int64_t ntrace = h.nburnin / h.nthinning + h.nreps / h.nthinning + 2;
-    const int64_t ltn = x->packed2 ? L * K * 4 : (int64_t)K * KT;
+    const int64_t ltn = x->packed2 ? L * 4 * h.kp : (int64_t)K * KT;
     auto layout = [&](Carve& cv) {
         h.ctl = cv.take<Ctl>(1);
         h.rstate = cv.take<Rng64>(1);
@@ -328,7 +369,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
         h.SumAlpha = cv.take<double>(S);
         h.rout = cv.take<double>(h.rlen);
         h.lnlTrace = cv.take<double>(ntrace);
-        h.red = cv.take<double>((int64_t)S * K + K + 1);
+        h.red = cv.take<double>(((int64_t)S * K + K + 1) * (1 + LPQ_BLOCKS));
         h.lnlp = cv.take<double>(h.nlnlp);
         c->ancestry = cv.take<double>((int64_t)N * K);
         c->d = cv.take<DevChain>(1);

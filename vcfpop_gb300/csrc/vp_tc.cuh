@@ -1,0 +1,260 @@
+// Tensor-core contraction for the batched no-admixture K-sweep (sm_103a).
+//
+//   D[m, n] = sum_k A[m, k] * (B0[n, k] + B1[n, k])        (B1 optional)
+//
+// A, B0, B1 are bf16, K-major (k contiguous) in global memory and are staged
+// into shared memory by TMA with the 128-byte swizzle; one thread issues
+// tcgen05.mma (kind::f16, bf16 x bf16 -> f32) into a TMEM accumulator of
+// 128 lanes x BN columns; four epilogue warps read it back with tcgen05.ld.
+// With B1 given, the hi and lo halves of a split-bf16 operand accumulate into
+// the same FP32 accumulator.
+//
+// Warp roles (192 threads): warp 0 TMA producer, warp 1 TMEM allocator and MMA
+// issuer, warps 2..5 epilogue (warp w reads TMEM lanes 32*(w%4)..+31).
+// Every mbarrier wait is bounded: on time-out the CTA records an error code
+// in *err, drains its own copies in flight (bounded), frees its TMEM and
+// returns.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vp {
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int BK = 64;                 // bf16 elements per 128-byte swizzle row
+constexpr int NTHREADS = 192;
+constexpr uint32_t SPIN_LIMIT = 1u << 26;
+
+struct GemmArgs {
+    int M, N;               // rows of A / D, columns of D (= rows of B)
+    int kblocks;            // K / BK of the whole problem
+    int kb_per_split;       // k-blocks handled by one CTA (grid.z splits K)
+    int BN;                 // columns per CTA (multiple of 16, <= 512)
+    int piece;              // columns per MMA instruction (<= 256, multiple of 16)
+    int nb;                 // 1 or 2 B operands
+    int stages;
+    int mode;               // 0: FP32 partials D[z][m][n]; 1: int32 transpose Dt[n][m] (no split)
+    float* out_f;           // mode 0: [splits][M][ldo]
+    int32_t* out_i;         // mode 1: [N][ldo]
+    int64_t ldo;
+    int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// bounded wait on a phase parity; returns false on time-out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t addr = smem_u32(bar);
+    for (uint32_t it = 0; it < SPIN_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), sm100 descriptor version 1
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
+    d |= (uint64_t)1 << 46;                 // version
+    d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor: D f32, A bf16, B bf16, both K-major, M = 128
+__device__ __forceinline__ uint32_t idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// dynamic shared memory: [stages][A tile | B0 tile | B1 tile] (1024-aligned),
+// then barriers
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_gemm_bf16(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB0,
+                const __grid_constant__ CUtensorMap mapB1, GemmArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t a_bytes = BM * BK * 2;
+    const uint32_t b_bytes = (uint32_t)g.BN * BK * 2;
+    const uint32_t stage_bytes = a_bytes + b_bytes * g.nb;
+    uint64_t* full = (uint64_t*)(smem + (size_t)stage_bytes * g.stages);
+    uint64_t* empty = full + g.stages;
+    uint64_t* accum = empty + g.stages;
+    uint32_t* tmem_holder = (uint32_t*)(accum + 1);
+    int* abort_flag = (int*)(tmem_holder + 1);
+
+    const int m0 = blockIdx.x * BM;
+    const int n0 = blockIdx.y * g.BN;
+    const int kb0 = blockIdx.z * g.kb_per_split;
+    const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
+    const int nk = kb1 - kb0;
+    uint32_t ncols = 32;
+    while ((int)ncols < g.BN) ncols <<= 1;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < g.stages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        mbar_init(accum, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_holder;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0 && nk > 0) {
+            int issued = 0;
+            for (int it = 0; it < nk; ++it) {
+                const int s = it % g.stages;
+                if (it >= g.stages && !mbar_wait(&empty[s], ((it / g.stages) & 1) ^ 1)) {
+                    atomicExch(g.err, 1);
+                    *(volatile int*)abort_flag = 1;
+                    break;
+                }
+                if (*(volatile int*)abort_flag) break;
+                unsigned char* st = smem + (size_t)s * stage_bytes;
+                mbar_expect_tx(&full[s], stage_bytes);
+                const int kx = (kb0 + it) * BK;
+                tma_load_2d(st, &mapA, &full[s], kx, m0);
+                for (int b = 0; b < g.nb; ++b) {
+                    unsigned char* bt = st + a_bytes + (size_t)b * b_bytes;
+                    const CUtensorMap* mb = b == 0 ? &mapB0 : &mapB1;
+                    for (int p = 0; p < g.BN; p += g.piece)
+                        tma_load_2d(bt + (size_t)p * BK * 2, mb, &full[s], kx, n0 + p);
+                }
+                issued = it + 1;
+            }
+            // drain: every issued stage must have landed before the CTA may exit
+            for (int it = (issued > g.stages ? issued - g.stages : 0); it < issued; ++it)
+                mbar_wait(&full[it % g.stages], (it / g.stages) & 1);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0 && nk > 0) {
+            bool ok = true;
+            for (int it = 0; it < nk; ++it) {
+                const int s = it % g.stages;
+                if (!mbar_wait(&full[s], (it / g.stages) & 1) || *(volatile int*)abort_flag) {
+                    atomicExch(g.err, 2);
+                    *(volatile int*)abort_flag = 1;
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                unsigned char* st = smem + (size_t)s * stage_bytes;
+                const uint32_t abase = smem_u32(st);
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint64_t ad = sw128_desc(abase + kk * 32);
+                    for (int b = 0; b < g.nb; ++b) {
+                        const uint32_t bbase = smem_u32(st + a_bytes + (size_t)b * b_bytes);
+                        for (int p = 0; p < g.BN; p += g.piece) {
+                            const int n = min(g.piece, g.BN - p);
+                            const uint64_t bd = sw128_desc(bbase + (uint32_t)p * BK * 2 + kk * 32);
+                            mma_bf16(tmem + (uint32_t)p, ad, bd, idesc_bf16(n), (it | kk | b) != 0);
+                        }
+                    }
+                }
+                mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+            }
+            if (ok) mma_commit(accum);
+            else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(accum)) : "memory");
+        }
+        if (lane == 0 && nk <= 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(accum)) : "memory");
+    } else {
+        // ---------------- epilogue ----------------
+        const int q = warp & 3;  // TMEM lane quarter this warp may read
+        const bool got = mbar_wait(accum, 0);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const bool valid = got && !*(volatile int*)abort_flag && nk > 0;
+        if (!got) atomicExch(g.err, 3);
+        const int row = m0 + q * 32 + lane;
+        for (int c0 = 0; c0 < g.BN; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+            if (!valid) continue;
+            if (g.mode == 0) {
+                if (row < g.M) {
+                    float* o = g.out_f + ((int64_t)blockIdx.z * g.M + row) * g.ldo + n0 + c0;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (n0 + c0 + j < g.N) o[j] = v[j];
+                }
+            } else {
+                if (row < g.M)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (n0 + c0 + j < g.N) g.out_i[(int64_t)(n0 + c0 + j) * g.ldo + row] = __float2int_rn(v[j]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+    }
+}
+
+inline size_t gemm_smem_bytes(int BN, int nb, int stages) {
+    size_t st = (size_t)BM * BK * 2 + (size_t)BN * BK * 2 * nb;
+    return st * stages + 1024 /*align slack*/ + 256 /*barriers*/;
+}
+
+}  // namespace tc
+}  // namespace vp

@@ -8,6 +8,7 @@ names and defaults are those of the -structure_* flags.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 
 import numpy as np
 
@@ -114,7 +115,7 @@ class Dataset:
         return o
 
     def __del__(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not sys.is_finalizing():
             B.lib().vp_dataset_free(self.h)
             self.h = None
 
@@ -140,7 +141,10 @@ class Context:
             self.h = None
 
     def __del__(self):
-        self.close()
+        # at interpreter exit the CUDA runtime may already be gone; the process
+        # teardown releases the device memory
+        if not sys.is_finalizing():
+            self.close()
 
 
 _DT = {1: np.float32, 2: np.float32, 3: np.uint16, 4: np.int32, 5: np.int32, 6: np.float64, 7: np.float64,
@@ -202,7 +206,8 @@ class Chain:
             self.h = None
 
     def __del__(self):
-        self.close()
+        if not sys.is_finalizing():
+            self.close()
 
 
 def finish(chains: list[Chain]) -> None:
