@@ -166,6 +166,17 @@ int vp_chain_step(vp_chain* c, int32_t step);
 int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes);
 int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t bytes);
 
+/* Error code recorded by the tensor-core kernels of this context (0 = none;
+ * non-zero means a pipeline wait timed out and that launch's output is void). */
+int vp_tc_status(vp_ctx* ctx);
+
+/* Diagnostic: D[s][m][n] = sum over this split's k of A[m,k] (B0[n,k] + B1[n,k])
+ * through the tensor-core kernel. A [M][K], B0/B1 [N][K] bf16 bit patterns,
+ * K % 64 == 0, N % BN == 0, BN % piece == 0, piece % 16 == 0, piece <= 256,
+ * BN <= 512; B1 may be NULL. D receives splits*M*N floats. */
+int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N, int32_t K,
+                       int32_t BN, int32_t piece, int32_t splits, int32_t stages, float* D);
+
 /* Kernel launches issued by this library since the context was opened. */
 int64_t vp_launch_count(vp_ctx* ctx);
 

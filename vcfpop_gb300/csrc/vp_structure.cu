@@ -7,8 +7,19 @@
 
 #include "vp_internal.h"
 #include "vp_kernels.cuh"
+#include "vp_tc.cuh"
 
 using namespace vp;
+
+struct TcOperands {
+    bool ready = false;
+    int64_t Apad = 0, Npad = 0;
+    __nv_bfloat16 *C = nullptr, *CT = nullptr;
+    float* logpbar = nullptr;
+    double* Bc = nullptr;
+    int* err = nullptr;
+    CUtensorMap mapC, mapCT;
+};
 
 struct vp_ctx {
     int device = 0;
@@ -19,6 +30,8 @@ struct vp_ctx {
     int32_t N = 0, S = 0, maxK = 0, maxploidy = 0, packed2 = 0;
     int64_t L = 0, KT = 0;
     int nsm = 132;
+    TcOperands tc;
+    struct TcBatch* batch = nullptr;
 };
 
 struct vp_chain {
@@ -34,9 +47,28 @@ struct vp_chain {
     double* ancestry = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graph_nodes = 0;
+    int32_t* own_ni = nullptr;   // the chain's own Ni (a tensor-core batch may redirect Ni)
+};
+
+// a set of no-admixture chains sharing one context, swept together with the
+// tensor-core contraction
+struct TcBatch {
+    std::vector<vp_chain*> chains;
+    void* mem = nullptr;
+    DevChain* dchains = nullptr;
+    int32_t *rowchain = nullptr, *rowk = nullptr, *row0 = nullptr;
+    int R = 0, Rpad = 0, G = 0, BN = 288, piece = 144, splits = 1;
+    __nv_bfloat16 *Whi = nullptr, *Wlo = nullptr, *OH = nullptr;
+    float* LLpart = nullptr;
+    int32_t* NiAll = nullptr;
+    CUtensorMap mapWhi, mapWlo, mapOH;
+    cudaGraphExec_t graph = nullptr;
+    int graph_nodes = 0;
 };
 
 namespace {
+void free_batch(vp_ctx* x);
+int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps);
 
 #define CK(call)                                                                  \
     do {                                                                          \
@@ -271,6 +303,7 @@ extern "C" int vp_close(vp_ctx* x) {
     if (!x) return VP_OK;
     cudaSetDevice(x->device);
     if (x->stream) cudaStreamSynchronize(x->stream);
+    if (x->batch) { cudaGraphExecDestroy(x->batch->graph); cudaFree(x->batch->mem); delete x->batch; x->batch = nullptr; }
     for (void* p : x->allocs) cudaFree(p);
     if (x->stream) cudaStreamDestroy(x->stream);
     delete x;
@@ -384,6 +417,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
     }
     Carve cv{(char*)c->mem};
     layout(cv);
+    c->own_ni = h.Ni;
     CK(cudaMemsetAsync(c->mem, 0, probe.off, x->stream));
     CK(cudaMemcpyAsync(c->d, &h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
     c->total = h.nburnin + h.nreps;
@@ -413,6 +447,9 @@ extern "C" int vp_chain_destroy(vp_chain* c) {
     if (!c) return VP_OK;
     cudaSetDevice(c->ctx->device);
     cudaStreamSynchronize(c->ctx->stream);
+    if (c->ctx->batch)
+        for (vp_chain* o : c->ctx->batch->chains)
+            if (o == c) { free_batch(c->ctx); break; }
     if (c->graph) cudaGraphExecDestroy(c->graph);
     cudaFree(c->mem);
     delete c;
@@ -445,6 +482,17 @@ extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
     for (int i = 0; i < n; ++i)
         if (!cs[i] || cs[i]->ctx != x) { vp_set_error("all chains of one vp_run must share a context"); return VP_E_ARG; }
     cudaSetDevice(x->device);
+    bool all_tc = true;
+    for (int i = 0; i < n; ++i) all_tc &= cs[i]->P.form == VP_FORM_TC;
+    if (all_tc) {
+        int step = nsweeps;
+        for (int i = 0; i < n; ++i) step = std::min(step, cs[i]->total - cs[i]->issued);
+        if (step <= 0) return VP_OK;
+        int rc = run_tc(x, cs, n, step);
+        if (rc) return rc;
+        for (int i = 0; i < n; ++i) cs[i]->issued += step;
+        return VP_OK;
+    }
     // chains with sweeps left; equal remaining counts share one graph
     int left = nsweeps;
     while (left > 0) {
@@ -616,4 +664,315 @@ extern "C" int vp_chain_step(vp_chain* c, int32_t step) {
     int rc = launch_step(c, step, 0);
     if (rc) return rc;
     return vp_sync(c->ctx);
+}
+
+// ===================== tensor-core K-sweep =====================
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// 2-D bf16 row-major [rows][ld] map with 64 x box_rows boxes, 128-byte swizzle
+int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows) {
+    EncodeTiledFn f = encode_fn();
+    if (!f) { vp_set_error("cuTensorMapEncodeTiled unavailable"); return VP_E_CUDA; }
+    cuuint64_t dims[2] = {cols, rows};
+    cuuint64_t strides[1] = {ld * 2};
+    cuuint32_t box[2] = {64, box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { vp_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return VP_E_CUDA; }
+    return VP_OK;
+}
+
+int launch_gemm(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CUtensorMap& B1, tc::GemmArgs g,
+                dim3 grid) {
+    size_t sm = tc::gemm_smem_bytes(g.BN, g.nb, g.stages);
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(tc::k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        attr = true;
+    }
+    if (sm > 227 * 1024) { vp_set_error("gemm tile needs %zu bytes of shared memory", sm); return VP_E_ARG; }
+    tc::k_gemm_bf16<<<grid, tc::NTHREADS, sm, x->stream>>>(A, B0, B1, g);
+    return check_launch(x, "k_gemm_bf16");
+}
+
+int tc_operands(vp_ctx* x) {
+    TcOperands& t = x->tc;
+    if (t.ready) return VP_OK;
+    if (!x->packed2) { vp_set_error("the tensor-core form needs biallelic diploid (packed) data"); return VP_E_ARG; }
+    const int64_t A = 2 * x->L;
+    t.Apad = (A + 63) / 64 * 64;
+    t.Npad = (x->N + 127) / 128 * 128;
+    size_t bytes = (size_t)t.Npad * t.Apad * 2 * 2 + t.Apad * 4 + t.Npad * 8 + 256;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) { vp_set_error("cudaMalloc(%zu) for tensor-core operands: %s", bytes, cudaGetErrorString(e)); return VP_E_MEM; }
+    x->allocs.push_back(p);
+    CK(cudaMemsetAsync(p, 0, bytes, x->stream));
+    char* q = (char*)p;
+    t.C = (__nv_bfloat16*)q; q += (size_t)t.Npad * t.Apad * 2;
+    t.CT = (__nv_bfloat16*)q; q += (size_t)t.Npad * t.Apad * 2;
+    t.logpbar = (float*)q; q += t.Apad * 4;
+    t.Bc = (double*)q; q += t.Npad * 8;
+    t.err = (int*)q;
+    tc::k_build_counts<<<dim3(cdiv(t.Npad, 256), (unsigned)x->L, 1), 256, 0, x->stream>>>(x->D, t.C, t.CT, t.Apad, t.Npad);
+    int rc = check_launch(x, "k_build_counts");
+    if (rc) return rc;
+    tc::k_allele_center<<<cdiv(x->L, 256), 256, 0, x->stream>>>(x->D, t.logpbar);
+    if ((rc = check_launch(x, "k_allele_center"))) return rc;
+    tc::k_center_const<<<cdiv((int64_t)x->N * 32, 256), 256, 0, x->stream>>>(x->D, t.logpbar, t.Bc);
+    if ((rc = check_launch(x, "k_center_const"))) return rc;
+    if ((rc = make_map(&t.mapC, t.C, t.Npad, t.Apad, t.Apad, 128))) return rc;
+    if ((rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128))) return rc;
+    t.ready = true;
+    return VP_OK;
+}
+
+int tc_splits(int64_t tiles, int nsm) {
+    // split the allele dimension so that the CTA count fills whole waves
+    int best = 1;
+    double beste = 0;
+    for (int s = 1; s <= 24; ++s) {
+        double ctas = (double)tiles * s, waves = ctas / nsm;
+        double eff = waves / std::ceil(waves);
+        if (eff > beste + 0.02) { beste = eff; best = s; }
+        if (eff > 0.93) break;
+    }
+    return best;
+}
+
+void free_batch(vp_ctx* x) {
+    if (!x->batch) return;
+    TcBatch* b = x->batch;
+    cudaStreamSynchronize(x->stream);
+    for (vp_chain* c : b->chains) {
+        // hand each chain its counts back
+        cudaMemcpy(c->own_ni, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice);
+        c->h.Ni = c->own_ni;
+        cudaMemcpy(c->d, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice);
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    }
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    cudaFree(b->mem);
+    delete b;
+    x->batch = nullptr;
+}
+
+int make_batch(vp_ctx* x, vp_chain** cs, int n) {
+    if (x->batch) {
+        TcBatch* b = x->batch;
+        if ((int)b->chains.size() == n && std::equal(b->chains.begin(), b->chains.end(), cs)) return VP_OK;
+        free_batch(x);
+    }
+    int rc = tc_operands(x);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i) {
+        const vp_params& P = cs[i]->P;
+        if (P.admix || P.locpriori || P.fmodel || cs[i]->h.nadmburnin > 0 || P.rng != VP_RNG_COUNTER) {
+            vp_set_error("the tensor-core form runs no-admixture chains without location prior, F model or "
+                         "admixture burn-in, with counter streams");
+            return VP_E_ARG;
+        }
+    }
+    auto* b = new TcBatch();
+    b->chains.assign(cs, cs + n);
+    std::vector<int32_t> rowchain, rowk, row0;
+    for (int i = 0; i < n; ++i) {
+        row0.push_back((int32_t)rowchain.size());
+        for (int k = 0; k < cs[i]->P.K; ++k) { rowchain.push_back(i); rowk.push_back(k); }
+    }
+    b->R = (int)rowchain.size();
+    b->G = (b->R + b->BN - 1) / b->BN;
+    b->Rpad = b->G * b->BN;
+    const TcOperands& t = x->tc;
+    const int64_t tiles = (t.Npad / 128) * b->G;
+    b->splits = tc_splits(tiles, x->nsm);
+    const int64_t kblocks = t.Apad / 64;
+    b->splits = (int)std::min<int64_t>(b->splits, kblocks);
+    Carve probe{nullptr};
+    auto lay = [&](Carve& cv) {
+        b->dchains = cv.take<DevChain>(n);
+        b->rowchain = cv.take<int32_t>(b->R);
+        b->rowk = cv.take<int32_t>(b->R);
+        b->row0 = cv.take<int32_t>(n);
+        b->Whi = cv.take<__nv_bfloat16>((int64_t)b->Rpad * t.Apad);
+        b->Wlo = cv.take<__nv_bfloat16>((int64_t)b->Rpad * t.Apad);
+        b->OH = cv.take<__nv_bfloat16>((int64_t)b->Rpad * t.Npad);
+        b->LLpart = cv.take<float>((int64_t)b->splits * x->N * b->Rpad);
+        b->NiAll = cv.take<int32_t>((int64_t)b->Rpad * x->KT);
+    };
+    lay(probe);
+    cudaError_t e = cudaMalloc(&b->mem, probe.off);
+    if (e != cudaSuccess) { delete b; vp_set_error("cudaMalloc(%zu) for the batch: %s", probe.off, cudaGetErrorString(e)); return VP_E_MEM; }
+    Carve cv{(char*)b->mem};
+    lay(cv);
+    CK(cudaMemsetAsync(b->mem, 0, probe.off, x->stream));
+    CK(cudaMemcpyAsync(b->rowchain, rowchain.data(), rowchain.size() * 4, cudaMemcpyHostToDevice, x->stream));
+    CK(cudaMemcpyAsync(b->rowk, rowk.data(), rowk.size() * 4, cudaMemcpyHostToDevice, x->stream));
+    CK(cudaMemcpyAsync(b->row0, row0.data(), row0.size() * 4, cudaMemcpyHostToDevice, x->stream));
+    // the batch's count contraction writes every chain's Ni inside NiAll
+    for (int i = 0; i < n; ++i) {
+        vp_chain* c = cs[i];
+        int32_t* dst = b->NiAll + (int64_t)row0[i] * x->KT;
+        CK(cudaMemcpyAsync(dst, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice, x->stream));
+        c->h.Ni = dst;
+        CK(cudaMemcpyAsync(c->d, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
+        CK(cudaMemcpyAsync(b->dchains + i, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    }
+    if ((rc = make_map(&b->mapWhi, b->Whi, b->Rpad, t.Apad, t.Apad, b->piece))) { x->batch = b; free_batch(x); return rc; }
+    if ((rc = make_map(&b->mapWlo, b->Wlo, b->Rpad, t.Apad, t.Apad, b->piece))) { x->batch = b; free_batch(x); return rc; }
+    if ((rc = make_map(&b->mapOH, b->OH, b->Rpad, t.Npad, t.Npad, b->piece))) { x->batch = b; free_batch(x); return rc; }
+    x->batch = b;
+    return VP_OK;
+}
+
+tc::BatchDev batch_dev(vp_ctx* x) {
+    TcBatch* b = x->batch;
+    tc::BatchDev d;
+    d.chains = b->dchains; d.rowchain = b->rowchain; d.rowk = b->rowk; d.row0 = b->row0;
+    d.R = b->R; d.Rpad = b->Rpad; d.nchains = (int)b->chains.size(); d.splits = b->splits;
+    d.Apad = x->tc.Apad; d.Npad = x->tc.Npad; d.Whi = b->Whi; d.Wlo = b->Wlo; d.OH = b->OH;
+    d.logpbar = x->tc.logpbar; d.Bc = x->tc.Bc; d.LLpart = b->LLpart;
+    return d;
+}
+
+int launch_tc_sweep(vp_ctx* x) {
+    TcBatch* b = x->batch;
+    const TcOperands& t = x->tc;
+    const int n = (int)b->chains.size();
+    tc::BatchDev bd = batch_dev(x);
+    cudaStream_t s = x->stream;
+    // UpdateP for all chains, with the split-bf16 centred log-frequency rows
+    LAUNCH(x, tc::k_update_p_tc, (dim3(cdiv(x->L, 256), b->R, 1), 256, 0, s), (bd));
+    // likelihood contraction: LL'[i, row] = sum_a C[i,a] (Whi + Wlo)[row, a]
+    {
+        tc::GemmArgs g{};
+        g.M = x->N; g.N = b->Rpad; g.kblocks = (int)(t.Apad / 64);
+        g.kb_per_split = (g.kblocks + b->splits - 1) / b->splits;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.stages = 2; g.mode = 0;
+        g.out_f = b->LLpart; g.ldo = b->Rpad; g.err = t.err;
+        int rc = launch_gemm(x, t.mapC, b->mapWhi, b->mapWlo, g, dim3((unsigned)(t.Npad / 128), b->G, b->splits));
+        if (rc) return rc;
+    }
+    // labels of every chain, one-hot rows for the count contraction
+    LAUNCH(x, tc::k_sample_tc, (dim3(cdiv(x->N, SAMPLE_BLOCK), n, 1), SAMPLE_BLOCK, 0, s), (bd));
+    // count contraction: Ni[row, a] = sum_i OH[row, i] C[i, a]
+    {
+        tc::GemmArgs g{};
+        g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / 64); g.kb_per_split = g.kblocks;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.stages = 4; g.mode = 1;
+        g.out_i = b->NiAll; g.ldo = x->KT; g.err = t.err;
+        int rc = launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, dim3((unsigned)(t.Apad / 128), b->G, 1));
+        if (rc) return rc;
+    }
+    // Record for every chain, then m += 1
+    unsigned ga = std::min<unsigned>(1024, cdiv((int64_t)16 * x->KT, 256));
+    LAUNCH(x, k_record, (dim3(1, 1, n), 256, 0, s), (b->dchains));
+    LAUNCH(x, k_accumulate, (dim3(ga, 1, n), 256, 0, s), (b->dchains, 0));
+    LAUNCH(x, k_advance, (dim3(1, 1, n), 32, 0, s), (b->dchains));
+    return VP_OK;
+}
+
+int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps) {
+    int rc = make_batch(x, cs, n);
+    if (rc) return rc;
+    TcBatch* b = x->batch;
+    if (!b->graph) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal));
+        int64_t before = x->launches;
+        rc = launch_tc_sweep(x);
+        cudaError_t e = cudaStreamEndCapture(x->stream, &g);
+        if (rc) { if (e == cudaSuccess) cudaGraphDestroy(g); return rc; }
+        if (e != cudaSuccess) { vp_set_error("graph capture failed: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+        b->graph_nodes = (int)(x->launches - before);
+        x->launches = before;
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { vp_set_error("graph instantiate failed: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+    }
+    for (int i = 0; i < nsweeps; ++i) {
+        CK(cudaGraphLaunch(b->graph, x->stream));
+        x->launches += b->graph_nodes;
+    }
+    return VP_OK;
+}
+
+}  // namespace
+
+extern "C" int vp_tc_status(vp_ctx* x) {
+    if (!x) { vp_set_error("null context"); return VP_E_ARG; }
+    if (!x->tc.ready) return 0;
+    int e = 0;
+    CK(cudaMemcpy(&e, x->tc.err, sizeof(int), cudaMemcpyDeviceToHost));
+    return e;
+}
+
+extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N,
+                                  int32_t K, int32_t BN, int32_t piece, int32_t splits, int32_t stages, float* D) {
+    if (!A || !B0 || !D || M <= 0 || N <= 0 || K <= 0 || K % 64 || N % BN || BN % piece || piece % 16 || piece > 256 ||
+        BN > 512 || splits < 1) {
+        vp_set_error("vp_debug_gemm_bf16: bad shape");
+        return VP_E_ARG;
+    }
+    vp_ctx tmp;
+    cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking);
+    const int64_t Mp = (M + 127) / 128 * 128;
+    void *dA, *dB0, *dB1 = nullptr, *dD;
+    int* err;
+    CK(cudaMalloc(&dA, (size_t)Mp * K * 2));
+    CK(cudaMemset(dA, 0, (size_t)Mp * K * 2));
+    CK(cudaMalloc(&dB0, (size_t)N * K * 2));
+    CK(cudaMalloc(&dD, (size_t)splits * M * N * 4));
+    CK(cudaMalloc(&err, 4));
+    CK(cudaMemset(err, 0, 4));
+    CK(cudaMemcpy(dA, A, (size_t)M * K * 2, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dB0, B0, (size_t)N * K * 2, cudaMemcpyHostToDevice));
+    if (B1) {
+        CK(cudaMalloc(&dB1, (size_t)N * K * 2));
+        CK(cudaMemcpy(dB1, B1, (size_t)N * K * 2, cudaMemcpyHostToDevice));
+    }
+    CUtensorMap ma, mb0, mb1;
+    int rc = make_map(&ma, dA, Mp, K, K, 128);
+    if (!rc) rc = make_map(&mb0, dB0, N, K, K, piece);
+    if (!rc) rc = make_map(&mb1, B1 ? dB1 : dB0, N, K, K, piece);
+    if (!rc) {
+        tc::GemmArgs g{};
+        g.M = M; g.N = N; g.kblocks = K / 64; g.kb_per_split = (g.kblocks + splits - 1) / splits;
+        g.BN = BN; g.piece = piece; g.nb = B1 ? 2 : 1; g.stages = stages; g.mode = 0;
+        g.out_f = (float*)dD; g.ldo = N; g.err = err;
+        rc = launch_gemm(&tmp, ma, mb0, mb1, g, dim3((unsigned)(Mp / 128), N / BN, splits));
+    }
+    int e = 0;
+    if (!rc) {
+        cudaError_t ce = cudaStreamSynchronize(tmp.stream);
+        if (ce != cudaSuccess) { vp_set_error("gemm: %s", cudaGetErrorString(ce)); rc = VP_E_CUDA; }
+        else {
+            cudaMemcpy(&e, err, 4, cudaMemcpyDeviceToHost);
+            cudaMemcpy(D, dD, (size_t)splits * M * N * 4, cudaMemcpyDeviceToHost);
+            if (e) { vp_set_error("gemm pipeline timed out (code %d)", e); rc = VP_E_CUDA; }
+        }
+    }
+    cudaFree(dA); cudaFree(dB0); if (dB1) cudaFree(dB1); cudaFree(dD); cudaFree(err);
+    cudaStreamDestroy(tmp.stream);
+    tmp.stream = nullptr;
+    return rc;
 }

@@ -25,7 +25,7 @@ namespace tc {
 constexpr int BM = 128;
 constexpr int BK = 64;                 // bf16 elements per 128-byte swizzle row
 constexpr int NTHREADS = 192;
-constexpr uint32_t SPIN_LIMIT = 1u << 26;
+constexpr uint32_t SPIN_LIMIT = 1u << 22;
 
 struct GemmArgs {
     int M, N;               // rows of A / D, columns of D (= rows of B)
@@ -211,8 +211,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
             }
-            if (ok) mma_commit(accum);
-            else asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(accum)) : "memory");
+            // also on the error path: the commit arrives only once every MMA this
+            // thread issued has finished writing TMEM
+            mma_commit(accum);
+            (void)ok;
         }
         if (lane == 0 && nk <= 0)
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(accum)) : "memory");
@@ -254,6 +256,159 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 inline size_t gemm_smem_bytes(int BN, int nb, int stages) {
     size_t st = (size_t)BM * BK * 2 + (size_t)BN * BK * 2 * nb;
     return st * stages + 1024 /*align slack*/ + 256 /*barriers*/;
+}
+
+}  // namespace tc
+}  // namespace vp
+
+#include <cuda_bf16.h>
+#include "vp_kernels.cuh"
+
+namespace vp {
+namespace tc {
+
+// ---- genotype-count operands of the batched K-sweep (biallelic diploid) ----
+// C  [Npad][Apad]: C[i][2l+a]  copies of allele a at locus l in individual i
+// CT [Apad][Npad]: the transpose (alleles x individuals)
+// Missing calls and the padding are zero.
+__global__ void k_build_counts(const DevData D, __nv_bfloat16* C, __nv_bfloat16* CT, int64_t Apad, int64_t Npad) {
+    const int64_t l = blockIdx.y;                   // one locus per grid row
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Npad) return;
+    float c0 = 0.f, c1 = 0.f;
+    if (i < D.N && l < D.L) {
+        int code = (D.g2[l * D.Nw + (i >> 4)] >> ((i & 15) * 2)) & 3;
+        if (code != 3) { c1 = (float)code; c0 = 2.f - code; }
+    }
+    const __nv_bfloat16 b0 = __float2bfloat16(c0), b1 = __float2bfloat16(c1);
+    C[(int64_t)i * Apad + 2 * l] = b0;
+    C[(int64_t)i * Apad + 2 * l + 1] = b1;
+    CT[(2 * l) * Npad + i] = b0;
+    CT[(2 * l + 1) * Npad + i] = b1;
+}
+
+// per-allele centring constant: ln of the dataset allele frequency (with a
+// pseudo-count), and B[i] = sum_a C[i][a] * ln pbar_a, computed once
+__global__ void k_allele_center(const DevData D, float* logpbar) {
+    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (l >= D.L) return;
+    int64_t n1 = 0, t = 0;
+    for (int i = 0; i < D.N; ++i) {
+        int code = (D.g2[l * D.Nw + (i >> 4)] >> ((i & 15) * 2)) & 3;
+        if (code != 3) { t += 2; n1 += code; }
+    }
+    logpbar[2 * l] = logf((float)(t - n1 + 1) / (float)(t + 2));
+    logpbar[2 * l + 1] = logf((float)(n1 + 1) / (float)(t + 2));
+}
+__global__ void k_center_const(const DevData D, const float* logpbar, double* Bc) {
+    // one warp per individual, Kahan sums per lane, FP64 across lanes
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= D.N) return;
+    const int i = warp;
+    float s = 0.f, cmp = 0.f;
+    for (int64_t l = lane; l < D.L; l += 32) {
+        int code = (D.g2[l * D.Nw + (i >> 4)] >> ((i & 15) * 2)) & 3;
+        if (code == 3) continue;
+        float v = (2.f - code) * logpbar[2 * l] + (float)code * logpbar[2 * l + 1];
+        float y = v - cmp, t = s + y;
+        cmp = (t - s) - y;
+        s = t;
+    }
+    double d = (double)s - (double)cmp;
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) Bc[i] = d;
+}
+
+struct BatchDev {
+    const DevChain* chains;   // [nchains]
+    const int32_t* rowchain;  // [R] chain of each cluster row
+    const int32_t* rowk;      // [R] cluster index within its chain
+    const int32_t* row0;      // [nchains] first row of each chain
+    int R, Rpad, nchains, splits;
+    int64_t Apad, Npad;
+    __nv_bfloat16 *Whi, *Wlo, *OH;
+    const float* logpbar;
+    const double* Bc;
+    const float* LLpart;      // [splits][N][Rpad]
+};
+
+// UpdateP for every chain of the batch (counter streams, the same Philox
+// counters as the per-chain kernel): p ~ Dirichlet(lambda + Ni), written to
+// Freq and, centred and split into bf16 hi + lo, to the rows of W
+__global__ void k_update_p_tc(BatchDev b) {
+    const int r = blockIdx.y;
+    const DevChain& c = b.chains[b.rowchain[r]];
+    const DevData& D = c.D;
+    const int k = b.rowk[r], m = c.ctl->m;
+    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (l >= D.L) return;
+    const int64_t kl = (int64_t)k * D.L + l;
+    const int64_t j = k * D.KT + D.off[l];
+    Philox ph;
+    ph.init(c.seed, ST_P | ((uint32_t)m << 4), (uint32_t)kl, (uint32_t)(kl >> 32));
+    float p[2], s = 0.f;
+    for (int a = 0; a < 2; ++a) {
+        float v = ph.gammaf((float)c.Lambda[k] + (float)c.Ni[j + a]);
+        p[a] = v;
+        s += v;
+    }
+    const float inv = 1.f / s;
+    for (int a = 0; a < 2; ++a) {
+        p[a] *= inv;
+        c.Freq[j + a] = p[a];
+        const float w = ln_freq(p[a]) - b.logpbar[2 * l + a];
+        const __nv_bfloat16 hi = __float2bfloat16(w);
+        const __nv_bfloat16 lo = __float2bfloat16(w - __bfloat162float(hi));
+        b.Whi[(int64_t)r * b.Apad + 2 * l + a] = hi;
+        b.Wlo[(int64_t)r * b.Apad + 2 * l + a] = lo;
+    }
+}
+
+// label draw for every (chain, individual) from the tensor-core likelihoods;
+// also writes the one-hot label rows OH that the count contraction reads
+__global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_tc(BatchDev b) {
+    const int ci = blockIdx.y;
+    const DevChain& c = b.chains[ci];
+    const DevData& D = c.D;
+    const int K = c.K, N = D.N, m = c.ctl->m;
+    const int r0 = b.row0[ci];
+    __shared__ double sh[32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double lnl = 0;
+    if (i < N) {
+        double ll[64];
+        for (int k = 0; k < K; ++k) {
+            double v = b.Bc[i];
+            for (int s = 0; s < b.splits; ++s) v += (double)b.LLpart[((int64_t)s * N + i) * b.Rpad + r0 + k];
+            ll[k] = v;
+            c.LL[(int64_t)i * K + k] = v;
+            c.Q[(int64_t)i * K + k] = 0.f;
+            c.Mi[(int64_t)i * K + k] = 0;
+        }
+        int z = -1;
+        if (D.vt[i]) {
+            double keep[64];
+            for (int k = 0; k < K; ++k) keep[k] = ll[k];
+            Philox ph;
+            ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0);
+            z = polylog(ll, K, ph.uniformd(), false, nullptr);
+            c.Q[(int64_t)i * K + z] = 1.f;
+            c.Z[i] = (uint16_t)z;
+            c.Mi[(int64_t)i * K + z] = (int32_t)D.vt[i];
+            lnl = keep[z];
+        }
+        for (int k = 0; k < K; ++k)
+            b.OH[(int64_t)(r0 + k) * b.Npad + i] = __float2bfloat16(k == z ? 1.f : 0.f);
+    }
+    double t = block_sum(lnl, sh);
+    if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
+    if (!last_block_done(c.ctl, gridDim.x)) return;
+    if (threadIdx.x == 0) {
+        double tot = 0;
+        for (int bb = 0; bb < (int)gridDim.x; ++bb) tot += c.lnlp[bb];
+        c.ctl->lnl = tot;
+        c.ctl->done = 0;
+    }
 }
 
 }  // namespace tc
