@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Benchmark of the STRUCTURE K-sweep on GB300: genotype-cluster updates/s.
+
+Workload (the batched K-sweep the metric is quoted on): N = 10,000 diploid
+individuals x L = 200,000 biallelic SNPs drawn from an 8-population F-model
+(F = 0.03, ancestral frequencies Beta(0.5, 0.5), 1% missing calls), seeded
+synthetic data; K = 1..10 x 10 replicates = 100 no-admixture chains sharing
+the genotype matrix. One step = one MCMC sweep of all 100 chains; one
+genotype-cluster update = one (individual, locus, cluster) term, so a step is
+N * L * sum(K) updates.
+
+  --form tc     the tensor-core split-BF16 form (default)
+  --form plain  the FP32 SIMT form of the same sweep
+  --impl reference  the CPU baseline: the reference algorithm's C port on the
+                host cores, one chain per thread, on a bounded locus sample
+
+Prints one JSON line (rank 0).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_IND, N_LOC, N_POP, FST, MISSING = 10_000, 200_000, 8, 0.03, 0.01
+KS = [k for k in range(1, 11) for _ in range(10)]
+METRIC = "genotype-cluster updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="tc", choices=["tc", "plain"])
+    ap.add_argument("--loci", type=int, default=N_LOC)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-sweeps", type=int, default=10)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- data
+def gen_packed_gpu(seed, N, L, P=N_POP, F=FST, miss=MISSING, chunk=20_000):
+    """F-model genotypes drawn on the GPU, returned as host 2-bit codes [L][ceil(N/16)]."""
+    import torch
+    torch.manual_seed(seed)
+    dev = "cuda"
+    g = torch.Generator(device=dev).manual_seed(seed)
+    anc = torch.distributions.Beta(torch.full((L,), 0.5, device=dev), torch.full((L,), 0.5, device=dev)).sample()
+    f = (1 - F) / F
+    a = (anc * f).clamp_min(1e-3).expand(P, L)
+    b = ((1 - anc) * f).clamp_min(1e-3).expand(P, L)
+    popf = torch.distributions.Beta(a, b).sample()  # [P, L]
+    pop = (torch.arange(N, device=dev) * P) // N
+    Nw = (N + 15) // 16
+    out = np.empty((L, Nw), dtype=np.uint32)
+    shifts = (torch.arange(16, device=dev, dtype=torch.int64) * 2)
+    for l0 in range(0, L, chunk):
+        l1 = min(L, l0 + chunk)
+        p = popf[:, l0:l1][pop]  # [N, Lc]
+        u = torch.rand((2, N, l1 - l0), device=dev, generator=g)
+        c1 = (u[0] < p).to(torch.int64) + (u[1] < p).to(torch.int64)
+        m = torch.rand((N, l1 - l0), device=dev, generator=g) < miss
+        code = torch.where(m, torch.full_like(c1, 3), c1).t().contiguous()  # [Lc, N]
+        pad = torch.full((l1 - l0, Nw * 16), 3, dtype=torch.int64, device=dev)
+        pad[:, :N] = code
+        words = (pad.view(l1 - l0, Nw, 16) << shifts).sum(dim=2).to(torch.int64) & 0xFFFFFFFF
+        out[l0:l1] = words.to(torch.int64).cpu().numpy().astype(np.uint32)
+    return out, pop.cpu().numpy().astype(np.int32)
+
+
+def gen_sample_cpu(seed, N, L):
+    from vcfpop_gb300 import synth
+    return synth.fmodel(seed, N, L, N_POP, FST, MISSING)
+
+
+# ---------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi clock and throttle-reason samples taken during the timed region."""
+
+    def __init__(self, index=0):
+        self.rows, self.proc, self.index = [], None, index
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------- CPU leg
+class CpuPort:
+    """The oracle -- the reference algorithm's C port -- on N x `loci` of the
+    same F-model, 100 chains, one chain at a time per host thread (the
+    reference's run-level parallelism)."""
+
+    def __init__(self, loci, chains_k, seed=7, threads=None):
+        from tests import orc
+        import ctypes as C
+        self.orc = orc
+        self.d = gen_sample_cpu(seed, N_IND, loci)
+        self.od = orc.Data(self.d)
+        self.L = self.od.field(1, np.int32).size
+        self.threads = threads or os.cpu_count()
+        self.chains = [orc.Chain(self.od, orc.params(K, 1000 + j, admix=0, nadmburnin=0, nburnin=1000, nreps=2000))
+                       for j, K in enumerate(chains_k)]
+        self.arr = (C.c_void_p * len(self.chains))(*[c.h for c in self.chains])
+        self.upd_sweep = N_IND * self.L * sum(chains_k)
+        orc.lib().orc_sweep_many(self.arr, len(self.chains), 0, self.threads, 1)   # init
+
+    def sweep(self, n=1):
+        t0 = time.perf_counter()
+        self.orc.lib().orc_sweep_many(self.arr, len(self.chains), n, self.threads, 0)
+        return time.perf_counter() - t0
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cp = CpuPort(500, KS)
+    cores, L = cp.threads, cp.L
+    for _ in range(args.warmup):
+        cp.sweep()
+    t = [cp.sweep() for _ in range(args.steps)]
+    rates = [cp.upd_sweep / x for x in t]
+    value = float(np.median(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(t)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32 (reference CPU)",
+            "data": "synthetic F-model, seeded",
+            "config": {"workload": f"K-sweep K=1..10 x 10 replicates, N={N_IND}, L sample={L} of {N_LOC} loci",
+                       "chains": len(KS), "host_threads": cores},
+            "cpu_baseline": {"value": value, "unit": "updates/s", "cores": cores, "kind": "port",
+                             "sample": f"N={N_IND} x {L} loci, 100 chains, one sweep per step"},
+            "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU leg
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    import ctypes as C
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    from vcfpop_gb300 import _lib as B
+    from vcfpop_gb300 import structure as S
+
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        peaks = {}
+    form = B.VP_FORM_TC if args.form == "tc" else B.VP_FORM_PLAIN
+
+    packed, pop = gen_packed_gpu(1234 + rank, N_IND, args.loci)
+    ds = S.Dataset(np.full(N_IND, 2, np.int32), np.full(args.loci, 2, np.int32), pop, N_POP, packed2=packed)
+    del packed
+    sumK = sum(KS)
+    upd_step = N_IND * ds.L * sumK
+
+    def make(ctx):
+        return [S.Chain(ctx, S.params(K, S.run_seed(1, j + 1), form=form, admix=0, nadmburnin=0,
+                                      nburnin=1000, nreps=2000)) for j, K in enumerate(KS)]
+
+    ctx = S.Context(ds, local)
+    chains = make(ctx)
+    lib = B.lib()
+    lib.vp_prof_enable(ctx.h, 1)
+    arr = (C.c_void_p * len(chains))(*[c.h for c in chains])
+    for _ in range(args.warmup):
+        B.check(lib.vp_run(arr, len(chains), 1))
+    ctx.sync()
+    stream = torch.cuda.ExternalStream(lib.vp_stream(ctx.h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.launches()
+    dom_ms, dom_n = 0.0, 0
+    ms, nl = C.c_double(), C.c_int32()
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            B.check(lib.vp_run(arr, len(chains), 1))
+            B.check(lib.vp_prof_read(ctx.h, C.byref(ms), C.byref(nl)))
+            dom_ms += ms.value
+            dom_n += nl.value
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = ctx.launches() - l0
+    total_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    tc_err = lib.vp_tc_status(ctx.h)
+    ms_step = total_ms / args.steps
+    value = upd_step * world / (ms_step / 1e3)
+
+    # dominant kernel roofline
+    dom_avg_ms = dom_ms / max(dom_n, 1)
+    if form == B.VP_FORM_TC:
+        A = 2 * ds.L
+        flops = 2.0 * N_IND * A * sumK  # algorithmic: the likelihood contraction [N x A] . [A x sumK]
+        achieved = flops / (dom_avg_ms / 1e3) / 1e12
+        peak = peaks.get("bf16_tflops_sustained", 1700.0)
+        roof = {"bound": "tensor", "kernel": "k_gemm_bf16 (likelihood contraction)", "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if "bf16_tflops_sustained" in peaks else "fallback",
+                "executed_tflops": 2 * flops * (((sumK + 287) // 288 * 288) / sumK) / (dom_avg_ms / 1e3) / 1e12,
+                "traffic": None}
+    else:
+        # per likelihood-stream launch (one chain): packed genotypes + frequencies + per-individual output
+        byts = [N_IND * ds.L / 4 + 4 * K * 2 * ds.L + 8 * N_IND * K for K in KS]
+        achieved = sum(byts) / len(byts) / (dom_avg_ms / 1e3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roof = {"bound": "hbm", "kernel": "k_loglik (likelihood stream)", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback", "traffic": None}
+    roof["avg_launch_ms"] = dom_avg_ms
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            tr = json.load(open(tfile)).get(args.form)
+            if tr:
+                roof["traffic"] = tr["bytes_per_launch_at_full_size"]
+        except Exception:
+            pass
+    for c in chains:
+        c.close()
+    ctx.close()
+
+    # ---- end to end through the C ABI: upload from pinned host memory, create
+    # the chains, sweep, read every chain's likelihood back, close
+    e2e_steps, e2e_ms = 3, []
+    h2d = ds.L * ((N_IND + 15) // 16) * 4 + ds.L * (4 + 8) + N_IND * (8 + 4)
+    d2h = 8 * len(KS)
+    for it in range(e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cx = S.Context(ds, local)
+        cs = make(cx)
+        a2 = (C.c_void_p * len(cs))(*[c.h for c in cs])
+        B.check(lib.vp_run(a2, len(cs), args.e2e_sweeps))
+        lnl = [c.get("LNL")[0] for c in cs]
+        for c in cs:
+            c.close()
+        cx.close()
+        dt = time.perf_counter() - t0
+        if it:
+            e2e_ms.append(dt * 1e3)
+        assert all(np.isfinite(lnl))
+    e2e_value = upd_step * args.e2e_sweeps * world / (np.median(e2e_ms) / 1e3)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cp = CpuPort(1000, KS)
+        cp.sweep()
+        dt = cp.sweep()
+        cpu = {"value": cp.upd_sweep / dt, "unit": "updates/s", "cores": cp.threads, "kind": "port",
+               "sample": f"N={N_IND} x {cp.L} loci sample, 100 chains (K=1..10 x 10), one timed sweep "
+                         f"after one warm-up sweep, {dt:.1f} s"}
+
+    line = {"metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 hi+lo x bf16 counts -> f32 (lnP(D) in f64)" if form else "f32",
+            "data": "synthetic F-model (8 pops, F=0.03, Beta(0.5,0.5) ancestry, 1% missing), seeded",
+            "config": {"workload": f"batched K-sweep: N={N_IND}, L={ds.L} biallelic SNPs, K=1..10 x 10 replicates "
+                                   f"= 100 no-admixture chains, one sweep of all chains per step",
+                       "form": args.form, "chains": len(KS), "sum_K": sumK, "updates_per_step": upd_step,
+                       "l2": "inputs larger than L2 (packed genotypes 0.5 GB; bf16 counts 2 x 8 GB)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "step": f"open context from pinned host buffers + create 100 chains + {args.e2e_sweeps} sweeps "
+                            f"+ read every chain's lnL + close", "ms_per_step": float(np.median(e2e_ms))},
+            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -177,6 +177,15 @@ int vp_tc_status(vp_ctx* ctx);
 int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N, int32_t K,
                        int32_t BN, int32_t piece, int32_t splits, int32_t stages, float* D);
 
+/* The CUDA stream (cudaStream_t) every launch of this context goes to. */
+void* vp_stream(vp_ctx* ctx);
+/* Record CUDA events around each launch of the sweep's dominant kernel (the
+ * likelihood stream of the plain form, the likelihood contraction of the
+ * tensor-core form), also inside the cached sweep graphs. */
+int vp_prof_enable(vp_ctx* ctx, int on);
+/* Synchronise, then sum the dominant-kernel durations of the last sweep. */
+int vp_prof_read(vp_ctx* ctx, double* ms, int32_t* launches);
+
 /* Kernel launches issued by this library since the context was opened. */
 int64_t vp_launch_count(vp_ctx* ctx);
 

@@ -11,6 +11,7 @@
 #include "orc_core.h"
 #include <stdlib.h>
 #include <stdio.h>
+#include <pthread.h>
 
 #define NEW(T, n) ((T*)calloc((size_t)((n) > 0 ? (n) : 1), sizeof(T)))
 
@@ -1080,4 +1081,30 @@ const void* orc_data_field(const orc_data* d, int f, int64_t* n) {
     }
     *n = 0;
     return 0;
+}
+
+/* ================= multi-chain runner (baseline timing) ================= */
+typedef struct { orc_chain** cs; int n, nsweeps, init; int next; pthread_mutex_t mu; } orc_pool;
+static void* orc_worker(void* arg) {
+    orc_pool* p = (orc_pool*)arg;
+    for (;;) {
+        pthread_mutex_lock(&p->mu);
+        int j = p->next++;
+        pthread_mutex_unlock(&p->mu);
+        if (j >= p->n) break;
+        if (p->init) orc_init(p->cs[j]);
+        for (int s = 0; s < p->nsweeps; ++s) orc_sweep(p->cs[j]);
+    }
+    return NULL;
+}
+void orc_sweep_many(orc_chain** cs, int n, int nsweeps, int nthreads, int init) {
+    orc_pool p;
+    p.cs = cs; p.n = n; p.nsweeps = nsweeps; p.init = init; p.next = 0;
+    pthread_mutex_init(&p.mu, NULL);
+    if (nthreads < 1) nthreads = 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+    for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, orc_worker, &p);
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    free(th);
+    pthread_mutex_destroy(&p.mu);
 }

@@ -126,6 +126,11 @@ double orc_record_lnl(orc_chain* c);    /* RecordCPU likelihood only, no side ef
  * on the chain except scratch). out must hold N*K doubles. */
 void orc_loglik_noadmix(orc_chain* c, double* out);
 
+/* Run nsweeps sweeps (after orc_init when init != 0) on each of n chains
+ * with nthreads host threads, one chain at a time per thread: the run-level
+ * parallelism of the reference's -structure_nstream (structure.cpp:2467-2499). */
+void orc_sweep_many(orc_chain** cs, int n, int nsweeps, int nthreads, int init);
+
 /* Output files in the reference's format (structure.cpp:86-401). */
 int orc_write_structure(orc_chain* c, const char* out_prefix, int rep, int id,
                         const char* const* ind_names, const char* const* pop_names,

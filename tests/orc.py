@@ -66,6 +66,8 @@ def lib():
         L.orc_r.argtypes = [P]
         L.orc_binaryq.restype = C.POINTER(C.c_int32)
         L.orc_binaryq.argtypes = [P]
+        L.orc_sweep_many.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.orc_sweep_many.restype = None
         L.orc_hash_ulong_c.restype = C.c_uint32
         L.orc_hash_ulong_c.argtypes = [C.c_uint64]
         _lib = L

@@ -9,7 +9,33 @@
 #include <cstring>
 #include <thread>
 
+#include <cuda_runtime.h>
+
 #include "vp_internal.h"
+
+template <typename T>
+void HostBuf<T>::release() {
+    if (!p) return;
+    if (pinned) cudaFreeHost(p);
+    else free(p);
+    p = nullptr;
+    n = 0;
+}
+template <typename T>
+void HostBuf<T>::resize(size_t m) {
+    release();
+    if (m == 0) return;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0 && cudaMallocHost((void**)&p, m * sizeof(T)) == cudaSuccess)
+        pinned = true;
+    else {
+        cudaGetLastError();
+        p = (T*)malloc(m * sizeof(T));
+        pinned = false;
+    }
+    n = m;
+}
+template struct HostBuf<uint32_t>;
 
 namespace {
 

@@ -6,11 +6,31 @@
 
 #include "../../include/vcfpop_structure.h"
 
+// host buffer that is page-locked when a CUDA device is present (so uploads
+// run at full copy-engine speed), plain heap memory otherwise
+template <typename T>
+struct HostBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    bool pinned = false;
+    HostBuf() = default;
+    HostBuf(const HostBuf&) = delete;
+    HostBuf& operator=(const HostBuf&) = delete;
+    ~HostBuf() { release(); }
+    void release();
+    void resize(size_t m);
+    T* data() { return p; }
+    const T* data() const { return p; }
+    size_t size() const { return n; }
+    T& operator[](size_t i) { return p[i]; }
+    const T& operator[](size_t i) const { return p[i]; }
+};
+
 struct vp_dataset {
     int32_t N = 0, S = 0, vmax = 0, maxploidy = 0, maxK = 0, Nw = 0;
     int64_t L = 0, KT = 0, coprime = 1;
     bool packed2 = false;
-    std::vector<uint32_t> g2;      // packed2: [L][Nw] 2-bit codes, sorted locus order
+    HostBuf<uint32_t> g2;          // packed2: [L][Nw] 2-bit codes, sorted locus order
     std::vector<uint8_t> gb;       // general: [L][N][vmax] allele per copy, 0xFF none
     std::vector<int32_t> k;        // [L] alleles
     std::vector<int64_t> off;      // [L] allele offsets

@@ -32,6 +32,14 @@ struct vp_ctx {
     int nsm = 132;
     TcOperands tc;
     struct TcBatch* batch = nullptr;
+    // cached graph of one sweep of a set of plain-form chains
+    std::vector<vp_chain*> pg_chains;
+    cudaGraphExec_t pg = nullptr;
+    int pg_nodes = 0;
+    // CUDA events around the dominant kernel of each sweep (likelihood stream
+    // or contraction), captured into the graphs when enabled
+    int prof = 0, prof_next = 0, prof_used = 0;
+    std::vector<cudaEvent_t> prof_ev;
 };
 
 struct vp_chain {
@@ -110,6 +118,19 @@ int upload(vp_ctx* ctx, const T* host, size_t n, const T** dev) {
 
 inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
+// begin/end markers around one launch of the dominant kernel
+void prof_mark(vp_ctx* x, bool begin) {
+    if (!x->prof) return;
+    int idx = x->prof_next * 2 + (begin ? 0 : 1);
+    while ((int)x->prof_ev.size() <= idx) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        x->prof_ev.push_back(e);
+    }
+    cudaEventRecord(x->prof_ev[idx], x->stream);
+    if (!begin) { x->prof_next++; x->prof_used = std::max(x->prof_used, x->prof_next); }
+}
+
 // bump allocator over one device allocation
 struct Carve {
     char* base;
@@ -128,6 +149,8 @@ int kc_for(int K) { return K <= 4 ? 4 : K <= 8 ? 8 : 16; }
 int launch_loglik(vp_chain* c, int force) {
     vp_ctx* x = c->ctx;
     dim3 g(cdiv(x->N, LL_BLOCK), c->h.nchunk, c->kgroups);
+    prof_mark(x, true);
+    struct End { vp_ctx* x; ~End() { prof_mark(x, false); } } end_{x};
     switch (c->kc) {
         case 4: LAUNCH(x, k_loglik<4>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
         case 8: LAUNCH(x, k_loglik<8>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
@@ -304,6 +327,8 @@ extern "C" int vp_close(vp_ctx* x) {
     cudaSetDevice(x->device);
     if (x->stream) cudaStreamSynchronize(x->stream);
     if (x->batch) { cudaGraphExecDestroy(x->batch->graph); cudaFree(x->batch->mem); delete x->batch; x->batch = nullptr; }
+    if (x->pg) cudaGraphExecDestroy(x->pg);
+    for (cudaEvent_t e : x->prof_ev) cudaEventDestroy(e);
     for (void* p : x->allocs) cudaFree(p);
     if (x->stream) cudaStreamDestroy(x->stream);
     delete x;
@@ -450,6 +475,13 @@ extern "C" int vp_chain_destroy(vp_chain* c) {
     if (c->ctx->batch)
         for (vp_chain* o : c->ctx->batch->chains)
             if (o == c) { free_batch(c->ctx); break; }
+    for (vp_chain* o : c->ctx->pg_chains)
+        if (o == c) {
+            cudaGraphExecDestroy(c->ctx->pg);
+            c->ctx->pg = nullptr;
+            c->ctx->pg_chains.clear();
+            break;
+        }
     if (c->graph) cudaGraphExecDestroy(c->graph);
     cudaFree(c->mem);
     delete c;
@@ -461,6 +493,8 @@ extern "C" int vp_chain_destroy(vp_chain* c) {
 static int capture_sweep(vp_chain** cs, int n, cudaGraphExec_t* exec, int* nodes) {
     vp_ctx* x = cs[0]->ctx;
     cudaGraph_t g;
+    x->prof_next = 0;
+    x->prof_used = 0;
     CK(cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal));
     int64_t before = x->launches;
     int rc = VP_OK;
@@ -493,7 +527,8 @@ extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
         for (int i = 0; i < n; ++i) cs[i]->issued += step;
         return VP_OK;
     }
-    // chains with sweeps left; equal remaining counts share one graph
+    // chains with sweeps left; a set of chains whose sweeps are all still
+    // pending shares one cached graph of a sweep
     int left = nsweeps;
     while (left > 0) {
         std::vector<vp_chain*> act;
@@ -503,33 +538,18 @@ extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
             if (rem > 0) { act.push_back(cs[i]); step = std::min(step, rem); }
         }
         if (act.empty()) break;
-        if (step >= 4 && act.size() == 1) {
-            vp_chain* c = act[0];
-            if (!c->graph) {
-                int rc = capture_sweep(&c, 1, &c->graph, &c->graph_nodes);
-                if (rc) return rc;
-            }
-            for (int s = 0; s < step; ++s) {
-                CK(cudaGraphLaunch(c->graph, x->stream));
-                x->launches += c->graph_nodes;
-            }
-        } else if (step >= 4) {
-            cudaGraphExec_t ex;
-            int nodes = 0;
-            int rc = capture_sweep(act.data(), (int)act.size(), &ex, &nodes);
+        if (x->pg && x->pg_chains != act) {
+            cudaGraphExecDestroy(x->pg);
+            x->pg = nullptr;
+        }
+        if (!x->pg) {
+            int rc = capture_sweep(act.data(), (int)act.size(), &x->pg, &x->pg_nodes);
             if (rc) return rc;
-            for (int s = 0; s < step; ++s) {
-                cudaError_t e = cudaGraphLaunch(ex, x->stream);
-                if (e != cudaSuccess) { cudaGraphExecDestroy(ex); vp_set_error("graph launch: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
-                x->launches += nodes;
-            }
-            cudaGraphExecDestroy(ex);
-        } else {
-            for (int s = 0; s < step; ++s)
-                for (vp_chain* c : act) {
-                    int rc = launch_sweep(c);
-                    if (rc) return rc;
-                }
+            x->pg_chains = act;
+        }
+        for (int s = 0; s < step; ++s) {
+            CK(cudaGraphLaunch(x->pg, x->stream));
+            x->launches += x->pg_nodes;
         }
         for (vp_chain* c : act) c->issued += step;
         left -= step;
@@ -869,7 +889,9 @@ int launch_tc_sweep(vp_ctx* x) {
         g.kb_per_split = (g.kblocks + b->splits - 1) / b->splits;
         g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.stages = 2; g.mode = 0;
         g.out_f = b->LLpart; g.ldo = b->Rpad; g.err = t.err;
+        prof_mark(x, true);
         int rc = launch_gemm(x, t.mapC, b->mapWhi, b->mapWlo, g, dim3((unsigned)(t.Npad / 128), b->G, b->splits));
+        prof_mark(x, false);
         if (rc) return rc;
     }
     // labels of every chain, one-hot rows for the count contraction
@@ -897,6 +919,8 @@ int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps) {
     TcBatch* b = x->batch;
     if (!b->graph) {
         cudaGraph_t g;
+        x->prof_next = 0;
+        x->prof_used = 0;
         CK(cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal));
         int64_t before = x->launches;
         rc = launch_tc_sweep(x);
@@ -975,4 +999,30 @@ extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const u
     cudaStreamDestroy(tmp.stream);
     tmp.stream = nullptr;
     return rc;
+}
+
+extern "C" void* vp_stream(vp_ctx* x) { return x ? (void*)x->stream : nullptr; }
+
+extern "C" int vp_prof_enable(vp_ctx* x, int on) {
+    if (!x) { vp_set_error("null context"); return VP_E_ARG; }
+    if (x->prof == on) return VP_OK;
+    x->prof = on;
+    // cached graphs were captured with or without the markers: re-capture
+    if (x->pg) { cudaGraphExecDestroy(x->pg); x->pg = nullptr; x->pg_chains.clear(); }
+    if (x->batch && x->batch->graph) { cudaGraphExecDestroy(x->batch->graph); x->batch->graph = nullptr; }
+    return VP_OK;
+}
+
+extern "C" int vp_prof_read(vp_ctx* x, double* ms, int32_t* launches) {
+    if (!x || !ms || !launches) { vp_set_error("null argument"); return VP_E_ARG; }
+    CK(cudaStreamSynchronize(x->stream));
+    double t = 0;
+    for (int j = 0; j < x->prof_used; ++j) {
+        float e = 0;
+        CK(cudaEventElapsedTime(&e, x->prof_ev[2 * j], x->prof_ev[2 * j + 1]));
+        t += e;
+    }
+    *ms = t;
+    *launches = x->prof_used;
+    return VP_OK;
 }
