@@ -1,0 +1,61 @@
+"""The drop-in driver against the reference program's own output files.
+
+vcfpop-gb300 takes the reference's flags and writes the reference's files. With
+the reference random streams its likelihood trace follows the golden file
+(written by the reference binary) at the start of the chain; for every golden
+case the files have the reference's layout line for line.
+"""
+import gzip
+import json
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+from vcfpop_gb300.build import CLI
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+CASES = json.load(open(os.path.join(GOLD, "cases.json")))
+NUM = re.compile(r"-?\d+\.\d+|nan")
+
+
+def _run(case, tmp, rng):
+    c = CASES[case]
+    vcf = os.path.join(tmp, "data.vcf")
+    with gzip.open(os.path.join(GOLD, c["data"]), "rb") as fi, open(vcf, "wb") as fo:
+        shutil.copyfileobj(fi, fo)
+    args = [CLI, f"-g_input={vcf}", f"-g_output={tmp}/out", f"-g_seed={c['seed']}", "-g_decimal=15",
+            f"-g_indtext={c['indtext']}", "-structure", "-structure_writelnl=yes", f"-gb300_rng={rng}"] + c["flags"]
+    subprocess.run(args, check=True)
+    return c
+
+
+def _shape(text):
+    return [NUM.sub("#", ln) for ln in text.replace("\r", "").split("\n")]
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_cli_files_have_reference_layout(case, tmp_path):
+    c = _run(case, str(tmp_path), "counter")
+    for f in c["files"]:
+        if f == "out.structure.txt":
+            continue
+        got = open(tmp_path / f, "rb").read().decode()
+        want = open(os.path.join(GOLD, case, f), "rb").read().decode()
+        assert _shape(got) == _shape(want), f
+        assert got.count("\r\n") == want.count("\r\n")
+
+
+@pytest.mark.parametrize("case", ["c1_noadmix", "adm_admix"])
+def test_cli_reference_streams_follow_golden_trace(case, tmp_path):
+    c = _run(case, str(tmp_path), "reference")
+    f = [x for x in c["files"] if x.endswith(".lnl.txt")][0]
+    got = [float(x) for x in NUM.findall(open(tmp_path / f).read())]
+    want = [float(x) for x in NUM.findall(open(os.path.join(GOLD, case, f)).read())]
+    assert len(got) == len(want)
+    for g, w in list(zip(got, want))[:3]:
+        assert abs(g - w) <= 1e-5 * abs(w), (g, w)

@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "--fmad=false", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"] + ARCH
 
 CU = ["vp_structure.cu"]
-CPP = ["vp_data.cpp"]
+CPP = ["vp_data.cpp"]  # vp_cli.cpp is the driver binary, built with g++ below
 
 
 def _newer(target, deps):
@@ -31,8 +31,10 @@ def _newer(target, deps):
 
 def build(verbose=False):
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    if not os.path.exists(CLI):
+        deps.append(CLI)
     deps.append(os.path.join(os.path.dirname(PKG), "include", "vcfpop_structure.h"))
-    if not _newer(LIB, deps):
+    if os.path.exists(CLI) and not _newer(LIB, deps) and not _newer(CLI, deps):
         return LIB
     objdir = os.path.join(PKG, "_build")
     os.makedirs(objdir, exist_ok=True)
@@ -52,6 +54,10 @@ def build(verbose=False):
     tmp = LIB + ".tmp"
     subprocess.check_call([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
     os.replace(tmp, LIB)
+    # the command-line driver links the library by its in-tree path
+    cli_obj = os.path.join(objdir, "vp_cli.o")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-c", os.path.join(CSRC, "vp_cli.cpp"), "-o", cli_obj])
+    subprocess.check_call(["g++", "-o", CLI, cli_obj, LIB, "-Wl,-rpath," + PKG, "-lz"])
     return LIB
 
 

@@ -1,0 +1,478 @@
+// vcfpop-gb300: drop-in driver for vcfpop's -structure analysis on one GPU.
+//
+// Takes the reference's flag block (-g_input, -g_output, -g_seed, -g_indtext,
+// -g_decimal, -g_delimiter, -g_linebreak and -structure_*,
+// src/parameters.cpp:584-627, 1230-1307), reads VCF (plain or gzip), groups
+// individuals by population as the reference does (src/filter.cpp:300-345),
+// runs every (K, replicate) run through libvcfpop_structure and writes the
+// reference's result files (src/structure.cpp:86-401):
+//   <out>.structure.k=K_rep=R_id=I.txt, its .lnl.txt with -structure_writelnl,
+//   and the summary <out>.structure.txt.
+// Extra flags: -gb300_rng=counter|reference, -gb300_form=plain|tc,
+// -gb300_device=D.
+#include <zlib.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/vcfpop_structure.h"
+
+namespace {
+
+struct Opts {
+    std::string input, output = "vcfpop", indtext;
+    int64_t seed = 0;
+    int decimal = 5;
+    std::string delim = "\t", lb = "\r\n";
+    int kmin = 1, kmax = 5, nruns = 1, diversity = 0, device = 0;
+    vp_params p;
+    std::vector<std::string> argv;
+};
+
+int yesno(const std::string& v) { return v == "yes" ? 1 : 0; }
+
+bool parse(int argc, char** argv, Opts& o) {
+    vp_params_default(&o.p);
+    o.p.rng = VP_RNG_COUNTER;
+    bool structure = false;
+    for (int i = 1; i < argc; ++i) {
+        std::string a = argv[i];
+        o.argv.push_back(a);
+        size_t eq = a.find('=');
+        std::string k = a.substr(0, eq), v = eq == std::string::npos ? "" : a.substr(eq + 1);
+        if (v.size() >= 2 && v.front() == '"' && v.back() == '"') v = v.substr(1, v.size() - 2);
+        if (k == "-structure") structure = true;
+        else if (k == "-g_input") o.input = v;
+        else if (k == "-g_output") o.output = v;
+        else if (k == "-g_seed") o.seed = atoll(v.c_str());
+        else if (k == "-g_decimal") o.decimal = atoi(v.c_str());
+        else if (k == "-g_indtext") o.indtext = v;
+        else if (k == "-g_delimiter") o.delim = v == "comma" ? "," : "\t";
+        else if (k == "-g_linebreak") o.lb = v == "unix" ? "\n" : "\r\n";
+        else if (k == "-gb300_rng") o.p.rng = v == "reference" ? VP_RNG_REFERENCE : VP_RNG_COUNTER;
+        else if (k == "-gb300_form") o.p.form = v == "tc" ? VP_FORM_TC : VP_FORM_PLAIN;
+        else if (k == "-gb300_device") o.device = atoi(v.c_str());
+        else if (k == "-structure_admix") o.p.admix = yesno(v);
+        else if (k == "-structure_locpriori") o.p.locpriori = yesno(v);
+        else if (k == "-structure_f") o.p.fmodel = yesno(v);
+        else if (k == "-structure_krange") sscanf(v.c_str(), "[%d,%d]", &o.kmin, &o.kmax);
+        else if (k == "-structure_nburnin") o.p.nburnin = atoi(v.c_str());
+        else if (k == "-structure_nreps") o.p.nreps = atoi(v.c_str());
+        else if (k == "-structure_nthinning") o.p.nthinning = atoi(v.c_str());
+        else if (k == "-structure_nruns") o.nruns = atoi(v.c_str());
+        else if (k == "-structure_nadmburnin") o.p.nadmburnin = atoi(v.c_str());
+        else if (k == "-structure_writelnl") o.p.writelnl = yesno(v);
+        else if (k == "-structure_diversity") o.diversity = yesno(v);
+        else if (k == "-structure_lambda") o.p.lambda = atof(v.c_str());
+        else if (k == "-structure_stdlambda") o.p.stdlambda = atof(v.c_str());
+        else if (k == "-structure_maxlambda") o.p.maxlambda = atof(v.c_str());
+        else if (k == "-structure_alpha") o.p.alpha = atof(v.c_str());
+        else if (k == "-structure_inferalpha") o.p.inferalpha = yesno(v);
+        else if (k == "-structure_diffalpha") o.p.diffalpha = yesno(v);
+        else if (k == "-structure_uniformalpha") o.p.uniformalpha = yesno(v);
+        else if (k == "-structure_stdalpha") o.p.stdalpha = atof(v.c_str());
+        else if (k == "-structure_maxalpha") o.p.maxalpha = atof(v.c_str());
+        else if (k == "-structure_alphapriora") o.p.alphapriora = atof(v.c_str());
+        else if (k == "-structure_alphapriorb") o.p.alphapriorb = atof(v.c_str());
+        else if (k == "-structure_metrofreq") o.p.metrofreq = atoi(v.c_str());
+        else if (k == "-structure_r") o.p.r = atof(v.c_str());
+        else if (k == "-structure_maxr") o.p.maxr = atof(v.c_str());
+        else if (k == "-structure_stdr") o.p.epsr = atof(v.c_str());
+        else if (k == "-structure_epseta") o.p.epseta = atof(v.c_str());
+        else if (k == "-structure_epsgamma") o.p.epsgamma = atof(v.c_str());
+        else if (k == "-structure_pmeanf") o.p.pmeanf = atof(v.c_str());
+        else if (k == "-structure_pstdf") o.p.pstdf = atof(v.c_str());
+        else if (k == "-structure_stdf") o.p.stdf = atof(v.c_str());
+        else if (k == "-structure_singlef") o.p.fsame = yesno(v);
+        // other -g_* and -structure_* flags (threads, SIMD, plots, streams) do
+        // not apply to the GPU path and are accepted silently
+    }
+    if (!structure) { fprintf(stderr, "vcfpop-gb300: only -structure is implemented\n"); return false; }
+    if (o.input.empty()) { fprintf(stderr, "vcfpop-gb300: -g_input is required\n"); return false; }
+    return true;
+}
+
+struct Vcf {
+    std::vector<std::string> inds, locs;
+    std::vector<int32_t> ploidy, k;
+    std::vector<int8_t> G;  // [L][N][vmax]
+    int vmax = 0;
+};
+
+bool read_vcf(const std::string& path, Vcf& v) {
+    gzFile f = gzopen(path.c_str(), "rb");
+    if (!f) return false;
+    std::vector<char> buf(1 << 24);
+    std::string line;
+    int64_t nl = 0;
+    auto getline_gz = [&](std::string& out) -> bool {
+        out.clear();
+        for (;;) {
+            if (!gzgets(f, buf.data(), (int)buf.size())) return !out.empty();
+            out += buf.data();
+            if (!out.empty() && out.back() == '\n') return true;
+        }
+    };
+    while (getline_gz(line)) {
+        while (!line.empty() && (line.back() == '\n' || line.back() == '\r')) line.pop_back();
+        if (line.rfind("##", 0) == 0) continue;
+        std::vector<std::string> cols;
+        size_t s0 = 0;
+        for (;;) {
+            size_t t = line.find('\t', s0);
+            cols.push_back(line.substr(s0, t == std::string::npos ? std::string::npos : t - s0));
+            if (t == std::string::npos) break;
+            s0 = t + 1;
+        }
+        if (line[0] == '#') {
+            for (size_t c = 9; c < cols.size(); ++c) v.inds.push_back(cols[c]);
+            continue;
+        }
+        const int N = (int)v.inds.size();
+        int nalt = 1;
+        for (char ch : cols[4]) nalt += ch == ',';
+        v.k.push_back(1 + nalt);
+        v.locs.push_back(cols[0] + "_" + cols[1]);
+        if (nl == 0) {
+            for (int i = 0; i < N; ++i) {
+                const std::string& g = cols[9 + i];
+                int p = 1;
+                for (char ch : g.substr(0, g.find(':'))) p += ch == '/' || ch == '|';
+                v.ploidy.push_back(p);
+                v.vmax = std::max(v.vmax, p);
+            }
+        }
+        size_t base = v.G.size();
+        v.G.resize(base + (size_t)N * v.vmax, -1);
+        for (int i = 0; i < N; ++i) {
+            std::string g = cols[9 + i];
+            g = g.substr(0, g.find(':'));
+            int8_t al[16];
+            int n = 0;
+            bool miss = false;
+            size_t q = 0;
+            while (q <= g.size() && n < 16) {
+                size_t e = g.find_first_of("/|", q);
+                std::string tok = g.substr(q, e == std::string::npos ? std::string::npos : e - q);
+                if (tok == "." || tok.empty()) miss = true;
+                else al[n] = (int8_t)atoi(tok.c_str());
+                n++;
+                if (e == std::string::npos) break;
+                q = e + 1;
+            }
+            if (miss) continue;
+            std::sort(al, al + n);
+            for (int c = 0; c < n && c < v.vmax; ++c) v.G[base + (size_t)i * v.vmax + c] = al[c];
+        }
+        nl++;
+    }
+    gzclose(f);
+    return nl > 0;
+}
+
+// -g_indtext="pop1:#1-#30,#40 pop2:#31-#39 ..." (1-based individual ranges)
+void populations(const std::string& spec, int N, std::vector<int>& popid, std::vector<std::string>& names) {
+    popid.assign(N, -1);
+    if (spec.empty()) { names = {"pop1"}; popid.assign(N, 0); return; }
+    size_t s0 = 0;
+    while (s0 < spec.size()) {
+        size_t e = spec.find(' ', s0);
+        std::string tok = spec.substr(s0, e == std::string::npos ? std::string::npos : e - s0);
+        s0 = e == std::string::npos ? spec.size() : e + 1;
+        size_t colon = tok.find(':');
+        if (colon == std::string::npos) continue;
+        int pid = (int)names.size();
+        names.push_back(tok.substr(0, colon));
+        std::string r = tok.substr(colon + 1);
+        size_t q = 0;
+        while (q < r.size()) {
+            size_t c = r.find(',', q);
+            std::string rg = r.substr(q, c == std::string::npos ? std::string::npos : c - q);
+            q = c == std::string::npos ? r.size() : c + 1;
+            int a = 0, b = 0;
+            if (sscanf(rg.c_str(), "#%d-#%d", &a, &b) != 2) { sscanf(rg.c_str(), "#%d", &a); b = a; }
+            for (int i = a; i <= b && i <= N; ++i)
+                if (i >= 1) popid[i - 1] = pid;
+        }
+    }
+    // individuals without a population go to an extra "pop0"-style group at the end
+    bool orphan = false;
+    for (int i = 0; i < N; ++i)
+        if (popid[i] < 0) { popid[i] = (int)names.size(); orphan = true; }
+    if (orphan) names.push_back("Unassigned");
+}
+
+struct Writer {
+    FILE* f;
+    const Opts& o;
+    char fmt[16];
+    Writer(FILE* f_, const Opts& o_) : f(f_), o(o_) { snprintf(fmt, sizeof fmt, "%%0.%df", o.decimal); }
+    void real(double v) {
+        if (std::isnan(v) || std::isinf(v)) fputs("nan", f);
+        else fprintf(f, fmt, v);
+    }
+    void s(const char* t) { fputs(t, f); }
+    void lb() { fputs(o.lb.c_str(), f); }
+    void d() { fputs(o.delim.c_str(), f); }
+};
+
+// WriteStructure (src/structure.cpp:86-377)
+void write_run(const Opts& o, const vp_params& P, const vp_result& r, int rep, int id, const std::vector<std::string>& inds,
+               const std::vector<std::string>& pnames, const std::vector<int>& popid, const std::vector<int32_t>& k,
+               const std::vector<std::string>& locs, int S, int maxK) {
+    char fn[8192];
+    const int K = r.K, N = r.N;
+    const int64_t L = (int64_t)k.size();
+    if (P.writelnl) {
+        snprintf(fn, sizeof fn, "%s.structure.k=%d_rep=%d_id=%d.lnl.txt", o.output.c_str(), K, rep, id);
+        FILE* f = fopen(fn, "wb");
+        Writer w(f, o);
+        fprintf(f, "%d", r.nburnin); w.lb();
+        w.s("Iteration"); w.d(); w.s("lnL"); w.lb();
+        int j = 0;
+        for (int i = 0; i < r.nburnin; i += r.nthinning) { fprintf(f, "%d", i); w.d(); w.real(r.lnl[j++]); w.lb(); }
+        for (int i = 0; i < r.nreps; i += r.nthinning) { fprintf(f, "%d", i + r.nburnin); w.d(); w.real(r.lnl[j++]); w.lb(); }
+        fclose(f);
+    }
+    snprintf(fn, sizeof fn, "%s.structure.k=%d_rep=%d_id=%d.txt", o.output.c_str(), K, rep, id);
+    FILE* f = fopen(fn, "wb");
+    Writer w(f, o);
+    w.lb(); w.lb(); w.s("Parameters:"); w.lb();
+    fprintf(f, "Seed=%lld", (long long)r.seed); w.lb();
+    fprintf(f, "Model=%s,%s,%s", P.admix ? "ADM" : "NOADM", P.locpriori ? "LOC" : "NOLOC", P.fmodel ? "F" : "NOF"); w.lb();
+    fprintf(f, "Number of cluster=%d", K); w.lb();
+    fprintf(f, "Replicate=%d", rep); w.lb();
+    fprintf(f, "Run id=%d", id); w.lb();
+    w.s("Mean value of ln likelihood="); w.real(r.rout[0]); w.lb();
+    w.s("Variance of ln likelihood="); w.real(r.rout[2]); w.lb();
+    w.s("Estimated Ln Prob of Data="); w.real(r.rout[3]); w.lb(); w.lb();
+    const int nf = P.fmodel ? (P.fsame ? 1 : K) : 0, nl = P.difflambda ? K : 1;
+    if (P.locpriori) {
+        w.lb(); w.s("Mean value of r="); w.real(r.rout[4 + nl]);
+        w.lb(); fprintf(f, "Mean value of global %s", P.admix ? "alpha" : "eta");
+        w.lb(); w.d(); w.s("Cluster"); w.lb();
+        for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
+        w.lb();
+        for (int j = 0; j < K; ++j) { w.d(); w.real(r.rout[4 + nl + 1 + j]); }
+        w.lb(); fprintf(f, "Mean value of local %s for each location", P.admix ? "alpha" : "gamma");
+        w.lb(); w.d(); w.s("Cluster"); w.lb(); w.s("Pop");
+        for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
+        for (int i = 0; i < S; ++i) {
+            w.lb(); w.s(pnames[i].c_str());
+            for (int j = 0; j < K; ++j) { w.d(); w.real(r.rout[4 + nl + 1 + K + i * K + j]); }
+        }
+    } else if (P.admix && P.inferalpha) {
+        if (!P.diffalpha) { w.lb(); w.s("Mean value of alpha="); w.real(r.rout[4 + nl]); }
+        else for (int j = 0; j < K; ++j) { w.lb(); fprintf(f, "Mean value of alpha_%d=", j + 1); w.real(r.rout[4 + nl + j]); }
+    }
+    if (P.fmodel) {
+        if (P.fsame) { w.lb(); w.s("Mean value of Fst="); w.real(r.rout[r.rlen - 1]); }
+        else {
+            w.lb(); w.s("Mean value of Fst"); w.lb(); w.d(); w.s("Cluster"); w.lb();
+            for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
+            w.lb();
+            for (int i = 0; i < nf; ++i) { w.d(); w.real(r.rout[r.rlen - nf + i]); }
+        }
+    }
+    // membership of each population from the final Q, Unify(float) per row
+    std::vector<float> O((size_t)S * K, 0.f);
+    w.lb(); w.lb(); fprintf(f, "Proportion of membership of each pre-defined population in each of the %d clusters", K);
+    w.lb(); w.d(); w.s("Cluster"); w.lb(); w.s("Pop");
+    for (int i = 0; i < N; ++i)
+        for (int kk = 0; kk < K; ++kk) O[(size_t)popid[i] * K + kk] += r.Q[(size_t)i * K + kk];
+    for (int s = 0; s < S; ++s) {
+        double sum = 0;
+        for (int kk = 0; kk < K; ++kk) sum += O[(size_t)s * K + kk];
+        double inv = 1.0 / (sum + K * 1e-10);
+        for (int kk = 0; kk < K; ++kk) O[(size_t)s * K + kk] = (float)(((double)O[(size_t)s * K + kk] + 1e-10) * inv);
+    }
+    for (int kk = 0; kk < K; ++kk) { w.d(); fprintf(f, "%d", kk + 1); }
+    for (int s = 0; s < S; ++s) {
+        w.lb(); w.s(pnames[s].c_str());
+        for (int kk = 0; kk < K; ++kk) { w.d(); w.real(O[(size_t)s * K + kk]); }
+    }
+    w.lb(); w.lb(); w.s("Inferred ancestry of individuals");
+    w.lb(); w.d(); w.d(); w.s("Cluster");
+    w.lb(); w.s("Ind"); w.d(); w.s("Pop"); w.d(); w.s("RegL1");
+    for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
+    for (int i = 0; i < N; ++i) {
+        w.lb(); w.s(inds[i].c_str()); w.d(); w.s(pnames[popid[i]].c_str()); w.d(); w.s("Total");
+        for (int kk = 0; kk < K; ++kk) { w.d(); w.real(r.ancestry[(size_t)i * K + kk]); }
+    }
+    // heterozygosity and net nucleotide distance from the mean frequencies
+    std::vector<double> H(K, 0.0), D((size_t)K * K, 0.0), H2((size_t)K * L, 0.0);
+    for (int kk = 0; kk < K; ++kk) {
+        const float* p = r.freqm + (size_t)kk * r.KT;
+        for (int64_t l = 0; l < L; ++l) {
+            double ss = 0;
+            for (int a = 0; a < k[l]; ++a) ss += (double)p[a] * (double)p[a];
+            H2[(size_t)kk * L + l] = 1 - ss;
+            H[kk] += 1 - ss;
+            p += k[l];
+        }
+        H[kk] /= L;
+        for (int j = 0; j <= kk; ++j) {
+            const float *p1 = r.freqm + (size_t)kk * r.KT, *p2 = r.freqm + (size_t)j * r.KT;
+            double dt = 0;
+            for (int64_t l = 0; l < L; ++l) {
+                double sp = 0;
+                for (int a = 0; a < k[l]; ++a) sp += (double)p1[a] * (double)p2[a];
+                dt += 1 - sp;
+                p1 += k[l]; p2 += k[l];
+            }
+            D[(size_t)j * K + kk] = D[(size_t)kk * K + j] = dt / L - (H[kk] + H[j]) / 2;
+        }
+    }
+    w.lb(); w.lb(); w.s("Allele-frequency divergence among pops (Net nucleotide distance)");
+    w.lb(); w.d(); w.s("Cluster"); w.lb(); w.s("Cluster");
+    for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
+    for (int i = 0; i < K; ++i) {
+        w.lb(); fprintf(f, "%d", i + 1);
+        for (int j = 0; j < K; ++j) { w.d(); w.real(D[(size_t)i * K + j]); }
+    }
+    if (o.diversity) {
+        w.lb(); w.lb(); w.s("Estimated genetic diversity in each cluster");
+        w.lb(); w.s("Locus"); w.d(); w.s("Cluster"); w.d(); w.s("Heterozygosity");
+        for (int a = 0; a < maxK; ++a) { w.d(); fprintf(f, "Allele%d", a); }
+        for (int kk = 0; kk < K; ++kk) { w.lb(); w.s(kk ? "" : "Average"); w.d(); fprintf(f, "%d", kk + 1); w.real(H[kk]); }
+        int64_t off = 0;
+        for (int64_t l = 0; l < L; ++l) {
+            for (int kk = 0; kk < K; ++kk) {
+                w.lb(); w.s(kk ? "" : locs[l].c_str()); w.d(); fprintf(f, "%d", kk + 1); w.d();
+                w.real(H2[(size_t)kk * L + l]);
+                for (int a = 0; a < k[l]; ++a) { w.d(); w.real(r.freqm[(size_t)kk * r.KT + off + a]); }
+            }
+            off += k[l];
+        }
+    }
+    fclose(f);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    Opts o;
+    if (!parse(argc, argv, o)) return 2;
+    Vcf v;
+    if (!read_vcf(o.input, v)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
+    const int N = (int)v.inds.size();
+    const int64_t L0 = (int64_t)v.k.size();
+    std::vector<int> pop;
+    std::vector<std::string> pnames;
+    populations(o.indtext, N, pop, pnames);
+    // group individuals by population in the populations' order (stable)
+    std::vector<int> perm(N);
+    for (int i = 0; i < N; ++i) perm[i] = i;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return pop[a] < pop[b]; });
+    std::vector<std::string> inds(N);
+    std::vector<int32_t> ploidy(N), popid(N);
+    std::vector<int8_t> G((size_t)L0 * N * v.vmax);
+    for (int j = 0; j < N; ++j) {
+        int i = perm[j];
+        inds[j] = v.inds[i]; ploidy[j] = v.ploidy[i]; popid[j] = pop[i];
+        for (int64_t l = 0; l < L0; ++l)
+            memcpy(&G[((size_t)l * N + j) * v.vmax], &v.G[((size_t)l * N + i) * v.vmax], v.vmax);
+    }
+    // drop populations without individuals, keeping the order
+    std::vector<int> remap(pnames.size(), -1);
+    std::vector<std::string> pn;
+    for (int j = 0; j < N; ++j)
+        if (remap[popid[j]] < 0) { remap[popid[j]] = (int)pn.size(); pn.push_back(pnames[popid[j]]); }
+    for (int j = 0; j < N; ++j) popid[j] = remap[popid[j]];
+    const int S = (int)pn.size();
+    bool biallelic_diploid = v.vmax == 2;
+    for (int i = 0; i < N && biallelic_diploid; ++i) biallelic_diploid = ploidy[i] == 2;
+    for (int64_t l = 0; l < L0 && biallelic_diploid; ++l) biallelic_diploid = v.k[l] == 2;
+    std::vector<uint32_t> packed;
+    vp_input in{};
+    in.n_ind = N; in.n_loc = L0; in.vmax = v.vmax; in.ploidy = ploidy.data(); in.n_alleles = v.k.data();
+    in.popid = popid.data(); in.n_pop = S;
+    if (biallelic_diploid) {
+        const int Nw = (N + 15) / 16;
+        packed.assign((size_t)L0 * Nw, 0);
+        for (int64_t l = 0; l < L0; ++l)
+            for (int i = 0; i < Nw * 16; ++i) {
+                int code = 3;
+                if (i < N) {
+                    const int8_t* g = &G[((size_t)l * N + i) * 2];
+                    if (g[0] >= 0) code = g[0] + g[1];
+                }
+                packed[(size_t)l * Nw + i / 16] |= (uint32_t)code << (2 * (i % 16));
+            }
+        in.packed2 = packed.data();
+    } else {
+        in.alleles = G.data();
+    }
+    vp_dataset* ds = nullptr;
+    if (vp_dataset_prepare(&in, &ds)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+    vp_dataset_info info;
+    vp_dataset_info_get(ds, &info);
+    std::vector<int64_t> order(info.n_loc);
+    vp_dataset_order(ds, order.data());
+    std::vector<int32_t> ks(info.n_loc);
+    std::vector<std::string> lnames(info.n_loc);
+    for (int64_t l = 0; l < info.n_loc; ++l) { ks[l] = v.k[order[l]]; lnames[l] = v.locs[order[l]]; }
+    vp_ctx* ctx = nullptr;
+    if (vp_open(ds, o.device, &ctx)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+    struct Run { int K, rep, id; vp_chain* c; };
+    std::vector<Run> runs;
+    int id = 0;
+    for (int K = o.kmin; K <= o.kmax; ++K)
+        for (int rep = 1; rep <= o.nruns; ++rep) {
+            ++id;
+            vp_params p = o.p;
+            p.K = K;
+            p.seed = vp_run_seed(o.seed, id);
+            vp_chain* c = nullptr;
+            if (vp_chain_create(ctx, &p, &c)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+            runs.push_back({K, rep, id, c});
+        }
+    std::vector<vp_chain*> cs;
+    for (auto& r : runs) cs.push_back(r.c);
+    if (vp_finish(cs.data(), (int)cs.size())) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+    std::vector<std::array<double, 3>> table;
+    for (auto& run : runs) {
+        vp_result r;
+        vp_chain_sizes(run.c, &r);
+        std::vector<double> rout(r.rlen), lnl(std::max(r.nlnl, 1)), anc((size_t)r.N * r.K);
+        std::vector<float> Q((size_t)r.N * r.K), fm((size_t)r.K * r.KT);
+        r.rout = rout.data(); r.lnl = lnl.data(); r.Q = Q.data(); r.ancestry = anc.data(); r.freqm = fm.data();
+        if (vp_chain_result(run.c, &r)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+        vp_params p = o.p;
+        p.K = run.K;
+        write_run(o, p, r, run.rep, run.id, inds, pn, popid, ks, lnames, S, info.max_alleles);
+        table.push_back({rout[0], rout[2], rout[3]});
+        vp_chain_destroy(run.c);
+    }
+    // summary (src/structure.cpp:379-401)
+    char fn[8192];
+    snprintf(fn, sizeof fn, "%s.structure.txt", o.output.c_str());
+    FILE* f = fopen(fn, "wb");
+    Writer w(f, o);
+    time_t now = time(nullptr);
+    char tb[64];
+    strftime(tb, sizeof tb, "%Y-%m-%d %H:%M:%S", localtime(&now));
+    w.s("##Bayesian clustering calculated by vcfpop-gb300 (vcfpop v1.08b -structure)"); w.lb();
+    w.s("#  Input: "); w.s(o.input.c_str()); w.lb();
+    w.s("#  Output: "); w.s(o.output.c_str()); w.lb();
+    w.s("#  Time: "); w.s(tb); w.lb();
+    w.s("#  Parameter: "); w.s(argv[0]); w.lb();
+    for (auto& a : o.argv) { w.s("#    "); w.s(a.c_str()); w.lb(); }
+    w.lb(); w.lb(); w.s("ID"); w.d(); w.s("k"); w.d(); w.s("rep"); w.d(); w.s("Mean lnL"); w.d(); w.s("Var lnL"); w.d(); w.s("lnP(D)");
+    for (size_t i = 0; i < runs.size(); ++i) {
+        w.lb(); fprintf(f, "%d", runs[i].id); w.d(); fprintf(f, "%d", runs[i].K); w.d(); fprintf(f, "%d", runs[i].rep); w.d();
+        w.real(table[i][0]); w.d(); w.real(table[i][1]); w.d(); w.real(table[i][2]);
+    }
+    fclose(f);
+    vp_close(ctx);
+    vp_dataset_free(ds);
+    return 0;
+}

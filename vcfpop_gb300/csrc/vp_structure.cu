@@ -127,7 +127,9 @@ void prof_mark(vp_ctx* x, bool begin) {
         cudaEventCreate(&e);
         x->prof_ev.push_back(e);
     }
-    cudaEventRecord(x->prof_ev[idx], x->stream);
+    // external: captured into a graph as an event-record node that fires on
+    // every replay (a plain record would only become a capture dependency)
+    cudaEventRecordWithFlags(x->prof_ev[idx], x->stream, cudaEventRecordExternal);
     if (!begin) { x->prof_next++; x->prof_used = std::max(x->prof_used, x->prof_next); }
 }
 
@@ -752,7 +754,8 @@ int tc_operands(vp_ctx* x) {
     t.logpbar = (float*)q; q += t.Apad * 4;
     t.Bc = (double*)q; q += t.Npad * 8;
     t.err = (int*)q;
-    tc::k_build_counts<<<dim3(cdiv(t.Npad, 256), (unsigned)x->L, 1), 256, 0, x->stream>>>(x->D, t.C, t.CT, t.Apad, t.Npad);
+    tc::k_build_counts<<<dim3((unsigned)(t.Npad / 64), cdiv(x->L, 64), 1), 256, 0, x->stream>>>(x->D, t.C, t.CT, t.Apad,
+                                                                                              t.Npad);
     int rc = check_launch(x, "k_build_counts");
     if (rc) return rc;
     tc::k_allele_center<<<cdiv(x->L, 256), 256, 0, x->stream>>>(x->D, t.logpbar);

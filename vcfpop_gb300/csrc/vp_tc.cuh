@@ -271,20 +271,42 @@ namespace tc {
 // C  [Npad][Apad]: C[i][2l+a]  copies of allele a at locus l in individual i
 // CT [Apad][Npad]: the transpose (alleles x individuals)
 // Missing calls and the padding are zero.
-__global__ void k_build_counts(const DevData D, __nv_bfloat16* C, __nv_bfloat16* CT, int64_t Apad, int64_t Npad) {
-    const int64_t l = blockIdx.y;                   // one locus per grid row
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= Npad) return;
-    float c0 = 0.f, c1 = 0.f;
-    if (i < D.N && l < D.L) {
-        int code = (D.g2[l * D.Nw + (i >> 4)] >> ((i & 15) * 2)) & 3;
-        if (code != 3) { c1 = (float)code; c0 = 2.f - code; }
+// one CTA = a tile of 64 loci x 64 individuals: the 2-bit codes are decoded
+// into shared memory, then written as contiguous rows of both layouts
+__global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bfloat16* C, __nv_bfloat16* CT,
+                                                      int64_t Apad, int64_t Npad) {
+    __shared__ uint8_t code[64][64 + 4];   // [locus][individual]
+    const int i0 = blockIdx.x * 64;
+    const int64_t l0 = (int64_t)blockIdx.y * 64;
+    for (int j = threadIdx.x; j < 64 * 4; j += blockDim.x) {
+        const int ll = j >> 2, w = j & 3;
+        const int64_t l = l0 + ll;
+        const int wi = (i0 >> 4) + w;
+        uint32_t word = (l < D.L && wi < D.Nw) ? D.g2[l * D.Nw + wi] : 0xFFFFFFFFu;
+        for (int b = 0; b < 16; ++b) {
+            const int i = i0 + w * 16 + b;
+            code[ll][w * 16 + b] = (i < D.N) ? (uint8_t)((word >> (2 * b)) & 3) : 3;
+        }
     }
-    const __nv_bfloat16 b0 = __float2bfloat16(c0), b1 = __float2bfloat16(c1);
-    C[(int64_t)i * Apad + 2 * l] = b0;
-    C[(int64_t)i * Apad + 2 * l + 1] = b1;
-    CT[(2 * l) * Npad + i] = b0;
-    CT[(2 * l + 1) * Npad + i] = b1;
+    __syncthreads();
+    // CT rows: allele 2l+a, 64 individuals
+    for (int j = threadIdx.x; j < 128 * 64; j += blockDim.x) {
+        const int ii = j & 63, ra = j >> 6, ll = ra >> 1, a = ra & 1;
+        const int64_t l = l0 + ll;
+        if (l >= D.L) continue;
+        const int c = code[ll][ii];
+        const float v = c == 3 ? 0.f : (a ? (float)c : 2.f - c);
+        CT[(2 * l + a) * Npad + i0 + ii] = __float2bfloat16(v);
+    }
+    // C rows: individual i, alleles 2*l0 .. 2*l0+127
+    for (int j = threadIdx.x; j < 64 * 128; j += blockDim.x) {
+        const int col = j & 127, ii = j >> 7, ll = col >> 1, a = col & 1;
+        const int64_t l = l0 + ll;
+        if (l >= D.L) continue;
+        const int c = code[ll][ii];
+        const float v = c == 3 ? 0.f : (a ? (float)c : 2.f - c);
+        C[(int64_t)(i0 + ii) * Apad + 2 * l + a] = __float2bfloat16(v);
+    }
 }
 
 // per-allele centring constant: ln of the dataset allele frequency (with a
