@@ -177,6 +177,18 @@ int vp_tc_status(vp_ctx* ctx);
 int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N, int32_t K,
                        int32_t BN, int32_t piece, int32_t splits, int32_t stages, float* D);
 
+/* The likelihood accumulation of UpdateQNoAdmix (src/structure.cpp:902-932;
+ * the part BAYESIAN<REAL>::UpdateQNoAdmixCUDA offloads, src/structureCUDA.cpp:
+ * 2123-2214) as one call on device buffers, for biallelic diploid data:
+ *   geno  [L][ceil(N/16)] 2-bit codes (count of allele 1, 3 = missing)
+ *   freq  [K][2L] allele frequencies, cluster-major, 2 alleles per locus
+ *   ll    [N][K] output: sum over loci and copies of ln p (a zero frequency
+ *         counts as 2^-1023, as in the reference's exponent-split product)
+ * Asynchronous on `stream` (NULL = default stream); takes stream-ordered
+ * scratch memory for the per-genotype table and per-chunk partial sums. */
+int vp_loglik_packed2(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const float* freq, int32_t K,
+                      double* ll, void* stream);
+
 /* The CUDA stream (cudaStream_t) every launch of this context goes to. */
 void* vp_stream(vp_ctx* ctx);
 /* Record CUDA events around each launch of the sweep's dominant kernel (the

@@ -1029,3 +1029,102 @@ extern "C" int vp_prof_read(vp_ctx* x, double* ms, int32_t* launches) {
     *launches = x->prof_used;
     return VP_OK;
 }
+
+// ===================== standalone likelihood call =====================
+namespace {
+
+// per-genotype log-probability table of the likelihood stream from the
+// frequencies of K clusters over L biallelic loci (freq [K][2L])
+__global__ void k_lt_from_freq(const float* freq, int K, int64_t L, int kp, float* lt) {
+    int64_t kl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (kl >= (int64_t)K * L) return;
+    const int k = (int)(kl / L);
+    const int64_t l = kl % L;
+    const float l0 = ln_freq(freq[k * 2 * L + 2 * l]), l1 = ln_freq(freq[k * 2 * L + 2 * l + 1]);
+    float* t = lt + l * 4 * kp + k;
+    t[0] = l0 + l0;
+    t[kp] = l0 + l1;
+    t[2 * kp] = l1 + l1;
+    t[3 * kp] = 0.f;
+}
+
+__global__ void k_ll_reduce(const DevChain* chains, double* ll) {
+    const DevChain& c = chains[0];
+    const int64_t n = (int64_t)c.D.N * c.K;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        double v = 0;
+        for (int ch = 0; ch < c.nchunk; ++ch) v += c.LLp[(int64_t)ch * n + j];
+        ll[j] = v;
+    }
+}
+
+struct LLPlan {
+    DevChain h{};
+    size_t scratch = 0;   // bytes: descriptor, table, partials
+    int kc = 16, kgroups = 1;
+};
+
+int ll_plan(int32_t N, int64_t L, int32_t K, int nsm, LLPlan* pl) {
+    if (N <= 0 || L <= 0 || K < 1 || K > 64) { vp_set_error("loglik: bad sizes"); return VP_E_ARG; }
+    DevChain& h = pl->h;
+    h.D.N = N; h.D.L = L; h.D.KT = 2 * L; h.D.Nw = (N + 15) / 16; h.D.packed2 = 1; h.D.vmax = 2; h.D.maxK = 2;
+    h.K = K;
+    h.kp = (K + 3) & ~3;
+    pl->kc = kc_for(K);
+    pl->kgroups = (K + pl->kc - 1) / pl->kc;
+    int64_t nbi = cdiv(N, LL_BLOCK) * (int64_t)pl->kgroups;
+    int64_t nch = std::min<int64_t>(std::max<int64_t>(1, (int64_t)nsm * 4 / nbi), std::max<int64_t>(1, L / 64));
+    h.lchunk = (int32_t)((L + nch - 1) / nch);
+    h.nchunk = (int32_t)((L + h.lchunk - 1) / h.lchunk);
+    Carve cv{nullptr};
+    cv.take<DevChain>(1);
+    cv.take<float>(L * 4 * h.kp);
+    cv.take<double>((int64_t)h.nchunk * N * K);
+    pl->scratch = cv.off + 256;
+    return VP_OK;
+}
+
+// run the likelihood stream with the given scratch (device memory, plan size)
+int ll_run(LLPlan& pl, const uint32_t* geno, const float* freq, double* ll, void* scratch, cudaStream_t s) {
+    DevChain h = pl.h;
+    Carve cv{(char*)(((uintptr_t)scratch + 255) & ~(uintptr_t)255)};
+    DevChain* d = cv.take<DevChain>(1);
+    h.lt = cv.take<float>(h.D.L * 4 * h.kp);
+    h.LLp = cv.take<double>((int64_t)h.nchunk * h.D.N * h.K);
+    h.D.g2 = geno;
+    CK(cudaMemcpyAsync(d, &h, sizeof(DevChain), cudaMemcpyHostToDevice, s));
+    k_lt_from_freq<<<cdiv((int64_t)h.K * h.D.L, 256), 256, 0, s>>>(freq, h.K, h.D.L, h.kp, h.lt);
+    dim3 g(cdiv(h.D.N, LL_BLOCK), h.nchunk, pl.kgroups);
+    switch (pl.kc) {
+        case 4: k_loglik<4><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+        case 8: k_loglik<8><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+        default: k_loglik<16><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+    }
+    k_ll_reduce<<<std::min<unsigned>(1024, cdiv((int64_t)h.D.N * h.K, 256)), 256, 0, s>>>(d, ll);
+    CK(cudaGetLastError());
+    return VP_OK;
+}
+
+int device_sms() {
+    int dev = 0, n = 132;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n;
+}
+
+}  // namespace
+
+extern "C" int vp_loglik_packed2(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const float* freq, int32_t K,
+                                 double* ll, void* stream) {
+    if (!geno || !freq || !ll) { vp_set_error("loglik: null pointer"); return VP_E_ARG; }
+    LLPlan pl;
+    int rc = ll_plan(n_ind, n_loc, K, device_sms(), &pl);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    void* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, pl.scratch, s);
+    if (e != cudaSuccess) { vp_set_error("loglik scratch (%zu bytes): %s", pl.scratch, cudaGetErrorString(e)); return VP_E_MEM; }
+    rc = ll_run(pl, geno, freq, ll, scratch, s);
+    cudaFreeAsync(scratch, s);
+    return rc;
+}
