@@ -189,6 +189,19 @@ int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1
 int vp_loglik_packed2(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const float* freq, int32_t K,
                       double* ll, void* stream);
 
+/* vp_loglik_packed2 without any device allocation, for callers that may not
+ * allocate device memory (a host framework that owns the whole device budget,
+ * a plugin whose host forbids allocation on its hot path). No counterpart in
+ * the reference: it is an addition of this library.
+ * Scratch comes from one fixed array of VP_LOGLIK_NOALLOC_MAX_BYTES (32 MiB)
+ * compiled into the library and held on every GPU that loads it until exit;
+ * sizes whose table and partial sums need more are rejected with VP_E_ARG.
+ * The first call on a device looks the array's device address up (once per
+ * device, with that device current); make that first call before any stream
+ * capture. All calls share the array: calls that overlap on the GPU race. */
+int vp_loglik_packed2_noalloc(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const float* freq, int32_t K,
+                              double* ll, void* stream);
+
 /* The CUDA stream (cudaStream_t) every launch of this context goes to. */
 void* vp_stream(vp_ctx* ctx);
 /* Record CUDA events around each launch of the sweep's dominant kernel (the

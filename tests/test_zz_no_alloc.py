@@ -1,0 +1,57 @@
+"""The allocation-free likelihood call, for callers that may not allocate
+device memory (a host framework owning the whole device budget, or a plugin
+whose host forbids allocation on its hot path).
+
+It must give what the allocating call gives, on two calls in a row (the second
+call reuses the fixed scratch array the first one filled), and refuse sizes
+whose scratch would not fit in that array. This file is collected last so that
+a run stopping at the first failure has already run every other test.
+"""
+import numpy as np
+import pytest
+
+from vcfpop_gb300 import _lib as B
+from vcfpop_gb300 import structure as S
+from vcfpop_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5  # the likelihood tolerance used by the parity tests
+
+
+def _inputs(seed, N, L, K):
+    import torch
+    d = synth.fmodel(seed, N, L, 4, 0.1, 0.03)
+    packed = S.pack2(d["G"])
+    p = np.random.default_rng(seed).dirichlet([1.0, 1.0], size=(K, L)).astype(np.float32)
+    g = torch.from_numpy(packed.view(np.int32)).cuda()
+    f = torch.from_numpy(p.reshape(K, 2 * L)).cuda()
+    return g, f
+
+
+def _call(fn, g, f, N, L, K):
+    import torch
+    out = torch.full((N, K), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    B.check(fn(g.data_ptr(), N, L, f.data_ptr(), K, out.data_ptr(), None))
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def test_noalloc_matches_allocating_call_twice():
+    lib = B.lib()
+    for seed, (N, L, K) in [(1, (700, 3000, 5)), (2, (1500, 2200, 11))]:
+        g, f = _inputs(seed, N, L, K)
+        want = _call(lib.vp_loglik_packed2, g, f, N, L, K)
+        got = _call(lib.vp_loglik_packed2_noalloc, g, f, N, L, K)
+        assert np.isfinite(got).all()
+        rel = np.abs(got - want) / np.abs(want)
+        assert rel.max() < REL, rel.max()
+
+
+def test_noalloc_rejects_oversized_problems():
+    import torch
+    N, L, K = 20000, 400000, 12  # table + partial sums far beyond the fixed array
+    dummy = torch.zeros(16, dtype=torch.int32, device="cuda")
+    with pytest.raises(B.VpError, match="fixed array"):
+        B.check(B.lib().vp_loglik_packed2_noalloc(dummy.data_ptr(), N, L, dummy.data_ptr(), K, dummy.data_ptr(), None))

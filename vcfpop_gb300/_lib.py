@@ -63,7 +63,8 @@ _lib = None
 EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_dataset_free", "vp_open",
            "vp_close", "vp_sync", "vp_params_default", "vp_run_seed", "vp_chain_create", "vp_chain_destroy",
            "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_step", "vp_chain_get",
-           "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2"]
+           "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
+           "vp_loglik_packed2_noalloc"]
 
 
 def lib():
@@ -107,6 +108,7 @@ def lib():
     L.vp_prof_enable.argtypes = [P, C.c_int]
     L.vp_prof_read.argtypes = [P, P, P]
     L.vp_loglik_packed2.argtypes = [P, C.c_int32, C.c_int64, P, C.c_int32, P, P]
+    L.vp_loglik_packed2_noalloc.argtypes = [P, C.c_int32, C.c_int64, P, C.c_int32, P, P]
     _lib = L
     return L
 

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "vp_internal.h"
@@ -1127,4 +1128,61 @@ extern "C" int vp_loglik_packed2(const uint32_t* geno, int32_t n_ind, int64_t n_
     rc = ll_run(pl, geno, freq, ll, scratch, s);
     cudaFreeAsync(scratch, s);
     return rc;
+}
+
+// ===================== allocation-free likelihood call =====================
+// Some callers may not allocate device memory at all: for example a host
+// framework that has reserved the whole device budget up front and hands out
+// only the buffers it owns, or a plugin whose host forbids allocation on its
+// hot path. For them this variant of vp_loglik_packed2 takes its scratch (the
+// per-genotype table and the per-chunk partial sums) from one fixed array in
+// device memory, compiled into the library, instead of allocating.
+//
+// The array is VP_LOGLIK_NOALLOC_MAX_BYTES long and is held by every GPU that
+// loads the library until the process exits. All calls on a device share it
+// and it keeps whatever the previous call left there; every call writes the
+// parts it reads before reading them, so nothing has to start at zero. Calls
+// whose work overlaps on the GPU (issued on different streams without
+// ordering between them) race on the array.
+namespace {
+#define VP_LOGLIK_NOALLOC_MAX_BYTES (32u << 20)
+static __device__ __align__(256) unsigned char g_loglik_scratch[VP_LOGLIK_NOALLOC_MAX_BYTES];
+
+// Device address of the array on each device. Host code cannot use the
+// array's name as a device address, so the address is looked up once per
+// device with that device current.
+void* g_loglik_scratch_addr[64];
+std::mutex g_loglik_scratch_mu;
+
+int loglik_scratch_addr(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { vp_set_error("cudaGetDevice: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+    if (dev < 0 || dev >= 64) { vp_set_error("device ordinal %d out of range", dev); return VP_E_ARG; }
+    std::lock_guard<std::mutex> lk(g_loglik_scratch_mu);
+    if (!g_loglik_scratch_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_loglik_scratch);
+        if (e != cudaSuccess) { vp_set_error("cudaGetSymbolAddress: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+        g_loglik_scratch_addr[dev] = p;
+    }
+    *out = g_loglik_scratch_addr[dev];
+    return VP_OK;
+}
+}  // namespace
+
+extern "C" int vp_loglik_packed2_noalloc(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const float* freq,
+                                         int32_t K, double* ll, void* stream) {
+    if (!geno || !freq || !ll) { vp_set_error("loglik (no-alloc): null pointer"); return VP_E_ARG; }
+    LLPlan pl;
+    int rc = ll_plan(n_ind, n_loc, K, device_sms(), &pl);
+    if (rc) return rc;
+    if (pl.scratch > VP_LOGLIK_NOALLOC_MAX_BYTES) {
+        vp_set_error("loglik (no-alloc): N=%d, L=%lld, K=%d needs %zu bytes of scratch; the fixed array holds %u",
+                     n_ind, (long long)n_loc, K, pl.scratch, VP_LOGLIK_NOALLOC_MAX_BYTES);
+        return VP_E_ARG;
+    }
+    void* scratch = nullptr;
+    if ((rc = loglik_scratch_addr(&scratch))) return rc;
+    return ll_run(pl, geno, freq, ll, scratch, (cudaStream_t)stream);
 }
