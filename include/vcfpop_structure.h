@@ -173,9 +173,10 @@ int vp_tc_status(vp_ctx* ctx);
 /* Diagnostic: D[s][m][n] = sum over this split's k of A[m,k] (B0[n,k] + B1[n,k])
  * through the tensor-core kernel. A [M][K], B0/B1 [N][K] bf16 bit patterns,
  * K % 64 == 0, N % BN == 0, BN % piece == 0, piece % 16 == 0, piece <= 256,
- * BN <= 512; B1 may be NULL. D receives splits*M*N floats. */
+ * mt (128-row A tiles per CTA) 1 or 2, BN * mt <= 512; B1 may be NULL.
+ * D receives splits*M*N floats. */
 int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N, int32_t K,
-                       int32_t BN, int32_t piece, int32_t splits, int32_t stages, float* D);
+                       int32_t BN, int32_t piece, int32_t splits, int32_t stages, int32_t mt, float* D);
 
 /* The likelihood accumulation of UpdateQNoAdmix (src/structure.cpp:902-932;
  * the part BAYESIAN<REAL>::UpdateQNoAdmixCUDA offloads, src/structureCUDA.cpp:

@@ -102,7 +102,7 @@ def lib():
     L.vp_launch_count.restype = C.c_int64
     L.vp_last_error.restype = C.c_char_p
     L.vp_tc_status.argtypes = [P]
-    L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 7 + [P]
+    L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 8 + [P]
     L.vp_stream.argtypes = [P]
     L.vp_stream.restype = P
     L.vp_prof_enable.argtypes = [P, C.c_int]

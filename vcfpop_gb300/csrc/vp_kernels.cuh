@@ -508,12 +508,24 @@ __global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevCha
         for (int j = 0; j < 2 * K; ++j) h[j * 32 + lane] = 0;
         if (l < D.L) {
             const uint32_t* row = D.g2 + l * D.Nw;
-            for (int i = lane; i < D.N; i += 32) {
-                int code = (__ldg(row + (i >> 4)) >> ((i & 15) * 2)) & 3;
-                if (code == 3) continue;
-                int z = c.Z[i];
-                h[(z * 2) * 32 + lane] += 2 - code;
-                h[(z * 2 + 1) * 32 + lane] += code;
+            // four independent loads in flight per lane
+            for (int i0 = lane; i0 < D.N; i0 += 128) {
+                uint32_t w[4];
+                int z[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int i = i0 + 32 * u;
+                    w[u] = i < D.N ? __ldg(row + (i >> 4)) : 0xFFFFFFFFu;
+                    z[u] = i < D.N ? (int)c.Z[i] : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int i = i0 + 32 * u;
+                    const int code = (w[u] >> ((i & 15) * 2)) & 3;
+                    if (code == 3) continue;
+                    h[(z[u] * 2) * 32 + lane] += 2 - code;
+                    h[(z[u] * 2 + 1) * 32 + lane] += code;
+                }
             }
             const int64_t o = D.off[l];
             for (int j = 0; j < 2 * K; ++j) {

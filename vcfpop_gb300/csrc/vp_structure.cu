@@ -66,7 +66,7 @@ struct TcBatch {
     void* mem = nullptr;
     DevChain* dchains = nullptr;
     int32_t *rowchain = nullptr, *rowk = nullptr, *row0 = nullptr;
-    int R = 0, Rpad = 0, G = 0, BN = 288, piece = 144, splits = 1;
+    int R = 0, Rpad = 0, G = 0, BN = 192, piece = 192, splits = 1;
     __nv_bfloat16 *Whi = nullptr, *Wlo = nullptr, *OH = nullptr;
     float* LLpart = nullptr;
     int32_t* NiAll = nullptr;
@@ -725,7 +725,7 @@ int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uin
 
 int launch_gemm(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CUtensorMap& B1, tc::GemmArgs g,
                 dim3 grid) {
-    size_t sm = tc::gemm_smem_bytes(g.BN, g.nb, g.stages);
+    size_t sm = tc::gemm_smem_bytes(g.BN, g.nb, g.stages, g.mt);
     static bool attr = false;
     if (!attr) {
         CK(cudaFuncSetAttribute(tc::k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
@@ -826,7 +826,7 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
     b->G = (b->R + b->BN - 1) / b->BN;
     b->Rpad = b->G * b->BN;
     const TcOperands& t = x->tc;
-    const int64_t tiles = (t.Npad / 128) * b->G;
+    const int64_t tiles = ((t.Npad + 255) / 256) * b->G;
     b->splits = tc_splits(tiles, x->nsm);
     const int64_t kblocks = t.Apad / 64;
     b->splits = (int)std::min<int64_t>(b->splits, kblocks);
@@ -891,10 +891,10 @@ int launch_tc_sweep(vp_ctx* x) {
         tc::GemmArgs g{};
         g.M = x->N; g.N = b->Rpad; g.kblocks = (int)(t.Apad / 64);
         g.kb_per_split = (g.kblocks + b->splits - 1) / b->splits;
-        g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.stages = 2; g.mode = 0;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.mt = 2; g.stages = 2; g.mode = 0;
         g.out_f = b->LLpart; g.ldo = b->Rpad; g.err = t.err;
         prof_mark(x, true);
-        int rc = launch_gemm(x, t.mapC, b->mapWhi, b->mapWlo, g, dim3((unsigned)(t.Npad / 128), b->G, b->splits));
+        int rc = launch_gemm(x, t.mapC, b->mapWhi, b->mapWlo, g, dim3(cdiv(t.Npad, 256), b->G, b->splits));
         prof_mark(x, false);
         if (rc) return rc;
     }
@@ -904,9 +904,9 @@ int launch_tc_sweep(vp_ctx* x) {
     {
         tc::GemmArgs g{};
         g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / 64); g.kb_per_split = g.kblocks;
-        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.stages = 4; g.mode = 1;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.mt = 2; g.stages = 3; g.mode = 1;
         g.out_i = b->NiAll; g.ldo = x->KT; g.err = t.err;
-        int rc = launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, dim3((unsigned)(t.Apad / 128), b->G, 1));
+        int rc = launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, dim3(cdiv(t.Apad, 256), b->G, 1));
         if (rc) return rc;
     }
     // Record for every chain, then m += 1
@@ -955,15 +955,16 @@ extern "C" int vp_tc_status(vp_ctx* x) {
 }
 
 extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N,
-                                  int32_t K, int32_t BN, int32_t piece, int32_t splits, int32_t stages, float* D) {
+                                  int32_t K, int32_t BN, int32_t piece, int32_t splits, int32_t stages, int32_t mt,
+                                  float* D) {
     if (!A || !B0 || !D || M <= 0 || N <= 0 || K <= 0 || K % 64 || N % BN || BN % piece || piece % 16 || piece > 256 ||
-        BN > 512 || splits < 1) {
+        (mt != 1 && mt != 2) || BN * mt > 512 || splits < 1) {
         vp_set_error("vp_debug_gemm_bf16: bad shape");
         return VP_E_ARG;
     }
     vp_ctx tmp;
     cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking);
-    const int64_t Mp = (M + 127) / 128 * 128;
+    const int64_t Mp = (M + 128 * mt - 1) / (128 * mt) * (128 * mt);
     void *dA, *dB0, *dB1 = nullptr, *dD;
     int* err;
     CK(cudaMalloc(&dA, (size_t)Mp * K * 2));
@@ -985,9 +986,9 @@ extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const u
     if (!rc) {
         tc::GemmArgs g{};
         g.M = M; g.N = N; g.kblocks = K / 64; g.kb_per_split = (g.kblocks + splits - 1) / splits;
-        g.BN = BN; g.piece = piece; g.nb = B1 ? 2 : 1; g.stages = stages; g.mode = 0;
+        g.BN = BN; g.piece = piece; g.nb = B1 ? 2 : 1; g.mt = mt; g.stages = stages; g.mode = 0;
         g.out_f = (float*)dD; g.ldo = N; g.err = err;
-        rc = launch_gemm(&tmp, ma, mb0, mb1, g, dim3((unsigned)(Mp / 128), N / BN, splits));
+        rc = launch_gemm(&tmp, ma, mb0, mb1, g, dim3((unsigned)(Mp / (128 * mt)), N / BN, splits));
     }
     int e = 0;
     if (!rc) {

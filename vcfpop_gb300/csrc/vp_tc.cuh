@@ -34,6 +34,7 @@ struct GemmArgs {
     int BN;                 // columns per CTA (multiple of 16, <= 512)
     int piece;              // columns per MMA instruction (<= 256, multiple of 16)
     int nb;                 // 1 or 2 B operands
+    int mt;                 // 128-row A tiles per CTA sharing the B tile (1 or 2)
     int stages;
     int mode;               // 0: FP32 partials D[z][m][n]; 1: int32 transpose Dt[n][m] (no split)
     float* out_f;           // mode 0: [splits][M][ldo]
@@ -122,7 +123,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t a_bytes = BM * BK * 2;
+    const uint32_t a_tile = BM * BK * 2;
+    const uint32_t a_bytes = a_tile * g.mt;
     const uint32_t b_bytes = (uint32_t)g.BN * BK * 2;
     const uint32_t stage_bytes = a_bytes + b_bytes * g.nb;
     uint64_t* full = (uint64_t*)(smem + (size_t)stage_bytes * g.stages);
@@ -131,13 +133,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     uint32_t* tmem_holder = (uint32_t*)(accum + 1);
     int* abort_flag = (int*)(tmem_holder + 1);
 
-    const int m0 = blockIdx.x * BM;
+    const int m0 = blockIdx.x * BM * g.mt;
     const int n0 = blockIdx.y * g.BN;
     const int kb0 = blockIdx.z * g.kb_per_split;
     const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
     const int nk = kb1 - kb0;
     uint32_t ncols = 32;
-    while ((int)ncols < g.BN) ncols <<= 1;
+    while ((int)ncols < g.BN * g.mt) ncols <<= 1;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < g.stages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 unsigned char* st = smem + (size_t)s * stage_bytes;
                 mbar_expect_tx(&full[s], stage_bytes);
                 const int kx = (kb0 + it) * BK;
-                tma_load_2d(st, &mapA, &full[s], kx, m0);
+                for (int t = 0; t < g.mt; ++t) tma_load_2d(st + (size_t)t * a_tile, &mapA, &full[s], kx, m0 + t * BM);
                 for (int b = 0; b < g.nb; ++b) {
                     unsigned char* bt = st + a_bytes + (size_t)b * b_bytes;
                     const CUtensorMap* mb = b == 0 ? &mapB0 : &mapB1;
@@ -198,17 +200,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 unsigned char* st = smem + (size_t)s * stage_bytes;
                 const uint32_t abase = smem_u32(st);
-                for (int kk = 0; kk < BK / 16; ++kk) {
-                    const uint64_t ad = sw128_desc(abase + kk * 32);
-                    for (int b = 0; b < g.nb; ++b) {
-                        const uint32_t bbase = smem_u32(st + a_bytes + (size_t)b * b_bytes);
-                        for (int p = 0; p < g.BN; p += g.piece) {
-                            const int n = min(g.piece, g.BN - p);
-                            const uint64_t bd = sw128_desc(bbase + (uint32_t)p * BK * 2 + kk * 32);
-                            mma_bf16(tmem + (uint32_t)p, ad, bd, idesc_bf16(n), (it | kk | b) != 0);
+                for (int kk = 0; kk < BK / 16; ++kk)
+                    for (int t = 0; t < g.mt; ++t) {
+                        const uint64_t ad = sw128_desc(abase + t * a_tile + kk * 32);
+                        for (int b = 0; b < g.nb; ++b) {
+                            const uint32_t bbase = smem_u32(st + a_bytes + (size_t)b * b_bytes);
+                            for (int p = 0; p < g.BN; p += g.piece) {
+                                const int n = min(g.piece, g.BN - p);
+                                const uint64_t bd = sw128_desc(bbase + (uint32_t)p * BK * 2 + kk * 32);
+                                mma_bf16(tmem + (uint32_t)(t * g.BN + p), ad, bd, idesc_bf16(n), (it | kk | b) != 0);
+                            }
                         }
                     }
-                }
                 mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
             }
             // also on the error path: the commit arrives only once every MMA this
@@ -225,23 +228,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const bool valid = got && !*(volatile int*)abort_flag && nk > 0;
         if (!got) atomicExch(g.err, 3);
-        const int row = m0 + q * 32 + lane;
-        for (int c0 = 0; c0 < g.BN; c0 += 16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-            if (!valid) continue;
-            if (g.mode == 0) {
-                if (row < g.M) {
-                    float* o = g.out_f + ((int64_t)blockIdx.z * g.M + row) * g.ldo + n0 + c0;
+        for (int t = 0; t < g.mt; ++t) {
+            const int row = m0 + t * BM + q * 32 + lane;
+            for (int c0 = 0; c0 < g.BN; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(t * g.BN + c0), v);
+                if (!valid) continue;
+                if (g.mode == 0) {
+                    if (row < g.M) {
+                        float* o = g.out_f + ((int64_t)blockIdx.z * g.M + row) * g.ldo + n0 + c0;
 #pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        if (n0 + c0 + j < g.N) o[j] = v[j];
+                        for (int j = 0; j < 16; ++j)
+                            if (n0 + c0 + j < g.N) o[j] = v[j];
+                    }
+                } else {
+                    if (row < g.M)
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            if (n0 + c0 + j < g.N) g.out_i[(int64_t)(n0 + c0 + j) * g.ldo + row] = __float2int_rn(v[j]);
                 }
-            } else {
-                if (row < g.M)
-#pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        if (n0 + c0 + j < g.N) g.out_i[(int64_t)(n0 + c0 + j) * g.ldo + row] = __float2int_rn(v[j]);
             }
         }
     }
@@ -253,8 +258,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
 }
 
-inline size_t gemm_smem_bytes(int BN, int nb, int stages) {
-    size_t st = (size_t)BM * BK * 2 + (size_t)BN * BK * 2 * nb;
+inline size_t gemm_smem_bytes(int BN, int nb, int stages, int mt = 1) {
+    size_t st = (size_t)BM * BK * 2 * mt + (size_t)BN * BK * 2 * nb;
     return st * stages + 1024 /*align slack*/ + 256 /*barriers*/;
 }
 
