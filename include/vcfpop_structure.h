@@ -172,11 +172,20 @@ int vp_tc_status(vp_ctx* ctx);
 
 /* Diagnostic: D[s][m][n] = sum over this split's k of A[m,k] (B0[n,k] + B1[n,k])
  * through the tensor-core kernel. A [M][K], B0/B1 [N][K] bf16 bit patterns,
- * K % 64 == 0, N % BN == 0, BN % piece == 0, piece % 16 == 0, piece <= 256,
- * mt (128-row A tiles per CTA) 1 or 2, BN * mt <= 512; B1 may be NULL.
- * D receives splits*M*N floats. */
+ * bk (K elements per pipeline stage) 32 or 64, K % bk == 0, N % BN == 0,
+ * BN % piece == 0, piece % 16 == 0, piece <= 256, mt (128-row A tiles per
+ * CTA) 1 or 2, BN * mt <= 512; B1 may be NULL. D receives splits*M*N floats.
+ * No reference counterpart (a test hook for the contraction kernel). */
 int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N, int32_t K,
-                       int32_t BN, int32_t piece, int32_t splits, int32_t stages, int32_t mt, float* D);
+                       int32_t BN, int32_t piece, int32_t splits, int32_t stages, int32_t mt, int32_t bk, float* D);
+
+/* Diagnostic: average device time in ms of `iters` launches of the
+ * contraction kernel on operands it allocates and fills itself (nb B operands;
+ * mode 0 FP32 partials [splits][M][N], mode 1 int32 transpose [N][M] with
+ * splits == 1). Shape rules as vp_debug_gemm_bf16. Used to choose tile and
+ * pipeline parameters; no reference counterpart. */
+int vp_debug_gemm_time(int32_t M, int32_t N, int32_t K, int32_t BN, int32_t piece, int32_t splits, int32_t stages,
+                       int32_t mt, int32_t bk, int32_t nb, int32_t mode, int32_t iters, double* ms);
 
 /* The likelihood accumulation of UpdateQNoAdmix (src/structure.cpp:902-932;
  * the part BAYESIAN<REAL>::UpdateQNoAdmixCUDA offloads, src/structureCUDA.cpp:
@@ -211,6 +220,50 @@ void* vp_stream(vp_ctx* ctx);
 int vp_prof_enable(vp_ctx* ctx, int on);
 /* Synchronise, then sum the dominant-kernel durations of the last sweep. */
 int vp_prof_read(vp_ctx* ctx, double* ms, int32_t* launches);
+
+/* ---- serving: many independent runs on one device ------------------------
+ * Replaces the reference's run scheduling (BAYESIAN<REAL>::CalcBayesian and
+ * BayesianThread, src/structure.cpp:2337-2501, with ManageCUDA's device
+ * slotting, src/structure.cpp:710-756), where each run owns one host thread
+ * and one device slot for its whole length.
+ * A server owns one scheduler thread on one device. Submitted runs queue in
+ * arrival order and start when their device bytes (dataset upload plus chain
+ * state) fit under mem_budget and fewer than max_active runs are active; each
+ * active run has its own context and stream, and the scheduler keeps up to
+ * two chunks of `chunk` sweeps queued per run, so runs of every size overlap
+ * on the GPU. Results stay on the device until the run is released.
+ * The dataset passed to vp_submit must stay alive until the run is done. */
+typedef struct vp_server vp_server;
+#define VP_REQ_QUEUED 0
+#define VP_REQ_RUNNING 1
+#define VP_REQ_DONE 2
+#define VP_REQ_FAILED 3
+typedef struct {
+    int32_t state;            /* VP_REQ_* */
+    int32_t rc;               /* status of a failed run */
+    int64_t sweeps_issued, sweeps_total;
+    int64_t device_bytes;     /* bytes the run holds (or will hold) on the device */
+    double t_submit, t_start, t_done;   /* seconds since vp_server_open */
+    char error[256];
+} vp_request_info;
+/* mem_budget 0 = 90% of the device's free memory at open; max_active 0 = 64;
+ * chunk 0 = 16 sweeps. */
+int vp_server_open(int device, int64_t mem_budget, int32_t max_active, int32_t chunk, vp_server** out);
+/* Queue one run (a chain of p on ds); *id identifies it. A run that could
+ * never fit under the budget is rejected with VP_E_MEM. */
+int vp_submit(vp_server* s, const vp_dataset* ds, const vp_params* p, int64_t* id);
+/* Non-blocking state of a run. */
+int vp_poll(vp_server* s, int64_t id, vp_request_info* info);
+/* Wait until the run is done or failed, at most timeout_s seconds (< 0: no
+ * limit); returns VP_E_STATE on time-out. */
+int vp_wait(vp_server* s, int64_t id, double timeout_s, vp_request_info* info);
+/* The finished run's chain, for vp_chain_sizes / vp_chain_result /
+ * vp_chain_get; valid until vp_release. */
+int vp_request_chain(vp_server* s, int64_t id, vp_chain** chain);
+/* Free a finished run's device memory and forget it. */
+int vp_release(vp_server* s, int64_t id);
+/* Stop the scheduler (active runs are abandoned) and free everything. */
+int vp_server_close(vp_server* s);
 
 /* Kernel launches issued by this library since the context was opened. */
 int64_t vp_launch_count(vp_ctx* ctx);

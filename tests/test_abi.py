@@ -87,3 +87,11 @@ def test_pack2_roundtrip():
             code = (int(P[l, i // 16]) >> (2 * (i % 16))) & 3
             g = d["G"][l, i]
             assert code == (3 if g[0] < 0 else int(g[0]) + int(g[1]))
+
+
+def test_server_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    with pytest.raises(B.VpError, match="no CUDA device"):
+        S.Server()

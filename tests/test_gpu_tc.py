@@ -22,29 +22,34 @@ def bf16_val(b):
     return (b.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
 
 
-def gemm(A, B0, B1, BN, piece, splits=1, stages=2, mt=1):
+def gemm(A, B0, B1, BN, piece, splits=1, stages=2, mt=1, bk=64):
     M, K = A.shape
     N = B0.shape[0]
     D = np.zeros((splits, M, N), np.float32)
     B.check(B.lib().vp_debug_gemm_bf16(A.ctypes.data, B0.ctypes.data, None if B1 is None else B1.ctypes.data,
-                                       M, N, K, BN, piece, splits, stages, mt, D.ctypes.data))
+                                       M, N, K, BN, piece, splits, stages, mt, bk, D.ctypes.data))
     return D.astype(np.float64).sum(0)
 
 
-@pytest.mark.parametrize("M,N,K,BN,piece,nb,splits,stages,mt", [
-    (128, 144, 64, 144, 144, 1, 1, 2, 1),
-    (256, 288, 512, 288, 144, 2, 1, 2, 1),
-    (200, 576, 1024, 288, 144, 2, 3, 2, 1),
-    (384, 288, 640, 288, 144, 1, 1, 4, 1),
-    (300, 384, 768, 192, 192, 2, 2, 2, 2),
-    (640, 192, 1024, 192, 192, 1, 1, 3, 2),
+# every tile shape compiled into the library, ragged M, split K, a K shorter
+# than the pipeline
+@pytest.mark.parametrize("M,N,K,BN,piece,nb,splits,stages,mt,bk", [
+    (300, 384, 768, 192, 192, 2, 2, 2, 2, 64),
+    (200, 576, 1024, 192, 192, 2, 3, 2, 2, 64),
+    (640, 192, 1024, 192, 192, 1, 1, 3, 2, 64),
+    (100, 192, 64, 192, 192, 1, 1, 3, 2, 64),
+    (256, 576, 512, 288, 144, 2, 1, 2, 1, 64),
+    (200, 576, 1024, 288, 144, 2, 3, 2, 1, 64),
+    (128, 256, 64, 256, 256, 1, 1, 2, 1, 64),
+    (384, 512, 640, 256, 256, 1, 1, 4, 1, 64),
+    (300, 384, 800, 192, 192, 2, 3, 5, 2, 32),
 ])
-def test_gemm_matches_float64(M, N, K, BN, piece, nb, splits, stages, mt):
-    rng = np.random.default_rng(M + N + K)
+def test_gemm_matches_float64(M, N, K, BN, piece, nb, splits, stages, mt, bk):
+    rng = np.random.default_rng(M + N + K + bk)
     A = bf16_bits(rng.integers(0, 3, (M, K)).astype(np.float32))       # allele counts 0..2
     B0 = bf16_bits(rng.normal(0, 1, (N, K)).astype(np.float32))
     B1 = bf16_bits(rng.normal(0, 1e-3, (N, K)).astype(np.float32)) if nb == 2 else None
-    D = gemm(A, B0, B1, BN, piece, splits, stages, mt)
+    D = gemm(A, B0, B1, BN, piece, splits, stages, mt, bk)
     Bsum = bf16_val(B0) + (bf16_val(B1) if B1 is not None else 0)
     ref = bf16_val(A) @ Bsum.T
     err = np.abs(D - ref).max() / max(1.0, np.abs(ref).max())

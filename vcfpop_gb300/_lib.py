@@ -53,6 +53,15 @@ class VpResult(C.Structure):
                 ("freqm", C.c_void_p)]
 
 
+class VpRequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("rc", C.c_int32), ("sweeps_issued", C.c_int64), ("sweeps_total", C.c_int64),
+                ("device_bytes", C.c_int64), ("t_submit", C.c_double), ("t_start", C.c_double),
+                ("t_done", C.c_double), ("error", C.c_char * 256)]
+
+
+VP_REQ_QUEUED, VP_REQ_RUNNING, VP_REQ_DONE, VP_REQ_FAILED = 0, 1, 2, 3
+
+
 class VpError(RuntimeError):
     pass
 
@@ -63,8 +72,9 @@ _lib = None
 EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_dataset_free", "vp_open",
            "vp_close", "vp_sync", "vp_params_default", "vp_run_seed", "vp_chain_create", "vp_chain_destroy",
            "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_step", "vp_chain_get",
-           "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
-           "vp_loglik_packed2_noalloc"]
+           "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
+           "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
+           "vp_release", "vp_server_close"]
 
 
 def lib():
@@ -102,13 +112,21 @@ def lib():
     L.vp_launch_count.restype = C.c_int64
     L.vp_last_error.restype = C.c_char_p
     L.vp_tc_status.argtypes = [P]
-    L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 8 + [P]
+    L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 9 + [P]
+    L.vp_debug_gemm_time.argtypes = [C.c_int32] * 12 + [P]
     L.vp_stream.argtypes = [P]
     L.vp_stream.restype = P
     L.vp_prof_enable.argtypes = [P, C.c_int]
     L.vp_prof_read.argtypes = [P, P, P]
     L.vp_loglik_packed2.argtypes = [P, C.c_int32, C.c_int64, P, C.c_int32, P, P]
     L.vp_loglik_packed2_noalloc.argtypes = [P, C.c_int32, C.c_int64, P, C.c_int32, P, P]
+    L.vp_server_open.argtypes = [C.c_int, C.c_int64, C.c_int32, C.c_int32, C.POINTER(P)]
+    L.vp_submit.argtypes = [P, P, C.POINTER(VpParams), C.POINTER(C.c_int64)]
+    L.vp_poll.argtypes = [P, C.c_int64, C.POINTER(VpRequestInfo)]
+    L.vp_wait.argtypes = [P, C.c_int64, C.c_double, C.POINTER(VpRequestInfo)]
+    L.vp_request_chain.argtypes = [P, C.c_int64, C.POINTER(P)]
+    L.vp_release.argtypes = [P, C.c_int64]
+    L.vp_server_close.argtypes = [P]
     _lib = L
     return L
 

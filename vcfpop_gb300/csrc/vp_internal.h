@@ -43,3 +43,11 @@ struct vp_dataset {
 };
 
 void vp_set_error(const char* fmt, ...);
+
+// device bytes a request (its context's uploads plus one chain) will hold;
+// -1 when the parameters are invalid
+int64_t vp_request_bytes(const vp_dataset* ds, const vp_params* P, int nsm);
+// vp_finish without the final wait
+int vp_finish_issue(vp_chain** cs, int32_t n);
+// sweeps issued so far and in total for one chain
+void vp_chain_progress(const vp_chain* c, int64_t* issued, int64_t* total);

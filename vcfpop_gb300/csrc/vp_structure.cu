@@ -14,6 +14,7 @@ using namespace vp;
 
 struct TcOperands {
     bool ready = false;
+    int bk = 64;              // K elements per pipeline stage of both contractions
     int64_t Apad = 0, Npad = 0;
     __nv_bfloat16 *C = nullptr, *CT = nullptr;
     float* logpbar = nullptr;
@@ -67,6 +68,9 @@ struct TcBatch {
     DevChain* dchains = nullptr;
     int32_t *rowchain = nullptr, *rowk = nullptr, *row0 = nullptr;
     int R = 0, Rpad = 0, G = 0, BN = 192, piece = 192, splits = 1;
+    // pipeline of the likelihood (1) and count (2) contractions: 128-row A
+    // tiles per CTA and shared-memory stages of bk K elements
+    int mt1 = 2, st1 = 2, mt2 = 2, st2 = 4;
     __nv_bfloat16 *Whi = nullptr, *Wlo = nullptr, *OH = nullptr;
     float* LLpart = nullptr;
     int32_t* NiAll = nullptr;
@@ -346,16 +350,57 @@ extern "C" int vp_sync(vp_ctx* x) {
 
 extern "C" int64_t vp_launch_count(vp_ctx* x) { return x ? x->launches : -1; }
 
-extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
-    if (!x || !P || !out) { vp_set_error("null argument"); return VP_E_ARG; }
-    if (P->K < 1 || P->K > 64) { vp_set_error("K must be in 1..64"); return VP_E_ARG; }
-    if (P->nthinning < 1 || P->nburnin < 0 || P->nreps < 0) { vp_set_error("bad MCMC lengths"); return VP_E_ARG; }
-    cudaSetDevice(x->device);
-    auto* c = new vp_chain();
-    c->ctx = x;
-    c->P = *P;
+namespace {
+// device layout of one chain's state inside its single allocation
+void chain_layout(Carve& cv, vp_chain* c, const vp_ctx* x) {
+    DevChain& h = c->h;
+    const vp_params* P = &c->P;
     const int K = P->K, N = x->N, S = x->S;
     const int64_t L = x->L, KT = x->KT;
+    const int64_t ntrace = h.nburnin / h.nthinning + h.nreps / h.nthinning + 2;
+    const int64_t ltn = x->packed2 ? L * 4 * h.kp : (int64_t)K * KT;
+    h.ctl = cv.take<Ctl>(1);
+    h.rstate = cv.take<Rng64>(1);
+    h.Freq = cv.take<float>(K * KT);
+    h.FreqM = cv.take<float>(K * KT);
+    h.FreqA = cv.take<float>(P->fmodel ? KT : 1);
+    h.lt = cv.take<float>(ltn);
+    h.Q = cv.take<float>((int64_t)N * K);
+    h.Qprop = cv.take<float>((int64_t)N * K);
+    h.Di = cv.take<float>((int64_t)S * K);
+    h.fbuf = cv.take<float>(64 * (x->maxK + 16));
+    h.Z = cv.take<uint16_t>(N + 32);
+    h.Mi = cv.take<int32_t>((int64_t)N * K);
+    h.Ni = cv.take<int32_t>(K * KT);
+    h.MiSum = cv.take<int64_t>((int64_t)N * K);
+    h.LLp = cv.take<double>((int64_t)h.nchunk * N * K);
+    h.LL = cv.take<double>((int64_t)N * K);
+    h.metro = cv.take<double>(N);
+    h.metrop = cv.take<double>((int64_t)h.nchunk * N);
+    h.Alpha = cv.take<double>(K);
+    h.Lambda = cv.take<double>(K);
+    h.f = cv.take<double>(K);
+    h.F = cv.take<double>(K);
+    h.Eta = cv.take<double>(K);
+    h.Gamma = cv.take<double>((int64_t)S * K);
+    h.AlphaLocal = cv.take<double>((int64_t)S * K);
+    h.SumAlpha = cv.take<double>(S);
+    h.rout = cv.take<double>(h.rlen);
+    h.lnlTrace = cv.take<double>(ntrace);
+    h.red = cv.take<double>(((int64_t)S * K + K + 1) * (1 + LPQ_BLOCKS));
+    h.lnlp = cv.take<double>(h.nlnlp);
+    c->ancestry = cv.take<double>((int64_t)N * K);
+    c->d = cv.take<DevChain>(1);
+}
+
+// validate the parameters and fill the chain's scalar state and launch
+// geometry; *bytes receives the size of its device allocation
+int chain_plan(const vp_ctx* x, const vp_params* P, vp_chain* c, size_t* bytes) {
+    if (P->K < 1 || P->K > 64) { vp_set_error("K must be in 1..64"); return VP_E_ARG; }
+    if (P->nthinning < 1 || P->nburnin < 0 || P->nreps < 0) { vp_set_error("bad MCMC lengths"); return VP_E_ARG; }
+    c->P = *P;
+    const int K = P->K, N = x->N, S = x->S;
+    const int64_t L = x->L;
     DevChain& h = c->h;
     h.D = x->D;
     h.K = K; h.admix = P->admix; h.locpriori = P->locpriori; h.fmodel = P->fmodel;
@@ -385,7 +430,6 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
         h.lchunk = (int32_t)((L + nch - 1) / nch);
         h.nchunk = (int32_t)((L + h.lchunk - 1) / h.lchunk);
     }
-    set_smem_limits();
     h.kp = (K + 3) & ~3;
     h.nsampblk = (int32_t)cdiv(N, SAMPLE_BLOCK);
     {
@@ -396,57 +440,57 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
         lc = (lc + ZA_LC - 1) / ZA_LC * ZA_LC;
         h.zadm_lc = (int32_t)std::max<int64_t>(lc, ZA_LC);
     }
-    if (zadm_smem(c) > 200 * 1024) { vp_set_error("K * max alleles too large for the admixture kernel"); delete c; return VP_E_ARG; }
+    if ((size_t)ZA_LC * x->maxK * (K | 1) * 4 + (size_t)ZA_LC * K * x->maxK * 4 > 200 * 1024) {
+        vp_set_error("K * max alleles too large for the admixture kernel");
+        return VP_E_ARG;
+    }
     h.nlnlp = (int32_t)std::max<int64_t>(std::max<int64_t>(cdiv(L, 128), (int64_t)cdiv(N, ZA_WARPS * 32) * cdiv(L, h.zadm_lc)),
                                          h.nsampblk);
-    const int64_t ntrace = h.nburnin / h.nthinning + h.nreps / h.nthinning + 2;
-    const int64_t ltn = x->packed2 ? L * 4 * h.kp : (int64_t)K * KT;
-    auto layout = [&](Carve& cv) {
-        h.ctl = cv.take<Ctl>(1);
-        h.rstate = cv.take<Rng64>(1);
-        h.Freq = cv.take<float>(K * KT);
-        h.FreqM = cv.take<float>(K * KT);
-        h.FreqA = cv.take<float>(P->fmodel ? KT : 1);
-        h.lt = cv.take<float>(ltn);
-        h.Q = cv.take<float>((int64_t)N * K);
-        h.Qprop = cv.take<float>((int64_t)N * K);
-        h.Di = cv.take<float>((int64_t)S * K);
-        h.fbuf = cv.take<float>(64 * (x->maxK + 16));
-        h.Z = cv.take<uint16_t>(N + 32);
-        h.Mi = cv.take<int32_t>((int64_t)N * K);
-        h.Ni = cv.take<int32_t>(K * KT);
-        h.MiSum = cv.take<int64_t>((int64_t)N * K);
-        h.LLp = cv.take<double>((int64_t)h.nchunk * N * K);
-        h.LL = cv.take<double>((int64_t)N * K);
-        h.metro = cv.take<double>(N);
-        h.metrop = cv.take<double>((int64_t)h.nchunk * N);
-        h.Alpha = cv.take<double>(K);
-        h.Lambda = cv.take<double>(K);
-        h.f = cv.take<double>(K);
-        h.F = cv.take<double>(K);
-        h.Eta = cv.take<double>(K);
-        h.Gamma = cv.take<double>((int64_t)S * K);
-        h.AlphaLocal = cv.take<double>((int64_t)S * K);
-        h.SumAlpha = cv.take<double>(S);
-        h.rout = cv.take<double>(h.rlen);
-        h.lnlTrace = cv.take<double>(ntrace);
-        h.red = cv.take<double>(((int64_t)S * K + K + 1) * (1 + LPQ_BLOCKS));
-        h.lnlp = cv.take<double>(h.nlnlp);
-        c->ancestry = cv.take<double>((int64_t)N * K);
-        c->d = cv.take<DevChain>(1);
-    };
     Carve probe{nullptr};
-    layout(probe);
-    cudaError_t e = cudaMalloc(&c->mem, probe.off);
+    chain_layout(probe, c, x);
+    *bytes = probe.off;
+    return VP_OK;
+}
+}  // namespace
+
+int64_t vp_request_bytes(const vp_dataset* ds, const vp_params* P, int nsm) {
+    vp_ctx g;
+    g.N = ds->N; g.S = ds->S; g.L = ds->L; g.KT = ds->KT; g.maxK = ds->maxK; g.maxploidy = ds->maxploidy;
+    g.packed2 = ds->packed2; g.nsm = nsm;
+    vp_chain c;
+    size_t chain = 0;
+    if (chain_plan(&g, P, &c, &chain)) return -1;
+    // the context's uploads (each rounded to the allocator's 512-byte grain)
+    auto r = [](size_t b) { return (int64_t)((b + 511) & ~(size_t)511); };
+    int64_t data = ds->packed2 ? r(ds->g2.size() * 4) : r(ds->gb.size());
+    data += r(ds->k.size() * 4) + r(ds->off.size() * 8) + r(ds->vt.size() * 8) + r(ds->popid.size() * 4) +
+            r(ds->pop_ind0.size() * 4) + r(ds->pop_nind.size() * 4) + r(ds->totfreq.size() * 4) +
+            r(ds->nhaplo.size() * 4);
+    return data + (int64_t)chain;
+}
+
+extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
+    if (!x || !P || !out) { vp_set_error("null argument"); return VP_E_ARG; }
+    cudaSetDevice(x->device);
+    auto* c = new vp_chain();
+    c->ctx = x;
+    size_t bytes = 0;
+    int prc = chain_plan(x, P, c, &bytes);
+    if (prc) { delete c; return prc; }
+    set_smem_limits();
+    const int K = P->K, N = x->N;
+    const int64_t L = x->L;
+    DevChain& h = c->h;
+    cudaError_t e = cudaMalloc(&c->mem, bytes);
     if (e != cudaSuccess) {
-        vp_set_error("cudaMalloc of %zu bytes for chain state failed: %s", probe.off, cudaGetErrorString(e));
+        vp_set_error("cudaMalloc of %zu bytes for chain state failed: %s", bytes, cudaGetErrorString(e));
         delete c;
         return VP_E_MEM;
     }
     Carve cv{(char*)c->mem};
-    layout(cv);
+    chain_layout(cv, c, x);
     c->own_ni = h.Ni;
-    CK(cudaMemsetAsync(c->mem, 0, probe.off, x->stream));
+    CK(cudaMemsetAsync(c->mem, 0, bytes, x->stream));
     CK(cudaMemcpyAsync(c->d, &h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
     c->total = h.nburnin + h.nreps;
     // InitFix / InitAdmix / InitLocPriori / InitFmodel
@@ -560,7 +604,9 @@ extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
     return VP_OK;
 }
 
-extern "C" int vp_finish(vp_chain** cs, int32_t n) {
+// the rest of every chain's sweeps and the final Arrange, queued on the
+// context's stream without waiting
+int vp_finish_issue(vp_chain** cs, int32_t n) {
     if (!cs || n <= 0) { vp_set_error("bad arguments"); return VP_E_ARG; }
     int mx = 0;
     for (int i = 0; i < n; ++i) mx = std::max(mx, cs[i]->total - cs[i]->issued);
@@ -575,7 +621,17 @@ extern "C" int vp_finish(vp_chain** cs, int32_t n) {
         if (rc) return rc;
         c->arranged = true;
     }
-    return vp_sync(x);
+    return VP_OK;
+}
+
+extern "C" int vp_finish(vp_chain** cs, int32_t n) {
+    int rc = vp_finish_issue(cs, n);
+    return rc ? rc : vp_sync(cs[0]->ctx);
+}
+
+void vp_chain_progress(const vp_chain* c, int64_t* issued, int64_t* total) {
+    *issued = c->issued;
+    *total = c->total;
 }
 
 extern "C" int vp_chain_sizes(vp_chain* c, vp_result* r) {
@@ -708,32 +764,59 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 2-D bf16 row-major [rows][ld] map with 64 x box_rows boxes, 128-byte swizzle
-int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows) {
+// 2-D bf16 row-major [rows][ld] map with box_cols x box_rows boxes; 64-column
+// boxes (128-byte rows) use the 128-byte swizzle, 32-column boxes the 64-byte one
+int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows,
+             uint32_t box_cols) {
+    if (box_cols != 64 && box_cols != 32) { vp_set_error("box width must be 32 or 64 columns"); return VP_E_ARG; }
     EncodeTiledFn f = encode_fn();
     if (!f) { vp_set_error("cuTensorMapEncodeTiled unavailable"); return VP_E_CUDA; }
     cuuint64_t dims[2] = {cols, rows};
     cuuint64_t strides[1] = {ld * 2};
-    cuuint32_t box[2] = {64, box_rows};
+    cuuint32_t box[2] = {box_cols, box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_cols == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { vp_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return VP_E_CUDA; }
     return VP_OK;
 }
 
-int launch_gemm(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CUtensorMap& B1, tc::GemmArgs g,
-                dim3 grid) {
-    size_t sm = tc::gemm_smem_bytes(g.BN, g.nb, g.stages, g.mt);
+template <int BKT, int MT, int NB, int BNT, int PIECE>
+int launch_gemm_t(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CUtensorMap& B1, const tc::GemmArgs& g,
+                  dim3 grid, size_t sm) {
+    auto kern = tc::k_gemm_bf16<BKT, MT, NB, BNT, PIECE>;
     static bool attr = false;
     if (!attr) {
-        CK(cudaFuncSetAttribute(tc::k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         attr = true;
     }
-    if (sm > 227 * 1024) { vp_set_error("gemm tile needs %zu bytes of shared memory", sm); return VP_E_ARG; }
-    tc::k_gemm_bf16<<<grid, tc::NTHREADS, sm, x->stream>>>(A, B0, B1, g);
+    kern<<<grid, tc::NTHREADS, sm, x->stream>>>(A, B0, B1, g);
     return check_launch(x, "k_gemm_bf16");
+}
+
+// the tile shapes compiled into the library (stage depth, 128-row A tiles
+// per CTA, B operands, columns per CTA, columns per MMA)
+#define VP_GEMM_TILES(X)          \
+    X(64, 2, 2, 192, 192)         \
+    X(64, 2, 1, 192, 192)         \
+    X(64, 1, 2, 288, 144)         \
+    X(64, 1, 1, 256, 256)         \
+    X(32, 2, 2, 192, 192)
+
+int launch_gemm(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CUtensorMap& B1, tc::GemmArgs g,
+                dim3 grid) {
+    if (g.bk != 32 && g.bk != 64) { vp_set_error("gemm stage depth must be 32 or 64"); return VP_E_ARG; }
+    size_t sm = tc::gemm_smem_bytes(g.BN, g.nb, g.stages, g.mt, g.bk);
+    if (sm > 227 * 1024) { vp_set_error("gemm tile needs %zu bytes of shared memory", sm); return VP_E_ARG; }
+#define VP_GEMM_CASE(bk_, mt_, nb_, bn_, pc_)                                               \
+    if (g.bk == bk_ && g.mt == mt_ && g.nb == nb_ && g.BN == bn_ && g.piece == pc_)        \
+        return launch_gemm_t<bk_, mt_, nb_, bn_, pc_>(x, A, B0, B1, g, grid, sm);
+    VP_GEMM_TILES(VP_GEMM_CASE)
+#undef VP_GEMM_CASE
+    vp_set_error("gemm tile (bk %d, mt %d, nb %d, BN %d, piece %d) is not compiled in", g.bk, g.mt, g.nb, g.BN, g.piece);
+    return VP_E_ARG;
 }
 
 int tc_operands(vp_ctx* x) {
@@ -763,8 +846,8 @@ int tc_operands(vp_ctx* x) {
     if ((rc = check_launch(x, "k_allele_center"))) return rc;
     tc::k_center_const<<<cdiv((int64_t)x->N * 32, 256), 256, 0, x->stream>>>(x->D, t.logpbar, t.Bc);
     if ((rc = check_launch(x, "k_center_const"))) return rc;
-    if ((rc = make_map(&t.mapC, t.C, t.Npad, t.Apad, t.Apad, 128))) return rc;
-    if ((rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128))) return rc;
+    if ((rc = make_map(&t.mapC, t.C, t.Npad, t.Apad, t.Apad, 128, t.bk))) return rc;
+    if ((rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128, t.bk))) return rc;
     t.ready = true;
     return VP_OK;
 }
@@ -826,9 +909,9 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
     b->G = (b->R + b->BN - 1) / b->BN;
     b->Rpad = b->G * b->BN;
     const TcOperands& t = x->tc;
-    const int64_t tiles = ((t.Npad + 255) / 256) * b->G;
+    const int64_t tiles = ((t.Npad + 128 * b->mt1 - 1) / (128 * b->mt1)) * b->G;
     b->splits = tc_splits(tiles, x->nsm);
-    const int64_t kblocks = t.Apad / 64;
+    const int64_t kblocks = t.Apad / t.bk;
     b->splits = (int)std::min<int64_t>(b->splits, kblocks);
     Carve probe{nullptr};
     auto lay = [&](Carve& cv) {
@@ -861,9 +944,13 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
         CK(cudaMemcpyAsync(b->dchains + i, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     }
-    if ((rc = make_map(&b->mapWhi, b->Whi, b->Rpad, t.Apad, t.Apad, b->piece))) { x->batch = b; free_batch(x); return rc; }
-    if ((rc = make_map(&b->mapWlo, b->Wlo, b->Rpad, t.Apad, t.Apad, b->piece))) { x->batch = b; free_batch(x); return rc; }
-    if ((rc = make_map(&b->mapOH, b->OH, b->Rpad, t.Npad, t.Npad, b->piece))) { x->batch = b; free_batch(x); return rc; }
+    if ((rc = make_map(&b->mapWhi, b->Whi, b->Rpad, t.Apad, t.Apad, b->piece, t.bk)) ||
+        (rc = make_map(&b->mapWlo, b->Wlo, b->Rpad, t.Apad, t.Apad, b->piece, t.bk)) ||
+        (rc = make_map(&b->mapOH, b->OH, b->Rpad, t.Npad, t.Npad, b->piece, t.bk))) {
+        x->batch = b;
+        free_batch(x);
+        return rc;
+    }
     x->batch = b;
     return VP_OK;
 }
@@ -889,12 +976,12 @@ int launch_tc_sweep(vp_ctx* x) {
     // likelihood contraction: LL'[i, row] = sum_a C[i,a] (Whi + Wlo)[row, a]
     {
         tc::GemmArgs g{};
-        g.M = x->N; g.N = b->Rpad; g.kblocks = (int)(t.Apad / 64);
+        g.M = x->N; g.N = b->Rpad; g.kblocks = (int)(t.Apad / t.bk);
         g.kb_per_split = (g.kblocks + b->splits - 1) / b->splits;
-        g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.mt = 2; g.stages = 2; g.mode = 0;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.mt = b->mt1; g.stages = b->st1; g.bk = t.bk; g.mode = 0;
         g.out_f = b->LLpart; g.ldo = b->Rpad; g.err = t.err;
         prof_mark(x, true);
-        int rc = launch_gemm(x, t.mapC, b->mapWhi, b->mapWlo, g, dim3(cdiv(t.Npad, 256), b->G, b->splits));
+        int rc = launch_gemm(x, t.mapC, b->mapWhi, b->mapWlo, g, dim3(cdiv(t.Npad, 128 * b->mt1), b->G, b->splits));
         prof_mark(x, false);
         if (rc) return rc;
     }
@@ -903,10 +990,10 @@ int launch_tc_sweep(vp_ctx* x) {
     // count contraction: Ni[row, a] = sum_i OH[row, i] C[i, a]
     {
         tc::GemmArgs g{};
-        g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / 64); g.kb_per_split = g.kblocks;
-        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.mt = 2; g.stages = 3; g.mode = 1;
+        g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / t.bk); g.kb_per_split = g.kblocks;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.mt = b->mt2; g.stages = b->st2; g.bk = t.bk; g.mode = 1;
         g.out_i = b->NiAll; g.ldo = x->KT; g.err = t.err;
-        int rc = launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, dim3(cdiv(t.Apad, 256), b->G, 1));
+        int rc = launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, dim3(cdiv(t.Apad, 128 * b->mt2), b->G, 1));
         if (rc) return rc;
     }
     // Record for every chain, then m += 1
@@ -956,9 +1043,9 @@ extern "C" int vp_tc_status(vp_ctx* x) {
 
 extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N,
                                   int32_t K, int32_t BN, int32_t piece, int32_t splits, int32_t stages, int32_t mt,
-                                  float* D) {
-    if (!A || !B0 || !D || M <= 0 || N <= 0 || K <= 0 || K % 64 || N % BN || BN % piece || piece % 16 || piece > 256 ||
-        (mt != 1 && mt != 2) || BN * mt > 512 || splits < 1) {
+                                  int32_t bk, float* D) {
+    if (!A || !B0 || !D || M <= 0 || N <= 0 || K <= 0 || (bk != 32 && bk != 64) || K % bk || N % BN || BN % piece ||
+        piece % 16 || piece > 256 || (mt != 1 && mt != 2) || BN * mt > 512 || splits < 1) {
         vp_set_error("vp_debug_gemm_bf16: bad shape");
         return VP_E_ARG;
     }
@@ -980,13 +1067,13 @@ extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const u
         CK(cudaMemcpy(dB1, B1, (size_t)N * K * 2, cudaMemcpyHostToDevice));
     }
     CUtensorMap ma, mb0, mb1;
-    int rc = make_map(&ma, dA, Mp, K, K, 128);
-    if (!rc) rc = make_map(&mb0, dB0, N, K, K, piece);
-    if (!rc) rc = make_map(&mb1, B1 ? dB1 : dB0, N, K, K, piece);
+    int rc = make_map(&ma, dA, Mp, K, K, 128, bk);
+    if (!rc) rc = make_map(&mb0, dB0, N, K, K, piece, bk);
+    if (!rc) rc = make_map(&mb1, B1 ? dB1 : dB0, N, K, K, piece, bk);
     if (!rc) {
         tc::GemmArgs g{};
-        g.M = M; g.N = N; g.kblocks = K / 64; g.kb_per_split = (g.kblocks + splits - 1) / splits;
-        g.BN = BN; g.piece = piece; g.nb = B1 ? 2 : 1; g.mt = mt; g.stages = stages; g.mode = 0;
+        g.M = M; g.N = N; g.kblocks = K / bk; g.kb_per_split = (g.kblocks + splits - 1) / splits;
+        g.BN = BN; g.piece = piece; g.nb = B1 ? 2 : 1; g.mt = mt; g.stages = stages; g.bk = bk; g.mode = 0;
         g.out_f = (float*)dD; g.ldo = N; g.err = err;
         rc = launch_gemm(&tmp, ma, mb0, mb1, g, dim3((unsigned)(Mp / (128 * mt)), N / BN, splits));
     }
@@ -1001,6 +1088,73 @@ extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const u
         }
     }
     cudaFree(dA); cudaFree(dB0); if (dB1) cudaFree(dB1); cudaFree(dD); cudaFree(err);
+    cudaStreamDestroy(tmp.stream);
+    tmp.stream = nullptr;
+    return rc;
+}
+
+extern "C" int vp_debug_gemm_time(int32_t M, int32_t N, int32_t K, int32_t BN, int32_t piece, int32_t splits,
+                                  int32_t stages, int32_t mt, int32_t bk, int32_t nb, int32_t mode, int32_t iters,
+                                  double* ms) {
+    if (!ms || M <= 0 || N <= 0 || K <= 0 || (bk != 32 && bk != 64) || K % bk || N % BN || BN % piece ||
+        piece % 16 || piece > 256 || (mt != 1 && mt != 2) || BN * mt > 512 || splits < 1 || (nb != 1 && nb != 2) ||
+        (mode != 0 && mode != 1) || (mode == 1 && splits != 1) || iters < 1) {
+        vp_set_error("vp_debug_gemm_time: bad shape");
+        return VP_E_ARG;
+    }
+    vp_ctx tmp;
+    cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking);
+    const int64_t Mp = (M + 128 * mt - 1) / (128 * mt) * (128 * mt);
+    void *dA = nullptr, *dB = nullptr, *dD = nullptr;
+    int* err = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = VP_OK;
+    do {
+        cudaError_t ce;
+        const size_t outb = mode == 0 ? (size_t)splits * M * N * 4 : (size_t)N * M * 4;
+        if ((ce = cudaMalloc(&dA, (size_t)Mp * K * 2)) != cudaSuccess || (ce = cudaMalloc(&dB, (size_t)2 * N * K * 2)) != cudaSuccess ||
+            (ce = cudaMalloc(&dD, outb)) != cudaSuccess || (ce = cudaMalloc(&err, 4)) != cudaSuccess) {
+            vp_set_error("vp_debug_gemm_time: %s", cudaGetErrorString(ce));
+            rc = VP_E_MEM;
+            break;
+        }
+        // small bf16 values (0x3C3C ~ 0.0115): the timing does not depend on them
+        cudaMemsetAsync(dA, 0x3C, (size_t)Mp * K * 2, tmp.stream);
+        cudaMemsetAsync(dB, 0x3C, (size_t)2 * N * K * 2, tmp.stream);
+        cudaMemsetAsync(err, 0, 4, tmp.stream);
+        CUtensorMap ma, mb0, mb1;
+        const uint16_t* b1 = (const uint16_t*)dB + (size_t)N * K;
+        if ((rc = make_map(&ma, dA, Mp, K, K, 128, bk)) || (rc = make_map(&mb0, dB, N, K, K, piece, bk)) ||
+            (rc = make_map(&mb1, b1, N, K, K, piece, bk)))
+            break;
+        tc::GemmArgs g{};
+        g.M = M; g.N = N; g.kblocks = K / bk; g.kb_per_split = (g.kblocks + splits - 1) / splits;
+        g.BN = BN; g.piece = piece; g.nb = nb; g.mt = mt; g.stages = stages; g.bk = bk; g.mode = mode;
+        g.out_f = (float*)dD; g.out_i = (int32_t*)dD; g.ldo = mode == 0 ? N : M; g.err = err;
+        const dim3 grid((unsigned)(Mp / (128 * mt)), N / BN, splits);
+        if ((rc = launch_gemm(&tmp, ma, mb0, mb1, g, grid))) break;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, tmp.stream);
+        for (int i = 0; i < iters && !rc; ++i) rc = launch_gemm(&tmp, ma, mb0, mb1, g, grid);
+        cudaEventRecord(e1, tmp.stream);
+        if (rc) break;
+        if ((ce = cudaStreamSynchronize(tmp.stream)) != cudaSuccess) {
+            vp_set_error("gemm: %s", cudaGetErrorString(ce));
+            rc = VP_E_CUDA;
+            break;
+        }
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        *ms = t / iters;
+        int e = 0;
+        cudaMemcpy(&e, err, 4, cudaMemcpyDeviceToHost);
+        if (e) { vp_set_error("gemm pipeline timed out (code %d)", e); rc = VP_E_CUDA; }
+    } while (0);
+    cudaStreamSynchronize(tmp.stream);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(err);
     cudaStreamDestroy(tmp.stream);
     tmp.stream = nullptr;
     return rc;

@@ -3,9 +3,11 @@
 //   D[m, n] = sum_k A[m, k] * (B0[n, k] + B1[n, k])        (B1 optional)
 //
 // A, B0, B1 are bf16, K-major (k contiguous) in global memory and are staged
-// into shared memory by TMA with the 128-byte swizzle; one thread issues
-// tcgen05.mma (kind::f16, bf16 x bf16 -> f32) into a TMEM accumulator of
-// 128 lanes x BN columns; four epilogue warps read it back with tcgen05.ld.
+// into shared memory by TMA, bk = 64 or 32 K elements per stage with the
+// 128- or 64-byte swizzle (smaller stages keep more of them in flight); one
+// thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> f32) into a TMEM
+// accumulator of 128 lanes x mt*BN columns; four epilogue warps read it back
+// with tcgen05.ld.
 // With B1 given, the hi and lo halves of a split-bf16 operand accumulate into
 // the same FP32 accumulator.
 //
@@ -23,19 +25,19 @@ namespace vp {
 namespace tc {
 
 constexpr int BM = 128;
-constexpr int BK = 64;                 // bf16 elements per 128-byte swizzle row
 constexpr int NTHREADS = 192;
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
 
 struct GemmArgs {
     int M, N;               // rows of A / D, columns of D (= rows of B)
-    int kblocks;            // K / BK of the whole problem
+    int kblocks;            // K / bk of the whole problem
     int kb_per_split;       // k-blocks handled by one CTA (grid.z splits K)
     int BN;                 // columns per CTA (multiple of 16, <= 512)
     int piece;              // columns per MMA instruction (<= 256, multiple of 16)
     int nb;                 // 1 or 2 B operands
     int mt;                 // 128-row A tiles per CTA sharing the B tile (1 or 2)
     int stages;
+    int bk;                 // K elements per stage: 64 (128-byte swizzle rows) or 32 (64-byte rows)
     int mode;               // 0: FP32 partials D[z][m][n]; 1: int32 transpose Dt[n][m] (no split)
     float* out_f;           // mode 0: [splits][M][ldo]
     int32_t* out_i;         // mode 1: [N][ldo]
@@ -76,22 +78,21 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (SBO), sm100 descriptor version 1
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+// shared-memory matrix descriptor: K-major, rows of bk bf16 (128 or 64
+// bytes) with the matching swizzle, 8-row groups 8 rows apart (SBO), sm100
+// descriptor version 1
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr, int bk) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-    d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
-    d |= (uint64_t)1 << 46;                 // version
-    d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+    d |= (uint64_t)1 << 16;                                 // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)((8 * bk * 2) >> 4) << 32;               // stride byte offset
+    d |= (uint64_t)1 << 46;                                 // version
+    d |= (uint64_t)(bk == 64 ? 2 : 4) << 61;                // SWIZZLE_128B or SWIZZLE_64B
     return d;
 }
 
-// instruction descriptor: D f32, A bf16, B bf16, both K-major, M = 128
-__device__ __forceinline__ uint32_t idesc_bf16(int n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-}
+// instruction descriptor (D f32, A bf16, B bf16, both K-major, M = 128):
+// bits 4-5 D format, 7-9 A format, 10-12 B format, 17-22 N/8, 24-28 M/16
 
 __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
     asm volatile(
@@ -115,41 +116,49 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// dynamic shared memory: [stages][A tile | B0 tile | B1 tile] (1024-aligned),
-// then barriers
+// dynamic shared memory: [stages][A tiles | B0 tile | B1 tile] (1024-aligned),
+// then barriers.
+// The tile shape is compile-time: one thread issues every MMA, and with the
+// shape fixed each MMA is two descriptor additions and the instruction
+// (rebuilding descriptors from runtime sizes made that thread, not the
+// tensor core, the limit).
+template <int BKT, int MT, int NB, int BNT, int PIECE>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_gemm_bf16(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB0,
                 const __grid_constant__ CUtensorMap mapB1, GemmArgs g) {
+    static_assert(BKT == 32 || BKT == 64, "stage depth");
+    static_assert(BNT % PIECE == 0 && PIECE % 16 == 0 && PIECE <= 256 && MT * BNT <= 512, "tile");
+    constexpr uint32_t A_TILE = BM * BKT * 2;
+    constexpr uint32_t A_BYTES = A_TILE * MT;
+    constexpr uint32_t B_BYTES = BNT * BKT * 2;
+    constexpr uint32_t STAGE = A_BYTES + B_BYTES * NB;
+    constexpr uint32_t NCOLS = MT * BNT <= 32 ? 32 : MT * BNT <= 64 ? 64 : MT * BNT <= 128 ? 128 : MT * BNT <= 256 ? 256 : 512;
+    constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(PIECE >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t a_tile = BM * BK * 2;
-    const uint32_t a_bytes = a_tile * g.mt;
-    const uint32_t b_bytes = (uint32_t)g.BN * BK * 2;
-    const uint32_t stage_bytes = a_bytes + b_bytes * g.nb;
-    uint64_t* full = (uint64_t*)(smem + (size_t)stage_bytes * g.stages);
-    uint64_t* empty = full + g.stages;
-    uint64_t* accum = empty + g.stages;
+    const int stages = g.stages;
+    uint64_t* full = (uint64_t*)(smem + (size_t)STAGE * stages);
+    uint64_t* empty = full + stages;
+    uint64_t* accum = empty + stages;
     uint32_t* tmem_holder = (uint32_t*)(accum + 1);
     int* abort_flag = (int*)(tmem_holder + 1);
 
-    const int m0 = blockIdx.x * BM * g.mt;
-    const int n0 = blockIdx.y * g.BN;
+    const int m0 = blockIdx.x * BM * MT;
+    const int n0 = blockIdx.y * BNT;
     const int kb0 = blockIdx.z * g.kb_per_split;
     const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
     const int nk = kb1 - kb0;
-    uint32_t ncols = 32;
-    while ((int)ncols < g.BN * g.mt) ncols <<= 1;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < g.stages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int s = 0; s < stages; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
         mbar_init(accum, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
-                     "r"(ncols));
+                     "r"(NCOLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -162,62 +171,65 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (lane == 0 && nk > 0) {
             int issued = 0;
             for (int it = 0; it < nk; ++it) {
-                const int s = it % g.stages;
-                if (it >= g.stages && !mbar_wait(&empty[s], ((it / g.stages) & 1) ^ 1)) {
+                const int s = it % stages;
+                if (it >= stages && !mbar_wait(&empty[s], ((it / stages) & 1) ^ 1)) {
                     atomicExch(g.err, 1);
                     *(volatile int*)abort_flag = 1;
                     break;
                 }
                 if (*(volatile int*)abort_flag) break;
-                unsigned char* st = smem + (size_t)s * stage_bytes;
-                mbar_expect_tx(&full[s], stage_bytes);
-                const int kx = (kb0 + it) * BK;
-                for (int t = 0; t < g.mt; ++t) tma_load_2d(st + (size_t)t * a_tile, &mapA, &full[s], kx, m0 + t * BM);
-                for (int b = 0; b < g.nb; ++b) {
-                    unsigned char* bt = st + a_bytes + (size_t)b * b_bytes;
-                    const CUtensorMap* mb = b == 0 ? &mapB0 : &mapB1;
-                    for (int p = 0; p < g.BN; p += g.piece)
-                        tma_load_2d(bt + (size_t)p * BK * 2, mb, &full[s], kx, n0 + p);
-                }
+                unsigned char* st = smem + (size_t)s * STAGE;
+                mbar_expect_tx(&full[s], STAGE);
+                const int kx = (kb0 + it) * BKT;
+#pragma unroll
+                for (int t = 0; t < MT; ++t) tma_load_2d(st + t * A_TILE, &mapA, &full[s], kx, m0 + t * BM);
+#pragma unroll
+                for (int b = 0; b < NB; ++b)
+#pragma unroll
+                    for (int p = 0; p < BNT; p += PIECE)
+                        tma_load_2d(st + A_BYTES + b * B_BYTES + p * BKT * 2, b == 0 ? &mapB0 : &mapB1, &full[s], kx,
+                                    n0 + p);
                 issued = it + 1;
             }
             // drain: every issued stage must have landed before the CTA may exit
-            for (int it = (issued > g.stages ? issued - g.stages : 0); it < issued; ++it)
-                mbar_wait(&full[it % g.stages], (it / g.stages) & 1);
+            for (int it = (issued > stages ? issued - stages : 0); it < issued; ++it)
+                mbar_wait(&full[it % stages], (it / stages) & 1);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0 && nk > 0) {
-            bool ok = true;
+            // descriptor of stage 0 at its first byte; the tiles' offsets are
+            // added to the address field in 16-byte units (a shared-memory
+            // address below 256 KB never carries out of its 14 bits)
+            const uint64_t d0 = sw_desc(smem_u32(smem), BKT);
             for (int it = 0; it < nk; ++it) {
-                const int s = it % g.stages;
-                if (!mbar_wait(&full[s], (it / g.stages) & 1) || *(volatile int*)abort_flag) {
+                const int s = it % stages;
+                if (!mbar_wait(&full[s], (it / stages) & 1) || *(volatile int*)abort_flag) {
                     atomicExch(g.err, 2);
                     *(volatile int*)abort_flag = 1;
-                    ok = false;
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                unsigned char* st = smem + (size_t)s * stage_bytes;
-                const uint32_t abase = smem_u32(st);
-                for (int kk = 0; kk < BK / 16; ++kk)
-                    for (int t = 0; t < g.mt; ++t) {
-                        const uint64_t ad = sw128_desc(abase + t * a_tile + kk * 32);
-                        for (int b = 0; b < g.nb; ++b) {
-                            const uint32_t bbase = smem_u32(st + a_bytes + (size_t)b * b_bytes);
-                            for (int p = 0; p < g.BN; p += g.piece) {
-                                const int n = min(g.piece, g.BN - p);
-                                const uint64_t bd = sw128_desc(bbase + (uint32_t)p * BK * 2 + kk * 32);
-                                mma_bf16(tmem + (uint32_t)(t * g.BN + p), ad, bd, idesc_bf16(n), (it | kk | b) != 0);
+                const uint64_t ds = d0 + (uint64_t)((s * STAGE) >> 4);
+                const uint32_t acc0 = it != 0;
+#pragma unroll
+                for (int kk = 0; kk < BKT / 16; ++kk)
+#pragma unroll
+                    for (int t = 0; t < MT; ++t) {
+                        const uint64_t ad = ds + (uint64_t)((t * A_TILE + kk * 32) >> 4);
+#pragma unroll
+                        for (int b = 0; b < NB; ++b)
+#pragma unroll
+                            for (int p = 0; p < BNT; p += PIECE) {
+                                const uint64_t bd = ds + (uint64_t)((A_BYTES + b * B_BYTES + p * BKT * 2 + kk * 32) >> 4);
+                                mma_bf16(tmem + (uint32_t)(t * BNT + p), ad, bd, IDESC, (kk | b) ? 1u : acc0);
                             }
-                        }
                     }
                 mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
             }
             // also on the error path: the commit arrives only once every MMA this
             // thread issued has finished writing TMEM
             mma_commit(accum);
-            (void)ok;
         }
         if (lane == 0 && nk <= 0)
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(accum)) : "memory");
@@ -228,11 +240,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const bool valid = got && !*(volatile int*)abort_flag && nk > 0;
         if (!got) atomicExch(g.err, 3);
-        for (int t = 0; t < g.mt; ++t) {
+#pragma unroll
+        for (int t = 0; t < MT; ++t) {
             const int row = m0 + t * BM + q * 32 + lane;
-            for (int c0 = 0; c0 < g.BN; c0 += 16) {
+            for (int c0 = 0; c0 < BNT; c0 += 16) {
                 float v[16];
-                tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(t * g.BN + c0), v);
+                tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(t * BNT + c0), v);
                 if (!valid) continue;
                 if (g.mode == 0) {
                     if (row < g.M) {
@@ -254,12 +267,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS));
     }
 }
 
-inline size_t gemm_smem_bytes(int BN, int nb, int stages, int mt = 1) {
-    size_t st = (size_t)BM * BK * 2 * mt + (size_t)BN * BK * 2 * nb;
+inline size_t gemm_smem_bytes(int BN, int nb, int stages, int mt, int bk) {
+    size_t st = (size_t)BM * bk * 2 * mt + (size_t)BN * bk * 2 * nb;
     return st * stages + 1024 /*align slack*/ + 256 /*barriers*/;
 }
 

@@ -187,23 +187,86 @@ class Chain:
 
     def result(self, final: bool = False) -> dict:
         """Results; `final` (after vp_finish) adds the normalised ancestry."""
-        r = B.VpResult()
-        B.check(B.lib().vp_chain_sizes(self.h, C.byref(r)))
-        out = dict(rout=np.zeros(r.rlen), lnl=np.zeros(max(r.nlnl, 0)), Q=np.zeros(r.N * r.K, np.float32),
-                   ancestry=np.zeros(r.N * r.K), freqm=np.zeros(r.K * r.KT, np.float32))
-        r.rout, r.lnl, r.Q = out["rout"].ctypes.data, out["lnl"].ctypes.data, out["Q"].ctypes.data
-        r.ancestry = out["ancestry"].ctypes.data if final else None
-        r.freqm = out["freqm"].ctypes.data
-        if not final:
-            del out["ancestry"]
-        B.check(B.lib().vp_chain_result(self.h, C.byref(r)))
-        out.update(K=r.K, N=r.N, nr=r.nr, nburnin=r.nburnin, nreps=r.nreps, nthinning=r.nthinning, seed=r.seed)
-        return out
+        return chain_result(self.h, final)
 
     def close(self):
         if getattr(self, "h", None):
             B.lib().vp_chain_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        if not sys.is_finalizing():
+            self.close()
+
+
+def chain_result(h, final: bool = False) -> dict:
+    r = B.VpResult()
+    B.check(B.lib().vp_chain_sizes(h, C.byref(r)))
+    out = dict(rout=np.zeros(r.rlen), lnl=np.zeros(max(r.nlnl, 0)), Q=np.zeros(r.N * r.K, np.float32),
+               ancestry=np.zeros(r.N * r.K), freqm=np.zeros(r.K * r.KT, np.float32))
+    r.rout, r.lnl, r.Q = out["rout"].ctypes.data, out["lnl"].ctypes.data, out["Q"].ctypes.data
+    r.ancestry = out["ancestry"].ctypes.data if final else None
+    r.freqm = out["freqm"].ctypes.data
+    if not final:
+        del out["ancestry"]
+    B.check(B.lib().vp_chain_result(h, C.byref(r)))
+    out.update(K=r.K, N=r.N, nr=r.nr, nburnin=r.nburnin, nreps=r.nreps, nthinning=r.nthinning, seed=r.seed)
+    return out
+
+
+_STATE = {B.VP_REQ_QUEUED: "queued", B.VP_REQ_RUNNING: "running", B.VP_REQ_DONE: "done", B.VP_REQ_FAILED: "failed"}
+
+
+class Server:
+    """Many independent runs on one device: a native scheduler thread admits
+    runs by device-memory budget and overlaps them on per-run streams
+    (vp_server_open / vp_submit / vp_poll / vp_wait / vp_release)."""
+
+    def __init__(self, device: int = 0, mem_budget: int = 0, max_active: int = 0, chunk: int = 0):
+        h = C.c_void_p()
+        B.check(B.lib().vp_server_open(device, mem_budget, max_active, chunk, C.byref(h)))
+        self.h = h
+        self._ds = {}
+
+    def submit(self, ds: Dataset, p: B.VpParams) -> int:
+        rid = C.c_int64()
+        B.check(B.lib().vp_submit(self.h, ds.h, C.byref(p), C.byref(rid)))
+        self._ds[rid.value] = ds          # the dataset must outlive the run
+        return rid.value
+
+    @staticmethod
+    def _info(i: B.VpRequestInfo) -> dict:
+        return dict(state=_STATE[i.state], rc=i.rc, sweeps_issued=i.sweeps_issued, sweeps_total=i.sweeps_total,
+                    device_bytes=i.device_bytes, t_submit=i.t_submit, t_start=i.t_start, t_done=i.t_done,
+                    error=i.error.decode())
+
+    def poll(self, rid: int) -> dict:
+        i = B.VpRequestInfo()
+        B.check(B.lib().vp_poll(self.h, rid, C.byref(i)))
+        return self._info(i)
+
+    def wait(self, rid: int, timeout: float = -1.0) -> dict:
+        i = B.VpRequestInfo()
+        B.check(B.lib().vp_wait(self.h, rid, timeout, C.byref(i)))
+        return self._info(i)
+
+    def chain(self, rid: int):
+        h = C.c_void_p()
+        B.check(B.lib().vp_request_chain(self.h, rid, C.byref(h)))
+        return h
+
+    def result(self, rid: int, final: bool = True) -> dict:
+        return chain_result(self.chain(rid), final)
+
+    def release(self, rid: int) -> None:
+        B.check(B.lib().vp_release(self.h, rid))
+        self._ds.pop(rid, None)
+
+    def close(self):
+        if getattr(self, "h", None):
+            B.lib().vp_server_close(self.h)
+            self.h = None
+            self._ds.clear()
 
     def __del__(self):
         if not sys.is_finalizing():
