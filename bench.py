@@ -1,18 +1,22 @@
 #!/usr/bin/env python
-"""Benchmark of the STRUCTURE K-sweep on GB300: genotype-cluster updates/s.
+"""Benchmark of the STRUCTURE sweep on GB300: genotype-cluster updates/s.
 
-Workload (the batched K-sweep the metric is quoted on): N = 10,000 diploid
-individuals x L = 200,000 biallelic SNPs drawn from an 8-population F-model
-(F = 0.03, ancestral frequencies Beta(0.5, 0.5), 1% missing calls), seeded
-synthetic data; K = 1..10 x 10 replicates = 100 no-admixture chains sharing
-the genotype matrix. One step = one MCMC sweep of all 100 chains; one
+Default workload (c3, the batched K-sweep the metric is quoted on): N = 10,000
+diploid individuals x L = 200,000 biallelic SNPs drawn from an 8-population
+F-model (F = 0.03, ancestral frequencies Beta(0.5, 0.5), 1% missing calls),
+seeded synthetic data; K = 1..10 x 10 replicates = 100 no-admixture chains
+sharing the genotype matrix. One step = one MCMC sweep of all 100 chains; one
 genotype-cluster update = one (individual, locus, cluster) term, so a step is
 N * L * sum(K) updates.
 
   --form tc     the tensor-core split-BF16 form (default)
   --form plain  the FP32 SIMT form of the same sweep
+  --workload c1|c2|c4   one chain of that case (vcfpop_gb300/workloads.py);
+                a step is one sweep
+  --workload c5 the serving stream: independent runs arriving at 50/s through
+                the native scheduler, against the same runs one at a time
   --impl reference  the CPU baseline: the reference algorithm's C port on the
-                host cores, one chain per thread, on a bounded locus sample
+                host cores on a bounded sample of the workload
 
 Prints one JSON line (rank 0).
 """
@@ -46,6 +50,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-sweeps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--requests", type=int, default=120, help="c5: runs in the stream")
+    ap.add_argument("--c5-scale", type=float, default=0.1, help="c5: scale of the N, L and run-length ranges")
     return ap.parse_args()
 
 
@@ -178,11 +185,270 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- c1, c2, c4: one chain
+SINGLE_DESC = {
+    "c1": "N=200 diploids, 3 pops, L=2,000 biallelic SNPs, F=0.1, 5% missing; K=3 no-admixture, 1,000 + 2,000 sweeps",
+    "c2": "N=2,000 x L=50,000 biallelic, Q~Dir(0.5), F=0.05, 2% missing; K=5 admixture, alpha inferred, 5,000 + 10,000 sweeps",
+    "c4": "N=5,000 autopolyploids (ploidy 2/4/6 at 2:1:1), 20 locations, L=20,000 loci with 2-8 alleles, F=0.08, "
+          "3% missing; K=8 admixture + location prior, 10,000 + 10,000 sweeps",
+}
+
+
+def _single(name):
+    from vcfpop_gb300 import workloads as W
+    d, run = getattr(W, name)()
+    run = dict(run)
+    K = run.pop("K")
+    return d, K, run
+
+
+def _sweep_bytes(ds, K, admix):
+    """Algorithmic bytes of the dominant kernel per launch: the genotype
+    matrix, the frequencies (and counts written back for the admixture form)
+    and the per-individual outputs."""
+    bg = ds.L * ((ds.N + 15) // 16) * 4 if ds.packed2 else ds.L * ds.N * ds.maxploidy
+    if admix:
+        return bg + 8 * K * ds.KT + 8 * ds.N * K
+    return bg + 4 * K * ds.KT + 8 * ds.N * K
+
+
+def cpu_sample_single(d, K, run, budget_s=12.0, max_sweeps=400):
+    """The oracle (the reference algorithm's C port), one chain on one core,
+    on the full dataset of the case: sweeps until about budget_s seconds."""
+    from tests import orc
+    import ctypes as C
+    od = orc.Data(d)
+    L = od.field(1, np.int32).size
+    p = orc.params(K, 1000, **run)
+    ch = orc.Chain(od, p)
+    arr = (C.c_void_p * 1)(ch.h)
+    orc.lib().orc_sweep_many(arr, 1, 0, 1, 1)
+    orc.lib().orc_sweep_many(arr, 1, 1, 1, 0)        # warm-up sweep
+    n, t0 = 0, time.perf_counter()
+    while n < max_sweeps and (time.perf_counter() - t0) < budget_s:
+        orc.lib().orc_sweep_many(arr, 1, 1, 1, 0)
+        n += 1
+    dt = time.perf_counter() - t0
+    N = d["G"].shape[1]
+    return N * L * K * n / dt, n, dt
+
+
+def bench_single(args):
+    import torch
+    import ctypes as C
+    from vcfpop_gb300 import _lib as B
+    from vcfpop_gb300 import structure as S
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    d, K, run = _single(args.workload)
+    ds = S.Dataset.from_synth(d)
+    admix = bool(run.get("admix"))
+    upd = ds.N * ds.L * K
+    lib = B.lib()
+    ctx = S.Context(ds, local)
+    ch = S.Chain(ctx, S.params(K, S.run_seed(1, 1), **run))
+    arr = (C.c_void_p * 1)(ch.h)
+    total = run["nburnin"] + run["nreps"] + (run.get("nadmburnin", 0) if not admix and not run.get("locpriori") else 0)
+    B.check(lib.vp_run(arr, 1, args.warmup))
+    ctx.sync()
+    # time enough sweeps for a region of about a second (within the run's length)
+    t0 = time.perf_counter()
+    B.check(lib.vp_run(arr, 1, 5))
+    ctx.sync()
+    per = (time.perf_counter() - t0) / 5
+    left = total - args.warmup - 5 - 8
+    n = int(max(args.steps, min(left, 1.0 / max(per, 1e-6))))
+    n = max(1, min(n, left))
+    stream = torch.cuda.ExternalStream(lib.vp_stream(ctx.h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launches()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        e0.record(stream)
+        B.check(lib.vp_run(arr, 1, n))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = ctx.launches() - l0
+    ms = e0.elapsed_time(e1) / n
+    # dominant kernel: average launch duration over a few more sweeps
+    lib.vp_prof_enable(ctx.h, 1)
+    dom, cnt = 0.0, 0
+    msv, nl = C.c_double(), C.c_int32()
+    for _ in range(6):
+        B.check(lib.vp_run(arr, 1, 1))
+        B.check(lib.vp_prof_read(ctx.h, C.byref(msv), C.byref(nl)))
+        dom += msv.value
+        cnt += nl.value
+    dom_ms = dom / max(cnt, 1)
+    byts = _sweep_bytes(ds, K, admix)
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = byts / (dom_ms / 1e3) / 1e9
+    l2 = byts < 120e6
+    roof = {"bound": "hbm", "kernel": "k_update_z_admix_ctr (per-copy labels)" if admix else "k_loglik (likelihood stream)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback", "traffic": None,
+            "avg_launch_ms": dom_ms, "bytes_per_launch": byts,
+            "note": "working set fits in L2 (129 MB): the fraction is against HBM bandwidth but served from L2" if l2 else ""}
+    ch.close()
+    ctx.close()
+
+    # end to end: open from host buffers, create, run, read results, close
+    e2e = None
+    if not args.no_e2e:
+        r2 = dict(run)
+        full = args.workload == "c1"
+        if not full:
+            r2["nburnin"], r2["nreps"] = 500, 500
+        e_sweeps = r2["nburnin"] + r2["nreps"] + (r2.get("nadmburnin", 0) if not admix and not r2.get("locpriori") else 0)
+        times = []
+        for it in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            cx = S.Context(ds, local)
+            c2 = S.Chain(cx, S.params(K, S.run_seed(1, 2), **r2))
+            S.finish([c2])
+            res = c2.result(final=True)
+            c2.close()
+            cx.close()
+            times.append(time.perf_counter() - t0)
+            assert np.isfinite(res["rout"]).all()
+        tt = min(times[1:]) if len(times) > 1 else times[0]
+        h2d = (ds.L * ((ds.N + 15) // 16) * 4 if ds.packed2 else ds.L * ds.N * ds.maxploidy) + ds.L * 12 + ds.N * 12
+        d2h = 8 * (ds.N * K * 2 + ds.KT * K) + 64
+        e2e = {"value": upd * e_sweeps / tt, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "step": ("one complete run" if full else f"a run of {e_sweeps} sweeps (500 + 500)") +
+                       ": open context from pinned host buffers, create the chain, every sweep, Arrange, read Q, "
+                       "ancestry, mean frequencies and lnL, close", "time_to_result_s": tt}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, ns, dt = cpu_sample_single(d, K, run)
+        cpu = {"value": v, "unit": "updates/s", "cores": 1, "kind": "port",
+               "sample": f"the same dataset, one chain on one host core, {ns} sweeps in {dt:.1f} s"}
+    line = {"metric": METRIC, "value": upd / (ms / 1e3), "unit": "updates/s", "n_gpus": world, "steps": n,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (lnP(D) accumulations in f64)",
+            "data": "synthetic F-model, seeded (vcfpop_gb300/workloads.py)",
+            "config": {"workload": f"{args.workload}: {SINGLE_DESC[args.workload]}; one step = one sweep",
+                       "form": "plain", "chains": 1, "updates_per_step": upd,
+                       "l2": "working set smaller than L2" if l2 else "inputs larger than L2",
+                       "parallelism": "1 GPU"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def reference_single(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    d, K, run = _single(args.workload)
+    v, ns, dt = cpu_sample_single(d, K, run, budget_s=60.0, max_sweeps=max(args.steps, 1))
+    N, L = d["G"].shape[1], d["G"].shape[0]
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "updates/s", "n_gpus": args.gpus,
+            "steps": ns, "warmup": 1, "ms_per_step": 1e3 * dt / ns, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64/f32 (reference CPU)", "data": "synthetic F-model, seeded",
+            "config": {"workload": f"{args.workload}: {SINGLE_DESC[args.workload]}; one step = one sweep",
+                       "chains": 1, "host_threads": 1},
+            "cpu_baseline": {"value": v, "unit": "updates/s", "cores": 1, "kind": "port",
+                             "sample": f"one chain, {ns} sweeps in {dt:.1f} s"},
+            "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- c5: serving
+def bench_serve(args):
+    import torch
+    from vcfpop_gb300 import _lib as B
+    from vcfpop_gb300 import structure as S
+    from vcfpop_gb300 import workloads as W
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    reqs = W.c5_requests(args.requests, seed=5 + rank, scale=args.c5_scale)
+    runs = []
+    for q in reqs:
+        packed, pop = gen_packed_gpu(q["seed"], q["N"], q["L"], P=q["pops"], F=0.05, miss=0.02)
+        ds = S.Dataset(np.full(q["N"], 2, np.int32), np.full(q["L"], 2, np.int32), pop, q["pops"], packed2=packed)
+        p = S.params(q["K"], q["seed"], admix=q["admix"], nburnin=q["nburnin"], nreps=q["nreps"], nadmburnin=0)
+        runs.append((q, ds, p))
+    upd = sum(ds.N * ds.L * q["K"] * (q["nburnin"] + q["nreps"]) for q, ds, p in runs)
+    h2d = sum(ds.L * ((ds.N + 15) // 16) * 4 + ds.L * 12 + ds.N * 12 for q, ds, p in runs)
+
+    def serve(max_active):
+        srv = S.Server(device=local, max_active=max_active, chunk=16)
+        ids = [None] * len(runs)
+        t0 = time.perf_counter()
+
+        def feeder():
+            for j, (q, ds, p) in enumerate(runs):
+                dt = t0 + q["t"] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                ids[j] = srv.submit(ds, p)
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        infos, lnl = [], []
+        for rid in ids:
+            inf = srv.wait(rid, 600.0)
+            assert inf["state"] == "done", inf
+            lnl.append(srv.result(rid)["rout"][0])
+            infos.append(inf)
+            srv.release(rid)
+        srv.close()
+        ttr = np.array([i["t_done"] - i["t_submit"] for i in infos])
+        span = max(i["t_done"] for i in infos) - min(i["t_submit"] for i in infos)
+        assert np.isfinite(lnl).all()
+        return {"updates_per_s": upd / span, "makespan_s": span, "p50_s": float(np.percentile(ttr, 50)),
+                "p99_s": float(np.percentile(ttr, 99)), "max_active": max_active}
+
+    with Clocks(local) as clk:
+        conc = serve(64)
+    alone = serve(1)
+    line = {"metric": METRIC, "value": conc["updates_per_s"] * world, "unit": "updates/s", "n_gpus": world,
+            "steps": 1, "warmup": 0, "ms_per_step": conc["makespan_s"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (lnP(D) accumulations in f64)",
+            "data": "synthetic F-model per run, seeded",
+            "config": {"workload": f"c5 serving: {len(runs)} independent runs, Poisson arrivals at 50/s, N log-uniform "
+                                   f"[{int(100 * args.c5_scale)}, {int(20000 * args.c5_scale)}], L log-uniform "
+                                   f"[{int(1000 * args.c5_scale)}, {int(200000 * args.c5_scale)}], K uniform 2..12, "
+                                   f"admixture p=0.5, {int(2000 * args.c5_scale)}-{int(20000 * args.c5_scale)} sweeps "
+                                   f"(ranges x{args.c5_scale} of the full case); one step = the whole stream",
+                       "form": "plain", "runs": len(runs), "updates_per_step": upd, "parallelism": "1 GPU"},
+            "serving": {"concurrent": conc, "one_at_a_time": alone},
+            "roofline": None, "cpu_baseline": None,
+            "e2e": {"value": conc["updates_per_s"] * world, "unit": "updates/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": 8 * len(runs),
+                    "step": "every run submitted from host buffers at its arrival time, uploaded, run, lnL read back"},
+            "gpu_launches": None, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- GPU leg
 def main():
     args = parse()
     if args.impl == "reference":
+        if args.workload in ("c1", "c2", "c4"):
+            return reference_single(args)
+        if args.workload == "c5":
+            print(json.dumps({"impl": "reference", "unavailable": "c5 reference arm: the reference runs one request "
+                              "at a time; bench.py --workload c5 reports that schedule on the GPU beside the "
+                              "concurrent one"}), flush=True)
+            return
         return reference_arm(args)
+    if args.workload in ("c1", "c2", "c4"):
+        return bench_single(args)
+    if args.workload == "c5":
+        return bench_serve(args)
     import torch
     import ctypes as C
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -215,8 +215,9 @@ int vp_loglik_packed2_noalloc(const uint32_t* geno, int32_t n_ind, int64_t n_loc
 /* The CUDA stream (cudaStream_t) every launch of this context goes to. */
 void* vp_stream(vp_ctx* ctx);
 /* Record CUDA events around each launch of the sweep's dominant kernel (the
- * likelihood stream of the plain form, the likelihood contraction of the
- * tensor-core form), also inside the cached sweep graphs. */
+ * likelihood stream of the plain no-admixture form, the per-copy label kernel
+ * of the admixture form, the likelihood contraction of the tensor-core form),
+ * also inside the cached sweep graphs. */
 int vp_prof_enable(vp_ctx* ctx, int on);
 /* Synchronise, then sum the dominant-kernel durations of the last sweep. */
 int vp_prof_read(vp_ctx* ctx, double* ms, int32_t* launches);

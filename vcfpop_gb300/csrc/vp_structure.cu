@@ -180,6 +180,8 @@ int launch_zadm_ctr(vp_chain* c, int force) {
     vp_ctx* x = c->ctx;
     dim3 g(cdiv(x->N, ZA_WARPS * 32), cdiv(x->L, c->h.zadm_lc), 1);
     size_t sm = zadm_smem(c);
+    prof_mark(x, true);
+    struct End { vp_ctx* x; ~End() { prof_mark(x, false); } } end_{x};
     switch (km_for(c->P.K)) {
         case 8: LAUNCH(x, k_update_z_admix_ctr<8>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
         case 16: LAUNCH(x, k_update_z_admix_ctr<16>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
@@ -221,11 +223,9 @@ int launch_step(vp_chain* c, int step, int force) {
         case VP_STEP_UPDATEQ: {
             const unsigned gi = cdiv(x->N, 256);
             if (!P.admix) {
-                if (!force || true) {
-                    int rc = launch_loglik(c, force);
-                    if (rc) return rc;
-                    LAUNCH(x, k_sample_noadmix, (dim3(ref ? 1 : c->h.nsampblk, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 0));
-                }
+                int rc = launch_loglik(c, force);
+                if (rc) return rc;
+                LAUNCH(x, k_sample_noadmix, (dim3(ref ? 1 : c->h.nsampblk, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 0));
                 if (c->h.nadmburnin > 0) LAUNCH(x, k_update_q_admix, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
             } else {
                 LAUNCH(x, k_update_q_admix, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));

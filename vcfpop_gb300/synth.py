@@ -28,13 +28,18 @@ def _drift(rng, anc, F):
 def fmodel(seed: int, n_ind: int, n_loc: int, n_pop: int, F: float,
            missing: float, admix_alpha: float | None = None,
            ploidy=2, n_alleles=2, anc_alpha: float = 0.5,
-           loc_ids=None, loc_alpha: float | None = None, q_scale: float = 2.0):
+           loc_ids=None, loc_alpha: float | None = None, q_scale: float = 2.0,
+           per_locus_origin: bool = False):
     """Draw one F-model dataset.
 
     ploidy: int, or array of per-individual ploidies.
     n_alleles: int, or array of per-locus allele counts.
     admix_alpha: None for discrete populations (equal sizes), else Q_i ~ Dir(alpha).
     loc_ids/loc_alpha: location ancestry Dir(loc_alpha) and Q_i ~ Dir(q_scale * loc ancestry).
+    per_locus_origin: draw the source population of every allele copy at every
+      locus from Q_i (the admixture model); otherwise one source per copy
+      slot of an individual across all loci (the committed golden fixtures
+      were drawn that way).
     Returns dict(G=int8[L,N,vmax], pop=int32[N], ploidy=int32[N], k=int32[L], Q=float[N,P]).
     """
     rng = np.random.default_rng(seed)
@@ -65,6 +70,17 @@ def fmodel(seed: int, n_ind: int, n_loc: int, n_pop: int, F: float,
     cumf = np.cumsum(popf, axis=2)  # [P, L, kmax]
     for c in range(vmax):
         has = ploidy > c
+        if per_locus_origin:
+            chunk = max(1, (1 << 22) // max(1, n_ind * kmax))
+            for l0 in range(0, n_loc, chunk):
+                l1 = min(n_loc, l0 + chunk)
+                u = rng.random((l1 - l0, n_ind))
+                src = np.minimum((u[:, :, None] > cumQ[None]).sum(axis=2), n_pop - 1)  # [Lc, N]
+                cf = cumf[src, np.arange(l0, l1)[:, None], :]                          # [Lc, N, kmax]
+                ua = rng.random((l1 - l0, n_ind))
+                al = np.minimum((ua[:, :, None] > cf).sum(axis=2), (k[l0:l1] - 1)[:, None])
+                G[l0:l1, has, c] = al[:, has]
+            continue
         u = rng.random(n_ind)
         src = np.minimum((u[:, None] > cumQ).sum(axis=1), n_pop - 1)  # origin of this copy
         ua = rng.random((n_loc, n_ind))
