@@ -578,7 +578,7 @@ def main():
 
     line = {"metric": METRIC, "value": value, "unit": "updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16 hi+lo x bf16 counts -> f32 (lnP(D) in f64)" if form else "f32",
+            "vs_baseline": None, "dtype": "likelihood bf16 hi+lo x bf16 counts -> f32; counts e4m3 x e4m3 -> f32 (exact); lnP(D) in f64" if form else "f32",
             "data": "synthetic F-model (8 pops, F=0.03, Beta(0.5,0.5) ancestry, 1% missing), seeded",
             "config": {"workload": f"batched K-sweep: N={N_IND}, L={ds.L} biallelic SNPs, K=1..10 x 10 replicates "
                                    f"= 100 no-admixture chains, one sweep of all chains per step",

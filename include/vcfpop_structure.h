@@ -179,13 +179,19 @@ int vp_tc_status(vp_ctx* ctx);
 int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int32_t M, int32_t N, int32_t K,
                        int32_t BN, int32_t piece, int32_t splits, int32_t stages, int32_t mt, int32_t bk, float* D);
 
+/* Diagnostic: D[m][n] = sum_k A[m,k] B[n,k] with e4m3 operands (raw bytes,
+ * A [M][K], B [N][K]) through the kernel's kind::f8f6f4 form, the one the
+ * count contraction uses; K % 128 == 0. No reference counterpart. */
+int vp_debug_gemm_e4m3(const uint8_t* A, const uint8_t* B, int32_t M, int32_t N, int32_t K, int32_t BN, int32_t piece,
+                       int32_t stages, int32_t mt, float* D);
+
 /* Diagnostic: average device time in ms of `iters` launches of the
- * contraction kernel on operands it allocates and fills itself (nb B operands;
- * mode 0 FP32 partials [splits][M][N], mode 1 int32 transpose [N][M] with
- * splits == 1). Shape rules as vp_debug_gemm_bf16. Used to choose tile and
- * pipeline parameters; no reference counterpart. */
+ * contraction kernel on operands it allocates and fills itself (esz 2 bf16 or
+ * 1 e4m3; nb B operands; mode 0 FP32 partials [splits][M][N], mode 1 int32
+ * transpose [N][M] with splits == 1; bk * esz = 64 or 128). Used to choose
+ * tile and pipeline parameters; no reference counterpart. */
 int vp_debug_gemm_time(int32_t M, int32_t N, int32_t K, int32_t BN, int32_t piece, int32_t splits, int32_t stages,
-                       int32_t mt, int32_t bk, int32_t nb, int32_t mode, int32_t iters, double* ms);
+                       int32_t mt, int32_t bk, int32_t esz, int32_t nb, int32_t mode, int32_t iters, double* ms);
 
 /* The likelihood accumulation of UpdateQNoAdmix (src/structure.cpp:902-932;
  * the part BAYESIAN<REAL>::UpdateQNoAdmixCUDA offloads, src/structureCUDA.cpp:

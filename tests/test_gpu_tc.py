@@ -56,6 +56,26 @@ def test_gemm_matches_float64(M, N, K, BN, piece, nb, splits, stages, mt, bk):
     assert err < 1e-5, err
 
 
+E4M3 = {0: 0x00, 1: 0x38, 2: 0x40, 3: 0x44, 4: 0x48}   # small integers, exact in e4m3
+
+
+@pytest.mark.parametrize("M,N,K,stages", [(300, 384, 1024, 4), (130, 192, 128, 2), (640, 576, 2048, 3)])
+def test_gemm_e4m3_counts_exact(M, N, K, stages):
+    """The count contraction's kind::f8f6f4 form: allele counts 0..2 times
+    one-hot labels, summed exactly in FP32."""
+    rng = np.random.default_rng(M * 7 + K)
+    A = rng.integers(0, 3, (M, K))
+    lab = rng.integers(0, N, K)
+    Bm = np.zeros((N, K), np.int64)
+    Bm[lab, np.arange(K)] = 1
+    enc = np.vectorize(E4M3.get)
+    A8 = np.ascontiguousarray(enc(A).astype(np.uint8))
+    B8 = np.ascontiguousarray(enc(Bm).astype(np.uint8))
+    D = np.zeros((M, N), np.float32)
+    B.check(B.lib().vp_debug_gemm_e4m3(A8.ctypes.data, B8.ctypes.data, M, N, K, 192, 192, stages, 2, D.ctypes.data))
+    assert np.array_equal(D.astype(np.int64), A @ Bm.T)
+
+
 def test_batched_tc_sweep_matches_plain():
     """Same Ni, same Philox draws: the tensor-core sweep and the plain FP32 sweep
     give the same frequencies, near-identical likelihoods, and the same labels

@@ -72,7 +72,7 @@ _lib = None
 EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_dataset_free", "vp_open",
            "vp_close", "vp_sync", "vp_params_default", "vp_run_seed", "vp_chain_create", "vp_chain_destroy",
            "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_step", "vp_chain_get",
-           "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
+           "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
            "vp_release", "vp_server_close"]
 
@@ -113,7 +113,8 @@ def lib():
     L.vp_last_error.restype = C.c_char_p
     L.vp_tc_status.argtypes = [P]
     L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 9 + [P]
-    L.vp_debug_gemm_time.argtypes = [C.c_int32] * 12 + [P]
+    L.vp_debug_gemm_time.argtypes = [C.c_int32] * 13 + [P]
+    L.vp_debug_gemm_e4m3.argtypes = [P, P] + [C.c_int32] * 7 + [P]
     L.vp_stream.argtypes = [P]
     L.vp_stream.restype = P
     L.vp_prof_enable.argtypes = [P, C.c_int]

@@ -241,6 +241,42 @@ struct Philox {
         if (small) g *= powf(uniformf(), 1.f / alpha);
         return g;
     }
+    // Two independent gamma(a0, 1), gamma(a1, 1) draws (a Beta draw for a
+    // biallelic locus). The first Marsaglia-Tsang attempt of both takes one
+    // Philox block: the cosine and sine normals of one Box-Muller pair and
+    // two acceptance uniforms; an attempt that is rejected (rare for shapes
+    // >= 1) continues as gammaf does, on further blocks.
+    __device__ inline void gamma2(float a0, float a1, float& g0, float& g1) {
+        const bool s0 = a0 < 1.f, s1 = a1 < 1.f;
+        const float b0 = s0 ? a0 + 1.f : a0, b1 = s1 ? a1 + 1.f : a1;
+        const float d0 = b0 - 1.f / 3.f, c0 = rsqrtf(9.f * d0);
+        const float d1 = b1 - 1.f / 3.f, c1 = rsqrtf(9.f * d1);
+        const float u1 = uniformf(), u2 = uniformf(), u3 = uniformf(), u4 = uniformf();
+        const float r = sqrtf(-2.0f * logf(u1));
+        float sn, cs;
+        sincospif(2.0f * u2, &sn, &cs);
+        const bool ok0 = mt_accept(d0, c0, r * cs, u3, g0);
+        const bool ok1 = mt_accept(d1, c1, r * sn, u4, g1);
+        if (!ok0) g0 = mt_more(d0, c0);
+        if (!ok1) g1 = mt_more(d1, c1);
+        if (s0) g0 *= powf(uniformf(), 1.f / a0);
+        if (s1) g1 *= powf(uniformf(), 1.f / a1);
+    }
+    // one Marsaglia-Tsang attempt with normal t and uniform u
+    __device__ static inline bool mt_accept(float d, float c, float t, float u, float& g) {
+        float v = 1.f + c * t;
+        if (v <= 0.f) return false;
+        v = v * v * v;
+        g = d * v;
+        if (u < 1.f - 0.0331f * t * t * t * t) return true;
+        return logf(u) < 0.5f * t * t + d * (1.f - v + logf(v));
+    }
+    __device__ inline float mt_more(float d, float c) {
+        float g = d;
+        for (int it = 0; it < 64; ++it)
+            if (mt_accept(d, c, normalf(), uniformf(), g)) break;
+        return g;
+    }
 };
 
 }  // namespace vp

@@ -276,10 +276,16 @@ __global__ void k_update_p_ctr(const DevChain* chains) {
     ph.init(c.seed, ST_P | ((uint32_t)m << 4), (uint32_t)kl, (uint32_t)(kl >> 32));
     float p[64];
     float s = 0;
-    for (int a = 0; a < k2; ++a) {
-        float v = ph.gammaf(prior_of(c, k, D.off[l] + a) + (float)c.Ni[j + a]);
-        p[a] = v;
-        s += v;
+    if (k2 == 2) {
+        // the same draws as the batched tensor-core UpdateP
+        ph.gamma2(prior_of(c, k, D.off[l]) + (float)c.Ni[j], prior_of(c, k, D.off[l] + 1) + (float)c.Ni[j + 1], p[0], p[1]);
+        s = p[0] + p[1];
+    } else {
+        for (int a = 0; a < k2; ++a) {
+            float v = ph.gammaf(prior_of(c, k, D.off[l] + a) + (float)c.Ni[j + a]);
+            p[a] = v;
+            s += v;
+        }
     }
     float inv = 1.f / s;
     for (int a = 0; a < k2; ++a) { p[a] *= inv; c.Freq[j + a] = p[a]; }

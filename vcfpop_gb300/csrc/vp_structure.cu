@@ -14,9 +14,11 @@ using namespace vp;
 
 struct TcOperands {
     bool ready = false;
-    int bk = 64;              // K elements per pipeline stage of both contractions
+    int bk = 64;              // bf16 K elements per pipeline stage of the likelihood contraction
+    int bk8 = 128;            // e4m3 K elements per stage of the count contraction
     int64_t Apad = 0, Npad = 0;
-    __nv_bfloat16 *C = nullptr, *CT = nullptr;
+    __nv_bfloat16* C = nullptr;   // [Npad][Apad] bf16 counts: the likelihood contraction's A
+    uint8_t* CT = nullptr;        // [Apad][Npad] e4m3 counts: the count contraction's A
     float* logpbar = nullptr;
     double* Bc = nullptr;
     int* err = nullptr;
@@ -71,7 +73,8 @@ struct TcBatch {
     // pipeline of the likelihood (1) and count (2) contractions: 128-row A
     // tiles per CTA and shared-memory stages of bk K elements
     int mt1 = 2, st1 = 2, mt2 = 2, st2 = 4;
-    __nv_bfloat16 *Whi = nullptr, *Wlo = nullptr, *OH = nullptr;
+    __nv_bfloat16 *Whi = nullptr, *Wlo = nullptr;
+    uint8_t* OH = nullptr;
     float* LLpart = nullptr;
     int32_t* NiAll = nullptr;
     CUtensorMap mapWhi, mapWlo, mapOH;
@@ -764,29 +767,32 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 2-D bf16 row-major [rows][ld] map with box_cols x box_rows boxes; 64-column
-// boxes (128-byte rows) use the 128-byte swizzle, 32-column boxes the 64-byte one
+// 2-D row-major [rows][ld] map of bf16 (esz 2) or bytes (esz 1) with
+// box_cols x box_rows boxes; 128-byte box rows use the 128-byte swizzle,
+// 64-byte rows the 64-byte one
 int make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows,
-             uint32_t box_cols) {
-    if (box_cols != 64 && box_cols != 32) { vp_set_error("box width must be 32 or 64 columns"); return VP_E_ARG; }
+             uint32_t box_cols, int esz = 2) {
+    const uint32_t rowb = box_cols * esz;
+    if ((rowb != 64 && rowb != 128) || (esz != 1 && esz != 2)) { vp_set_error("box rows must be 64 or 128 bytes"); return VP_E_ARG; }
     EncodeTiledFn f = encode_fn();
     if (!f) { vp_set_error("cuTensorMapEncodeTiled unavailable"); return VP_E_CUDA; }
     cuuint64_t dims[2] = {cols, rows};
-    cuuint64_t strides[1] = {ld * 2};
+    cuuint64_t strides[1] = {ld * esz};
     cuuint32_t box[2] = {box_cols, box_rows};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_cols == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+    CUresult r = f(m, esz == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 2,
+                   const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, rowb == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { vp_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return VP_E_CUDA; }
     return VP_OK;
 }
 
-template <int BKT, int MT, int NB, int BNT, int PIECE>
+template <int BKT, int ESZ, int MT, int NB, int BNT, int PIECE>
 int launch_gemm_t(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CUtensorMap& B1, const tc::GemmArgs& g,
                   dim3 grid, size_t sm) {
-    auto kern = tc::k_gemm_bf16<BKT, MT, NB, BNT, PIECE>;
+    auto kern = tc::k_gemm_bf16<BKT, ESZ, MT, NB, BNT, PIECE>;
     static bool attr = false;
     if (!attr) {
         CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
@@ -796,26 +802,29 @@ int launch_gemm_t(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const 
     return check_launch(x, "k_gemm_bf16");
 }
 
-// the tile shapes compiled into the library (stage depth, 128-row A tiles
-// per CTA, B operands, columns per CTA, columns per MMA)
-#define VP_GEMM_TILES(X)          \
-    X(64, 2, 2, 192, 192)         \
-    X(64, 2, 1, 192, 192)         \
-    X(64, 1, 2, 288, 144)         \
-    X(64, 1, 1, 256, 256)         \
-    X(32, 2, 2, 192, 192)
+// the tile shapes compiled into the library (K elements per stage, element
+// bytes, 128-row A tiles per CTA, B operands, columns per CTA, columns per MMA)
+#define VP_GEMM_TILES(X)             \
+    X(64, 2, 2, 2, 192, 192)         \
+    X(64, 2, 2, 1, 192, 192)         \
+    X(128, 1, 2, 1, 192, 192)        \
+    X(64, 2, 1, 2, 288, 144)         \
+    X(64, 2, 1, 1, 256, 256)         \
+    X(32, 2, 2, 2, 192, 192)
 
 int launch_gemm(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CUtensorMap& B1, tc::GemmArgs g,
                 dim3 grid) {
-    if (g.bk != 32 && g.bk != 64) { vp_set_error("gemm stage depth must be 32 or 64"); return VP_E_ARG; }
-    size_t sm = tc::gemm_smem_bytes(g.BN, g.nb, g.stages, g.mt, g.bk);
+    if (g.esz != 1 && g.esz != 2) { vp_set_error("gemm element size must be 1 or 2 bytes"); return VP_E_ARG; }
+    if (g.bk * g.esz != 64 && g.bk * g.esz != 128) { vp_set_error("gemm stage rows must be 64 or 128 bytes"); return VP_E_ARG; }
+    size_t sm = tc::gemm_smem_bytes(g.BN, g.nb, g.stages, g.mt, g.bk, g.esz);
     if (sm > 227 * 1024) { vp_set_error("gemm tile needs %zu bytes of shared memory", sm); return VP_E_ARG; }
-#define VP_GEMM_CASE(bk_, mt_, nb_, bn_, pc_)                                               \
-    if (g.bk == bk_ && g.mt == mt_ && g.nb == nb_ && g.BN == bn_ && g.piece == pc_)        \
-        return launch_gemm_t<bk_, mt_, nb_, bn_, pc_>(x, A, B0, B1, g, grid, sm);
+#define VP_GEMM_CASE(bk_, es_, mt_, nb_, bn_, pc_)                                                        \
+    if (g.bk == bk_ && g.esz == es_ && g.mt == mt_ && g.nb == nb_ && g.BN == bn_ && g.piece == pc_)      \
+        return launch_gemm_t<bk_, es_, mt_, nb_, bn_, pc_>(x, A, B0, B1, g, grid, sm);
     VP_GEMM_TILES(VP_GEMM_CASE)
 #undef VP_GEMM_CASE
-    vp_set_error("gemm tile (bk %d, mt %d, nb %d, BN %d, piece %d) is not compiled in", g.bk, g.mt, g.nb, g.BN, g.piece);
+    vp_set_error("gemm tile (bk %d, esz %d, mt %d, nb %d, BN %d, piece %d) is not compiled in", g.bk, g.esz, g.mt, g.nb,
+                 g.BN, g.piece);
     return VP_E_ARG;
 }
 
@@ -826,7 +835,7 @@ int tc_operands(vp_ctx* x) {
     const int64_t A = 2 * x->L;
     t.Apad = (A + 63) / 64 * 64;
     t.Npad = (x->N + 127) / 128 * 128;
-    size_t bytes = (size_t)t.Npad * t.Apad * 2 * 2 + t.Apad * 4 + t.Npad * 8 + 256;
+    size_t bytes = (size_t)t.Npad * t.Apad * 2 + (size_t)t.Npad * t.Apad + 256 + t.Apad * 4 + t.Npad * 8 + 256;
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, bytes);
     if (e != cudaSuccess) { vp_set_error("cudaMalloc(%zu) for tensor-core operands: %s", bytes, cudaGetErrorString(e)); return VP_E_MEM; }
@@ -834,7 +843,7 @@ int tc_operands(vp_ctx* x) {
     CK(cudaMemsetAsync(p, 0, bytes, x->stream));
     char* q = (char*)p;
     t.C = (__nv_bfloat16*)q; q += (size_t)t.Npad * t.Apad * 2;
-    t.CT = (__nv_bfloat16*)q; q += (size_t)t.Npad * t.Apad * 2;
+    t.CT = (uint8_t*)q; q += ((size_t)t.Npad * t.Apad + 255) / 256 * 256;
     t.logpbar = (float*)q; q += t.Apad * 4;
     t.Bc = (double*)q; q += t.Npad * 8;
     t.err = (int*)q;
@@ -847,7 +856,7 @@ int tc_operands(vp_ctx* x) {
     tc::k_center_const<<<cdiv((int64_t)x->N * 32, 256), 256, 0, x->stream>>>(x->D, t.logpbar, t.Bc);
     if ((rc = check_launch(x, "k_center_const"))) return rc;
     if ((rc = make_map(&t.mapC, t.C, t.Npad, t.Apad, t.Apad, 128, t.bk))) return rc;
-    if ((rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128, t.bk))) return rc;
+    if ((rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128, t.bk8, 1))) return rc;
     t.ready = true;
     return VP_OK;
 }
@@ -921,7 +930,7 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
         b->row0 = cv.take<int32_t>(n);
         b->Whi = cv.take<__nv_bfloat16>((int64_t)b->Rpad * t.Apad);
         b->Wlo = cv.take<__nv_bfloat16>((int64_t)b->Rpad * t.Apad);
-        b->OH = cv.take<__nv_bfloat16>((int64_t)b->Rpad * t.Npad);
+        b->OH = cv.take<uint8_t>((int64_t)b->Rpad * t.Npad);
         b->LLpart = cv.take<float>((int64_t)b->splits * x->N * b->Rpad);
         b->NiAll = cv.take<int32_t>((int64_t)b->Rpad * x->KT);
     };
@@ -946,7 +955,7 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
     }
     if ((rc = make_map(&b->mapWhi, b->Whi, b->Rpad, t.Apad, t.Apad, b->piece, t.bk)) ||
         (rc = make_map(&b->mapWlo, b->Wlo, b->Rpad, t.Apad, t.Apad, b->piece, t.bk)) ||
-        (rc = make_map(&b->mapOH, b->OH, b->Rpad, t.Npad, t.Npad, b->piece, t.bk))) {
+        (rc = make_map(&b->mapOH, b->OH, b->Rpad, t.Npad, t.Npad, b->piece, t.bk8, 1))) {
         x->batch = b;
         free_batch(x);
         return rc;
@@ -978,7 +987,7 @@ int launch_tc_sweep(vp_ctx* x) {
         tc::GemmArgs g{};
         g.M = x->N; g.N = b->Rpad; g.kblocks = (int)(t.Apad / t.bk);
         g.kb_per_split = (g.kblocks + b->splits - 1) / b->splits;
-        g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.mt = b->mt1; g.stages = b->st1; g.bk = t.bk; g.mode = 0;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.mt = b->mt1; g.stages = b->st1; g.bk = t.bk; g.esz = 2; g.mode = 0;
         g.out_f = b->LLpart; g.ldo = b->Rpad; g.err = t.err;
         prof_mark(x, true);
         int rc = launch_gemm(x, t.mapC, b->mapWhi, b->mapWlo, g, dim3(cdiv(t.Npad, 128 * b->mt1), b->G, b->splits));
@@ -990,10 +999,13 @@ int launch_tc_sweep(vp_ctx* x) {
     // count contraction: Ni[row, a] = sum_i OH[row, i] C[i, a]
     {
         tc::GemmArgs g{};
-        g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / t.bk); g.kb_per_split = g.kblocks;
-        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.mt = b->mt2; g.stages = b->st2; g.bk = t.bk; g.mode = 1;
+        g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / t.bk8); g.kb_per_split = g.kblocks;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.mt = b->mt2; g.stages = b->st2; g.bk = t.bk8; g.esz = 1; g.mode = 1;
         g.out_i = b->NiAll; g.ldo = x->KT; g.err = t.err;
-        int rc = launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, dim3(cdiv(t.Apad, 128 * b->mt2), b->G, 1));
+        const unsigned mtiles = cdiv(t.Apad, 128 * b->mt2);
+        g.group_major = mtiles <= 65535;     // grid.y limit; otherwise row tiles on x
+        const dim3 grid = g.group_major ? dim3(b->G, mtiles, 1) : dim3(mtiles, b->G, 1);
+        int rc = launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, grid);
         if (rc) return rc;
     }
     // Record for every chain, then m += 1
@@ -1073,7 +1085,7 @@ extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const u
     if (!rc) {
         tc::GemmArgs g{};
         g.M = M; g.N = N; g.kblocks = K / bk; g.kb_per_split = (g.kblocks + splits - 1) / splits;
-        g.BN = BN; g.piece = piece; g.nb = B1 ? 2 : 1; g.mt = mt; g.stages = stages; g.bk = bk; g.mode = 0;
+        g.BN = BN; g.piece = piece; g.nb = B1 ? 2 : 1; g.mt = mt; g.stages = stages; g.bk = bk; g.esz = 2; g.mode = 0;
         g.out_f = (float*)dD; g.ldo = N; g.err = err;
         rc = launch_gemm(&tmp, ma, mb0, mb1, g, dim3((unsigned)(Mp / (128 * mt)), N / BN, splits));
     }
@@ -1093,10 +1105,59 @@ extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const u
     return rc;
 }
 
+extern "C" int vp_debug_gemm_e4m3(const uint8_t* A, const uint8_t* B, int32_t M, int32_t N, int32_t K, int32_t BN,
+                                  int32_t piece, int32_t stages, int32_t mt, float* D) {
+    if (!A || !B || !D || M <= 0 || N <= 0 || K <= 0 || K % 128 || N % BN || BN % piece || piece % 16 || piece > 256 ||
+        (mt != 1 && mt != 2) || BN * mt > 512) {
+        vp_set_error("vp_debug_gemm_e4m3: bad shape");
+        return VP_E_ARG;
+    }
+    vp_ctx tmp;
+    cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking);
+    const int64_t Mp = (M + 128 * mt - 1) / (128 * mt) * (128 * mt);
+    void *dA = nullptr, *dB = nullptr, *dD = nullptr;
+    int* err = nullptr;
+    int rc = VP_OK;
+    do {
+        cudaError_t ce;
+        if ((ce = cudaMalloc(&dA, (size_t)Mp * K)) != cudaSuccess || (ce = cudaMalloc(&dB, (size_t)N * K)) != cudaSuccess ||
+            (ce = cudaMalloc(&dD, (size_t)M * N * 4)) != cudaSuccess || (ce = cudaMalloc(&err, 4)) != cudaSuccess) {
+            vp_set_error("vp_debug_gemm_e4m3: %s", cudaGetErrorString(ce));
+            rc = VP_E_MEM;
+            break;
+        }
+        cudaMemset(dA, 0, (size_t)Mp * K);
+        cudaMemset(err, 0, 4);
+        cudaMemcpy(dA, A, (size_t)M * K, cudaMemcpyHostToDevice);
+        cudaMemcpy(dB, B, (size_t)N * K, cudaMemcpyHostToDevice);
+        CUtensorMap ma, mb;
+        if ((rc = make_map(&ma, dA, Mp, K, K, 128, 128, 1)) || (rc = make_map(&mb, dB, N, K, K, piece, 128, 1))) break;
+        tc::GemmArgs g{};
+        g.M = M; g.N = N; g.kblocks = K / 128; g.kb_per_split = g.kblocks;
+        g.BN = BN; g.piece = piece; g.nb = 1; g.mt = mt; g.stages = stages; g.bk = 128; g.esz = 1; g.mode = 0;
+        g.out_f = (float*)dD; g.ldo = N; g.err = err; g.group_major = 1;   // the count contraction's order
+        if ((rc = launch_gemm(&tmp, ma, mb, mb, g, dim3(N / BN, (unsigned)(Mp / (128 * mt)), 1)))) break;
+        if ((ce = cudaStreamSynchronize(tmp.stream)) != cudaSuccess) {
+            vp_set_error("gemm: %s", cudaGetErrorString(ce));
+            rc = VP_E_CUDA;
+            break;
+        }
+        int e = 0;
+        cudaMemcpy(&e, err, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(D, dD, (size_t)M * N * 4, cudaMemcpyDeviceToHost);
+        if (e) { vp_set_error("gemm pipeline timed out (code %d)", e); rc = VP_E_CUDA; }
+    } while (0);
+    cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(err);
+    cudaStreamDestroy(tmp.stream);
+    tmp.stream = nullptr;
+    return rc;
+}
+
 extern "C" int vp_debug_gemm_time(int32_t M, int32_t N, int32_t K, int32_t BN, int32_t piece, int32_t splits,
-                                  int32_t stages, int32_t mt, int32_t bk, int32_t nb, int32_t mode, int32_t iters,
-                                  double* ms) {
-    if (!ms || M <= 0 || N <= 0 || K <= 0 || (bk != 32 && bk != 64) || K % bk || N % BN || BN % piece ||
+                                  int32_t stages, int32_t mt, int32_t bk, int32_t esz, int32_t nb, int32_t mode,
+                                  int32_t iters, double* ms) {
+    if (!ms || M <= 0 || N <= 0 || K <= 0 || (esz != 1 && esz != 2) || (bk * esz != 64 && bk * esz != 128) || K % bk ||
+        N % BN || BN % piece ||
         piece % 16 || piece > 256 || (mt != 1 && mt != 2) || BN * mt > 512 || splits < 1 || (nb != 1 && nb != 2) ||
         (mode != 0 && mode != 1) || (mode == 1 && splits != 1) || iters < 1) {
         vp_set_error("vp_debug_gemm_time: bad shape");
@@ -1112,26 +1173,29 @@ extern "C" int vp_debug_gemm_time(int32_t M, int32_t N, int32_t K, int32_t BN, i
     do {
         cudaError_t ce;
         const size_t outb = mode == 0 ? (size_t)splits * M * N * 4 : (size_t)N * M * 4;
-        if ((ce = cudaMalloc(&dA, (size_t)Mp * K * 2)) != cudaSuccess || (ce = cudaMalloc(&dB, (size_t)2 * N * K * 2)) != cudaSuccess ||
+        if ((ce = cudaMalloc(&dA, (size_t)Mp * K * esz)) != cudaSuccess ||
+            (ce = cudaMalloc(&dB, (size_t)2 * N * K * esz)) != cudaSuccess ||
             (ce = cudaMalloc(&dD, outb)) != cudaSuccess || (ce = cudaMalloc(&err, 4)) != cudaSuccess) {
             vp_set_error("vp_debug_gemm_time: %s", cudaGetErrorString(ce));
             rc = VP_E_MEM;
             break;
         }
-        // small bf16 values (0x3C3C ~ 0.0115): the timing does not depend on them
-        cudaMemsetAsync(dA, 0x3C, (size_t)Mp * K * 2, tmp.stream);
-        cudaMemsetAsync(dB, 0x3C, (size_t)2 * N * K * 2, tmp.stream);
+        // small values (bf16 0x3C3C ~ 0.0115, e4m3 0x3C = 1.5): the timing does not depend on them
+        cudaMemsetAsync(dA, 0x3C, (size_t)Mp * K * esz, tmp.stream);
+        cudaMemsetAsync(dB, 0x3C, (size_t)2 * N * K * esz, tmp.stream);
         cudaMemsetAsync(err, 0, 4, tmp.stream);
         CUtensorMap ma, mb0, mb1;
-        const uint16_t* b1 = (const uint16_t*)dB + (size_t)N * K;
-        if ((rc = make_map(&ma, dA, Mp, K, K, 128, bk)) || (rc = make_map(&mb0, dB, N, K, K, piece, bk)) ||
-            (rc = make_map(&mb1, b1, N, K, K, piece, bk)))
+        const char* b1 = (const char*)dB + (size_t)N * K * esz;
+        if ((rc = make_map(&ma, dA, Mp, K, K, 128, bk, esz)) || (rc = make_map(&mb0, dB, N, K, K, piece, bk, esz)) ||
+            (rc = make_map(&mb1, b1, N, K, K, piece, bk, esz)))
             break;
         tc::GemmArgs g{};
         g.M = M; g.N = N; g.kblocks = K / bk; g.kb_per_split = (g.kblocks + splits - 1) / splits;
-        g.BN = BN; g.piece = piece; g.nb = nb; g.mt = mt; g.stages = stages; g.bk = bk; g.mode = mode;
+        g.BN = BN; g.piece = piece; g.nb = nb; g.mt = mt; g.stages = stages; g.bk = bk; g.esz = esz; g.mode = mode;
         g.out_f = (float*)dD; g.out_i = (int32_t*)dD; g.ldo = mode == 0 ? N : M; g.err = err;
-        const dim3 grid((unsigned)(Mp / (128 * mt)), N / BN, splits);
+        g.group_major = mode == 1 && Mp / (128 * mt) <= 65535;   // as the count contraction
+        const dim3 grid = g.group_major ? dim3(N / BN, (unsigned)(Mp / (128 * mt)), splits)
+                                        : dim3((unsigned)(Mp / (128 * mt)), N / BN, splits);
         if ((rc = launch_gemm(&tmp, ma, mb0, mb1, g, grid))) break;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);

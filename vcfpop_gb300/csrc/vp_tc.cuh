@@ -37,8 +37,11 @@ struct GemmArgs {
     int nb;                 // 1 or 2 B operands
     int mt;                 // 128-row A tiles per CTA sharing the B tile (1 or 2)
     int stages;
-    int bk;                 // K elements per stage: 64 (128-byte swizzle rows) or 32 (64-byte rows)
+    int bk;                 // K elements per stage (rows of bk * esz bytes: 128 or 64)
+    int esz;                // element bytes: 2 bf16 (kind::f16), 1 e4m3 (kind::f8f6f4)
     int mode;               // 0: FP32 partials D[z][m][n]; 1: int32 transpose Dt[n][m] (no split)
+    int group_major;        // 1: blockIdx.x is the column group and blockIdx.y the row tile, so the
+                            //    groups that share an A tile run side by side and A streams from DRAM once
     float* out_f;           // mode 0: [splits][M][ldo]
     int32_t* out_i;         // mode 1: [N][ldo]
     int64_t ldo;
@@ -78,22 +81,29 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
-// shared-memory matrix descriptor: K-major, rows of bk bf16 (128 or 64
-// bytes) with the matching swizzle, 8-row groups 8 rows apart (SBO), sm100
+// shared-memory matrix descriptor: K-major, rows of `row` bytes (128 or 64)
+// with the matching swizzle, 8-row groups 8 rows apart (SBO), sm100
 // descriptor version 1
-__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr, int bk) {
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr, int row) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFF);
     d |= (uint64_t)1 << 16;                                 // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)((8 * bk * 2) >> 4) << 32;               // stride byte offset
+    d |= (uint64_t)((8 * row) >> 4) << 32;                  // stride byte offset
     d |= (uint64_t)1 << 46;                                 // version
-    d |= (uint64_t)(bk == 64 ? 2 : 4) << 61;                // SWIZZLE_128B or SWIZZLE_64B
+    d |= (uint64_t)(row == 128 ? 2 : 4) << 61;              // SWIZZLE_128B or SWIZZLE_64B
     return d;
 }
 
-// instruction descriptor (D f32, A bf16, B bf16, both K-major, M = 128):
-// bits 4-5 D format, 7-9 A format, 10-12 B format, 17-22 N/8, 24-28 M/16
+// instruction descriptor (D f32, both operands K-major, M = 128): bits 4-5
+// D format (1 = f32), 7-9 A format and 10-12 B format (kind::f16: 1 = bf16;
+// kind::f8f6f4: 0 = e4m3), 17-22 N/8, 24-28 M/16
 
+// kind::f8f6f4 (e4m3 x e4m3 -> f32): 32 K elements (32 bytes) per instruction
+__device__ __forceinline__ void mma_e4m3(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
 __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
@@ -122,18 +132,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // shape fixed each MMA is two descriptor additions and the instruction
 // (rebuilding descriptors from runtime sizes made that thread, not the
 // tensor core, the limit).
-template <int BKT, int MT, int NB, int BNT, int PIECE>
+template <int BKT, int ESZ, int MT, int NB, int BNT, int PIECE>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_gemm_bf16(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB0,
                 const __grid_constant__ CUtensorMap mapB1, GemmArgs g) {
-    static_assert(BKT == 32 || BKT == 64, "stage depth");
+    constexpr int ROW = BKT * ESZ;    // bytes per K row of a stage
+    static_assert((ROW == 64 || ROW == 128) && (ESZ == 1 || ESZ == 2), "stage depth");
     static_assert(BNT % PIECE == 0 && PIECE % 16 == 0 && PIECE <= 256 && MT * BNT <= 512, "tile");
-    constexpr uint32_t A_TILE = BM * BKT * 2;
+    constexpr uint32_t A_TILE = BM * ROW;
     constexpr uint32_t A_BYTES = A_TILE * MT;
-    constexpr uint32_t B_BYTES = BNT * BKT * 2;
+    constexpr uint32_t B_BYTES = BNT * ROW;
     constexpr uint32_t STAGE = A_BYTES + B_BYTES * NB;
     constexpr uint32_t NCOLS = MT * BNT <= 32 ? 32 : MT * BNT <= 64 ? 64 : MT * BNT <= 128 ? 128 : MT * BNT <= 256 ? 256 : 512;
-    constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(PIECE >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+    constexpr uint32_t FMT = ESZ == 2 ? 1u : 0u;   // bf16 / e4m3
+    constexpr uint32_t IDESC = (1u << 4) | (FMT << 7) | (FMT << 10) | ((uint32_t)(PIECE >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -144,8 +156,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     uint32_t* tmem_holder = (uint32_t*)(accum + 1);
     int* abort_flag = (int*)(tmem_holder + 1);
 
-    const int m0 = blockIdx.x * BM * MT;
-    const int n0 = blockIdx.y * BNT;
+    const int m0 = (g.group_major ? blockIdx.y : blockIdx.x) * BM * MT;
+    const int n0 = (g.group_major ? blockIdx.x : blockIdx.y) * BNT;
     const int kb0 = blockIdx.z * g.kb_per_split;
     const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
     const int nk = kb1 - kb0;
@@ -187,7 +199,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 for (int b = 0; b < NB; ++b)
 #pragma unroll
                     for (int p = 0; p < BNT; p += PIECE)
-                        tma_load_2d(st + A_BYTES + b * B_BYTES + p * BKT * 2, b == 0 ? &mapB0 : &mapB1, &full[s], kx,
+                        tma_load_2d(st + A_BYTES + b * B_BYTES + p * ROW, b == 0 ? &mapB0 : &mapB1, &full[s], kx,
                                     n0 + p);
                 issued = it + 1;
             }
@@ -201,7 +213,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // descriptor of stage 0 at its first byte; the tiles' offsets are
             // added to the address field in 16-byte units (a shared-memory
             // address below 256 KB never carries out of its 14 bits)
-            const uint64_t d0 = sw_desc(smem_u32(smem), BKT);
+            const uint64_t d0 = sw_desc(smem_u32(smem), ROW);
             for (int it = 0; it < nk; ++it) {
                 const int s = it % stages;
                 if (!mbar_wait(&full[s], (it / stages) & 1) || *(volatile int*)abort_flag) {
@@ -212,8 +224,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint64_t ds = d0 + (uint64_t)((s * STAGE) >> 4);
                 const uint32_t acc0 = it != 0;
+                // one MMA consumes 32 bytes of K: 16 bf16 or 32 e4m3
 #pragma unroll
-                for (int kk = 0; kk < BKT / 16; ++kk)
+                for (int kk = 0; kk < ROW / 32; ++kk)
 #pragma unroll
                     for (int t = 0; t < MT; ++t) {
                         const uint64_t ad = ds + (uint64_t)((t * A_TILE + kk * 32) >> 4);
@@ -221,8 +234,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         for (int b = 0; b < NB; ++b)
 #pragma unroll
                             for (int p = 0; p < BNT; p += PIECE) {
-                                const uint64_t bd = ds + (uint64_t)((A_BYTES + b * B_BYTES + p * BKT * 2 + kk * 32) >> 4);
-                                mma_bf16(tmem + (uint32_t)(t * BNT + p), ad, bd, IDESC, (kk | b) ? 1u : acc0);
+                                const uint64_t bd = ds + (uint64_t)((A_BYTES + b * B_BYTES + p * ROW + kk * 32) >> 4);
+                                if (ESZ == 2) mma_bf16(tmem + (uint32_t)(t * BNT + p), ad, bd, IDESC, (kk | b) ? 1u : acc0);
+                                else mma_e4m3(tmem + (uint32_t)(t * BNT + p), ad, bd, IDESC, (kk | b) ? 1u : acc0);
                             }
                     }
                 mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
@@ -271,8 +285,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
 }
 
-inline size_t gemm_smem_bytes(int BN, int nb, int stages, int mt, int bk) {
-    size_t st = (size_t)BM * bk * 2 * mt + (size_t)BN * bk * 2 * nb;
+inline size_t gemm_smem_bytes(int BN, int nb, int stages, int mt, int bk, int esz) {
+    size_t st = (size_t)BM * bk * esz * mt + (size_t)BN * bk * esz * nb;
     return st * stages + 1024 /*align slack*/ + 256 /*barriers*/;
 }
 
@@ -286,12 +300,13 @@ namespace vp {
 namespace tc {
 
 // ---- genotype-count operands of the batched K-sweep (biallelic diploid) ----
-// C  [Npad][Apad]: C[i][2l+a]  copies of allele a at locus l in individual i
-// CT [Apad][Npad]: the transpose (alleles x individuals)
-// Missing calls and the padding are zero.
+// C  [Npad][Apad]: C[i][2l+a]  copies of allele a at locus l in individual i (bf16)
+// CT [Apad][Npad]: the transpose (alleles x individuals) as e4m3 bytes
+// Missing calls and the padding are zero. 0, 1 and 2 are exact in both types.
+constexpr uint8_t E4M3_ONE = 0x38, E4M3_TWO = 0x40;
 // one CTA = a tile of 64 loci x 64 individuals: the 2-bit codes are decoded
 // into shared memory, then written as contiguous rows of both layouts
-__global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bfloat16* C, __nv_bfloat16* CT,
+__global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bfloat16* C, uint8_t* CT,
                                                       int64_t Apad, int64_t Npad) {
     __shared__ uint8_t code[64][64 + 4];   // [locus][individual]
     const int i0 = blockIdx.x * 64;
@@ -313,8 +328,8 @@ __global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bflo
         const int64_t l = l0 + ll;
         if (l >= D.L) continue;
         const int c = code[ll][ii];
-        const float v = c == 3 ? 0.f : (a ? (float)c : 2.f - c);
-        CT[(2 * l + a) * Npad + i0 + ii] = __float2bfloat16(v);
+        const int v = c == 3 ? 0 : (a ? c : 2 - c);
+        CT[(2 * l + a) * Npad + i0 + ii] = v == 0 ? 0 : v == 1 ? E4M3_ONE : E4M3_TWO;
     }
     // C rows: individual i, alleles 2*l0 .. 2*l0+127
     for (int j = threadIdx.x; j < 64 * 128; j += blockDim.x) {
@@ -366,7 +381,8 @@ struct BatchDev {
     const int32_t* row0;      // [nchains] first row of each chain
     int R, Rpad, nchains, splits;
     int64_t Apad, Npad;
-    __nv_bfloat16 *Whi, *Wlo, *OH;
+    __nv_bfloat16 *Whi, *Wlo;
+    uint8_t* OH;              // [Rpad][Npad] one-hot labels, e4m3
     const float* logpbar;
     const double* Bc;
     const float* LLpart;      // [splits][N][Rpad]
@@ -386,13 +402,9 @@ __global__ void k_update_p_tc(BatchDev b) {
     const int64_t j = k * D.KT + D.off[l];
     Philox ph;
     ph.init(c.seed, ST_P | ((uint32_t)m << 4), (uint32_t)kl, (uint32_t)(kl >> 32));
-    float p[2], s = 0.f;
-    for (int a = 0; a < 2; ++a) {
-        float v = ph.gammaf((float)c.Lambda[k] + (float)c.Ni[j + a]);
-        p[a] = v;
-        s += v;
-    }
-    const float inv = 1.f / s;
+    float p[2];
+    ph.gamma2((float)c.Lambda[k] + (float)c.Ni[j], (float)c.Lambda[k] + (float)c.Ni[j + 1], p[0], p[1]);
+    const float inv = 1.f / (p[0] + p[1]);
     for (int a = 0; a < 2; ++a) {
         p[a] *= inv;
         c.Freq[j + a] = p[a];
@@ -438,7 +450,7 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_tc(BatchDev b) {
             lnl = keep[z];
         }
         for (int k = 0; k < K; ++k)
-            b.OH[(int64_t)(r0 + k) * b.Npad + i] = __float2bfloat16(k == z ? 1.f : 0.f);
+            b.OH[(int64_t)(r0 + k) * b.Npad + i] = k == z ? E4M3_ONE : 0;
     }
     double t = block_sum(lnl, sh);
     if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
