@@ -247,3 +247,43 @@ def test_fmodel_steps(model):
         gc.step("UPDATEF")
         ff_g = gc.get("FF")
         assert np.allclose(ff_g, np.concatenate([oc.get("f"), oc.get("F")]), rtol=1e-9)
+
+
+def _allele_copies(d, ds):
+    """Copies of every allele at every kept locus, in the library's sorted
+    locus order and allele offsets; typed copies per individual."""
+    order = ds.order()
+    G = d["G"][order]                                  # [L, N, v]
+    k = d["k"][order].astype(np.int64)
+    off = np.concatenate([[0], np.cumsum(k)[:-1]])
+    cnt = np.zeros(int(k.sum()), np.int64)
+    for a in range(int(k.max())):
+        c = (G == a).sum(axis=(1, 2))
+        sel = a < k
+        cnt[off[sel] + a] = c[sel]
+    typed = (G >= 0).sum(axis=(0, 2))
+    return cnt, typed
+
+
+@pytest.mark.parametrize("data,K", [("adm", 5), ("adm", 13), ("poly", 4), ("poly", 6)])
+def test_update_z_admix_counter_streams_count_every_copy(data, K):
+    """The counter-stream per-copy kernel (warp-reduced histogram: packed
+    redux.sync bins for K * max alleles <= 40, match_any groups above):
+    summed over clusters, Ni holds every allele copy of the data exactly once
+    and Mi every typed copy of each individual."""
+    d = _adm_small() if data == "adm" else _poly_small()
+    ds = S.Dataset.from_synth(d)
+    ctx = S.Context(ds)
+    gc = S.Chain(ctx, S.params(K, 777, admix=1))
+    cnt, typed = _allele_copies(d, ds)
+    rng = np.random.default_rng(K)
+    for m in (0, 3):
+        gc.set("M", np.array([m], np.int32))
+        gc.step("UPDATEP")
+        gc.set("Q", rng.dirichlet(np.full(K, 0.7), ds.N).astype(np.float32))
+        gc.step("UPDATEZ")
+        ni = gc.get("NI").astype(np.int64).reshape(K, ds.KT)
+        mi = gc.get("MI").astype(np.int64).reshape(ds.N, K)
+        assert np.array_equal(ni.sum(axis=0), cnt), f"allele copies lost or doubled at m={m}"
+        assert np.array_equal(mi.sum(axis=1), typed), f"typed copies lost or doubled at m={m}"
+        assert (ni >= 0).all() and ni.sum() > 0

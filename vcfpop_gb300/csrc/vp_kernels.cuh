@@ -762,20 +762,29 @@ __global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
 // CTA = 8 warps = 256 individuals; grid.y splits the loci into ranges that a
 // CTA walks in slices of ZA_LC loci. A lane keeps its individual's Q row and
 // its Mi counts in registers; the slice's frequencies are staged in shared
-// memory; the per-copy increments of Ni are aggregated across the warp
-// (lanes with equal cluster and allele) before one shared-memory add, and the
-// slice histogram is flushed to Ni with one global atomic per entry.
+// memory. The per-copy increments of Ni are reduced across the warp before
+// they reach the slice histogram in shared memory: with at most ZA_PACKED
+// (cluster, allele) bins, each lane's bin becomes a 1 in one of five 6-bit
+// fields of a word and redux.sync adds the words of the 32 lanes (one
+// reduction per five bins), then lane j adds bin j; with more bins, lanes
+// with equal bins are grouped by __match_any_sync and one of them adds the
+// group's size. The slice histogram is flushed to Ni with one global atomic
+// per non-zero entry. KM is the cluster count rounded up to a compiled size;
+// EXACT means K == KM.
 constexpr int ZA_WARPS = 8;
 constexpr int ZA_LC = 16;
-template <int KM>
+constexpr int ZA_PACKED = 40;
+template <int KM, bool EXACT>
 __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevChain* chains, int force) {
     extern __shared__ unsigned char smraw[];
     const DevChain& c = chains[blockIdx.z];
     const DevData& D = c.D;
-    const int K = c.K, m = c.ctl->m, MK = D.maxK;
+    const int K = EXACT ? KM : c.K, m = c.ctl->m, MK = D.maxK;
     if (!force && binaryq_at(c, m)) return;
     __shared__ double sh[32];
     const int KPAD = K | 1;                                       // odd stride: no bank conflicts
+    const int nbins = K * MK;
+    const bool packed = nbins <= ZA_PACKED;
     float* sF = reinterpret_cast<float*>(smraw);                  // [ZA_LC][MK][KPAD]
     int32_t* hs = reinterpret_cast<int32_t*>(sF + ZA_LC * MK * KPAD);  // [ZA_LC][K][MK]
     const int lane = threadIdx.x & 31;
@@ -784,7 +793,7 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
     float q[KM];
     int32_t mi[KM];
 #pragma unroll
-    for (int k = 0; k < KM; ++k) { q[k] = (live && k < K) ? c.Q[(int64_t)i * K + k] : 0.f; mi[k] = 0; }
+    for (int k = 0; k < KM; ++k) { q[k] = (live && (EXACT || k < K)) ? c.Q[(int64_t)i * K + k] : 0.f; mi[k] = 0; }
     const int64_t lb0 = (int64_t)blockIdx.y * c.zadm_lc, lb1 = min(D.L, lb0 + c.zadm_lc);
     float ls = 0.f, lc = 0.f;  // Kahan sum of ln(sum_k q_k p)
     for (int64_t l0 = lb0; l0 < lb1; l0 += ZA_LC) {
@@ -805,34 +814,55 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
             Philox ph;
             ph.init(c.seed, ST_Z | ((uint32_t)m << 4), (uint32_t)l, (uint32_t)i);
             float lacc = 0.f;
+            int32_t* hl = hs + ll * nbins;
             for (int a = 0; a < D.vmax; ++a) {
                 const bool act = a < cp.n;
-                const unsigned am = __ballot_sync(0xffffffffu, act);
-                if (!act) continue;
-                const int al = cp.a[a];
-                const float* f = sF + (ll * MK + al) * KPAD;
-                float sx = 0.f;
+                int key = -1;
+                if (act) {
+                    const int al = cp.a[a];
+                    const float* f = sF + (ll * MK + al) * KPAD;
+                    float sx = 0.f;
 #pragma unroll
-                for (int k = 0; k < KM; ++k)
-                    if (k < K) sx += q[k] * f[k];
-                lacc += logf(sx);
-                // Poly (src/statistics.cpp:357-385) on the same float weights
-                float t = ph.uniformf() * (sx + (float)(VP_MIN_FREQ * K));
-                int k2 = K - 1;
-                bool found = false;
+                    for (int k = 0; k < KM; ++k)
+                        if (EXACT || k < K) sx += q[k] * f[k];
+                    lacc += logf(sx);
+                    // Poly (src/statistics.cpp:357-385) on the same float weights
+                    float t = ph.uniformf() * (sx + (float)(VP_MIN_FREQ * K));
+                    int k2 = K - 1;
+                    bool found = false;
 #pragma unroll
-                for (int k = 0; k < KM; ++k) {
-                    if (k < K && !found) {
-                        const float w = q[k] * f[k] + (float)VP_MIN_FREQ;
-                        if (t < w) { k2 = k; found = true; }
-                        else t -= w;
+                    for (int k = 0; k < KM; ++k) {
+                        if ((EXACT || k < K) && !found) {
+                            const float w = q[k] * f[k] + (float)VP_MIN_FREQ;
+                            if (t < w) { k2 = k; found = true; }
+                            else t -= w;
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < KM; ++k) mi[k] += (k == k2);
+                    key = k2 * MK + al;
+                }
+                if (packed) {
+                    // every lane of the warp takes part (a < vmax is warp-uniform)
+                    uint32_t mine = 0;
+#pragma unroll
+                    for (int w = 0; w < (ZA_PACKED + 4) / 5; ++w) {
+                        if (w * 5 >= nbins) break;
+                        const uint32_t v = (key >= 0 && key / 5 == w) ? 1u << (6 * (key % 5)) : 0u;
+                        const uint32_t sw = __reduce_add_sync(0xffffffffu, v);
+                        if (lane / 5 == w) mine = sw;
+                    }
+                    if (lane < nbins) {
+                        const int cnt = (int)((mine >> (6 * (lane % 5))) & 63u);
+                        if (cnt) atomicAdd(&hl[lane], cnt);
+                    }
+                } else {
+                    const unsigned am = __ballot_sync(0xffffffffu, act);
+                    if (act) {
+                        const unsigned grp = __match_any_sync(am, key);
+                        if (lane == __ffs(grp) - 1) atomicAdd(&hl[key], __popc(grp));
                     }
                 }
-#pragma unroll
-                for (int k = 0; k < KM; ++k) mi[k] += (k == k2);
-                const int key = k2 * MK + al;
-                const unsigned grp = __match_any_sync(am, key);
-                if (lane == __ffs(grp) - 1) atomicAdd(&hs[(ll * K + k2) * MK + al], __popc(grp));
             }
             float y = lacc - lc, tt = ls + y;
             lc = (tt - ls) - y;
@@ -849,7 +879,7 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
     if (live)
 #pragma unroll
         for (int k = 0; k < KM; ++k)
-            if (k < K && mi[k]) atomicAdd(&c.Mi[(int64_t)i * K + k], mi[k]);
+            if ((EXACT || k < K) && mi[k]) atomicAdd(&c.Mi[(int64_t)i * K + k], mi[k]);
     double t = block_sum((double)ls - (double)lc, sh);
     if (threadIdx.x == 0) c.lnlp[blockIdx.y * gridDim.x + blockIdx.x] = t;
 }

@@ -177,7 +177,10 @@ size_t zadm_smem(const vp_chain* c) {
     const int K = c->P.K, MK = c->ctx->maxK;
     return (size_t)ZA_LC * MK * (K | 1) * 4 + (size_t)ZA_LC * K * MK * 4;
 }
-int km_for(int K) { return K <= 8 ? 8 : K <= 16 ? 16 : K <= 32 ? 32 : 64; }
+// instantiations of the per-copy label kernel: exact cluster counts up to
+// 12, then padded sizes
+#define VP_ZADM_EXACT(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12)
+#define VP_ZADM_PADDED(X) X(16) X(32) X(64)
 
 int launch_zadm_ctr(vp_chain* c, int force) {
     vp_ctx* x = c->ctx;
@@ -185,13 +188,17 @@ int launch_zadm_ctr(vp_chain* c, int force) {
     size_t sm = zadm_smem(c);
     prof_mark(x, true);
     struct End { vp_ctx* x; ~End() { prof_mark(x, false); } } end_{x};
-    switch (km_for(c->P.K)) {
-        case 8: LAUNCH(x, k_update_z_admix_ctr<8>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
-        case 16: LAUNCH(x, k_update_z_admix_ctr<16>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
-        case 32: LAUNCH(x, k_update_z_admix_ctr<32>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
-        default: LAUNCH(x, k_update_z_admix_ctr<64>, (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); break;
-    }
-    return VP_OK;
+    const int K = c->P.K;
+#define VP_ZE(n) \
+    if (K == n) { LAUNCH(x, (k_update_z_admix_ctr<n, true>), (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); return VP_OK; }
+#define VP_ZP(n) \
+    if (K <= n) { LAUNCH(x, (k_update_z_admix_ctr<n, false>), (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); return VP_OK; }
+    VP_ZADM_EXACT(VP_ZE)
+    VP_ZADM_PADDED(VP_ZP)
+#undef VP_ZE
+#undef VP_ZP
+    vp_set_error("K = %d out of range", K);
+    return VP_E_ARG;
 }
 
 void set_smem_limits() {
@@ -200,10 +207,12 @@ void set_smem_limits() {
     done = true;
     const int big = 200 * 1024;
     cudaFuncSetAttribute(k_count_noadmix, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_update_z_admix_ctr<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_update_z_admix_ctr<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_update_z_admix_ctr<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_update_z_admix_ctr<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+#define VP_ZE(n) cudaFuncSetAttribute(k_update_z_admix_ctr<n, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+#define VP_ZP(n) cudaFuncSetAttribute(k_update_z_admix_ctr<n, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    VP_ZADM_EXACT(VP_ZE)
+    VP_ZADM_PADDED(VP_ZP)
+#undef VP_ZE
+#undef VP_ZP
 }
 
 int launch_step(vp_chain* c, int step, int force) {
