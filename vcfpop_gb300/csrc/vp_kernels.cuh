@@ -446,6 +446,66 @@ __device__ void sample_one(const DevChain& c, int i, int m, bool ref, Rng64* r, 
     c.Mi[(int64_t)i * K + z] = (int32_t)D.vt[i];
     *lnl += keep[z];
 }
+// counter streams: one warp per individual. Lane k holds cluster k (and
+// k + 32): it sums the chunk partials of its clusters, and the maximum, the
+// normaliser and the categorical search (the first cluster whose cumulative
+// weight exceeds the uniform) are warp reductions, a prefix scan and a
+// ballot. Returns, in every lane, LL[i, z] of the drawn label.
+__device__ double sample_warp(const DevChain& c, int i, int m, int lane) {
+    const DevData& D = c.D;
+    const int K = c.K, N = D.N;
+    const int k0 = lane, k1 = lane + 32;
+    const bool h0 = k0 < K, h1 = k1 < K;
+    double v0 = 0, v1 = 0;
+    for (int ch = 0; ch < c.nchunk; ++ch) {
+        const double* p = c.LLp + ((int64_t)ch * N + i) * K;
+        if (h0) v0 += p[k0];
+        if (h1) v1 += p[k1];
+    }
+    double* LL = c.LL + (int64_t)i * K;
+    float* Q = c.Q + (int64_t)i * K;
+    int32_t* Mi = c.Mi + (int64_t)i * K;
+    if (h0) LL[k0] = v0;
+    if (h1) LL[k1] = v1;
+    const int vt = (int)D.vt[i];
+    if (vt == 0) {
+        if (h0) { Q[k0] = 0.f; Mi[k0] = 0; }
+        if (h1) { Q[k1] = 0.f; Mi[k1] = 0; }
+        return 0;
+    }
+    double w0 = v0, w1 = v1;
+    if (c.locpriori) {
+        const double* g = c.Gamma + D.popid[i] * K;
+        if (h0) w0 += log(g[k0]);
+        if (h1) w1 += log(g[k1]);
+    }
+    double mx = fmax(h0 ? w0 : -1.79769313486231570e+308, h1 ? w1 : -1.79769313486231570e+308);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const double e0 = h0 ? ((w0 - mx) < -23 ? VP_MIN_FREQ : exp(w0 - mx)) : 0.0;
+    const double e1 = h1 ? ((w1 - mx) < -23 ? VP_MIN_FREQ : exp(w1 - mx)) : 0.0;
+    // inclusive prefix sums of the weights in cluster order
+    double c0 = e0, c1 = e1;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double a0 = __shfl_up_sync(0xffffffffu, c0, o), a1 = __shfl_up_sync(0xffffffffu, c1, o);
+        if (lane >= o) { c0 += a0; c1 += a1; }
+    }
+    const double tot0 = __shfl_sync(0xffffffffu, c0, 31);
+    c1 += tot0;
+    const double s = __shfl_sync(0xffffffffu, c1, 31) + VP_MIN_FREQ * K;
+    double u = 0;
+    if (lane == 0) { Philox ph; ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0); u = ph.uniformd(); }
+    const double t = __shfl_sync(0xffffffffu, u, 0) * s;
+    int z = K - 1;
+    const unsigned b0 = __ballot_sync(0xffffffffu, h0 && t < c0);
+    const unsigned b1 = __ballot_sync(0xffffffffu, h1 && t < c1);
+    if (b0) z = __ffs(b0) - 1;
+    else if (b1) z = 32 + __ffs(b1) - 1;
+    if (h0) { Q[k0] = k0 == z ? 1.f : 0.f; Mi[k0] = k0 == z ? vt : 0; }
+    if (h1) { Q[k1] = k1 == z ? 1.f : 0.f; Mi[k1] = k1 == z ? vt : 0; }
+    if (lane == 0) c.Z[i] = (uint16_t)z;
+    return __shfl_sync(0xffffffffu, z < 32 ? v0 : v1, z & 31);
+}
+
 __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain* chains, int force) {
     const DevChain& c = chains[blockIdx.z];
     const DevData& D = c.D;
@@ -472,10 +532,11 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain*
             c.ctl->lnl = lnl;
         }
     } else {
+        const int lane = threadIdx.x & 31;
+        const int i = blockIdx.x * (SAMPLE_BLOCK / 32) + (threadIdx.x >> 5);
         double lnl = 0;
-        int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i < N) sample_one(c, i, m, false, nullptr, &lnl);
-        double t = block_sum(lnl, sh);
+        if (i < N) lnl = sample_warp(c, i, m, lane);
+        double t = block_sum(lane == 0 ? lnl : 0.0, sh);
         if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
         if (!last_block_done(c.ctl, gridDim.x)) return;
         if (threadIdx.x == 0) {

@@ -433,17 +433,18 @@ int chain_plan(const vp_ctx* x, const vp_params* P, vp_chain* c, size_t* bytes) 
     h.rlen = P->locpriori ? 4 + nl + 1 + K + K * S + nf : 4 + nl + na + nf;
     c->kc = kc_for(K);
     c->kgroups = (K + c->kc - 1) / c->kc;
-    // locus chunks for the likelihood passes: enough CTAs to fill the SMs
+    // locus chunks for the likelihood passes: about 12 CTAs per SM, so that
+    // enough warps are resident to cover the genotype stream's latency
     {
         int64_t nbi = cdiv(N, LL_BLOCK) * (int64_t)c->kgroups;
-        int64_t want = std::max<int64_t>(1, (int64_t)x->nsm * 4 / std::max<int64_t>(nbi, 1));
+        int64_t want = std::max<int64_t>(1, (int64_t)x->nsm * 12 / std::max<int64_t>(nbi, 1));
         int64_t maxc = std::max<int64_t>(1, L / 64);
         int64_t nch = std::min(want, maxc);
         h.lchunk = (int32_t)((L + nch - 1) / nch);
         h.nchunk = (int32_t)((L + h.lchunk - 1) / h.lchunk);
     }
     h.kp = (K + 3) & ~3;
-    h.nsampblk = (int32_t)cdiv(N, SAMPLE_BLOCK);
+    h.nsampblk = (int32_t)cdiv(N, SAMPLE_BLOCK / 32);   // counter-stream sampling: a warp per individual
     {
         // loci per CTA of the per-copy label kernel: about 4 CTAs per SM
         int64_t nx = cdiv(N, ZA_WARPS * 32);
