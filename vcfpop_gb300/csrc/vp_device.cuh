@@ -92,6 +92,11 @@ __device__ inline double ref_mylog(double v) {
 __device__ inline float ln_freq(float p) {
     return p > 0.f ? logf(p) : -709.0895657128241f;
 }
+// the same with the hardware logarithm (absolute error about 2^-21), for
+// the centred tensor-core weights, whose bf16 hi + lo split keeps 16 bits
+__device__ inline float ln_freq_fast(float p) {
+    return p > 0.f ? __logf(p) : -709.0895657128241f;
+}
 
 // ---------------- RNG<double>: xorshift128+ ----------------
 struct Rng64 {
@@ -245,22 +250,35 @@ struct Philox {
     // biallelic locus). The first Marsaglia-Tsang attempt of both takes one
     // Philox block: the cosine and sine normals of one Box-Muller pair and
     // two acceptance uniforms; an attempt that is rejected (rare for shapes
-    // >= 1) continues as gammaf does, on further blocks.
+    // >= 1) continues as gammaf does, on further blocks. The Box-Muller
+    // radius and angle use the hardware approximations (__logf, __sincosf of
+    // an angle in [-pi, pi)): the counter streams are not matched to the
+    // reference's draws, and these calls are the bulk of the kernel's issue.
     __device__ inline void gamma2(float a0, float a1, float& g0, float& g1) {
         const bool s0 = a0 < 1.f, s1 = a1 < 1.f;
         const float b0 = s0 ? a0 + 1.f : a0, b1 = s1 ? a1 + 1.f : a1;
         const float d0 = b0 - 1.f / 3.f, c0 = rsqrtf(9.f * d0);
         const float d1 = b1 - 1.f / 3.f, c1 = rsqrtf(9.f * d1);
         const float u1 = uniformf(), u2 = uniformf(), u3 = uniformf(), u4 = uniformf();
-        const float r = sqrtf(-2.0f * logf(u1));
+        const float r = sqrtf(-2.0f * __logf(u1));
         float sn, cs;
-        sincospif(2.0f * u2, &sn, &cs);
+        __sincosf(6.283185307179586f * u2 - 3.141592653589793f, &sn, &cs);
         const bool ok0 = mt_accept(d0, c0, r * cs, u3, g0);
         const bool ok1 = mt_accept(d1, c1, r * sn, u4, g1);
         if (!ok0) g0 = mt_more(d0, c0);
         if (!ok1) g1 = mt_more(d1, c1);
         if (s0) g0 *= powf(uniformf(), 1.f / a0);
         if (s1) g1 *= powf(uniformf(), 1.f / a1);
+    }
+    // Beta(a0, a1) as the normalised pair of gamma2, (p0, p1) summing to 1:
+    // the biallelic Dirichlet draw of UpdateP, shared by the per-chain and
+    // batched kernels so that both give the same frequencies
+    __device__ inline void dirichlet2(float a0, float a1, float& p0, float& p1) {
+        float g0, g1;
+        gamma2(a0, a1, g0, g1);
+        const float inv = __fdividef(1.f, g0 + g1);
+        p0 = g0 * inv;
+        p1 = g1 * inv;
     }
     // one Marsaglia-Tsang attempt with normal t and uniform u
     __device__ static inline bool mt_accept(float d, float c, float t, float u, float& g) {
@@ -269,7 +287,7 @@ struct Philox {
         v = v * v * v;
         g = d * v;
         if (u < 1.f - 0.0331f * t * t * t * t) return true;
-        return logf(u) < 0.5f * t * t + d * (1.f - v + logf(v));
+        return __logf(u) < 0.5f * t * t + d * (1.f - v + __logf(v));
     }
     __device__ inline float mt_more(float d, float c) {
         float g = d;

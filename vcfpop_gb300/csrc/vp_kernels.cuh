@@ -275,20 +275,21 @@ __global__ void k_update_p_ctr(const DevChain* chains) {
     Philox ph;
     ph.init(c.seed, ST_P | ((uint32_t)m << 4), (uint32_t)kl, (uint32_t)(kl >> 32));
     float p[64];
-    float s = 0;
     if (k2 == 2) {
         // the same draws as the batched tensor-core UpdateP
-        ph.gamma2(prior_of(c, k, D.off[l]) + (float)c.Ni[j], prior_of(c, k, D.off[l] + 1) + (float)c.Ni[j + 1], p[0], p[1]);
-        s = p[0] + p[1];
+        ph.dirichlet2(prior_of(c, k, D.off[l]) + (float)c.Ni[j], prior_of(c, k, D.off[l] + 1) + (float)c.Ni[j + 1], p[0],
+                      p[1]);
     } else {
+        float s = 0;
         for (int a = 0; a < k2; ++a) {
             float v = ph.gammaf(prior_of(c, k, D.off[l] + a) + (float)c.Ni[j + a]);
             p[a] = v;
             s += v;
         }
+        const float inv = 1.f / s;
+        for (int a = 0; a < k2; ++a) p[a] *= inv;
     }
-    float inv = 1.f / s;
-    for (int a = 0; a < k2; ++a) { p[a] *= inv; c.Freq[j + a] = p[a]; }
+    for (int a = 0; a < k2; ++a) c.Freq[j + a] = p[a];
     write_lt(c, k, l, p, k2);
 }
 
@@ -402,6 +403,12 @@ __device__ __forceinline__ int polylog(double* ll, int K, double u01, bool ref, 
     return K - 1;
 }
 
+// PolyLog for counter streams: the same draw, with the weights
+// exp(LL_k - max) evaluated in single precision (within 1e-7 of the double
+// weights; FP64 exp is slow on this part) and summed and searched in double.
+// The counter-stream draw is not matched to the reference's stream.
+__device__ __forceinline__ double weight_ctr(double d) { return d < -23 ? VP_MIN_FREQ : (double)__expf((float)d); }
+
 // UpdateQNoAdmix label draw (src/structure.cpp:891-900) plus the state the
 // reference rebuilds afterwards: Q one-hot, Mi[i, Z_i] = vt_i
 // (src/structure.cpp:1305-1310), Di for the location prior (1151-1158) and the
@@ -481,8 +488,8 @@ __device__ double sample_warp(const DevChain& c, int i, int m, int lane) {
     }
     double mx = fmax(h0 ? w0 : -1.79769313486231570e+308, h1 ? w1 : -1.79769313486231570e+308);
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    const double e0 = h0 ? ((w0 - mx) < -23 ? VP_MIN_FREQ : exp(w0 - mx)) : 0.0;
-    const double e1 = h1 ? ((w1 - mx) < -23 ? VP_MIN_FREQ : exp(w1 - mx)) : 0.0;
+    const double e0 = h0 ? weight_ctr(w0 - mx) : 0.0;
+    const double e1 = h1 ? weight_ctr(w1 - mx) : 0.0;
     // inclusive prefix sums of the weights in cluster order
     double c0 = e0, c1 = e1;
     for (int o = 1; o < 32; o <<= 1) {

@@ -991,7 +991,9 @@ int launch_tc_sweep(vp_ctx* x) {
     tc::BatchDev bd = batch_dev(x);
     cudaStream_t s = x->stream;
     // UpdateP for all chains, with the split-bf16 centred log-frequency rows
-    LAUNCH(x, tc::k_update_p_tc, (dim3(cdiv(x->L, 256), b->R, 1), 256, 0, s), (bd));
+    // about 16 blocks per SM in all (about 3 waves): each thread walks many loci
+    const unsigned upx = std::max<unsigned>(1, std::min<unsigned>(cdiv(x->L, 256), cdiv((int64_t)x->nsm * 16, b->R)));
+    LAUNCH(x, tc::k_update_p_tc, (dim3(upx, b->R, 1), 256, 0, s), (bd));
     // likelihood contraction: LL'[i, row] = sum_a C[i,a] (Whi + Wlo)[row, a]
     {
         tc::GemmArgs g{};

@@ -390,30 +390,106 @@ struct BatchDev {
 
 // UpdateP for every chain of the batch (counter streams, the same Philox
 // counters as the per-chain kernel): p ~ Dirichlet(lambda + Ni), written to
-// Freq and, centred and split into bf16 hi + lo, to the rows of W
-__global__ void k_update_p_tc(BatchDev b) {
+// Freq and, centred and split into bf16 hi + lo, to the rows of W.
+// grid.y = cluster row; a thread walks loci with a stride of the grid's
+// width, so the chain's parameters are fetched once per thread, not per locus.
+// Biallelic data: allele offsets are 2l.
+__global__ void __launch_bounds__(256) k_update_p_tc(BatchDev b) {
     const int r = blockIdx.y;
     const DevChain& c = b.chains[b.rowchain[r]];
-    const DevData& D = c.D;
+    const int64_t L = c.D.L;
     const int k = b.rowk[r], m = c.ctl->m;
-    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (l >= D.L) return;
-    const int64_t kl = (int64_t)k * D.L + l;
-    const int64_t j = k * D.KT + D.off[l];
-    Philox ph;
-    ph.init(c.seed, ST_P | ((uint32_t)m << 4), (uint32_t)kl, (uint32_t)(kl >> 32));
-    float p[2];
-    ph.gamma2((float)c.Lambda[k] + (float)c.Ni[j], (float)c.Lambda[k] + (float)c.Ni[j + 1], p[0], p[1]);
-    const float inv = 1.f / (p[0] + p[1]);
-    for (int a = 0; a < 2; ++a) {
-        p[a] *= inv;
-        c.Freq[j + a] = p[a];
-        const float w = ln_freq(p[a]) - b.logpbar[2 * l + a];
-        const __nv_bfloat16 hi = __float2bfloat16(w);
-        const __nv_bfloat16 lo = __float2bfloat16(w - __bfloat162float(hi));
-        b.Whi[(int64_t)r * b.Apad + 2 * l + a] = hi;
-        b.Wlo[(int64_t)r * b.Apad + 2 * l + a] = lo;
+    const uint64_t seed = c.seed;
+    const float lam = (float)c.Lambda[k];
+    const int32_t* Ni = c.Ni + (int64_t)k * c.D.KT;
+    float* Freq = c.Freq + (int64_t)k * c.D.KT;
+    __nv_bfloat162* Whi = reinterpret_cast<__nv_bfloat162*>(b.Whi + (int64_t)r * b.Apad);
+    __nv_bfloat162* Wlo = reinterpret_cast<__nv_bfloat162*>(b.Wlo + (int64_t)r * b.Apad);
+    const float2* lpb = reinterpret_cast<const float2*>(b.logpbar);
+    const int2* Ni2 = reinterpret_cast<const int2*>(Ni);
+    float2* F2 = reinterpret_cast<float2*>(Freq);
+    for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < L; l += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kl = (int64_t)k * L + l;
+        Philox ph;
+        ph.init(seed, ST_P | ((uint32_t)m << 4), (uint32_t)kl, (uint32_t)(kl >> 32));
+        const int2 n = Ni2[l];
+        float p0, p1;
+        ph.dirichlet2(lam + (float)n.x, lam + (float)n.y, p0, p1);
+        F2[l] = make_float2(p0, p1);
+        const float2 lb = lpb[l];
+        const float w0 = ln_freq_fast(p0) - lb.x, w1 = ln_freq_fast(p1) - lb.y;
+        const __nv_bfloat16 h0 = __float2bfloat16(w0), h1 = __float2bfloat16(w1);
+        Whi[l] = __halves2bfloat162(h0, h1);
+        Wlo[l] = __halves2bfloat162(__float2bfloat16(w0 - __bfloat162float(h0)), __float2bfloat16(w1 - __bfloat162float(h1)));
     }
+}
+
+// One (chain, individual). The split-K partials sum, in FP32, to the centred
+// log-likelihood; the individual's constant B_i cancels from the label
+// weights exp(LL_k - max), so the draw runs in FP32 on the centred sums (the
+// GEMM accumulated them in FP32; a float uniform) and only LL itself, B_i +
+// the centred sum, is formed in FP64. K <= KM with the values in registers;
+// larger K goes through a separate (not inlined) copy with local arrays, so
+// it does not raise the kernel's registers.
+template <int KM, bool WIDE>
+__device__ __forceinline__ double sample_tc_body(const BatchDev& b, const DevChain& c, int i, int m, int r0) {
+    const DevData& D = c.D;
+    const int K = c.K, N = D.N;
+    constexpr int UNR = WIDE ? 1 : KM;   // the wide copy keeps its loops rolled (arrays in local memory)
+    float sf[KM];
+    const double bc = b.Bc[i];
+#pragma unroll UNR
+    for (int k = 0; k < KM; ++k) {
+        if (k >= K) break;
+        float v = 0.f;
+        for (int s = 0; s < b.splits; ++s) v += b.LLpart[((int64_t)s * N + i) * b.Rpad + r0 + k];
+        sf[k] = v;
+        c.LL[(int64_t)i * K + k] = bc + (double)v;
+    }
+    int z = -1;
+    double lnl = 0;
+    if (D.vt[i]) {
+        float mx = -3.402823466e+38f;
+#pragma unroll UNR
+        for (int k = 0; k < KM; ++k)
+            if (k < K && !(sf[k] < mx)) mx = sf[k];
+        float s = (float)(VP_MIN_FREQ * K);
+#pragma unroll UNR
+        for (int k = 0; k < KM; ++k)
+            if (k < K) s += sf[k] - mx < -23.f ? (float)VP_MIN_FREQ : __expf(sf[k] - mx);
+        Philox ph;
+        ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0);
+        float t = ph.uniformf() * s;
+        z = K - 1;
+        bool found = false;
+#pragma unroll UNR
+        for (int k = 0; k < KM; ++k) {
+            if (k < K && !found) {
+                const float w = sf[k] - mx < -23.f ? (float)VP_MIN_FREQ : __expf(sf[k] - mx);
+                if (t < w) { z = k; found = true; }
+                else t -= w;
+            }
+        }
+        float vz = 0.f;
+#pragma unroll UNR
+        for (int k = 0; k < KM; ++k)
+            if (k == z) vz = sf[k];
+        lnl = bc + (double)vz;
+        c.Z[i] = (uint16_t)z;
+    }
+    const int vt = (int)D.vt[i];
+#pragma unroll UNR
+    for (int k = 0; k < KM; ++k) {
+        if (k >= K) break;
+        c.Q[(int64_t)i * K + k] = k == z ? 1.f : 0.f;
+        c.Mi[(int64_t)i * K + k] = k == z ? vt : 0;
+        b.OH[(int64_t)(r0 + k) * b.Npad + i] = k == z ? E4M3_ONE : 0;
+    }
+    return lnl;
+}
+
+__device__ __noinline__ double sample_tc_wide(const BatchDev& b, const DevChain& c, int i, int m, int r0) {
+    return sample_tc_body<64, true>(b, c, i, m, r0);
 }
 
 // label draw for every (chain, individual) from the tensor-core likelihoods;
@@ -421,37 +497,12 @@ __global__ void k_update_p_tc(BatchDev b) {
 __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_tc(BatchDev b) {
     const int ci = blockIdx.y;
     const DevChain& c = b.chains[ci];
-    const DevData& D = c.D;
-    const int K = c.K, N = D.N, m = c.ctl->m;
+    const int K = c.K, N = c.D.N, m = c.ctl->m;
     const int r0 = b.row0[ci];
     __shared__ double sh[32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double lnl = 0;
-    if (i < N) {
-        double ll[64];
-        for (int k = 0; k < K; ++k) {
-            double v = b.Bc[i];
-            for (int s = 0; s < b.splits; ++s) v += (double)b.LLpart[((int64_t)s * N + i) * b.Rpad + r0 + k];
-            ll[k] = v;
-            c.LL[(int64_t)i * K + k] = v;
-            c.Q[(int64_t)i * K + k] = 0.f;
-            c.Mi[(int64_t)i * K + k] = 0;
-        }
-        int z = -1;
-        if (D.vt[i]) {
-            double keep[64];
-            for (int k = 0; k < K; ++k) keep[k] = ll[k];
-            Philox ph;
-            ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0);
-            z = polylog(ll, K, ph.uniformd(), false, nullptr);
-            c.Q[(int64_t)i * K + z] = 1.f;
-            c.Z[i] = (uint16_t)z;
-            c.Mi[(int64_t)i * K + z] = (int32_t)D.vt[i];
-            lnl = keep[z];
-        }
-        for (int k = 0; k < K; ++k)
-            b.OH[(int64_t)(r0 + k) * b.Npad + i] = k == z ? E4M3_ONE : 0;
-    }
+    if (i < N) lnl = K <= 16 ? sample_tc_body<16, false>(b, c, i, m, r0) : sample_tc_wide(b, c, i, m, r0);
     double t = block_sum(lnl, sh);
     if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
     if (!last_block_done(c.ctl, gridDim.x)) return;
