@@ -185,6 +185,37 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- output reductions
+def output_reductions(ctx, ds, args, rank):
+    """WriteStructure's heterozygosity / net-distance / per-locus diversity
+    reductions of one finished K = 10 chain on this dataset: the device call
+    (vp_chain_divergence, copies included) and, as its CPU baseline, the
+    reference loops restated in the oracle, on the same mean frequencies."""
+    from vcfpop_gb300 import structure as S
+    K = 10
+    ch = S.Chain(ctx, S.params(K, S.run_seed(1, 999), admix=0, nadmburnin=0, nburnin=0, nreps=1, nthinning=1))
+    S.finish([ch])
+    ch.divergence(per_locus=True)
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        got = ch.divergence(per_locus=True)
+    dev_ms = (time.perf_counter() - t0) / reps * 1e3
+    out = {"what": f"H[K], D[K,K] and per-locus H[K,L] of one K={K} chain, L={ds.L}, KT={ds.KT}",
+           "device_ms": dev_ms, "kernels": "k_divergence_pairs, k_divergence_finish, k_heterozygosity"}
+    if rank == 0 and not args.no_cpu_baseline:
+        from tests import orc
+        fm = ch.result(final=True)["freqm"]
+        k = np.full(ds.L, 2, np.int32)
+        t0 = time.perf_counter()
+        ref = orc.divergence(fm, k, K, per_locus=True)
+        out["cpu_baseline_ms"] = (time.perf_counter() - t0) * 1e3
+        out["cpu_baseline_kind"] = "port (the reference's WriteStructure loops, one core)"
+        out["max_abs_diff_D"] = float(np.abs(ref["D"] - got["D"]).max())
+    ch.close()
+    return out
+
+
 # ---------------------------------------------------------------- c1, c2, c4: one chain
 SINGLE_DESC = {
     "c1": "N=200 diploids, 3 pops, L=2,000 biallelic SNPs, F=0.1, 5% missing; K=3 no-admixture, 1,000 + 2,000 sweeps",
@@ -543,6 +574,7 @@ def main():
             pass
     for c in chains:
         c.close()
+    outputs = output_reductions(ctx, ds, args, rank)
     ctx.close()
 
     # ---- end to end through the C ABI: upload from pinned host memory, create
@@ -589,7 +621,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "step": f"open context from pinned host buffers + create 100 chains + {args.e2e_sweeps} sweeps "
                             f"+ read every chain's lnL + close", "ms_per_step": float(np.median(e2e_ms)) if e2e_ms else None},
-            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err}
+            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "outputs": outputs}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

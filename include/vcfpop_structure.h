@@ -136,6 +136,15 @@ typedef struct {
 int vp_chain_sizes(vp_chain* c, vp_result* sizes);
 int vp_chain_result(vp_chain* c, vp_result* out);
 
+/* Output reductions of WriteStructure (src/structure.cpp:293-324) on the
+ * device, from a finished chain's mean frequencies: H[K] the mean expected
+ * heterozygosity of each cluster, D[K*K] the net nucleotide distance between
+ * clusters, and (Hl != NULL) Hl[K*L] the per-locus heterozygosity of the
+ * diversity table (-structure_diversity). Host buffers; synchronous. Sums are
+ * FP64 of exact float products, in a fixed order (not the reference's
+ * sequential order, so the last bits may differ). */
+int vp_chain_divergence(vp_chain* c, double* H, double* D, double* Hl);
+
 /* ---- single steps and state access (parity tests, debugging) ------------- */
 #define VP_STEP_UPDATEP 1
 #define VP_STEP_UPDATEQ 2

@@ -1108,3 +1108,33 @@ void orc_sweep_many(orc_chain** cs, int n, int nsweeps, int nthreads, int init) 
     free(th);
     pthread_mutex_destroy(&p.mu);
 }
+
+/* structure.cpp:293-324: per-locus 1 - SumSquare, and 1 - SumProd summed over
+ * loci for every pair, both in double from float frequencies */
+void orc_divergence(const float* freqm, const int32_t* k, int64_t L, int64_t KT, int K, double* H, double* D,
+                    double* Hl) {
+    for (int a = 0; a < K; ++a) {
+        const float* p = freqm + a * KT;
+        H[a] = 0;
+        for (int64_t l = 0; l < L; ++l) {
+            double ss = 0;
+            for (int b = 0; b < k[l]; ++b) ss += (double)p[b] * (double)p[b];
+            if (Hl) Hl[a * L + l] = 1 - ss;
+            H[a] += 1 - ss;
+            p += k[l];
+        }
+        H[a] /= L;
+        for (int j = 0; j <= a; ++j) {
+            const float *p1 = freqm + a * KT, *p2 = freqm + j * KT;
+            double dt = 0;
+            for (int64_t l = 0; l < L; ++l) {
+                double sp = 0;
+                for (int b = 0; b < k[l]; ++b) sp += (double)p1[b] * (double)p2[b];
+                dt += 1 - sp;
+                p1 += k[l];
+                p2 += k[l];
+            }
+            D[j * K + a] = D[a * K + j] = dt / L - (H[a] + H[j]) / 2;
+        }
+    }
+}

@@ -131,6 +131,12 @@ void orc_loglik_noadmix(orc_chain* c, double* out);
  * parallelism of the reference's -structure_nstream (structure.cpp:2467-2499). */
 void orc_sweep_many(orc_chain** cs, int n, int nsweeps, int nthreads, int init);
 
+/* WriteStructure's heterozygosity and net nucleotide distance
+ * (structure.cpp:293-324) on mean frequencies freqm[K][KT] of L loci with
+ * k[l] alleles each: H[K], D[K*K], Hl[K*L] (Hl may be NULL). */
+void orc_divergence(const float* freqm, const int32_t* k, int64_t L, int64_t KT, int K, double* H, double* D,
+                    double* Hl);
+
 /* Output files in the reference's format (structure.cpp:86-401). */
 int orc_write_structure(orc_chain* c, const char* out_prefix, int rep, int id,
                         const char* const* ind_names, const char* const* pop_names,

@@ -68,6 +68,8 @@ def lib():
         L.orc_binaryq.argtypes = [P]
         L.orc_sweep_many.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_sweep_many.restype = None
+        L.orc_divergence.argtypes = [P, P, C.c_int64, C.c_int64, C.c_int, P, P, P]
+        L.orc_divergence.restype = None
         L.orc_hash_ulong_c.restype = C.c_uint32
         L.orc_hash_ulong_c.argtypes = [C.c_uint64]
         _lib = L
@@ -175,3 +177,15 @@ class Chain:
         if getattr(self, "h", None) and not sys.is_finalizing():
             lib().orc_chain_free(self.h)
             self.h = None
+
+
+def divergence(freqm, k, K, per_locus=False):
+    """The reference's H, D (and per-locus H) on mean frequencies [K][KT]."""
+    freqm = np.ascontiguousarray(freqm, np.float32)
+    k = np.ascontiguousarray(k, np.int32)
+    L, KT = len(k), int(k.sum())
+    H, D = np.zeros(K), np.zeros((K, K))
+    Hl = np.zeros((K, L)) if per_locus else None
+    lib().orc_divergence(freqm.ctypes.data, k.ctypes.data, L, KT, K, H.ctypes.data, D.ctypes.data,
+                         None if Hl is None else Hl.ctypes.data)
+    return dict(H=H, D=D, Hl=Hl)

@@ -40,3 +40,30 @@ def test_oracle_matches_reference(case, oracle_build, tmp_path):
         got = open(tmp_path / f, "rb").read()
         want = open(ref, "rb").read()
         assert got == want, f"{case}/{f} differs from the reference output"
+
+
+def _d_block(path, K):
+    lines = open(path, "rb").read().decode().replace("\r", "").split("\n")
+    i = next(j for j, ln in enumerate(lines) if ln.startswith("Allele-frequency divergence among pops"))
+    return [[float(v) for v in lines[i + 3 + r].split("\t")[1:1 + K]] for r in range(K)]
+
+
+def test_oracle_divergence_reproduces_reference_d_block(oracle_build):
+    """orc_divergence (the heterozygosity / net nucleotide distance loops of
+    WriteStructure) on the oracle's finished c1 chain gives the D block the
+    reference program printed for the same run, to its 15 printed decimals."""
+    import numpy as np
+    from vcfpop_gb300 import synth
+    from . import orc
+    c = CASES["c1_noadmix"]
+    d = synth.fmodel(1, 200, 2000, 3, 0.1, 0.05)          # the c1 data make_golden.py wrote
+    od = orc.Data(d)
+    K = 3
+    seed = orc.lib().orc_hash_ulong_c(c["seed"] + 1)     # run id 1
+    oc = orc.Chain(od, orc.params(K, seed, admix=0, nadmburnin=0, nburnin=100, nreps=200, writelnl=1))
+    orc.lib().orc_run(oc.h)
+    k = od.field(1, np.int32)
+    out = orc.divergence(oc.get("FREQM"), k, K, per_locus=True)
+    want = np.array(_d_block(os.path.join(GOLD, "c1_noadmix", "out.structure.k=3_rep=1_id=1.txt"), K))
+    assert np.abs(out["D"] - want).max() < 1e-14, (out["D"], want)
+    assert np.allclose(out["Hl"].mean(axis=1), out["H"])

@@ -71,7 +71,7 @@ _lib = None
 # every exported symbol of include/vcfpop_structure.h
 EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_dataset_free", "vp_open",
            "vp_close", "vp_sync", "vp_params_default", "vp_run_seed", "vp_chain_create", "vp_chain_destroy",
-           "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_step", "vp_chain_get",
+           "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_divergence", "vp_chain_step", "vp_chain_get",
            "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
            "vp_release", "vp_server_close"]
@@ -105,6 +105,7 @@ def lib():
     L.vp_finish.argtypes = [C.POINTER(P), C.c_int32]
     L.vp_chain_sizes.argtypes = [P, C.POINTER(VpResult)]
     L.vp_chain_result.argtypes = [P, C.POINTER(VpResult)]
+    L.vp_chain_divergence.argtypes = [P, P, P, P]
     L.vp_chain_step.argtypes = [P, C.c_int32]
     L.vp_chain_get.argtypes = [P, C.c_int32, P, C.c_size_t]
     L.vp_chain_set.argtypes = [P, C.c_int32, P, C.c_size_t]

@@ -225,9 +225,12 @@ struct Writer {
 };
 
 // WriteStructure (src/structure.cpp:86-377)
+// H, D, H2: the run's heterozygosity, net nucleotide distance and per-locus
+// heterozygosity, reduced on the device (vp_chain_divergence)
 void write_run(const Opts& o, const vp_params& P, const vp_result& r, int rep, int id, const std::vector<std::string>& inds,
                const std::vector<std::string>& pnames, const std::vector<int>& popid, const std::vector<int32_t>& k,
-               const std::vector<std::string>& locs, int S, int maxK) {
+               const std::vector<std::string>& locs, int S, int maxK, const std::vector<double>& H,
+               const std::vector<double>& D, const std::vector<double>& H2) {
     char fn[8192];
     const int K = r.K, N = r.N;
     const int64_t L = (int64_t)k.size();
@@ -306,30 +309,6 @@ void write_run(const Opts& o, const vp_params& P, const vp_result& r, int rep, i
     for (int i = 0; i < N; ++i) {
         w.lb(); w.s(inds[i].c_str()); w.d(); w.s(pnames[popid[i]].c_str()); w.d(); w.s("Total");
         for (int kk = 0; kk < K; ++kk) { w.d(); w.real(r.ancestry[(size_t)i * K + kk]); }
-    }
-    // heterozygosity and net nucleotide distance from the mean frequencies
-    std::vector<double> H(K, 0.0), D((size_t)K * K, 0.0), H2((size_t)K * L, 0.0);
-    for (int kk = 0; kk < K; ++kk) {
-        const float* p = r.freqm + (size_t)kk * r.KT;
-        for (int64_t l = 0; l < L; ++l) {
-            double ss = 0;
-            for (int a = 0; a < k[l]; ++a) ss += (double)p[a] * (double)p[a];
-            H2[(size_t)kk * L + l] = 1 - ss;
-            H[kk] += 1 - ss;
-            p += k[l];
-        }
-        H[kk] /= L;
-        for (int j = 0; j <= kk; ++j) {
-            const float *p1 = r.freqm + (size_t)kk * r.KT, *p2 = r.freqm + (size_t)j * r.KT;
-            double dt = 0;
-            for (int64_t l = 0; l < L; ++l) {
-                double sp = 0;
-                for (int a = 0; a < k[l]; ++a) sp += (double)p1[a] * (double)p2[a];
-                dt += 1 - sp;
-                p1 += k[l]; p2 += k[l];
-            }
-            D[(size_t)j * K + kk] = D[(size_t)kk * K + j] = dt / L - (H[kk] + H[j]) / 2;
-        }
     }
     w.lb(); w.lb(); w.s("Allele-frequency divergence among pops (Net nucleotide distance)");
     w.lb(); w.d(); w.s("Cluster"); w.lb(); w.s("Cluster");
@@ -448,7 +427,12 @@ int main(int argc, char** argv) {
         if (vp_chain_result(run.c, &r)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
         vp_params p = o.p;
         p.K = run.K;
-        write_run(o, p, r, run.rep, run.id, inds, pn, popid, ks, lnames, S, info.max_alleles);
+        std::vector<double> H(r.K), D((size_t)r.K * r.K), H2(o.diversity ? (size_t)r.K * info.n_loc : 0);
+        if (vp_chain_divergence(run.c, H.data(), D.data(), o.diversity ? H2.data() : nullptr)) {
+            fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error());
+            return 1;
+        }
+        write_run(o, p, r, run.rep, run.id, inds, pn, popid, ks, lnames, S, info.max_alleles, H, D, H2);
         table.push_back({rout[0], rout[2], rout[3]});
         vp_chain_destroy(run.c);
     }

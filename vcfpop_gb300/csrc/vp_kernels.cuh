@@ -1411,4 +1411,71 @@ __global__ void k_arrange(const DevChain* chains, double* ancestry) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Output reductions of WriteStructure (src/structure.cpp:293-324) on the mean
+// frequencies of a finished run: for every pair j <= k of clusters,
+//   G[k][j] = sum over loci of (1 - sum over alleles of p_k p_j)
+// in FP64 from exact float x float products (the reference's SumProd /
+// SumSquare of float frequencies into double). G[k][k] is the heterozygosity
+// sum, so H[k] = G[k][k] / L and D[k][j] = G[k][j] / L - (H[k] + H[j]) / 2.
+// grid.x = pair, grid.y = locus chunk; one FP64 partial per (pair, chunk),
+// summed in a fixed order by k_divergence_finish.
+constexpr int DIV_CHUNKS = 64;
+__global__ void __launch_bounds__(256) k_divergence_pairs(const DevChain* chains, double* part) {
+    const DevChain& c = chains[0];
+    const DevData& D = c.D;
+    __shared__ double sh[32];
+    int q = blockIdx.x, k = 0;
+    while (q > k) { q -= k + 1; ++k; }
+    const int j = q;
+    const float* pk = c.FreqM + (int64_t)k * D.KT;
+    const float* pj = c.FreqM + (int64_t)j * D.KT;
+    const int64_t per = (D.L + gridDim.y - 1) / gridDim.y;
+    const int64_t l0 = (int64_t)blockIdx.y * per, l1 = min(D.L, l0 + per);
+    double acc = 0;
+    for (int64_t l = l0 + threadIdx.x; l < l1; l += blockDim.x) {
+        const int64_t o = D.off[l];
+        const int k2 = D.k[l];
+        double sp = 0;
+        for (int a = 0; a < k2; ++a) sp += (double)pk[o + a] * (double)pj[o + a];
+        acc += 1 - sp;
+    }
+    const double t = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * gridDim.y + blockIdx.y] = t;
+}
+__global__ void k_divergence_finish(const DevChain* chains, const double* part, int nchunks, double* H, double* Dm) {
+    const DevChain& c = chains[0];
+    const int K = c.K;
+    const double L = (double)c.D.L;
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        for (int k = 0; k < K; ++k) {
+            const int q = k * (k + 1) / 2 + k;
+            double g = 0;
+            for (int b = 0; b < nchunks; ++b) g += part[(int64_t)q * nchunks + b];
+            H[k] = g / L;
+        }
+        for (int k = 0; k < K; ++k)
+            for (int j = 0; j <= k; ++j) {
+                const int q = k * (k + 1) / 2 + j;
+                double g = 0;
+                for (int b = 0; b < nchunks; ++b) g += part[(int64_t)q * nchunks + b];
+                Dm[j * K + k] = Dm[k * K + j] = g / L - (H[k] + H[j]) / 2;
+            }
+    }
+}
+// per-locus heterozygosity 1 - sum_a p^2 of every cluster (the diversity table)
+__global__ void k_heterozygosity(const DevChain* chains, double* Hl) {
+    const DevChain& c = chains[0];
+    const DevData& D = c.D;
+    const int64_t n = (int64_t)c.K * D.L;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t / D.L);
+        const int64_t l = t % D.L;
+        const float* p = c.FreqM + (int64_t)k * D.KT + D.off[l];
+        double ss = 0;
+        for (int a = 0; a < D.k[l]; ++a) ss += (double)p[a] * (double)p[a];
+        Hl[t] = 1 - ss;
+    }
+}
+
 }  // namespace vp

@@ -647,6 +647,46 @@ void vp_chain_progress(const vp_chain* c, int64_t* issued, int64_t* total) {
     *total = c->total;
 }
 
+extern "C" int vp_chain_divergence(vp_chain* c, double* H, double* D, double* Hl) {
+    if (!c || !H || !D) { vp_set_error("null argument"); return VP_E_ARG; }
+    if (!c->arranged) { vp_set_error("the chain is not finished (vp_finish arranges the mean frequencies)"); return VP_E_STATE; }
+    vp_ctx* x = c->ctx;
+    cudaSetDevice(x->device);
+    const int K = c->P.K;
+    const int npairs = K * (K + 1) / 2;
+    const int nch = (int)std::min<int64_t>(DIV_CHUNKS, std::max<int64_t>(1, x->L / 256));
+    const size_t pb = (size_t)npairs * nch * 8, hb = (size_t)K * 8, db = (size_t)K * K * 8;
+    const size_t lb = Hl ? (size_t)K * x->L * 8 : 0;
+    char* buf = nullptr;
+    CK(cudaMallocAsync((void**)&buf, pb + hb + db + lb + 64, x->stream));
+    double* part = (double*)buf;
+    double* dH = (double*)(buf + pb);
+    double* dD = (double*)(buf + pb + hb);
+    double* dHl = (double*)(buf + pb + hb + db);
+    int rc = VP_OK;
+    do {
+        k_divergence_pairs<<<dim3(npairs, nch, 1), 256, 0, x->stream>>>(c->d, part);
+        if ((rc = check_launch(x, "k_divergence_pairs"))) break;
+        k_divergence_finish<<<1, 32, 0, x->stream>>>(c->d, part, nch, dH, dD);
+        if ((rc = check_launch(x, "k_divergence_finish"))) break;
+        if (Hl) {
+            k_heterozygosity<<<std::min<unsigned>(4096, cdiv((int64_t)K * x->L, 256)), 256, 0, x->stream>>>(c->d, dHl);
+            if ((rc = check_launch(x, "k_heterozygosity"))) break;
+        }
+        cudaError_t e;
+        if ((e = cudaMemcpyAsync(H, dH, hb, cudaMemcpyDeviceToHost, x->stream)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(D, dD, db, cudaMemcpyDeviceToHost, x->stream)) != cudaSuccess ||
+            (Hl && (e = cudaMemcpyAsync(Hl, dHl, lb, cudaMemcpyDeviceToHost, x->stream)) != cudaSuccess)) {
+            vp_set_error("divergence copy-out failed: %s", cudaGetErrorString(e));
+            rc = VP_E_CUDA;
+        }
+    } while (0);
+    cudaFreeAsync(buf, x->stream);
+    cudaError_t e = cudaStreamSynchronize(x->stream);
+    if (!rc && e != cudaSuccess) { vp_set_error("divergence failed: %s", cudaGetErrorString(e)); rc = VP_E_CUDA; }
+    return rc;
+}
+
 extern "C" int vp_chain_sizes(vp_chain* c, vp_result* r) {
     if (!c || !r) { vp_set_error("null argument"); return VP_E_ARG; }
     memset(r, 0, sizeof *r);

@@ -189,6 +189,16 @@ class Chain:
         """Results; `final` (after vp_finish) adds the normalised ancestry."""
         return chain_result(self.h, final)
 
+    def divergence(self, per_locus: bool = False) -> dict:
+        """Heterozygosity H[K], net nucleotide distance D[K, K] (and the
+        per-locus heterozygosity [K, L]) of a finished chain, on the device."""
+        K, L = self.p.K, self.ctx.ds.L
+        H, D = np.zeros(K), np.zeros((K, K))
+        Hl = np.zeros((K, L)) if per_locus else None
+        B.check(B.lib().vp_chain_divergence(self.h, H.ctypes.data, D.ctypes.data,
+                                            None if Hl is None else Hl.ctypes.data))
+        return dict(H=H, D=D, Hl=Hl)
+
     def close(self):
         if getattr(self, "h", None):
             B.lib().vp_chain_destroy(self.h)
