@@ -42,7 +42,7 @@ METRIC = "genotype-cluster updates/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=150)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="tc", choices=["tc", "plain"])
@@ -601,7 +601,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cp = CpuPort(1000, KS)
+        cp = CpuPort(8000, KS)
         cp.sweep()
         dt = cp.sweep()
         cpu = {"value": cp.upd_sweep / dt, "unit": "updates/s", "cores": cp.threads, "kind": "port",
