@@ -185,6 +185,48 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- VCF ingest
+def vcf_text(packed, N):
+    """A biallelic diploid VCF data section (GT only) with the given calls."""
+    L = packed.shape[0]
+    shifts = (np.arange(16, dtype=np.uint32) * 2)
+    codes = ((packed[:, :, None] >> shifts) & 3).reshape(L, -1)[:, :N].astype(np.uint8)
+    table = np.frombuffer(b"0/0\t0/1\t1/1\t./.\t", dtype=np.uint8).reshape(4, 4)
+    body = table[codes]                          # [L, N, 4]
+    body[:, -1, 3] = ord("\n")
+    out = bytearray()
+    for l in range(L):
+        out += f"1\t{l + 1}\t.\tA\tC\t.\tPASS\t.\tGT\t".encode()
+        out += body[l].tobytes()
+    return bytes(out)
+
+
+def vcf_ingest(packed, N, args, rank, loci=20000):
+    """Device ingest of a VCF data section of `loci` lines of this dataset
+    (vp_vcf_pack2: upload from host memory, parse, packed matrix back) and,
+    as its CPU baseline, the oracle's line-by-line parse on one core."""
+    from vcfpop_gb300 import structure as S
+    text = vcf_text(packed[:loci], N)
+    S.vcf_pack2(text[:text.index(b"\n", len(text) // 8) + 1], N)   # warm-up on whole lines (context, allocator)
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        got, _ = S.vcf_pack2(text, N)
+    dev = (time.perf_counter() - t0) / reps
+    out = {"what": f"{loci} lines x {N} samples, {len(text) / 1e9:.2f} GB of VCF text, GT only",
+           "device_ms": dev * 1e3, "device_gbs": len(text) / dev / 1e9,
+           "exact": bool(np.array_equal(got, packed[:loci]))}
+    if rank == 0 and not args.no_cpu_baseline:
+        from tests import orc
+        t0 = time.perf_counter()
+        ref = orc.vcf_pack2(text, N, loci)
+        cpu = time.perf_counter() - t0
+        out.update({"cpu_baseline_ms": cpu * 1e3, "cpu_baseline_gbs": len(text) / cpu / 1e9,
+                    "cpu_baseline_kind": "port (the oracle's line-by-line GT parse, one core)",
+                    "cpu_equal": bool(np.array_equal(ref, got))})
+    return out
+
+
 # ---------------------------------------------------------------- output reductions
 def output_reductions(ctx, ds, args, rank):
     """WriteStructure's heterozygosity / net-distance / per-locus diversity
@@ -499,6 +541,7 @@ def main():
     form = B.VP_FORM_TC if args.form == "tc" else B.VP_FORM_PLAIN
 
     packed, pop = gen_packed_gpu(1234 + rank, N_IND, args.loci)
+    ingest = vcf_ingest(packed, N_IND, args, rank)
     ds = S.Dataset(np.full(N_IND, 2, np.int32), np.full(args.loci, 2, np.int32), pop, N_POP, packed2=packed)
     del packed
     sumK = sum(KS)
@@ -621,7 +664,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "step": f"open context from pinned host buffers + create 100 chains + {args.e2e_sweeps} sweeps "
                             f"+ read every chain's lnL + close", "ms_per_step": float(np.median(e2e_ms)) if e2e_ms else None},
-            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "outputs": outputs}
+            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "outputs": outputs, "ingest": ingest}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -237,6 +237,21 @@ int vp_prof_enable(vp_ctx* ctx, int on);
 /* Synchronise, then sum the dominant-kernel durations of the last sweep. */
 int vp_prof_read(vp_ctx* ctx, double* ms, int32_t* launches);
 
+/* ---- VCF ingest on the device ---------------------------------------------
+ * Replaces the genotype part of the reference's VCF loader (LoadVCF /
+ * AddVCFGenotype and GENO_WRITER, src/load.cpp) for biallelic diploid data.
+ * text[bytes] holds the data lines of a VCF (everything after the #CHROM
+ * header line), n_ind samples per line. Writes packed[n_loc][ceil(n_ind/16)]
+ * 2-bit codes (copies of allele 1; 3 = missing, also for a half-missing call
+ * and the padding), the input of vp_input.packed2, and, if line_start is not
+ * NULL, the n_loc + 1 byte offsets of the lines (their ends). With
+ * max_loci == 0 it only counts the lines into *n_loc. A line that is not
+ * biallelic, has a call that is not a diploid 0/1 genotype, or does not
+ * start its FORMAT with GT fails with VP_E_ARG naming the line; such data
+ * goes through a general reader. */
+int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int device, uint32_t* packed, int64_t max_loci,
+                 int64_t* line_start, int64_t* n_loc);
+
 /* ---- serving: many independent runs on one device ------------------------
  * Replaces the reference's run scheduling (BAYESIAN<REAL>::CalcBayesian and
  * BayesianThread, src/structure.cpp:2337-2501, with ManageCUDA's device

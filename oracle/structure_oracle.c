@@ -10,6 +10,7 @@
 #include "structure_oracle.h"
 #include "orc_core.h"
 #include <stdlib.h>
+#include <string.h>
 #include <stdio.h>
 #include <pthread.h>
 
@@ -1137,4 +1138,56 @@ void orc_divergence(const float* freqm, const int32_t* k, int64_t L, int64_t KT,
             D[j * K + a] = D[a * K + j] = dt / L - (H[a] + H[j]) / 2;
         }
     }
+}
+
+/* load.cpp AddVCFGenotype for biallelic diploid calls: one line at a time,
+ * fields split at tabs, the GT part of each sample field split at '/' or '|' */
+int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packed, int64_t max_loci) {
+    const int Nw = (n_ind + 15) / 16;
+    const char* p = text;
+    const char* end = text + bytes;
+    int64_t l = 0;
+    while (p < end) {
+        const char* e = memchr(p, '\n', (size_t)(end - p));
+        const char* le = e ? e : end;
+        if (le > p && le[-1] == '\r') --le;
+        if (l >= max_loci) return -(l + 1);
+        uint32_t* row = packed + l * Nw;
+        memset(row, 0, (size_t)Nw * 4);
+        int field = 0, nalt = 0;
+        const char* f = p;
+        while (f <= le) {
+            const char* t = memchr(f, '\t', (size_t)(le - f));
+            const char* fe = t ? t : le;
+            if (field == 4) {           /* alleles: REF + the comma-separated ALT list */
+                nalt = 2;
+                for (const char* c = f; c < fe; ++c) nalt += *c == ',';
+            } else if (field == 8) {
+                if (!(fe - f >= 2 && f[0] == 'G' && f[1] == 'T' && (fe - f == 2 || f[2] == ':'))) return -(l + 1);
+            } else if (field >= 9) {
+                const int i = field - 9;
+                if (i >= n_ind) return -(l + 1);
+                const char* g = f;
+                const char* ge = memchr(f, ':', (size_t)(fe - f));
+                if (!ge) ge = fe;
+                if (ge - g != 3 || (g[1] != '/' && g[1] != '|')) return -(l + 1);
+                int miss = 0, sum = 0;
+                for (int c = 0; c < 3; c += 2) {
+                    if (g[c] == '.') miss = 1;
+                    else if (g[c] == '0' || g[c] == '1') sum += g[c] - '0';
+                    else return -(l + 1);
+                }
+                row[i >> 4] |= (uint32_t)(miss ? 3 : sum) << (2 * (i & 15));
+            }
+            ++field;
+            if (!t) break;
+            f = t + 1;
+        }
+        if (field != 9 + n_ind || nalt != 2) return -(l + 1);
+        for (int i = n_ind; i < Nw * 16; ++i) row[i >> 4] |= 3u << (2 * (i & 15));
+        ++l;
+        if (!e) break;
+        p = e + 1;
+    }
+    return l;
 }

@@ -10,6 +10,7 @@
  */
 #ifndef STRUCTURE_ORACLE_H
 #define STRUCTURE_ORACLE_H
+#include <stddef.h>
 #include <stdint.h>
 #ifdef __cplusplus
 extern "C" {
@@ -130,6 +131,15 @@ void orc_loglik_noadmix(orc_chain* c, double* out);
  * with nthreads host threads, one chain at a time per thread: the run-level
  * parallelism of the reference's -structure_nstream (structure.cpp:2467-2499). */
 void orc_sweep_many(orc_chain** cs, int n, int nsweeps, int nthreads, int init);
+
+/* Genotypes of the data lines of a biallelic diploid VCF (the text after the
+ * #CHROM line) as 2-bit codes per call, packed 16 to a word: the copies of
+ * allele 1, 3 for a missing or half-missing call and for the padding. The
+ * GT key is the first FORMAT key; alleles are separated by '/' or '|'
+ * (the reference's VCF genotype reader, load.cpp AddVCFGenotype, for this
+ * case). Returns the number of lines, or -(line number) of the first line
+ * that is not biallelic diploid 0/1 data. */
+int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packed, int64_t max_loci);
 
 /* WriteStructure's heterozygosity and net nucleotide distance
  * (structure.cpp:293-324) on mean frequencies freqm[K][KT] of L loci with

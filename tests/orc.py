@@ -70,6 +70,8 @@ def lib():
         L.orc_sweep_many.restype = None
         L.orc_divergence.argtypes = [P, P, C.c_int64, C.c_int64, C.c_int, P, P, P]
         L.orc_divergence.restype = None
+        L.orc_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int, P, C.c_int64]
+        L.orc_vcf_pack2.restype = C.c_int64
         L.orc_hash_ulong_c.restype = C.c_uint32
         L.orc_hash_ulong_c.argtypes = [C.c_uint64]
         _lib = L
@@ -189,3 +191,14 @@ def divergence(freqm, k, K, per_locus=False):
     lib().orc_divergence(freqm.ctypes.data, k.ctypes.data, L, KT, K, H.ctypes.data, D.ctypes.data,
                          None if Hl is None else Hl.ctypes.data)
     return dict(H=H, D=D, Hl=Hl)
+
+
+def vcf_pack2(text: bytes, n_ind: int, max_loci: int):
+    """The oracle's biallelic diploid VCF genotype parse: (packed, lines) or
+    raises naming the first unsupported line."""
+    packed = np.zeros((max_loci, (n_ind + 15) // 16), np.uint32)
+    buf = np.frombuffer(text, dtype=np.uint8)
+    n = lib().orc_vcf_pack2(buf.ctypes.data, len(text), n_ind, packed.ctypes.data, max_loci)
+    if n < 0:
+        raise ValueError(f"data line {-n} is not biallelic diploid 0/1 data")
+    return packed[:n]

@@ -95,3 +95,11 @@ def test_server_without_gpu_fails_loudly():
         pytest.skip("GPU present")
     with pytest.raises(B.VpError, match="no CUDA device"):
         S.Server()
+
+
+def test_vcf_ingest_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    with pytest.raises(B.VpError, match="no CUDA device"):
+        S.vcf_pack2(b"1\t1\t.\tA\tC\t.\tPASS\t.\tGT\t0/1\n", 1)

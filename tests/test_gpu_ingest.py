@@ -1,0 +1,102 @@
+"""VCF genotype ingest on the device (vp_vcf_pack2) against the packing of
+the genotypes the VCF was written from: bit-exact on the committed golden
+VCFs and on synthetic files with phased/unphased calls, extra FORMAT keys,
+CRLF line ends, a missing final line feed and half-missing calls; lines
+outside the fast path fail with their line number."""
+import gzip
+import os
+
+import numpy as np
+import pytest
+
+from vcfpop_gb300 import _lib as B
+from vcfpop_gb300 import structure as S
+from vcfpop_gb300 import synth
+
+from . import orc
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _data_section(text: bytes):
+    i = text.index(b"\n#CHROM")
+    return text[text.index(b"\n", i + 1) + 1:]
+
+
+def _vcf(G, phased=False, extra=False, crlf=False, tail=True):
+    L, N, _ = G.shape
+    sep = "|" if phased else "/"
+    lines = []
+    for l in range(L):
+        calls = []
+        for i in range(N):
+            a, b = G[l, i]
+            c = "./." if a < 0 else f"{a}{sep}{b}"
+            calls.append(c + (":7" if extra else ""))
+        fmt = "GT:DP" if extra else "GT"
+        lines.append(f"1\t{l + 1}\t.\tA\tC\t.\tPASS\t.\t{fmt}\t" + "\t".join(calls))
+    nl = "\r\n" if crlf else "\n"
+    s = nl.join(lines) + (nl if tail else "")
+    return s.encode()
+
+
+@pytest.mark.parametrize("name,args", [("c1", (1, 200, 2000, 3, 0.1, 0.05)), ("adm", (2, 120, 400, 4, 0.05, 0.02))])
+def test_golden_vcfs_pack_exactly(name, args):
+    kw = dict(admix_alpha=0.5) if name == "adm" else {}
+    d = synth.fmodel(*args, **kw)                      # the data make_golden.py wrote
+    text = gzip.open(os.path.join(GOLD, f"{name}.vcf.gz"), "rb").read()
+    packed, starts = S.vcf_pack2(_data_section(text), d["G"].shape[1])
+    assert packed.shape[0] == d["G"].shape[0]
+    assert np.array_equal(packed, S.pack2(d["G"]))
+
+
+@pytest.mark.parametrize("phased,extra,crlf,tail", [(False, False, False, True), (True, True, False, True),
+                                                    (False, True, True, False), (True, False, True, True)])
+def test_synthetic_variants_pack_exactly(phased, extra, crlf, tail):
+    d = synth.fmodel(81, 333, 257, 3, 0.1, 0.1)         # 333 samples: a ragged last word
+    G = d["G"].copy()
+    if phased:
+        G = G[:, :, ::-1].copy()                       # 1|0 as well as 0|1
+        G[G[:, :, 0] < 0] = -1
+    text = _vcf(G, phased, extra, crlf, tail)
+    packed, starts = S.vcf_pack2(text, 333)
+    assert np.array_equal(packed, S.pack2(d["G"]))     # codes count allele 1: the copy order does not matter
+    assert np.array_equal(packed, orc.vcf_pack2(text, 333, packed.shape[0]))
+    assert starts[0] == 0 and starts[-1] == len(text)
+
+
+def test_half_missing_call_is_missing():
+    G = np.array([[[0, 1], [1, 1], [0, 0]]], np.int8)
+    text = _vcf(G).replace(b"\t1/1", b"\t1/.")
+    packed, _ = S.vcf_pack2(text, 3)
+    assert packed[0, 0] & 0x3F == (1 | (3 << 2) | (0 << 4))
+
+
+@pytest.mark.parametrize("bad,what", [(b"A\tC,G", "2 alleles"), (b"\t0\t", "diploid"), (b"GT\t", "GT is not")])
+def test_unsupported_lines_name_the_line(bad, what):
+    d = synth.fmodel(82, 20, 30, 2, 0.1, 0.0)
+    text = _vcf(d["G"])
+    lines = text.split(b"\n")
+    if bad == b"A\tC,G":
+        lines[4] = lines[4].replace(b"A\tC", b"A\tC,G", 1)
+    elif bad == b"\t0\t":
+        parts = lines[4].split(b"\t")
+        parts[12] = b"0"
+        lines[4] = b"\t".join(parts)
+    else:
+        lines[4] = lines[4].replace(b"\tGT\t", b"\tDP:GT\t", 1)
+    with pytest.raises(B.VpError, match=f"data line 5: .*{what}"):
+        S.vcf_pack2(b"\n".join(lines), 20)
+
+
+def test_packed_vcf_runs_a_chain():
+    d = synth.fmodel(83, 400, 1500, 3, 0.1, 0.02)
+    packed, _ = S.vcf_pack2(_vcf(d["G"]), 400)
+    ds = S.Dataset(np.full(400, 2, np.int32), np.full(1500, 2, np.int32), d["pop"], 3, packed2=packed)
+    ref = S.Dataset.from_synth(d)
+    assert np.array_equal(ds.order(), ref.order())
+    ctx = S.Context(ds)
+    ch = S.Chain(ctx, S.params(3, 5, admix=0, nadmburnin=0, nburnin=5, nreps=5))
+    S.finish([ch])
+    assert np.isfinite(ch.result()["rout"]).all()

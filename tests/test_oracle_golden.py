@@ -67,3 +67,19 @@ def test_oracle_divergence_reproduces_reference_d_block(oracle_build):
     want = np.array(_d_block(os.path.join(GOLD, "c1_noadmix", "out.structure.k=3_rep=1_id=1.txt"), K))
     assert np.abs(out["D"] - want).max() < 1e-14, (out["D"], want)
     assert np.allclose(out["Hl"].mean(axis=1), out["H"])
+
+
+@pytest.mark.parametrize("name,args,kw", [("c1", (1, 200, 2000, 3, 0.1, 0.05), {}),
+                                         ("adm", (2, 120, 400, 4, 0.05, 0.02), {"admix_alpha": 0.5})])
+def test_oracle_vcf_parse_matches_golden_data(name, args, kw, oracle_build):
+    """The oracle's VCF genotype parse, on the committed golden VCFs, gives the
+    2-bit packing of the genotypes those files were written from."""
+    import numpy as np
+    from vcfpop_gb300 import structure as S
+    from vcfpop_gb300 import synth
+    from . import orc
+    d = synth.fmodel(*args, **kw)
+    t = gzip.open(os.path.join(GOLD, f"{name}.vcf.gz"), "rb").read()
+    i = t.index(b"\n#CHROM")
+    data = t[t.index(b"\n", i + 1) + 1:]
+    assert np.array_equal(orc.vcf_pack2(data, d["G"].shape[1], d["G"].shape[0]), S.pack2(d["G"]))

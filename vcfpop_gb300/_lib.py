@@ -74,7 +74,7 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_divergence", "vp_chain_step", "vp_chain_get",
            "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
-           "vp_release", "vp_server_close"]
+           "vp_release", "vp_server_close", "vp_vcf_pack2"]
 
 
 def lib():
@@ -129,6 +129,7 @@ def lib():
     L.vp_request_chain.argtypes = [P, C.c_int64, C.POINTER(P)]
     L.vp_release.argtypes = [P, C.c_int64]
     L.vp_server_close.argtypes = [P]
+    L.vp_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int32, C.c_int, P, C.c_int64, P, P]
     _lib = L
     return L
 

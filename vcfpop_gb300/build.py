@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -ffp-contract=off build; hot loops that want FMA use explicit intrinsics.
 FLAGS = ["-O3", "--fmad=false", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"] + ARCH
 
-CU = ["vp_structure.cu"]
+CU = ["vp_structure.cu", "vp_ingest.cu"]
 CPP = ["vp_data.cpp", "vp_server.cpp"]  # vp_cli.cpp is the driver binary, built with g++ below
 
 

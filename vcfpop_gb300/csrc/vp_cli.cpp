@@ -178,6 +178,75 @@ bool read_vcf(const std::string& path, Vcf& v) {
     return nl > 0;
 }
 
+// The whole file in memory (gzip or plain), then its genotypes parsed on the
+// device into the 2-bit matrix (vp_vcf_pack2). Biallelic diploid data only:
+// returns false (the host reader takes over) for anything else.
+bool read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
+    gzFile f = gzopen(o.input.c_str(), "rb");
+    if (!f) return false;
+    std::vector<char> text;
+    size_t n = 0;
+    text.resize(1 << 26);
+    for (;;) {
+        if (text.size() - n < (1u << 24)) text.resize(text.size() * 2);
+        int got = gzread(f, text.data() + n, (unsigned)std::min<size_t>(text.size() - n, 1u << 30));
+        if (got <= 0) break;
+        n += (size_t)got;
+    }
+    gzclose(f);
+    // header: skip ## lines, take the sample names of the #CHROM line
+    size_t p = 0;
+    while (p < n && text[p] == '#' && p + 1 < n && text[p + 1] == '#') {
+        const char* e = (const char*)memchr(text.data() + p, '\n', n - p);
+        if (!e) return false;
+        p = (size_t)(e - text.data()) + 1;
+    }
+    if (p >= n || text[p] != '#') return false;
+    const char* he = (const char*)memchr(text.data() + p, '\n', n - p);
+    if (!he) return false;
+    std::string hdr(text.data() + p, he - (text.data() + p));
+    while (!hdr.empty() && hdr.back() == '\r') hdr.pop_back();
+    int col = 0;
+    size_t s0 = 0;
+    for (;;) {
+        size_t t = hdr.find('\t', s0);
+        if (col >= 9) v.inds.push_back(hdr.substr(s0, t == std::string::npos ? std::string::npos : t - s0));
+        ++col;
+        if (t == std::string::npos) break;
+        s0 = t + 1;
+    }
+    const int N = (int)v.inds.size();
+    if (N == 0) return false;
+    const char* data = he + 1;
+    const size_t bytes = n - (size_t)(data - text.data());
+    int64_t L = 0;
+    for (const char* q = data; (q = (const char*)memchr(q, '\n', bytes - (q - data))); ++q) ++L;
+    if (bytes && data[bytes - 1] != '\n') ++L;
+    if (L == 0) return false;
+    const int Nw = (N + 15) / 16;
+    packed.assign((size_t)L * Nw, 0);
+    std::vector<int64_t> starts(L + 1);
+    int64_t got = 0;
+    if (vp_vcf_pack2(data, bytes, N, o.device, packed.data(), L, starts.data(), &got) || got != L) {
+        fprintf(stderr, "vcfpop-gb300: device ingest not used (%s); reading on the host\n", vp_last_error());
+        v.inds.clear();
+        packed.clear();
+        return false;
+    }
+    v.vmax = 2;
+    v.ploidy.assign(N, 2);
+    v.k.assign(L, 2);
+    v.locs.resize(L);
+    for (int64_t l = 0; l < L; ++l) {
+        const char* a = data + starts[l];
+        const char* t1 = (const char*)memchr(a, '\t', data + starts[l + 1] - a);
+        const char* t2 = t1 ? (const char*)memchr(t1 + 1, '\t', data + starts[l + 1] - t1 - 1) : nullptr;
+        if (!t1 || !t2) return false;
+        v.locs[l] = std::string(a, t1 - a) + "_" + std::string(t1 + 1, t2 - t1 - 1);
+    }
+    return true;
+}
+
 // -g_indtext="pop1:#1-#30,#40 pop2:#31-#39 ..." (1-based individual ranges)
 void populations(const std::string& spec, int N, std::vector<int>& popid, std::vector<std::string>& names) {
     popid.assign(N, -1);
@@ -341,7 +410,9 @@ int main(int argc, char** argv) {
     Opts o;
     if (!parse(argc, argv, o)) return 2;
     Vcf v;
-    if (!read_vcf(o.input, v)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
+    std::vector<uint32_t> dev_packed;   // device-parsed 2-bit matrix, file order of individuals
+    const bool dev_ingest = read_vcf_device(o, v, dev_packed);
+    if (!dev_ingest && !read_vcf(o.input, v)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
     const int N = (int)v.inds.size();
     const int64_t L0 = (int64_t)v.k.size();
     std::vector<int> pop;
@@ -353,12 +424,15 @@ int main(int argc, char** argv) {
     std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return pop[a] < pop[b]; });
     std::vector<std::string> inds(N);
     std::vector<int32_t> ploidy(N), popid(N);
-    std::vector<int8_t> G((size_t)L0 * N * v.vmax);
+    std::vector<int8_t> G(dev_ingest ? 0 : (size_t)L0 * N * v.vmax);
+    bool identity = true;
     for (int j = 0; j < N; ++j) {
         int i = perm[j];
+        identity &= i == j;
         inds[j] = v.inds[i]; ploidy[j] = v.ploidy[i]; popid[j] = pop[i];
-        for (int64_t l = 0; l < L0; ++l)
-            memcpy(&G[((size_t)l * N + j) * v.vmax], &v.G[((size_t)l * N + i) * v.vmax], v.vmax);
+        if (!dev_ingest)
+            for (int64_t l = 0; l < L0; ++l)
+                memcpy(&G[((size_t)l * N + j) * v.vmax], &v.G[((size_t)l * N + i) * v.vmax], v.vmax);
     }
     // drop populations without individuals, keeping the order
     std::vector<int> remap(pnames.size(), -1);
@@ -374,7 +448,23 @@ int main(int argc, char** argv) {
     vp_input in{};
     in.n_ind = N; in.n_loc = L0; in.vmax = v.vmax; in.ploidy = ploidy.data(); in.n_alleles = v.k.data();
     in.popid = popid.data(); in.n_pop = S;
-    if (biallelic_diploid) {
+    if (dev_ingest && identity) {
+        in.packed2 = dev_packed.data();
+    } else if (dev_ingest) {
+        // regroup the individuals of the device-parsed matrix by population
+        const int Nw = (N + 15) / 16;
+        packed.assign((size_t)L0 * Nw, 0);
+        for (int64_t l = 0; l < L0; ++l) {
+            const uint32_t* src = &dev_packed[(size_t)l * Nw];
+            uint32_t* dst = &packed[(size_t)l * Nw];
+            for (int j = 0; j < Nw * 16; ++j) {
+                uint32_t code = 3;
+                if (j < N) code = (src[perm[j] >> 4] >> (2 * (perm[j] & 15))) & 3u;
+                dst[j >> 4] |= code << (2 * (j & 15));
+            }
+        }
+        in.packed2 = packed.data();
+    } else if (biallelic_diploid) {
         const int Nw = (N + 15) / 16;
         packed.assign((size_t)L0 * Nw, 0);
         for (int64_t l = 0; l < L0; ++l)

@@ -1,0 +1,356 @@
+// VCF genotype ingest on the device: the data lines of a VCF (the text after
+// the #CHROM header line) become the 2-bit packed genotype matrix of a
+// biallelic diploid dataset, the store the STRUCTURE sweep reads.
+//
+// The reference reads VCF line by line on the host (LoadVCF / AddVCFGenotype,
+// src/load.cpp; GENO_WRITER packs the genotype ids). Here the text is uploaded
+// once and parsed in parallel:
+//   0. upload: through two pinned staging buffers, the host copy of one
+//      overlapping the DMA of the other;
+//   1. line index: one warp per 4 KB chunk (coalesced 16-byte loads) counts
+//      its line feeds, an exclusive scan of the counts, then the warp writes
+//      the start offsets of its lines in order;
+//   2. one CTA per line: the threads split the line's bytes, a block scan
+//      numbers the tabs, the tab before field 5 (ALT) gives the allele count,
+//      the FORMAT field must start with GT, and the owner of the tab before
+//      each sample field decodes its call ("a/b" or "a|b", a and b in {0, 1,
+//      .}, ending at ':', tab or end of line) into a shared-memory row of
+//      packed words, written out coalesced.
+// A line outside this fast path (not two alleles, a call that is not diploid
+// 0/1, GT not the first FORMAT key, a wrong field count) is reported with its
+// line number; the caller then uses a general reader.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "vp_internal.h"
+
+namespace {
+
+constexpr int CHUNK = 4096;
+constexpr int PB = 256;  // threads per line CTA
+
+#define CKI(call)                                                                 \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            vp_set_error("%s failed: %s", #call, cudaGetErrorString(e_));         \
+            return VP_E_CUDA;                                                     \
+        }                                                                         \
+    } while (0)
+
+// line feeds among the 16 bytes at p (bytes at or past n do not count)
+__device__ __forceinline__ uint32_t lf_mask16(const char* t, int64_t p, int64_t n) {
+    uint32_t m = 0;
+    if (p + 16 <= n) {
+        const uint4 v = *reinterpret_cast<const uint4*>(t + p);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t eq = __vcmpeq4(w[j], 0x0A0A0A0Au);   // 0xFF per matching byte
+#pragma unroll
+            for (int b = 0; b < 4; ++b) m |= ((eq >> (8 * b)) & 1u) << (4 * j + b);
+        }
+    } else {
+        for (int j = 0; j < 16 && p + j < n; ++j) m |= (uint32_t)(t[p + j] == '\n') << j;
+    }
+    return m;
+}
+
+// one warp per chunk of CHUNK bytes: lane L reads 16 bytes at 16 * (32 * it + L)
+__global__ void k_count_lf(const char* t, int64_t n, int64_t nchunks, int64_t* cnt) {
+    const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (c >= nchunks) return;
+    const int64_t s = c * CHUNK;
+    int k = 0;
+    for (int it = 0; it < CHUNK / 512; ++it) {
+        const int64_t p = s + (int64_t)(it * 32 + lane) * 16;
+        if (p < n) k += __popc(lf_mask16(t, p, n));
+    }
+    for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    if (lane == 0) cnt[c] = k;
+}
+
+// exclusive scan of n counts in one CTA (n up to a few million: chunked)
+__global__ void k_scan(int64_t* v, int64_t n) {
+    __shared__ int64_t sh[1024];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t base = 0; base < n; base += 1024) {
+        const int64_t i = base + threadIdx.x;
+        const int64_t x = i < n ? v[i] : 0;
+        sh[threadIdx.x] = x;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            int64_t y = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += y;
+            __syncthreads();
+        }
+        if (i < n) v[i] = carry + sh[threadIdx.x] - x;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += sh[1023];
+        __syncthreads();
+    }
+}
+
+// start offsets of the lines: line 0 at 0, line j + 1 after the j-th line
+// feed; the warp of a chunk walks it in 512-byte steps, and a warp prefix
+// sum of the lanes' counts puts their line feeds in order
+__global__ void k_line_starts(const char* t, int64_t n, int64_t nchunks, const int64_t* pre, int64_t* start) {
+    const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (c >= nchunks) return;
+    const int64_t s = c * CHUNK;
+    int64_t j = pre[c];
+    for (int it = 0; it < CHUNK / 512; ++it) {
+        const int64_t p = s + (int64_t)(it * 32 + lane) * 16;
+        uint32_t m = p < n ? lf_mask16(t, p, n) : 0u;
+        const int cntl = __popc(m);
+        int incl = cntl;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        int64_t q = j + incl - cntl;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            start[++q] = p + b + 1;
+        }
+        j += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+struct LineOut {
+    int32_t* bad;     // [L] 0 = ok, else a reason code
+    int32_t* nalt;    // [L] ALT alleles
+};
+
+// one CTA per line
+__global__ void __launch_bounds__(PB) k_parse_lines(const char* t, const int64_t* start, int64_t L, int N, int Nw,
+                                                    uint32_t* packed, LineOut out) {
+    extern __shared__ uint32_t row[];   // [Nw]
+    __shared__ int warp_tabs[PB / 32];
+    __shared__ int err;
+    __shared__ int nalt_s;
+    const int64_t l = blockIdx.x;
+    if (l >= L) return;
+    const int64_t s = start[l];
+    int64_t e = start[l + 1];
+    // trim the line feed (and a carriage return before it)
+    if (e > s && t[e - 1] == '\n') --e;
+    if (e > s && t[e - 1] == '\r') --e;
+    for (int w = threadIdx.x; w < Nw; w += PB) row[w] = 0;
+    if (threadIdx.x == 0) { err = 0; nalt_s = 0; }
+    const int64_t len = e - s;
+    const int64_t seg = (len + PB - 1) / PB;
+    const int64_t a = s + min(len, (int64_t)threadIdx.x * seg), b = s + min(len, (int64_t)(threadIdx.x + 1) * seg);
+    int mine = 0;
+    for (int64_t p = a; p < b; ++p) mine += t[p] == '\t';
+    // block exclusive scan of the tab counts
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tabs[warp] = incl;
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += warp_tabs[w];
+    int total = 0;
+    for (int w = 0; w < PB / 32; ++w) total += warp_tabs[w];
+    int f = before + incl - mine;   // index of the next tab this thread meets
+    if (threadIdx.x == 0 && total != 8 + N) err = 1;   // 9 fixed fields + N samples
+    for (int64_t p = a; p < b; ++p) {
+        if (t[p] != '\t') continue;
+        const int field = f + 1;    // the field that starts after this tab
+        ++f;
+        const char* q = t + p + 1;
+        const int64_t room = e - (p + 1);
+        if (field == 4) {          // ALT: alleles = commas + 1
+            int commas = 0;
+            for (int64_t r = 0; r < room && q[r] != '\t'; ++r) commas += q[r] == ',';
+            nalt_s = commas + 1;
+        } else if (field == 8) {   // FORMAT must start with GT
+            if (!(room >= 2 && q[0] == 'G' && q[1] == 'T' && (room == 2 || q[2] == ':' || q[2] == '\t'))) err = 2;
+        } else if (field >= 9) {
+            const int i = field - 9;
+            if (i >= N) { err = 1; continue; }
+            // "x/y" or "x|y", x, y in {0, 1, .}, then ':' or tab or end of line
+            if (room < 3 || (q[1] != '/' && q[1] != '|') || (room > 3 && q[3] != ':' && q[3] != '\t')) { err = 3; continue; }
+            const char x = q[0], y = q[2];
+            const bool mx = x == '.', my = y == '.';
+            if ((!mx && x != '0' && x != '1') || (!my && y != '0' && y != '1')) { err = 3; continue; }
+            const uint32_t code = (mx || my) ? 3u : (uint32_t)((x - '0') + (y - '0'));
+            atomicOr(&row[i >> 4], code << (2 * (i & 15)));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int bad = err;
+        if (!bad && nalt_s != 1) bad = 4;
+        out.bad[l] = bad;
+        out.nalt[l] = nalt_s;
+    }
+    // padding individuals of the last word are missing (3)
+    for (int w = threadIdx.x; w < Nw; w += PB) {
+        uint32_t v = row[w];
+        const int i0 = w * 16;
+        for (int j = 0; j < 16; ++j)
+            if (i0 + j >= N) v |= 3u << (2 * j);
+        packed[l * (int64_t)Nw + w] = v;
+    }
+}
+
+// host text -> device through two pinned staging buffers: the host copy into
+// one overlaps the DMA out of the other
+int upload_staged(char* dst, const char* src, int64_t n, cudaStream_t st) {
+    constexpr size_t STAGE = 32u << 20;
+    char* stage[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int rc = VP_OK;
+    if (cudaMallocHost((void**)&stage[0], STAGE) != cudaSuccess || cudaMallocHost((void**)&stage[1], STAGE) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming) != cudaSuccess) {
+        vp_set_error("pinned staging buffers for the upload could not be allocated");
+        rc = VP_E_MEM;
+    }
+    int b = 0;
+    bool used[2] = {false, false};
+    for (int64_t off = 0; !rc && off < n; off += STAGE, b ^= 1) {
+        const size_t len = (size_t)std::min<int64_t>(STAGE, n - off);
+        if (used[b] && cudaEventSynchronize(ev[b]) != cudaSuccess) { vp_set_error("upload failed"); rc = VP_E_CUDA; break; }
+        memcpy(stage[b], src + off, len);
+        cudaError_t e = cudaMemcpyAsync(dst + off, stage[b], len, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[b], st);
+        if (e != cudaSuccess) { vp_set_error("upload failed: %s", cudaGetErrorString(e)); rc = VP_E_CUDA; break; }
+        used[b] = true;
+    }
+    // the staging buffers are released only after their copies completed
+    for (int j = 0; j < 2; ++j)
+        if (used[j]) cudaEventSynchronize(ev[j]);
+    for (int j = 0; j < 2; ++j) {
+        if (ev[j]) cudaEventDestroy(ev[j]);
+        if (stage[j]) cudaFreeHost(stage[j]);
+    }
+    return rc;
+}
+
+const char* reason(int code) {
+    switch (code) {
+        case 1: return "the number of fields is not 9 + the number of samples";
+        case 2: return "GT is not the first FORMAT key";
+        case 3: return "a call is not a diploid 0/1 genotype";
+        case 4: return "the locus does not have exactly 2 alleles";
+    }
+    return "unknown";
+}
+
+}  // namespace
+
+extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int device, uint32_t* packed,
+                            int64_t max_loci, int64_t* line_start, int64_t* n_loc) {
+    if (!text || !n_loc || n_ind <= 0 || (max_loci > 0 && !packed)) { vp_set_error("bad arguments"); return VP_E_ARG; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
+    if (device < 0 || device >= ndev) { vp_set_error("device %d out of range", device); return VP_E_ARG; }
+    CKI(cudaSetDevice(device));
+    const int Nw = (n_ind + 15) / 16;
+    if ((size_t)Nw * 4 > 200 * 1024) { vp_set_error("too many samples for one line row in shared memory"); return VP_E_ARG; }
+    cudaStream_t st;
+    CKI(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const int64_t n = (int64_t)bytes;
+    const int64_t nchunks = (n + CHUNK - 1) / CHUNK;
+    char* dt = nullptr;
+    int64_t *cnt = nullptr, *starts = nullptr;
+    int rc = VP_OK;
+    do {
+        cudaError_t e;
+        if ((e = cudaMallocAsync((void**)&dt, n + 1, st)) != cudaSuccess ||
+            (e = cudaMallocAsync((void**)&cnt, (nchunks + 1) * 8, st)) != cudaSuccess) {
+            vp_set_error("device allocation for the text failed: %s", cudaGetErrorString(e));
+            rc = VP_E_MEM;
+            break;
+        }
+        if ((rc = upload_staged(dt, text, n, st))) break;
+        const unsigned g = (unsigned)((nchunks * 32 + 255) / 256);
+        k_count_lf<<<g, 256, 0, st>>>(dt, n, nchunks, cnt);
+        cudaMemsetAsync(cnt + nchunks, 0, 8, st);
+        k_scan<<<1, 1024, 0, st>>>(cnt, nchunks + 1);
+        int64_t nlf = 0;
+        if ((e = cudaMemcpyAsync(&nlf, cnt + nchunks, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+            vp_set_error("line index failed: %s", cudaGetErrorString(e));
+            rc = VP_E_CUDA;
+            break;
+        }
+        // a last line without a line feed counts too
+        const bool tail = n > 0 && text[n - 1] != '\n';
+        const int64_t L = nlf + (tail ? 1 : 0);
+        *n_loc = L;
+        if (max_loci <= 0) break;                       // size query
+        if (L > max_loci) { vp_set_error("%lld loci, buffer holds %lld", (long long)L, (long long)max_loci); rc = VP_E_ARG; break; }
+        if (L == 0) break;
+        if ((e = cudaMallocAsync((void**)&starts, (nlf + 2) * 8, st)) != cudaSuccess) {
+            vp_set_error("device allocation failed: %s", cudaGetErrorString(e));
+            rc = VP_E_MEM;
+            break;
+        }
+        cudaMemsetAsync(starts, 0, 8, st);
+        k_line_starts<<<g, 256, 0, st>>>(dt, n, nchunks, cnt, starts);
+        // the end of the last line
+        int64_t endv = n;
+        cudaMemcpyAsync(starts + L, &endv, 8, cudaMemcpyHostToDevice, st);
+        uint32_t* dp = nullptr;
+        int32_t* flags = nullptr;
+        if ((e = cudaMallocAsync((void**)&dp, (size_t)L * Nw * 4, st)) != cudaSuccess ||
+            (e = cudaMallocAsync((void**)&flags, (size_t)L * 8, st)) != cudaSuccess) {
+            vp_set_error("device allocation failed: %s", cudaGetErrorString(e));
+            rc = VP_E_MEM;
+            if (dp) cudaFreeAsync(dp, st);
+            break;
+        }
+        for (int64_t l0 = 0; l0 < L; l0 += 1 << 30) {
+            const unsigned nb = (unsigned)std::min<int64_t>(L - l0, 1 << 30);
+            k_parse_lines<<<nb, PB, (size_t)Nw * 4, st>>>(dt, starts + l0, nb, n_ind, Nw, dp + l0 * Nw,
+                                                          LineOut{flags + l0, flags + L + l0});
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            vp_set_error("parse launch failed: %s", cudaGetErrorString(e));
+            rc = VP_E_CUDA;
+        }
+        std::vector<int32_t> hb(L);
+        if (!rc && ((e = cudaMemcpyAsync(packed, dp, (size_t)L * Nw * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                    (e = cudaMemcpyAsync(hb.data(), flags, (size_t)L * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                    (line_start && (e = cudaMemcpyAsync(line_start, starts, (size_t)(L + 1) * 8, cudaMemcpyDeviceToHost,
+                                                        st)) != cudaSuccess))) {
+            vp_set_error("copy-out failed: %s", cudaGetErrorString(e));
+            rc = VP_E_CUDA;
+        }
+        cudaFreeAsync(dp, st);
+        cudaFreeAsync(flags, st);
+        if (!rc && (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+            vp_set_error("parse failed: %s", cudaGetErrorString(e));
+            rc = VP_E_CUDA;
+        }
+        if (!rc)
+            for (int64_t l = 0; l < L; ++l)
+                if (hb[l]) {
+                    vp_set_error("data line %lld: %s", (long long)(l + 1), reason(hb[l]));
+                    rc = VP_E_ARG;
+                    break;
+                }
+    } while (0);
+    if (starts) cudaFreeAsync(starts, st);
+    if (cnt) cudaFreeAsync(cnt, st);
+    if (dt) cudaFreeAsync(dt, st);
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    return rc;
+}

@@ -209,6 +209,20 @@ class Chain:
             self.close()
 
 
+def vcf_pack2(text: bytes, n_ind: int, device: int = 0):
+    """Parse the data lines of a biallelic diploid VCF on the device: returns
+    (packed [L][ceil(N/16)] uint32 2-bit codes, line offsets [L + 1])."""
+    buf = np.frombuffer(text, dtype=np.uint8)
+    # a well-formed line holds 9 fields and n_ind calls of 3 bytes, each after a tab
+    L = len(text) // (4 * n_ind + 17) + 1
+    packed = np.empty((L, (n_ind + 15) // 16), np.uint32)
+    starts = np.empty(L + 1, np.int64)
+    n = C.c_int64()
+    B.check(B.lib().vp_vcf_pack2(buf.ctypes.data, len(text), n_ind, device, packed.ctypes.data, max(L, 1),
+                                 starts.ctypes.data, C.byref(n)))
+    return packed[:n.value], starts[:n.value + 1]
+
+
 def chain_result(h, final: bool = False) -> dict:
     r = B.VpResult()
     B.check(B.lib().vp_chain_sizes(h, C.byref(r)))
