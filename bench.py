@@ -227,6 +227,37 @@ def vcf_ingest(packed, N, args, rank, loci=20000):
     return out
 
 
+# ---------------------------------------------------------------- locus filter
+def locus_filter_leg(packed, N, args, rank, sample=20000):
+    """The -f_* locus filter (vp_locus_filter_pack2: statistics and pass
+    flags of every locus, copies included) on the whole packed matrix, and as
+    its CPU baseline the oracle's restatement on one core over a sample of
+    loci, scaled to the same count."""
+    from vcfpop_gb300 import structure as S
+    f = S.locus_filter_spec(bmaf=(0.05, 0.5), ptype=(0.9, 1.0), he=(0.05, 0.5))
+    S.locus_filter(packed[:1000], N, f)               # warm-up
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        keep, _ = S.locus_filter(packed, N, f)
+    dev = (time.perf_counter() - t0) / reps
+    out = {"what": f"{packed.shape[0]} loci x {N} samples ({packed.nbytes / 1e9:.2f} GB packed), "
+                   f"-f_bmaf=[0.05,0.5] -f_ptype=[0.9,1] -f_he=[0.05,0.5]",
+           "device_ms": dev * 1e3, "device_gbs": packed.nbytes / dev / 1e9, "kept": int(keep.sum())}
+    if rank == 0 and not args.no_cpu_baseline:
+        from tests import orc
+        o = orc.LocusFilter()
+        for name, _ in orc.LocusFilter._fields_:
+            setattr(o, name, getattr(f, name))
+        n = min(sample, packed.shape[0])
+        t0 = time.perf_counter()
+        okeep, _ = orc.locus_filter_pack2(packed[:n], N, o)
+        cpu = (time.perf_counter() - t0) * packed.shape[0] / n
+        out.update({"cpu_baseline_ms": cpu * 1e3, "cpu_baseline_kind": f"port (the oracle on one core, {n} loci, scaled)",
+                    "cpu_equal_on_sample": bool(np.array_equal(okeep, keep[:n]))})
+    return out
+
+
 # ---------------------------------------------------------------- output reductions
 def output_reductions(ctx, ds, args, rank):
     """WriteStructure's heterozygosity / net-distance / per-locus diversity
@@ -542,6 +573,7 @@ def main():
 
     packed, pop = gen_packed_gpu(1234 + rank, N_IND, args.loci)
     ingest = vcf_ingest(packed, N_IND, args, rank)
+    lfilter = locus_filter_leg(packed, N_IND, args, rank)
     ds = S.Dataset(np.full(N_IND, 2, np.int32), np.full(args.loci, 2, np.int32), pop, N_POP, packed2=packed)
     del packed
     sumK = sum(KS)
@@ -664,7 +696,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "step": f"open context from pinned host buffers + create 100 chains + {args.e2e_sweeps} sweeps "
                             f"+ read every chain's lnL + close", "ms_per_step": float(np.median(e2e_ms)) if e2e_ms else None},
-            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "outputs": outputs, "ingest": ingest}
+            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "outputs": outputs, "ingest": ingest, "locus_filter": lfilter}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

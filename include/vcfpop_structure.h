@@ -252,6 +252,28 @@ int vp_prof_read(vp_ctx* ctx, double* ms, int32_t* launches);
 int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int device, uint32_t* packed, int64_t max_loci,
                  int64_t* line_start, int64_t* n_loc);
 
+/* Locus filter of the reference (-f_bmaf, -f_k, -f_n, -f_ptype, -f_he, -f_ho,
+ * -f_pic, -f_ae, -f_I: MarkerDiversity, src/filter.cpp:485-507, on the
+ * statistics of DIVERSITY::CalcDiversity, src/diversity.cpp:144-311). Each
+ * window is used when its flag is set; a locus fails when no call is typed
+ * or any used statistic falls outside its window (a NaN statistic passes,
+ * as in the reference). The HWE test filter (-f_pval) is not included. */
+typedef struct {
+    int32_t bmaf_b, k_b, n_b, ptype_b, he_b, ho_b, pic_b, ae_b, I_b;
+    int32_t k_min, k_max, n_min, n_max;
+    int32_t single;   /* statistics in float (the reference's REAL under -g_float=single), else double */
+    double bmaf_min, bmaf_max, ptype_min, ptype_max, he_min, he_max, ho_min, ho_max;
+    double pic_min, pic_max, ae_min, ae_max, I_min, I_max;
+} vp_locus_filter;
+#define VP_LOCUS_STATS 9   /* n, k, ptype, bmaf, he, ho, pic, ae, I */
+/* The statistics and the pass flag of every locus of a packed biallelic
+ * diploid matrix (packed[n_loc][ceil(n_ind/16)], as vp_input.packed2) on the
+ * device: keep[n_loc] = 1 if the locus passes; stats[n_loc][VP_LOCUS_STATS]
+ * (optional) in double, NaN where the reference leaves a statistic
+ * undefined (fewer than 2 alleles). Host buffers; synchronous. */
+int vp_locus_filter_pack2(const uint32_t* packed, int64_t n_loc, int32_t n_ind, const vp_locus_filter* f, int device,
+                          uint8_t* keep, double* stats);
+
 /* ---- serving: many independent runs on one device ------------------------
  * Replaces the reference's run scheduling (BAYESIAN<REAL>::CalcBayesian and
  * BayesianThread, src/structure.cpp:2337-2501, with ManageCUDA's device

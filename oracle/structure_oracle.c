@@ -1191,3 +1191,75 @@ int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packe
     }
     return l;
 }
+
+/* diversity.cpp:144-311 for one biallelic diploid locus, with REAL the
+ * reference's float type: genotype counts, allele counts in REAL, Unify
+ * (math2.cpp: ((double)A + MIN_FREQ) / (sum + n MIN_FREQ), stored in REAL),
+ * CountK (misc.h: alleles above MIN_FREQ), the statistics in REAL; then the
+ * MarkerDiversity conditions (filter.cpp:494-507) against double windows */
+#define ORC_LOCUS_STATS(REAL, LOG)                                                                       \
+    do {                                                                                                 \
+        REAL fre[2] = {0, 0}, ho = 0, how = 0;                                                           \
+        int n = 0, nhaplo = 0;                                                                           \
+        for (int g = 0; g < 3; ++g) {                                                                    \
+            const unsigned c = gcount[g];                                                                \
+            if (!c) continue;                                                                            \
+            nhaplo += 2 * c;                                                                             \
+            ho += (g == 1 ? 1.0 : 0.0) * c * 2 * 1; /* HIndex * c * v * (v - 1) */                       \
+            how += c * 2 * 1;                                                                            \
+            n += c;                                                                                      \
+            fre[0] += (REAL)(c * (2 - g));                                                               \
+            fre[1] += (REAL)(c * g);                                                                     \
+        }                                                                                                \
+        ptype = n / (REAL)n_ind;                                                                         \
+        nn = n;                                                                                          \
+        if (n) {                                                                                         \
+            const double invsum = 1.0 / ((double)fre[0] + (double)fre[1] + 2 * MINF);                    \
+            fre[0] = (REAL)(((double)fre[0] + MINF) * invsum);                                           \
+            fre[1] = (REAL)(((double)fre[1] + MINF) * invsum);                                           \
+            k = (fre[0] > MINF) + (fre[1] > MINF);                                                       \
+        }                                                                                                \
+        if (k >= 2) {                                                                                    \
+            REAL Iv = 0, b = 1, a2 = 0, picv = 0;                                                        \
+            hoo = ho / how;                                                                              \
+            const int nh = (int)(nhaplo + 0.5);                                                          \
+            for (int a = 0; a < 2; ++a) {                                                                \
+                const REAL af = fre[a];                                                                  \
+                if (af * nh < 1e-5) continue;                                                            \
+                if (af > 1e-5) Iv += -af * LOG(af);                                                      \
+                if (b > af) b = af;                                                                      \
+                a2 += af * af;                                                                           \
+                for (int c = a + 1; c < 2; ++c)                                                          \
+                    if (fre[c] > 0) picv += 2 * af * fre[c] * (1 - af * fre[c]);                         \
+            }                                                                                            \
+            if (b > 0.5) b = 1 - b;                                                                      \
+            bmaf = b; he = 1 - a2; ae = 1 / a2; I = Iv; pic = picv;                                      \
+        }                                                                                                \
+    } while (0)
+
+void orc_locus_filter_pack2(const uint32_t* packed, int64_t L, int n_ind, const orc_locus_filter* f, uint8_t* keep,
+                            double* stats) {
+    const int Nw = (n_ind + 15) / 16;
+    const double MINF = 1e-10, NANV = 0.0 / 0.0;
+    for (int64_t l = 0; l < L; ++l) {
+        unsigned gcount[4] = {0, 0, 0, 0};
+        for (int i = 0; i < n_ind; ++i) gcount[(packed[l * Nw + (i >> 4)] >> (2 * (i & 15))) & 3]++;
+        int k = 0, nn = 0;
+        double ptype, bmaf = NANV, he = NANV, hoo = NANV, pic = NANV, ae = NANV, I = NANV;
+        if (f->single) ORC_LOCUS_STATS(float, logf);
+        else ORC_LOCUS_STATS(double, log);
+#define OUT(v, lo, hi) ((v) < (lo) || (v) > (hi))
+        const int fail = k == 0 || (f->bmaf_b && k == 2 && OUT(bmaf, f->bmaf_min, f->bmaf_max)) ||
+                         (f->k_b && (k < f->k_min || k > f->k_max)) || (f->n_b && (nn < f->n_min || nn > f->n_max)) ||
+                         (f->ptype_b && OUT(ptype, f->ptype_min, f->ptype_max)) ||
+                         (f->he_b && OUT(he, f->he_min, f->he_max)) || (f->ho_b && OUT(hoo, f->ho_min, f->ho_max)) ||
+                         (f->pic_b && OUT(pic, f->pic_min, f->pic_max)) || (f->ae_b && OUT(ae, f->ae_min, f->ae_max)) ||
+                         (f->I_b && OUT(I, f->I_min, f->I_max));
+#undef OUT
+        keep[l] = fail ? 0 : 1;
+        if (stats) {
+            double* o = stats + l * 9;
+            o[0] = nn; o[1] = k; o[2] = ptype; o[3] = bmaf; o[4] = he; o[5] = hoo; o[6] = pic; o[7] = ae; o[8] = I;
+        }
+    }
+}

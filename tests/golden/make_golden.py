@@ -68,6 +68,12 @@ CASES = {
                                          "-structure_singlef=yes", "-structure_nadmburnin=10",
                                          "-structure_krange=[2,2]", "-structure_nburnin=20",
                                          "-structure_nreps=40"]),
+    # the locus filter (-f_filter with diversity windows) and the per-locus
+    # diversity table, which lists the loci that survive; checked by the
+    # filter tests rather than by a whole-file comparison with the oracle
+    "c1_filter": ("c1", 3, ["-f", "-f_bmaf=[0.15,0.5]", "-f_ptype=[0.96,1]", "-f_ho=[0.1,0.6]",
+                            "-structure_krange=[2,2]", "-structure_nburnin=10", "-structure_nreps=20",
+                            "-structure_nadmburnin=0", "-structure_admix=no", "-structure_diversity=yes"]),
 }
 
 
@@ -96,7 +102,9 @@ def main():
         ind = data[dname][1]
         args = [REF, f"-g_input={vcf}", "-g_format=vcf", f"-g_output={work}/out", f"-g_seed={seed}",
                 f"-g_indtext={ind}"] + COMMON + flags
-        subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        # the reference waits for Enter after an error: give it no terminal, and a time limit
+        subprocess.run(args, check=True, stdin=subprocess.DEVNULL, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+                       timeout=600)
         files = sorted(f for f in os.listdir(work) if f.startswith("out.structure"))
         for f in files:
             shutil.copy(os.path.join(work, f), os.path.join(out, f))

@@ -71,6 +71,8 @@ def lib():
         L.orc_divergence.argtypes = [P, P, C.c_int64, C.c_int64, C.c_int, P, P, P]
         L.orc_divergence.restype = None
         L.orc_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int, P, C.c_int64]
+        L.orc_locus_filter_pack2.argtypes = [P, C.c_int64, C.c_int, P, P, P]
+        L.orc_locus_filter_pack2.restype = None
         L.orc_vcf_pack2.restype = C.c_int64
         L.orc_hash_ulong_c.restype = C.c_uint32
         L.orc_hash_ulong_c.argtypes = [C.c_uint64]
@@ -202,3 +204,21 @@ def vcf_pack2(text: bytes, n_ind: int, max_loci: int):
     if n < 0:
         raise ValueError(f"data line {-n} is not biallelic diploid 0/1 data")
     return packed[:n]
+
+
+class LocusFilter(C.Structure):
+    """The layout of orc_locus_filter (and of vp_locus_filter)."""
+    _fields_ = [(n, C.c_int32) for n in ("bmaf_b", "k_b", "n_b", "ptype_b", "he_b", "ho_b", "pic_b", "ae_b", "I_b",
+                                         "k_min", "k_max", "n_min", "n_max", "single")] + \
+               [(n, C.c_double) for n in ("bmaf_min", "bmaf_max", "ptype_min", "ptype_max", "he_min", "he_max",
+                                          "ho_min", "ho_max", "pic_min", "pic_max", "ae_min", "ae_max", "I_min",
+                                          "I_max")]
+
+
+def locus_filter_pack2(packed, n_ind, f):
+    packed = np.ascontiguousarray(packed, np.uint32)
+    L = packed.shape[0]
+    keep = np.zeros(L, np.uint8)
+    stats = np.zeros((L, 9))
+    lib().orc_locus_filter_pack2(packed.ctypes.data, L, n_ind, C.byref(f), keep.ctypes.data, stats.ctypes.data)
+    return keep, stats

@@ -29,7 +29,8 @@ def _run(case, tmp, rng):
     with gzip.open(os.path.join(GOLD, c["data"]), "rb") as fi, open(vcf, "wb") as fo:
         shutil.copyfileobj(fi, fo)
     args = [CLI, f"-g_input={vcf}", f"-g_output={tmp}/out", f"-g_seed={c['seed']}", "-g_decimal=15",
-            f"-g_indtext={c['indtext']}", "-structure", "-structure_writelnl=yes", f"-gb300_rng={rng}"] + c["flags"]
+            f"-g_indtext={c['indtext']}", "-g_float=single", "-structure", "-structure_writelnl=yes",
+            f"-gb300_rng={rng}"] + c["flags"]
     subprocess.run(args, check=True)
     return c
 
@@ -59,3 +60,17 @@ def test_cli_reference_streams_follow_golden_trace(case, tmp_path):
     assert len(got) == len(want)
     for g, w in list(zip(got, want))[:3]:
         assert abs(g - w) <= 1e-5 * abs(w), (g, w)
+
+
+def test_cli_locus_filter_keeps_the_reference_loci(tmp_path):
+    """-f with -f_* windows: the diversity table lists the loci the reference
+    program kept, by name, in its order."""
+    c = _run("c1_filter", str(tmp_path), "counter")
+    f = [x for x in c["files"] if x.endswith("_id=1.txt")][0]
+
+    def loci(path):
+        lines = open(path, "rb").read().decode().replace("\r", "").split("\n")
+        i = next(j for j, ln in enumerate(lines) if ln.startswith("Estimated genetic diversity in each cluster"))
+        return [ln.split("\t")[0] for ln in lines[i + 2:] if ln.split("\t")[0] not in ("", "Average")]
+
+    assert loci(tmp_path / f) == loci(os.path.join(GOLD, "c1_filter", f))

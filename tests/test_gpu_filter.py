@@ -1,0 +1,54 @@
+"""The -f_* locus filter on the device (vp_locus_filter_pack2) against the
+oracle's restatement of CalcDiversity / MarkerDiversity, which is pinned to
+the loci the reference program kept (test_oracle_locus_filter_matches_reference)."""
+import numpy as np
+import pytest
+
+from vcfpop_gb300 import structure as S
+from vcfpop_gb300 import synth
+
+from . import orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _orc_filter(f):
+    o = orc.LocusFilter()
+    for name, _ in orc.LocusFilter._fields_:
+        setattr(o, name, getattr(f, name))
+    return o
+
+
+def _compare(packed, N, f):
+    keep, stats = S.locus_filter(packed, N, f)
+    okeep, ostats = orc.locus_filter_pack2(packed, N, _orc_filter(f))
+    assert np.array_equal(keep, okeep)
+    # every statistic bit for bit but Shannon's I, whose log may differ in the last place
+    both = ~np.isnan(ostats)
+    assert np.array_equal(np.isnan(stats), np.isnan(ostats))
+    assert np.array_equal(stats[:, :8][both[:, :8]], ostats[:, :8][both[:, :8]])
+    assert np.allclose(stats[:, 8][both[:, 8]], ostats[:, 8][both[:, 8]], rtol=1e-6)
+    return keep
+
+
+def test_golden_filter_case_on_device():
+    d = synth.fmodel(1, 200, 2000, 3, 0.1, 0.05)
+    f = S.locus_filter_spec(bmaf=(0.15, 0.5), ptype=(0.96, 1.0), ho=(0.1, 0.6))
+    keep = _compare(S.pack2(d["G"]), 200, f)
+    assert 0 < keep.sum() < 2000
+
+
+@pytest.mark.parametrize("single", [True, False])
+def test_every_window_with_edge_loci(single):
+    d = synth.fmodel(91, 333, 3000, 4, 0.05, 0.05)
+    G = d["G"].copy()
+    G[:20] = -1                     # no call typed
+    G[20:40] = 0                    # monomorphic
+    G[40:60, :, :] = np.where(G[40:60] >= 0, 1, -1)   # monomorphic in the other allele
+    G[60:80, 5:] = -1               # almost nothing typed
+    packed = S.pack2(G)
+    windows = [dict(), dict(k=(2, 2)), dict(n=(300, 333)), dict(he=(0.1, 0.45)), dict(pic=(0.05, 0.3)),
+               dict(ae=(1.2, 1.9)), dict(I=(0.2, 0.6)), dict(bmaf=(0.05, 0.5), ptype=(0.9, 1.0), ho=(0.0, 0.5))]
+    for w in windows:
+        keep = _compare(packed, 333, S.locus_filter_spec(single=single, **w))
+        assert not keep[:20].any()

@@ -22,7 +22,12 @@ def _summary_table(path):
     return [ln for ln in lines[i:] if ln.strip()]
 
 
-@pytest.mark.parametrize("case", sorted(CASES))
+# cases whose flags the oracle's driver does not take (the locus filter) are
+# checked by their own tests
+WHOLE = sorted(c for c in CASES if "-f" not in CASES[c]["flags"])
+
+
+@pytest.mark.parametrize("case", WHOLE)
 def test_oracle_matches_reference(case, oracle_build, tmp_path):
     c = CASES[case]
     vcf = tmp_path / "data.vcf"
@@ -83,3 +88,40 @@ def test_oracle_vcf_parse_matches_golden_data(name, args, kw, oracle_build):
     i = t.index(b"\n#CHROM")
     data = t[t.index(b"\n", i + 1) + 1:]
     assert np.array_equal(orc.vcf_pack2(data, d["G"].shape[1], d["G"].shape[0]), S.pack2(d["G"]))
+
+
+def _diversity_loci(path):
+    """Locus names of the per-locus diversity table of a run file."""
+    lines = open(path, "rb").read().decode().replace("\r", "").split("\n")
+    i = next(j for j, ln in enumerate(lines) if ln.startswith("Estimated genetic diversity in each cluster"))
+    names = []
+    for ln in lines[i + 2:]:
+        if not ln.strip():
+            break
+        head = ln.split("\t")[0]
+        if head and head != "Average":
+            names.append(head)
+    return names
+
+
+def test_oracle_locus_filter_matches_reference(oracle_build):
+    """The oracle's locus filter (statistics of CalcDiversity, conditions of
+    MarkerDiversity) keeps exactly the loci the reference program kept under
+    -f -f_bmaf=[0.15,0.5] -f_ptype=[0.96,1] -f_ho=[0.1,0.6]: the loci listed
+    in its diversity table (those passing, less the monomorphic ones that
+    STRUCTURE drops). The statistics are in float, as the reference computes
+    them under -g_float=single: 5 loci with ptype = 192/200 fall just below
+    0.96 in float and are dropped, as the reference dropped them."""
+    import numpy as np
+    from vcfpop_gb300 import structure as S
+    from vcfpop_gb300 import synth
+    from . import orc
+    d = synth.fmodel(1, 200, 2000, 3, 0.1, 0.05)          # the c1 data make_golden.py wrote
+    packed = S.pack2(d["G"])
+    f = orc.LocusFilter(bmaf_b=1, bmaf_min=0.15, bmaf_max=0.5, ptype_b=1, ptype_min=0.96, ptype_max=1.0,
+                        ho_b=1, ho_min=0.1, ho_max=0.6, single=1)      # the golden runs use -g_float=single
+    keep, stats = orc.locus_filter_pack2(packed, 200, f)
+    kept = {f"1_snp{l + 1}" for l in range(len(keep)) if keep[l] and stats[l, 1] >= 2}
+    want = set(_diversity_loci(os.path.join(GOLD, "c1_filter", "out.structure.k=2_rep=1_id=1.txt")))
+    assert 0 < len(want) < 2000
+    assert kept == want

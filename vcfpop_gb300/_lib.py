@@ -62,6 +62,14 @@ class VpRequestInfo(C.Structure):
 VP_REQ_QUEUED, VP_REQ_RUNNING, VP_REQ_DONE, VP_REQ_FAILED = 0, 1, 2, 3
 
 
+class VpLocusFilter(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("bmaf_b", "k_b", "n_b", "ptype_b", "he_b", "ho_b", "pic_b", "ae_b", "I_b",
+                                         "k_min", "k_max", "n_min", "n_max", "single")] + \
+               [(n, C.c_double) for n in ("bmaf_min", "bmaf_max", "ptype_min", "ptype_max", "he_min", "he_max",
+                                          "ho_min", "ho_max", "pic_min", "pic_max", "ae_min", "ae_max", "I_min",
+                                          "I_max")]
+
+
 class VpError(RuntimeError):
     pass
 
@@ -74,7 +82,7 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_divergence", "vp_chain_step", "vp_chain_get",
            "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
-           "vp_release", "vp_server_close", "vp_vcf_pack2"]
+           "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2"]
 
 
 def lib():
@@ -130,6 +138,7 @@ def lib():
     L.vp_release.argtypes = [P, C.c_int64]
     L.vp_server_close.argtypes = [P]
     L.vp_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int32, C.c_int, P, C.c_int64, P, P]
+    L.vp_locus_filter_pack2.argtypes = [P, C.c_int64, C.c_int32, C.POINTER(VpLocusFilter), C.c_int, P, P]
     _lib = L
     return L
 

@@ -33,6 +33,8 @@ struct Opts {
     int decimal = 5;
     std::string delim = "\t", lb = "\r\n";
     int kmin = 1, kmax = 5, nruns = 1, diversity = 0, device = 0;
+    bool filter = false;          // -f, with -f_* windows: the locus filter
+    vp_locus_filter lf{};
     vp_params p;
     std::vector<std::string> argv;
 };
@@ -92,6 +94,18 @@ bool parse(int argc, char** argv, Opts& o) {
         else if (k == "-structure_pstdf") o.p.pstdf = atof(v.c_str());
         else if (k == "-structure_stdf") o.p.stdf = atof(v.c_str());
         else if (k == "-structure_singlef") o.p.fsame = yesno(v);
+        else if (k == "-f") o.filter = true;
+        else if (k == "-g_float") o.lf.single = v == "single";
+        else if (k == "-f_bmaf") o.lf.bmaf_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.bmaf_min, &o.lf.bmaf_max) == 2;
+        else if (k == "-f_k") o.lf.k_b = sscanf(v.c_str(), "[%d,%d]", &o.lf.k_min, &o.lf.k_max) == 2;
+        else if (k == "-f_n") o.lf.n_b = sscanf(v.c_str(), "[%d,%d]", &o.lf.n_min, &o.lf.n_max) == 2;
+        else if (k == "-f_ptype") o.lf.ptype_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.ptype_min, &o.lf.ptype_max) == 2;
+        else if (k == "-f_he") o.lf.he_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.he_min, &o.lf.he_max) == 2;
+        else if (k == "-f_ho") o.lf.ho_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.ho_min, &o.lf.ho_max) == 2;
+        else if (k == "-f_pic") o.lf.pic_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.pic_min, &o.lf.pic_max) == 2;
+        else if (k == "-f_ae") o.lf.ae_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.ae_min, &o.lf.ae_max) == 2;
+        else if (k == "-f_I") o.lf.I_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.I_min, &o.lf.I_max) == 2;
+        else if (k == "-f_pval") { fprintf(stderr, "vcfpop-gb300: the HWE filter -f_pval is not implemented\n"); return false; }
         // other -g_* and -structure_* flags (threads, SIMD, plots, streams) do
         // not apply to the GPU path and are accepted silently
     }
@@ -140,7 +154,8 @@ bool read_vcf(const std::string& path, Vcf& v) {
         int nalt = 1;
         for (char ch : cols[4]) nalt += ch == ',';
         v.k.push_back(1 + nalt);
-        v.locs.push_back(cols[0] + "_" + cols[1]);
+        // the reference's default locus name: CHROM_ID (CHROM_POS without an ID)
+        v.locs.push_back(cols[0] + "_" + (cols[2] != "." ? cols[2] : cols[1]));
         if (nl == 0) {
             for (int i = 0; i < N; ++i) {
                 const std::string& g = cols[9 + i];
@@ -238,11 +253,15 @@ bool read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
     v.k.assign(L, 2);
     v.locs.resize(L);
     for (int64_t l = 0; l < L; ++l) {
+        // CHROM_ID, or CHROM_POS without an ID (the reference's default locus name)
         const char* a = data + starts[l];
-        const char* t1 = (const char*)memchr(a, '\t', data + starts[l + 1] - a);
-        const char* t2 = t1 ? (const char*)memchr(t1 + 1, '\t', data + starts[l + 1] - t1 - 1) : nullptr;
-        if (!t1 || !t2) return false;
-        v.locs[l] = std::string(a, t1 - a) + "_" + std::string(t1 + 1, t2 - t1 - 1);
+        const char* e = data + starts[l + 1];
+        const char* t1 = (const char*)memchr(a, '\t', e - a);
+        const char* t2 = t1 ? (const char*)memchr(t1 + 1, '\t', e - t1 - 1) : nullptr;
+        const char* t3 = t2 ? (const char*)memchr(t2 + 1, '\t', e - t2 - 1) : nullptr;
+        if (!t1 || !t2 || !t3) return false;
+        std::string id(t2 + 1, t3 - t2 - 1);
+        v.locs[l] = std::string(a, t1 - a) + "_" + (id != "." ? id : std::string(t1 + 1, t2 - t1 - 1));
     }
     return true;
 }
@@ -479,6 +498,37 @@ int main(int argc, char** argv) {
         in.packed2 = packed.data();
     } else {
         in.alleles = G.data();
+    }
+    // the locus filter (-f with -f_* windows: src/filter.cpp MarkerDiversity)
+    // on the packed matrix, on the device; loci that fail are dropped here
+    const vp_locus_filter& lf = o.lf;
+    const bool windows = lf.bmaf_b || lf.k_b || lf.n_b || lf.ptype_b || lf.he_b || lf.ho_b || lf.pic_b || lf.ae_b || lf.I_b;
+    std::vector<uint32_t> kept_packed;
+    if (o.filter && windows) {
+        if (!in.packed2) { fprintf(stderr, "vcfpop-gb300: the locus filter needs biallelic diploid data\n"); return 1; }
+        const int Nw = (N + 15) / 16;
+        std::vector<uint8_t> keep(L0);
+        if (vp_locus_filter_pack2(in.packed2, L0, N, &lf, o.device, keep.data(), nullptr)) {
+            fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error());
+            return 1;
+        }
+        int64_t nk = 0;
+        for (int64_t l = 0; l < L0; ++l) nk += keep[l];
+        kept_packed.resize((size_t)nk * Nw);
+        std::vector<int32_t> k2;
+        std::vector<std::string> locs2;
+        for (int64_t l = 0, j = 0; l < L0; ++l)
+            if (keep[l]) {
+                memcpy(&kept_packed[(size_t)j++ * Nw], in.packed2 + (size_t)l * Nw, (size_t)Nw * 4);
+                k2.push_back(v.k[l]);
+                locs2.push_back(v.locs[l]);
+            }
+        v.k.swap(k2);
+        v.locs.swap(locs2);
+        in.packed2 = kept_packed.data();
+        in.n_loc = nk;
+        in.n_alleles = v.k.data();
+        fprintf(stderr, "vcfpop-gb300: locus filter kept %lld of %lld loci\n", (long long)nk, (long long)L0);
     }
     vp_dataset* ds = nullptr;
     if (vp_dataset_prepare(&in, &ds)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }

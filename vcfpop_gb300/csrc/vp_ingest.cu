@@ -354,3 +354,134 @@ extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int d
     cudaStreamDestroy(st);
     return rc;
 }
+
+// ---------------------------------------------------------------------------
+// Locus filter on the packed matrix. One warp per locus: the lanes count the
+// four 2-bit codes of their words (popcounts of the low and high bit planes),
+// lane 0 derives the reference's statistics for a biallelic diploid locus
+// (counts c0 = 0/0, c1 = 0/1, c2 = 1/1):
+//   n = c0 + c1 + c2, nhaplo = 2n, allele counts 2c0 + c1 and c1 + 2c2,
+//   frequencies as Unify gives them ((count + 1e-10) / (2n + 2e-10)),
+//   k = alleles above 1e-10, ptype = n / N, and for k = 2: bmaf, he = 1 - a2,
+//   ho = c1 / n (HIndex 1 for a heterozygote), pic, ae = 1 / a2, I.
+namespace {
+__device__ __forceinline__ float rlog(float x) { return logf(x); }
+__device__ __forceinline__ double rlog(double x) { return log(x); }
+
+// CalcDiversity's statistics for one biallelic diploid locus in the
+// reference's REAL (float under -g_float=single): allele counts in REAL,
+// Unify in double stored in REAL, CountK above 1e-10, then the statistics
+template <typename REAL>
+__device__ void locus_stats(int c0, int c1, int c2, int N, int& k, double& ptype, double& bmaf, double& he, double& ho,
+                            double& pic, double& ae, double& I) {
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    const int n = c0 + c1 + c2;
+    ptype = (double)((REAL)n / (REAL)N);
+    k = 0;
+    bmaf = he = ho = pic = ae = I = nan;
+    if (n == 0) return;
+    REAL fre[2] = {(REAL)(2 * c0 + c1), (REAL)(c1 + 2 * c2)};
+    const double invsum = 1.0 / ((double)fre[0] + (double)fre[1] + 2 * 1e-10);
+    fre[0] = (REAL)(((double)fre[0] + 1e-10) * invsum);
+    fre[1] = (REAL)(((double)fre[1] + 1e-10) * invsum);
+    k = (fre[0] > 1e-10) + (fre[1] > 1e-10);
+    if (k < 2) return;
+    const REAL hoR = (REAL)(2.0 * c1) / (REAL)(2.0 * n);
+    const int nh = 2 * n;
+    REAL Iv = 0, b = 1, a2 = 0, picv = 0;
+    for (int a = 0; a < 2; ++a) {
+        const REAL af = fre[a];
+        if (af * nh < 1e-5) continue;
+        if (af > 1e-5) Iv += -af * rlog(af);
+        if (b > af) b = af;
+        a2 += af * af;
+        if (a == 0 && fre[1] > 0) picv += 2 * af * fre[1] * (1 - af * fre[1]);
+    }
+    if (b > 0.5) b = 1 - b;
+    bmaf = b;
+    he = (REAL)(1 - a2);
+    ho = hoR;
+    pic = picv;
+    ae = (REAL)(1 / a2);
+    I = Iv;
+}
+
+__device__ __forceinline__ bool outside(double v, double lo, double hi) { return v < lo || v > hi; }
+
+__global__ void k_locus_filter(const uint32_t* packed, int64_t L, int N, int Nw, vp_locus_filter f, uint8_t* keep,
+                               double* stats) {
+    const int64_t l = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (l >= L) return;
+    const uint32_t* row = packed + l * Nw;
+    int c1 = 0, c2 = 0, c3 = 0;
+    for (int w = lane; w < Nw; w += 32) {
+        const uint32_t v = row[w];
+        const uint32_t lo = v & 0x55555555u, hi = (v >> 1) & 0x55555555u;
+        c1 += __popc(lo & ~hi);
+        c2 += __popc(hi & ~lo);
+        c3 += __popc(lo & hi);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+        c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+        c3 += __shfl_xor_sync(0xffffffffu, c3, o);
+    }
+    if (lane) return;
+    const int c0 = Nw * 16 - c1 - c2 - c3;  // padding calls are coded missing (3)
+    const int n = c0 + c1 + c2;
+    double ptype, bmaf, he, ho, pic, ae, I;
+    int k;
+    if (f.single) locus_stats<float>(c0, c1, c2, N, k, ptype, bmaf, he, ho, pic, ae, I);
+    else locus_stats<double>(c0, c1, c2, N, k, ptype, bmaf, he, ho, pic, ae, I);
+    const bool fail = k == 0 || (f.bmaf_b && k == 2 && outside(bmaf, f.bmaf_min, f.bmaf_max)) ||
+                      (f.k_b && (k < f.k_min || k > f.k_max)) || (f.n_b && (n < f.n_min || n > f.n_max)) ||
+                      (f.ptype_b && outside(ptype, f.ptype_min, f.ptype_max)) ||
+                      (f.he_b && outside(he, f.he_min, f.he_max)) || (f.ho_b && outside(ho, f.ho_min, f.ho_max)) ||
+                      (f.pic_b && outside(pic, f.pic_min, f.pic_max)) || (f.ae_b && outside(ae, f.ae_min, f.ae_max)) ||
+                      (f.I_b && outside(I, f.I_min, f.I_max));
+    keep[l] = fail ? 0 : 1;
+    if (stats) {
+        double* o = stats + l * VP_LOCUS_STATS;
+        o[0] = n; o[1] = k; o[2] = ptype; o[3] = bmaf; o[4] = he; o[5] = ho; o[6] = pic; o[7] = ae; o[8] = I;
+    }
+}
+}  // namespace
+
+extern "C" int vp_locus_filter_pack2(const uint32_t* packed, int64_t n_loc, int32_t n_ind, const vp_locus_filter* f,
+                                     int device, uint8_t* keep, double* stats) {
+    if (!packed || !f || !keep || n_loc < 0 || n_ind <= 0) { vp_set_error("bad arguments"); return VP_E_ARG; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
+    if (device < 0 || device >= ndev) { vp_set_error("device %d out of range", device); return VP_E_ARG; }
+    if (n_loc == 0) return VP_OK;
+    CKI(cudaSetDevice(device));
+    const int Nw = (n_ind + 15) / 16;
+    cudaStream_t st;
+    CKI(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t pb = (size_t)n_loc * Nw * 4, sb = stats ? (size_t)n_loc * VP_LOCUS_STATS * 8 : 0;
+    char* buf = nullptr;
+    int rc = VP_OK;
+    cudaError_t e = cudaMallocAsync((void**)&buf, pb + 256 + (size_t)n_loc + 256 + sb, st);
+    if (e != cudaSuccess) { vp_set_error("device allocation failed: %s", cudaGetErrorString(e)); rc = VP_E_MEM; }
+    if (!rc) {
+        uint32_t* dp = (uint32_t*)buf;
+        uint8_t* dk = (uint8_t*)(buf + (pb + 255) / 256 * 256);
+        double* ds = stats ? (double*)(buf + (pb + 255) / 256 * 256 + ((size_t)n_loc + 255) / 256 * 256) : nullptr;
+        rc = upload_staged((char*)dp, (const char*)packed, (int64_t)pb, st);
+        if (!rc) {
+            k_locus_filter<<<(unsigned)((n_loc * 32 + 255) / 256), 256, 0, st>>>(dp, n_loc, n_ind, Nw, *f, dk, ds);
+            if ((e = cudaGetLastError()) != cudaSuccess ||
+                (e = cudaMemcpyAsync(keep, dk, (size_t)n_loc, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                (ds && (e = cudaMemcpyAsync(stats, ds, sb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) ||
+                (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+                vp_set_error("locus filter failed: %s", cudaGetErrorString(e));
+                rc = VP_E_CUDA;
+            }
+        }
+        cudaFreeAsync(buf, st);
+    }
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    return rc;
+}

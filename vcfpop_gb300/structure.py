@@ -223,6 +223,35 @@ def vcf_pack2(text: bytes, n_ind: int, device: int = 0):
     return packed[:n.value], starts[:n.value + 1]
 
 
+LOCUS_STATS = ("n", "k", "ptype", "bmaf", "he", "ho", "pic", "ae", "I")
+
+
+def locus_filter_spec(single: bool = True, **windows) -> B.VpLocusFilter:
+    """A locus filter from -f_* windows given as name=(min, max), names as in
+    LOCUS_STATS (bmaf, k, n, ptype, he, ho, pic, ae, I)."""
+    f = B.VpLocusFilter()
+    f.single = 1 if single else 0
+    for name, (lo, hi) in windows.items():
+        if name not in LOCUS_STATS:
+            raise ValueError(f"unknown locus statistic {name}")
+        setattr(f, f"{name}_b", 1)
+        setattr(f, f"{name}_min", lo)
+        setattr(f, f"{name}_max", hi)
+    return f
+
+
+def locus_filter(packed: np.ndarray, n_ind: int, f: B.VpLocusFilter, device: int = 0):
+    """Per-locus statistics and the pass flags of the -f_* locus filter on the
+    device: (keep [L] uint8, stats [L][9])."""
+    packed = np.ascontiguousarray(packed, np.uint32)
+    L = packed.shape[0]
+    keep = np.zeros(L, np.uint8)
+    stats = np.zeros((L, len(LOCUS_STATS)))
+    B.check(B.lib().vp_locus_filter_pack2(packed.ctypes.data, L, n_ind, C.byref(f), device, keep.ctypes.data,
+                                          stats.ctypes.data))
+    return keep, stats
+
+
 def chain_result(h, final: bool = False) -> dict:
     r = B.VpResult()
     B.check(B.lib().vp_chain_sizes(h, C.byref(r)))
