@@ -342,10 +342,10 @@ def bench_single(args):
     import ctypes as C
     from vcfpop_gb300 import _lib as B
     from vcfpop_gb300 import structure as S
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from vcfpop_gb300 import replicas as R
+    rank, world, local = R.env()
     torch.cuda.set_device(local)
+    R.init("nccl")
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -373,14 +373,17 @@ def bench_single(args):
     stream = torch.cuda.ExternalStream(lib.vp_stream(ctx.h))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = ctx.launches()
+    n = int(R.max_over_ranks(n) if world > 1 else n)   # every replica times the same number of sweeps
+    R.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
         e0.record(stream)
         B.check(lib.vp_run(arr, 1, n))
         e1.record(stream)
         torch.cuda.synchronize()
+        R.barrier()
     launches = ctx.launches() - l0
-    ms = e0.elapsed_time(e1) / n
+    ms = R.max_over_ranks(e0.elapsed_time(e1)) / n
     # dominant kernel: average launch duration over a few more sweeps
     lib.vp_prof_enable(ctx.h, 1)
     dom, cnt = 0.0, 0
@@ -423,10 +426,10 @@ def bench_single(args):
             cx.close()
             times.append(time.perf_counter() - t0)
             assert np.isfinite(res["rout"]).all()
-        tt = min(times[1:]) if len(times) > 1 else times[0]
+        tt = R.max_over_ranks(min(times[1:]) if len(times) > 1 else times[0])
         h2d = (ds.L * ((ds.N + 15) // 16) * 4 if ds.packed2 else ds.L * ds.N * ds.maxploidy) + ds.L * 12 + ds.N * 12
         d2h = 8 * (ds.N * K * 2 + ds.KT * K) + 64
-        e2e = {"value": upd * e_sweeps / tt, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+        e2e = {"value": upd * e_sweeps * world / tt, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "step": ("one complete run" if full else f"a run of {e_sweeps} sweeps (500 + 500)") +
                        ": open context from pinned host buffers, create the chain, every sweep, Arrange, read Q, "
                        "ancestry, mean frequencies and lnL, close", "time_to_result_s": tt}
@@ -435,17 +438,18 @@ def bench_single(args):
         v, ns, dt = cpu_sample_single(d, K, run)
         cpu = {"value": v, "unit": "updates/s", "cores": 1, "kind": "port",
                "sample": f"the same dataset, one chain on one host core, {ns} sweeps in {dt:.1f} s"}
-    line = {"metric": METRIC, "value": upd / (ms / 1e3), "unit": "updates/s", "n_gpus": world, "steps": n,
+    line = {"metric": METRIC, "value": upd * world / (ms / 1e3), "unit": "updates/s", "n_gpus": world, "steps": n,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (lnP(D) accumulations in f64)",
             "data": "synthetic F-model, seeded (vcfpop_gb300/workloads.py)",
             "config": {"workload": f"{args.workload}: {SINGLE_DESC[args.workload]}; one step = one sweep",
                        "form": "plain", "chains": 1, "updates_per_step": upd,
                        "l2": "working set smaller than L2" if l2 else "inputs larger than L2",
-                       "parallelism": "1 GPU"},
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    R.finish()
 
 
 def reference_single(args):
@@ -555,13 +559,10 @@ def main():
         return bench_serve(args)
     import torch
     import ctypes as C
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from vcfpop_gb300 import replicas as R
+    rank, world, local = R.env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", init_method="env://")
+    R.init("nccl")
     from vcfpop_gb300 import _lib as B
     from vcfpop_gb300 import structure as S
 
@@ -593,8 +594,7 @@ def main():
     ctx.sync()
     stream = torch.cuda.ExternalStream(lib.vp_stream(ctx.h))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        torch.distributed.barrier()
+    R.barrier()
     torch.cuda.synchronize()
     l0 = ctx.launches()
     dom_ms, dom_n = 0.0, 0
@@ -608,12 +608,9 @@ def main():
             dom_n += nl.value
         e1.record(stream)
         torch.cuda.synchronize()
+        R.barrier()
     launches = ctx.launches() - l0
-    total_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = R.max_over_ranks(e0.elapsed_time(e1))   # the slowest replica sets the job time
     tc_err = lib.vp_tc_status(ctx.h)
     ms_step = total_ms / args.steps
     value = upd_step * world / (ms_step / 1e3)
@@ -699,8 +696,7 @@ def main():
             "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "outputs": outputs, "ingest": ingest, "locus_filter": lfilter}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    R.finish()
 
 
 if __name__ == "__main__":
