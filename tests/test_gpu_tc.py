@@ -101,3 +101,17 @@ def test_batched_tc_sweep_matches_plain():
             assert np.array_equal(p.get("NI"), t.get("NI"))
             lp, lt = p.get("LNL")[0], t.get("LNL")[0]
             assert abs(lp - lt) <= 1e-6 * abs(lp)
+
+
+def test_deferred_initial_counts_equal_plain():
+    """A tensor-core chain leaves its initial counts to its batch; read before
+    any batch exists they are computed on demand, and equal the plain chain's."""
+    d = synth.fmodel(52, 600, 1200, 3, 0.05, 0.02)
+    ds = S.Dataset.from_synth(d)
+    ctx = S.Context(ds)
+    kw = dict(admix=0, nadmburnin=0, nburnin=5, nreps=5)
+    for K in (2, 4):
+        p = S.Chain(ctx, S.params(K, 700 + K, **kw))
+        t = S.Chain(ctx, S.params(K, 700 + K, form=B.VP_FORM_TC, **kw))
+        assert np.array_equal(p.get("Z"), t.get("Z"))
+        assert np.array_equal(p.get("NI"), t.get("NI"))

@@ -60,6 +60,10 @@ struct vp_chain {
     cudaGraphExec_t graph = nullptr;
     int graph_nodes = 0;
     int32_t* own_ni = nullptr;   // the chain's own Ni (a tensor-core batch may redirect Ni)
+    // the initial allele counts (the no-admixture UpdateZ of InitFix) are
+    // not computed yet: a tensor-core chain leaves them to its batch, which
+    // counts every chain in one count contraction
+    bool counts_pending = false;
 };
 
 // a set of no-admixture chains sharing one context, swept together with the
@@ -85,6 +89,8 @@ struct TcBatch {
 namespace {
 void free_batch(vp_ctx* x);
 int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps);
+int launch_counts_gemm(vp_ctx* x);
+tc::BatchDev batch_dev(vp_ctx* x);
 
 #define CK(call)                                                                  \
     do {                                                                          \
@@ -304,6 +310,17 @@ int launch_sweep(vp_chain* c) {
 
 }  // namespace
 
+// the deferred initial counts of a tensor-core chain, for any use outside
+// its batch
+int ensure_counts(vp_chain* c) {
+    if (!c->counts_pending) return VP_OK;
+    vp_ctx* x = c->ctx;
+    k_count_noadmix<<<cdiv(x->L, COUNT_WARPS), COUNT_WARPS * 32, count_smem(c), x->stream>>>(c->d, 1);
+    int rc = check_launch(x, "k_count_noadmix");
+    if (!rc) c->counts_pending = false;
+    return rc;
+}
+
 extern "C" int vp_open(const vp_dataset* ds, int device, vp_ctx** out) {
     if (!ds || !out) { vp_set_error("null argument"); return VP_E_ARG; }
     int ndev = 0;
@@ -516,6 +533,12 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
         if (singlez) {
             k_init_z_single<<<P->rng ? cdiv(N, 256) : 1, P->rng ? 256 : 32, 0, s>>>(c->d);
             if ((rc = check_launch(x, "k_init_z_single"))) break;
+            const bool batched = P->form == VP_FORM_TC && x->packed2 && !P->locpriori && !P->fmodel &&
+                                 P->rng == VP_RNG_COUNTER;
+            if (batched) {
+                c->counts_pending = true;
+                break;
+            }
             k_count_noadmix<<<cdiv(L, COUNT_WARPS), COUNT_WARPS * 32, count_smem(c), s>>>(c->d, 1);
             if ((rc = check_launch(x, "k_count_noadmix"))) break;
         } else {
@@ -587,6 +610,8 @@ extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
         for (int i = 0; i < n; ++i) cs[i]->issued += step;
         return VP_OK;
     }
+    for (int i = 0; i < n; ++i)
+        if (int rc0 = ensure_counts(cs[i])) return rc0;
     // chains with sweeps left; a set of chains whose sweeps are all still
     // pending shares one cached graph of a sweep
     int left = nsweeps;
@@ -747,6 +772,7 @@ static int field_ptr(vp_chain* c, int f, void** p, size_t* bytes) {
 extern "C" int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes) {
     if (!c || !host) { vp_set_error("null argument"); return VP_E_ARG; }
     cudaSetDevice(c->ctx->device);
+    if (int rc0 = ensure_counts(c)) return rc0;
     CK(cudaStreamSynchronize(c->ctx->stream));
     if (field == VP_F_FF) {
         size_t K = c->P.K;
@@ -766,6 +792,8 @@ extern "C" int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes
 extern "C" int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t bytes) {
     if (!c || !host) { vp_set_error("null argument"); return VP_E_ARG; }
     cudaSetDevice(c->ctx->device);
+    if (field == VP_F_NI) c->counts_pending = false;   // the caller's counts replace them
+    else if (int rc0 = ensure_counts(c)) return rc0;
     CK(cudaStreamSynchronize(c->ctx->stream));
     if (field == VP_F_FF) {
         size_t K = c->P.K;
@@ -793,7 +821,9 @@ extern "C" int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t
 extern "C" int vp_chain_step(vp_chain* c, int32_t step) {
     if (!c) { vp_set_error("null chain"); return VP_E_ARG; }
     cudaSetDevice(c->ctx->device);
-    int rc = launch_step(c, step, 0);
+    int rc = ensure_counts(c);
+    if (rc) return rc;
+    rc = launch_step(c, step, 0);
     if (rc) return rc;
     return vp_sync(c->ctx);
 }
@@ -1011,6 +1041,16 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
         return rc;
     }
     x->batch = b;
+    // initial counts the chains left to the batch: one-hot rows of their
+    // initial labels through the count contraction, for every chain at once
+    bool pending = false;
+    for (int i = 0; i < n; ++i) pending |= cs[i]->counts_pending;
+    if (pending) {
+        tc::BatchDev bd = batch_dev(x);
+        LAUNCH(x, tc::k_onehot_from_z, (dim3(cdiv(x->N, 256), n, 1), 256, 0, x->stream), (bd));
+        if ((rc = launch_counts_gemm(x))) return rc;
+        for (int i = 0; i < n; ++i) cs[i]->counts_pending = false;
+    }
     return VP_OK;
 }
 
@@ -1049,6 +1089,20 @@ int launch_tc_sweep(vp_ctx* x) {
     // labels of every chain, one-hot rows for the count contraction
     LAUNCH(x, tc::k_sample_tc, (dim3(cdiv(x->N, SAMPLE_BLOCK), n, 1), SAMPLE_BLOCK, 0, s), (bd));
     // count contraction: Ni[row, a] = sum_i OH[row, i] C[i, a]
+    if (int rc = launch_counts_gemm(x)) return rc;
+    // Record for every chain, then m += 1
+    unsigned ga = std::min<unsigned>(1024, cdiv((int64_t)16 * x->KT, 256));
+    LAUNCH(x, k_record, (dim3(1, 1, n), 256, 0, s), (b->dchains));
+    LAUNCH(x, k_accumulate, (dim3(ga, 1, n), 256, 0, s), (b->dchains, 0));
+    LAUNCH(x, k_advance, (dim3(1, 1, n), 32, 0, s), (b->dchains));
+    return VP_OK;
+}
+
+// the count contraction of the batch: Ni[row, a] = sum_i OH[row, i] C[i, a]
+// into every chain's Ni (e4m3 operands, exact)
+int launch_counts_gemm(vp_ctx* x) {
+    TcBatch* b = x->batch;
+    const TcOperands& t = x->tc;
     {
         tc::GemmArgs g{};
         g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / t.bk8); g.kb_per_split = g.kblocks;
@@ -1057,15 +1111,8 @@ int launch_tc_sweep(vp_ctx* x) {
         const unsigned mtiles = cdiv(t.Apad, 128 * b->mt2);
         g.group_major = mtiles <= 65535;     // grid.y limit; otherwise row tiles on x
         const dim3 grid = g.group_major ? dim3(b->G, mtiles, 1) : dim3(mtiles, b->G, 1);
-        int rc = launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, grid);
-        if (rc) return rc;
+        return launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, grid);
     }
-    // Record for every chain, then m += 1
-    unsigned ga = std::min<unsigned>(1024, cdiv((int64_t)16 * x->KT, 256));
-    LAUNCH(x, k_record, (dim3(1, 1, n), 256, 0, s), (b->dchains));
-    LAUNCH(x, k_accumulate, (dim3(ga, 1, n), 256, 0, s), (b->dchains, 0));
-    LAUNCH(x, k_advance, (dim3(1, 1, n), 32, 0, s), (b->dchains));
-    return VP_OK;
 }
 
 int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps) {

@@ -424,6 +424,17 @@ __global__ void __launch_bounds__(256) k_update_p_tc(BatchDev b) {
     }
 }
 
+// one-hot rows of every chain's current labels (the initial counts of a
+// batch: the count contraction of these rows is the no-admixture UpdateZ)
+__global__ void k_onehot_from_z(BatchDev b) {
+    const int ci = blockIdx.y;
+    const DevChain& c = b.chains[ci];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.D.N) return;
+    const int r0 = b.row0[ci], z = c.Z[i];
+    for (int k = 0; k < c.K; ++k) b.OH[(int64_t)(r0 + k) * b.Npad + i] = k == z ? E4M3_ONE : 0;
+}
+
 // One (chain, individual). The split-K partials sum, in FP32, to the centred
 // log-likelihood; the individual's constant B_i cancels from the label
 // weights exp(LL_k - max), so the draw runs in FP32 on the centred sums (the
