@@ -227,6 +227,12 @@ int vp_loglik_packed2(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const 
 int vp_loglik_packed2_noalloc(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const float* freq, int32_t K,
                               double* ll, void* stream);
 
+/* Contexts, chains and batches take device memory from a stream-ordered
+ * pool per device that keeps freed blocks for the next run (no map/unmap
+ * between runs, frees do not wait for the device). This gives the kept
+ * blocks back to the device (after a device synchronisation). */
+int vp_release_memory(int device);
+
 /* The CUDA stream (cudaStream_t) every launch of this context goes to. */
 void* vp_stream(vp_ctx* ctx);
 /* Record CUDA events around each launch of the sweep's dominant kernel (the

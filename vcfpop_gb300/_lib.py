@@ -82,7 +82,7 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_divergence", "vp_chain_step", "vp_chain_get",
            "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
-           "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2"]
+           "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2", "vp_release_memory"]
 
 
 def lib():
@@ -124,6 +124,7 @@ def lib():
     L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 9 + [P]
     L.vp_debug_gemm_time.argtypes = [C.c_int32] * 13 + [P]
     L.vp_debug_gemm_e4m3.argtypes = [P, P] + [C.c_int32] * 7 + [P]
+    L.vp_release_memory.argtypes = [C.c_int]
     L.vp_stream.argtypes = [P]
     L.vp_stream.restype = P
     L.vp_prof_enable.argtypes = [P, C.c_int]

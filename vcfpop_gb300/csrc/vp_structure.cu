@@ -118,12 +118,41 @@ int check_launch(vp_ctx* ctx, const char* what) {
         if (rc_) return rc_;                    \
     } while (0)
 
+// The library's device memory: one stream-ordered pool per device that keeps
+// freed blocks for the next context, chain or batch, so repeated runs do not
+// pay to map and unmap memory (and a free does not wait for the device);
+// vp_release_memory gives the kept blocks back.
+cudaMemPool_t lib_pool(int device) {
+    static std::mutex mu;
+    static std::vector<cudaMemPool_t> pools;
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)pools.size() <= device) pools.resize(device + 1, nullptr);
+    if (!pools[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        if (cudaMemPoolCreate(&pools[device], &props) != cudaSuccess) return nullptr;
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pools[device], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    return pools[device];
+}
+cudaError_t dev_alloc(void** p, size_t bytes, int device, cudaStream_t s) {
+    cudaMemPool_t pool = lib_pool(device);
+    if (!pool) return cudaErrorMemoryAllocation;
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+void dev_free(void* p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+}
+
 template <typename T>
 int upload(vp_ctx* ctx, const T* host, size_t n, const T** dev) {
     if (n == 0) { *dev = nullptr; return VP_OK; }
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
-    if (e != cudaSuccess) { vp_set_error("cudaMalloc(%zu) failed: %s", n * sizeof(T), cudaGetErrorString(e)); return VP_E_MEM; }
+    cudaError_t e = dev_alloc(&p, n * sizeof(T), ctx->device, ctx->stream);
+    if (e != cudaSuccess) { vp_set_error("device allocation of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e)); return VP_E_MEM; }
     ctx->allocs.push_back(p);
     CK(cudaMemcpyAsync(p, host, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
     *dev = (const T*)p;
@@ -362,11 +391,14 @@ extern "C" int vp_close(vp_ctx* x) {
     if (!x) return VP_OK;
     cudaSetDevice(x->device);
     if (x->stream) cudaStreamSynchronize(x->stream);
-    if (x->batch) { cudaGraphExecDestroy(x->batch->graph); cudaFree(x->batch->mem); delete x->batch; x->batch = nullptr; }
+    if (x->batch) { cudaGraphExecDestroy(x->batch->graph); dev_free(x->batch->mem, x->stream); delete x->batch; x->batch = nullptr; }
     if (x->pg) cudaGraphExecDestroy(x->pg);
     for (cudaEvent_t e : x->prof_ev) cudaEventDestroy(e);
-    for (void* p : x->allocs) cudaFree(p);
-    if (x->stream) cudaStreamDestroy(x->stream);
+    for (void* p : x->allocs) dev_free(p, x->stream);
+    if (x->stream) {
+        cudaStreamSynchronize(x->stream);
+        cudaStreamDestroy(x->stream);
+    }
     delete x;
     return VP_OK;
 }
@@ -511,9 +543,9 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
     const int K = P->K, N = x->N;
     const int64_t L = x->L;
     DevChain& h = c->h;
-    cudaError_t e = cudaMalloc(&c->mem, bytes);
+    cudaError_t e = dev_alloc(&c->mem, bytes, x->device, x->stream);
     if (e != cudaSuccess) {
-        vp_set_error("cudaMalloc of %zu bytes for chain state failed: %s", bytes, cudaGetErrorString(e));
+        vp_set_error("device allocation of %zu bytes for chain state failed: %s", bytes, cudaGetErrorString(e));
         delete c;
         return VP_E_MEM;
     }
@@ -546,7 +578,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
             if ((rc = check_launch(x, "k_init_admix"))) break;
         }
     } while (0);
-    if (rc) { cudaFree(c->mem); delete c; return rc; }
+    if (rc) { dev_free(c->mem, x->stream); delete c; return rc; }
     *out = c;
     return VP_OK;
 }
@@ -566,7 +598,7 @@ extern "C" int vp_chain_destroy(vp_chain* c) {
             break;
         }
     if (c->graph) cudaGraphExecDestroy(c->graph);
-    cudaFree(c->mem);
+    dev_free(c->mem, c->ctx->stream);   // after every launch already queued for the chain
     delete c;
     return VP_OK;
 }
@@ -917,8 +949,8 @@ int tc_operands(vp_ctx* x) {
     t.Npad = (x->N + 127) / 128 * 128;
     size_t bytes = (size_t)t.Npad * t.Apad * 2 + (size_t)t.Npad * t.Apad + 256 + t.Apad * 4 + t.Npad * 8 + 256;
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if (e != cudaSuccess) { vp_set_error("cudaMalloc(%zu) for tensor-core operands: %s", bytes, cudaGetErrorString(e)); return VP_E_MEM; }
+    cudaError_t e = dev_alloc(&p, bytes, x->device, x->stream);
+    if (e != cudaSuccess) { vp_set_error("device allocation of %zu bytes for tensor-core operands: %s", bytes, cudaGetErrorString(e)); return VP_E_MEM; }
     x->allocs.push_back(p);
     CK(cudaMemsetAsync(p, 0, bytes, x->stream));
     char* q = (char*)p;
@@ -931,9 +963,9 @@ int tc_operands(vp_ctx* x) {
                                                                                               t.Npad);
     int rc = check_launch(x, "k_build_counts");
     if (rc) return rc;
-    tc::k_allele_center<<<cdiv(x->L, 256), 256, 0, x->stream>>>(x->D, t.logpbar);
+    tc::k_allele_center<<<cdiv(x->L * 32, 256), 256, 0, x->stream>>>(x->D, t.logpbar);
     if ((rc = check_launch(x, "k_allele_center"))) return rc;
-    tc::k_center_const<<<cdiv((int64_t)x->N * 32, 256), 256, 0, x->stream>>>(x->D, t.logpbar, t.Bc);
+    tc::k_center_const<<<cdiv((int64_t)x->N * 32, 256), 256, 0, x->stream>>>(x->D, t.C, t.Apad, t.logpbar, t.Bc);
     if ((rc = check_launch(x, "k_center_const"))) return rc;
     if ((rc = make_map(&t.mapC, t.C, t.Npad, t.Apad, t.Apad, 128, t.bk))) return rc;
     if ((rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128, t.bk8, 1))) return rc;
@@ -957,16 +989,15 @@ int tc_splits(int64_t tiles, int nsm) {
 void free_batch(vp_ctx* x) {
     if (!x->batch) return;
     TcBatch* b = x->batch;
-    cudaStreamSynchronize(x->stream);
     for (vp_chain* c : b->chains) {
-        // hand each chain its counts back
-        cudaMemcpy(c->own_ni, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice);
+        // hand each chain its counts back (stream-ordered after the batch's work)
+        cudaMemcpyAsync(c->own_ni, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice, x->stream);
         c->h.Ni = c->own_ni;
-        cudaMemcpy(c->d, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice);
+        cudaMemcpyAsync(c->d, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream);
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     }
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    cudaFree(b->mem);
+    dev_free(b->mem, x->stream);
     delete b;
     x->batch = nullptr;
 }
@@ -1015,8 +1046,8 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
         b->NiAll = cv.take<int32_t>((int64_t)b->Rpad * x->KT);
     };
     lay(probe);
-    cudaError_t e = cudaMalloc(&b->mem, probe.off);
-    if (e != cudaSuccess) { delete b; vp_set_error("cudaMalloc(%zu) for the batch: %s", probe.off, cudaGetErrorString(e)); return VP_E_MEM; }
+    cudaError_t e = dev_alloc(&b->mem, probe.off, x->device, x->stream);
+    if (e != cudaSuccess) { delete b; vp_set_error("device allocation of %zu bytes for the batch: %s", probe.off, cudaGetErrorString(e)); return VP_E_MEM; }
     Carve cv{(char*)b->mem};
     lay(cv);
     CK(cudaMemsetAsync(b->mem, 0, probe.off, x->stream));
@@ -1324,6 +1355,18 @@ extern "C" int vp_debug_gemm_time(int32_t M, int32_t N, int32_t K, int32_t BN, i
 }
 
 extern "C" void* vp_stream(vp_ctx* x) { return x ? (void*)x->stream : nullptr; }
+
+extern "C" int vp_release_memory(int device) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
+    if (device < 0 || device >= ndev) { vp_set_error("device %d out of range", device); return VP_E_ARG; }
+    cudaMemPool_t pool = lib_pool(device);
+    if (!pool) { vp_set_error("no memory pool on device %d", device); return VP_E_CUDA; }
+    CK(cudaSetDevice(device));
+    CK(cudaDeviceSynchronize());
+    CK(cudaMemPoolTrimTo(pool, 0));
+    return VP_OK;
+}
 
 extern "C" int vp_prof_enable(vp_ctx* x, int on) {
     if (!x) { vp_set_error("null context"); return VP_E_ARG; }

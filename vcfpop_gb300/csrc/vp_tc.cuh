@@ -344,34 +344,57 @@ __global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bflo
 
 // per-allele centring constant: ln of the dataset allele frequency (with a
 // pseudo-count), and B[i] = sum_a C[i][a] * ln pbar_a, computed once
+// one warp per locus: the lanes popcount the bit planes of the locus's
+// packed words (codes 1 and 2 count copies of allele 1; 3 is missing or
+// padding)
 __global__ void k_allele_center(const DevData D, float* logpbar) {
-    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t l = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (l >= D.L) return;
-    int64_t n1 = 0, t = 0;
-    for (int i = 0; i < D.N; ++i) {
-        int code = (D.g2[l * D.Nw + (i >> 4)] >> ((i & 15) * 2)) & 3;
-        if (code != 3) { t += 2; n1 += code; }
+    int n1 = 0, miss = 0;
+    for (int w = lane; w < D.Nw; w += 32) {
+        const uint32_t v = D.g2[l * D.Nw + w];
+        const uint32_t lo = v & 0x55555555u, hi = (v >> 1) & 0x55555555u;
+        n1 += __popc(lo & ~hi) + 2 * __popc(hi & ~lo);
+        miss += __popc(lo & hi);
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        n1 += __shfl_xor_sync(0xffffffffu, n1, o);
+        miss += __shfl_xor_sync(0xffffffffu, miss, o);
+    }
+    if (lane) return;
+    const int64_t t = 2 * ((int64_t)D.Nw * 16 - miss);
     logpbar[2 * l] = logf((float)(t - n1 + 1) / (float)(t + 2));
     logpbar[2 * l + 1] = logf((float)(n1 + 1) / (float)(t + 2));
 }
-__global__ void k_center_const(const DevData D, const float* logpbar, double* Bc) {
-    // one warp per individual, Kahan sums per lane, FP64 across lanes
+// B[i] = sum_a C[i][a] ln pbar_a: one warp per individual over its contiguous
+// bf16 count row (8 values per 16-byte load), Kahan sums per lane, FP64
+// across lanes
+__global__ void k_center_const(const DevData D, const __nv_bfloat16* C, int64_t Apad, const float* logpbar,
+                               double* Bc) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= D.N) return;
-    const int i = warp;
+    const uint4* row = reinterpret_cast<const uint4*>(C + (int64_t)warp * Apad);
+    const int64_t n8 = Apad / 8;
     float s = 0.f, cmp = 0.f;
-    for (int64_t l = lane; l < D.L; l += 32) {
-        int code = (D.g2[l * D.Nw + (i >> 4)] >> ((i & 15) * 2)) & 3;
-        if (code == 3) continue;
-        float v = (2.f - code) * logpbar[2 * l] + (float)code * logpbar[2 * l + 1];
-        float y = v - cmp, t = s + y;
+    for (int64_t j = lane; j < n8; j += 32) {
+        const uint4 v = row[j];
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float c0 = __uint_as_float(w[q] << 16), c1 = __uint_as_float(w[q] & 0xFFFF0000u);
+            const int64_t a = j * 8 + 2 * q;
+            if (c0 != 0.f) acc += c0 * logpbar[a];
+            if (c1 != 0.f) acc += c1 * logpbar[a + 1];
+        }
+        const float y = acc - cmp, t = s + y;
         cmp = (t - s) - y;
         s = t;
     }
     double d = (double)s - (double)cmp;
     for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if (lane == 0) Bc[i] = d;
+    if (lane == 0) Bc[warp] = d;
 }
 
 struct BatchDev {
