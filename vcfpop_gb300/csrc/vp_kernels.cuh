@@ -1332,11 +1332,10 @@ __global__ void k_update_f(const DevChain* chains) {
 
 // Record (src/structure.cpp:1941-2045): likelihood trace, running sums of the
 // likelihood and parameters, then m += 1. One block per chain.
-__global__ void k_record(const DevChain* chains) {
-    const DevChain& c = chains[blockIdx.z];
+// the scalar part of Record at sweep m, by one block
+__device__ void record_scalars(const DevChain& c, int m, double* sh) {
     const DevData& D = c.D;
-    const int K = c.K, m = c.ctl->m;
-    __shared__ double sh[32];
+    const int K = c.K;
     if (record_at(c, m)) {
         double like;
         if (binaryq_at(c, m)) like = c.ctl->lnl;
@@ -1369,6 +1368,12 @@ __global__ void k_record(const DevChain* chains) {
     }
 }
 
+__global__ void k_record(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    __shared__ double sh[32];
+    record_scalars(c, c.ctl->m, sh);
+}
+
 // the element-wise part of Record: MiSum += Mi on every recorded sweep,
 // FreqM += Freq after burn-in; the last kernel of a sweep also advances m
 __global__ void k_accumulate(const DevChain* chains, int advance) {
@@ -1386,6 +1391,29 @@ __global__ void k_accumulate(const DevChain* chains, int advance) {
 __global__ void k_advance(const DevChain* chains) {
     const DevChain& c = chains[blockIdx.z];
     if (threadIdx.x == 0 && blockIdx.x == 0) c.ctl->m++;
+}
+
+// Record and the advance of m in one launch (the end of a captured sweep):
+// every block adds its share of MiSum / FreqM; the last block to finish
+// (after all blocks have read m) does the scalar Record and m += 1
+__global__ void k_record_sweep(const DevChain* chains) {
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    __shared__ double sh[32];
+    const int m = c.ctl->m;
+    if (record_at(c, m)) {
+        int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t j = tid; j < (int64_t)D.N * c.K; j += nt) c.MiSum[j] += c.Mi[j];
+        if (m >= c.nburnin)
+            for (int64_t j = tid; j < (int64_t)c.K * D.KT; j += nt) c.FreqM[j] += c.Freq[j];
+    }
+    if (!last_block_done(c.ctl, gridDim.x)) return;
+    record_scalars(c, m, sh);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        c.ctl->done = 0;
+        c.ctl->m = m + 1;
+    }
 }
 
 // Arrange (src/structure.cpp:1860-1869)

@@ -329,11 +329,17 @@ int launch_step(vp_chain* c, int step, int force) {
 
 int launch_sweep(vp_chain* c) {
     static const int seq[] = {VP_STEP_UPDATEP, VP_STEP_UPDATEQ, VP_STEP_LOCPRIORI, VP_STEP_UPDATEZ, VP_STEP_ALPHA,
-                              VP_STEP_UPDATEA, VP_STEP_UPDATEF, VP_STEP_RECORD, VP_STEP_NEXT};
+                              VP_STEP_UPDATEA, VP_STEP_UPDATEF};
     for (int st : seq) {
         int rc = launch_step(c, st, 0);
         if (rc) return rc;
     }
+    // Record and m += 1 as one launch
+    vp_ctx* x = c->ctx;
+    // at most 128 blocks: the element-wise part only runs on recorded sweeps,
+    // and every block takes part in the last-block count
+    LAUNCH(x, k_record_sweep, (dim3(std::min<unsigned>(128, cdiv((int64_t)c->P.K * x->KT, 256)), 1, 1), 256, 0, x->stream),
+           (c->d));
     return VP_OK;
 }
 
@@ -1122,10 +1128,8 @@ int launch_tc_sweep(vp_ctx* x) {
     // count contraction: Ni[row, a] = sum_i OH[row, i] C[i, a]
     if (int rc = launch_counts_gemm(x)) return rc;
     // Record for every chain, then m += 1
-    unsigned ga = std::min<unsigned>(1024, cdiv((int64_t)16 * x->KT, 256));
-    LAUNCH(x, k_record, (dim3(1, 1, n), 256, 0, s), (b->dchains));
-    LAUNCH(x, k_accumulate, (dim3(ga, 1, n), 256, 0, s), (b->dchains, 0));
-    LAUNCH(x, k_advance, (dim3(1, 1, n), 32, 0, s), (b->dchains));
+    unsigned ga = std::min<unsigned>(128, cdiv((int64_t)16 * x->KT, 256));
+    LAUNCH(x, k_record_sweep, (dim3(ga, 1, n), 256, 0, s), (b->dchains));
     return VP_OK;
 }
 
