@@ -75,11 +75,16 @@ def test_reference_streams_admixture_trace():
     assert rel[:3].max() < 1e-5, rel
 
 
-@pytest.mark.parametrize("model", ["noadmix", "admix"])
+@pytest.mark.parametrize("model", ["noadmix", "admix", "admix_locprior"])
 def test_counter_streams_match_oracle_statistically(model):
     if model == "noadmix":
         d = synth.fmodel(41, 120, 500, 3, 0.1, 0.05)
         K, kw = 3, dict(admix=0, nadmburnin=0, nburnin=100, nreps=300)
+    elif model == "admix_locprior":
+        # location prior with admixture: the local alpha steps run one
+        # location per thread on their own streams
+        d = synth.fmodel(43, 160, 500, 3, 0.05, 0.02, loc_ids=np.repeat(np.arange(8), 20), loc_alpha=1.0)
+        K, kw = 3, dict(admix=1, locpriori=1, nburnin=150, nreps=300)
     else:
         d = synth.fmodel(42, 120, 500, 3, 0.05, 0.02, admix_alpha=0.5)
         K, kw = 3, dict(admix=1, nburnin=150, nreps=300)

@@ -222,6 +222,11 @@ struct Philox {
         uint64_t h = next(), l = next();
         return ((double)(((h << 32) | l) >> 11) + 1.0) * (1.0 / 9007199254740992.0);
     }
+    // standard normal in double precision (Box-Muller on two double uniforms)
+    __device__ inline double normald() {
+        const double u1 = uniformd(), u2 = uniformd();
+        return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+    }
     __device__ inline float normalf() {
         float u1 = uniformf(), u2 = uniformf();
         float r = sqrtf(-2.0f * logf(u1));

@@ -53,7 +53,8 @@ struct DevChain {
 };
 
 // step ids folded into Philox counters
-enum : uint32_t { ST_INITZ = 1, ST_P = 2, ST_Q = 3, ST_METRO_P = 4, ST_METRO_A = 5, ST_Z = 6, ST_A = 7, ST_INITADM = 8 };
+enum : uint32_t { ST_INITZ = 1, ST_P = 2, ST_Q = 3, ST_METRO_P = 4, ST_METRO_A = 5, ST_Z = 6, ST_A = 7, ST_INITADM = 8,
+                  ST_ALPHA = 9 };
 
 __device__ __forceinline__ bool binaryq_at(const DevChain& c, int m) { return !c.admix && m >= c.nadmburnin; }
 __device__ __forceinline__ bool metro_turn(const DevChain& c, int m) { return c.admix && c.metrofreq > 0 && m % c.metrofreq == 0; }
@@ -1044,9 +1045,63 @@ __global__ void k_logprod_q(const DevChain* chains) {
 
 // UpdateAlpha (src/structure.cpp:1499-1594), reference stream
 // RNG(seed + m, SALT_UPDATEALPHA), on one thread
+// counter streams, location prior with admixture: the K global steps on one
+// thread, then the local steps with one thread per location (a location's K
+// steps stay in order: they share its SumAlpha), each location on its own
+// Philox stream
+__device__ void update_alpha_locprior_ctr(const DevChain& c, int m) {
+    const DevData& D = c.D;
+    const int K = c.K, S = D.S;
+    const double r = c.ctl->r;
+    if (threadIdx.x == 0) {
+        Philox ph;
+        ph.init(c.seed, ST_ALPHA | ((uint32_t)m << 4), 0xFFFFFFFFu, 0);
+        for (int k = 0; k < K; ++k) {
+            double am = c.Alpha[k] + c.stdalpha * ph.normald();
+            if (am > 0 && am < c.maxalpha) {
+                double d = am - c.Alpha[k];
+                double dlnL = S * (d * r * ref_mylog(r) + lgamma(r * c.Alpha[k]) - lgamma(r * am));
+                double lp = 0;   // ln of the product over locations of AlphaLocal[., k]
+                for (int sl = 0; sl < S; ++sl) lp += ref_mylog(c.AlphaLocal[sl * K + k]);
+                dlnL += r * d * lp;
+                if (dlnL >= VP_NZERO || ph.uniformd() < exp(dlnL)) c.Alpha[k] = am;
+            }
+        }
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < S; s += blockDim.x) {
+        Philox ph;
+        ph.init(c.seed, ST_ALPHA | ((uint32_t)m << 4), (uint32_t)s, 1);
+        if (m % 10 == 0) {
+            double t = 0;
+            for (int k = 0; k < K; ++k) t += c.AlphaLocal[s * K + k];
+            c.SumAlpha[s] = t;
+        }
+        const int snind = D.pop_nind[s];
+        for (int k = 0; k < K; ++k) {
+            double ao = c.AlphaLocal[s * K + k], am = ao + c.stdalpha * ph.normald();
+            if (am > 0 && am < c.maxalpha) {
+                double d = am - ao;
+                double dlnL = (r * c.Alpha[k] - 1) * ref_mylog(am / ao) - d * r +
+                              snind * (lgamma(c.SumAlpha[s] + d) - lgamma(am) - lgamma(c.SumAlpha[s]) + lgamma(ao));
+                dlnL += d * c.red[s * K + k];
+                if (dlnL >= VP_NZERO || ph.uniformd() < exp(dlnL)) {
+                    c.AlphaLocal[s * K + k] = am;
+                    c.SumAlpha[s] += d;
+                }
+            }
+        }
+    }
+}
+
 __global__ void k_update_alpha(const DevChain* chains) {
     const DevChain& c = chains[blockIdx.z];
-    if (threadIdx.x || blockIdx.x) return;
+    if (blockIdx.x) return;
+    if (c.rng != 0 && c.locpriori && c.admix) {
+        update_alpha_locprior_ctr(c, c.ctl->m);
+        return;
+    }
+    if (threadIdx.x) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m, S = D.S, N = D.N;
     Rng64 rng; rng.init(c.seed + (uint64_t)m, VP_SALT_UPDATEALPHA);

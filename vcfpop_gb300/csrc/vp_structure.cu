@@ -303,7 +303,7 @@ int launch_step(vp_chain* c, int step, int force) {
         case VP_STEP_ALPHA:
             if ((P.inferalpha && (P.admix || c->h.nadmburnin > 0)) || (P.locpriori && P.admix)) {
                 LAUNCH(x, k_logprod_q, (dim3(ref ? std::max(1, (x->S * K + 255) / 256) : LPQ_BLOCKS, 1, 1), 256, 0, s), (c->d));
-                LAUNCH(x, k_update_alpha, (dim3(1, 1, 1), 32, 0, s), (c->d));
+                LAUNCH(x, k_update_alpha, (dim3(1, 1, 1), 128, 0, s), (c->d));
             }
             return VP_OK;
         case VP_STEP_UPDATEA:
