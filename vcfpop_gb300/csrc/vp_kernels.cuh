@@ -831,15 +831,15 @@ __global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
 // CTA = 8 warps = 256 individuals; grid.y splits the loci into ranges that a
 // CTA walks in slices of ZA_LC loci. A lane keeps its individual's Q row and
 // its Mi counts in registers; the slice's frequencies are staged in shared
-// memory. The per-copy increments of Ni are reduced across the warp before
-// they reach the slice histogram in shared memory: with at most ZA_PACKED
-// (cluster, allele) bins, each lane's bin becomes a 1 in one of five 6-bit
-// fields of a word and redux.sync adds the words of the 32 lanes (one
-// reduction per five bins), then lane j adds bin j; with more bins, lanes
-// with equal bins are grouped by __match_any_sync and one of them adds the
-// group's size. The slice histogram is flushed to Ni with one global atomic
-// per non-zero entry. KM is the cluster count rounded up to a compiled size;
-// EXACT means K == KM.
+// memory. With at most ZA_PACKED (cluster, allele) bins the per-copy
+// increments of Ni are reduced across the warp before they reach the slice
+// histogram in shared memory: each lane's bin becomes a 1 in one of five
+// 6-bit fields of a word and redux.sync adds the words of the 32 lanes (one
+// reduction per five bins), then lane j adds bin j; with more bins (multi-
+// allelic data) each copy adds to the shared histogram directly (measured
+// faster there than grouping lanes with __match_any_sync). The slice
+// histogram is flushed to Ni with one global atomic per non-zero entry. KM is
+// the cluster count rounded up to a compiled size; EXACT means K == KM.
 constexpr int ZA_WARPS = 8;
 constexpr int ZA_LC = 16;
 constexpr int ZA_PACKED = 40;
@@ -925,12 +925,8 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
                         const int cnt = (int)((mine >> (6 * (lane % 5))) & 63u);
                         if (cnt) atomicAdd(&hl[lane], cnt);
                     }
-                } else {
-                    const unsigned am = __ballot_sync(0xffffffffu, act);
-                    if (act) {
-                        const unsigned grp = __match_any_sync(am, key);
-                        if (lane == __ffs(grp) - 1) atomicAdd(&hl[key], __popc(grp));
-                    }
+                } else if (act) {
+                    atomicAdd(&hl[key], 1);
                 }
             }
             float y = lacc - lc, tt = ls + y;
