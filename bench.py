@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-sweeps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="c3: skip the plain-form comparison sweeps")
+    ap.add_argument("--tune", type=int, default=2, choices=[0, 1, 2],
+                    help="c3: autotuner effort for the batched contractions before warm-up (0: built-in defaults)")
     ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--requests", type=int, default=120, help="c5: runs in the stream")
     ap.add_argument("--c5-scale", type=float, default=0.1, help="c5: scale of the N, L and run-length ranges")
@@ -542,6 +545,62 @@ def bench_serve(args):
 
 
 # ---------------------------------------------------------------- GPU leg
+def lnp_rel_err(chains):
+    """Largest relative error of the chains' last lnP(D) against the FP64
+    evaluation of the same state: without admixture Record's lnP(D) is the sum
+    of Ni x ln p over clusters, loci and alleles."""
+    worst = 0.0
+    for c in chains:
+        ni, p = c.get("NI"), c.get("FREQ")
+        m = ni > 0
+        want = float(np.sum(ni[m].astype(np.float64) * np.log(p[m].astype(np.float64))))
+        worst = max(worst, abs(float(c.get("LNL")[0]) - want) / abs(want))
+    return worst
+
+
+def recorded_lnp_err(ctx):
+    """The batched form's recorded lnP(D) on the full-size data: 10 chains
+    (K = 1..10) that record every sweep, against the FP64 evaluation."""
+    from vcfpop_gb300 import _lib as B
+    from vcfpop_gb300 import structure as S
+    chains = [S.Chain(ctx, S.params(K, S.run_seed(2, K), form=B.VP_FORM_TC, admix=0, nadmburnin=0, nburnin=0,
+                                    nreps=100, nthinning=1, writelnl=1)) for K in range(1, 11)]
+    S.run_chains(chains, 2)
+    err = lnp_rel_err(chains)
+    for c in chains:
+        c.close()
+    return err
+
+
+def plain_form_leg(ctx, lib, upd_step, world, steps=3):
+    """The same 100 chains in the plain FP32 form on the same context: a few
+    timed sweeps (after one untimed), for the batched-over-plain ratio."""
+    import ctypes as C
+    import torch
+    from vcfpop_gb300 import _lib as B
+    from vcfpop_gb300 import replicas as R
+    from vcfpop_gb300 import structure as S
+    chains = [S.Chain(ctx, S.params(K, S.run_seed(1, j + 1), form=B.VP_FORM_PLAIN, admix=0, nadmburnin=0,
+                                    nburnin=1000, nreps=2000)) for j, K in enumerate(KS)]
+    arr = (C.c_void_p * len(chains))(*[c.h for c in chains])
+    B.check(lib.vp_run(arr, len(chains), 1))
+    ctx.sync()
+    stream = torch.cuda.ExternalStream(lib.vp_stream(ctx.h))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    R.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    B.check(lib.vp_run(arr, len(chains), steps))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = R.max_over_ranks(e0.elapsed_time(e1)) / steps
+    err = lnp_rel_err(chains)
+    for c in chains:
+        c.close()
+    return {"value": upd_step * world / (ms / 1e3), "ms_per_step": ms, "steps": steps, "warmup": 1,
+            "lnp_rel_err_max": err}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -587,6 +646,12 @@ def main():
     ctx = S.Context(ds, local)
     chains = make(ctx)
     lib = B.lib()
+    tuning = None
+    if form == B.VP_FORM_TC and args.tune:
+        t0 = time.perf_counter()
+        tuning = S.tune(chains, args.tune)
+        tuning["effort"] = args.tune
+        tuning["seconds"] = time.perf_counter() - t0
     lib.vp_prof_enable(ctx.h, 1)
     arr = (C.c_void_p * len(chains))(*[c.h for c in chains])
     for _ in range(args.warmup):
@@ -644,8 +709,24 @@ def main():
                 roof["traffic"] = tr["bytes_per_launch_at_full_size"]
         except Exception:
             pass
+    sweep_ll_err = lnp_rel_err(chains)
     for c in chains:
         c.close()
+    lnp_err = None
+    if form == B.VP_FORM_TC:
+        lnp_err = {"max": recorded_lnp_err(ctx), "chains": 10, "bound": 1e-6,
+                   "what": "lnP(D) recorded by the batched form on full-size data (K=1..10, thinning 1, 2 sweeps)",
+                   "against": "FP64 sum of Ni x ln p over the same state, Record's lnP(D) (structure.cpp:1902-1938)",
+                   "sweep_ll_max": sweep_ll_err,
+                   "sweep_ll_what": "the 100 timed chains' per-sweep sum of the likelihood contraction (FP32 "
+                                    "accumulation), used for the label draws only"}
+    plain = None
+    if form == B.VP_FORM_TC and not args.no_plain:
+        plain = plain_form_leg(ctx, lib, upd_step, world)
+        lnp_err["plain_max"] = plain.pop("lnp_rel_err_max")
+    elif form != B.VP_FORM_TC:
+        lnp_err = {"max": sweep_ll_err, "chains": len(chains), "bound": 1e-6,
+                   "against": "FP64 sum of Ni x ln p over the same state, Record's lnP(D) (structure.cpp:1902-1938)"}
     outputs = output_reductions(ctx, ds, args, rank)
     ctx.close()
 
@@ -692,8 +773,11 @@ def main():
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "step": f"open context from pinned host buffers + create 100 chains + {args.e2e_sweeps} sweeps "
-                            f"+ read every chain's lnL + close", "ms_per_step": float(np.median(e2e_ms)) if e2e_ms else None},
-            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "outputs": outputs, "ingest": ingest, "locus_filter": lfilter}
+                            f"+ read every chain's lnL + close (launch configuration from the tuner's cache)", "ms_per_step": float(np.median(e2e_ms)) if e2e_ms else None},
+            "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "lnp_rel_err": lnp_err,
+            "plain_form": plain, "batched_over_plain": value / plain["value"] if plain else None,
+            "tuning": tuning,
+            "outputs": outputs, "ingest": ingest, "locus_filter": lfilter}
     if rank == 0:
         print(json.dumps(line), flush=True)
     R.finish()

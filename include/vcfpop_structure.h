@@ -179,6 +179,42 @@ int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t bytes);
  * non-zero means a pipeline wait timed out and that launch's output is void). */
 int vp_tc_status(vp_ctx* ctx);
 
+/* Launch configuration of the batched sweep's two tensor-core contractions
+ * (no reference counterpart: the reference has no batched form). The
+ * likelihood contraction [N x alleles] . [alleles x cluster rows] runs tiles
+ * of `row_tiles` x 128 individuals by `cols` cluster rows (`piece` rows per
+ * MMA), `bk` alleles per shared-memory stage, `stages` stages, the alleles
+ * split `splits` ways (0: the whole-wave rule), and with `group_major` the
+ * column groups of one individual tile launch next to each other. The count
+ * contraction has `count_stages` and `count_group_major`. Compiled tiles
+ * (bk, row_tiles, cols, piece): (64, 2, 192, 192), (64, 1, 288, 144),
+ * (32, 2, 192, 192). */
+typedef struct vp_tc_config {
+    int32_t bk, row_tiles, cols, piece, stages, splits, group_major;
+    int32_t count_stages, count_group_major;
+    int32_t candidates;            /* vp_tune: configurations timed */
+    float ms_likelihood;           /* vp_tune: device ms per launch, chosen configuration */
+    float ms_counts;
+    float ms_likelihood_default;   /* vp_tune: device ms per launch, configuration before tuning */
+    float ms_counts_default;
+} vp_tc_config;
+
+/* Autotuner of the batched sweep (no reference counterpart). Times the
+ * contractions of the batch of these tensor-core chains (one context) under
+ * candidate configurations on the device, keeps the fastest for the batch and
+ * for every later batch of the same shape (individuals, alleles, cluster
+ * rows, SMs) in this process, and, when the environment variable
+ * VP_TUNE_CACHE names a file, appends it there for later processes. effort
+ * 0 times the current configuration only; 1 also every pipeline depth, split
+ * count and CTA order of its tile; 2 every compiled tile as well. Chain state
+ * is unchanged. `out` (may be null) receives the choice and the timings. */
+int vp_tune(vp_chain** chains, int32_t n, int32_t effort, vp_tc_config* out);
+/* Sets the configuration of the batch of these chains (timings ignored);
+ * VP_E_ARG if it is not compiled in or does not fit. */
+int vp_tc_configure(vp_chain** chains, int32_t n, const vp_tc_config* cfg);
+/* The configuration the batch of these chains runs with. */
+int vp_tc_config_get(vp_chain** chains, int32_t n, vp_tc_config* out);
+
 /* Diagnostic: D[s][m][n] = sum over this split's k of A[m,k] (B0[n,k] + B1[n,k])
  * through the tensor-core kernel. A [M][K], B0/B1 [N][K] bf16 bit patterns,
  * bk (K elements per pipeline stage) 32 or 64, K % bk == 0, N % BN == 0,

@@ -103,6 +103,42 @@ def test_batched_tc_sweep_matches_plain():
             assert abs(lp - lt) <= 1e-6 * abs(lp)
 
 
+def _lnp_fp64(ch):
+    """lnP(D) of a no-admixture chain's current state in FP64: Record's sum
+    (structure.cpp:1902-1938) is the sum of Ni x ln p over clusters, loci and
+    alleles (pinned on the oracle by test_oracle_golden)."""
+    ni, p = ch.get("NI").astype(np.float64), ch.get("FREQ").astype(np.float64)
+    return float(np.sum(ni[ni > 0] * np.log(p[ni > 0])))
+
+
+def test_lnp_relative_error_against_fp64_at_most_1e6():
+    """Tolerance 1e-6 relative: the recorded lnP(D) of the batched split-bf16
+    form and of the plain FP32 form against the FP64 evaluation of the same
+    state, on every one of several recorded sweeps (thinning 1), for chains of
+    K = 1..8 in one batch. The data follow the K-sweep benchmark's F-model (8
+    populations, F = 0.03). The batch runs one split of all alleles (the
+    longest FP32 accumulation of the likelihood contraction), so the recorded
+    value must not come from that accumulation."""
+    d = synth.fmodel(53, 3000, 20000, 8, 0.03, 0.01)
+    ds = S.Dataset.from_synth(d)
+    ctx = S.Context(ds)
+    kw = dict(admix=0, nadmburnin=0, nburnin=0, nreps=50, nthinning=1, writelnl=1)
+    Ks = list(range(1, 9))
+    tc = [S.Chain(ctx, S.params(K, 400 + K, form=B.VP_FORM_TC, **kw)) for K in Ks]
+    plain = [S.Chain(ctx, S.params(K, 500 + K, **kw)) for K in Ks]
+    S.tc_configure(tc, splits=1)
+    worst = 0.0
+    for _ in range(4):
+        S.run_chains(tc, 1)
+        S.run_chains(plain, 1)
+        for ch in tc + plain:
+            want, got = _lnp_fp64(ch), ch.get("LNL")[0]
+            worst = max(worst, abs(got - want) / abs(want))
+            assert abs(got - want) <= 1e-6 * abs(want), (got, want, abs(got - want) / abs(want))
+    assert worst < 1e-6
+    assert B.lib().vp_tc_status(ctx.h) == 0
+
+
 def test_deferred_initial_counts_equal_plain():
     """A tensor-core chain leaves its initial counts to its batch; read before
     any batch exists they are computed on demand, and equal the plain chain's."""
@@ -115,3 +151,103 @@ def test_deferred_initial_counts_equal_plain():
         t = S.Chain(ctx, S.params(K, 700 + K, form=B.VP_FORM_TC, **kw))
         assert np.array_equal(p.get("Z"), t.get("Z"))
         assert np.array_equal(p.get("NI"), t.get("NI"))
+
+
+TILES = [(64, 2, 192, 192), (64, 1, 288, 144), (32, 2, 192, 192)]
+
+
+def _tc_set(ctx, Ks, seed0):
+    return [S.Chain(ctx, S.params(K, seed0 + j, form=B.VP_FORM_TC, admix=0, nadmburnin=0, nburnin=20, nreps=20))
+            for j, K in enumerate(Ks)]
+
+
+def _state(chains):
+    return [{f: c.get(f) for f in ("Z", "NI", "FREQ", "LL", "LNL")} for c in chains]
+
+
+def test_every_tc_configuration_gives_the_same_sweep():
+    """Every compiled tile, pipeline depth and CTA order of both contractions,
+    at one split count: with 64-allele stages the sweep is bit-identical to
+    the default configuration's (the same FP32 accumulation order per
+    output); with 32-allele stages the likelihoods agree to 1e-5 relative
+    and the first sweep's frequencies exactly."""
+    d = synth.fmodel(54, 700, 2000, 4, 0.05, 0.01)
+    ds = S.Dataset.from_synth(d)
+    ctx = S.Context(ds)
+    Ks = [10] * 40          # 400 cluster rows, padded to 576: whole groups of 192 and of 288
+    ref, ran = None, 0
+    for bk, mt, cols, piece in TILES:
+        for stages in range(2, 7):
+            for gm in (0, 1):
+                chains = _tc_set(ctx, Ks, 600)
+                try:
+                    S.tc_configure(chains, bk=bk, row_tiles=mt, cols=cols, piece=piece, stages=stages, splits=3,
+                                   group_major=gm, count_stages=2 + (stages + gm) % 3, count_group_major=1 - gm)
+                except B.VpError:
+                    for c in chains:
+                        c.close()
+                    continue        # does not fit in shared memory
+                cfg = S.tc_config(chains)
+                assert (cfg["bk"], cfg["cols"], cfg["stages"], cfg["splits"], cfg["group_major"]) == \
+                    (bk, cols, stages, 3, gm)
+                S.run_chains(chains, 1)
+                one = _state(chains)
+                S.run_chains(chains, 1)
+                two = _state(chains)
+                assert B.lib().vp_tc_status(ctx.h) == 0
+                for c in chains:
+                    c.close()
+                ran += 1
+                if ref is None:
+                    ref = (one, two)
+                    continue
+                for a, b in zip(ref[0], one):
+                    assert np.array_equal(a["FREQ"], b["FREQ"])
+                    if bk == 64:
+                        for f in a:
+                            assert np.array_equal(a[f], b[f]), (bk, cols, stages, gm, f)
+                    else:
+                        assert np.abs(a["LL"] - b["LL"]).max() <= 1e-5 * np.abs(a["LL"]).max()
+                        assert (a["Z"] != b["Z"]).mean() < 1e-3
+                if bk == 64:
+                    for a, b in zip(ref[1], two):
+                        for f in a:
+                            assert np.array_equal(a[f], b[f]), (bk, cols, stages, gm, f)
+    assert ran >= 12
+
+
+def test_tune_keeps_chain_state_and_serves_later_batches(tmp_path, monkeypatch):
+    """vp_tune times candidates on the batch without changing any chain's
+    state, keeps the fastest for the batch, hands it to the next batch of the
+    same shape, and appends it to the VP_TUNE_CACHE file."""
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("VP_TUNE_CACHE", str(cache))
+    d = synth.fmodel(55, 900, 2500, 4, 0.05, 0.01)
+    ds = S.Dataset.from_synth(d)
+    ctx = S.Context(ds)
+    Ks = [2, 3, 4, 5, 6, 7, 8] * 8
+    chains = _tc_set(ctx, Ks, 800)
+    S.run_chains(chains, 2)
+    before = _state(chains)
+    info = S.tune(chains, effort=2)
+    after = _state(chains)
+    for a, b in zip(before, after):
+        for f in a:
+            assert np.array_equal(a[f], b[f]), f
+    assert info["candidates"] > 8
+    for k in ("ms_likelihood", "ms_counts", "ms_likelihood_default", "ms_counts_default"):
+        assert 0 < info[k] < 1e3, (k, info)
+    assert info["ms_counts"] <= info["ms_counts_default"]
+    cfg = S.tc_config(chains)
+    for k in ("bk", "row_tiles", "cols", "piece", "stages", "splits", "group_major", "count_stages",
+              "count_group_major"):
+        assert cfg[k] == info[k], k
+    S.run_chains(chains, 2)
+    assert B.lib().vp_tc_status(ctx.h) == 0
+    lines = cache.read_text().split("\n")
+    assert len([ln for ln in lines if len(ln.split()) == 13]) >= 1
+    ctx2 = S.Context(ds)
+    other = _tc_set(ctx2, Ks, 900)
+    cfg2 = S.tc_config(other)
+    for k in ("bk", "cols", "stages", "splits", "group_major", "count_stages", "count_group_major"):
+        assert cfg2[k] == cfg[k], k

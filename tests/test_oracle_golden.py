@@ -125,3 +125,24 @@ def test_oracle_locus_filter_matches_reference(oracle_build):
     want = set(_diversity_loci(os.path.join(GOLD, "c1_filter", "out.structure.k=2_rep=1_id=1.txt")))
     assert 0 < len(want) < 2000
     assert kept == want
+
+
+def test_oracle_record_lnl_is_counts_times_log_frequencies(oracle_build):
+    """Without admixture, Record's lnP(D) (structure.cpp:1902-1938) is the sum
+    over clusters, loci and alleles of Ni x ln p at the state it is recorded
+    in: the identity the full-size lnP(D) error figure of the batched form is
+    measured with."""
+    import numpy as np
+    from tests import orc
+    from vcfpop_gb300 import synth
+    d = synth.fmodel(71, 150, 400, 3, 0.1, 0.05)
+    od = orc.Data(d)
+    for K in (2, 4):
+        oc = orc.Chain(od, orc.params(K, 900 + K, admix=0, nadmburnin=0, nburnin=5, nreps=5))
+        oc.init()
+        for _ in range(3):
+            oc.step("sweep")
+            got = orc.lib().orc_record_lnl(oc.h)
+            ni, p = oc.get("NI").astype(np.float64), oc.get("FREQ").astype(np.float64)
+            want = float(np.sum(ni[ni > 0] * np.log(p[ni > 0])))
+            assert abs(got - want) <= 1e-12 * abs(want), (K, got, want)

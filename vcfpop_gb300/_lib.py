@@ -70,6 +70,15 @@ class VpLocusFilter(C.Structure):
                                           "I_max")]
 
 
+class VpTcConfig(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("bk", "row_tiles", "cols", "piece", "stages", "splits", "group_major",
+                                         "count_stages", "count_group_major", "candidates")] + \
+               [(n, C.c_float) for n in ("ms_likelihood", "ms_counts", "ms_likelihood_default", "ms_counts_default")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class VpError(RuntimeError):
     pass
 
@@ -82,7 +91,8 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_run", "vp_finish", "vp_chain_sizes", "vp_chain_result", "vp_chain_divergence", "vp_chain_step", "vp_chain_get",
            "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
-           "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2", "vp_release_memory"]
+           "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2", "vp_release_memory",
+           "vp_tune", "vp_tc_configure", "vp_tc_config_get"]
 
 
 def lib():
@@ -121,6 +131,9 @@ def lib():
     L.vp_launch_count.restype = C.c_int64
     L.vp_last_error.restype = C.c_char_p
     L.vp_tc_status.argtypes = [P]
+    L.vp_tune.argtypes = [C.POINTER(P), C.c_int32, C.c_int32, C.POINTER(VpTcConfig)]
+    L.vp_tc_configure.argtypes = [C.POINTER(P), C.c_int32, C.POINTER(VpTcConfig)]
+    L.vp_tc_config_get.argtypes = [C.POINTER(P), C.c_int32, C.POINTER(VpTcConfig)]
     L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 9 + [P]
     L.vp_debug_gemm_time.argtypes = [C.c_int32] * 13 + [P]
     L.vp_debug_gemm_e4m3.argtypes = [P, P] + [C.c_int32] * 7 + [P]

@@ -92,11 +92,6 @@ __device__ inline double ref_mylog(double v) {
 __device__ inline float ln_freq(float p) {
     return p > 0.f ? logf(p) : -709.0895657128241f;
 }
-// the same with the hardware logarithm (absolute error about 2^-21), for
-// the centred tensor-core weights, whose bf16 hi + lo split keeps 16 bits
-__device__ inline float ln_freq_fast(float p) {
-    return p > 0.f ? __logf(p) : -709.0895657128241f;
-}
 
 // ---------------- RNG<double>: xorshift128+ ----------------
 struct Rng64 {

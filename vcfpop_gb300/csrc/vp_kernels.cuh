@@ -1446,19 +1446,55 @@ __global__ void k_advance(const DevChain* chains) {
 
 // Record and the advance of m in one launch (the end of a captured sweep):
 // every block adds its share of MiSum / FreqM; the last block to finish
-// (after all blocks have read m) does the scalar Record and m += 1
-__global__ void k_record_sweep(const DevChain* chains) {
+// (after all blocks have read m) does the scalar Record and m += 1.
+// With `exact` (the chains of a tensor-core batch), a recorded sweep's
+// lnP(D) is formed from the counts: without admixture Record's sum over
+// individuals and allele copies of ln p (src/structure.cpp:1902-1938) equals
+// the sum over clusters, loci and alleles of Ni x ln p, with Ni the counts of
+// the labels just drawn and p the frequencies they were drawn with. Each
+// thread adds its products (all <= 0) with a compensated FP32 sum, the
+// blocks' sums go to exact[chain][block] and the last block adds them in
+// block order in FP64: within about 1e-7 relative. The batch's per-sweep sum
+// from the likelihood contraction, whose FP32 accumulation over 10^5 and
+// more alleles per split drifts by a few 1e-6 relative, serves the label
+// draws only.
+__global__ void k_record_sweep(const DevChain* chains, double* exact) {
     const DevChain& c = chains[blockIdx.z];
     const DevData& D = c.D;
     __shared__ double sh[32];
     const int m = c.ctl->m;
-    if (record_at(c, m)) {
+    const bool rec = record_at(c, m);
+    if (rec) {
         int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
         for (int64_t j = tid; j < (int64_t)D.N * c.K; j += nt) c.MiSum[j] += c.Mi[j];
-        if (m >= c.nburnin)
+        const bool fm = m >= c.nburnin;
+        if (exact) {
+            float s = 0.f, cmp = 0.f;
+            for (int64_t j = tid; j < (int64_t)c.K * D.KT; j += nt) {
+                const float p = c.Freq[j];
+                if (fm) c.FreqM[j] += p;
+                const int n = c.Ni[j];
+                if (n) {
+                    const float y = (float)n * ln_freq(p) - cmp, t = s + y;
+                    cmp = (t - s) - y;
+                    s = t;
+                }
+            }
+            const double bs = block_sum((double)s - (double)cmp, sh);
+            if (threadIdx.x == 0) exact[(int64_t)blockIdx.z * gridDim.x + blockIdx.x] = bs;
+        } else if (fm) {
             for (int64_t j = tid; j < (int64_t)c.K * D.KT; j += nt) c.FreqM[j] += c.Freq[j];
+        }
     }
     if (!last_block_done(c.ctl, gridDim.x)) return;
+    if (rec && exact) {
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int q = 0; q < (int)gridDim.x; ++q) t += exact[(int64_t)blockIdx.z * gridDim.x + q];
+            c.ctl->lnl = t;
+        }
+        __syncthreads();
+    }
     record_scalars(c, m, sh);
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -66,22 +66,36 @@ struct vp_chain {
     bool counts_pending = false;
 };
 
+// launch configuration of a batch's two contractions: the likelihood
+// contraction's tile (K elements per stage, 128-row tiles of individuals and
+// cluster rows per CTA, rows per MMA), pipeline depth, split-K count and CTA
+// order, and the count contraction's pipeline depth and CTA order
+struct TcChoice {
+    int bk1 = 64, mt1 = 2, bn1 = 192, piece1 = 192, st1 = 2, splits = 0 /* 0: whole waves */, gm1 = 0;
+    int st2 = 4, gm2 = 1;
+};
+
 // a set of no-admixture chains sharing one context, swept together with the
 // tensor-core contraction
 struct TcBatch {
     std::vector<vp_chain*> chains;
     void* mem = nullptr;
     DevChain* dchains = nullptr;
+    DevChain** dptrs = nullptr;     // each chain's own device header
+    double* lnlrec = nullptr;       // [chain][block] sums of a recorded sweep's lnP(D)
     int32_t *rowchain = nullptr, *rowk = nullptr, *row0 = nullptr;
+    // cluster rows padded to whole 192-row column groups of the count
+    // contraction (BN cluster rows per CTA, piece per MMA)
     int R = 0, Rpad = 0, G = 0, BN = 192, piece = 192, splits = 1;
-    // pipeline of the likelihood (1) and count (2) contractions: 128-row A
-    // tiles per CTA and shared-memory stages of bk K elements
-    int mt1 = 2, st1 = 2, mt2 = 2, st2 = 4;
+    // the count contraction's 128-row A tiles per CTA (compiled in)
+    int mt2 = 2;
+    TcChoice cfg;
+    int G1 = 0;               // column groups of the likelihood contraction (Rpad / cfg.bn1)
     __nv_bfloat16 *Whi = nullptr, *Wlo = nullptr;
     uint8_t* OH = nullptr;
     float* LLpart = nullptr;
     int32_t* NiAll = nullptr;
-    CUtensorMap mapWhi, mapWlo, mapOH;
+    CUtensorMap mapC1, mapWhi, mapWlo, mapOH;
     cudaGraphExec_t graph = nullptr;
     int graph_nodes = 0;
 };
@@ -339,7 +353,7 @@ int launch_sweep(vp_chain* c) {
     // at most 128 blocks: the element-wise part only runs on recorded sweeps,
     // and every block takes part in the last-block count
     LAUNCH(x, k_record_sweep, (dim3(std::min<unsigned>(128, cdiv((int64_t)c->P.K * x->KT, 256)), 1, 1), 256, 0, x->stream),
-           (c->d));
+           (c->d, nullptr));
     return VP_OK;
 }
 
@@ -936,6 +950,10 @@ int launch_gemm(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CU
     if (g.bk * g.esz != 64 && g.bk * g.esz != 128) { vp_set_error("gemm stage rows must be 64 or 128 bytes"); return VP_E_ARG; }
     size_t sm = tc::gemm_smem_bytes(g.BN, g.nb, g.stages, g.mt, g.bk, g.esz);
     if (sm > 227 * 1024) { vp_set_error("gemm tile needs %zu bytes of shared memory", sm); return VP_E_ARG; }
+    // a CTA whose accumulators take more than half of the SM's 512 TMEM
+    // columns allocates all of them: reserve more than half of the SM's
+    // shared memory too, so that no second CTA lands on its SM to wait
+    if (g.mt * g.BN > 256) sm = std::max<size_t>(sm, 115 * 1024);
 #define VP_GEMM_CASE(bk_, es_, mt_, nb_, bn_, pc_)                                                        \
     if (g.bk == bk_ && g.esz == es_ && g.mt == mt_ && g.nb == nb_ && g.BN == bn_ && g.piece == pc_)      \
         return launch_gemm_t<bk_, es_, mt_, nb_, bn_, pc_>(x, A, B0, B1, g, grid, sm);
@@ -953,26 +971,34 @@ int tc_operands(vp_ctx* x) {
     const int64_t A = 2 * x->L;
     t.Apad = (A + 63) / 64 * 64;
     t.Npad = (x->N + 127) / 128 * 128;
-    size_t bytes = (size_t)t.Npad * t.Apad * 2 + (size_t)t.Npad * t.Apad + 256 + t.Apad * 4 + t.Npad * 8 + 256;
+    const size_t cbytes = (size_t)t.Npad * t.Apad * 2, ctbytes = ((size_t)t.Npad * t.Apad + 255) / 256 * 256;
+    // locus groups of the operand build (BUILD_TILES tiles of 64 loci each)
+    const unsigned groups = cdiv(cdiv(x->L, 64), tc::BUILD_TILES);
+    const size_t tail = t.Apad * 4 + t.Npad * 8 + 256 + (size_t)groups * t.Npad * 4;
     void* p = nullptr;
-    cudaError_t e = dev_alloc(&p, bytes, x->device, x->stream);
-    if (e != cudaSuccess) { vp_set_error("device allocation of %zu bytes for tensor-core operands: %s", bytes, cudaGetErrorString(e)); return VP_E_MEM; }
+    cudaError_t e = dev_alloc(&p, cbytes + ctbytes + tail, x->device, x->stream);
+    if (e != cudaSuccess) {
+        vp_set_error("device allocation of %zu bytes for tensor-core operands: %s", cbytes + ctbytes + tail,
+                     cudaGetErrorString(e));
+        return VP_E_MEM;
+    }
     x->allocs.push_back(p);
-    CK(cudaMemsetAsync(p, 0, bytes, x->stream));
     char* q = (char*)p;
-    t.C = (__nv_bfloat16*)q; q += (size_t)t.Npad * t.Apad * 2;
-    t.CT = (uint8_t*)q; q += ((size_t)t.Npad * t.Apad + 255) / 256 * 256;
+    t.C = (__nv_bfloat16*)q; q += cbytes;
+    t.CT = (uint8_t*)q; q += ctbytes;
+    CK(cudaMemsetAsync(q, 0, tail, x->stream));     // C and CT are written whole by k_build_counts
     t.logpbar = (float*)q; q += t.Apad * 4;
     t.Bc = (double*)q; q += t.Npad * 8;
-    t.err = (int*)q;
-    tc::k_build_counts<<<dim3((unsigned)(t.Npad / 64), cdiv(x->L, 64), 1), 256, 0, x->stream>>>(x->D, t.C, t.CT, t.Apad,
-                                                                                              t.Npad);
-    int rc = check_launch(x, "k_build_counts");
-    if (rc) return rc;
+    t.err = (int*)q; q += 256;
+    float* part = (float*)q;
     tc::k_allele_center<<<cdiv(x->L * 32, 256), 256, 0, x->stream>>>(x->D, t.logpbar);
-    if ((rc = check_launch(x, "k_allele_center"))) return rc;
-    tc::k_center_const<<<cdiv((int64_t)x->N * 32, 256), 256, 0, x->stream>>>(x->D, t.C, t.Apad, t.logpbar, t.Bc);
-    if ((rc = check_launch(x, "k_center_const"))) return rc;
+    int rc = check_launch(x, "k_allele_center");
+    if (rc) return rc;
+    tc::k_build_counts<<<dim3((unsigned)(t.Npad / 128), groups, 1), 256, 0, x->stream>>>(x->D, t.C, t.CT, t.Apad, t.Npad,
+                                                                                      t.logpbar, part);
+    if ((rc = check_launch(x, "k_build_counts"))) return rc;
+    tc::k_center_sum<<<cdiv(x->N, 256), 256, 0, x->stream>>>(x->D, part, (int)groups, t.Npad, t.Bc);
+    if ((rc = check_launch(x, "k_center_sum"))) return rc;
     if ((rc = make_map(&t.mapC, t.C, t.Npad, t.Apad, t.Apad, 128, t.bk))) return rc;
     if ((rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128, t.bk8, 1))) return rc;
     t.ready = true;
@@ -992,26 +1018,151 @@ int tc_splits(int64_t tiles, int nsm) {
     return best;
 }
 
+// ---- launch configurations of the batched contractions and their tuner ----
+// the likelihood-contraction tiles compiled in with two B operands (hi, lo):
+// bf16 K elements per stage, 128-row tiles per CTA, cluster rows per CTA and
+// per MMA
+const int kTiles1[][4] = {{64, 2, 192, 192}, {64, 1, 288, 144}, {32, 2, 192, 192}};
+constexpr int kMaxStages = 6, kMaxSplits = 64;
+
+int64_t gemm1_tiles(const vp_ctx* x, int Rpad, const TcChoice& c) {
+    return cdiv(x->tc.Npad, 128 * c.mt1) * (int64_t)(Rpad / c.bn1);
+}
+
+int choice_error(const vp_ctx* x, int Rpad, const TcChoice& c) {
+    (void)x;
+    bool tile = false;
+    for (const auto& t : kTiles1) tile |= c.bk1 == t[0] && c.mt1 == t[1] && c.bn1 == t[2] && c.piece1 == t[3];
+    if (!tile) {
+        vp_set_error("likelihood tile (bk %d, row tiles %d, cols %d, piece %d) is not compiled in", c.bk1, c.mt1, c.bn1,
+                     c.piece1);
+        return VP_E_ARG;
+    }
+    if (Rpad % c.bn1) { vp_set_error("%d padded cluster rows are not whole groups of %d", Rpad, c.bn1); return VP_E_ARG; }
+    if (c.st1 < 2 || c.st1 > kMaxStages || tc::gemm_smem_bytes(c.bn1, 2, c.st1, c.mt1, c.bk1, 2) > 227 * 1024) {
+        vp_set_error("likelihood pipeline of %d stages does not fit", c.st1);
+        return VP_E_ARG;
+    }
+    if (c.st2 < 2 || c.st2 > kMaxStages || tc::gemm_smem_bytes(192, 1, c.st2, 2, 128, 1) > 227 * 1024) {
+        vp_set_error("count pipeline of %d stages does not fit", c.st2);
+        return VP_E_ARG;
+    }
+    if (c.splits < 0 || c.splits > kMaxSplits || (c.gm1 != 0 && c.gm1 != 1) || (c.gm2 != 0 && c.gm2 != 1)) {
+        vp_set_error("bad split count or CTA order");
+        return VP_E_ARG;
+    }
+    return VP_OK;
+}
+
+// choices measured by vp_tune, per (individuals, padded alleles, cluster
+// rows, SMs); with VP_TUNE_CACHE naming a file they are read from it at the
+// first lookup and appended to it when measured
+struct TuneKey {
+    int64_t N, A;
+    int R, nsm;
+    bool operator==(const TuneKey& o) const { return N == o.N && A == o.A && R == o.R && nsm == o.nsm; }
+};
+std::mutex g_tune_mu;
+std::vector<std::pair<TuneKey, TcChoice>> g_tuned;
+bool g_tune_loaded = false;
+
+void tune_put_locked(const TuneKey& k, const TcChoice& c) {
+    for (auto& e : g_tuned)
+        if (e.first == k) { e.second = c; return; }
+    g_tuned.push_back({k, c});
+}
+
+void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = getenv("VP_TUNE_CACHE");
+    FILE* f = path && *path ? fopen(path, "r") : nullptr;
+    if (!f) return;
+    long long N, A;
+    TuneKey k;
+    TcChoice c;
+    while (fscanf(f, "%lld %lld %d %d %d %d %d %d %d %d %d %d %d", &N, &A, &k.R, &k.nsm, &c.bk1, &c.mt1, &c.bn1,
+                  &c.piece1, &c.st1, &c.splits, &c.gm1, &c.st2, &c.gm2) == 13) {
+        k.N = N; k.A = A;
+        tune_put_locked(k, c);
+    }
+    fclose(f);
+}
+
+TuneKey tune_key(const vp_ctx* x, int R) { return TuneKey{x->N, x->tc.Apad, R, x->nsm}; }
+
+TcChoice tuned_choice(const vp_ctx* x, int R) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    tune_load_locked();
+    const TuneKey k = tune_key(x, R);
+    for (const auto& e : g_tuned)
+        if (e.first == k) return e.second;
+    return TcChoice{};
+}
+
+void tune_store(const vp_ctx* x, int R, const TcChoice& c) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    tune_load_locked();
+    const TuneKey k = tune_key(x, R);
+    tune_put_locked(k, c);
+    const char* path = getenv("VP_TUNE_CACHE");
+    if (FILE* f = path && *path ? fopen(path, "a") : nullptr) {
+        fprintf(f, "%lld %lld %d %d %d %d %d %d %d %d %d %d %d\n", (long long)k.N, (long long)k.A, k.R, k.nsm, c.bk1,
+                c.mt1, c.bn1, c.piece1, c.st1, c.splits, c.gm1, c.st2, c.gm2);
+        fclose(f);
+    }
+}
+
+// the likelihood contraction of the current batch under choice c
+int launch_gemm1(vp_ctx* x, const TcChoice& c, const CUtensorMap& A, const CUtensorMap& W0, const CUtensorMap& W1,
+                 int splits, float* out) {
+    const TcOperands& t = x->tc;
+    const TcBatch* b = x->batch;
+    tc::GemmArgs g{};
+    g.M = x->N; g.N = b->Rpad; g.kblocks = (int)(t.Apad / c.bk1);
+    g.kb_per_split = (g.kblocks + splits - 1) / splits;
+    g.BN = c.bn1; g.piece = c.piece1; g.nb = 2; g.mt = c.mt1; g.stages = c.st1; g.bk = c.bk1; g.esz = 2; g.mode = 0;
+    g.group_major = c.gm1;
+    g.out_f = out; g.ldo = b->Rpad; g.err = t.err;
+    const unsigned mtiles = cdiv(t.Npad, 128 * c.mt1), groups = (unsigned)(b->Rpad / c.bn1);
+    return launch_gemm(x, A, W0, W1, g, c.gm1 ? dim3(groups, mtiles, splits) : dim3(mtiles, groups, splits));
+}
+
+// copies each batch chain's header to the chain's own device header
+__global__ void k_scatter_chains(const DevChain* src, DevChain* const* dst, int n) {
+    static_assert(sizeof(DevChain) % 4 == 0, "DevChain copies as 32-bit words");
+    if (blockIdx.x >= n) return;
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(src + blockIdx.x);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst[blockIdx.x]);
+    for (int j = threadIdx.x; j < (int)(sizeof(DevChain) / 4); j += blockDim.x) d[j] = a[j];
+}
+
 void free_batch(vp_ctx* x) {
     if (!x->batch) return;
     TcBatch* b = x->batch;
-    for (vp_chain* c : b->chains) {
+    const int n = (int)b->chains.size();
+    std::vector<DevChain> hc(n);
+    for (int i = 0; i < n; ++i) {
+        vp_chain* c = b->chains[i];
         // hand each chain its counts back (stream-ordered after the batch's work)
         cudaMemcpyAsync(c->own_ni, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice, x->stream);
         c->h.Ni = c->own_ni;
-        cudaMemcpyAsync(c->d, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream);
+        hc[i] = c->h;
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     }
+    cudaMemcpyAsync(b->dchains, hc.data(), n * sizeof(DevChain), cudaMemcpyHostToDevice, x->stream);
+    k_scatter_chains<<<n, 128, 0, x->stream>>>(b->dchains, b->dptrs, n);
+    x->launches++;
     if (b->graph) cudaGraphExecDestroy(b->graph);
     dev_free(b->mem, x->stream);
     delete b;
     x->batch = nullptr;
 }
 
-int make_batch(vp_ctx* x, vp_chain** cs, int n) {
+int make_batch(vp_ctx* x, vp_chain** cs, int n, const TcChoice* force) {
     if (x->batch) {
         TcBatch* b = x->batch;
-        if ((int)b->chains.size() == n && std::equal(b->chains.begin(), b->chains.end(), cs)) return VP_OK;
+        if (!force && (int)b->chains.size() == n && std::equal(b->chains.begin(), b->chains.end(), cs)) return VP_OK;
         free_batch(x);
     }
     int rc = tc_operands(x);
@@ -1035,13 +1186,21 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
     b->G = (b->R + b->BN - 1) / b->BN;
     b->Rpad = b->G * b->BN;
     const TcOperands& t = x->tc;
-    const int64_t tiles = ((t.Npad + 128 * b->mt1 - 1) / (128 * b->mt1)) * b->G;
-    b->splits = tc_splits(tiles, x->nsm);
-    const int64_t kblocks = t.Apad / t.bk;
+    b->cfg = force ? *force : tuned_choice(x, b->R);
+    if (choice_error(x, b->Rpad, b->cfg)) {
+        if (force) { delete b; return VP_E_ARG; }
+        b->cfg = TcChoice{};
+    }
+    b->G1 = b->Rpad / b->cfg.bn1;
+    b->splits = b->cfg.splits > 0 ? b->cfg.splits : tc_splits(gemm1_tiles(x, b->Rpad, b->cfg), x->nsm);
+    const int64_t kblocks = t.Apad / b->cfg.bk1;
     b->splits = (int)std::min<int64_t>(b->splits, kblocks);
+    b->splits = (int)cdiv(kblocks, cdiv(kblocks, b->splits));   // splits that hold k-blocks
     Carve probe{nullptr};
     auto lay = [&](Carve& cv) {
         b->dchains = cv.take<DevChain>(n);
+        b->dptrs = cv.take<DevChain*>(n);
+        b->lnlrec = cv.take<double>((int64_t)n * 128);
         b->rowchain = cv.take<int32_t>(b->R);
         b->rowk = cv.take<int32_t>(b->R);
         b->row0 = cv.take<int32_t>(n);
@@ -1061,17 +1220,26 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n) {
     CK(cudaMemcpyAsync(b->rowk, rowk.data(), rowk.size() * 4, cudaMemcpyHostToDevice, x->stream));
     CK(cudaMemcpyAsync(b->row0, row0.data(), row0.size() * 4, cudaMemcpyHostToDevice, x->stream));
     // the batch's count contraction writes every chain's Ni inside NiAll
+    // (counts still pending are computed there below); the chains' device
+    // headers are updated by one upload and a scatter kernel
+    std::vector<DevChain> hc(n);
+    std::vector<DevChain*> hp(n);
     for (int i = 0; i < n; ++i) {
         vp_chain* c = cs[i];
         int32_t* dst = b->NiAll + (int64_t)row0[i] * x->KT;
-        CK(cudaMemcpyAsync(dst, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice, x->stream));
+        if (!c->counts_pending)
+            CK(cudaMemcpyAsync(dst, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice, x->stream));
         c->h.Ni = dst;
-        CK(cudaMemcpyAsync(c->d, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
-        CK(cudaMemcpyAsync(b->dchains + i, &c->h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
+        hc[i] = c->h;
+        hp[i] = c->d;
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     }
-    if ((rc = make_map(&b->mapWhi, b->Whi, b->Rpad, t.Apad, t.Apad, b->piece, t.bk)) ||
-        (rc = make_map(&b->mapWlo, b->Wlo, b->Rpad, t.Apad, t.Apad, b->piece, t.bk)) ||
+    CK(cudaMemcpyAsync(b->dchains, hc.data(), n * sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
+    CK(cudaMemcpyAsync(b->dptrs, hp.data(), n * sizeof(DevChain*), cudaMemcpyHostToDevice, x->stream));
+    LAUNCH(x, k_scatter_chains, (n, 128, 0, x->stream), (b->dchains, b->dptrs, n));
+    if ((rc = make_map(&b->mapC1, t.C, t.Npad, t.Apad, t.Apad, 128, b->cfg.bk1)) ||
+        (rc = make_map(&b->mapWhi, b->Whi, b->Rpad, t.Apad, t.Apad, b->cfg.piece1, b->cfg.bk1)) ||
+        (rc = make_map(&b->mapWlo, b->Wlo, b->Rpad, t.Apad, t.Apad, b->cfg.piece1, b->cfg.bk1)) ||
         (rc = make_map(&b->mapOH, b->OH, b->Rpad, t.Npad, t.Npad, b->piece, t.bk8, 1))) {
         x->batch = b;
         free_batch(x);
@@ -1113,13 +1281,8 @@ int launch_tc_sweep(vp_ctx* x) {
     LAUNCH(x, tc::k_update_p_tc, (dim3(upx, b->R, 1), 256, 0, s), (bd));
     // likelihood contraction: LL'[i, row] = sum_a C[i,a] (Whi + Wlo)[row, a]
     {
-        tc::GemmArgs g{};
-        g.M = x->N; g.N = b->Rpad; g.kblocks = (int)(t.Apad / t.bk);
-        g.kb_per_split = (g.kblocks + b->splits - 1) / b->splits;
-        g.BN = b->BN; g.piece = b->piece; g.nb = 2; g.mt = b->mt1; g.stages = b->st1; g.bk = t.bk; g.esz = 2; g.mode = 0;
-        g.out_f = b->LLpart; g.ldo = b->Rpad; g.err = t.err;
         prof_mark(x, true);
-        int rc = launch_gemm(x, t.mapC, b->mapWhi, b->mapWlo, g, dim3(cdiv(t.Npad, 128 * b->mt1), b->G, b->splits));
+        int rc = launch_gemm1(x, b->cfg, b->mapC1, b->mapWhi, b->mapWlo, b->splits, b->LLpart);
         prof_mark(x, false);
         if (rc) return rc;
     }
@@ -1129,7 +1292,7 @@ int launch_tc_sweep(vp_ctx* x) {
     if (int rc = launch_counts_gemm(x)) return rc;
     // Record for every chain, then m += 1
     unsigned ga = std::min<unsigned>(128, cdiv((int64_t)16 * x->KT, 256));
-    LAUNCH(x, k_record_sweep, (dim3(ga, 1, n), 256, 0, s), (b->dchains));
+    LAUNCH(x, k_record_sweep, (dim3(ga, 1, n), 256, 0, s), (b->dchains, b->lnlrec));
     return VP_OK;
 }
 
@@ -1141,17 +1304,17 @@ int launch_counts_gemm(vp_ctx* x) {
     {
         tc::GemmArgs g{};
         g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / t.bk8); g.kb_per_split = g.kblocks;
-        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.mt = b->mt2; g.stages = b->st2; g.bk = t.bk8; g.esz = 1; g.mode = 1;
-        g.out_i = b->NiAll; g.ldo = x->KT; g.err = t.err;
+        g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.mt = b->mt2; g.stages = b->cfg.st2; g.bk = t.bk8; g.esz = 1;
+        g.mode = 1; g.out_i = b->NiAll; g.ldo = x->KT; g.err = t.err;
         const unsigned mtiles = cdiv(t.Apad, 128 * b->mt2);
-        g.group_major = mtiles <= 65535;     // grid.y limit; otherwise row tiles on x
+        g.group_major = b->cfg.gm2 && mtiles <= 65535;     // grid.y limit; otherwise row tiles on x
         const dim3 grid = g.group_major ? dim3(b->G, mtiles, 1) : dim3(mtiles, b->G, 1);
         return launch_gemm(x, t.mapCT, b->mapOH, b->mapOH, g, grid);
     }
 }
 
 int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps) {
-    int rc = make_batch(x, cs, n);
+    int rc = make_batch(x, cs, n, nullptr);
     if (rc) return rc;
     TcBatch* b = x->batch;
     if (!b->graph) {
@@ -1178,6 +1341,213 @@ int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps) {
 }
 
 }  // namespace
+
+namespace {
+// mean device time of `iters` launches of fn after one untimed launch, on the
+// context's stream; a launch whose pipeline wait gave up marks the candidate
+// unusable (infinite time) and the flag is cleared
+template <class F>
+int time_candidate(vp_ctx* x, F fn, int iters, float* ms) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); vp_set_error("cudaEventCreate failed"); return VP_E_CUDA; }
+    int rc = fn();
+    if (!rc) {
+        cudaEventRecord(e0, x->stream);
+        for (int i = 0; i < iters && !rc; ++i) rc = fn();
+        cudaEventRecord(e1, x->stream);
+    }
+    const cudaError_t e = cudaStreamSynchronize(x->stream);
+    float t = 0.f;
+    if (!rc && e == cudaSuccess) cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) { vp_set_error("tuning launch failed: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+    if (rc) return rc;
+    int flag = 0;
+    CK(cudaMemcpy(&flag, x->tc.err, sizeof flag, cudaMemcpyDeviceToHost));
+    if (flag) {
+        CK(cudaMemset(x->tc.err, 0, sizeof flag));
+        *ms = INFINITY;
+        return VP_OK;
+    }
+    *ms = t / iters;
+    return VP_OK;
+}
+
+// split counts to try: the whole-wave rule's, then the best wave fill, each
+// a count whose splits all hold k-blocks
+std::vector<int> split_candidates(const vp_ctx* x, int64_t tiles, int64_t kblocks, int keep) {
+    auto norm = [&](int64_t s) { return (int)cdiv(kblocks, cdiv(kblocks, std::max<int64_t>(1, std::min(s, kblocks)))); };
+    std::vector<int> out{norm(tc_splits(tiles, x->nsm))};
+    std::vector<std::pair<double, int>> v;
+    for (int s = 1; s <= std::min<int64_t>(kMaxSplits, kblocks); ++s) {
+        if (norm(s) != s) continue;
+        const double w = (double)tiles * s / x->nsm;
+        v.push_back({-w / std::ceil(w), s});
+    }
+    std::sort(v.begin(), v.end());
+    for (const auto& e : v) {
+        if ((int)out.size() >= keep) break;
+        if (std::find(out.begin(), out.end(), e.second) == out.end()) out.push_back(e.second);
+    }
+    return out;
+}
+
+bool same_gemm1(const TcChoice& a, const TcChoice& b) {
+    return a.bk1 == b.bk1 && a.mt1 == b.mt1 && a.bn1 == b.bn1 && a.piece1 == b.piece1 && a.st1 == b.st1 &&
+           a.splits == b.splits && a.gm1 == b.gm1;
+}
+
+// times the current batch's contractions under candidate configurations
+// (effort 0: the current one; 1: its tile with every pipeline depth, split
+// count and CTA order; 2: every compiled tile as well) and returns the
+// fastest. The likelihood contraction writes a scratch buffer; the count
+// contraction recomputes the chains' counts from their labels, which leaves
+// them unchanged.
+int tune_batch(vp_ctx* x, int effort, TcChoice* best, vp_tc_config* info) {
+    TcBatch* b = x->batch;
+    const TcOperands& t = x->tc;
+    TcChoice cur = b->cfg;
+    cur.splits = b->splits;
+    std::vector<TcChoice> c1{cur};
+    for (const auto& tl : kTiles1) {
+        TcChoice c = cur;
+        c.bk1 = tl[0]; c.mt1 = tl[1]; c.bn1 = tl[2]; c.piece1 = tl[3];
+        const bool tile = c.bk1 == cur.bk1 && c.mt1 == cur.mt1 && c.bn1 == cur.bn1 && c.piece1 == cur.piece1;
+        if (effort == 0 || (effort < 2 && !tile) || b->Rpad % c.bn1) continue;
+        const std::vector<int> ss = split_candidates(x, gemm1_tiles(x, b->Rpad, c), t.Apad / c.bk1, 4);
+        for (int st = 2; st <= kMaxStages; ++st) {
+            if (tc::gemm_smem_bytes(c.bn1, 2, st, c.mt1, c.bk1, 2) > 227 * 1024) break;
+            for (int gm = 0; gm < 2; ++gm)
+                for (int sp : ss) {
+                    TcChoice d = c;
+                    d.st1 = st; d.gm1 = gm; d.splits = sp;
+                    bool dup = false;
+                    for (const auto& e : c1) dup |= same_gemm1(e, d);
+                    if (!dup) c1.push_back(d);
+                }
+        }
+    }
+    int smax = 1;
+    for (const auto& c : c1) smax = std::max(smax, c.splits);
+    void* scratch = nullptr;
+    cudaError_t e = dev_alloc(&scratch, (size_t)smax * x->N * b->Rpad * 4, x->device, x->stream);
+    if (e != cudaSuccess) { vp_set_error("tuning scratch: %s", cudaGetErrorString(e)); return VP_E_MEM; }
+    const int iters = effort ? 2 : 3;
+    float best1 = INFINITY;
+    TcChoice bc = cur;
+    int rc = VP_OK;
+    for (size_t i = 0; i < c1.size() && !rc; ++i) {
+        const TcChoice& c = c1[i];
+        CUtensorMap mA, mW0, mW1;
+        if ((rc = make_map(&mA, t.C, t.Npad, t.Apad, t.Apad, 128, c.bk1)) ||
+            (rc = make_map(&mW0, b->Whi, b->Rpad, t.Apad, t.Apad, c.piece1, c.bk1)) ||
+            (rc = make_map(&mW1, b->Wlo, b->Rpad, t.Apad, t.Apad, c.piece1, c.bk1)))
+            break;
+        float ms = 0.f;
+        rc = time_candidate(x, [&] { return launch_gemm1(x, c, mA, mW0, mW1, c.splits, (float*)scratch); }, iters, &ms);
+        if (rc) break;
+        // the label kernel reads every split's partial plane once
+        const float score = ms + (float)((double)c.splits * x->N * b->Rpad * 4 / 6.0e9);
+        if (i == 0) info->ms_likelihood_default = ms;
+        if (score < best1) { best1 = score; bc = c; info->ms_likelihood = ms; }
+    }
+    dev_free(scratch, x->stream);
+    if (rc) return rc;
+    // count contraction: pipeline depth and CTA order, on one-hot rows of the
+    // chains' current labels
+    {
+        tc::BatchDev bd = batch_dev(x);
+        LAUNCH(x, tc::k_onehot_from_z, (dim3(cdiv(x->N, 256), (unsigned)b->chains.size(), 1), 256, 0, x->stream), (bd));
+    }
+    const TcChoice save = b->cfg;
+    float best2 = INFINITY;
+    int bst2 = save.st2, bgm2 = save.gm2, ncand = (int)c1.size();
+    for (int pass = 0; pass < 2 && !rc; ++pass)
+        for (int st = 2; st <= kMaxStages && !rc; ++st) {
+            if (tc::gemm_smem_bytes(192, 1, st, 2, 128, 1) > 227 * 1024) break;
+            for (int gm = 0; gm < 2 && !rc; ++gm) {
+                const bool is_cur = st == save.st2 && gm == save.gm2;
+                if (pass == 0 ? !is_cur : (is_cur || effort == 0)) continue;   // the current one first
+                b->cfg.st2 = st;
+                b->cfg.gm2 = gm;
+                float ms = 0.f;
+                rc = time_candidate(x, [&] { return launch_counts_gemm(x); }, iters, &ms);
+                ++ncand;
+                if (rc) break;
+                if (pass == 0) info->ms_counts_default = ms;
+                if (ms < best2) { best2 = ms; bst2 = st; bgm2 = gm; info->ms_counts = ms; }
+            }
+        }
+    b->cfg = save;
+    if (rc) return rc;
+    *best = bc;
+    best->st2 = bst2;
+    best->gm2 = bgm2;
+    info->candidates = ncand;
+    return VP_OK;
+}
+
+void fill_config(const TcBatch* b, vp_tc_config* o) {
+    o->bk = b->cfg.bk1; o->row_tiles = b->cfg.mt1; o->cols = b->cfg.bn1; o->piece = b->cfg.piece1;
+    o->stages = b->cfg.st1; o->splits = b->splits; o->group_major = b->cfg.gm1;
+    o->count_stages = b->cfg.st2; o->count_group_major = b->cfg.gm2;
+}
+
+int tc_chain_set(vp_chain** cs, int32_t n, vp_ctx** out) {
+    if (!cs || n <= 0) { vp_set_error("no chains"); return VP_E_ARG; }
+    for (int i = 0; i < n; ++i) {
+        if (!cs[i] || cs[i]->ctx != cs[0]->ctx) { vp_set_error("the chains must share one context"); return VP_E_ARG; }
+        if (cs[i]->P.form != VP_FORM_TC) { vp_set_error("chain %d is not a tensor-core chain", i); return VP_E_ARG; }
+    }
+    *out = cs[0]->ctx;
+    return VP_OK;
+}
+}  // namespace
+
+extern "C" int vp_tune(vp_chain** cs, int32_t n, int32_t effort, vp_tc_config* out) {
+    vp_ctx* x = nullptr;
+    if (int rc = tc_chain_set(cs, n, &x)) return rc;
+    if (effort < 0 || effort > 2) { vp_set_error("effort must be 0, 1 or 2"); return VP_E_ARG; }
+    cudaSetDevice(x->device);
+    int rc = make_batch(x, cs, n, nullptr);
+    if (rc) return rc;
+    vp_tc_config info{};
+    TcChoice best;
+    if ((rc = tune_batch(x, effort, &best, &info))) return rc;
+    if (effort > 0) {
+        if ((rc = make_batch(x, cs, n, &best))) return rc;
+        tune_store(x, x->batch->R, best);
+    }
+    if (out) {
+        fill_config(x->batch, &info);
+        *out = info;
+    }
+    return VP_OK;
+}
+
+extern "C" int vp_tc_configure(vp_chain** cs, int32_t n, const vp_tc_config* cfg) {
+    vp_ctx* x = nullptr;
+    if (int rc = tc_chain_set(cs, n, &x)) return rc;
+    if (!cfg) { vp_set_error("null configuration"); return VP_E_ARG; }
+    cudaSetDevice(x->device);
+    TcChoice c;
+    c.bk1 = cfg->bk; c.mt1 = cfg->row_tiles; c.bn1 = cfg->cols; c.piece1 = cfg->piece; c.st1 = cfg->stages;
+    c.splits = cfg->splits; c.gm1 = cfg->group_major; c.st2 = cfg->count_stages; c.gm2 = cfg->count_group_major;
+    return make_batch(x, cs, n, &c);
+}
+
+extern "C" int vp_tc_config_get(vp_chain** cs, int32_t n, vp_tc_config* out) {
+    vp_ctx* x = nullptr;
+    if (int rc = tc_chain_set(cs, n, &x)) return rc;
+    if (!out) { vp_set_error("null output"); return VP_E_ARG; }
+    cudaSetDevice(x->device);
+    if (int rc = make_batch(x, cs, n, nullptr)) return rc;
+    *out = vp_tc_config{};
+    fill_config(x->batch, out);
+    return VP_OK;
+}
 
 extern "C" int vp_tc_status(vp_ctx* x) {
     if (!x) { vp_set_error("null context"); return VP_E_ARG; }

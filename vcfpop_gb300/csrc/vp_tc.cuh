@@ -304,41 +304,102 @@ namespace tc {
 // CT [Apad][Npad]: the transpose (alleles x individuals) as e4m3 bytes
 // Missing calls and the padding are zero. 0, 1 and 2 are exact in both types.
 constexpr uint8_t E4M3_ONE = 0x38, E4M3_TWO = 0x40;
-// one CTA = a tile of 64 loci x 64 individuals: the 2-bit codes are decoded
-// into shared memory, then written as contiguous rows of both layouts
-__global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bfloat16* C, uint8_t* CT,
-                                                      int64_t Apad, int64_t Npad) {
-    __shared__ uint8_t code[64][64 + 4];   // [locus][individual]
-    const int i0 = blockIdx.x * 64;
-    const int64_t l0 = (int64_t)blockIdx.y * 64;
-    for (int j = threadIdx.x; j < 64 * 4; j += blockDim.x) {
-        const int ll = j >> 2, w = j & 3;
-        const int64_t l = l0 + ll;
-        const int wi = (i0 >> 4) + w;
-        uint32_t word = (l < D.L && wi < D.Nw) ? D.g2[l * D.Nw + wi] : 0xFFFFFFFFu;
-        for (int b = 0; b < 16; ++b) {
-            const int i = i0 + w * 16 + b;
-            code[ll][w * 16 + b] = (i < D.N) ? (uint8_t)((word >> (2 * b)) & 3) : 3;
+// One CTA = 128 individuals x BUILD_TILES tiles of 64 loci. Per tile the
+// 2-bit codes are decoded into shared memory and written as whole 128-byte
+// lines of both layouts: CT rows (allele 2l+a, 128 individuals as e4m3
+// bytes) and C rows (individual i, 64 loci x 2 alleles as bf16). The grid
+// covers [Npad] x [Apad] entirely (padding individuals and loci are written
+// as zeros), so the operands need no clearing beforehand. The same pass adds
+// the centring constant's share of its loci, B_i += sum over non-missing
+// calls of 2 ln pbar_0 + c (ln pbar_1 - ln pbar_0) (c copies of allele 1), per
+// thread in FP32; the CTA's sums go to part[blockIdx.y][i] and k_center_sum
+// adds them in FP64 in a fixed order.
+constexpr int BUILD_TILES = 8;
+__global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bfloat16* C, uint8_t* CT, int64_t Apad,
+                                                      int64_t Npad, const float* logpbar, float* part) {
+    __shared__ __align__(16) uint8_t code[64][128 + 16];   // [locus][individual]; 3 = missing or padding
+    const int t = threadIdx.x;
+    const int i0 = blockIdx.x * 128;
+    const int seg = t & 15;          // C pieces: 8 columns = 4 loci x 2 alleles
+    float acc[8];                    // B_i shares of rows (t >> 4) + 16 p
+#pragma unroll
+    for (int p = 0; p < 8; ++p) acc[p] = 0.f;
+    for (int tile = 0; tile < BUILD_TILES; ++tile) {
+        const int64_t l0 = ((int64_t)blockIdx.y * BUILD_TILES + tile) * 64;
+        if (2 * l0 >= Apad) break;
+        __syncthreads();
+        for (int j = t; j < 64 * 8; j += 256) {
+            const int ll = j >> 3, w = j & 7;
+            const int64_t l = l0 + ll;
+            const int wi = (i0 >> 4) + w;
+            const uint32_t word = (l < D.L && wi < D.Nw) ? D.g2[l * D.Nw + wi] : 0xFFFFFFFFu;
+            uint32_t q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                uint32_t v = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const int bb = u * 4 + b, i = i0 + w * 16 + bb;
+                    v |= (i < D.N ? (word >> (2 * bb)) & 3u : 3u) << (8 * b);
+                }
+                q[u] = v;
+            }
+            *reinterpret_cast<uint4*>(&code[ll][w * 16]) = make_uint4(q[0], q[1], q[2], q[3]);
+        }
+        __syncthreads();
+        // CT rows 2l+a: eight 16-byte pieces per row
+        for (int j = t; j < 128 * 8; j += 256) {
+            const int ra = j >> 3, pc = j & 7, ll = ra >> 1, a = ra & 1;
+            const int64_t row = 2 * (l0 + ll) + a;
+            if (row >= Apad) continue;
+            const uint4 cw = *reinterpret_cast<const uint4*>(&code[ll][pc * 16]);
+            const uint32_t in[4] = {cw.x, cw.y, cw.z, cw.w};
+            // code c -> e4m3 copies of allele a: byte permutation tables
+            // (allele 1: c; allele 0: 2 - c; missing: 0)
+            const uint32_t lut = a ? 0x00403800u : 0x00003840u;
+            uint32_t o[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t v = in[u];
+                const uint32_t sel = (v & 0xFu) | ((v >> 4) & 0xF0u) | ((v >> 8) & 0xF00u) | ((v >> 12) & 0xF000u);
+                o[u] = __byte_perm(lut, 0u, sel);
+            }
+            *reinterpret_cast<uint4*>(CT + row * Npad + i0 + pc * 16) = make_uint4(o[0], o[1], o[2], o[3]);
+        }
+        // C rows: sixteen 16-byte pieces per row; this thread's column piece
+        // is fixed (seg), its rows are (t >> 4) + 16 p
+        const int64_t col = 2 * l0 + seg * 8;
+        if (col < Apad) {
+            float base[4], dif[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t l = l0 + seg * 4 + u;
+                const float p0 = l < D.L ? logpbar[2 * l] : 0.f, p1 = l < D.L ? logpbar[2 * l + 1] : 0.f;
+                base[u] = 2.f * p0;
+                dif[u] = p1 - p0;
+            }
+#pragma unroll
+            for (int p = 0; p < 8; ++p) {
+                const int ii = (t >> 4) + 16 * p;
+                uint32_t w[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t c = code[seg * 4 + u][ii];
+                    // bf16 pairs (allele 0 low, allele 1 high) of (2-c, c); missing 0
+                    w[u] = c == 0u ? 0x00004000u : c == 1u ? 0x3F803F80u : c == 2u ? 0x40000000u : 0u;
+                    if (c != 3u) acc[p] += fmaf((float)c, dif[u], base[u]);
+                }
+                *reinterpret_cast<uint4*>(C + (int64_t)(i0 + ii) * Apad + col) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
         }
     }
-    __syncthreads();
-    // CT rows: allele 2l+a, 64 individuals
-    for (int j = threadIdx.x; j < 128 * 64; j += blockDim.x) {
-        const int ii = j & 63, ra = j >> 6, ll = ra >> 1, a = ra & 1;
-        const int64_t l = l0 + ll;
-        if (l >= D.L) continue;
-        const int c = code[ll][ii];
-        const int v = c == 3 ? 0 : (a ? c : 2 - c);
-        CT[(2 * l + a) * Npad + i0 + ii] = v == 0 ? 0 : v == 1 ? E4M3_ONE : E4M3_TWO;
-    }
-    // C rows: individual i, alleles 2*l0 .. 2*l0+127
-    for (int j = threadIdx.x; j < 64 * 128; j += blockDim.x) {
-        const int col = j & 127, ii = j >> 7, ll = col >> 1, a = col & 1;
-        const int64_t l = l0 + ll;
-        if (l >= D.L) continue;
-        const int c = code[ll][ii];
-        const float v = c == 3 ? 0.f : (a ? (float)c : 2.f - c);
-        C[(int64_t)(i0 + ii) * Apad + 2 * l + a] = __float2bfloat16(v);
+    // the 16 column pieces of a row sit in 16 consecutive lanes
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        float v = acc[p];
+        for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        const int i = i0 + (t >> 4) + 16 * p;
+        if (seg == 0 && i < D.N) part[(int64_t)blockIdx.y * Npad + i] = v;
     }
 }
 
@@ -367,34 +428,14 @@ __global__ void k_allele_center(const DevData D, float* logpbar) {
     logpbar[2 * l] = logf((float)(t - n1 + 1) / (float)(t + 2));
     logpbar[2 * l + 1] = logf((float)(n1 + 1) / (float)(t + 2));
 }
-// B[i] = sum_a C[i][a] ln pbar_a: one warp per individual over its contiguous
-// bf16 count row (8 values per 16-byte load), Kahan sums per lane, FP64
-// across lanes
-__global__ void k_center_const(const DevData D, const __nv_bfloat16* C, int64_t Apad, const float* logpbar,
-                               double* Bc) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= D.N) return;
-    const uint4* row = reinterpret_cast<const uint4*>(C + (int64_t)warp * Apad);
-    const int64_t n8 = Apad / 8;
-    float s = 0.f, cmp = 0.f;
-    for (int64_t j = lane; j < n8; j += 32) {
-        const uint4 v = row[j];
-        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-        float acc = 0.f;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float c0 = __uint_as_float(w[q] << 16), c1 = __uint_as_float(w[q] & 0xFFFF0000u);
-            const int64_t a = j * 8 + 2 * q;
-            if (c0 != 0.f) acc += c0 * logpbar[a];
-            if (c1 != 0.f) acc += c1 * logpbar[a + 1];
-        }
-        const float y = acc - cmp, t = s + y;
-        cmp = (t - s) - y;
-        s = t;
-    }
-    double d = (double)s - (double)cmp;
-    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if (lane == 0) Bc[warp] = d;
+// B[i] = sum_a C[i][a] ln pbar_a: the locus groups' FP32 shares written by
+// k_build_counts, added in FP64 in group order (deterministic)
+__global__ void k_center_sum(const DevData D, const float* part, int groups, int64_t Npad, double* Bc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.N) return;
+    double t = 0.0;
+    for (int r = 0; r < groups; ++r) t += (double)part[(int64_t)r * Npad + i];
+    Bc[i] = t;
 }
 
 struct BatchDev {
@@ -440,7 +481,7 @@ __global__ void __launch_bounds__(256) k_update_p_tc(BatchDev b) {
         ph.dirichlet2(lam + (float)n.x, lam + (float)n.y, p0, p1);
         F2[l] = make_float2(p0, p1);
         const float2 lb = lpb[l];
-        const float w0 = ln_freq_fast(p0) - lb.x, w1 = ln_freq_fast(p1) - lb.y;
+        const float w0 = ln_freq(p0) - lb.x, w1 = ln_freq(p1) - lb.y;
         const __nv_bfloat16 h0 = __float2bfloat16(w0), h1 = __float2bfloat16(w1);
         Whi[l] = __halves2bfloat162(h0, h1);
         Wlo[l] = __halves2bfloat162(__float2bfloat16(w0 - __bfloat162float(h0)), __float2bfloat16(w1 - __bfloat162float(h1)));

@@ -332,6 +332,34 @@ def finish(chains: list[Chain]) -> None:
     B.check(B.lib().vp_finish(arr, len(chains)))
 
 
+def _chain_array(chains):
+    return (C.c_void_p * len(chains))(*[c.h for c in chains])
+
+
+def tune(chains: list[Chain], effort: int = 1) -> dict:
+    """Autotune the batched sweep of these tensor-core chains (vp_tune): the
+    chosen launch configuration and the device times before and after."""
+    cfg = B.VpTcConfig()
+    B.check(B.lib().vp_tune(_chain_array(chains), len(chains), effort, C.byref(cfg)))
+    return cfg.as_dict()
+
+
+def tc_configure(chains: list[Chain], **kw) -> None:
+    """Set the batch's launch configuration (vp_tc_configure); unnamed fields
+    keep their current values."""
+    cfg = B.VpTcConfig()
+    B.check(B.lib().vp_tc_config_get(_chain_array(chains), len(chains), C.byref(cfg)))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    B.check(B.lib().vp_tc_configure(_chain_array(chains), len(chains), C.byref(cfg)))
+
+
+def tc_config(chains: list[Chain]) -> dict:
+    cfg = B.VpTcConfig()
+    B.check(B.lib().vp_tc_config_get(_chain_array(chains), len(chains), C.byref(cfg)))
+    return cfg.as_dict()
+
+
 def run_chains(chains: list[Chain], nsweeps: int | None = None) -> None:
     """Advance chains that share a context together (shared launches, one graph)."""
     arr = (C.c_void_p * len(chains))(*[c.h for c in chains])
