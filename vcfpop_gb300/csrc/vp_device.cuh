@@ -212,7 +212,8 @@ struct Philox {
         return r;
     }
     // uniform in (0, 1]
-    __device__ inline float uniformf() { return ((float)(next() >> 8) + 1.0f) * (1.0f / 16777216.0f); }
+    __device__ static inline float to_uniformf(uint32_t x) { return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f); }
+    __device__ inline float uniformf() { return to_uniformf(next()); }
     __device__ inline double uniformd() {
         uint64_t h = next(), l = next();
         return ((double)(((h << 32) | l) >> 11) + 1.0) * (1.0 / 9007199254740992.0);

@@ -54,7 +54,7 @@ struct DevChain {
 
 // step ids folded into Philox counters
 enum : uint32_t { ST_INITZ = 1, ST_P = 2, ST_Q = 3, ST_METRO_P = 4, ST_METRO_A = 5, ST_Z = 6, ST_A = 7, ST_INITADM = 8,
-                  ST_ALPHA = 9 };
+                  ST_ALPHA = 9, ST_ZSLICE = 10 };
 
 __device__ __forceinline__ bool binaryq_at(const DevChain& c, int m) { return !c.admix && m >= c.nadmburnin; }
 __device__ __forceinline__ bool metro_turn(const DevChain& c, int m) { return c.admix && c.metrofreq > 0 && m % c.metrofreq == 0; }
@@ -840,6 +840,11 @@ __global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
 // faster there than grouping lanes with __match_any_sync). The slice
 // histogram is flushed to Ni with one global atomic per non-zero entry. KM is
 // the cluster count rounded up to a compiled size; EXACT means K == KM.
+// Uniforms: one Philox stream per (individual, slice of ZA_LC loci); every
+// locus takes vmax consecutive draws, used or not, so a block of four serves
+// two diploid loci and a missing call shifts nothing.
+// Record's likelihood, the sum of ln(sum_k q_k p) over copies, is formed only
+// on sweeps that Record reads (thinning points) or when the step is forced.
 constexpr int ZA_WARPS = 8;
 constexpr int ZA_LC = 16;
 constexpr int ZA_PACKED = 40;
@@ -865,6 +870,7 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
     for (int k = 0; k < KM; ++k) { q[k] = (live && (EXACT || k < K)) ? c.Q[(int64_t)i * K + k] : 0.f; mi[k] = 0; }
     const int64_t lb0 = (int64_t)blockIdx.y * c.zadm_lc, lb1 = min(D.L, lb0 + c.zadm_lc);
     float ls = 0.f, lc = 0.f;  // Kahan sum of ln(sum_k q_k p)
+    const bool rec = force || record_at(c, m);
     for (int64_t l0 = lb0; l0 < lb1; l0 += ZA_LC) {
         const int nl = (int)min((int64_t)ZA_LC, lb1 - l0);
         __syncthreads();
@@ -876,16 +882,17 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
         }
         for (int j = threadIdx.x; j < ZA_LC * K * MK; j += blockDim.x) hs[j] = 0;
         __syncthreads();
+        Philox ph;
+        ph.init(c.seed, ST_ZSLICE | ((uint32_t)m << 4), (uint32_t)(l0 / ZA_LC), (uint32_t)i);
         for (int ll = 0; ll < nl; ++ll) {
             const int64_t l = l0 + ll;
             Copies cp;
             if (live) load_copies(D, l, i, cp); else cp.n = 0;
-            Philox ph;
-            ph.init(c.seed, ST_Z | ((uint32_t)m << 4), (uint32_t)l, (uint32_t)i);
             float lacc = 0.f;
             int32_t* hl = hs + ll * nbins;
             for (int a = 0; a < D.vmax; ++a) {
                 const bool act = a < cp.n;
+                const float u = ph.uniformf();
                 int key = -1;
                 if (act) {
                     const int al = cp.a[a];
@@ -894,9 +901,9 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
 #pragma unroll
                     for (int k = 0; k < KM; ++k)
                         if (EXACT || k < K) sx += q[k] * f[k];
-                    lacc += logf(sx);
+                    if (rec) lacc += logf(sx);
                     // Poly (src/statistics.cpp:357-385) on the same float weights
-                    float t = ph.uniformf() * (sx + (float)(VP_MIN_FREQ * K));
+                    float t = u * (sx + (float)(VP_MIN_FREQ * K));
                     int k2 = K - 1;
                     bool found = false;
 #pragma unroll
