@@ -864,6 +864,8 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * (ZA_WARPS * 32) + threadIdx.x;
     const bool live = i < D.N;
+    constexpr int NPK = (KM + 7) / 8;
+    static_assert(ZA_LC * 10 < 256, "8-bit label counts per slice");
     float q[KM];
     int32_t mi[KM];
 #pragma unroll
@@ -884,6 +886,9 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
         __syncthreads();
         Philox ph;
         ph.init(c.seed, ST_ZSLICE | ((uint32_t)m << 4), (uint32_t)(l0 / ZA_LC), (uint32_t)i);
+        uint64_t pk[NPK];
+#pragma unroll
+        for (int w = 0; w < NPK; ++w) pk[w] = 0;
         for (int ll = 0; ll < nl; ++ll) {
             const int64_t l = l0 + ll;
             Copies cp;
@@ -897,10 +902,12 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
                 if (act) {
                     const int al = cp.a[a];
                     const float* f = sF + (ll * MK + al) * KPAD;
-                    float sx = 0.f;
+                    float sx = 0.f, pq[KM];
 #pragma unroll
-                    for (int k = 0; k < KM; ++k)
-                        if (EXACT || k < K) sx += q[k] * f[k];
+                    for (int k = 0; k < KM; ++k) {
+                        pq[k] = (EXACT || k < K) ? q[k] * f[k] : 0.f;
+                        sx += pq[k];
+                    }
                     if (rec) lacc += logf(sx);
                     // Poly (src/statistics.cpp:357-385) on the same float weights
                     float t = u * (sx + (float)(VP_MIN_FREQ * K));
@@ -909,13 +916,16 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
 #pragma unroll
                     for (int k = 0; k < KM; ++k) {
                         if ((EXACT || k < K) && !found) {
-                            const float w = q[k] * f[k] + (float)VP_MIN_FREQ;
+                            const float w = pq[k] + (float)VP_MIN_FREQ;
                             if (t < w) { k2 = k; found = true; }
                             else t -= w;
                         }
                     }
+                    // this slice's label counts, 8 bits per cluster (at most
+                    // ZA_LC x 10 copies per slice)
 #pragma unroll
-                    for (int k = 0; k < KM; ++k) mi[k] += (k == k2);
+                    for (int w = 0; w < NPK; ++w)
+                        if (w == (k2 >> 3)) pk[w] += 1ull << (8 * (k2 & 7));
                     key = k2 * MK + al;
                 }
                 if (packed) {
@@ -940,6 +950,8 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
             lc = (tt - ls) - y;
             ls = tt;
         }
+#pragma unroll
+        for (int k = 0; k < KM; ++k) mi[k] += (int32_t)((pk[k >> 3] >> (8 * (k & 7))) & 0xFFu);
         __syncthreads();
         for (int j = threadIdx.x; j < ZA_LC * K * MK; j += blockDim.x) {
             int v = hs[j];
