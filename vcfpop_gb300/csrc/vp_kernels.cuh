@@ -15,6 +15,7 @@ constexpr int SUB = 32;         // loci per FP32 sub-sum before folding into FP6
 
 struct DevData {
     int32_t N, S, vmax, maxploidy, maxK, Nw, packed2;
+    int32_t popcontig;    // every population's individuals are consecutive
     int64_t L, KT, coprime;
     const uint32_t* g2;   // [L][Nw]
     const uint8_t* gb;    // [L][N][vmax]
@@ -1031,6 +1032,24 @@ __global__ void k_logprod_q(const DevChain* chains) {
         }
         return;
     }
+    if (mode == 2 && D.popcontig) {
+        // counter streams, one sequence per (location, cluster) over the
+        // location's consecutive rows: one block per location, one block sum
+        // per cluster (deterministic)
+        for (int sp = blockIdx.x; sp < D.S; sp += gridDim.x) {
+            const int64_t r0 = D.pop_ind0[sp], n = D.pop_nind[sp];
+            for (int k = 0; k < K; ++k) {
+                double v = 0;
+                for (int64_t rr = threadIdx.x; rr < n; rr += blockDim.x) {
+                    const float q = c.Q[(r0 + rr) * K + k];
+                    v += q > 0.f ? (double)logf(q) : -709.0895657128241;
+                }
+                v = block_sum(v, sh);
+                if (threadIdx.x == 0) c.red[sp * K + k] = v;
+            }
+        }
+        return;
+    }
     // counter streams: sum of ln Q per sequence, per-block partials reduced by
     // the last block in a fixed order
     double* part = c.red + (D.S * K + K + 1);   // [LPQ_BLOCKS][nseq]
@@ -1060,48 +1079,70 @@ __global__ void k_logprod_q(const DevChain* chains) {
 
 // UpdateAlpha (src/structure.cpp:1499-1594), reference stream
 // RNG(seed + m, SALT_UPDATEALPHA), on one thread
-// counter streams, location prior with admixture: the K global steps on one
-// thread, then the local steps with one thread per location (a location's K
-// steps stay in order: they share its SumAlpha), each location on its own
-// Philox stream
+// counter streams, location prior with admixture. The K global steps are
+// independent of one another (each moves Alpha[k] against AlphaLocal[., k]):
+// one thread per cluster, each on its own Philox stream. A location's K
+// local steps share its SumAlpha and stay in order on one thread, but every
+// term that does not involve SumAlpha (the proposal on its own Philox
+// stream, ln(am/ao), lgamma(am), lgamma(ao), the ln Q sum) is formed first by
+// one thread per (location, cluster); the ordered pass then adds the two
+// SumAlpha lgamma terms and decides. Needs blockDim.x >= K.
 __device__ void update_alpha_locprior_ctr(const DevChain& c, int m) {
     const DevData& D = c.D;
     const int K = c.K, S = D.S;
     const double r = c.ctl->r;
-    if (threadIdx.x == 0) {
+    const int t = threadIdx.x;
+    if (t < K) {
+        const int k = t;
         Philox ph;
-        ph.init(c.seed, ST_ALPHA | ((uint32_t)m << 4), 0xFFFFFFFFu, 0);
-        for (int k = 0; k < K; ++k) {
-            double am = c.Alpha[k] + c.stdalpha * ph.normald();
-            if (am > 0 && am < c.maxalpha) {
-                double d = am - c.Alpha[k];
-                double dlnL = S * (d * r * ref_mylog(r) + lgamma(r * c.Alpha[k]) - lgamma(r * am));
-                double lp = 0;   // ln of the product over locations of AlphaLocal[., k]
-                for (int sl = 0; sl < S; ++sl) lp += ref_mylog(c.AlphaLocal[sl * K + k]);
-                dlnL += r * d * lp;
-                if (dlnL >= VP_NZERO || ph.uniformd() < exp(dlnL)) c.Alpha[k] = am;
-            }
+        ph.init(c.seed, ST_ALPHA | ((uint32_t)m << 4), 0xFFFFFFFFu, 2u + (uint32_t)k);
+        const double a0 = c.Alpha[k], am = a0 + c.stdalpha * ph.normald();
+        if (am > 0 && am < c.maxalpha) {
+            const double d = am - a0;
+            double dlnL = S * (d * r * ref_mylog(r) + lgamma(r * a0) - lgamma(r * am));
+            double lp = 0;   // ln of the product over locations of AlphaLocal[., k]
+            for (int sl = 0; sl < S; ++sl) lp += ref_mylog(c.AlphaLocal[sl * K + k]);
+            dlnL += r * d * lp;
+            if (dlnL >= VP_NZERO || ph.uniformd() < exp(dlnL)) c.Alpha[k] = am;
         }
     }
     __syncthreads();
-    for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    // proposals and the SumAlpha-free part of each local log ratio, [S][K] x
+    // (proposal, partial ratio, uniform), in the region of c.red that holds
+    // k_logprod_q's block partials (reduced before this kernel runs)
+    double* pre = c.red + ((int64_t)S * K + K + 1);
+    for (int j = t; j < S * K; j += blockDim.x) {
+        const int s = j / K, k = j % K;
         Philox ph;
-        ph.init(c.seed, ST_ALPHA | ((uint32_t)m << 4), (uint32_t)s, 1);
+        ph.init(c.seed, ST_ALPHA | ((uint32_t)m << 4), (uint32_t)s, 2u + (uint32_t)k);
+        const double ao = c.AlphaLocal[j], am = ao + c.stdalpha * ph.normald();
+        const double u = ph.uniformd();
+        double part = 0.0;
+        if (am > 0 && am < c.maxalpha) {
+            const double d = am - ao;
+            part = (r * c.Alpha[k] - 1) * ref_mylog(am / ao) - d * r + D.pop_nind[s] * (lgamma(ao) - lgamma(am)) +
+                   d * c.red[j];
+        }
+        pre[3 * (int64_t)j] = am;
+        pre[3 * (int64_t)j + 1] = part;
+        pre[3 * (int64_t)j + 2] = u;
+    }
+    __syncthreads();
+    for (int s = t; s < S; s += blockDim.x) {
         if (m % 10 == 0) {
-            double t = 0;
-            for (int k = 0; k < K; ++k) t += c.AlphaLocal[s * K + k];
-            c.SumAlpha[s] = t;
+            double tt = 0;
+            for (int k = 0; k < K; ++k) tt += c.AlphaLocal[s * K + k];
+            c.SumAlpha[s] = tt;
         }
         const int snind = D.pop_nind[s];
         for (int k = 0; k < K; ++k) {
-            double ao = c.AlphaLocal[s * K + k], am = ao + c.stdalpha * ph.normald();
+            const int64_t j = (int64_t)s * K + k;
+            const double ao = c.AlphaLocal[j], am = pre[3 * j];
             if (am > 0 && am < c.maxalpha) {
-                double d = am - ao;
-                double dlnL = (r * c.Alpha[k] - 1) * ref_mylog(am / ao) - d * r +
-                              snind * (lgamma(c.SumAlpha[s] + d) - lgamma(am) - lgamma(c.SumAlpha[s]) + lgamma(ao));
-                dlnL += d * c.red[s * K + k];
-                if (dlnL >= VP_NZERO || ph.uniformd() < exp(dlnL)) {
-                    c.AlphaLocal[s * K + k] = am;
+                const double d = am - ao;
+                const double dlnL = pre[3 * j + 1] + snind * (lgamma(c.SumAlpha[s] + d) - lgamma(c.SumAlpha[s]));
+                if (dlnL >= VP_NZERO || pre[3 * j + 2] < exp(dlnL)) {
+                    c.AlphaLocal[j] = am;
                     c.SumAlpha[s] += d;
                 }
             }

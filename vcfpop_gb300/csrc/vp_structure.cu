@@ -390,6 +390,10 @@ extern "C" int vp_open(const vp_dataset* ds, int device, vp_ctx** out) {
     DevData& D = x->D;
     D.N = ds->N; D.S = ds->S; D.vmax = ds->vmax; D.maxploidy = ds->maxploidy; D.maxK = ds->maxK; D.Nw = ds->Nw;
     D.packed2 = ds->packed2; D.L = ds->L; D.KT = ds->KT; D.coprime = ds->coprime;
+    D.popcontig = 1;
+    for (int32_t sp = 0; sp < ds->S; ++sp)
+        for (int32_t j = 0; j < ds->pop_nind[sp]; ++j)
+            if (ds->popid[ds->pop_ind0[sp] + j] != sp) { D.popcontig = 0; break; }
     int rc = 0;
     if (ds->packed2) rc |= upload(x, ds->g2.data(), ds->g2.size(), &D.g2);
     else rc |= upload(x, ds->gb.data(), ds->gb.size(), &D.gb);
