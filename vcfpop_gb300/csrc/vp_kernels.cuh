@@ -708,38 +708,17 @@ __global__ void k_metro_propose(const DevChain* chains, int force) {
     }
 }
 
-// log likelihood ratio of the proposals: sum over loci and copies of
-// ln( sum_k q'_k p / sum_k q_k p ), one thread per individual
-__global__ void __launch_bounds__(LL_BLOCK) k_metro_ratio(const DevChain* chains, int force) {
-    const DevChain& c = chains[blockIdx.z];
-    const DevData& D = c.D;
-    const int K = c.K, m = c.ctl->m;
-    if (!force && !metro_turn(c, m)) return;
-    const int i = blockIdx.x * LL_BLOCK + threadIdx.x;
-    const int64_t l0 = (int64_t)blockIdx.y * c.lchunk, l1 = min(D.L, l0 + c.lchunk);
-    if (i >= D.N || l0 >= D.L) return;
-    float q1[64], q0[64];
-    for (int k = 0; k < K; ++k) { q1[k] = c.Qprop[(int64_t)i * K + k]; q0[k] = c.Q[(int64_t)i * K + k]; }
-    double accd = 0;
-    float acc = 0.f;
-    int cnt = 0;
-    for (int64_t l = l0; l < l1; ++l) {
-        Copies cp;
-        load_copies(D, l, i, cp);
-        const float* p = c.Freq + D.off[l];
-        for (int a = 0; a < cp.n; ++a) {
-            float s1 = 0.f, s2 = 0.f;
-            for (int k = 0; k < K; ++k) {
-                float pk = p[(int64_t)k * D.KT + cp.a[a]];
-                s1 += q1[k] * pk;
-                s2 += q0[k] * pk;
-            }
-            acc += logf(s1 / s2);
-        }
-        if (++cnt == SUB) { cnt = 0; accd += acc; acc = 0.f; }
-    }
-    c.metrop[(int64_t)blockIdx.y * D.N + i] = accd + (double)acc;
-}
+// log likelihood ratio of the proposals (UpdateQMetro, src/structure.cpp:
+// 1006-1086): the sum over loci and copies of ln( sum_k q'_k p / sum_k q_k p ).
+// Warp = 32 individuals (one per lane), CTA = 8 warps; grid.y = the locus
+// chunks whose partials k_metro_accept adds. A CTA stages each slice of
+// ZA_LC loci's frequencies in shared memory ([ZA_LC][MK][KPAD], odd stride)
+// and keeps Q and Q' rows in registers (K <= KM; EXACT: K == KM). FP32 sums
+// over SUB loci fold into FP64 (the same operations in the same order for
+// every K). Defined after the per-copy label kernel, whose slice constants it
+// shares.
+template <int KM, bool EXACT>
+__global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int force);
 
 __global__ void k_metro_accept(const DevChain* chains, int force) {
     const DevChain& c = chains[blockIdx.z];
@@ -967,6 +946,58 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
             if ((EXACT || k < K) && mi[k]) atomicAdd(&c.Mi[(int64_t)i * K + k], mi[k]);
     double t = block_sum((double)ls - (double)lc, sh);
     if (threadIdx.x == 0) c.lnlp[blockIdx.y * gridDim.x + blockIdx.x] = t;
+}
+
+template <int KM, bool EXACT>
+__global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int force) {
+    extern __shared__ unsigned char smraw[];
+    const DevChain& c = chains[blockIdx.z];
+    const DevData& D = c.D;
+    const int K = EXACT ? KM : c.K, m = c.ctl->m, MK = D.maxK;
+    if (!force && !metro_turn(c, m)) return;
+    const int KPAD = K | 1;
+    float* sF = reinterpret_cast<float*>(smraw);   // [ZA_LC][MK][KPAD]
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < D.N;
+    float q1[KM], q0[KM];
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+        const bool on = live && (EXACT || k < K);
+        q1[k] = on ? c.Qprop[(int64_t)i * K + k] : 0.f;
+        q0[k] = on ? c.Q[(int64_t)i * K + k] : 0.f;
+    }
+    const int64_t lc0 = (int64_t)blockIdx.y * c.lchunk, lc1 = min(D.L, lc0 + c.lchunk);
+    double accd = 0;
+    float acc = 0.f;
+    int cnt = 0;
+    for (int64_t l0 = lc0; l0 < lc1; l0 += ZA_LC) {
+        const int nl = (int)min((int64_t)ZA_LC, lc1 - l0);
+        __syncthreads();
+        for (int j = threadIdx.x; j < ZA_LC * MK * KPAD; j += blockDim.x) {
+            const int k = j % KPAD, a = (j / KPAD) % MK, ll = j / (KPAD * MK);
+            float v = 0.f;
+            if (ll < nl && k < K && a < D.k[l0 + ll]) v = __ldg(c.Freq + (int64_t)k * D.KT + D.off[l0 + ll] + a);
+            sF[j] = v;
+        }
+        __syncthreads();
+        for (int ll = 0; ll < nl; ++ll) {
+            Copies cp;
+            if (live) load_copies(D, l0 + ll, i, cp); else cp.n = 0;
+            for (int a = 0; a < cp.n; ++a) {
+                const float* f = sF + (ll * MK + cp.a[a]) * KPAD;
+                float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+                for (int k = 0; k < KM; ++k)
+                    if (EXACT || k < K) {
+                        s1 += q1[k] * f[k];
+                        s2 += q0[k] * f[k];
+                    }
+                acc += logf(s1 / s2);
+            }
+            if (++cnt == SUB) { cnt = 0; accd += acc; acc = 0.f; }
+        }
+    }
+    if (live) c.metrop[(int64_t)blockIdx.y * D.N + i] = accd + (double)acc;
 }
 
 // ---------------------------------------------------------------------------

@@ -250,6 +250,24 @@ int launch_zadm_ctr(vp_chain* c, int force) {
     return VP_E_ARG;
 }
 
+// the Metropolis ratio kernel on the same K instantiations as the label kernel
+int launch_metro_ratio(vp_chain* c, int force) {
+    vp_ctx* x = c->ctx;
+    const dim3 g(cdiv(x->N, 256), c->h.nchunk, 1);
+    const size_t sm = (size_t)ZA_LC * x->maxK * (c->P.K | 1) * 4;
+    const int K = c->P.K;
+#define VP_ME(n) \
+    if (K == n) { LAUNCH(x, (k_metro_ratio<n, true>), (g, 256, sm, x->stream), (c->d, force)); return VP_OK; }
+#define VP_MP(n) \
+    if (K <= n) { LAUNCH(x, (k_metro_ratio<n, false>), (g, 256, sm, x->stream), (c->d, force)); return VP_OK; }
+    VP_ZADM_EXACT(VP_ME)
+    VP_ZADM_PADDED(VP_MP)
+#undef VP_ME
+#undef VP_MP
+    vp_set_error("K = %d out of range", K);
+    return VP_E_ARG;
+}
+
 void set_smem_limits() {
     static bool done = false;
     if (done) return;
@@ -262,6 +280,12 @@ void set_smem_limits() {
     VP_ZADM_PADDED(VP_ZP)
 #undef VP_ZE
 #undef VP_ZP
+#define VP_ME(n) cudaFuncSetAttribute(k_metro_ratio<n, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+#define VP_MP(n) cudaFuncSetAttribute(k_metro_ratio<n, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    VP_ZADM_EXACT(VP_ME)
+    VP_ZADM_PADDED(VP_MP)
+#undef VP_ME
+#undef VP_MP
 }
 
 int launch_step(vp_chain* c, int step, int force) {
@@ -292,7 +316,7 @@ int launch_step(vp_chain* c, int step, int force) {
                 LAUNCH(x, k_update_q_admix, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
                 if (P.metrofreq > 0) {
                     LAUNCH(x, k_metro_propose, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
-                    LAUNCH(x, k_metro_ratio, (dim3(cdiv(x->N, LL_BLOCK), c->h.nchunk, 1), LL_BLOCK, 0, s), (c->d, 0));
+                    if (int rc = launch_metro_ratio(c, 0)) return rc;
                     LAUNCH(x, k_metro_accept, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
                 }
             }
