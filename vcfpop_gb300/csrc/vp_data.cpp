@@ -211,6 +211,16 @@ extern "C" int vp_dataset_prepare(const vp_input* in, vp_dataset** out) {
                     d->maxploidy = std::max(d->maxploidy, in->ploidy[i]);
                 }
         }
+        // with mixed ploidy the per-copy kernels take individuals in ascending
+        // ploidy, so that a warp's lanes loop over the same number of copies
+        bool mixed = false;
+        for (int i = 1; i < N; ++i) mixed |= in->ploidy[i] != in->ploidy[0];
+        if (mixed) {
+            d->perm.resize(N);
+            for (int i = 0; i < N; ++i) d->perm[i] = i;
+            std::stable_sort(d->perm.begin(), d->perm.end(),
+                             [&](int32_t a, int32_t b) { return in->ploidy[a] < in->ploidy[b]; });
+        }
     }
     // 4. total-population frequencies and typed copies in the FILTERED INPUT
     //    order: CalcFreq runs before the sort (src/function.cpp:4690-4694,

@@ -205,12 +205,20 @@ struct Philox {
         }
         return c;
     }
+    // pos counts the draws taken from buf; at 4 or more the next draw starts
+    // a new block, pos - 4 draws past its start (skip() only moves pos)
     __device__ inline uint32_t next() {
-        if (pos == 4) { buf = round10(ctr, key); ctr.w++; pos = 0; }
+        if (pos >= 4) {
+            ctr.w += (uint32_t)((pos - 4) >> 2);
+            buf = round10(ctr, key);
+            ctr.w++;
+            pos = (pos - 4) & 3;
+        }
         uint32_t r = pos == 0 ? buf.x : pos == 1 ? buf.y : pos == 2 ? buf.z : buf.w;
         pos++;
         return r;
     }
+    __device__ inline void skip(int n) { pos += n; }
     // uniform in (0, 1]
     __device__ static inline float to_uniformf(uint32_t x) { return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f); }
     __device__ inline float uniformf() { return to_uniformf(next()); }

@@ -37,6 +37,7 @@ struct vp_dataset {
     std::vector<int64_t> vt;       // [N] typed copies per individual
     std::vector<int64_t> order;    // [L] sorted position -> input locus
     std::vector<int32_t> popid, pop_ind0, pop_nind;
+    std::vector<int32_t> perm;     // individuals in ascending ploidy (empty: one ploidy)
     std::vector<float> totfreq;    // [KT] total-population frequency, pre-sort layout
     std::vector<int32_t> nhaplo;   // [L] typed copies per locus, pre-sort order
     std::vector<int64_t> kdis;     // [maxK+1] loci with k alleles

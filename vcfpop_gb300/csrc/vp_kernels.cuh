@@ -27,6 +27,7 @@ struct DevData {
     const int32_t* pop_nind;
     const float* totfreq;
     const int32_t* nhaplo;
+    const int32_t* perm;   // [N] individuals in ascending ploidy, or null (one ploidy)
 };
 
 struct Ctl {
@@ -842,8 +843,9 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
     float* sF = reinterpret_cast<float*>(smraw);                  // [ZA_LC][MK][KPAD]
     int32_t* hs = reinterpret_cast<int32_t*>(sF + ZA_LC * MK * KPAD);  // [ZA_LC][K][MK]
     const int lane = threadIdx.x & 31;
-    const int i = blockIdx.x * (ZA_WARPS * 32) + threadIdx.x;
-    const bool live = i < D.N;
+    const int slot = blockIdx.x * (ZA_WARPS * 32) + threadIdx.x;
+    const bool live = slot < D.N;
+    const int i = live && D.perm ? D.perm[slot] : slot;   // ascending ploidy with mixed ploidy
     constexpr int NPK = (KM + 7) / 8;
     static_assert(ZA_LC * 10 < 256, "8-bit label counts per slice");
     float q[KM];
@@ -875,7 +877,10 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
             if (live) load_copies(D, l, i, cp); else cp.n = 0;
             float lacc = 0.f;
             int32_t* hl = hs + ll * nbins;
-            for (int a = 0; a < D.vmax; ++a) {
+            // with mixed ploidy the warp loops over its largest copy count;
+            // every individual's stream still advances by vmax draws per locus
+            const int nw = D.perm ? (int)__reduce_max_sync(0xffffffffu, (unsigned)cp.n) : D.vmax;
+            for (int a = 0; a < nw; ++a) {
                 const bool act = a < cp.n;
                 const float u = ph.uniformf();
                 int key = -1;
@@ -926,6 +931,7 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
                     atomicAdd(&hl[key], 1);
                 }
             }
+            ph.skip(D.vmax - nw);
             float y = lacc - lc, tt = ls + y;
             lc = (tt - ls) - y;
             ls = tt;
@@ -957,8 +963,9 @@ __global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int
     if (!force && !metro_turn(c, m)) return;
     const int KPAD = K | 1;
     float* sF = reinterpret_cast<float*>(smraw);   // [ZA_LC][MK][KPAD]
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = i < D.N;
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = slot < D.N;
+    const int i = live && D.perm ? D.perm[slot] : slot;   // ascending ploidy with mixed ploidy
     float q1[KM], q0[KM];
 #pragma unroll
     for (int k = 0; k < KM; ++k) {

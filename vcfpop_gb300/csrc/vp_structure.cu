@@ -429,6 +429,8 @@ extern "C" int vp_open(const vp_dataset* ds, int device, vp_ctx** out) {
     rc |= upload(x, ds->pop_nind.data(), ds->pop_nind.size(), &D.pop_nind);
     rc |= upload(x, ds->totfreq.data(), ds->totfreq.size(), &D.totfreq);
     rc |= upload(x, ds->nhaplo.data(), ds->nhaplo.size(), &D.nhaplo);
+    D.perm = nullptr;
+    if (!ds->perm.empty()) rc |= upload(x, ds->perm.data(), ds->perm.size(), &D.perm);
     if (rc) { vp_close(x); return rc < 0 ? rc : VP_E_CUDA; }
     if (cudaStreamSynchronize(x->stream) != cudaSuccess) { vp_set_error("upload failed"); vp_close(x); return VP_E_CUDA; }
     *out = x;
@@ -575,7 +577,7 @@ int64_t vp_request_bytes(const vp_dataset* ds, const vp_params* P, int nsm) {
     int64_t data = ds->packed2 ? r(ds->g2.size() * 4) : r(ds->gb.size());
     data += r(ds->k.size() * 4) + r(ds->off.size() * 8) + r(ds->vt.size() * 8) + r(ds->popid.size() * 4) +
             r(ds->pop_ind0.size() * 4) + r(ds->pop_nind.size() * 4) + r(ds->totfreq.size() * 4) +
-            r(ds->nhaplo.size() * 4);
+            r(ds->nhaplo.size() * 4) + (ds->perm.empty() ? 0 : r(ds->perm.size() * 4));
     return data + (int64_t)chain;
 }
 
