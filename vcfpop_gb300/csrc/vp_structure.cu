@@ -191,6 +191,15 @@ void prof_mark(vp_ctx* x, bool begin) {
 }
 
 // bump allocator over one device allocation
+// writes a chain's device header from the launch's own parameter (no host
+// copy to stage)
+__global__ void k_set_chain(DevChain* dst, const DevChain h) {
+    static_assert(sizeof(DevChain) % 4 == 0 && sizeof(DevChain) <= 4000, "DevChain as a kernel parameter");
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(&h);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    for (int j = threadIdx.x; j < (int)(sizeof(DevChain) / 4); j += blockDim.x) d[j] = a[j];
+}
+
 struct Carve {
     char* base;
     size_t off = 0;
@@ -603,7 +612,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
     chain_layout(cv, c, x);
     c->own_ni = h.Ni;
     CK(cudaMemsetAsync(c->mem, 0, bytes, x->stream));
-    CK(cudaMemcpyAsync(c->d, &h, sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
+    LAUNCH(x, k_set_chain, (1, 128, 0, x->stream), (c->d, h));
     c->total = h.nburnin + h.nreps;
     // InitFix / InitAdmix / InitLocPriori / InitFmodel
     cudaStream_t s = x->stream;
@@ -636,10 +645,14 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
 extern "C" int vp_chain_destroy(vp_chain* c) {
     if (!c) return VP_OK;
     cudaSetDevice(c->ctx->device);
-    cudaStreamSynchronize(c->ctx->stream);
+    bool in_batch = false, in_pg = false;
     if (c->ctx->batch)
-        for (vp_chain* o : c->ctx->batch->chains)
-            if (o == c) { free_batch(c->ctx); break; }
+        for (vp_chain* o : c->ctx->batch->chains) in_batch |= o == c;
+    for (vp_chain* o : c->ctx->pg_chains) in_pg |= o == c;
+    // graphs are destroyed only once their launches are done; the chain's
+    // memory is freed in stream order and needs no wait
+    if (in_batch || in_pg || c->graph) cudaStreamSynchronize(c->ctx->stream);
+    if (in_batch) free_batch(c->ctx);
     for (vp_chain* o : c->ctx->pg_chains)
         if (o == c) {
             cudaGraphExecDestroy(c->ctx->pg);
@@ -867,7 +880,8 @@ extern "C" int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes
     int rc = field_ptr(c, field, &p, &n);
     if (rc) return rc;
     if (bytes != n) { vp_set_error("field %d holds %zu bytes, not %zu", field, n, bytes); return VP_E_ARG; }
-    CK(cudaMemcpy(host, p, n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(host, p, n, cudaMemcpyDeviceToHost, c->ctx->stream));
+    CK(cudaStreamSynchronize(c->ctx->stream));
     return VP_OK;
 }
 
