@@ -48,6 +48,9 @@ void vp_set_error(const char* fmt, ...);
 // device bytes a request (its context's uploads plus one chain) will hold;
 // -1 when the parameters are invalid
 int64_t vp_request_bytes(const vp_dataset* ds, const vp_params* P, int nsm);
+// vp_open with the context's stream at a CUDA stream priority (lower numbers
+// run first; 0 is the default)
+int vp_open_ex(const vp_dataset* ds, int device, int priority, vp_ctx** out);
 // vp_finish without the final wait
 int vp_finish_issue(vp_chain** cs, int32_t n);
 // sweeps issued so far and in total for one chain

@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -54,6 +55,7 @@ struct Req {
 
 struct vp_server {
     int device = 0, nsm = 0;
+    int prio_least = 0, prio_greatest = 0;   // cudaDeviceGetStreamPriorityRange
     int64_t budget = 0, used = 0;
     int max_active = 64, chunk = 16;
     Clock::time_point t0;
@@ -95,9 +97,27 @@ void fail(vp_server* s, Req* r, int rc, const char* what) {
     s->cv_done.notify_all();
 }
 
+// stream priority of a run: the device's priority levels spread over the
+// decades of its expected work (updates x sweeps, admixture sweeps counted
+// 4x), smaller runs first, so that a short run is not held behind the blocks
+// of long ones. Priorities change only the order in which the device takes
+// up queued blocks; results do not depend on them.
+int run_priority(const vp_server* s, const Req* r) {
+    if (s->prio_least == s->prio_greatest) return s->prio_least;
+    vp_dataset_info di{};
+    vp_dataset_info_get(r->ds, &di);
+    const double sweeps = (double)r->P.nburnin + r->P.nreps + r->P.nadmburnin;
+    const double work = (double)di.n_ind * (double)di.n_loc * r->P.K * std::max(1.0, sweeps) * (r->P.admix ? 4.0 : 1.0);
+    const int levels = s->prio_least - s->prio_greatest + 1;
+    // decades from 1e7 (a few milliseconds of device time) upwards
+    int idx = (int)std::floor(std::log10(std::max(work, 1.0)) - 7.0);
+    idx = std::min(std::max(idx, 0), levels - 1);
+    return s->prio_greatest + idx;
+}
+
 // upload the dataset, create the chain and the two completion events
 int start_run(vp_server* s, Req* r) {
-    int rc = vp_open(r->ds, s->device, &r->ctx);
+    int rc = vp_open_ex(r->ds, s->device, run_priority(s, r), &r->ctx);
     if (rc) return rc;
     rc = vp_chain_create(r->ctx, &r->P, &r->chain);
     if (rc) return rc;
@@ -241,6 +261,8 @@ extern "C" int vp_server_open(int device, int64_t mem_budget, int32_t max_active
     auto* s = new vp_server();
     s->device = device;
     cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, device);
+    if (cudaDeviceGetStreamPriorityRange(&s->prio_least, &s->prio_greatest) != cudaSuccess)
+        s->prio_least = s->prio_greatest = 0;
     if (mem_budget == 0) {
         size_t fr = 0, tot = 0;
         if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { delete s; vp_set_error("cudaMemGetInfo failed"); return VP_E_CUDA; }

@@ -403,7 +403,9 @@ int ensure_counts(vp_chain* c) {
     return rc;
 }
 
-extern "C" int vp_open(const vp_dataset* ds, int device, vp_ctx** out) {
+extern "C" int vp_open(const vp_dataset* ds, int device, vp_ctx** out) { return vp_open_ex(ds, device, 0, out); }
+
+int vp_open_ex(const vp_dataset* ds, int device, int priority, vp_ctx** out) {
     if (!ds || !out) { vp_set_error("null argument"); return VP_E_ARG; }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
@@ -413,7 +415,7 @@ extern "C" int vp_open(const vp_dataset* ds, int device, vp_ctx** out) {
     x->device = device;
     cudaSetDevice(device);
     cudaDeviceGetAttribute(&x->nsm, cudaDevAttrMultiProcessorCount, device);
-    if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithPriority(&x->stream, cudaStreamNonBlocking, priority) != cudaSuccess) {
         vp_set_error("cudaStreamCreate failed");
         delete x;
         return VP_E_CUDA;
