@@ -712,7 +712,7 @@ __global__ void k_metro_propose(const DevChain* chains, int force) {
 // log likelihood ratio of the proposals (UpdateQMetro, src/structure.cpp:
 // 1006-1086): the sum over loci and copies of ln( sum_k q'_k p / sum_k q_k p ).
 // Warp = 32 individuals (one per lane), CTA = 8 warps; grid.y = the locus
-// chunks whose partials k_metro_accept adds. A CTA stages each slice of
+// ranges of the per-copy label kernel, whose partials k_metro_accept adds. A CTA stages each slice of
 // ZA_LC loci's frequencies in shared memory ([ZA_LC][MK][KPAD], odd stride)
 // and keeps Q and Q' rows in registers (K <= KM; EXACT: K == KM). FP32 sums
 // over SUB loci fold into FP64 (the same operations in the same order for
@@ -732,7 +732,8 @@ __global__ void k_metro_accept(const DevChain* chains, int force) {
     if (ref) r = *c.rstate;
     for (int i = ref ? 0 : blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += ref ? 1 : gridDim.x * blockDim.x) {
         double d = 0;
-        for (int ch = 0; ch < c.nchunk; ++ch) d += c.metrop[(int64_t)ch * D.N + i];
+        const int nm = (int)((D.L + c.zadm_lc - 1) / c.zadm_lc);   // k_metro_ratio's locus ranges
+        for (int ch = 0; ch < nm; ++ch) d += c.metrop[(int64_t)ch * D.N + i];
         c.metro[i] = d;
         if (D.vt[i] == 0) continue;
         double u;
@@ -973,7 +974,7 @@ __global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int
         q1[k] = on ? c.Qprop[(int64_t)i * K + k] : 0.f;
         q0[k] = on ? c.Q[(int64_t)i * K + k] : 0.f;
     }
-    const int64_t lc0 = (int64_t)blockIdx.y * c.lchunk, lc1 = min(D.L, lc0 + c.lchunk);
+    const int64_t lc0 = (int64_t)blockIdx.y * c.zadm_lc, lc1 = min(D.L, lc0 + c.zadm_lc);
     double accd = 0;
     float acc = 0.f;
     int cnt = 0;

@@ -262,7 +262,7 @@ int launch_zadm_ctr(vp_chain* c, int force) {
 // the Metropolis ratio kernel on the same K instantiations as the label kernel
 int launch_metro_ratio(vp_chain* c, int force) {
     vp_ctx* x = c->ctx;
-    const dim3 g(cdiv(x->N, 256), c->h.nchunk, 1);
+    const dim3 g(cdiv(x->N, 256), cdiv(x->L, c->h.zadm_lc), 1);
     const size_t sm = (size_t)ZA_LC * x->maxK * (c->P.K | 1) * 4;
     const int K = c->P.K;
 #define VP_ME(n) \
@@ -498,7 +498,8 @@ void chain_layout(Carve& cv, vp_chain* c, const vp_ctx* x) {
     h.LLp = cv.take<double>((int64_t)h.nchunk * N * K);
     h.LL = cv.take<double>((int64_t)N * K);
     h.metro = cv.take<double>(N);
-    h.metrop = cv.take<double>((int64_t)h.nchunk * N);
+    // Metropolis partials: one per locus range of the per-copy kernels
+    h.metrop = cv.take<double>((int64_t)cdiv(L, h.zadm_lc) * N);
     h.Alpha = cv.take<double>(K);
     h.Lambda = cv.take<double>(K);
     h.f = cv.take<double>(K);
