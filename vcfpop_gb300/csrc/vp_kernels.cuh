@@ -636,6 +636,97 @@ __global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevCha
     }
 }
 
+// UpdateZNoAdmix counts (src/structure.cpp:1257-1348) for 2-bit packed data,
+// from bit planes. A CTA first writes, for each cluster k of its group and
+// each word w of 16 individuals, the mask with bit 2j set when individual
+// 16w + j has label k (shared memory, KC x Nw words), then walks loci with one
+// warp per locus and the lanes over the locus's words: with lo/hi the two bit
+// planes of the codes (1 = one copy of allele 1, 2 = two, 3 = missing),
+//   allele-1 copies in cluster k = popc(lo & m) + 2 popc(hi & m) - 3 popc(lo & hi & m)
+//   typed calls in cluster k     = n_k - popc(lo & hi & m)
+// and allele-0 copies = 2 x typed - allele-1 copies. Integer and exact; the
+// same Ni as k_count_noadmix. grid.z = cluster groups of KC.
+template <int KC>
+__global__ void __launch_bounds__(256) k_count_packed(const DevChain* chains, int kgroups, int force) {
+    extern __shared__ uint32_t smask[];   // [KC][Nw] masks, then [KC] cluster sizes
+    const DevChain& c = chains[blockIdx.z / kgroups];
+    const int kg0 = (blockIdx.z % kgroups) * KC;
+    const DevData& D = c.D;
+    const int K = c.K, Nw = D.Nw;
+    if (!force && !binaryq_at(c, c.ctl->m)) return;
+    const int kn = min(KC, K - kg0);
+    int32_t* nk = reinterpret_cast<int32_t*>(smask + (size_t)KC * Nw);
+    if (threadIdx.x < KC) nk[threadIdx.x] = 0;
+    __syncthreads();
+    int cnt[KC];
+#pragma unroll
+    for (int k = 0; k < KC; ++k) cnt[k] = 0;
+    for (int w = threadIdx.x; w < Nw; w += blockDim.x) {
+        uint32_t mk[KC];
+#pragma unroll
+        for (int k = 0; k < KC; ++k) mk[k] = 0;
+        for (int j = 0; j < 16; ++j) {
+            const int i = 16 * w + j;
+            const int z = i < D.N ? (int)c.Z[i] - kg0 : -1;
+#pragma unroll
+            for (int k = 0; k < KC; ++k)
+                if (z == k) mk[k] |= 1u << (2 * j);
+        }
+#pragma unroll
+        for (int k = 0; k < KC; ++k) {
+            smask[(size_t)k * Nw + w] = mk[k];
+            cnt[k] += __popc(mk[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < KC; ++k)
+        if (cnt[k]) atomicAdd(&nk[k], cnt[k]);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    for (int64_t l = (int64_t)blockIdx.x * nwarp + warp; l < D.L; l += (int64_t)gridDim.x * nwarp) {
+        const uint32_t* row = D.g2 + l * Nw;
+        int a1[KC], n3[KC];
+#pragma unroll
+        for (int k = 0; k < KC; ++k) { a1[k] = 0; n3[k] = 0; }
+        // two words per lane in flight
+        for (int w0 = lane; w0 < Nw; w0 += 64) {
+            const int w1 = w0 + 32;
+            const uint32_t g0 = __ldg(row + w0), g1 = w1 < Nw ? __ldg(row + w1) : 0xFFFFFFFFu;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int w = h ? w1 : w0;
+                if (w >= Nw) break;
+                const uint32_t g = h ? g1 : g0;
+                const uint32_t lo = g & 0x55555555u, hi = (g >> 1) & 0x55555555u, ms = lo & hi;
+#pragma unroll
+                for (int k = 0; k < KC; ++k) {
+                    if (k < kn) {
+                        const uint32_t m = smask[(size_t)k * Nw + w];
+                        const int p3 = __popc(ms & m);
+                        a1[k] += __popc(lo & m) + 2 * __popc(hi & m) - 3 * p3;
+                        n3[k] += p3;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < KC; ++k) {
+            if (k < kn) {
+                int v = a1[k], u = n3[k];
+                for (int o = 16; o > 0; o >>= 1) {
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                    u += __shfl_xor_sync(0xffffffffu, u, o);
+                }
+                if (lane == 0) {
+                    const int64_t o2 = (int64_t)(kg0 + k) * D.KT + D.off[l];
+                    c.Ni[o2] = 2 * (nk[k] - u) - v;
+                    c.Ni[o2 + 1] = v;
+                }
+            }
+        }
+    }
+}
+
 // Dirichlet draw of one individual's admixture proportions from alpha + counts
 __device__ __forceinline__ void dirichlet_ref(Rng64& r, float* q, const double* a, const int32_t* b, int K) {
     double s = 0;

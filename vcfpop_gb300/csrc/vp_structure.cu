@@ -283,6 +283,9 @@ void set_smem_limits() {
     done = true;
     const int big = 200 * 1024;
     cudaFuncSetAttribute(k_count_noadmix, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_count_packed<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_count_packed<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_count_packed<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 #define VP_ZE(n) cudaFuncSetAttribute(k_update_z_admix_ctr<n, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 #define VP_ZP(n) cudaFuncSetAttribute(k_update_z_admix_ctr<n, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     VP_ZADM_EXACT(VP_ZE)
@@ -295,6 +298,31 @@ void set_smem_limits() {
     VP_ZADM_PADDED(VP_MP)
 #undef VP_ME
 #undef VP_MP
+}
+
+// the no-admixture counts: from bit planes on 2-bit packed data with at
+// least 32 words per locus (N >= 512) when the masks of a cluster group fit in
+// shared memory, else the per-individual pass
+int launch_count(vp_chain* c, int force) {
+    vp_ctx* x = c->ctx;
+    const int K = c->P.K;
+    if (x->packed2) {
+        const int kc = K <= 4 ? 4 : K <= 8 ? 8 : 16;
+        const int kgroups = (K + kc - 1) / kc;
+        const size_t sm = (size_t)kc * x->D.Nw * 4 + kc * 4;
+        if (sm <= 200 * 1024 && x->D.Nw >= 32) {
+            const dim3 g((unsigned)std::min<int64_t>(cdiv(x->L, 8), (int64_t)x->nsm * 8), 1, (unsigned)kgroups);
+            switch (kc) {
+                case 4: LAUNCH(x, k_count_packed<4>, (g, 256, sm, x->stream), (c->d, kgroups, force)); break;
+                case 8: LAUNCH(x, k_count_packed<8>, (g, 256, sm, x->stream), (c->d, kgroups, force)); break;
+                default: LAUNCH(x, k_count_packed<16>, (g, 256, sm, x->stream), (c->d, kgroups, force)); break;
+            }
+            return VP_OK;
+        }
+    }
+    LAUNCH(x, k_count_noadmix, (dim3(cdiv(x->L, COUNT_WARPS), 1, 1), COUNT_WARPS * 32, count_smem(c), x->stream),
+           (c->d, force));
+    return VP_OK;
 }
 
 int launch_step(vp_chain* c, int step, int force) {
@@ -336,7 +364,7 @@ int launch_step(vp_chain* c, int step, int force) {
             return VP_OK;
         case VP_STEP_UPDATEZ:
             if (!P.admix)
-                LAUNCH(x, k_count_noadmix, (dim3(cdiv(x->L, COUNT_WARPS), 1, 1), COUNT_WARPS * 32, count_smem(c), s), (c->d, 0));
+                if (int rc = launch_count(c, 0)) return rc;
             if (P.admix || c->h.nadmburnin > 0) {
                 LAUNCH(x, k_zero_counts, (dim3(std::min<unsigned>(1024, cdiv((int64_t)K * x->KT, 256)), 1, 1), 256, 0, s), (c->d, 0));
                 if (ref)
@@ -396,9 +424,7 @@ int launch_sweep(vp_chain* c) {
 // its batch
 int ensure_counts(vp_chain* c) {
     if (!c->counts_pending) return VP_OK;
-    vp_ctx* x = c->ctx;
-    k_count_noadmix<<<cdiv(x->L, COUNT_WARPS), COUNT_WARPS * 32, count_smem(c), x->stream>>>(c->d, 1);
-    int rc = check_launch(x, "k_count_noadmix");
+    int rc = launch_count(c, 1);
     if (!rc) c->counts_pending = false;
     return rc;
 }
@@ -638,8 +664,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
                 c->counts_pending = true;
                 break;
             }
-            k_count_noadmix<<<cdiv(L, COUNT_WARPS), COUNT_WARPS * 32, count_smem(c), s>>>(c->d, 1);
-            if ((rc = check_launch(x, "k_count_noadmix"))) break;
+            if ((rc = launch_count(c, 1))) break;
         } else {
             k_init_admix<<<cdiv(L, 128), 128, 0, s>>>(c->d);
             if ((rc = check_launch(x, "k_init_admix"))) break;
