@@ -406,12 +406,6 @@ __device__ __forceinline__ int polylog(double* ll, int K, double u01, bool ref, 
     return K - 1;
 }
 
-// PolyLog for counter streams: the same draw, with the weights
-// exp(LL_k - max) evaluated in single precision (within 1e-7 of the double
-// weights; FP64 exp is slow on this part) and summed and searched in double.
-// The counter-stream draw is not matched to the reference's stream.
-__device__ __forceinline__ double weight_ctr(double d) { return d < -23 ? VP_MIN_FREQ : (double)__expf((float)d); }
-
 // UpdateQNoAdmix label draw (src/structure.cpp:891-900) plus the state the
 // reference rebuilds afterwards: Q one-hot, Mi[i, Z_i] = vt_i
 // (src/structure.cpp:1305-1310), Di for the location prior (1151-1158) and the
@@ -457,16 +451,21 @@ __device__ void sample_one(const DevChain& c, int i, int m, bool ref, Rng64* r, 
     *lnl += keep[z];
 }
 // counter streams: one warp per individual. Lane k holds cluster k (and
-// k + 32): it sums the chunk partials of its clusters, and the maximum, the
-// normaliser and the categorical search (the first cluster whose cumulative
-// weight exceeds the uniform) are warp reductions, a prefix scan and a
-// ballot. Returns, in every lane, LL[i, z] of the drawn label.
+// k + 32): it sums the chunk partials of its clusters in FP64, and the
+// maximum (FP64), the normaliser and the categorical search (the first
+// cluster whose cumulative weight exceeds the uniform) are warp reductions,
+// a prefix scan and a ballot, the weights exp(LL_k - max) and the search in
+// FP32. The counter-stream draw is not matched to the reference's stream.
+// Returns, in every lane, LL[i, z] of the drawn label.
 __device__ double sample_warp(const DevChain& c, int i, int m, int lane) {
     const DevData& D = c.D;
     const int K = c.K, N = D.N;
     const int k0 = lane, k1 = lane + 32;
     const bool h0 = k0 < K, h1 = k1 < K;
     double v0 = 0, v1 = 0;
+    // unrolled so that the partials' loads are in flight together; the adds
+    // keep chunk order
+#pragma unroll 8
     for (int ch = 0; ch < c.nchunk; ++ch) {
         const double* p = c.LLp + ((int64_t)ch * N + i) * K;
         if (h0) v0 += p[k0];
@@ -489,22 +488,25 @@ __device__ double sample_warp(const DevChain& c, int i, int m, int lane) {
         if (h0) w0 += log(g[k0]);
         if (h1) w1 += log(g[k1]);
     }
+    // the maximum in FP64; the weights exp(LL_k - max), their prefix sums and
+    // the draw in FP32 (FP64 arithmetic is slow on this part)
     double mx = fmax(h0 ? w0 : -1.79769313486231570e+308, h1 ? w1 : -1.79769313486231570e+308);
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    const double e0 = h0 ? weight_ctr(w0 - mx) : 0.0;
-    const double e1 = h1 ? weight_ctr(w1 - mx) : 0.0;
+    const float d0 = (float)(w0 - mx), d1 = (float)(w1 - mx);
+    const float e0 = h0 ? (d0 < -23.f ? (float)VP_MIN_FREQ : __expf(d0)) : 0.f;
+    const float e1 = h1 ? (d1 < -23.f ? (float)VP_MIN_FREQ : __expf(d1)) : 0.f;
     // inclusive prefix sums of the weights in cluster order
-    double c0 = e0, c1 = e1;
+    float c0 = e0, c1 = e1;
     for (int o = 1; o < 32; o <<= 1) {
-        const double a0 = __shfl_up_sync(0xffffffffu, c0, o), a1 = __shfl_up_sync(0xffffffffu, c1, o);
+        const float a0 = __shfl_up_sync(0xffffffffu, c0, o), a1 = __shfl_up_sync(0xffffffffu, c1, o);
         if (lane >= o) { c0 += a0; c1 += a1; }
     }
-    const double tot0 = __shfl_sync(0xffffffffu, c0, 31);
+    const float tot0 = __shfl_sync(0xffffffffu, c0, 31);
     c1 += tot0;
-    const double s = __shfl_sync(0xffffffffu, c1, 31) + VP_MIN_FREQ * K;
-    double u = 0;
-    if (lane == 0) { Philox ph; ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0); u = ph.uniformd(); }
-    const double t = __shfl_sync(0xffffffffu, u, 0) * s;
+    const float s = __shfl_sync(0xffffffffu, c1, 31) + (float)(VP_MIN_FREQ * K);
+    float u = 0.f;
+    if (lane == 0) { Philox ph; ph.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 0); u = ph.uniformf(); }
+    const float t = __shfl_sync(0xffffffffu, u, 0) * s;
     int z = K - 1;
     const unsigned b0 = __ballot_sync(0xffffffffu, h0 && t < c0);
     const unsigned b1 = __ballot_sync(0xffffffffu, h1 && t < c1);

@@ -517,6 +517,7 @@ __device__ __forceinline__ double sample_tc_body(const BatchDev& b, const DevCha
     for (int k = 0; k < KM; ++k) {
         if (k >= K) break;
         float v = 0.f;
+#pragma unroll 4
         for (int s = 0; s < b.splits; ++s) v += b.LLpart[((int64_t)s * N + i) * b.Rpad + r0 + k];
         sf[k] = v;
         c.LL[(int64_t)i * K + k] = bc + (double)v;
