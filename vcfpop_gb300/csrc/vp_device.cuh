@@ -92,6 +92,12 @@ __device__ inline double ref_mylog(double v) {
 __device__ inline float ln_freq(float p) {
     return p > 0.f ? logf(p) : -709.0895657128241f;
 }
+// the same with the hardware logarithm (absolute error about 2^-21), for the
+// centred tensor-core weights, which serve the label draws only (a recorded
+// lnP(D) is formed from the counts with ln_freq)
+__device__ inline float ln_freq_fast(float p) {
+    return p > 0.f ? __logf(p) : -709.0895657128241f;
+}
 
 // ---------------- RNG<double>: xorshift128+ ----------------
 struct Rng64 {
@@ -219,6 +225,13 @@ struct Philox {
         return r;
     }
     __device__ inline void skip(int n) { pos += n; }
+    // the stream's first block, consumed whole (right after init)
+    __device__ inline uint4 first_block() {
+        buf = round10(ctr, key);
+        ctr.w++;
+        pos = 4;
+        return buf;
+    }
     // uniform in (0, 1]
     __device__ static inline float to_uniformf(uint32_t x) { return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f); }
     __device__ inline float uniformf() { return to_uniformf(next()); }
@@ -256,8 +269,8 @@ struct Philox {
         return g;
     }
     // Two independent gamma(a0, 1), gamma(a1, 1) draws (a Beta draw for a
-    // biallelic locus). The first Marsaglia-Tsang attempt of both takes one
-    // Philox block: the cosine and sine normals of one Box-Muller pair and
+    // biallelic locus), on a stream fresh from init. The first Marsaglia-Tsang
+    // attempt of both takes the stream's first Philox block: the cosine and sine normals of one Box-Muller pair and
     // two acceptance uniforms; an attempt that is rejected (rare for shapes
     // >= 1) continues as gammaf does, on further blocks. The Box-Muller
     // radius and angle use the hardware approximations (__logf, __sincosf of
@@ -268,7 +281,10 @@ struct Philox {
         const float b0 = s0 ? a0 + 1.f : a0, b1 = s1 ? a1 + 1.f : a1;
         const float d0 = b0 - 1.f / 3.f, c0 = rsqrtf(9.f * d0);
         const float d1 = b1 - 1.f / 3.f, c1 = rsqrtf(9.f * d1);
-        const float u1 = uniformf(), u2 = uniformf(), u3 = uniformf(), u4 = uniformf();
+        // the first block of the stream gives the four uniforms directly; a
+        // rejected attempt continues with the next block
+        const uint4 b4 = first_block();
+        const float u1 = to_uniformf(b4.x), u2 = to_uniformf(b4.y), u3 = to_uniformf(b4.z), u4 = to_uniformf(b4.w);
         const float r = sqrtf(-2.0f * __logf(u1));
         float sn, cs;
         __sincosf(6.283185307179586f * u2 - 3.141592653589793f, &sn, &cs);

@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(256) k_update_p_tc(BatchDev b) {
         ph.dirichlet2(lam + (float)n.x, lam + (float)n.y, p0, p1);
         F2[l] = make_float2(p0, p1);
         const float2 lb = lpb[l];
-        const float w0 = ln_freq(p0) - lb.x, w1 = ln_freq(p1) - lb.y;
+        const float w0 = ln_freq_fast(p0) - lb.x, w1 = ln_freq_fast(p1) - lb.y;
         const __nv_bfloat16 h0 = __float2bfloat16(w0), h1 = __float2bfloat16(w1);
         Whi[l] = __halves2bfloat162(h0, h1);
         Wlo[l] = __halves2bfloat162(__float2bfloat16(w0 - __bfloat162float(h0)), __float2bfloat16(w1 - __bfloat162float(h1)));
