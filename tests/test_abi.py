@@ -103,3 +103,16 @@ def test_vcf_ingest_without_gpu_fails_loudly():
         pytest.skip("GPU present")
     with pytest.raises(B.VpError, match="no CUDA device"):
         S.vcf_pack2(b"1\t1\t.\tA\tC\t.\tPASS\t.\tGT\t0/1\n", 1)
+
+
+def test_tuner_entry_points_reject_bad_arguments():
+    """vp_tune, vp_tc_configure and vp_tc_config_get check their arguments
+    before any device call: no chains, a null chain, a null configuration."""
+    L = B.lib()
+    cfg = B.VpTcConfig()
+    none = (ctypes.c_void_p * 1)()
+    assert L.vp_tune(none, 0, 1, ctypes.byref(cfg)) == -1   # VP_E_ARG
+    assert L.vp_tune(none, 1, 1, ctypes.byref(cfg)) == -1   # VP_E_ARG
+    assert L.vp_tc_configure(none, 1, None) == -1   # VP_E_ARG
+    assert L.vp_tc_config_get(none, 0, ctypes.byref(cfg)) == -1   # VP_E_ARG
+    assert "chain" in L.vp_last_error().decode()
