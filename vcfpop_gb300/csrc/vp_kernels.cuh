@@ -55,7 +55,7 @@ struct DevChain {
 };
 
 // step ids folded into Philox counters
-enum : uint32_t { ST_INITZ = 1, ST_P = 2, ST_Q = 3, ST_METRO_P = 4, ST_METRO_A = 5, ST_Z = 6, ST_A = 7, ST_INITADM = 8,
+enum : uint32_t { ST_INITZ = 1, ST_P = 2, ST_Q = 3, ST_METRO_P = 4, ST_METRO_A = 5, ST_A = 7, ST_INITADM = 8,
                   ST_ALPHA = 9, ST_ZSLICE = 10 };
 
 __device__ __forceinline__ bool binaryq_at(const DevChain& c, int m) { return !c.admix && m >= c.nadmburnin; }
