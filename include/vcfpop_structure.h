@@ -238,6 +238,16 @@ int vp_debug_gemm_e4m3(const uint8_t* A, const uint8_t* B, int32_t M, int32_t N,
 int vp_debug_gemm_time(int32_t M, int32_t N, int32_t K, int32_t BN, int32_t piece, int32_t splits, int32_t stages,
                        int32_t mt, int32_t bk, int32_t esz, int32_t nb, int32_t mode, int32_t iters, double* ms);
 
+/* Diagnostic (no reference counterpart; the reference's checkErrors exits):
+ * the tensor-core pipeline's failure path without a device fault. Runs one
+ * small contraction whose stage barriers expect 16 bytes more than their
+ * copies bring, so every pipeline wait runs out after a short poll limit
+ * (*status_timeout: the error code the kernel recorded, non-zero), then the
+ * same contraction with the right byte counts on the same device
+ * (*status_after: 0) and the largest difference of its result from the exact
+ * one (*max_err_after). */
+int vp_debug_gemm_wait_timeout(int32_t* status_timeout, int32_t* status_after, double* max_err_after);
+
 /* The likelihood accumulation of UpdateQNoAdmix (src/structure.cpp:902-932;
  * the part BAYESIAN<REAL>::UpdateQNoAdmixCUDA offloads, src/structureCUDA.cpp:
  * 2123-2214) as one call on device buffers, for biallelic diploid data:

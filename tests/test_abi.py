@@ -116,3 +116,12 @@ def test_tuner_entry_points_reject_bad_arguments():
     assert L.vp_tc_configure(none, 1, None) == -1   # VP_E_ARG
     assert L.vp_tc_config_get(none, 0, ctypes.byref(cfg)) == -1   # VP_E_ARG
     assert "chain" in L.vp_last_error().decode()
+
+
+def test_wait_timeout_diagnostic_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    st, after, err = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_double(0)
+    assert B.lib().vp_debug_gemm_wait_timeout(ctypes.byref(st), ctypes.byref(after), ctypes.byref(err)) != 0
+    assert "no CUDA device" in B.lib().vp_last_error().decode()

@@ -251,3 +251,15 @@ def test_tune_keeps_chain_state_and_serves_later_batches(tmp_path, monkeypatch):
     cfg2 = S.tc_config(other)
     for k in ("bk", "cols", "stages", "splits", "group_major", "count_stages", "count_group_major"):
         assert cfg2[k] == cfg[k], k
+
+
+def test_pipeline_wait_runs_out_with_an_error_status_and_the_device_stays_usable():
+    """Failure detection without a fault: a contraction whose stage barriers
+    never complete (they expect 16 bytes more than their copies bring) ends
+    with a non-zero error status after its bounded waits, and the same
+    contraction launched right after on the same device is exact."""
+    st, after, err = C.c_int32(0), C.c_int32(-1), C.c_double(-1.0)
+    B.check(B.lib().vp_debug_gemm_wait_timeout(C.byref(st), C.byref(after), C.byref(err)))
+    assert st.value in (1, 2, 3), st.value
+    assert after.value == 0
+    assert err.value == 0.0

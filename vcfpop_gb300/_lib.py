@@ -92,7 +92,7 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
            "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2", "vp_release_memory",
-           "vp_tune", "vp_tc_configure", "vp_tc_config_get"]
+           "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout"]
 
 
 def lib():
@@ -137,6 +137,7 @@ def lib():
     L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 9 + [P]
     L.vp_debug_gemm_time.argtypes = [C.c_int32] * 13 + [P]
     L.vp_debug_gemm_e4m3.argtypes = [P, P] + [C.c_int32] * 7 + [P]
+    L.vp_debug_gemm_wait_timeout.argtypes = [C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     L.vp_release_memory.argtypes = [C.c_int]
     L.vp_stream.argtypes = [P]
     L.vp_stream.restype = P

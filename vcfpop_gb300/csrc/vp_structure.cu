@@ -1,6 +1,7 @@
 // Host side of the device STRUCTURE sweep: contexts, chain state, the launch
 // sequence of one sweep, CUDA-graph replay, and the C ABI.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -1683,6 +1684,73 @@ extern "C" int vp_debug_gemm_bf16(const uint16_t* A, const uint16_t* B0, const u
     cudaFree(dA); cudaFree(dB0); if (dB1) cudaFree(dB1); cudaFree(dD); cudaFree(err);
     cudaStreamDestroy(tmp.stream);
     tmp.stream = nullptr;
+    return rc;
+}
+
+// Failure path of the tensor-core pipeline without a fault: one small
+// contraction whose stage barriers expect 16 bytes more than their copies
+// bring, so every pipeline wait runs out; then the same contraction with the
+// right byte counts on the same device, checked against its exact result.
+extern "C" int vp_debug_gemm_wait_timeout(int32_t* status_timeout, int32_t* status_after, double* max_err_after) {
+    if (!status_timeout || !status_after || !max_err_after) { vp_set_error("null argument"); return VP_E_ARG; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
+    constexpr int M = 256, N = 192, K = 256;
+    // small integers times multiples of 1/8: every product and sum is exact in FP32
+    std::vector<uint16_t> hA((size_t)M * K), hB((size_t)N * K);
+    auto bf = [](float v) { uint32_t u; memcpy(&u, &v, 4); return (uint16_t)(u >> 16); };
+    std::vector<double> ref((size_t)M * N, 0.0);
+    for (int m = 0; m < M; ++m)
+        for (int k = 0; k < K; ++k) hA[(size_t)m * K + k] = bf((float)((m * 7 + k * 3) % 3));
+    for (int n = 0; n < N; ++n)
+        for (int k = 0; k < K; ++k) hB[(size_t)n * K + k] = bf((float)(((n * 5 + k) % 17) - 8) / 8.f);
+    for (int m = 0; m < M; ++m)
+        for (int n = 0; n < N; ++n) {
+            double t = 0;
+            for (int k = 0; k < K; ++k) t += (double)((m * 7 + k * 3) % 3) * ((((n * 5 + k) % 17) - 8) / 8.0);
+            ref[(size_t)m * N + n] = t;
+        }
+    vp_ctx tmp;
+    CK(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
+    void *dA = nullptr, *dB = nullptr, *dD = nullptr;
+    int* err = nullptr;
+    int rc = VP_OK;
+    std::vector<float> D((size_t)M * N);
+    do {
+        if (cudaMalloc(&dA, hA.size() * 2) != cudaSuccess || cudaMalloc(&dB, hB.size() * 2) != cudaSuccess ||
+            cudaMalloc(&dD, D.size() * 4) != cudaSuccess || cudaMalloc(&err, 4) != cudaSuccess) {
+            vp_set_error("allocation failed");
+            rc = VP_E_MEM;
+            break;
+        }
+        cudaMemcpy(dA, hA.data(), hA.size() * 2, cudaMemcpyHostToDevice);
+        cudaMemcpy(dB, hB.data(), hB.size() * 2, cudaMemcpyHostToDevice);
+        CUtensorMap ma, mb;
+        if ((rc = make_map(&ma, dA, M, K, K, 128, 64)) || (rc = make_map(&mb, dB, N, K, K, 192, 64))) break;
+        tc::GemmArgs g{};
+        g.M = M; g.N = N; g.kblocks = K / 64; g.kb_per_split = g.kblocks;
+        g.BN = 192; g.piece = 192; g.nb = 1; g.mt = 2; g.stages = 2; g.bk = 64; g.esz = 2; g.mode = 0;
+        g.out_f = (float*)dD; g.ldo = N; g.err = err;
+        for (int pass = 0; pass < 2 && !rc; ++pass) {
+            g.tx_extra = pass == 0 ? 16 : 0;
+            g.spin_limit = pass == 0 ? (1u << 12) : 0;   // short waits for the pass that times out
+            cudaMemset(err, 0, 4);
+            cudaMemset(dD, 0, D.size() * 4);
+            if ((rc = launch_gemm(&tmp, ma, mb, mb, g, dim3(1, 1, 1)))) break;
+            const cudaError_t ce = cudaStreamSynchronize(tmp.stream);
+            if (ce != cudaSuccess) { vp_set_error("contraction failed: %s", cudaGetErrorString(ce)); rc = VP_E_CUDA; break; }
+            int e = 0;
+            cudaMemcpy(&e, err, 4, cudaMemcpyDeviceToHost);
+            (pass == 0 ? *status_timeout : *status_after) = e;
+        }
+        if (rc) break;
+        cudaMemcpy(D.data(), dD, D.size() * 4, cudaMemcpyDeviceToHost);
+        double worst = 0;
+        for (size_t j = 0; j < D.size(); ++j) worst = std::max(worst, std::abs((double)D[j] - ref[j]));
+        *max_err_after = worst;
+    } while (0);
+    cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(err);
+    cudaStreamDestroy(tmp.stream);
     return rc;
 }
 

@@ -46,6 +46,9 @@ struct GemmArgs {
     int32_t* out_i;         // mode 1: [N][ldo]
     int64_t ldo;
     int* err;
+    int tx_extra;           // diagnostics only: bytes a stage barrier expects beyond what its copies
+                            // bring (> 0 makes every stage wait run out: the time-out path under test)
+    uint32_t spin_limit;    // polls per bounded wait (0: SPIN_LIMIT)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -59,9 +62,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 // bounded wait on a phase parity; returns false on time-out
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = SPIN_LIMIT) {
     uint32_t addr = smem_u32(bar);
-    for (uint32_t it = 0; it < SPIN_LIMIT; ++it) {
+    for (uint32_t it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -178,20 +181,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_holder;
 
+    const uint32_t lim = g.spin_limit ? g.spin_limit : SPIN_LIMIT;
     if (warp == 0) {
         // ---------------- TMA producer ----------------
         if (lane == 0 && nk > 0) {
             int issued = 0;
             for (int it = 0; it < nk; ++it) {
                 const int s = it % stages;
-                if (it >= stages && !mbar_wait(&empty[s], ((it / stages) & 1) ^ 1)) {
+                if (it >= stages && !mbar_wait(&empty[s], ((it / stages) & 1) ^ 1, lim)) {
                     atomicExch(g.err, 1);
                     *(volatile int*)abort_flag = 1;
                     break;
                 }
                 if (*(volatile int*)abort_flag) break;
                 unsigned char* st = smem + (size_t)s * STAGE;
-                mbar_expect_tx(&full[s], STAGE);
+                mbar_expect_tx(&full[s], STAGE + g.tx_extra);
                 const int kx = (kb0 + it) * BKT;
 #pragma unroll
                 for (int t = 0; t < MT; ++t) tma_load_2d(st + t * A_TILE, &mapA, &full[s], kx, m0 + t * BM);
@@ -205,7 +209,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             // drain: every issued stage must have landed before the CTA may exit
             for (int it = (issued > stages ? issued - stages : 0); it < issued; ++it)
-                mbar_wait(&full[it % stages], (it / stages) & 1);
+                mbar_wait(&full[it % stages], (it / stages) & 1, lim);
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint64_t d0 = sw_desc(smem_u32(smem), ROW);
             for (int it = 0; it < nk; ++it) {
                 const int s = it % stages;
-                if (!mbar_wait(&full[s], (it / stages) & 1) || *(volatile int*)abort_flag) {
+                if (!mbar_wait(&full[s], (it / stages) & 1, lim) || *(volatile int*)abort_flag) {
                     atomicExch(g.err, 2);
                     *(volatile int*)abort_flag = 1;
                     break;
@@ -250,7 +254,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     } else {
         // ---------------- epilogue ----------------
         const int q = warp & 3;  // TMEM lane quarter this warp may read
-        const bool got = mbar_wait(accum, 0);
+        const bool got = mbar_wait(accum, 0, lim);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const bool valid = got && !*(volatile int*)abort_flag && nk > 0;
         if (!got) atomicExch(g.err, 3);
