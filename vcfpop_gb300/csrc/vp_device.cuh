@@ -147,11 +147,14 @@ struct Rng64 {
         double t, v, u;
         double d = a - 0.333333333333333;
         double c = 1.0 / (sqrt(d) * 3.0);
-        for (;;) {
+        // bounded: valid shapes accept within a few attempts (the reference's
+        // draws are reproduced exactly); a NaN shape would otherwise loop forever
+        for (int attempt = 0; attempt < 4096; ++attempt) {
+            int tries = 0;
             do {
                 t = normal();
                 v = 1.0 + c * t;
-            } while (v <= 0);
+            } while (v <= 0 && ++tries < 4096);
             v = v * v * v;
             u = uniform();
             if (u < 1.0 - 0.0331 * t * t * t * t) break;
