@@ -23,14 +23,14 @@ CASES = json.load(open(os.path.join(GOLD, "cases.json")))
 NUM = re.compile(r"-?\d+\.\d+|nan")
 
 
-def _run(case, tmp, rng):
+def _run(case, tmp, rng, form="plain"):
     c = CASES[case]
     vcf = os.path.join(tmp, "data.vcf")
     with gzip.open(os.path.join(GOLD, c["data"]), "rb") as fi, open(vcf, "wb") as fo:
         shutil.copyfileobj(fi, fo)
     args = [CLI, f"-g_input={vcf}", f"-g_output={tmp}/out", f"-g_seed={c['seed']}", "-g_decimal=15",
             f"-g_indtext={c['indtext']}", "-g_float=single", "-structure", "-structure_writelnl=yes",
-            f"-gb300_rng={rng}"] + c["flags"]
+            f"-gb300_rng={rng}", f"-gb300_form={form}"] + c["flags"]
     subprocess.run(args, check=True)
     return c
 
@@ -74,3 +74,24 @@ def test_cli_locus_filter_keeps_the_reference_loci(tmp_path):
         return [ln.split("\t")[0] for ln in lines[i + 2:] if ln.split("\t")[0] not in ("", "Average")]
 
     assert loci(tmp_path / f) == loci(os.path.join(GOLD, "c1_filter", f))
+
+
+def test_cli_tensor_core_form_writes_the_reference_files(tmp_path):
+    """-gb300_form=tc on a no-admixture case: the reference's file layout, and
+    the first recorded lnP(D) equal to the plain form's (same state, same
+    Philox draws) within 1e-5."""
+    (tmp_path / "tc").mkdir()
+    (tmp_path / "plain").mkdir()
+    c = _run("c1_noadmix", str(tmp_path / "tc"), "counter", form="tc")
+    _run("c1_noadmix", str(tmp_path / "plain"), "counter", form="plain")
+    for f in c["files"]:
+        if f == "out.structure.txt":
+            continue
+        got = open(tmp_path / "tc" / f, "rb").read().decode()
+        want = open(os.path.join(GOLD, "c1_noadmix", f), "rb").read().decode()
+        assert _shape(got) == _shape(want), f
+    f = [x for x in c["files"] if x.endswith(".lnl.txt")][0]
+    tc = [float(x) for x in NUM.findall(open(tmp_path / "tc" / f).read())]
+    pl = [float(x) for x in NUM.findall(open(tmp_path / "plain" / f).read())]
+    assert len(tc) == len(pl) > 0
+    assert abs(tc[0] - pl[0]) <= 1e-5 * abs(pl[0]), (tc[0], pl[0])
