@@ -213,7 +213,7 @@ struct Carve {
     }
 };
 
-int kc_for(int K) { return K <= 4 ? 4 : K <= 8 ? 8 : 16; }
+int kc_for(int K) { return K <= 4 ? 4 : K <= 8 ? 8 : K <= 12 ? 12 : 16; }
 
 int launch_loglik(vp_chain* c, int force) {
     vp_ctx* x = c->ctx;
@@ -223,6 +223,7 @@ int launch_loglik(vp_chain* c, int force) {
     switch (c->kc) {
         case 4: LAUNCH(x, k_loglik<4>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
         case 8: LAUNCH(x, k_loglik<8>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
+        case 12: LAUNCH(x, k_loglik<12>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
         default: LAUNCH(x, k_loglik<16>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
     }
     return VP_OK;
@@ -1979,6 +1980,7 @@ int ll_run(LLPlan& pl, const uint32_t* geno, const float* freq, double* ll, void
     switch (pl.kc) {
         case 4: k_loglik<4><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
         case 8: k_loglik<8><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+        case 12: k_loglik<12><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
         default: k_loglik<16><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
     }
     k_ll_reduce<<<std::min<unsigned>(1024, cdiv((int64_t)h.D.N * h.K, 256)), 256, 0, s>>>(d, ll);
