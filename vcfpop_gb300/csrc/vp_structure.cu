@@ -1354,9 +1354,23 @@ int launch_tc_sweep(vp_ctx* x) {
     const int n = (int)b->chains.size();
     tc::BatchDev bd = batch_dev(x);
     cudaStream_t s = x->stream;
-    // UpdateP for all chains, with the split-bf16 centred log-frequency rows
-    // about 16 blocks per SM in all (about 3 waves): each thread walks many loci
-    const unsigned upx = std::max<unsigned>(1, std::min<unsigned>(cdiv(x->L, 256), cdiv((int64_t)x->nsm * 16, b->R)));
+    // UpdateP for all chains, with the split-bf16 centred log-frequency rows:
+    // R rows x upx blocks, each thread walking many loci; upx between 2 and 16
+    // (at most one block per 256 loci) chosen so that the blocks fill whole
+    // waves of the kernel's resident blocks
+    unsigned upx = 1;
+    {
+        static int per_sm = 0;
+        if (!per_sm && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::k_update_p_tc, 256, 0) != cudaSuccess)
+            per_sm = 4;
+        const double slots = (double)x->nsm * std::max(1, per_sm);
+        const unsigned hi = std::max<unsigned>(1, std::min<unsigned>(16, cdiv(x->L, 256)));
+        double best = -1;
+        for (unsigned u = std::min(2u, hi); u <= hi; ++u) {
+            const double w = (double)u * b->R / slots, eff = w / std::ceil(w);
+            if (eff > best + 0.01) { best = eff; upx = u; }
+        }
+    }
     LAUNCH(x, tc::k_update_p_tc, (dim3(upx, b->R, 1), 256, 0, s), (bd));
     // likelihood contraction: LL'[i, row] = sum_a C[i,a] (Whi + Wlo)[row, a]
     {
