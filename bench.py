@@ -768,7 +768,7 @@ def main():
             "config": {"workload": f"batched K-sweep: N={N_IND}, L={ds.L} biallelic SNPs, K=1..10 x 10 replicates "
                                    f"= 100 no-admixture chains, one sweep of all chains per step",
                        "form": args.form, "chains": len(KS), "sum_K": sumK, "updates_per_step": upd_step,
-                       "l2": "inputs larger than L2 (packed genotypes 0.5 GB; bf16 counts 2 x 8 GB)",
+                       "l2": "inputs larger than L2 (packed genotypes 0.5 GB; count operands 7.8 GB bf16 + 3.9 GB e4m3)",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
