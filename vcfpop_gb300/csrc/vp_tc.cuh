@@ -328,15 +328,28 @@ __global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bflo
     float acc[8];                    // B_i shares of rows (t >> 4) + 16 p
 #pragma unroll
     for (int p = 0; p < 8; ++p) acc[p] = 0.f;
+    // a tile's 512 packed words, two per thread (j = t, t + 256); the next
+    // tile's are loaded while this tile's rows are written
+    auto load_words = [&](int64_t lt0, uint32_t* wv) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = t + 256 * h, ll = j >> 3, w = j & 7;
+            const int64_t l = lt0 + ll;
+            const int wi = (i0 >> 4) + w;
+            wv[h] = (l < D.L && wi < D.Nw) ? D.g2[l * D.Nw + wi] : 0xFFFFFFFFu;
+        }
+    };
+    const int64_t lbase = (int64_t)blockIdx.y * BUILD_TILES * 64;
+    uint32_t wcur[2];
+    load_words(lbase, wcur);
     for (int tile = 0; tile < BUILD_TILES; ++tile) {
-        const int64_t l0 = ((int64_t)blockIdx.y * BUILD_TILES + tile) * 64;
+        const int64_t l0 = lbase + (int64_t)tile * 64;
         if (2 * l0 >= Apad) break;
         __syncthreads();
-        for (int j = t; j < 64 * 8; j += 256) {
-            const int ll = j >> 3, w = j & 7;
-            const int64_t l = l0 + ll;
-            const int wi = (i0 >> 4) + w;
-            const uint32_t word = (l < D.L && wi < D.Nw) ? D.g2[l * D.Nw + wi] : 0xFFFFFFFFu;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = t + 256 * h, ll = j >> 3, w = j & 7;
+            const uint32_t word = wcur[h];
             uint32_t q[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
@@ -351,6 +364,8 @@ __global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bflo
             *reinterpret_cast<uint4*>(&code[ll][w * 16]) = make_uint4(q[0], q[1], q[2], q[3]);
         }
         __syncthreads();
+        uint32_t wnext[2] = {0xFFFFFFFFu, 0xFFFFFFFFu};
+        if (tile + 1 < BUILD_TILES && 2 * (l0 + 64) < Apad) load_words(l0 + 64, wnext);
         // CT rows 2l+a: eight 16-byte pieces per row
         for (int j = t; j < 128 * 8; j += 256) {
             const int ra = j >> 3, pc = j & 7, ll = ra >> 1, a = ra & 1;
@@ -396,6 +411,8 @@ __global__ void __launch_bounds__(256) k_build_counts(const DevData D, __nv_bflo
                 *reinterpret_cast<uint4*>(C + (int64_t)(i0 + ii) * Apad + col) = make_uint4(w[0], w[1], w[2], w[3]);
             }
         }
+        wcur[0] = wnext[0];
+        wcur[1] = wnext[1];
     }
     // the 16 column pieces of a row sit in 16 consecutive lanes
 #pragma unroll
