@@ -70,6 +70,8 @@ typedef struct {
 int vp_dataset_info_get(const vp_dataset* ds, vp_dataset_info* info);
 /* sorted position -> input locus index, L entries */
 int vp_dataset_order(const vp_dataset* ds, int64_t* order);
+/* Drops the caller's reference: a dataset submitted to a server stays alive
+ * until its request is released or the server is closed. */
 void vp_dataset_free(vp_dataset* ds);
 
 /* ---- device context ------------------------------------------------------ */
@@ -77,6 +79,8 @@ typedef struct vp_ctx vp_ctx;
 /* Upload the packed genotype matrix once (replaces CopyStructureMemory,
  * src/structureCUDA.cpp:969-1094, and its per-device replicas). */
 int vp_open(const vp_dataset* ds, int device, vp_ctx** out);
+/* Closing a context also destroys its chains that are still open; their
+ * handles are invalid afterwards. */
 int vp_close(vp_ctx* ctx);
 int vp_sync(vp_ctx* ctx);
 

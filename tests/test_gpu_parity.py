@@ -102,14 +102,16 @@ def test_update_p(data):
         assert (u == 0).mean() > 0.99
 
 
-@pytest.mark.parametrize("packed", [True, False])
-def test_loglik_and_labels_noadmix(packed):
-    od, oc, ds, ctx, gc = _pair(_c1_small(), packed=packed, K=3, admix=0, nadmburnin=0)
+# K = 3 and 10 take the 4- and 12-cluster likelihood templates, K = 20 two
+# cluster groups of 16
+@pytest.mark.parametrize("packed,K", [(True, 3), (False, 3), (True, 10), (False, 10), (True, 20)])
+def test_loglik_and_labels_noadmix(packed, K):
+    od, oc, ds, ctx, gc = _pair(_c1_small(), packed=packed, K=K, admix=0, nadmburnin=0)
     oc.step("update_p")
     _sync_state(oc, gc)
-    ll_o = oc.loglik().reshape(-1, 3)
+    ll_o = oc.loglik().reshape(-1, K)
     gc.step("LOGLIK")
-    ll_g = gc.get("LL").reshape(-1, 3)
+    ll_g = gc.get("LL").reshape(-1, K)
     rel = np.abs(ll_g - ll_o) / np.maximum(np.abs(ll_o), 1e-300)
     assert rel.max() < REL, rel.max()
     # labels drawn by PolyLog from the same uniforms
@@ -265,12 +267,14 @@ def _allele_copies(d, ds):
     return cnt, typed
 
 
-@pytest.mark.parametrize("data,K", [("adm", 5), ("adm", 13), ("poly", 4), ("poly", 6)])
+@pytest.mark.parametrize("data,K", [("adm", 5), ("adm", 13), ("adm", 16), ("adm", 20), ("poly", 4), ("poly", 6), ("poly", 14)])
 def test_update_z_admix_counter_streams_count_every_copy(data, K):
     """The counter-stream per-copy kernel (warp-reduced histogram: packed
-    redux.sync bins for K * max alleles <= 40, match_any groups above):
-    summed over clusters, Ni holds every allele copy of the data exactly once
-    and Mi every typed copy of each individual."""
+    redux.sync bins for K * max alleles <= 32, one per lane (K = 16 on
+    biallelic data is the largest), a shared atomic per copy above;
+    exact-K templates up to 12, padded ones above; mixed-ploidy warps): summed
+    over clusters, Ni holds every allele copy of the data exactly once and Mi
+    every typed copy of each individual."""
     d = _adm_small() if data == "adm" else _poly_small()
     ds = S.Dataset.from_synth(d)
     ctx = S.Context(ds)

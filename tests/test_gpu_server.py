@@ -122,3 +122,41 @@ def test_close_with_runs_in_flight():
     for j in range(4):
         srv.submit(ds, S.params(3, S.run_seed(4, j + 1), nburnin=200, nreps=200, nadmburnin=0))
     srv.close()                   # abandons the active runs, frees everything
+
+
+def test_dataset_freed_before_its_run_ends():
+    """A request holds its own reference to the dataset: the caller may free
+    its handle right after vp_submit."""
+    ds, p = _runs()[0]
+    ctx = S.Context(ds)
+    ch = S.Chain(ctx, p)
+    S.finish([ch])
+    direct = ch.result(final=True)
+    ctx.close()
+    d2 = S.Dataset.from_synth(synth.fmodel(61, 300, 1500, 3, 0.08, 0.02))
+    srv = S.Server(max_active=1)
+    rid = srv.submit(d2, p)
+    B.lib().vp_dataset_free(d2.h)
+    d2.h = None
+    _same(_collect(srv, rid)[0], direct)
+    srv.close()
+
+
+def test_context_closed_before_its_chains():
+    """vp_close destroys the chains still open on the context; a chain wrapper
+    finalised after its context (as the collector may order a reference
+    cycle) does not touch the freed context."""
+    ds, p = _runs()[2]
+    ctx = S.Context(ds)
+    chains = [S.Chain(ctx, p) for _ in range(3)]
+    chains[0].close()
+    chains[1].run(5)
+    ctx.close()
+    for ch in chains:
+        ch.close()
+        assert ch.h is None
+    ctx2 = S.Context(ds)          # the device is still usable
+    ch = S.Chain(ctx2, p)
+    ch.run(3)
+    ch.close()
+    ctx2.close()

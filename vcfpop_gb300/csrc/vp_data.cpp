@@ -286,7 +286,11 @@ extern "C" int vp_dataset_order(const vp_dataset* d, int64_t* order) {
     return VP_OK;
 }
 
-extern "C" void vp_dataset_free(vp_dataset* d) { delete d; }
+extern "C" void vp_dataset_free(vp_dataset* d) {
+    if (d && d->refs.fetch_sub(1, std::memory_order_acq_rel) == 1) delete d;
+}
+
+void vp_dataset_retain(const vp_dataset* d) { const_cast<vp_dataset*>(d)->refs.fetch_add(1, std::memory_order_relaxed); }
 
 extern "C" void vp_params_default(vp_params* p) {
     memset(p, 0, sizeof *p);

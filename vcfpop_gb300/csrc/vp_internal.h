@@ -1,6 +1,8 @@
 // Internal types shared by the host translation units of the library.
 #pragma once
 #include <stdint.h>
+
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -27,6 +29,7 @@ struct HostBuf {
 };
 
 struct vp_dataset {
+    std::atomic<int> refs{1};      // the caller's handle plus each server request holding it
     int32_t N = 0, S = 0, vmax = 0, maxploidy = 0, maxK = 0, Nw = 0;
     int64_t L = 0, KT = 0, coprime = 1;
     bool packed2 = false;
@@ -51,6 +54,8 @@ int64_t vp_request_bytes(const vp_dataset* ds, const vp_params* P, int nsm);
 // vp_open with the context's stream at a CUDA stream priority (lower numbers
 // run first; 0 is the default)
 int vp_open_ex(const vp_dataset* ds, int device, int priority, vp_ctx** out);
+// one more reference to a dataset; vp_dataset_free drops one
+void vp_dataset_retain(const vp_dataset* ds);
 // vp_finish without the final wait
 int vp_finish_issue(vp_chain** cs, int32_t n);
 // sweeps issued so far and in total for one chain

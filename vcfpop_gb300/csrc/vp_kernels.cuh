@@ -906,11 +906,11 @@ __global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
 // CTA = 8 warps = 256 individuals; grid.y splits the loci into ranges that a
 // CTA walks in slices of ZA_LC loci. A lane keeps its individual's Q row and
 // its Mi counts in registers; the slice's frequencies are staged in shared
-// memory. With at most ZA_PACKED (cluster, allele) bins the per-copy
-// increments of Ni are reduced across the warp before they reach the slice
-// histogram in shared memory: each lane's bin becomes a 1 in one of five
-// 6-bit fields of a word and redux.sync adds the words of the 32 lanes (one
-// reduction per five bins), then lane j adds bin j; with more bins (multi-
+// memory. With at most ZA_PACKED = 32 (cluster, allele) bins, one per lane,
+// the per-copy increments of Ni are reduced across the warp before they reach
+// the slice histogram in shared memory: each lane's bin becomes a 1 in one of
+// five 6-bit fields of a word and redux.sync adds the words of the 32 lanes
+// (one reduction per five bins), then lane j adds bin j; with more bins (multi-
 // allelic data) each copy adds to the shared histogram directly (measured
 // faster there than grouping lanes with __match_any_sync). The slice
 // histogram is flushed to Ni with one global atomic per non-zero entry. KM is
@@ -922,7 +922,8 @@ __global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
 // on sweeps that Record reads (thinning points) or when the step is forced.
 constexpr int ZA_WARPS = 8;
 constexpr int ZA_LC = 16;
-constexpr int ZA_PACKED = 40;
+constexpr int ZA_PACKED = 32;   // lane j flushes bin j
+static_assert(ZA_PACKED <= 32, "one histogram bin per lane");
 template <int KM, bool EXACT>
 __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevChain* chains, int force) {
     extern __shared__ unsigned char smraw[];

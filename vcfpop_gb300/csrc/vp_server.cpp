@@ -49,6 +49,8 @@ struct Req {
     int head = 0;            // event slot of the oldest of them
     bool finishing = false;  // the last chunk (with Arrange) is queued
     int64_t issued = 0, total = 0;
+    // the request holds its own reference to the dataset until it is deleted
+    ~Req() { if (ds) vp_dataset_free(const_cast<vp_dataset*>(ds)); }
 };
 
 }  // namespace
@@ -288,6 +290,7 @@ extern "C" int vp_submit(vp_server* s, const vp_dataset* ds, const vp_params* p,
         return VP_E_MEM;
     }
     auto* r = new Req();
+    vp_dataset_retain(ds);
     r->ds = ds;
     r->P = *p;
     r->bytes = bytes;

@@ -31,6 +31,7 @@ struct vp_ctx {
     cudaStream_t stream = nullptr;
     DevData D{};
     std::vector<void*> allocs;
+    std::vector<vp_chain*> chains;   // open chains: vp_close destroys those left
     int64_t launches = 0;
     int32_t N = 0, S = 0, maxK = 0, maxploidy = 0, packed2 = 0;
     int64_t L = 0, KT = 0;
@@ -479,6 +480,7 @@ int vp_open_ex(const vp_dataset* ds, int device, int priority, vp_ctx** out) {
 extern "C" int vp_close(vp_ctx* x) {
     if (!x) return VP_OK;
     cudaSetDevice(x->device);
+    for (vp_chain* c : std::vector<vp_chain*>(x->chains)) vp_chain_destroy(c);
     if (x->stream) cudaStreamSynchronize(x->stream);
     if (x->batch) { cudaGraphExecDestroy(x->batch->graph); dev_free(x->batch->mem, x->stream); delete x->batch; x->batch = nullptr; }
     if (x->pg) cudaGraphExecDestroy(x->pg);
@@ -673,6 +675,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
         }
     } while (0);
     if (rc) { dev_free(c->mem, x->stream); delete c; return rc; }
+    x->chains.push_back(c);
     *out = c;
     return VP_OK;
 }
@@ -697,6 +700,8 @@ extern "C" int vp_chain_destroy(vp_chain* c) {
         }
     if (c->graph) cudaGraphExecDestroy(c->graph);
     dev_free(c->mem, c->ctx->stream);   // after every launch already queued for the chain
+    auto& open = c->ctx->chains;
+    open.erase(std::remove(open.begin(), open.end(), c), open.end());
     delete c;
     return VP_OK;
 }

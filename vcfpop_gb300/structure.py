@@ -200,8 +200,11 @@ class Chain:
         return dict(H=H, D=D, Hl=Hl)
 
     def close(self):
+        # a closed context has already destroyed its chains (the collector may
+        # finalise the context first when both sit in one reference cycle)
         if getattr(self, "h", None):
-            B.lib().vp_chain_destroy(self.h)
+            if getattr(self.ctx, "h", None):
+                B.lib().vp_chain_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -279,12 +282,12 @@ class Server:
         h = C.c_void_p()
         B.check(B.lib().vp_server_open(device, mem_budget, max_active, chunk, C.byref(h)))
         self.h = h
-        self._ds = {}
 
     def submit(self, ds: Dataset, p: B.VpParams) -> int:
         rid = C.c_int64()
+        # the request keeps its own reference to the dataset: freeing `ds`
+        # before the run ends is safe
         B.check(B.lib().vp_submit(self.h, ds.h, C.byref(p), C.byref(rid)))
-        self._ds[rid.value] = ds          # the dataset must outlive the run
         return rid.value
 
     @staticmethod
@@ -313,13 +316,11 @@ class Server:
 
     def release(self, rid: int) -> None:
         B.check(B.lib().vp_release(self.h, rid))
-        self._ds.pop(rid, None)
 
     def close(self):
         if getattr(self, "h", None):
             B.lib().vp_server_close(self.h)
             self.h = None
-            self._ds.clear()
 
     def __del__(self):
         if not sys.is_finalizing():
