@@ -751,6 +751,36 @@ def main():
             e2e_ms.append(dt * 1e3)
         assert all(np.isfinite(lnl))
     e2e_value = upd_step * args.e2e_sweeps * world / (np.median(e2e_ms) / 1e3) if e2e_ms else None
+    # one more step, untimed, with a wait after each phase: where the time
+    # outside the sweeps goes (the first vp_run call builds the batch's
+    # operands and counts the initial labels before its sweep)
+    phases = None
+    if not args.no_e2e:
+        ph, t = {}, time.perf_counter()
+
+        def mark(name):
+            nonlocal t
+            torch.cuda.synchronize()
+            now = time.perf_counter()
+            ph[name] = round((now - t) * 1e3, 3)
+            t = now
+
+        cx = S.Context(ds, local)
+        mark("open_upload")
+        cs = make(cx)
+        mark("create_chains")
+        a2 = (C.c_void_p * len(cs))(*[c.h for c in cs])
+        B.check(lib.vp_run(a2, len(cs), 1))
+        mark("batch_build_and_first_sweep")
+        B.check(lib.vp_run(a2, len(cs), args.e2e_sweeps - 1))
+        mark(f"next_{args.e2e_sweeps - 1}_sweeps")
+        lnl = [c.get("LNL")[0] for c in cs]
+        mark("read_lnl")
+        for c in cs:
+            c.close()
+        cx.close()
+        mark("close")
+        phases = ph
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -773,7 +803,8 @@ def main():
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "step": f"open context from pinned host buffers + create 100 chains + {args.e2e_sweeps} sweeps "
-                            f"+ read every chain's lnL + close (launch configuration from the tuner's cache)", "ms_per_step": float(np.median(e2e_ms)) if e2e_ms else None},
+                            f"+ read every chain's lnL + close (launch configuration from the tuner's cache)", "ms_per_step": float(np.median(e2e_ms)) if e2e_ms else None,
+                    "phases_ms": phases},
             "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "lnp_rel_err": lnp_err,
             "plain_form": plain, "batched_over_plain": value / plain["value"] if plain else None,
             "tuning": tuning,

@@ -77,7 +77,10 @@ void vp_dataset_free(vp_dataset* ds);
 /* ---- device context ------------------------------------------------------ */
 typedef struct vp_ctx vp_ctx;
 /* Upload the packed genotype matrix once (replaces CopyStructureMemory,
- * src/structureCUDA.cpp:969-1094, and its per-device replicas). */
+ * src/structureCUDA.cpp:969-1094, and its per-device replicas). The genotype
+ * copy runs on the context's stream after the call returns; the context holds
+ * a reference to the dataset until vp_close, and a failed copy is reported by
+ * the next call that waits for the stream. */
 int vp_open(const vp_dataset* ds, int device, vp_ctx** out);
 /* Closing a context also destroys its chains that are still open; their
  * handles are invalid afterwards. */

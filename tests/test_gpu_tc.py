@@ -153,6 +153,30 @@ def test_deferred_initial_counts_equal_plain():
         assert np.array_equal(p.get("NI"), t.get("NI"))
 
 
+def test_plain_steps_on_a_batch_chain_equal_plain_chain():
+    """A chain made for a tensor-core batch carves the plain form's likelihood
+    table and partials only on its first plain-form step; stepped in the plain
+    form it then follows a plain chain of the same seed bit for bit, also when
+    its frequencies were set before that first step."""
+    d = synth.fmodel(53, 500, 900, 3, 0.05, 0.02)
+    ds = S.Dataset.from_synth(d)
+    ctx = S.Context(ds)
+    kw = dict(admix=0, nadmburnin=0, nburnin=5, nreps=5)
+    for K in (3, 6):
+        p = S.Chain(ctx, S.params(K, 900 + K, **kw))
+        t = S.Chain(ctx, S.params(K, 900 + K, form=B.VP_FORM_TC, **kw))
+        p.step("UPDATEP")
+        t.set("FREQ", p.get("FREQ"))
+        for name in ("LOGLIK", "UPDATEQ", "UPDATEZ", "UPDATEP", "LOGLIK"):
+            p.step(name)
+            t.step(name)
+        for f in ("FREQ", "LL", "Z", "NI"):
+            assert np.array_equal(p.get(f), t.get(f)), f
+        t.close()
+        p.close()
+    ctx.close()
+
+
 TILES = [(64, 2, 192, 192), (64, 1, 288, 144), (32, 2, 192, 192)]
 
 

@@ -32,6 +32,9 @@ struct vp_ctx {
     DevData D{};
     std::vector<void*> allocs;
     std::vector<vp_chain*> chains;   // open chains: vp_close destroys those left
+    // the dataset whose pinned genotype words the upload reads: held (one
+    // reference) until vp_close, so vp_open need not wait for the copy
+    const vp_dataset* hold = nullptr;
     int64_t launches = 0;
     int32_t N = 0, S = 0, maxK = 0, maxploidy = 0, packed2 = 0;
     int64_t L = 0, KT = 0;
@@ -66,6 +69,10 @@ struct vp_chain {
     // not computed yet: a tensor-core chain leaves them to its batch, which
     // counts every chain in one count contraction
     bool counts_pending = false;
+    // a chain made for a tensor-core batch carves the plain form's likelihood
+    // table and chunk partials (lt, LLp) only on its first plain-form use
+    bool plain_lazy = false;
+    void* plain_mem = nullptr;
 };
 
 // launch configuration of a batch's two contractions: the likelihood
@@ -432,6 +439,35 @@ int ensure_counts(vp_chain* c) {
     return rc;
 }
 
+__global__ void k_set_plain(DevChain* dst, float* lt, double* LLp) {
+    dst->lt = lt;
+    dst->LLp = LLp;
+}
+
+// the plain form's scratch of a chain made for a tensor-core batch, carved on
+// its first plain-form use; the likelihood table is filled from the current
+// frequencies
+int ensure_plain(vp_chain* c) {
+    if (!c->plain_lazy || c->plain_mem) return VP_OK;
+    vp_ctx* x = c->ctx;
+    DevChain& h = c->h;
+    const int64_t ltn = x->packed2 ? x->L * 4 * h.kp : (int64_t)c->P.K * x->KT;
+    const size_t lt_bytes = ((size_t)ltn * 4 + 255) & ~(size_t)255;
+    const size_t bytes = lt_bytes + (size_t)h.nchunk * x->N * c->P.K * 8;
+    cudaError_t e = dev_alloc(&c->plain_mem, bytes, x->device, x->stream);
+    if (e != cudaSuccess) {
+        c->plain_mem = nullptr;
+        vp_set_error("device allocation of %zu bytes for the plain form failed: %s", bytes, cudaGetErrorString(e));
+        return VP_E_MEM;
+    }
+    CK(cudaMemsetAsync(c->plain_mem, 0, bytes, x->stream));
+    h.lt = (float*)c->plain_mem;
+    h.LLp = (double*)((char*)c->plain_mem + lt_bytes);
+    LAUNCH(x, k_set_plain, (1, 1, 0, x->stream), (c->d, h.lt, h.LLp));
+    LAUNCH(x, k_refresh_lt, (cdiv((int64_t)c->P.K * x->L, 256), 256, 0, x->stream), (c->d));
+    return VP_OK;
+}
+
 extern "C" int vp_open(const vp_dataset* ds, int device, vp_ctx** out) { return vp_open_ex(ds, device, 0, out); }
 
 int vp_open_ex(const vp_dataset* ds, int device, int priority, vp_ctx** out) {
@@ -458,9 +494,11 @@ int vp_open_ex(const vp_dataset* ds, int device, int priority, vp_ctx** out) {
     for (int32_t sp = 0; sp < ds->S; ++sp)
         for (int32_t j = 0; j < ds->pop_nind[sp]; ++j)
             if (ds->popid[ds->pop_ind0[sp] + j] != sp) { D.popcontig = 0; break; }
+    vp_dataset_retain(ds);
+    x->hold = ds;
+    // the small (pageable) arrays first: a copy from pageable memory may wait
+    // for the stream, which must not wait for the genotype copy
     int rc = 0;
-    if (ds->packed2) rc |= upload(x, ds->g2.data(), ds->g2.size(), &D.g2);
-    else rc |= upload(x, ds->gb.data(), ds->gb.size(), &D.gb);
     rc |= upload(x, ds->k.data(), ds->k.size(), &D.k);
     rc |= upload(x, ds->off.data(), ds->off.size(), &D.off);
     rc |= upload(x, ds->vt.data(), ds->vt.size(), &D.vt);
@@ -471,8 +509,11 @@ int vp_open_ex(const vp_dataset* ds, int device, int priority, vp_ctx** out) {
     rc |= upload(x, ds->nhaplo.data(), ds->nhaplo.size(), &D.nhaplo);
     D.perm = nullptr;
     if (!ds->perm.empty()) rc |= upload(x, ds->perm.data(), ds->perm.size(), &D.perm);
+    // the genotypes last, without a wait: chain set-up on the host overlaps
+    // the copy, and every later use of them is ordered after it on the stream
+    if (ds->packed2) rc |= upload(x, ds->g2.data(), ds->g2.size(), &D.g2);
+    else rc |= upload(x, ds->gb.data(), ds->gb.size(), &D.gb);
     if (rc) { vp_close(x); return rc < 0 ? rc : VP_E_CUDA; }
-    if (cudaStreamSynchronize(x->stream) != cudaSuccess) { vp_set_error("upload failed"); vp_close(x); return VP_E_CUDA; }
     *out = x;
     return VP_OK;
 }
@@ -490,6 +531,7 @@ extern "C" int vp_close(vp_ctx* x) {
         cudaStreamSynchronize(x->stream);
         cudaStreamDestroy(x->stream);
     }
+    if (x->hold) vp_dataset_free(const_cast<vp_dataset*>(x->hold));
     delete x;
     return VP_OK;
 }
@@ -504,6 +546,13 @@ extern "C" int64_t vp_launch_count(vp_ctx* x) { return x ? x->launches : -1; }
 
 namespace {
 // device layout of one chain's state inside its single allocation
+// chains that a tensor-core batch runs: no-admixture, no location prior, no
+// F model, counter streams, 2-bit data
+bool tc_batchable(const vp_ctx* x, const vp_params* P, const DevChain& h) {
+    return P->form == VP_FORM_TC && x->packed2 && !P->locpriori && !P->fmodel && P->rng == VP_RNG_COUNTER &&
+           h.nadmburnin == 0 && !P->admix;
+}
+
 void chain_layout(Carve& cv, vp_chain* c, const vp_ctx* x) {
     DevChain& h = c->h;
     const vp_params* P = &c->P;
@@ -516,7 +565,7 @@ void chain_layout(Carve& cv, vp_chain* c, const vp_ctx* x) {
     h.Freq = cv.take<float>(K * KT);
     h.FreqM = cv.take<float>(K * KT);
     h.FreqA = cv.take<float>(P->fmodel ? KT : 1);
-    h.lt = cv.take<float>(ltn);
+    h.lt = c->plain_lazy ? nullptr : cv.take<float>(ltn);
     h.Q = cv.take<float>((int64_t)N * K);
     h.Qprop = cv.take<float>((int64_t)N * K);
     h.Di = cv.take<float>((int64_t)S * K);
@@ -525,7 +574,7 @@ void chain_layout(Carve& cv, vp_chain* c, const vp_ctx* x) {
     h.Mi = cv.take<int32_t>((int64_t)N * K);
     h.Ni = cv.take<int32_t>(K * KT);
     h.MiSum = cv.take<int64_t>((int64_t)N * K);
-    h.LLp = cv.take<double>((int64_t)h.nchunk * N * K);
+    h.LLp = c->plain_lazy ? nullptr : cv.take<double>((int64_t)h.nchunk * N * K);
     h.LL = cv.take<double>((int64_t)N * K);
     h.metro = cv.take<double>(N);
     // Metropolis partials: one per locus range of the per-copy kernels
@@ -605,6 +654,7 @@ int chain_plan(const vp_ctx* x, const vp_params* P, vp_chain* c, size_t* bytes) 
     }
     h.nlnlp = (int32_t)std::max<int64_t>(std::max<int64_t>(cdiv(L, 128), (int64_t)cdiv(N, ZA_WARPS * 32) * cdiv(L, h.zadm_lc)),
                                          h.nsampblk);
+    c->plain_lazy = tc_batchable(x, P, h);
     Carve probe{nullptr};
     chain_layout(probe, c, x);
     *bytes = probe.off;
@@ -662,9 +712,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
         if (singlez) {
             k_init_z_single<<<P->rng ? cdiv(N, 256) : 1, P->rng ? 256 : 32, 0, s>>>(c->d);
             if ((rc = check_launch(x, "k_init_z_single"))) break;
-            const bool batched = P->form == VP_FORM_TC && x->packed2 && !P->locpriori && !P->fmodel &&
-                                 P->rng == VP_RNG_COUNTER;
-            if (batched) {
+            if (c->plain_lazy) {
                 c->counts_pending = true;
                 break;
             }
@@ -699,6 +747,7 @@ extern "C" int vp_chain_destroy(vp_chain* c) {
             break;
         }
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    dev_free(c->plain_mem, c->ctx->stream);
     dev_free(c->mem, c->ctx->stream);   // after every launch already queued for the chain
     auto& open = c->ctx->chains;
     open.erase(std::remove(open.begin(), open.end(), c), open.end());
@@ -745,8 +794,10 @@ extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
         for (int i = 0; i < n; ++i) cs[i]->issued += step;
         return VP_OK;
     }
-    for (int i = 0; i < n; ++i)
+    for (int i = 0; i < n; ++i) {
         if (int rc0 = ensure_counts(cs[i])) return rc0;
+        if (int rc0 = ensure_plain(cs[i])) return rc0;
+    }
     // chains with sweeps left; a set of chains whose sweeps are all still
     // pending shares one cached graph of a sweep
     int left = nsweeps;
@@ -943,7 +994,7 @@ extern "C" int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t
     if (rc) return rc;
     if (bytes != n) { vp_set_error("field %d holds %zu bytes, not %zu", field, n, bytes); return VP_E_ARG; }
     CK(cudaMemcpy(p, host, n, cudaMemcpyHostToDevice));
-    if (field == VP_F_FREQ) {
+    if (field == VP_F_FREQ && c->h.lt) {
         // keep the likelihood lookup table in step with the frequencies
         vp_ctx* x = c->ctx;
         k_refresh_lt<<<cdiv((int64_t)c->P.K * x->L, 256), 256, 0, x->stream>>>(c->d);
@@ -958,6 +1009,7 @@ extern "C" int vp_chain_step(vp_chain* c, int32_t step) {
     if (!c) { vp_set_error("null chain"); return VP_E_ARG; }
     cudaSetDevice(c->ctx->device);
     int rc = ensure_counts(c);
+    if (!rc) rc = ensure_plain(c);
     if (rc) return rc;
     rc = launch_step(c, step, 0);
     if (rc) return rc;
