@@ -287,10 +287,20 @@ int launch_metro_ratio(vp_chain* c, int force) {
     return VP_E_ARG;
 }
 
-void set_smem_limits() {
-    static bool done = false;
-    if (done) return;
-    done = true;
+// true the first time it is called for a device (kernel attributes belong to
+// each device's context); safe from several host threads
+bool first_on_device(std::mutex& mu, std::vector<char>& seen, int device) {
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)seen.size() <= device) seen.resize(device + 1, 0);
+    if (seen[device]) return false;
+    seen[device] = 1;
+    return true;
+}
+
+void set_smem_limits(int device) {
+    static std::mutex mu;
+    static std::vector<char> seen;
+    if (!first_on_device(mu, seen, device)) return;
     const int big = 200 * 1024;
     cudaFuncSetAttribute(k_count_noadmix, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_count_packed<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -686,7 +696,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
     size_t bytes = 0;
     int prc = chain_plan(x, P, c, &bytes);
     if (prc) { delete c; return prc; }
-    set_smem_limits();
+    set_smem_limits(x->device);
     const int K = P->K, N = x->N;
     const int64_t L = x->L;
     DevChain& h = c->h;
@@ -947,7 +957,9 @@ static int field_ptr(vp_chain* c, int f, void** p, size_t* bytes) {
         case VP_F_M: *p = &h.ctl->m; *bytes = 4; return VP_OK;
         case VP_F_LNL: *p = &h.ctl->lnl; *bytes = 8; return VP_OK;
         case VP_F_FREQA: *p = h.FreqA; *bytes = c->P.fmodel ? KT * 4 : 0; return VP_OK;
-        case VP_F_FF: *p = h.f; *bytes = 2 * K * 8; return VP_OK;  // f and F are adjacent 256-aligned? no
+        // f[K] then F[K]: two separate allocations, copied one by one in
+        // vp_chain_get / vp_chain_set
+        case VP_F_FF: *p = h.f; *bytes = 2 * K * 8; return VP_OK;
         case VP_F_DI: *p = h.Di; *bytes = S * K * 4; return VP_OK;
         case VP_F_METRO: *p = h.metro; *bytes = N * 8; return VP_OK;
     }
@@ -1024,14 +1036,14 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 EncodeTiledFn encode_fn() {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    static const EncodeTiledFn fn = [] {
         cudaDriverEntryPointQueryResult q;
         void* p = nullptr;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (EncodeTiledFn)p;
-    }
+            return (EncodeTiledFn)p;
+        return (EncodeTiledFn) nullptr;
+    }();
     return fn;
 }
 
@@ -1061,11 +1073,10 @@ template <int BKT, int ESZ, int MT, int NB, int BNT, int PIECE>
 int launch_gemm_t(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const CUtensorMap& B1, const tc::GemmArgs& g,
                   dim3 grid, size_t sm) {
     auto kern = tc::k_gemm_bf16<BKT, ESZ, MT, NB, BNT, PIECE>;
-    static bool attr = false;
-    if (!attr) {
+    static std::mutex mu;
+    static std::vector<char> seen;
+    if (first_on_device(mu, seen, x->device))
         CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-        attr = true;
-    }
     kern<<<grid, tc::NTHREADS, sm, x->stream>>>(A, B0, B1, g);
     return check_launch(x, "k_gemm_bf16");
 }
@@ -1417,9 +1428,11 @@ int launch_tc_sweep(vp_ctx* x) {
     // waves of the kernel's resident blocks
     unsigned upx = 1;
     {
-        static int per_sm = 0;
-        if (!per_sm && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::k_update_p_tc, 256, 0) != cudaSuccess)
-            per_sm = 4;
+        static const int per_sm = [] {
+            int v = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, tc::k_update_p_tc, 256, 0) != cudaSuccess || v < 1) v = 4;
+            return v;
+        }();
         const double slots = (double)x->nsm * std::max(1, per_sm);
         const unsigned hi = std::max<unsigned>(1, std::min<unsigned>(16, cdiv(x->L, 256)));
         double best = -1;
