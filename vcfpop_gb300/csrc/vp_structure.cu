@@ -709,13 +709,18 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
     Carve cv{(char*)c->mem};
     chain_layout(cv, c, x);
     c->own_ni = h.Ni;
-    CK(cudaMemsetAsync(c->mem, 0, bytes, x->stream));
-    LAUNCH(x, k_set_chain, (1, 128, 0, x->stream), (c->d, h));
     c->total = h.nburnin + h.nreps;
     // InitFix / InitAdmix / InitLocPriori / InitFmodel
     cudaStream_t s = x->stream;
     int rc = VP_OK;
     do {
+        if ((e = cudaMemsetAsync(c->mem, 0, bytes, s)) != cudaSuccess) {
+            vp_set_error("cudaMemsetAsync of chain state failed: %s", cudaGetErrorString(e));
+            rc = VP_E_CUDA;
+            break;
+        }
+        k_set_chain<<<1, 128, 0, s>>>(c->d, h);
+        if ((rc = check_launch(x, "k_set_chain"))) break;
         k_init_state<<<dim3(std::min<unsigned>(1024, cdiv(std::max<int64_t>(L, (int64_t)N * K), 256)), 1, 1), 256, 0, s>>>(c->d);
         if ((rc = check_launch(x, "k_init_state"))) break;
         const bool singlez = h.nadmburnin == 0 && !P->admix;
@@ -1362,10 +1367,20 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n, const TcChoice* force) {
     if (e != cudaSuccess) { delete b; vp_set_error("device allocation of %zu bytes for the batch: %s", probe.off, cudaGetErrorString(e)); return VP_E_MEM; }
     Carve cv{(char*)b->mem};
     lay(cv);
-    CK(cudaMemsetAsync(b->mem, 0, probe.off, x->stream));
-    CK(cudaMemcpyAsync(b->rowchain, rowchain.data(), rowchain.size() * 4, cudaMemcpyHostToDevice, x->stream));
-    CK(cudaMemcpyAsync(b->rowk, rowk.data(), rowk.size() * 4, cudaMemcpyHostToDevice, x->stream));
-    CK(cudaMemcpyAsync(b->row0, row0.data(), row0.size() * 4, cudaMemcpyHostToDevice, x->stream));
+    // a failure before the chains' device headers are rewritten leaves the
+    // chains as they were
+    auto undo = [&](const char* what, cudaError_t err) {
+        for (int i = 0; i < n; ++i) cs[i]->h.Ni = cs[i]->own_ni;
+        dev_free(b->mem, x->stream);
+        delete b;
+        vp_set_error("%s failed: %s", what, cudaGetErrorString(err));
+        return VP_E_CUDA;
+    };
+    if ((e = cudaMemsetAsync(b->mem, 0, probe.off, x->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b->rowchain, rowchain.data(), rowchain.size() * 4, cudaMemcpyHostToDevice, x->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b->rowk, rowk.data(), rowk.size() * 4, cudaMemcpyHostToDevice, x->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b->row0, row0.data(), row0.size() * 4, cudaMemcpyHostToDevice, x->stream)) != cudaSuccess)
+        return undo("batch upload", e);
     // the batch's count contraction writes every chain's Ni inside NiAll
     // (counts still pending are computed there below); the chains' device
     // headers are updated by one upload and a scatter kernel
@@ -1374,16 +1389,21 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n, const TcChoice* force) {
     for (int i = 0; i < n; ++i) {
         vp_chain* c = cs[i];
         int32_t* dst = b->NiAll + (int64_t)row0[i] * x->KT;
-        if (!c->counts_pending)
-            CK(cudaMemcpyAsync(dst, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice, x->stream));
+        if (!c->counts_pending &&
+            (e = cudaMemcpyAsync(dst, c->h.Ni, (size_t)c->P.K * x->KT * 4, cudaMemcpyDeviceToDevice, x->stream)) != cudaSuccess)
+            return undo("copy of a chain's counts into the batch", e);
         c->h.Ni = dst;
         hc[i] = c->h;
         hp[i] = c->d;
-        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     }
-    CK(cudaMemcpyAsync(b->dchains, hc.data(), n * sizeof(DevChain), cudaMemcpyHostToDevice, x->stream));
-    CK(cudaMemcpyAsync(b->dptrs, hp.data(), n * sizeof(DevChain*), cudaMemcpyHostToDevice, x->stream));
-    LAUNCH(x, k_scatter_chains, (n, 128, 0, x->stream), (b->dchains, b->dptrs, n));
+    if ((e = cudaMemcpyAsync(b->dchains, hc.data(), n * sizeof(DevChain), cudaMemcpyHostToDevice, x->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b->dptrs, hp.data(), n * sizeof(DevChain*), cudaMemcpyHostToDevice, x->stream)) != cudaSuccess)
+        return undo("batch header upload", e);
+    k_scatter_chains<<<n, 128, 0, x->stream>>>(b->dchains, b->dptrs, n);
+    x->launches++;
+    if ((e = cudaGetLastError()) != cudaSuccess) return undo("launch of k_scatter_chains", e);
+    for (int i = 0; i < n; ++i)
+        if (cs[i]->graph) { cudaGraphExecDestroy(cs[i]->graph); cs[i]->graph = nullptr; }
     if ((rc = make_map(&b->mapC1, t.C, t.Npad, t.Apad, t.Apad, 128, b->cfg.bk1)) ||
         (rc = make_map(&b->mapWhi, b->Whi, b->Rpad, t.Apad, t.Apad, b->cfg.piece1, b->cfg.bk1)) ||
         (rc = make_map(&b->mapWlo, b->Wlo, b->Rpad, t.Apad, t.Apad, b->cfg.piece1, b->cfg.bk1)) ||
