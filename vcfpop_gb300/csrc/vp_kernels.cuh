@@ -80,6 +80,16 @@ __device__ T block_sum(T v, T* sh) {
     return r;  // valid in thread 0
 }
 
+// the sum of n per-block partials by a whole block (thread j adds partials j,
+// j + blockDim.x, ..., then one block reduction): the last block of a grid
+// uses it instead of one thread walking every partial through a chain of
+// dependent loads. Same order on every launch of a grid; valid in thread 0.
+__device__ __forceinline__ double block_sum_partials(const double* p, int n, double* sh) {
+    double v = 0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) v += p[j];
+    return block_sum(v, sh);
+}
+
 // ---------------------------------------------------------------------------
 // initialisation: InitFix (src/structure.cpp:466-553), InitLocPriori (651-675),
 // InitFmodel (677-708)
@@ -551,9 +561,8 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain*
         double t = block_sum(lane == 0 ? lnl : 0.0, sh);
         if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
         if (!last_block_done(c.ctl, gridDim.x)) return;
+        const double tot = block_sum_partials(c.lnlp, gridDim.x, sh);
         if (threadIdx.x == 0) {
-            double tot = 0;
-            for (int b = 0; b < (int)gridDim.x; ++b) tot += c.lnlp[b];
             c.ctl->lnl = tot;
             c.ctl->done = 0;
         }
@@ -1681,11 +1690,8 @@ __global__ void k_record_sweep(const DevChain* chains, double* exact) {
     }
     if (!last_block_done(c.ctl, gridDim.x)) return;
     if (rec && exact) {
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int q = 0; q < (int)gridDim.x; ++q) t += exact[(int64_t)blockIdx.z * gridDim.x + q];
-            c.ctl->lnl = t;
-        }
+        const double t = block_sum_partials(exact + (int64_t)blockIdx.z * gridDim.x, gridDim.x, sh);
+        if (threadIdx.x == 0) c.ctl->lnl = t;
         __syncthreads();
     }
     record_scalars(c, m, sh);

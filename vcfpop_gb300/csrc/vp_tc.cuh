@@ -603,9 +603,8 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_tc(BatchDev b) {
     double t = block_sum(lnl, sh);
     if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
     if (!last_block_done(c.ctl, gridDim.x)) return;
+    const double tot = block_sum_partials(c.lnlp, gridDim.x, sh);
     if (threadIdx.x == 0) {
-        double tot = 0;
-        for (int bb = 0; bb < (int)gridDim.x; ++bb) tot += c.lnlp[bb];
         c.ctl->lnl = tot;
         c.ctl->done = 0;
     }
