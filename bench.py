@@ -701,6 +701,26 @@ def main():
                 "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback", "traffic": None}
     roof["avg_launch_ms"] = dom_avg_ms
+    # the batched UpdateP of the same sweeps: Dirichlet draws per second, from
+    # CUDA events around its launch inside the sweep graph (after the timed
+    # steps; the chains run a few more of their sweeps)
+    updatep = None
+    if form == B.VP_FORM_TC:
+        lib.vp_prof_enable(ctx.h, 2)
+        up_ms = []
+        for it in range(4):
+            B.check(lib.vp_run(arr, len(chains), 1))
+            B.check(lib.vp_prof_read(ctx.h, C.byref(ms), C.byref(nl)))
+            if it:
+                up_ms.append(ms.value / max(nl.value, 1))
+        lib.vp_prof_enable(ctx.h, 1)
+        draws = sumK * ds.KT
+        up = float(np.median(up_ms))
+        # algorithmic bytes: Ni read, Freq and the two W rows written (4 bytes each per draw, W 2 + 2)
+        up_bytes = draws * (4 + 4 + 2 + 2)
+        updatep = {"kernel": "tc::k_update_p_tc", "gamma_draws_per_sweep": draws, "avg_launch_ms": up,
+                   "draws_per_s": draws / (up / 1e3), "gbs": up_bytes / (up / 1e3) / 1e9,
+                   "bound": "instruction issue (Philox-4x32-10 block + two Marsaglia-Tsang gammas per biallelic locus)"}
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tfile):
         try:
@@ -807,7 +827,7 @@ def main():
                     "phases_ms": phases},
             "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "lnp_rel_err": lnp_err,
             "plain_form": plain, "batched_over_plain": value / plain["value"] if plain else None,
-            "tuning": tuning,
+            "tuning": tuning, "updatep": updatep,
             "outputs": outputs, "ingest": ingest, "locus_filter": lfilter}
     if rank == 0:
         print(json.dumps(line), flush=True)

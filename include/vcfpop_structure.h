@@ -288,12 +288,13 @@ int vp_release_memory(int device);
 
 /* The CUDA stream (cudaStream_t) every launch of this context goes to. */
 void* vp_stream(vp_ctx* ctx);
-/* Record CUDA events around each launch of the sweep's dominant kernel (the
- * likelihood stream of the plain no-admixture form, the per-copy label kernel
- * of the admixture form, the likelihood contraction of the tensor-core form),
- * also inside the cached sweep graphs. */
+/* on = 1: record CUDA events around each launch of the sweep's dominant
+ * kernel (the likelihood stream of the plain no-admixture form, the per-copy
+ * label kernel of the admixture form, the likelihood contraction of the
+ * tensor-core form), also inside the cached sweep graphs; on = 2: around the
+ * tensor-core form's batched UpdateP instead; 0: off. */
 int vp_prof_enable(vp_ctx* ctx, int on);
-/* Synchronise, then sum the dominant-kernel durations of the last sweep. */
+/* Synchronise, then sum the profiled kernel's durations of the last sweep. */
 int vp_prof_read(vp_ctx* ctx, double* ms, int32_t* launches);
 
 /* ---- VCF ingest on the device ---------------------------------------------

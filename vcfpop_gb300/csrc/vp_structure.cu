@@ -184,9 +184,11 @@ int upload(vp_ctx* ctx, const T* host, size_t n, const T** dev) {
 
 inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
-// begin/end markers around one launch of the dominant kernel
-void prof_mark(vp_ctx* x, bool begin) {
-    if (!x->prof) return;
+// begin/end markers around one launch of the profiled kernel: the dominant
+// kernel (profiling mode 1) or the tensor-core form's UpdateP (mode 2)
+enum { PROF_DOMINANT = 1, PROF_UPDATEP_TC = 2 };
+void prof_mark(vp_ctx* x, bool begin, int kind = PROF_DOMINANT) {
+    if (x->prof != kind) return;
     int idx = x->prof_next * 2 + (begin ? 0 : 1);
     while ((int)x->prof_ev.size() <= idx) {
         cudaEvent_t e;
@@ -1461,7 +1463,9 @@ int launch_tc_sweep(vp_ctx* x) {
             if (eff > best + 0.01) { best = eff; upx = u; }
         }
     }
+    prof_mark(x, true, PROF_UPDATEP_TC);
     LAUNCH(x, tc::k_update_p_tc, (dim3(upx, b->R, 1), 256, 0, s), (bd));
+    prof_mark(x, false, PROF_UPDATEP_TC);
     // likelihood contraction: LL'[i, row] = sum_a C[i,a] (Whi + Wlo)[row, a]
     {
         prof_mark(x, true);
@@ -1994,6 +1998,7 @@ extern "C" int vp_release_memory(int device) {
 
 extern "C" int vp_prof_enable(vp_ctx* x, int on) {
     if (!x) { vp_set_error("null context"); return VP_E_ARG; }
+    if (on < 0 || on > PROF_UPDATEP_TC) { vp_set_error("profiling mode %d: 0, 1 or 2", on); return VP_E_ARG; }
     if (x->prof == on) return VP_OK;
     x->prof = on;
     // cached graphs were captured with or without the markers: re-capture
