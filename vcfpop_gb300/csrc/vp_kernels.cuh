@@ -101,13 +101,10 @@ __global__ void k_init_state(const DevChain* chains) {
     for (int64_t l = tid; l < D.L; l += nt) {
         int k2 = D.k[l];
         float v = k2 == 2 ? 0.5f : (float)(1.0 / k2);
+        // the chain's memory was zeroed when it was allocated: FreqM, Ni,
+        // Mi, MiSum and Z start at zero without a store here
         for (int k = 0; k < K; ++k)
-            for (int a = 0; a < k2; ++a) {
-                int64_t j = k * D.KT + D.off[l] + a;
-                c.Freq[j] = c.fmodel ? (float)c.lambda : v;
-                c.FreqM[j] = 0.f;
-                c.Ni[j] = 0;
-            }
+            for (int a = 0; a < k2; ++a) c.Freq[k * D.KT + D.off[l] + a] = c.fmodel ? (float)c.lambda : v;
         if (c.fmodel) {
             // the total-population frequencies are laid out in pre-sort order but
             // read with this (sorted) locus' offset and index, as in the reference
@@ -117,12 +114,7 @@ __global__ void k_init_state(const DevChain* chains) {
                 c.FreqA[D.off[l] + a] = (float)((c.lambda + p2[a] * nh) / (k2 * c.lambda + nh));
         }
     }
-    for (int64_t j = tid; j < (int64_t)D.N * K; j += nt) {
-        c.Q[j] = (float)(1.0 / K);
-        c.Mi[j] = 0;
-        c.MiSum[j] = 0;
-    }
-    for (int64_t i = tid; i < D.N; i += nt) c.Z[i] = 0;
+    for (int64_t j = tid; j < (int64_t)D.N * K; j += nt) c.Q[j] = (float)(1.0 / K);
     if (tid < K) {
         c.Alpha[tid] = c.alpha;
         c.Lambda[tid] = c.lambda;
