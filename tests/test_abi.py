@@ -125,3 +125,65 @@ def test_wait_timeout_diagnostic_without_gpu_fails_loudly():
     st, after, err = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_double(0)
     assert B.lib().vp_debug_gemm_wait_timeout(ctypes.byref(st), ctypes.byref(after), ctypes.byref(err)) != 0
     assert "no CUDA device" in B.lib().vp_last_error().decode()
+
+
+class _RecordingLib:
+    """Stands in for the library: records close/destroy calls by handle."""
+
+    def __init__(self):
+        self.calls = []
+
+    def vp_close(self, h):
+        self.calls.append(("close", h))
+        return 0
+
+    def vp_chain_destroy(self, h):
+        self.calls.append(("destroy", h))
+        return 0
+
+
+def _wrappers(n_chains):
+    ctx = S.Context.__new__(S.Context)
+    ctx.h = 100
+    chains = []
+    for j in range(n_chains):
+        ch = S.Chain.__new__(S.Chain)
+        ch.h, ch.ctx = 200 + j, ctx
+        chains.append(ch)
+    return ctx, chains
+
+
+@pytest.mark.parametrize("context_first", [True, False])
+def test_chain_wrappers_never_destroy_after_their_context_closed(monkeypatch, context_first):
+    """The library's vp_close destroys a context's open chains, so a chain
+    wrapper closed after its context must not call vp_chain_destroy on the
+    freed chain; closed first, it destroys it as usual."""
+    fake = _RecordingLib()
+    monkeypatch.setattr(B, "lib", lambda: fake)
+    ctx, chains = _wrappers(2)
+    order = [ctx] + chains if context_first else chains + [ctx]
+    for o in order:
+        o.close()
+        o.close()                              # idempotent
+    expect = [("close", 100)] if context_first else [("destroy", 200), ("destroy", 201), ("close", 100)]
+    assert fake.calls == expect
+    assert ctx.h is None and all(c.h is None for c in chains)
+
+
+def test_collected_reference_cycle_never_destroys_after_close(monkeypatch):
+    """A failing test's traceback can hold a context and its chains in one
+    reference cycle; the collector then runs their finalisers in any order.
+    Whatever the order, no chain is destroyed after its context closed."""
+    import gc
+    fake = _RecordingLib()
+    monkeypatch.setattr(B, "lib", lambda: fake)
+    ctx, chains = _wrappers(3)
+    box = {"ctx": ctx, "chains": chains}
+    box["self"] = box                          # the cycle
+    ctx.cycle = box
+    del ctx, chains, box
+    gc.collect()
+    names = [c[0] for c in fake.calls]
+    assert names.count("close") == 1
+    closed_at = names.index("close")
+    assert "destroy" not in names[closed_at:]
