@@ -3,7 +3,8 @@
  * hashing, random-number and log-product primitives used by its STRUCTURE path.
  *
  * Nothing in the product links this file. Only tests/, __graft_entry__.smoke()
- * and bench.py's CPU-baseline leg call it, as the checker.
+ * and bench.py's CPU-baseline leg call it, to check and time the GPU library
+ * against it.
  *
  * Each function names the reference file:line it restates (vcfpop v1.08b,
  * paths relative to the project's src/ folder). Arithmetic follows the

@@ -1,8 +1,8 @@
 """ctypes handle on the oracle (oracle/_build/liborc.so): test infrastructure.
 
 The oracle is the CPU restatement of the reference's STRUCTURE path, pinned
-byte-for-byte to the reference program by tests/test_oracle_golden.py. Tests use
-it as the checker for the GPU library, never the other way round.
+byte-for-byte to the reference program by tests/test_oracle_golden.py. Tests
+compare the GPU library against it, never the other way round.
 """
 import ctypes as C
 import os
