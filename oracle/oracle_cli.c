@@ -185,8 +185,10 @@ int main(int argc, char** argv) {
     orc_owned_data* od = orc_data_build(N, L, vmax, G, ploidy, k, popid, pops.n);
     const orc_data* D = orc_data_view(od);
     const int64_t* order = orc_data_order(od);
-    char** lsorted = malloc(sizeof(char*) * L);
-    for (int64_t l = 0; l < L; ++l) lsorted[l] = locs.names[order[l]];
+    /* order[] has one entry per locus kept by the monomorphic filter:
+     * sorted position -> input locus */
+    char** lsorted = malloc(sizeof(char*) * (size_t)(D->L > 0 ? D->L : 1));
+    for (int64_t l = 0; l < D->L; ++l) lsorted[l] = locs.names[order[l]];
     int total = (kmax - kmin + 1) * nruns, id = 0;
     double* res = calloc(total * 3, sizeof(double));
     int* rk = calloc(total, sizeof(int)); int* rr = calloc(total, sizeof(int));

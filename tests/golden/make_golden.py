@@ -6,7 +6,9 @@ thread and the scalar math path. The per-run output files it writes are stored
 next to the VCF; ``tests/test_oracle_golden.py`` checks that the oracle
 restatement reproduces them byte for byte.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [case ...]
+With case names, only those cases are run (their VCF is written if missing)
+and merged into cases.json; the other fixtures stay as they are.
 """
 import gzip
 import json
@@ -37,7 +39,11 @@ def datasets():
     poly = synth.fmodel(3, 120, 300, 3, 0.08, 0.03, ploidy=np.array([2, 2, 4, 6] * 30),
                         n_alleles=np.random.default_rng(0).integers(2, 9, 300), anc_alpha=1.0,
                         loc_ids=ids, loc_alpha=1.0)
+    # 7 individuals, one of them without a single typed call
+    tiny = synth.fmodel(4, 7, 60, 2, 0.1, 0.05)
+    tiny["G"][:, 3, :] = -1
     return {
+        "tiny": (tiny, synth.indtext(tiny["pop"])),
         "c1": (c1, synth.indtext(c1["pop"])),
         "adm": (adm, "popA:#1-#60 popB:#61-#120"),
         "poly": (poly, synth.indtext(ids)),
@@ -68,6 +74,16 @@ CASES = {
                                          "-structure_singlef=yes", "-structure_nadmburnin=10",
                                          "-structure_krange=[2,2]", "-structure_nburnin=20",
                                          "-structure_nreps=40"]),
+    # edge cases: one cluster; a handful of individuals, one untyped; the
+    # general genotype layout without location prior or F model
+    "c1_k1": ("c1", 11, ["-structure_krange=[1,2]", "-structure_nburnin=10", "-structure_nreps=20",
+                         "-structure_nadmburnin=0", "-structure_admix=no", "-structure_nthinning=3"]),
+    "tiny_noadmix": ("tiny", 12, ["-structure_krange=[1,3]", "-structure_nburnin=10", "-structure_nreps=20",
+                                  "-structure_nadmburnin=0", "-structure_admix=no"]),
+    "tiny_admix": ("tiny", 13, ["-structure_admix=yes", "-structure_krange=[2,2]", "-structure_nburnin=10",
+                                "-structure_nreps=20"]),
+    "poly_noadmix": ("poly", 14, ["-structure_admix=no", "-structure_krange=[2,2]", "-structure_nburnin=10",
+                                  "-structure_nreps=20", "-structure_nadmburnin=5"]),
     # the locus filter (-f_filter with diversity windows) and the per-locus
     # diversity table, which lists the loci that survive; checked by the
     # filter tests rather than by a whole-file comparison with the oracle
@@ -77,12 +93,14 @@ CASES = {
 }
 
 
-def main():
+def main(only=None):
     if not os.path.exists(REF):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"])
     data = datasets()
     for name, (d, ind) in data.items():
         path = os.path.join(HERE, f"{name}.vcf.gz")
+        if only and (os.path.exists(path) or all(CASES[c][0] != name for c in only)):
+            continue
         with tempfile.NamedTemporaryFile("w", suffix=".vcf", delete=False) as t:
             tmp = t.name
         synth.write_vcf(tmp, d)
@@ -90,7 +108,12 @@ def main():
             shutil.copyfileobj(fi, fo)
         os.unlink(tmp)
     manifest = {}
+    if only:
+        with open(os.path.join(HERE, "cases.json")) as f:
+            manifest = json.load(f)
     for case, (dname, seed, flags) in CASES.items():
+        if only and case not in only:
+            continue
         out = os.path.join(HERE, case)
         if os.path.isdir(out):
             shutil.rmtree(out)
@@ -117,4 +140,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)
