@@ -57,6 +57,25 @@ def test_dataset_prepare_matches_oracle_polyploid():
     assert ds.KT == int(od.field(1, np.int32).sum())
 
 
+@pytest.mark.parametrize("packed", [True, False])
+def test_dataset_prepare_matches_oracle_with_filtered_loci(packed):
+    """Seven individuals, one without a typed call: many loci are monomorphic
+    and dropped, so the sort order maps over the kept loci only; the library's
+    order (input indices), allele counts and offsets equal the oracle's."""
+    d = synth.fmodel(4, 7, 60, 2, 0.1, 0.05)
+    d["G"][:, 3, :] = -1
+    ds, od = _compare_dataset(d, packed)
+    assert 0 < ds.L < 60
+    order = ds.order()
+    assert len(np.unique(order)) == ds.L and order.max() < 60
+    k_or = od.field(1, np.int32)
+    assert ds.KT == int(k_or.sum())
+    # every kept locus is polymorphic among the typed calls
+    for l in order:
+        g = d["G"][l][d["G"][l][:, 0] >= 0]
+        assert len(np.unique(g)) > 1
+
+
 def test_dataset_rejects_bad_input():
     with pytest.raises(B.VpError):
         S.Dataset(np.array([2, 2], np.int32), np.array([2], np.int32), np.array([1, 0], np.int32), 2,
