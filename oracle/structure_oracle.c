@@ -234,7 +234,13 @@ static void init_fix(orc_chain* c) {
     int nl = c->P.difflambda ? K : 1;
     c->rlen = c->P.locpriori ? 4 + nl + 1 + K + K * c->S + nf : 4 + nl + na + nf;
     c->rout = NEW(double, c->rlen);
-    if (c->P.writelnl) { c->lnL = NEW(double, c->nburnin / c->nthinning + c->nreps / c->nthinning + 1); c->nlnL = 0; }
+    /* Record writes at m % nthinning == 0 in burn-in and every nthinning-th
+     * sweep after it: ceil(nburnin / t) + ceil(nreps / t) values */
+    if (c->P.writelnl) {
+        const int t = c->nthinning;
+        c->lnL = NEW(double, (c->nburnin + t - 1) / t + (c->nreps + t - 1) / t + 1);
+        c->nlnL = 0;
+    }
     for (int64_t l = 0; l < c->L; ++l) {
         int k2 = c->D->k[l];
         if (k2 == 2) continue;
