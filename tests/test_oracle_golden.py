@@ -146,3 +146,35 @@ def test_oracle_record_lnl_is_counts_times_log_frequencies(oracle_build):
             ni, p = oc.get("NI").astype(np.float64), oc.get("FREQ").astype(np.float64)
             want = float(np.sum(ni[ni > 0] * np.log(p[ni > 0])))
             assert abs(got - want) <= 1e-12 * abs(want), (K, got, want)
+
+
+SANITIZED = ["c1_k1", "tiny_noadmix", "tiny_admix", "poly_noadmix", "adm_admix"]
+
+
+def test_oracle_driver_runs_clean_under_sanitizers(tmp_path):
+    """The oracle's driver built with AddressSanitizer and UBSan, on the golden
+    cases that stress its bookkeeping (loci dropped by the monomorphic filter,
+    thinning that does not divide the run, K = 1, admixture): no memory or
+    undefined-behaviour error, and the same files as the reference."""
+    src = os.path.join(os.path.dirname(HERE), "oracle")
+    exe = str(tmp_path / "orc_cli_san")
+    r = subprocess.run(["gcc", "-O1", "-g", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math",
+                        "-fsanitize=address,undefined", "-fno-sanitize-recover=all", "-w", "-o", exe,
+                        os.path.join(src, "oracle_cli.c"), os.path.join(src, "structure_oracle.c"), "-lm", "-lpthread"],
+                       capture_output=True)
+    if r.returncode:
+        pytest.skip("no sanitizer runtime for gcc here")
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
+    for case in SANITIZED:
+        c = CASES[case]
+        w = tmp_path / case
+        w.mkdir()
+        with gzip.open(os.path.join(GOLD, c["data"]), "rb") as fi, open(w / "data.vcf", "wb") as fo:
+            shutil.copyfileobj(fi, fo)
+        r = subprocess.run([exe, f"-g_input={w / 'data.vcf'}", f"-g_output={w}/out", f"-g_seed={c['seed']}",
+                            "-g_decimal=15", f"-g_indtext={c['indtext']}", "-structure_writelnl=yes"] + c["flags"],
+                           capture_output=True, text=True, env=env, timeout=600)
+        assert r.returncode == 0, f"{case}: {r.stderr[:2000]}"
+        for f in c["files"]:
+            if f != "out.structure.txt":
+                assert open(w / f, "rb").read() == open(os.path.join(GOLD, case, f), "rb").read(), f"{case}/{f}"
