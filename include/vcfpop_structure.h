@@ -178,6 +178,9 @@ int vp_chain_divergence(vp_chain* c, double* H, double* D, double* Hl);
 #define VP_F_LOCP 12    /* double: r, Eta[K], Gamma[S*K], AlphaLocal[S*K], SumAlpha[S] */
 #define VP_F_DI 13      /* float [S*K] */
 #define VP_F_METRO 14   /* double [N] last Metropolis log ratio */
+/* One step at the chain's current sweep index m; VP_E_STATE once m has
+ * reached nburnin (+ admixture burn-in) + nreps. vp_chain_set(VP_F_M) takes
+ * indices 0..nburnin + nreps only. */
 int vp_chain_step(vp_chain* c, int32_t step);
 int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes);
 int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t bytes);
@@ -276,7 +279,10 @@ int vp_loglik_packed2(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const 
  * sizes whose table and partial sums need more are rejected with VP_E_ARG.
  * The first call on a device looks the array's device address up (once per
  * device, with that device current); make that first call before any stream
- * capture. All calls share the array: calls that overlap on the GPU race. */
+ * capture. The address is kept for the life of the process: after a
+ * cudaDeviceReset (or anything else that destroys the device's primary
+ * context) this entry point must not be called again in that process.
+ * All calls share the array: calls that overlap on the GPU race. */
 int vp_loglik_packed2_noalloc(const uint32_t* geno, int32_t n_ind, int64_t n_loc, const float* freq, int32_t K,
                               double* ll, void* stream);
 

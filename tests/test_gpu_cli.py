@@ -95,3 +95,37 @@ def test_cli_tensor_core_form_writes_the_reference_files(tmp_path):
     pl = [float(x) for x in NUM.findall(open(tmp_path / "plain" / f).read())]
     assert len(tc) == len(pl) > 0
     assert abs(tc[0] - pl[0]) <= 1e-5 * abs(pl[0]), (tc[0], pl[0])
+
+
+def test_cli_default_flags_run_the_tensor_core_batch(tmp_path):
+    """The reference's default no-admixture K-sweep (-structure_admix=no
+    -structure_krange=[1,4], default nadmburnin = 500 admixture burn-in
+    sweeps) reaches the tensor-core form without any extra flag: the burn-in
+    runs in the plain form, then every run joins the batch. Against the same
+    runs forced into the plain form: the admixture burn-in records are equal
+    bit for bit, the first single-label record within 1e-5, and the files keep
+    the reference's layout."""
+    vcf = os.path.join(str(tmp_path), "data.vcf")
+    with gzip.open(os.path.join(GOLD, "c1.vcf.gz"), "rb") as fi, open(vcf, "wb") as fo:
+        shutil.copyfileobj(fi, fo)
+    out = {}
+    for form in ("default", "plain"):
+        d = tmp_path / form
+        d.mkdir()
+        args = [CLI, f"-g_input={vcf}", f"-g_output={d}/out", "-g_seed=5", "-g_decimal=15", "-structure",
+                "-structure_admix=no", "-structure_krange=[1,4]", "-structure_nburnin=30", "-structure_nreps=40",
+                "-structure_nthinning=1",
+                "-structure_writelnl=yes"] + ([] if form == "default" else ["-gb300_form=plain"])
+        r = subprocess.run(args, check=True, capture_output=True, text=True)
+        assert ("tensor-core form" in r.stderr) == (form == "default"), r.stderr
+        out[form] = d
+    for K in range(1, 5):
+        f = f"out.structure.k={K}_rep=1_id={K}.lnl.txt"
+        tc = [float(x) for x in NUM.findall(open(out["default"] / f).read())]
+        pl = [float(x) for x in NUM.findall(open(out["plain"] / f).read())]
+        assert len(tc) == len(pl) == 500 + 30 + 40
+        assert tc[:500] == pl[:500]
+        assert abs(tc[500] - pl[500]) <= 1e-5 * abs(pl[500])
+        g = open(out["default"] / f"out.structure.k={K}_rep=1_id={K}.txt", "rb").read().decode()
+        p = open(out["plain"] / f"out.structure.k={K}_rep=1_id={K}.txt", "rb").read().decode()
+        assert _shape(g) == _shape(p)

@@ -154,3 +154,34 @@ def test_k_out_of_range_rejected():
         with pytest.raises(B.VpError, match="K must be"):
             S.Chain(ctx, S.params(K, 1))
     ctx.close()
+
+
+def test_no_step_past_the_end_of_the_run():
+    """A caller driving its own loop is stopped at the end of the run: the
+    trace is sized for nburnin + nreps sweeps, so a further Record or sweep
+    index would write beyond it. The sweep index may not be set outside the
+    run either."""
+    d = synth.fmodel(71, 40, 30, 2, 0.1, 0.05)
+    ds = S.Dataset.from_synth(d)
+    ctx = S.Context(ds)
+    c = S.Chain(ctx, S.params(2, 5, admix=0, nadmburnin=0, nburnin=2, nreps=2, nthinning=1, writelnl=1))
+    S.finish([c])
+    assert int(c.get("M")[0]) == 4
+    for step in ("RECORD", "NEXT", "UPDATEP"):
+        with pytest.raises(B.VpError, match="is over"):
+            c.step(step)
+    with pytest.raises(B.VpError, match="outside the run"):
+        c.set("M", np.array([5], np.int32))
+    with pytest.raises(B.VpError, match="outside the run"):
+        c.set("M", np.array([-1], np.int32))
+    r = c.result(final=True)
+    assert len(r["lnl"]) == 4 and np.isfinite(r["lnl"]).all()
+    # rewinding inside the run is allowed; repeated Records at one sweep
+    # index stop at the trace's capacity (ceil(2/1) + ceil(2/1) + 2 records)
+    c.set("M", np.array([3], np.int32))
+    for _ in range(4):
+        c.step("RECORD")
+    assert len(c.result(final=True)["lnl"]) == 6
+    c.step("NEXT")
+    with pytest.raises(B.VpError, match="is over"):
+        c.step("NEXT")

@@ -287,3 +287,43 @@ def test_pipeline_wait_runs_out_with_an_error_status_and_the_device_stays_usable
     assert st.value in (1, 2, 3), st.value
     assert after.value == 0
     assert err.value == 0.0
+
+
+def test_tc_chain_runs_its_admixture_burn_in_in_the_plain_form():
+    """The reference's default no-admixture run starts with nadmburnin
+    sweeps drawn per allele copy (src/structure.cpp:460-462). A tensor-core
+    chain runs those sweeps in the plain form, then joins the batch: through
+    the burn-in its trace equals the plain chain's bit for bit (same kernels,
+    same Philox draws), and at the first single-label sweep, whose state is
+    the same, its likelihood agrees within 1e-5."""
+    d = synth.fmodel(57, 800, 2500, 3, 0.05, 0.02)
+    ds = S.Dataset.from_synth(d)
+    ctx = S.Context(ds)
+    kw = dict(admix=0, nadmburnin=12, nburnin=4, nreps=6, nthinning=1, writelnl=1)
+    Ks = [1, 2, 4]
+    plain = [S.Chain(ctx, S.params(K, 700 + K, **kw)) for K in Ks]
+    tc = [S.Chain(ctx, S.params(K, 700 + K, form=B.VP_FORM_TC, **kw)) for K in Ks]
+    S.finish(plain)
+    S.finish(tc)
+    assert B.lib().vp_tc_status(ctx.h) == 0
+    for p, t in zip(plain, tc):
+        rp, rt = p.result(final=True), t.result(final=True)
+        assert len(rp["lnl"]) == len(rt["lnl"]) == 12 + 4 + 6
+        assert np.array_equal(rp["lnl"][:12], rt["lnl"][:12])
+        assert abs(rp["lnl"][12] - rt["lnl"][12]) <= 1e-5 * abs(rp["lnl"][12])
+        assert np.isfinite(rt["lnl"]).all() and np.isfinite(rt["rout"][:4]).all()
+        assert rt["nr"] == 6
+
+
+def test_tc_chains_in_burn_in_refuse_the_tuner():
+    """The batch only holds chains past their admixture burn-in."""
+    d = synth.fmodel(58, 300, 800, 2, 0.05, 0.02)
+    ctx = S.Context(S.Dataset.from_synth(d))
+    tc = [S.Chain(ctx, S.params(K, 70 + K, form=B.VP_FORM_TC, admix=0, nadmburnin=3, nburnin=2, nreps=2))
+          for K in (2, 3)]
+    with pytest.raises(B.VpError, match="admixture burn-in"):
+        S.tune(tc, 0)
+    S.run_chains(tc, 3)
+    S.tune(tc, 0)
+    S.finish(tc)
+    assert all(np.isfinite(c.result(final=True)["rout"][3]) for c in tc)

@@ -55,3 +55,45 @@ def test_noalloc_rejects_oversized_problems():
     dummy = torch.zeros(16, dtype=torch.int32, device="cuda")
     with pytest.raises(B.VpError, match="fixed array"):
         B.check(B.lib().vp_loglik_packed2_noalloc(dummy.data_ptr(), N, L, dummy.data_ptr(), K, dummy.data_ptr(), None))
+
+
+def test_noalloc_at_the_size_limit():
+    """The largest locus count whose scratch still fits the fixed array gives
+    what the allocating call gives; one locus more is refused with VP_E_ARG.
+    The limit is found by bisection on the call's own answer (a refused call
+    does no device work), so the test follows the plan's alignment slack."""
+    import torch
+    lib = B.lib()
+    N, K, L_hi = 64, 4, 600_000      # 600,000 loci need about 38 MB of scratch
+    rng = np.random.default_rng(11)
+    words = rng.integers(0, 2**32, size=(L_hi, (N + 15) // 16), dtype=np.uint64).astype(np.uint32)
+    g = torch.from_numpy(words.view(np.int32)).cuda()
+    p = rng.dirichlet([1.0, 1.0], size=(K, L_hi)).astype(np.float32)   # [K][L][2]
+    out = torch.empty((N, K), dtype=torch.float64, device="cuda")
+
+    def fits(L):
+        f = torch.from_numpy(np.ascontiguousarray(p[:, :L].reshape(K, 2 * L))).cuda()
+        torch.cuda.synchronize()
+        rc = lib.vp_loglik_packed2_noalloc(g.data_ptr(), N, L, f.data_ptr(), K, out.data_ptr(), None)
+        torch.cuda.synchronize()
+        assert rc in (0, B.VP_E_ARG), rc
+        return rc == 0, f
+
+    lo, hi = 1, L_hi
+    assert fits(lo)[0] and not fits(hi)[0]
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        if fits(mid)[0]:
+            lo = mid
+        else:
+            hi = mid
+    assert 400_000 < lo < L_hi
+    _, f = fits(lo)
+    want = _call(lib.vp_loglik_packed2, g, f, N, lo, K)
+    for _ in range(2):
+        got = _call(lib.vp_loglik_packed2_noalloc, g, f, N, lo, K)
+        assert np.isfinite(got).all()
+        assert (np.abs(got - want) / np.abs(want)).max() < REL
+    _, f1 = fits(lo + 1)
+    assert lib.vp_loglik_packed2_noalloc(g.data_ptr(), N, lo + 1, f1.data_ptr(), K, out.data_ptr(), None) == B.VP_E_ARG
+    assert b"fixed array" in lib.vp_last_error()

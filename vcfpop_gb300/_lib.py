@@ -12,6 +12,7 @@ from .build import LIB
 
 VP_RNG_REFERENCE, VP_RNG_COUNTER = 0, 1
 VP_FORM_PLAIN, VP_FORM_TC = 0, 1
+VP_OK, VP_E_ARG, VP_E_CUDA, VP_E_MEM, VP_E_STATE, VP_E_NODEV = 0, -1, -2, -3, -4, -5
 
 STEP = dict(UPDATEP=1, UPDATEQ=2, LOCPRIORI=3, UPDATEZ=4, ALPHA=5, UPDATEA=6, UPDATEF=7, RECORD=8, NEXT=9,
             LOGLIK=10)

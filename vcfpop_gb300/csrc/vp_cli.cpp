@@ -8,8 +8,10 @@
 // reference's result files (src/structure.cpp:86-401):
 //   <out>.structure.k=K_rep=R_id=I.txt, its .lnl.txt with -structure_writelnl,
 //   and the summary <out>.structure.txt.
-// Extra flags: -gb300_rng=counter|reference, -gb300_form=plain|tc,
-// -gb300_device=D.
+// Extra flags: -gb300_rng=counter|reference, -gb300_form=plain|tc|auto
+// (auto, the default: the tensor-core form wherever it applies),
+// -gb300_device=D. Filters of the reference that are not implemented are
+// refused.
 #include <zlib.h>
 
 #include <algorithm>
@@ -33,6 +35,7 @@ struct Opts {
     int decimal = 5;
     std::string delim = "\t", lb = "\r\n";
     int kmin = 1, kmax = 5, nruns = 1, diversity = 0, device = 0;
+    int form = -1;                // -gb300_form: VP_FORM_*, or -1 = tensor-core form where it applies
     bool filter = false;          // -f, with -f_* windows: the locus filter
     vp_locus_filter lf{};
     vp_params p;
@@ -60,7 +63,7 @@ bool parse(int argc, char** argv, Opts& o) {
         else if (k == "-g_delimiter") o.delim = v == "comma" ? "," : "\t";
         else if (k == "-g_linebreak") o.lb = v == "unix" ? "\n" : "\r\n";
         else if (k == "-gb300_rng") o.p.rng = v == "reference" ? VP_RNG_REFERENCE : VP_RNG_COUNTER;
-        else if (k == "-gb300_form") o.p.form = v == "tc" ? VP_FORM_TC : VP_FORM_PLAIN;
+        else if (k == "-gb300_form") o.form = v == "tc" ? VP_FORM_TC : v == "plain" ? VP_FORM_PLAIN : -1;
         else if (k == "-gb300_device") o.device = atoi(v.c_str());
         else if (k == "-structure_admix") o.p.admix = yesno(v);
         else if (k == "-structure_locpriori") o.p.locpriori = yesno(v);
@@ -105,7 +108,15 @@ bool parse(int argc, char** argv, Opts& o) {
         else if (k == "-f_pic") o.lf.pic_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.pic_min, &o.lf.pic_max) == 2;
         else if (k == "-f_ae") o.lf.ae_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.ae_min, &o.lf.ae_max) == 2;
         else if (k == "-f_I") o.lf.I_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.I_min, &o.lf.I_max) == 2;
-        else if (k == "-f_pval") { fprintf(stderr, "vcfpop-gb300: the HWE filter -f_pval is not implemented\n"); return false; }
+        else if (k.rfind("-f_", 0) == 0) {
+            // every other filter of the reference (-f_pval, -f_qual, -f_dp,
+            // -f_gq, -f_itype, -f_iploidy, -f_windowsize, ...) would change
+            // which loci or calls the clustering sees: refuse it rather than
+            // run on unfiltered data
+            fprintf(stderr, "vcfpop-gb300: the filter %s is not implemented (implemented: -f_bmaf -f_k -f_n "
+                            "-f_ptype -f_he -f_ho -f_pic -f_ae -f_I)\n", k.c_str());
+            return false;
+        }
         // other -g_* and -structure_* flags (threads, SIMD, plots, streams) do
         // not apply to the GPU path and are accepted silently
     }
@@ -541,6 +552,14 @@ int main(int argc, char** argv) {
     for (int64_t l = 0; l < info.n_loc; ++l) { ks[l] = v.k[order[l]]; lnames[l] = v.locs[order[l]]; }
     vp_ctx* ctx = nullptr;
     if (vp_open(ds, o.device, &ctx)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+    // the tensor-core K-sweep runs no-admixture chains without location
+    // prior or F model, with counter streams, on biallelic diploid data; the
+    // default picks it for every run where it applies (the no-admixture
+    // burn-in runs in the plain form first)
+    if (o.form >= 0) o.p.form = o.form;
+    else o.p.form = !o.p.admix && !o.p.locpriori && !o.p.fmodel && o.p.rng == VP_RNG_COUNTER && info.packed2
+                        ? VP_FORM_TC : VP_FORM_PLAIN;
+    fprintf(stderr, "vcfpop-gb300: %s form\n", o.p.form == VP_FORM_TC ? "tensor-core" : "plain");
     struct Run { int K, rep, id; vp_chain* c; };
     std::vector<Run> runs;
     int id = 0;

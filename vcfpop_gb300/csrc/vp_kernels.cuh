@@ -41,6 +41,7 @@ struct DevChain {
     int32_t K, admix, locpriori, fmodel, nburnin, nreps, nthinning, nadmburnin, writelnl;
     int32_t metrofreq, inferalpha, diffalpha, uniformalpha, fsame, difflambda, rlen, rng, nchunk, lchunk;
     int32_t zadm_tn, nlnlp, kp, nsampblk, zadm_lc;
+    int32_t ntrace;       // capacity of lnlTrace in records
     double lambda, alpha, stdalpha, maxalpha, alphapriora, alphapriorb, maxr, epsr, epseta, epsgamma;
     double pmeanf, pstdf, stdf;
     uint64_t seed;
@@ -1590,7 +1591,7 @@ __device__ void record_scalars(const DevChain& c, int m, double* sh) {
             like = block_sum(v, sh);
         }
         if (threadIdx.x == 0) {
-            if (c.writelnl) c.lnlTrace[c.ctl->nlnl++] = like;
+            if (c.writelnl && c.ctl->nlnl < c.ntrace) c.lnlTrace[c.ctl->nlnl++] = like;
             if (m >= c.nburnin) {
                 c.ctl->nr++;
                 c.rout[0] += like;

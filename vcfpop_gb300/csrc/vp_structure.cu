@@ -112,7 +112,7 @@ struct TcBatch {
 namespace {
 void free_batch(vp_ctx* x);
 int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps);
-int launch_counts_gemm(vp_ctx* x);
+int launch_counts_gemm(vp_ctx* x, int32_t* out = nullptr);
 tc::BatchDev batch_dev(vp_ctx* x);
 
 #define CK(call)                                                                  \
@@ -570,7 +570,7 @@ void chain_layout(Carve& cv, vp_chain* c, const vp_ctx* x) {
     const vp_params* P = &c->P;
     const int K = P->K, N = x->N, S = x->S;
     const int64_t L = x->L, KT = x->KT;
-    const int64_t ntrace = h.nburnin / h.nthinning + h.nreps / h.nthinning + 2;
+    const int64_t ntrace = h.ntrace;
     const int64_t ltn = x->packed2 ? L * 4 * h.kp : (int64_t)K * KT;
     h.ctl = cv.take<Ctl>(1);
     h.rstate = cv.take<Rng64>(1);
@@ -633,6 +633,9 @@ int chain_plan(const vp_ctx* x, const vp_params* P, vp_chain* c, size_t* bytes) 
     int na = P->admix ? (P->diffalpha ? K : 1) : 0;
     int nl = P->difflambda ? K : 1;
     h.rlen = P->locpriori ? 4 + nl + 1 + K + K * S + nf : 4 + nl + na + nf;
+    // lnL trace records: ceil(nburnin / t) + ceil(nreps / t), plus slack;
+    // Record never writes more than this many
+    h.ntrace = (int32_t)(h.nburnin / h.nthinning + h.nreps / h.nthinning + 2);
     c->kc = kc_for(K);
     c->kgroups = (K + c->kc - 1) / c->kc;
     // locus chunks for the likelihood passes: about 12 CTAs per SM, so that
@@ -794,29 +797,13 @@ static int capture_sweep(vp_chain** cs, int n, cudaGraphExec_t* exec, int* nodes
     return VP_OK;
 }
 
-extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
-    if (!cs || n <= 0 || nsweeps < 0) { vp_set_error("bad arguments"); return VP_E_ARG; }
-    vp_ctx* x = cs[0]->ctx;
-    for (int i = 0; i < n; ++i)
-        if (!cs[i] || cs[i]->ctx != x) { vp_set_error("all chains of one vp_run must share a context"); return VP_E_ARG; }
-    cudaSetDevice(x->device);
-    bool all_tc = true;
-    for (int i = 0; i < n; ++i) all_tc &= cs[i]->P.form == VP_FORM_TC;
-    if (all_tc) {
-        int step = nsweeps;
-        for (int i = 0; i < n; ++i) step = std::min(step, cs[i]->total - cs[i]->issued);
-        if (step <= 0) return VP_OK;
-        int rc = run_tc(x, cs, n, step);
-        if (rc) return rc;
-        for (int i = 0; i < n; ++i) cs[i]->issued += step;
-        return VP_OK;
-    }
+// plain-form sweeps of a set of chains of one context: chains with sweeps
+// left share one cached graph of a sweep while their set does not change
+static int run_plain(vp_ctx* x, vp_chain** cs, int n, int nsweeps) {
     for (int i = 0; i < n; ++i) {
         if (int rc0 = ensure_counts(cs[i])) return rc0;
         if (int rc0 = ensure_plain(cs[i])) return rc0;
     }
-    // chains with sweeps left; a set of chains whose sweeps are all still
-    // pending shares one cached graph of a sweep
     int left = nsweeps;
     while (left > 0) {
         std::vector<vp_chain*> act;
@@ -840,6 +827,46 @@ extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
             x->launches += x->pg_nodes;
         }
         for (vp_chain* c : act) c->issued += step;
+        left -= step;
+    }
+    return VP_OK;
+}
+
+extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
+    if (!cs || n <= 0 || nsweeps < 0) { vp_set_error("bad arguments"); return VP_E_ARG; }
+    vp_ctx* x = cs[0]->ctx;
+    for (int i = 0; i < n; ++i)
+        if (!cs[i] || cs[i]->ctx != x) { vp_set_error("all chains of one vp_run must share a context"); return VP_E_ARG; }
+    cudaSetDevice(x->device);
+    bool all_tc = true;
+    for (int i = 0; i < n; ++i) all_tc &= cs[i]->P.form == VP_FORM_TC;
+    if (!all_tc) return run_plain(x, cs, n, nsweeps);
+    // Tensor-core chains: the sweeps of the no-admixture burn-in (m <
+    // nadmburnin, src/structure.cpp:460-462, where Q and Z are drawn per
+    // allele copy as with admixture) run in the plain form; from the first
+    // single-label sweep on a chain runs in the batch. Each round advances
+    // every chain with sweeps left by the same number of sweeps, up to the
+    // next phase change or end of a chain.
+    int left = nsweeps;
+    while (left > 0) {
+        std::vector<vp_chain*> burn, batch;
+        int step = left;
+        for (int i = 0; i < n; ++i) {
+            vp_chain* c = cs[i];
+            if (c->issued >= c->total) continue;
+            const int phase_end = c->issued < c->h.nadmburnin ? c->h.nadmburnin : c->total;
+            (c->issued < c->h.nadmburnin ? burn : batch).push_back(c);
+            step = std::min(step, phase_end - c->issued);
+        }
+        if (burn.empty() && batch.empty()) break;
+        if (!burn.empty()) {
+            // run_plain advances these chains' issued counts itself
+            if (int rc = run_plain(x, burn.data(), (int)burn.size(), step)) return rc;
+        }
+        if (!batch.empty()) {
+            if (int rc = run_tc(x, batch.data(), (int)batch.size(), step)) return rc;
+            for (vp_chain* c : batch) c->issued += step;
+        }
         left -= step;
     }
     return VP_OK;
@@ -1012,6 +1039,13 @@ extern "C" int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t
     int rc = field_ptr(c, field, &p, &n);
     if (rc) return rc;
     if (bytes != n) { vp_set_error("field %d holds %zu bytes, not %zu", field, n, bytes); return VP_E_ARG; }
+    if (field == VP_F_M) {
+        const int32_t m = *(const int32_t*)host;
+        if (m < 0 || m > c->total) {
+            vp_set_error("sweep index %d outside the run's 0..%d", m, c->total);
+            return VP_E_ARG;
+        }
+    }
     CK(cudaMemcpy(p, host, n, cudaMemcpyHostToDevice));
     if (field == VP_F_FREQ && c->h.lt) {
         // keep the likelihood lookup table in step with the frequencies
@@ -1030,6 +1064,15 @@ extern "C" int vp_chain_step(vp_chain* c, int32_t step) {
     int rc = ensure_counts(c);
     if (!rc) rc = ensure_plain(c);
     if (rc) return rc;
+    // no step past the end of the run: Record and the sweep index would
+    // run beyond the state sized for nburnin + nreps sweeps
+    int32_t m = 0;
+    CK(cudaMemcpyAsync(&m, &c->h.ctl->m, sizeof m, cudaMemcpyDeviceToHost, c->ctx->stream));
+    CK(cudaStreamSynchronize(c->ctx->stream));
+    if (m >= c->total) {
+        vp_set_error("sweep index %d: the run has %d sweeps (nburnin + nreps) and is over", m, c->total);
+        return VP_E_STATE;
+    }
     rc = launch_step(c, step, 0);
     if (rc) return rc;
     return vp_sync(c->ctx);
@@ -1323,9 +1366,9 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n, const TcChoice* force) {
     if (rc) return rc;
     for (int i = 0; i < n; ++i) {
         const vp_params& P = cs[i]->P;
-        if (P.admix || P.locpriori || P.fmodel || cs[i]->h.nadmburnin > 0 || P.rng != VP_RNG_COUNTER) {
-            vp_set_error("the tensor-core form runs no-admixture chains without location prior, F model or "
-                         "admixture burn-in, with counter streams");
+        if (P.admix || P.locpriori || P.fmodel || cs[i]->issued < cs[i]->h.nadmburnin || P.rng != VP_RNG_COUNTER) {
+            vp_set_error("the tensor-core form runs no-admixture chains without location prior or F model, with "
+                         "counter streams, past their admixture burn-in");
             return VP_E_ARG;
         }
     }
@@ -1484,15 +1527,15 @@ int launch_tc_sweep(vp_ctx* x) {
 }
 
 // the count contraction of the batch: Ni[row, a] = sum_i OH[row, i] C[i, a]
-// into every chain's Ni (e4m3 operands, exact)
-int launch_counts_gemm(vp_ctx* x) {
+// into every chain's Ni (e4m3 operands, exact), or into `out` ([Rpad][KT])
+int launch_counts_gemm(vp_ctx* x, int32_t* out) {
     TcBatch* b = x->batch;
     const TcOperands& t = x->tc;
     {
         tc::GemmArgs g{};
         g.M = (int)(2 * x->L); g.N = b->Rpad; g.kblocks = (int)(t.Npad / t.bk8); g.kb_per_split = g.kblocks;
         g.BN = b->BN; g.piece = b->piece; g.nb = 1; g.mt = b->mt2; g.stages = b->cfg.st2; g.bk = t.bk8; g.esz = 1;
-        g.mode = 1; g.out_i = b->NiAll; g.ldo = x->KT; g.err = t.err;
+        g.mode = 1; g.out_i = out ? out : b->NiAll; g.ldo = x->KT; g.err = t.err;
         const unsigned mtiles = cdiv(t.Apad, 128 * b->mt2);
         g.group_major = b->cfg.gm2 && mtiles <= 65535;     // grid.y limit; otherwise row tiles on x
         const dim3 grid = g.group_major ? dim3(b->G, mtiles, 1) : dim3(mtiles, b->G, 1);
@@ -1643,11 +1686,15 @@ int tune_batch(vp_ctx* x, int effort, TcChoice* best, vp_tc_config* info) {
     dev_free(scratch, x->stream);
     if (rc) return rc;
     // count contraction: pipeline depth and CTA order, on one-hot rows of the
-    // chains' current labels
+    // chains' current labels, into a scratch matrix (the chains' own counts
+    // may come from per-copy draws that the labels do not give back)
     {
         tc::BatchDev bd = batch_dev(x);
         LAUNCH(x, tc::k_onehot_from_z, (dim3(cdiv(x->N, 256), (unsigned)b->chains.size(), 1), 256, 0, x->stream), (bd));
     }
+    int32_t* ni_scratch = nullptr;
+    e = dev_alloc((void**)&ni_scratch, (size_t)b->Rpad * x->KT * 4, x->device, x->stream);
+    if (e != cudaSuccess) { vp_set_error("tuning scratch: %s", cudaGetErrorString(e)); return VP_E_MEM; }
     const TcChoice save = b->cfg;
     float best2 = INFINITY;
     int bst2 = save.st2, bgm2 = save.gm2, ncand = (int)c1.size();
@@ -1660,7 +1707,7 @@ int tune_batch(vp_ctx* x, int effort, TcChoice* best, vp_tc_config* info) {
                 b->cfg.st2 = st;
                 b->cfg.gm2 = gm;
                 float ms = 0.f;
-                rc = time_candidate(x, [&] { return launch_counts_gemm(x); }, iters, &ms);
+                rc = time_candidate(x, [&] { return launch_counts_gemm(x, ni_scratch); }, iters, &ms);
                 ++ncand;
                 if (rc) break;
                 if (pass == 0) info->ms_counts_default = ms;
@@ -1668,6 +1715,7 @@ int tune_batch(vp_ctx* x, int effort, TcChoice* best, vp_tc_config* info) {
             }
         }
     b->cfg = save;
+    dev_free(ni_scratch, x->stream);
     if (rc) return rc;
     *best = bc;
     best->st2 = bst2;
@@ -2083,7 +2131,9 @@ int ll_run(LLPlan& pl, const uint32_t* geno, const float* freq, double* ll, void
     h.lt = cv.take<float>(h.D.L * 4 * h.kp);
     h.LLp = cv.take<double>((int64_t)h.nchunk * h.D.N * h.K);
     h.D.g2 = geno;
-    CK(cudaMemcpyAsync(d, &h, sizeof(DevChain), cudaMemcpyHostToDevice, s));
+    // the descriptor travels as the kernel's parameter: no host buffer has
+    // to outlive the call
+    k_set_chain<<<1, 128, 0, s>>>(d, h);
     k_lt_from_freq<<<cdiv((int64_t)h.K * h.D.L, 256), 256, 0, s>>>(freq, h.K, h.D.L, h.kp, h.lt);
     dim3 g(cdiv(h.D.N, LL_BLOCK), h.nchunk, pl.kgroups);
     switch (pl.kc) {
@@ -2141,7 +2191,8 @@ static __device__ __align__(256) unsigned char g_loglik_scratch[VP_LOGLIK_NOALLO
 
 // Device address of the array on each device. Host code cannot use the
 // array's name as a device address, so the address is looked up once per
-// device with that device current.
+// device with that device current. The cached address belongs to the
+// device's primary context: it is not valid after a device reset.
 void* g_loglik_scratch_addr[64];
 std::mutex g_loglik_scratch_mu;
 
