@@ -1001,6 +1001,23 @@ static int field_ptr(vp_chain* c, int f, void** p, size_t* bytes) {
     return VP_E_ARG;
 }
 
+// the location-prior state, five arrays in one host buffer: r, Eta[K],
+// Gamma[S*K], AlphaLocal[S*K], SumAlpha[S] (all double)
+static int locp_copy(vp_chain* c, void* host, size_t bytes, bool to_device) {
+    const size_t K = c->P.K, S = c->ctx->S;
+    const size_t want = 8 * (1 + K + 2 * S * K + S);
+    if (bytes != want) { vp_set_error("field %d holds %zu bytes, not %zu", VP_F_LOCP, want, bytes); return VP_E_ARG; }
+    struct Part { void* dev; size_t n; } parts[] = {{&c->h.ctl->r, 1}, {c->h.Eta, K}, {c->h.Gamma, S * K},
+                                                     {c->h.AlphaLocal, S * K}, {c->h.SumAlpha, S}};
+    char* h = (char*)host;
+    for (const Part& p : parts) {
+        if (to_device) CK(cudaMemcpy(p.dev, h, p.n * 8, cudaMemcpyHostToDevice));
+        else CK(cudaMemcpy(h, p.dev, p.n * 8, cudaMemcpyDeviceToHost));
+        h += p.n * 8;
+    }
+    return VP_OK;
+}
+
 extern "C" int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes) {
     if (!c || !host) { vp_set_error("null argument"); return VP_E_ARG; }
     cudaSetDevice(c->ctx->device);
@@ -1013,6 +1030,7 @@ extern "C" int vp_chain_get(vp_chain* c, int32_t field, void* host, size_t bytes
         CK(cudaMemcpy((char*)host + K * 8, c->h.F, K * 8, cudaMemcpyDeviceToHost));
         return VP_OK;
     }
+    if (field == VP_F_LOCP) return locp_copy(c, host, bytes, false);
     void* p; size_t n;
     int rc = field_ptr(c, field, &p, &n);
     if (rc) return rc;
@@ -1035,6 +1053,7 @@ extern "C" int vp_chain_set(vp_chain* c, int32_t field, const void* host, size_t
         CK(cudaMemcpy(c->h.F, (const char*)host + K * 8, K * 8, cudaMemcpyHostToDevice));
         return VP_OK;
     }
+    if (field == VP_F_LOCP) return locp_copy(c, const_cast<void*>(host), bytes, true);
     void* p; size_t n;
     int rc = field_ptr(c, field, &p, &n);
     if (rc) return rc;

@@ -148,7 +148,7 @@ class Context:
 
 
 _DT = {1: np.float32, 2: np.float32, 3: np.uint16, 4: np.int32, 5: np.int32, 6: np.float64, 7: np.float64,
-       8: np.int32, 9: np.float64, 10: np.float32, 11: np.float64, 13: np.float32, 14: np.float64}
+       8: np.int32, 9: np.float64, 10: np.float32, 11: np.float64, 12: np.float64, 13: np.float32, 14: np.float64}
 
 
 class Chain:
@@ -165,7 +165,7 @@ class Chain:
         ds = self.ctx.ds
         K = self.p.K
         return {1: K * ds.KT, 2: ds.N * K, 3: ds.N, 4: K * ds.KT, 5: ds.N * K, 6: ds.N * K, 7: K, 8: 1, 9: 1,
-                10: ds.KT, 11: 2 * K, 13: ds.S * K, 14: ds.N}[field]
+                10: ds.KT, 11: 2 * K, 12: 1 + K + 2 * ds.S * K + ds.S, 13: ds.S * K, 14: ds.N}[field]
 
     def get(self, name: str) -> np.ndarray:
         f = B.FIELD[name]

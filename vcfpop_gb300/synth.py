@@ -68,26 +68,41 @@ def fmodel(seed: int, n_ind: int, n_loc: int, n_pop: int, F: float,
     G = np.full((n_loc, n_ind, vmax), -1, dtype=np.int8)
     cumQ = np.cumsum(Q, axis=1)
     cumf = np.cumsum(popf, axis=2)  # [P, L, kmax]
+    # inverse-CDF draws, one threshold at a time: the origin is the number of
+    # cumulative ancestry proportions below u, the allele the number of
+    # cumulative frequencies of the origin below ua (capped at k - 1)
     for c in range(vmax):
         has = ploidy > c
         if per_locus_origin:
-            chunk = max(1, (1 << 22) // max(1, n_ind * kmax))
+            chunk = max(1, (1 << 22) // max(1, n_ind * kmax))        # loci per pair of uniform draws
+            sub = max(1, (1 << 18) // max(1, n_ind))                  # loci per cache-sized pass
             for l0 in range(0, n_loc, chunk):
                 l1 = min(n_loc, l0 + chunk)
                 u = rng.random((l1 - l0, n_ind))
-                src = np.minimum((u[:, :, None] > cumQ[None]).sum(axis=2), n_pop - 1)  # [Lc, N]
-                cf = cumf[src, np.arange(l0, l1)[:, None], :]                          # [Lc, N, kmax]
                 ua = rng.random((l1 - l0, n_ind))
-                al = np.minimum((ua[:, :, None] > cf).sum(axis=2), (k[l0:l1] - 1)[:, None])
-                G[l0:l1, has, c] = al[:, has]
+                for r0 in range(0, l1 - l0, sub):
+                    r1 = min(l1 - l0, r0 + sub)
+                    src = np.zeros((r1 - r0, n_ind), np.int32)                                 # [rows, N]
+                    for p in range(n_pop - 1):
+                        src += u[r0:r1] > cumQ[:, p][None, :]
+                    idx = src + (np.arange(r1 - r0, dtype=np.int32) * n_pop)[:, None]          # (locus, origin)
+                    al = np.zeros((r1 - r0, n_ind), np.int8)
+                    for a in range(kmax - 1):
+                        thr = np.ascontiguousarray(cumf[:, l0 + r0:l0 + r1, a].T).reshape(-1)  # [rows * P]
+                        al += ua[r0:r1] > np.take(thr, idx)
+                    al = np.minimum(al, (k[l0 + r0:l0 + r1] - 1)[:, None])
+                    G[l0 + r0:l0 + r1, has, c] = al[:, has]
             continue
         u = rng.random(n_ind)
-        src = np.minimum((u[:, None] > cumQ).sum(axis=1), n_pop - 1)  # origin of this copy
+        src = np.zeros(n_ind, np.int64)                                           # origin of this copy
+        for p in range(n_pop - 1):
+            src += u > cumQ[:, p]
         ua = rng.random((n_loc, n_ind))
-        cf = cumf[src]  # [N, L, kmax]
-        al = (ua.T[:, :, None] > cf).sum(axis=2)  # [N, L]
-        al = np.minimum(al, (k - 1)[None, :])
-        G[:, has, c] = al.T[:, has]
+        al = np.zeros((n_loc, n_ind), np.int64)
+        for a in range(kmax - 1):
+            al += ua > cumf[src, :, a].T                                            # [L, N]
+        al = np.minimum(al, (k - 1)[:, None])
+        G[:, has, c] = al[:, has]
     miss = rng.random((n_loc, n_ind)) < missing
     G[miss] = -1
     # unphased: sort the copies of each call ascending, missing stays missing
