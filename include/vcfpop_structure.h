@@ -152,6 +152,24 @@ int vp_chain_result(vp_chain* c, vp_result* out);
  * sequential order, so the last bits may differ). */
 int vp_chain_divergence(vp_chain* c, double* H, double* D, double* Hl);
 
+/* The result files of one finished run (after vp_finish) in the reference's
+ * format: WriteStructure, src/structure.cpp:86-377, which writes
+ * <prefix>.structure.k=K_rep=R_id=I.txt and, with writelnl, its .lnl.txt.
+ * The numbers are the chain's (vp_chain_result) and the device reductions'
+ * (vp_chain_divergence). Synchronous; host memory only. */
+typedef struct {
+    const char* prefix;             /* -g_output */
+    int32_t rep, id;                /* replicate and run id of the file names */
+    const char* const* ind_names;   /* [N] individuals in the dataset's order */
+    const char* const* pop_names;   /* [S] populations (locations) */
+    const char* const* loc_names;   /* [n_loc] loci in vp_input's (input) order */
+    int32_t decimal;                /* -g_decimal */
+    int32_t comma;                  /* -g_delimiter=comma (else tab) */
+    int32_t unix_lb;                /* -g_linebreak=unix (else CR LF) */
+    int32_t diversity;              /* -structure_diversity */
+} vp_write_opts;
+int vp_write_structure(vp_chain* c, const vp_write_opts* o);
+
 /* ---- single steps and state access (parity tests, debugging) ------------- */
 #define VP_STEP_UPDATEP 1
 #define VP_STEP_UPDATEQ 2

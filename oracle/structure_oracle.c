@@ -1076,6 +1076,7 @@ void* orc_field(orc_chain* c, int f, int64_t* n) {
     return NULL;
 }
 int32_t* orc_m(orc_chain* c) { return &c->m; }
+int32_t* orc_nlnl(orc_chain* c) { return &c->nlnL; }
 double* orc_r(orc_chain* c) { return &c->r; }
 int32_t* orc_binaryq(orc_chain* c) { return &c->binaryq; }
 const void* orc_data_field(const orc_data* d, int f, int64_t* n) {

@@ -174,6 +174,7 @@ uint32_t orc_hash_ulong_c(uint64_t v);
  *  20 lnL trace f64, 21 MiSum i64, 22 FreqM f32). *n receives the element count. */
 void* orc_field(orc_chain* c, int field, int64_t* n);
 int32_t* orc_m(orc_chain* c);
+int32_t* orc_nlnl(orc_chain* c);        /* records in the lnL trace (settable, up to its capacity) */
 double* orc_r(orc_chain* c);
 int32_t* orc_binaryq(orc_chain* c);
 /* dataset arrays: 1 k, 2 off(i64), 3 vt(i64), 4 gcopies(u8), 5 galleles(u8) */

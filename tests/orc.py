@@ -62,6 +62,10 @@ def lib():
         L.orc_data_field.argtypes = [P, C.c_int, C.POINTER(C.c_int64)]
         L.orc_m.restype = C.POINTER(C.c_int32)
         L.orc_m.argtypes = [P]
+        L.orc_nlnl.restype = C.POINTER(C.c_int32)
+        L.orc_nlnl.argtypes = [P]
+        L.orc_write_structure.argtypes = [P, C.c_char_p, C.c_int, C.c_int, P, P, P, C.c_int, C.c_int]
+        L.orc_write_structure.restype = C.c_int
         L.orc_r.restype = C.POINTER(C.c_double)
         L.orc_r.argtypes = [P]
         L.orc_binaryq.restype = C.POINTER(C.c_int32)

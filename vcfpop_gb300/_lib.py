@@ -80,6 +80,13 @@ class VpTcConfig(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class VpWriteOpts(C.Structure):
+    _fields_ = [("prefix", C.c_char_p), ("rep", C.c_int32), ("id", C.c_int32),
+                ("ind_names", C.POINTER(C.c_char_p)), ("pop_names", C.POINTER(C.c_char_p)),
+                ("loc_names", C.POINTER(C.c_char_p)), ("decimal", C.c_int32), ("comma", C.c_int32),
+                ("unix_lb", C.c_int32), ("diversity", C.c_int32)]
+
+
 class VpError(RuntimeError):
     pass
 
@@ -93,7 +100,7 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
            "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2", "vp_release_memory",
-           "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout"]
+           "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout", "vp_write_structure"]
 
 
 def lib():
@@ -155,6 +162,7 @@ def lib():
     L.vp_server_close.argtypes = [P]
     L.vp_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int32, C.c_int, P, C.c_int64, P, P]
     L.vp_locus_filter_pack2.argtypes = [P, C.c_int64, C.c_int32, C.POINTER(VpLocusFilter), C.c_int, P, P]
+    L.vp_write_structure.argtypes = [P, C.POINTER(VpWriteOpts)]
     _lib = L
     return L
 

@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "--fmad=false", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"] + ARCH
 
 CU = ["vp_structure.cu", "vp_ingest.cu"]
-CPP = ["vp_data.cpp", "vp_server.cpp"]  # vp_cli.cpp is the driver binary, built with g++ below
+CPP = ["vp_data.cpp", "vp_server.cpp", "vp_write.cpp"]  # vp_cli.cpp is the driver binary, built with g++ below
 
 
 def _newer(target, deps):

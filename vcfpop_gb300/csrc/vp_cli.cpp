@@ -323,117 +323,6 @@ struct Writer {
     void d() { fputs(o.delim.c_str(), f); }
 };
 
-// WriteStructure (src/structure.cpp:86-377)
-// H, D, H2: the run's heterozygosity, net nucleotide distance and per-locus
-// heterozygosity, reduced on the device (vp_chain_divergence)
-void write_run(const Opts& o, const vp_params& P, const vp_result& r, int rep, int id, const std::vector<std::string>& inds,
-               const std::vector<std::string>& pnames, const std::vector<int>& popid, const std::vector<int32_t>& k,
-               const std::vector<std::string>& locs, int S, int maxK, const std::vector<double>& H,
-               const std::vector<double>& D, const std::vector<double>& H2) {
-    char fn[8192];
-    const int K = r.K, N = r.N;
-    const int64_t L = (int64_t)k.size();
-    if (P.writelnl) {
-        snprintf(fn, sizeof fn, "%s.structure.k=%d_rep=%d_id=%d.lnl.txt", o.output.c_str(), K, rep, id);
-        FILE* f = fopen(fn, "wb");
-        Writer w(f, o);
-        fprintf(f, "%d", r.nburnin); w.lb();
-        w.s("Iteration"); w.d(); w.s("lnL"); w.lb();
-        int j = 0;
-        for (int i = 0; i < r.nburnin; i += r.nthinning) { fprintf(f, "%d", i); w.d(); w.real(r.lnl[j++]); w.lb(); }
-        for (int i = 0; i < r.nreps; i += r.nthinning) { fprintf(f, "%d", i + r.nburnin); w.d(); w.real(r.lnl[j++]); w.lb(); }
-        fclose(f);
-    }
-    snprintf(fn, sizeof fn, "%s.structure.k=%d_rep=%d_id=%d.txt", o.output.c_str(), K, rep, id);
-    FILE* f = fopen(fn, "wb");
-    Writer w(f, o);
-    w.lb(); w.lb(); w.s("Parameters:"); w.lb();
-    fprintf(f, "Seed=%lld", (long long)r.seed); w.lb();
-    fprintf(f, "Model=%s,%s,%s", P.admix ? "ADM" : "NOADM", P.locpriori ? "LOC" : "NOLOC", P.fmodel ? "F" : "NOF"); w.lb();
-    fprintf(f, "Number of cluster=%d", K); w.lb();
-    fprintf(f, "Replicate=%d", rep); w.lb();
-    fprintf(f, "Run id=%d", id); w.lb();
-    w.s("Mean value of ln likelihood="); w.real(r.rout[0]); w.lb();
-    w.s("Variance of ln likelihood="); w.real(r.rout[2]); w.lb();
-    w.s("Estimated Ln Prob of Data="); w.real(r.rout[3]); w.lb(); w.lb();
-    const int nf = P.fmodel ? (P.fsame ? 1 : K) : 0, nl = P.difflambda ? K : 1;
-    if (P.locpriori) {
-        w.lb(); w.s("Mean value of r="); w.real(r.rout[4 + nl]);
-        w.lb(); fprintf(f, "Mean value of global %s", P.admix ? "alpha" : "eta");
-        w.lb(); w.d(); w.s("Cluster"); w.lb();
-        for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
-        w.lb();
-        for (int j = 0; j < K; ++j) { w.d(); w.real(r.rout[4 + nl + 1 + j]); }
-        w.lb(); fprintf(f, "Mean value of local %s for each location", P.admix ? "alpha" : "gamma");
-        w.lb(); w.d(); w.s("Cluster"); w.lb(); w.s("Pop");
-        for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
-        for (int i = 0; i < S; ++i) {
-            w.lb(); w.s(pnames[i].c_str());
-            for (int j = 0; j < K; ++j) { w.d(); w.real(r.rout[4 + nl + 1 + K + i * K + j]); }
-        }
-    } else if (P.admix && P.inferalpha) {
-        if (!P.diffalpha) { w.lb(); w.s("Mean value of alpha="); w.real(r.rout[4 + nl]); }
-        else for (int j = 0; j < K; ++j) { w.lb(); fprintf(f, "Mean value of alpha_%d=", j + 1); w.real(r.rout[4 + nl + j]); }
-    }
-    if (P.fmodel) {
-        if (P.fsame) { w.lb(); w.s("Mean value of Fst="); w.real(r.rout[r.rlen - 1]); }
-        else {
-            w.lb(); w.s("Mean value of Fst"); w.lb(); w.d(); w.s("Cluster"); w.lb();
-            for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
-            w.lb();
-            for (int i = 0; i < nf; ++i) { w.d(); w.real(r.rout[r.rlen - nf + i]); }
-        }
-    }
-    // membership of each population from the final Q, Unify(float) per row
-    std::vector<float> O((size_t)S * K, 0.f);
-    w.lb(); w.lb(); fprintf(f, "Proportion of membership of each pre-defined population in each of the %d clusters", K);
-    w.lb(); w.d(); w.s("Cluster"); w.lb(); w.s("Pop");
-    for (int i = 0; i < N; ++i)
-        for (int kk = 0; kk < K; ++kk) O[(size_t)popid[i] * K + kk] += r.Q[(size_t)i * K + kk];
-    for (int s = 0; s < S; ++s) {
-        double sum = 0;
-        for (int kk = 0; kk < K; ++kk) sum += O[(size_t)s * K + kk];
-        double inv = 1.0 / (sum + K * 1e-10);
-        for (int kk = 0; kk < K; ++kk) O[(size_t)s * K + kk] = (float)(((double)O[(size_t)s * K + kk] + 1e-10) * inv);
-    }
-    for (int kk = 0; kk < K; ++kk) { w.d(); fprintf(f, "%d", kk + 1); }
-    for (int s = 0; s < S; ++s) {
-        w.lb(); w.s(pnames[s].c_str());
-        for (int kk = 0; kk < K; ++kk) { w.d(); w.real(O[(size_t)s * K + kk]); }
-    }
-    w.lb(); w.lb(); w.s("Inferred ancestry of individuals");
-    w.lb(); w.d(); w.d(); w.s("Cluster");
-    w.lb(); w.s("Ind"); w.d(); w.s("Pop"); w.d(); w.s("RegL1");
-    for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
-    for (int i = 0; i < N; ++i) {
-        w.lb(); w.s(inds[i].c_str()); w.d(); w.s(pnames[popid[i]].c_str()); w.d(); w.s("Total");
-        for (int kk = 0; kk < K; ++kk) { w.d(); w.real(r.ancestry[(size_t)i * K + kk]); }
-    }
-    w.lb(); w.lb(); w.s("Allele-frequency divergence among pops (Net nucleotide distance)");
-    w.lb(); w.d(); w.s("Cluster"); w.lb(); w.s("Cluster");
-    for (int j = 0; j < K; ++j) { w.d(); fprintf(f, "%d", j + 1); }
-    for (int i = 0; i < K; ++i) {
-        w.lb(); fprintf(f, "%d", i + 1);
-        for (int j = 0; j < K; ++j) { w.d(); w.real(D[(size_t)i * K + j]); }
-    }
-    if (o.diversity) {
-        w.lb(); w.lb(); w.s("Estimated genetic diversity in each cluster");
-        w.lb(); w.s("Locus"); w.d(); w.s("Cluster"); w.d(); w.s("Heterozygosity");
-        for (int a = 0; a < maxK; ++a) { w.d(); fprintf(f, "Allele%d", a); }
-        for (int kk = 0; kk < K; ++kk) { w.lb(); w.s(kk ? "" : "Average"); w.d(); fprintf(f, "%d", kk + 1); w.real(H[kk]); }
-        int64_t off = 0;
-        for (int64_t l = 0; l < L; ++l) {
-            for (int kk = 0; kk < K; ++kk) {
-                w.lb(); w.s(kk ? "" : locs[l].c_str()); w.d(); fprintf(f, "%d", kk + 1); w.d();
-                w.real(H2[(size_t)kk * L + l]);
-                for (int a = 0; a < k[l]; ++a) { w.d(); w.real(r.freqm[(size_t)kk * r.KT + off + a]); }
-            }
-            off += k[l];
-        }
-    }
-    fclose(f);
-}
-
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -545,11 +434,6 @@ int main(int argc, char** argv) {
     if (vp_dataset_prepare(&in, &ds)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
     vp_dataset_info info;
     vp_dataset_info_get(ds, &info);
-    std::vector<int64_t> order(info.n_loc);
-    vp_dataset_order(ds, order.data());
-    std::vector<int32_t> ks(info.n_loc);
-    std::vector<std::string> lnames(info.n_loc);
-    for (int64_t l = 0; l < info.n_loc; ++l) { ks[l] = v.k[order[l]]; lnames[l] = v.locs[order[l]]; }
     vp_ctx* ctx = nullptr;
     if (vp_open(ds, o.device, &ctx)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
     // the tensor-core K-sweep runs no-admixture chains without location
@@ -576,22 +460,27 @@ int main(int argc, char** argv) {
     std::vector<vp_chain*> cs;
     for (auto& r : runs) cs.push_back(r.c);
     if (vp_finish(cs.data(), (int)cs.size())) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+    // the run files through the library's writer (WriteStructure), from each
+    // chain's device state
+    std::vector<const char*> ind_c, pop_c, loc_c;
+    for (auto& n : inds) ind_c.push_back(n.c_str());
+    for (auto& n : pn) pop_c.push_back(n.c_str());
+    for (auto& n : v.locs) loc_c.push_back(n.c_str());
+    vp_write_opts wo{};
+    wo.prefix = o.output.c_str();
+    wo.ind_names = ind_c.data(); wo.pop_names = pop_c.data(); wo.loc_names = loc_c.data();
+    wo.decimal = o.decimal; wo.comma = o.delim == ","; wo.unix_lb = o.lb == "\n"; wo.diversity = o.diversity;
     std::vector<std::array<double, 3>> table;
     for (auto& run : runs) {
+        wo.rep = run.rep;
+        wo.id = run.id;
+        if (vp_write_structure(run.c, &wo)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
         vp_result r;
         vp_chain_sizes(run.c, &r);
-        std::vector<double> rout(r.rlen), lnl(std::max(r.nlnl, 1)), anc((size_t)r.N * r.K);
-        std::vector<float> Q((size_t)r.N * r.K), fm((size_t)r.K * r.KT);
-        r.rout = rout.data(); r.lnl = lnl.data(); r.Q = Q.data(); r.ancestry = anc.data(); r.freqm = fm.data();
-        if (vp_chain_result(run.c, &r)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
-        vp_params p = o.p;
-        p.K = run.K;
-        std::vector<double> H(r.K), D((size_t)r.K * r.K), H2(o.diversity ? (size_t)r.K * info.n_loc : 0);
-        if (vp_chain_divergence(run.c, H.data(), D.data(), o.diversity ? H2.data() : nullptr)) {
-            fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error());
-            return 1;
-        }
-        write_run(o, p, r, run.rep, run.id, inds, pn, popid, ks, lnames, S, info.max_alleles, H, D, H2);
+        std::vector<double> rout(r.rlen);
+        vp_result q{};
+        q.rout = rout.data();
+        if (vp_chain_result(run.c, &q)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
         table.push_back({rout[0], rout[2], rout[3]});
         vp_chain_destroy(run.c);
     }

@@ -60,3 +60,6 @@ void vp_dataset_retain(const vp_dataset* ds);
 int vp_finish_issue(vp_chain** cs, int32_t n);
 // sweeps issued so far and in total for one chain
 void vp_chain_progress(const vp_chain* c, int64_t* issued, int64_t* total);
+// the dataset a chain's context holds, and the chain's parameters
+const vp_dataset* vp_chain_dataset(const vp_chain* c);
+void vp_chain_params(const vp_chain* c, vp_params* p);

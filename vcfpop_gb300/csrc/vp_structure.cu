@@ -897,6 +897,9 @@ extern "C" int vp_finish(vp_chain** cs, int32_t n) {
     return rc ? rc : vp_sync(cs[0]->ctx);
 }
 
+const vp_dataset* vp_chain_dataset(const vp_chain* c) { return c->ctx->hold; }
+void vp_chain_params(const vp_chain* c, vp_params* p) { *p = c->P; }
+
 void vp_chain_progress(const vp_chain* c, int64_t* issued, int64_t* total) {
     *issued = c->issued;
     *total = c->total;

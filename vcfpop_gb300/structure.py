@@ -189,6 +189,17 @@ class Chain:
         """Results; `final` (after vp_finish) adds the normalised ancestry."""
         return chain_result(self.h, final)
 
+    def write(self, prefix: str, rep: int, run_id: int, ind_names, pop_names, loc_names, decimal: int = 5,
+              diversity: bool = False, comma: bool = False, unix: bool = False) -> None:
+        """The run's result files in the reference's format (vp_write_structure);
+        loc_names in the dataset's input locus order."""
+        def arr(names):
+            return (C.c_char_p * len(names))(*[n.encode() for n in names])
+        keep = [arr(ind_names), arr(pop_names), arr(loc_names)]
+        o = B.VpWriteOpts(prefix.encode(), rep, run_id, keep[0], keep[1], keep[2], decimal, int(comma), int(unix),
+                          int(diversity))
+        B.check(B.lib().vp_write_structure(self.h, C.byref(o)))
+
     def divergence(self, per_locus: bool = False) -> dict:
         """Heterozygosity H[K], net nucleotide distance D[K, K] (and the
         per-locus heterozygosity [K, L]) of a finished chain, on the device."""
