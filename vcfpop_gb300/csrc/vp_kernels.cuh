@@ -305,10 +305,13 @@ __global__ void k_update_p_ctr(const DevChain* chains) {
 // copies of ln p_{k,l,allele}. One thread per individual, 128 per CTA; grid.y
 // splits the loci into chunks whose FP64 partials are summed in a fixed order
 // by the sampling kernel. Biallelic diploid data: each 32-locus slice of the
-// genotype words and of the per-genotype log-probability table is staged in
-// shared memory, and a thread adds table[code][k] for its individual; FP32
-// sums over a slice are folded into Kahan-compensated FP32 totals (FP64 adds
-// are slow on this part), converted to FP64 once per chunk.
+// per-genotype log-probability table is staged in shared memory and folded
+// into a table per locus pair (16 code pairs: the sum of the two loci's
+// entries), so one 16-byte shared load and four adds serve two loci and four
+// clusters; the slice's genotype words are staged transposed, so a thread
+// takes the codes of four loci with one 16-byte load. FP32 sums over a slice
+// are folded into Kahan-compensated FP32 totals (FP64 adds are slow on this
+// part), converted to FP64 once per chunk.
 constexpr int LL_SL = 32;
 template <int KC>
 __device__ __forceinline__ void kahan_fold(float* acc, float* s, float* cmp) {
@@ -321,11 +324,18 @@ __device__ __forceinline__ void kahan_fold(float* acc, float* s, float* cmp) {
         acc[k] = 0.f;
     }
 }
+// row stride (floats) of the staged tables: 16-byte chunks in an odd count,
+// so rows that differ by fewer than 8 land on different banks
+template <int KC>
+__host__ __device__ constexpr int ll_stride() { return (KC / 4) % 2 ? KC : KC + 4; }
 template <int KC>
 __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int kgroups, int force) {
-    constexpr int TS = KC + 4;  // padded stride of one genotype row of the table
+    constexpr int TS = ll_stride<KC>();
+    constexpr int GW = LL_BLOCK / 16;          // genotype words per CTA and locus
+    constexpr int GS = LL_SL + 4;              // padded row of the transposed words
     __shared__ __align__(16) float sT[LL_SL][4][TS];
-    __shared__ uint32_t sG[LL_SL][LL_BLOCK / 16];
+    __shared__ __align__(16) float sP[LL_SL / 2][16][TS];
+    __shared__ __align__(16) uint32_t sG[GW][GS];
     const DevChain& c = chains[blockIdx.z / kgroups];
     const int kg0 = (blockIdx.z % kgroups) * KC;
     const DevData& D = c.D;
@@ -342,29 +352,41 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
     const bool live = i < D.N;
     if (D.packed2) {
         const int w0 = i0 >> 4;
+        const int wsel = threadIdx.x >> 4, sh = (threadIdx.x & 15) * 2;
         for (int64_t ls = l0; ls < l1; ls += LL_SL) {
             const int nl = (int)min((int64_t)LL_SL, l1 - ls);
             __syncthreads();
+            // single-locus rows (zero past the chunk: those loci add nothing)
             for (int j = threadIdx.x; j < LL_SL * 4 * KC; j += LL_BLOCK) {
                 int kk = j % KC, code = (j / KC) & 3, ll = j / (4 * KC);
                 float v = 0.f;
                 if (ll < nl && kg0 + kk < K) v = __ldg(c.lt + ((ls + ll) * 4 + code) * c.kp + kg0 + kk);
                 sT[ll][code][kk] = v;
             }
-            for (int j = threadIdx.x; j < LL_SL * (LL_BLOCK / 16); j += LL_BLOCK) {
-                int w = j % (LL_BLOCK / 16), ll = j / (LL_BLOCK / 16);
-                sG[ll][w] = (ll < nl && w0 + w < D.Nw) ? __ldg(D.g2 + (ls + ll) * D.Nw + w0 + w) : 0xFFFFFFFFu;
+            for (int j = threadIdx.x; j < LL_SL * GW; j += LL_BLOCK) {
+                int ll = j % LL_SL, w = j / LL_SL;
+                sG[w][ll] = (ll < nl && w0 + w < D.Nw) ? __ldg(D.g2 + (ls + ll) * D.Nw + w0 + w) : 0xFFFFFFFFu;
             }
             __syncthreads();
-            const int wsel = threadIdx.x >> 4, sh = (threadIdx.x & 15) * 2;
-#pragma unroll 4
-            for (int ll = 0; ll < nl; ++ll) {
-                const int code = (sG[ll][wsel] >> sh) & 3;
-                const float4* t = reinterpret_cast<const float4*>(&sT[ll][code][0]);
+            // pair rows: sP[p][a | b << 2] = sT[2p][a] + sT[2p + 1][b]
+            for (int j = threadIdx.x; j < (LL_SL / 2) * 16 * KC; j += LL_BLOCK) {
+                int kk = j % KC, cp = (j / KC) & 15, p = j / (16 * KC);
+                sP[p][cp][kk] = sT[2 * p][cp & 3][kk] + sT[2 * p + 1][cp >> 2][kk];
+            }
+            __syncthreads();
+            const uint4* gw = reinterpret_cast<const uint4*>(&sG[wsel][0]);
+#pragma unroll 2
+            for (int q = 0; q < LL_SL / 4; ++q) {
+                const uint4 g = gw[q];
+                const int ca = ((g.x >> sh) & 3) | (((g.y >> sh) & 3) << 2);
+                const int cb = ((g.z >> sh) & 3) | (((g.w >> sh) & 3) << 2);
+                const float4* ta = reinterpret_cast<const float4*>(&sP[2 * q][ca][0]);
+                const float4* tb = reinterpret_cast<const float4*>(&sP[2 * q + 1][cb][0]);
 #pragma unroll
-                for (int q = 0; q < KC / 4; ++q) {
-                    float4 v = t[q];
-                    acc[4 * q] += v.x; acc[4 * q + 1] += v.y; acc[4 * q + 2] += v.z; acc[4 * q + 3] += v.w;
+                for (int r = 0; r < KC / 4; ++r) {
+                    const float4 va = ta[r], vb = tb[r];
+                    acc[4 * r] += va.x; acc[4 * r + 1] += va.y; acc[4 * r + 2] += va.z; acc[4 * r + 3] += va.w;
+                    acc[4 * r] += vb.x; acc[4 * r + 1] += vb.y; acc[4 * r + 2] += vb.z; acc[4 * r + 3] += vb.w;
                 }
             }
             kahan_fold<KC>(acc, s, cmp);
