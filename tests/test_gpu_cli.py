@@ -129,3 +129,33 @@ def test_cli_default_flags_run_the_tensor_core_batch(tmp_path):
         g = open(out["default"] / f"out.structure.k={K}_rep=1_id={K}.txt", "rb").read().decode()
         p = open(out["plain"] / f"out.structure.k={K}_rep=1_id={K}.txt", "rb").read().decode()
         assert _shape(g) == _shape(p)
+
+
+def test_cli_individual_filter_runs_on_the_kept_individuals(tmp_path):
+    """-f -f_itype=[0.9,1]: the run's ancestry table lists exactly the
+    individuals whose typed-locus count passes the reference's window
+    (src/filter.cpp:457-465), in file order."""
+    import numpy as np
+    from vcfpop_gb300 import synth
+    d = synth.fmodel(5, 100, 800, 2, 0.1, 0.02)
+    extra = np.random.default_rng(5).random((800, 100)) < 0.3
+    extra[:, 1::4] = extra[:, 2::4] = extra[:, 3::4] = False
+    d["G"][extra] = -1
+    vcf = str(tmp_path / "d.vcf")
+    synth.write_vcf(vcf, d)
+    L = d["G"].shape[0]
+    ntype = (d["G"][:, :, 0] >= 0).sum(axis=0)
+    keep = np.where((ntype >= int(0.9 * L + 0.5)) & (ntype <= int(L + 0.5)))[0]
+    subprocess.run([CLI, f"-g_input={vcf}", f"-g_output={tmp_path}/out", "-structure", "-f", "-f_itype=[0.9,1]",
+                    "-structure_krange=[2,2]", "-structure_nburnin=10", "-structure_nreps=20",
+                    "-structure_admix=no", "-structure_nadmburnin=0"], check=True)
+    lines = open(tmp_path / "out.structure.k=2_rep=1_id=1.txt", "rb").read().decode().replace("\r", "").split("\n")
+    i = next(j for j, ln in enumerate(lines) if ln.startswith("Inferred ancestry of individuals"))
+    names = []
+    for ln in lines[i + 3:]:
+        if not ln.strip():
+            break
+        names.append(ln.split("\t")[0])
+    header = open(vcf).read().split("\n")
+    samples = next(h for h in header if h.startswith("#CHROM")).split("\t")[9:]
+    assert names == [samples[j] for j in keep]

@@ -38,6 +38,10 @@ struct Opts {
     int form = -1;                // -gb300_form: VP_FORM_*, or -1 = tensor-core form where it applies
     bool filter = false;          // -f, with -f_* windows: the locus filter
     vp_locus_filter lf{};
+    // the individual filter (-f_itype, -f_iploidy), applied before the locus filter
+    bool itype_b = false, iploidy_b = false;
+    double itype_min = 0, itype_max = 0;
+    int iploidy_min = 0, iploidy_max = 0;
     vp_params p;
     std::vector<std::string> argv;
 };
@@ -48,6 +52,7 @@ bool parse(int argc, char** argv, Opts& o) {
     vp_params_default(&o.p);
     o.p.rng = VP_RNG_COUNTER;
     bool structure = false;
+    std::vector<std::string> unimplemented;
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
         o.argv.push_back(a);
@@ -108,17 +113,21 @@ bool parse(int argc, char** argv, Opts& o) {
         else if (k == "-f_pic") o.lf.pic_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.pic_min, &o.lf.pic_max) == 2;
         else if (k == "-f_ae") o.lf.ae_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.ae_min, &o.lf.ae_max) == 2;
         else if (k == "-f_I") o.lf.I_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.I_min, &o.lf.I_max) == 2;
-        else if (k.rfind("-f_", 0) == 0) {
-            // every other filter of the reference (-f_pval, -f_qual, -f_dp,
-            // -f_gq, -f_itype, -f_iploidy, -f_windowsize, ...) would change
-            // which loci or calls the clustering sees: refuse it rather than
-            // run on unfiltered data
-            fprintf(stderr, "vcfpop-gb300: the filter %s is not implemented (implemented: -f_bmaf -f_k -f_n "
-                            "-f_ptype -f_he -f_ho -f_pic -f_ae -f_I)\n", k.c_str());
-            return false;
-        }
+        else if (k == "-f_itype") o.itype_b = sscanf(v.c_str(), "[%lf,%lf]", &o.itype_min, &o.itype_max) == 2;
+        else if (k == "-f_iploidy") o.iploidy_b = sscanf(v.c_str(), "[%d,%d]", &o.iploidy_min, &o.iploidy_max) == 2;
+        else if (k.rfind("-f_", 0) == 0) unimplemented.push_back(k);
         // other -g_* and -structure_* flags (threads, SIMD, plots, streams) do
         // not apply to the GPU path and are accepted silently
+    }
+    // the reference applies its -f_* windows only under -f
+    // (src/parameters.cpp:1336-1343); every other filter of the reference
+    // (-f_pval, -f_qual, -f_dp, -f_gq, -f_windowsize, ...) would change which
+    // loci, calls or individuals the clustering sees: refuse it rather than
+    // run on unfiltered data
+    if (o.filter && !unimplemented.empty()) {
+        fprintf(stderr, "vcfpop-gb300: the filter %s is not implemented (implemented: -f_bmaf -f_k -f_n -f_ptype "
+                        "-f_he -f_ho -f_pic -f_ae -f_I -f_itype -f_iploidy)\n", unimplemented[0].c_str());
+        return false;
     }
     if (!structure) { fprintf(stderr, "vcfpop-gb300: only -structure is implemented\n"); return false; }
     if (o.input.empty()) { fprintf(stderr, "vcfpop-gb300: -g_input is required\n"); return false; }
@@ -323,6 +332,79 @@ struct Writer {
     void d() { fputs(o.delim.c_str(), f); }
 };
 
+// The individual filter (MarkerIndividual and RemoveIndividual,
+// src/filter.cpp:398-475 and 565-605), which the reference applies before the
+// locus filter. -f_itype: an individual is removed when its count of typed
+// loci lies outside (int64)(min * L + 0.5) .. (int64)(max * L + 0.5).
+// -f_iploidy: the reference compares the window with the smallest and the
+// largest ploidy over all individuals (the globals minploidy and maxploidy;
+// an individual without any typed call counts as ploidy 0), not with each
+// individual's own, so either every individual passes or every one is
+// removed, which the reference reports as an error; that is reproduced.
+bool individual_filter(const Opts& o, Vcf& v, bool dev_ingest, std::vector<uint32_t>& packed, std::vector<int>& pop) {
+    const int N = (int)v.inds.size();
+    const int64_t L = (int64_t)v.k.size();
+    const int Nw = (N + 15) / 16;
+    std::vector<int64_t> ntype(N, 0);
+    std::vector<int> vmin(N, 100), vmax(N, 0);
+    for (int64_t l = 0; l < L; ++l)
+        for (int i = 0; i < N; ++i) {
+            bool typed;
+            if (dev_ingest) typed = ((packed[(size_t)l * Nw + (i >> 4)] >> (2 * (i & 15))) & 3u) != 3u;
+            else typed = v.G[((size_t)l * N + i) * v.vmax] >= 0;
+            if (typed) {
+                ntype[i]++;
+                vmin[i] = std::min(vmin[i], v.ploidy[i]);
+                vmax[i] = std::max(vmax[i], v.ploidy[i]);
+            }
+        }
+    int minploidy = 100, maxploidy = 0;
+    for (int i = 0; i < N; ++i) {
+        minploidy = std::min(minploidy, vmin[i] == 100 ? 0 : vmin[i]);
+        maxploidy = std::max(maxploidy, vmax[i]);
+    }
+    const int64_t tmin = (int64_t)(o.itype_min * L + 0.5), tmax = (int64_t)(o.itype_max * L + 0.5);
+    std::vector<int> keep;
+    for (int i = 0; i < N; ++i) {
+        bool pass = true;
+        if (o.itype_b && (tmin > ntype[i] || ntype[i] > tmax)) pass = false;
+        if (o.iploidy_b && (o.iploidy_min > minploidy || minploidy > o.iploidy_max)) pass = false;
+        if (o.iploidy_b && (o.iploidy_min > maxploidy || maxploidy > o.iploidy_max)) pass = false;
+        if (pass) keep.push_back(i);
+    }
+    if (keep.empty()) {
+        fprintf(stderr, "vcfpop-gb300: all %d individuals are excluded from the analysis by the individual filter\n", N);
+        return false;
+    }
+    fprintf(stderr, "vcfpop-gb300: individual filter kept %d of %d individuals\n", (int)keep.size(), N);
+    if ((int)keep.size() == N) return true;
+    const int M = (int)keep.size(), Mw = (M + 15) / 16;
+    std::vector<std::string> inds(M);
+    std::vector<int32_t> ploidy(M);
+    std::vector<int> pp(M);
+    for (int j = 0; j < M; ++j) { inds[j] = v.inds[keep[j]]; ploidy[j] = v.ploidy[keep[j]]; pp[j] = pop[keep[j]]; }
+    if (dev_ingest) {
+        std::vector<uint32_t> np((size_t)L * Mw, 0);
+        for (int64_t l = 0; l < L; ++l)
+            for (int j = 0; j < Mw * 16; ++j) {
+                uint32_t code = 3;
+                if (j < M) code = (packed[(size_t)l * Nw + (keep[j] >> 4)] >> (2 * (keep[j] & 15))) & 3u;
+                np[(size_t)l * Mw + (j >> 4)] |= code << (2 * (j & 15));
+            }
+        packed.swap(np);
+    } else {
+        std::vector<int8_t> G((size_t)L * M * v.vmax);
+        for (int64_t l = 0; l < L; ++l)
+            for (int j = 0; j < M; ++j)
+                memcpy(&G[((size_t)l * M + j) * v.vmax], &v.G[((size_t)l * N + keep[j]) * v.vmax], v.vmax);
+        v.G.swap(G);
+    }
+    v.inds.swap(inds);
+    v.ploidy.swap(ploidy);
+    pop.swap(pp);
+    return true;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -332,11 +414,15 @@ int main(int argc, char** argv) {
     std::vector<uint32_t> dev_packed;   // device-parsed 2-bit matrix, file order of individuals
     const bool dev_ingest = read_vcf_device(o, v, dev_packed);
     if (!dev_ingest && !read_vcf(o.input, v)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
-    const int N = (int)v.inds.size();
+    const int N0 = (int)v.inds.size();
     const int64_t L0 = (int64_t)v.k.size();
     std::vector<int> pop;
     std::vector<std::string> pnames;
-    populations(o.indtext, N, pop, pnames);
+    populations(o.indtext, N0, pop, pnames);
+    if (o.filter && (o.itype_b || o.iploidy_b)) {
+        if (!individual_filter(o, v, dev_ingest, dev_packed, pop)) return 1;
+    }
+    const int N = (int)v.inds.size();
     // group individuals by population in the populations' order (stable)
     std::vector<int> perm(N);
     for (int i = 0; i < N; ++i) perm[i] = i;
