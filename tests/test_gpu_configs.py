@@ -164,7 +164,7 @@ def test_c2_admixture_steps(c2):
     Mi bit-exact, Record's admixture likelihood within 1e-5), one Metropolis
     Q step and one alpha step."""
     od, oc, ds, ctx, gc = _pair(c2, 5, admix=1, inferalpha=1, nburnin=5000, nreps=10000)
-    assert ds.N == 2000 and d["G"].shape[0] == 50000   # L before the monomorphic filter
+    assert ds.N == 2000 and c2["G"].shape[0] == 50000   # L before the monomorphic filter
     assert np.array_equal(gc.get("MI"), oc.get("MI").astype(np.int32))
     assert np.array_equal(gc.get("NI"), oc.get("NI"))
     # UpdateZ at a Gibbs sweep, after the oracle's UpdateP and UpdateQ

@@ -65,6 +65,27 @@ __device__ __forceinline__ bool record_at(const DevChain& c, int m) {
     return (c.writelnl && m < c.nburnin && m % c.nthinning == 0) || (m >= c.nburnin && (m - c.nburnin) % c.nthinning == 0);
 }
 
+// The block a kernel of the sweep works on. A launch of one chain (or of a
+// tensor-core batch) uses the hardware indices. A cohort launch -- one launch
+// of a kernel for the chains of several runs, each with its own dataset --
+// passes a map with one entry per block: {the index that blockIdx.z would
+// have in the chain's own launch, with the chain's slot in the cohort's
+// DevChain array folded in; blockIdx.x and blockIdx.y of that launch; its
+// gridDim.x}, so every chain's blocks do exactly the work, in the same
+// decomposition and order, that its own launch would (no kernel of the sweep
+// reads gridDim.y).
+struct VBlock {
+    int x, y, z, gx;
+};
+__device__ __forceinline__ VBlock vblock(const int4* map) {
+    if (!map) return VBlock{(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.x};
+    const int4 t = __ldg(map + blockIdx.x);
+    return VBlock{t.y, t.z, t.x, t.w};
+}
+// a cohort keeps launching for runs whose sweeps are all done; their blocks
+// return at once
+__device__ __forceinline__ bool run_over(const DevChain& c) { return c.ctl->m >= c.nburnin + c.nreps; }
+
 // ---------------------------------------------------------------------------
 // block reductions
 template <typename T>
@@ -240,8 +261,10 @@ __global__ void k_refresh_lt(const DevChain* chains) {
 
 // reference streams: 128 block streams RNG(seed + m*128 + b, SALT_UPDATEP),
 // each serial over its share of the K*L range
-__global__ void k_update_p_ref(const DevChain* chains) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_update_p_ref(const DevChain* chains, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
     int b = threadIdx.x;
@@ -268,11 +291,13 @@ __global__ void k_update_p_ref(const DevChain* chains) {
 }
 
 // counter streams: one thread per (k, l)
-__global__ void k_update_p_ctr(const DevChain* chains) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_update_p_ctr(const DevChain* chains, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
-    int64_t kl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t kl = vb.x * (int64_t)blockDim.x + threadIdx.x;
     if (kl >= (int64_t)K * D.L) return;
     int k = (int)(kl / D.L);
     int64_t l = kl % D.L;
@@ -329,21 +354,23 @@ __device__ __forceinline__ void kahan_fold(float* acc, float* s, float* cmp) {
 template <int KC>
 __host__ __device__ constexpr int ll_stride() { return (KC / 4) % 2 ? KC : KC + 4; }
 template <int KC>
-__global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int kgroups, int force) {
+__global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int kgroups, int force, const int4* map = nullptr) {
     constexpr int TS = ll_stride<KC>();
     constexpr int GW = LL_BLOCK / 16;          // genotype words per CTA and locus
     constexpr int GS = LL_SL + 4;              // padded row of the transposed words
     __shared__ __align__(16) float sT[LL_SL][4][TS];
     __shared__ __align__(16) float sP[LL_SL / 2][16][TS];
     __shared__ __align__(16) uint32_t sG[GW][GS];
-    const DevChain& c = chains[blockIdx.z / kgroups];
-    const int kg0 = (blockIdx.z % kgroups) * KC;
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z / kgroups];
+    if (map && run_over(c)) return;
+    const int kg0 = (vb.z % kgroups) * KC;
     const DevData& D = c.D;
     const int K = c.K;
     if (!force && !binaryq_at(c, c.ctl->m)) return;
-    const int i0 = blockIdx.x * LL_BLOCK;
+    const int i0 = vb.x * LL_BLOCK;
     const int i = i0 + threadIdx.x;
-    const int64_t l0 = (int64_t)blockIdx.y * c.lchunk;
+    const int64_t l0 = (int64_t)vb.y * c.lchunk;
     const int64_t l1 = min(D.L, l0 + c.lchunk);
     if (l0 >= D.L) return;
     float acc[KC], s[KC], cmp[KC];
@@ -407,7 +434,7 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
         kahan_fold<KC>(acc, s, cmp);
     }
     if (!live) return;
-    double* out = c.LLp + ((int64_t)blockIdx.y * D.N + i) * K;
+    double* out = c.LLp + ((int64_t)vb.y * D.N + i) * K;
 #pragma unroll
     for (int k = 0; k < KC; ++k)
         if (kg0 + k < K) out[kg0 + k] = (double)s[k] - (double)cmp[k];
@@ -543,8 +570,10 @@ __device__ double sample_warp(const DevChain& c, int i, int m, int lane) {
     return __shfl_sync(0xffffffffu, z < 32 ? v0 : v1, z & 31);
 }
 
-__global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain* chains, int force) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain* chains, int force, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K, N = D.N, m = c.ctl->m;
     if (!force && !binaryq_at(c, m)) return;
@@ -552,7 +581,7 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain*
     const bool ref = c.rng == 0;
     if (force) {
         // likelihood only (parity tests): sum the chunk partials
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+        for (int i = vb.x * blockDim.x + threadIdx.x; i < N; i += vb.gx * blockDim.x)
             for (int k = 0; k < K; ++k) {
                 double v = 0;
                 for (int ch = 0; ch < c.nchunk; ++ch) v += c.LLp[((int64_t)ch * N + i) * K + k];
@@ -561,7 +590,7 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain*
         return;
     }
     if (ref) {
-        if (blockIdx.x) return;
+        if (vb.x) return;
         if (threadIdx.x == 0) {
             Rng64 r; r.init(c.seed + (uint64_t)m, VP_SALT_UPDATEQ);
             double lnl = 0;
@@ -570,13 +599,13 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain*
         }
     } else {
         const int lane = threadIdx.x & 31;
-        const int i = blockIdx.x * (SAMPLE_BLOCK / 32) + (threadIdx.x >> 5);
+        const int i = vb.x * (SAMPLE_BLOCK / 32) + (threadIdx.x >> 5);
         double lnl = 0;
         if (i < N) lnl = sample_warp(c, i, m, lane);
         double t = block_sum(lane == 0 ? lnl : 0.0, sh);
-        if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
-        if (!last_block_done(c.ctl, gridDim.x)) return;
-        const double tot = block_sum_partials(c.lnlp, gridDim.x, sh);
+        if (threadIdx.x == 0) c.lnlp[vb.x] = t;
+        if (!last_block_done(c.ctl, vb.gx)) return;
+        const double tot = block_sum_partials(c.lnlp, vb.gx, sh);
         if (threadIdx.x == 0) {
             c.ctl->lnl = tot;
             c.ctl->done = 0;
@@ -598,14 +627,16 @@ __global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_noadmix(const DevChain*
 // labels) into a lane-private shared histogram (no atomics, no conflicts), and
 // the warp reduces it. General data: per-warp shared histogram with atomics.
 constexpr int COUNT_WARPS = 4;
-__global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevChain* chains, int force) {
+__global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevChain* chains, int force, const int4* map = nullptr) {
     extern __shared__ int32_t hist[];
-    const DevChain& c = chains[blockIdx.z];
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K;
     if (!force && !binaryq_at(c, c.ctl->m)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t l = (int64_t)blockIdx.x * COUNT_WARPS + warp;
+    const int64_t l = (int64_t)vb.x * COUNT_WARPS + warp;
     if (D.packed2) {
         int32_t* h = hist + warp * (2 * K * 32);
         for (int j = 0; j < 2 * K; ++j) h[j * 32 + lane] = 0;
@@ -673,10 +704,12 @@ __global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevCha
 // and allele-0 copies = 2 x typed - allele-1 copies. Integer and exact; the
 // same Ni as k_count_noadmix. grid.z = cluster groups of KC.
 template <int KC>
-__global__ void __launch_bounds__(256) k_count_packed(const DevChain* chains, int kgroups, int force) {
+__global__ void __launch_bounds__(256) k_count_packed(const DevChain* chains, int kgroups, int force, const int4* map = nullptr) {
     extern __shared__ uint32_t smask[];   // [KC][Nw] masks, then [KC] cluster sizes
-    const DevChain& c = chains[blockIdx.z / kgroups];
-    const int kg0 = (blockIdx.z % kgroups) * KC;
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z / kgroups];
+    if (map && run_over(c)) return;
+    const int kg0 = (vb.z % kgroups) * KC;
     const DevData& D = c.D;
     const int K = c.K, Nw = D.Nw;
     if (!force && !binaryq_at(c, c.ctl->m)) return;
@@ -709,7 +742,7 @@ __global__ void __launch_bounds__(256) k_count_packed(const DevChain* chains, in
         if (cnt[k]) atomicAdd(&nk[k], cnt[k]);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-    for (int64_t l = (int64_t)blockIdx.x * nwarp + warp; l < D.L; l += (int64_t)gridDim.x * nwarp) {
+    for (int64_t l = (int64_t)vb.x * nwarp + warp; l < D.L; l += (int64_t)vb.gx * nwarp) {
         const uint32_t* row = D.g2 + l * Nw;
         int a1[KC], n3[KC];
 #pragma unroll
@@ -777,8 +810,10 @@ __device__ __forceinline__ void dirichlet_ctr(Philox& p, float* q, const double*
 
 // UpdateQAdmix (src/structure.cpp:984-1004): Q_i ~ Dirichlet(alpha + Mi_i),
 // used by the admixture model and the no-admixture burn-in
-__global__ void k_update_q_admix(const DevChain* chains, int force) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_update_q_admix(const DevChain* chains, int force, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
     if (!force) {
@@ -786,7 +821,7 @@ __global__ void k_update_q_admix(const DevChain* chains, int force) {
         if (!c.admix && m >= c.nadmburnin) return;
     }
     if (c.rng == 0) {
-        if (blockIdx.x || threadIdx.x) return;
+        if (vb.x || threadIdx.x) return;
         Rng64 r; r.init(c.seed + (uint64_t)m, VP_SALT_UPDATEQ);
         for (int i = 0; i < D.N; ++i)
             if (D.vt[i])
@@ -794,7 +829,7 @@ __global__ void k_update_q_admix(const DevChain* chains, int force) {
                               c.Mi + (int64_t)i * K, K);
         return;
     }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
+    for (int i = vb.x * blockDim.x + threadIdx.x; i < D.N; i += vb.gx * blockDim.x) {
         if (!D.vt[i]) continue;
         Philox p; p.init(c.seed, ST_Q | ((uint32_t)m << 4), (uint32_t)i, 1);
         dirichlet_ctr(p, c.Q + (int64_t)i * K, c.locpriori ? c.AlphaLocal + D.popid[i] * K : c.Alpha,
@@ -803,13 +838,15 @@ __global__ void k_update_q_admix(const DevChain* chains, int force) {
 }
 
 // UpdateQMetro (src/structure.cpp:1006-1086): proposals Q'_i ~ Dirichlet(alpha)
-__global__ void k_metro_propose(const DevChain* chains, int force) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_metro_propose(const DevChain* chains, int force, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
     if (!force && !metro_turn(c, m)) return;
     if (c.rng == 0) {
-        if (blockIdx.x || threadIdx.x) return;
+        if (vb.x || threadIdx.x) return;
         Rng64 r; r.init(c.seed + (uint64_t)m, VP_SALT_UPDATEQ);
         for (int i = 0; i < D.N; ++i)
             if (D.vt[i])
@@ -818,7 +855,7 @@ __global__ void k_metro_propose(const DevChain* chains, int force) {
         *c.rstate = r;  // the acceptance draws continue this stream
         return;
     }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
+    for (int i = vb.x * blockDim.x + threadIdx.x; i < D.N; i += vb.gx * blockDim.x) {
         if (!D.vt[i]) continue;
         Philox p; p.init(c.seed, ST_METRO_P | ((uint32_t)m << 4), (uint32_t)i, 0);
         dirichlet_ctr(p, c.Qprop + (int64_t)i * K, c.locpriori ? c.AlphaLocal + D.popid[i] * K : c.Alpha,
@@ -836,18 +873,20 @@ __global__ void k_metro_propose(const DevChain* chains, int force) {
 // every K). Defined after the per-copy label kernel, whose slice constants it
 // shares.
 template <int KM, bool EXACT>
-__global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int force);
+__global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int force, const int4* map = nullptr);
 
-__global__ void k_metro_accept(const DevChain* chains, int force) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_metro_accept(const DevChain* chains, int force, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
     if (!force && !metro_turn(c, m)) return;
     const bool ref = c.rng == 0;
-    if (ref && (blockIdx.x || threadIdx.x)) return;
+    if (ref && (vb.x || threadIdx.x)) return;
     Rng64 r;
     if (ref) r = *c.rstate;
-    for (int i = ref ? 0 : blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += ref ? 1 : gridDim.x * blockDim.x) {
+    for (int i = ref ? 0 : vb.x * blockDim.x + threadIdx.x; i < D.N; i += ref ? 1 : vb.gx * blockDim.x) {
         double d = 0;
         const int nm = (int)((D.L + c.zadm_lc - 1) / c.zadm_lc);   // k_metro_ratio's locus ranges
         for (int ch = 0; ch < nm; ++ch) d += c.metrop[(int64_t)ch * D.N + i];
@@ -866,10 +905,12 @@ __global__ void k_metro_accept(const DevChain* chains, int force) {
 }
 
 // Zero Mi and Ni ahead of the per-copy label draws
-__global__ void k_zero_counts(const DevChain* chains, int force) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_zero_counts(const DevChain* chains, int force, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     if (!force && binaryq_at(c, c.ctl->m)) return;
-    int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+    int64_t tid = vb.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)vb.gx * blockDim.x;
     for (int64_t j = tid; j < (int64_t)c.D.N * c.K; j += nt) c.Mi[j] = 0;
     for (int64_t j = tid; j < (int64_t)c.K * c.D.KT; j += nt) c.Ni[j] = 0;
     for (int64_t j = tid; j < c.nlnlp; j += nt) c.lnlp[j] = 0;
@@ -894,13 +935,15 @@ __device__ __forceinline__ int poly_f(const float* w, int K, float u01_or_neg, R
 // SALT_UPDATEZ), drawing maxploidy numbers per individual whether or not the
 // copies are typed. Also sums ln(sum_k q_k p) over copies: the admixture
 // likelihood Record needs (src/structure.cpp:1917-1925).
-__global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_update_z_admix_ref(const DevChain* chains, int force, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
     if (!force && binaryq_at(c, m)) return;
     __shared__ double sh[32];
-    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t l = vb.x * (int64_t)blockDim.x + threadIdx.x;
     double lnl = 0;
     if (l < D.L) {
         Rng32 r;
@@ -923,7 +966,7 @@ __global__ void k_update_z_admix_ref(const DevChain* chains, int force) {
         }
     }
     double t = block_sum(lnl, sh);
-    if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
+    if (threadIdx.x == 0) c.lnlp[vb.x] = t;
 }
 
 // UpdateZAdmix with counter streams. Warp = 32 individuals (one per lane),
@@ -949,9 +992,11 @@ constexpr int ZA_LC = 16;
 constexpr int ZA_PACKED = 32;   // lane j flushes bin j
 static_assert(ZA_PACKED <= 32, "one histogram bin per lane");
 template <int KM, bool EXACT>
-__global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevChain* chains, int force) {
+__global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevChain* chains, int force, const int4* map = nullptr) {
     extern __shared__ unsigned char smraw[];
-    const DevChain& c = chains[blockIdx.z];
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = EXACT ? KM : c.K, m = c.ctl->m, MK = D.maxK;
     if (!force && binaryq_at(c, m)) return;
@@ -962,7 +1007,7 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
     float* sF = reinterpret_cast<float*>(smraw);                  // [ZA_LC][MK][KPAD]
     int32_t* hs = reinterpret_cast<int32_t*>(sF + ZA_LC * MK * KPAD);  // [ZA_LC][K][MK]
     const int lane = threadIdx.x & 31;
-    const int slot = blockIdx.x * (ZA_WARPS * 32) + threadIdx.x;
+    const int slot = vb.x * (ZA_WARPS * 32) + threadIdx.x;
     const bool live = slot < D.N;
     const int i = live && D.perm ? D.perm[slot] : slot;   // ascending ploidy with mixed ploidy
     constexpr int NPK = (KM + 7) / 8;
@@ -971,7 +1016,7 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
     int32_t mi[KM];
 #pragma unroll
     for (int k = 0; k < KM; ++k) { q[k] = (live && (EXACT || k < K)) ? c.Q[(int64_t)i * K + k] : 0.f; mi[k] = 0; }
-    const int64_t lb0 = (int64_t)blockIdx.y * c.zadm_lc, lb1 = min(D.L, lb0 + c.zadm_lc);
+    const int64_t lb0 = (int64_t)vb.y * c.zadm_lc, lb1 = min(D.L, lb0 + c.zadm_lc);
     float ls = 0.f, lc = 0.f;  // Kahan sum of ln(sum_k q_k p)
     const bool rec = force || record_at(c, m);
     for (int64_t l0 = lb0; l0 < lb1; l0 += ZA_LC) {
@@ -1070,19 +1115,21 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
         for (int k = 0; k < KM; ++k)
             if ((EXACT || k < K) && mi[k]) atomicAdd(&c.Mi[(int64_t)i * K + k], mi[k]);
     double t = block_sum((double)ls - (double)lc, sh);
-    if (threadIdx.x == 0) c.lnlp[blockIdx.y * gridDim.x + blockIdx.x] = t;
+    if (threadIdx.x == 0) c.lnlp[vb.y * vb.gx + vb.x] = t;
 }
 
 template <int KM, bool EXACT>
-__global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int force) {
+__global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int force, const int4* map) {
     extern __shared__ unsigned char smraw[];
-    const DevChain& c = chains[blockIdx.z];
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = EXACT ? KM : c.K, m = c.ctl->m, MK = D.maxK;
     if (!force && !metro_turn(c, m)) return;
     const int KPAD = K | 1;
     float* sF = reinterpret_cast<float*>(smraw);   // [ZA_LC][MK][KPAD]
-    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const int slot = vb.x * blockDim.x + threadIdx.x;
     const bool live = slot < D.N;
     const int i = live && D.perm ? D.perm[slot] : slot;   // ascending ploidy with mixed ploidy
     float q1[KM], q0[KM];
@@ -1092,7 +1139,7 @@ __global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int
         q1[k] = on ? c.Qprop[(int64_t)i * K + k] : 0.f;
         q0[k] = on ? c.Q[(int64_t)i * K + k] : 0.f;
     }
-    const int64_t lc0 = (int64_t)blockIdx.y * c.zadm_lc, lc1 = min(D.L, lc0 + c.zadm_lc);
+    const int64_t lc0 = (int64_t)vb.y * c.zadm_lc, lc1 = min(D.L, lc0 + c.zadm_lc);
     double accd = 0;
     float acc = 0.f;
     int cnt = 0;
@@ -1123,7 +1170,7 @@ __global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int
             if (++cnt == SUB) { cnt = 0; accd += acc; acc = 0.f; }
         }
     }
-    if (live) c.metrop[(int64_t)blockIdx.y * D.N + i] = accd + (double)acc;
+    if (live) c.metrop[(int64_t)vb.y * D.N + i] = accd + (double)acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -1169,8 +1216,10 @@ __device__ double logprod_d_serial(const double* a, int64_t n, int64_t sep) {
 // Reference streams use the serial exponent-split product (a zero resets its
 // running mantissa, as in the reference); counter streams a parallel sum.
 constexpr int LPQ_BLOCKS = 64;
-__global__ void k_logprod_q(const DevChain* chains) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_logprod_q(const DevChain* chains, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
     __shared__ double sh[32];
@@ -1180,7 +1229,7 @@ __global__ void k_logprod_q(const DevChain* chains) {
     else return;
     if (c.rng == 0) {
         // reference streams: the serial exponent-split product, one thread per sequence
-        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseq; s += gridDim.x * blockDim.x) {
+        for (int s = vb.x * blockDim.x + threadIdx.x; s < nseq; s += vb.gx * blockDim.x) {
             const float* base; int64_t n, sep;
             if (mode == 2) { int sp = s / K, k = s % K; base = c.Q + (int64_t)D.pop_ind0[sp] * K + k; n = D.pop_nind[sp]; sep = K; }
             else if (mode == 1) { base = c.Q + s; n = D.N; sep = K; }
@@ -1193,7 +1242,7 @@ __global__ void k_logprod_q(const DevChain* chains) {
         // counter streams, one sequence per (location, cluster) over the
         // location's consecutive rows: one block per location, one block sum
         // per cluster (deterministic)
-        for (int sp = blockIdx.x; sp < D.S; sp += gridDim.x) {
+        for (int sp = vb.x; sp < D.S; sp += vb.gx) {
             const int64_t r0 = D.pop_ind0[sp], n = D.pop_nind[sp];
             for (int k = 0; k < K; ++k) {
                 double v = 0;
@@ -1213,8 +1262,8 @@ __global__ void k_logprod_q(const DevChain* chains) {
     const int64_t NK = (int64_t)D.N * K;
     for (int s = 0; s < nseq; ++s) {
         double v = 0;
-        const int64_t per = (NK + gridDim.x - 1) / gridDim.x;
-        const int64_t j0 = blockIdx.x * per, j1 = min(NK, j0 + per);
+        const int64_t per = (NK + vb.gx - 1) / vb.gx;
+        const int64_t j0 = vb.x * per, j1 = min(NK, j0 + per);
         for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
             const int i = (int)(j / K), k = (int)(j % K);
             const int sq = mode == 2 ? D.popid[i] * K + k : mode == 1 ? k : 0;
@@ -1223,12 +1272,12 @@ __global__ void k_logprod_q(const DevChain* chains) {
             v += q > 0.f ? (double)logf(q) : -709.0895657128241;
         }
         v = block_sum(v, sh);
-        if (threadIdx.x == 0) part[blockIdx.x * nseq + s] = v;
+        if (threadIdx.x == 0) part[vb.x * nseq + s] = v;
     }
-    if (!last_block_done(c.ctl, gridDim.x)) return;
+    if (!last_block_done(c.ctl, vb.gx)) return;
     for (int s = threadIdx.x; s < nseq; s += blockDim.x) {
         double t = 0;
-        for (int b2 = 0; b2 < (int)gridDim.x; ++b2) t += part[b2 * nseq + s];
+        for (int b2 = 0; b2 < (int)vb.gx; ++b2) t += part[b2 * nseq + s];
         c.red[s] = t;
     }
     if (threadIdx.x == 0) c.ctl->done = 0;
@@ -1307,9 +1356,11 @@ __device__ void update_alpha_locprior_ctr(const DevChain& c, int m) {
     }
 }
 
-__global__ void k_update_alpha(const DevChain* chains) {
-    const DevChain& c = chains[blockIdx.z];
-    if (blockIdx.x) return;
+__global__ void k_update_alpha(const DevChain* chains, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
+    if (vb.x) return;
     if (c.rng != 0 && c.locpriori && c.admix) {
         update_alpha_locprior_ctr(c, c.ctl->m);
         return;
@@ -1378,9 +1429,11 @@ __global__ void k_update_alpha(const DevChain* chains) {
 }
 
 // UpdateLocPriori (src/structure.cpp:1168-1255), one thread
-__global__ void k_update_locpriori(const DevChain* chains) {
-    const DevChain& c = chains[blockIdx.z];
-    if (threadIdx.x || blockIdx.x || !c.locpriori) return;
+__global__ void k_update_locpriori(const DevChain* chains, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
+    if (threadIdx.x || vb.x || !c.locpriori) return;
     const DevData& D = c.D;
     const int K = c.K, S = D.S, m = c.ctl->m;
     Rng64 rng; rng.init(c.seed + (uint64_t)m, VP_SALT_UPDATELOC);
@@ -1513,14 +1566,16 @@ __device__ void update_a2_locus(const DevChain& c, int64_t l, int64_t pshift, Rn
     if (dlnL >= VP_NZERO || u < exp(dlnL)) { pa[m1] = (float)pm1; pa[n1] = (float)pn1; }
 }
 
-__global__ void k_update_a(const DevChain* chains) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_update_a(const DevChain* chains, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     if (!c.fmodel) return;
     const DevData& D = c.D;
     const int m = c.ctl->m;
     const bool one = hash_ulong(c.seed + (uint64_t)m) & 1;
     if (c.rng == 0) {
-        int b = blockIdx.x * blockDim.x + threadIdx.x;
+        int b = vb.x * blockDim.x + threadIdx.x;
         if (b >= 32) return;
         int64_t l0 = b * D.L / 32, l1 = (b + 1) * D.L / 32;
         Rng64 r; r.init(c.seed + (uint64_t)(m * 32 + b), VP_SALT_UPDATEA);
@@ -1537,7 +1592,7 @@ __global__ void k_update_a(const DevChain* chains) {
         }
         return;
     }
-    int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t l = vb.x * (int64_t)blockDim.x + threadIdx.x;
     if (l >= D.L) return;
     Philox ph; ph.init(c.seed, ST_A | ((uint32_t)m << 4), (uint32_t)l, 0);
     float pb[64], pc[64];
@@ -1548,8 +1603,10 @@ __global__ void k_update_a(const DevChain* chains) {
 // UpdateF (src/structure.cpp:1806-1858): per-cluster F with a Normal random
 // walk. One block per chain: thread 0 owns the stream, the block reduces the
 // sum over all alleles for each proposal.
-__global__ void k_update_f(const DevChain* chains) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_update_f(const DevChain* chains, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     if (!c.fmodel) return;
     const DevData& D = c.D;
     const int K = c.K, m = c.ctl->m;
@@ -1675,14 +1732,16 @@ __global__ void k_advance(const DevChain* chains) {
 // from the likelihood contraction, whose FP32 accumulation over 10^5 and
 // more alleles per split drifts by a few 1e-6 relative, serves the label
 // draws only.
-__global__ void k_record_sweep(const DevChain* chains, double* exact) {
-    const DevChain& c = chains[blockIdx.z];
+__global__ void k_record_sweep(const DevChain* chains, double* exact, const int4* map = nullptr) {
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z];
+    if (map && run_over(c)) return;
     const DevData& D = c.D;
     __shared__ double sh[32];
     const int m = c.ctl->m;
     const bool rec = record_at(c, m);
     if (rec) {
-        int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+        int64_t tid = vb.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)vb.gx * blockDim.x;
         for (int64_t j = tid; j < (int64_t)D.N * c.K; j += nt) c.MiSum[j] += c.Mi[j];
         const bool fm = m >= c.nburnin;
         if (exact) {
@@ -1698,14 +1757,14 @@ __global__ void k_record_sweep(const DevChain* chains, double* exact) {
                 }
             }
             const double bs = block_sum((double)s - (double)cmp, sh);
-            if (threadIdx.x == 0) exact[(int64_t)blockIdx.z * gridDim.x + blockIdx.x] = bs;
+            if (threadIdx.x == 0) exact[(int64_t)vb.z * vb.gx + vb.x] = bs;
         } else if (fm) {
             for (int64_t j = tid; j < (int64_t)c.K * D.KT; j += nt) c.FreqM[j] += c.Freq[j];
         }
     }
-    if (!last_block_done(c.ctl, gridDim.x)) return;
+    if (!last_block_done(c.ctl, vb.gx)) return;
     if (rec && exact) {
-        const double t = block_sum_partials(exact + (int64_t)blockIdx.z * gridDim.x, gridDim.x, sh);
+        const double t = block_sum_partials(exact + (int64_t)vb.z * vb.gx, vb.gx, sh);
         if (threadIdx.x == 0) c.ctl->lnl = t;
         __syncthreads();
     }

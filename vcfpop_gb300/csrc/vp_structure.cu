@@ -26,8 +26,24 @@ struct TcOperands {
     CUtensorMap mapC, mapCT;
 };
 
+// one kernel launch of a chain's sweep: the kernel, its launch shape and its
+// scalar arguments (nint ints, or nint == -1: the null accumulator of
+// k_record_sweep); the kernel's first argument is the chain's device header
+// and its last the cohort block map (null here)
+struct SweepRec {
+    struct vp_chain* c;
+    const void* fn;
+    const char* name;
+    dim3 grid, block;
+    size_t smem;
+    int nint, i0, i1;
+};
+
 struct vp_ctx {
     int device = 0;
+    // set while a cohort records this context's chains' sweeps: launches are
+    // appended here instead of issued
+    std::vector<SweepRec>* rec = nullptr;
     cudaStream_t stream = nullptr;
     DevData D{};
     std::vector<void*> allocs;
@@ -141,6 +157,34 @@ int check_launch(vp_ctx* ctx, const char* what) {
         if (rc_) return rc_;                    \
     } while (0)
 
+// one launch of a sweep kernel for one chain (or, while a cohort records, its
+// record): argument list (chain header, the scalar arguments, block map)
+int sweep_launch(vp_chain* c, const void* fn, const char* name, dim3 g, dim3 b, size_t sm, int nint, int i0 = 0,
+                 int i1 = 0) {
+    vp_ctx* x = c->ctx;
+    if (x->rec) {
+        x->rec->push_back(SweepRec{c, fn, name, g, b, sm, nint, i0, i1});
+        return VP_OK;
+    }
+    const DevChain* d = c->d;
+    const int4* map = nullptr;
+    double* none = nullptr;
+    void* args[4];
+    int k = 0;
+    args[k++] = (void*)&d;
+    if (nint < 0) args[k++] = (void*)&none;
+    if (nint >= 1) args[k++] = (void*)&i0;
+    if (nint >= 2) args[k++] = (void*)&i1;
+    args[k++] = (void*)&map;
+    cudaLaunchKernel(fn, g, b, args, sm, x->stream);
+    return check_launch(x, name);
+}
+#define SL(c, fn, g, b, sm, ...)                                                                   \
+    do {                                                                                           \
+        int rc_ = sweep_launch(c, (const void*)&fn, #fn, dim3 g, dim3 b, (size_t)(sm), __VA_ARGS__); \
+        if (rc_) return rc_;                                                                       \
+    } while (0)
+
 // The library's device memory: one stream-ordered pool per device that keeps
 // freed blocks for the next context, chain or batch, so repeated runs do not
 // pay to map and unmap memory (and a free does not wait for the device);
@@ -188,7 +232,7 @@ inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b);
 // kernel (profiling mode 1) or the tensor-core form's UpdateP (mode 2)
 enum { PROF_DOMINANT = 1, PROF_UPDATEP_TC = 2 };
 void prof_mark(vp_ctx* x, bool begin, int kind = PROF_DOMINANT) {
-    if (x->prof != kind) return;
+    if (x->prof != kind || x->rec) return;
     int idx = x->prof_next * 2 + (begin ? 0 : 1);
     while ((int)x->prof_ev.size() <= idx) {
         cudaEvent_t e;
@@ -231,10 +275,10 @@ int launch_loglik(vp_chain* c, int force) {
     prof_mark(x, true);
     struct End { vp_ctx* x; ~End() { prof_mark(x, false); } } end_{x};
     switch (c->kc) {
-        case 4: LAUNCH(x, k_loglik<4>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
-        case 8: LAUNCH(x, k_loglik<8>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
-        case 12: LAUNCH(x, k_loglik<12>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
-        default: LAUNCH(x, k_loglik<16>, (g, LL_BLOCK, 0, x->stream), (c->d, c->kgroups, force)); break;
+        case 4: SL(c, k_loglik<4>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+        case 8: SL(c, k_loglik<8>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+        case 12: SL(c, k_loglik<12>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+        default: SL(c, k_loglik<16>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
     }
     return VP_OK;
 }
@@ -260,9 +304,9 @@ int launch_zadm_ctr(vp_chain* c, int force) {
     struct End { vp_ctx* x; ~End() { prof_mark(x, false); } } end_{x};
     const int K = c->P.K;
 #define VP_ZE(n) \
-    if (K == n) { LAUNCH(x, (k_update_z_admix_ctr<n, true>), (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); return VP_OK; }
+    if (K == n) { SL(c, (k_update_z_admix_ctr<n, true>), (g), (ZA_WARPS * 32), sm, 1, force); return VP_OK; }
 #define VP_ZP(n) \
-    if (K <= n) { LAUNCH(x, (k_update_z_admix_ctr<n, false>), (g, ZA_WARPS * 32, sm, x->stream), (c->d, force)); return VP_OK; }
+    if (K <= n) { SL(c, (k_update_z_admix_ctr<n, false>), (g), (ZA_WARPS * 32), sm, 1, force); return VP_OK; }
     VP_ZADM_EXACT(VP_ZE)
     VP_ZADM_PADDED(VP_ZP)
 #undef VP_ZE
@@ -278,9 +322,9 @@ int launch_metro_ratio(vp_chain* c, int force) {
     const size_t sm = (size_t)ZA_LC * x->maxK * (c->P.K | 1) * 4;
     const int K = c->P.K;
 #define VP_ME(n) \
-    if (K == n) { LAUNCH(x, (k_metro_ratio<n, true>), (g, 256, sm, x->stream), (c->d, force)); return VP_OK; }
+    if (K == n) { SL(c, (k_metro_ratio<n, true>), (g), (256), sm, 1, force); return VP_OK; }
 #define VP_MP(n) \
-    if (K <= n) { LAUNCH(x, (k_metro_ratio<n, false>), (g, 256, sm, x->stream), (c->d, force)); return VP_OK; }
+    if (K <= n) { SL(c, (k_metro_ratio<n, false>), (g), (256), sm, 1, force); return VP_OK; }
     VP_ZADM_EXACT(VP_ME)
     VP_ZADM_PADDED(VP_MP)
 #undef VP_ME
@@ -335,33 +379,31 @@ int launch_count(vp_chain* c, int force) {
         if (sm <= 200 * 1024 && x->D.Nw >= 32) {
             const dim3 g((unsigned)std::min<int64_t>(cdiv(x->L, 8), (int64_t)x->nsm * 8), 1, (unsigned)kgroups);
             switch (kc) {
-                case 4: LAUNCH(x, k_count_packed<4>, (g, 256, sm, x->stream), (c->d, kgroups, force)); break;
-                case 8: LAUNCH(x, k_count_packed<8>, (g, 256, sm, x->stream), (c->d, kgroups, force)); break;
-                default: LAUNCH(x, k_count_packed<16>, (g, 256, sm, x->stream), (c->d, kgroups, force)); break;
+                case 4: SL(c, k_count_packed<4>, (g), (256), sm, 2, kgroups, force); break;
+                case 8: SL(c, k_count_packed<8>, (g), (256), sm, 2, kgroups, force); break;
+                default: SL(c, k_count_packed<16>, (g), (256), sm, 2, kgroups, force); break;
             }
             return VP_OK;
         }
     }
-    LAUNCH(x, k_count_noadmix, (dim3(cdiv(x->L, COUNT_WARPS), 1, 1), COUNT_WARPS * 32, count_smem(c), x->stream),
-           (c->d, force));
+    SL(c, k_count_noadmix, (cdiv(x->L, COUNT_WARPS), 1, 1), (COUNT_WARPS * 32), count_smem(c), 1, force);
     return VP_OK;
 }
 
 int launch_step(vp_chain* c, int step, int force) {
     vp_ctx* x = c->ctx;
-    cudaStream_t s = x->stream;
     const vp_params& P = c->P;
     const int K = P.K;
     const bool ref = P.rng == VP_RNG_REFERENCE;
     switch (step) {
         case VP_STEP_UPDATEP:
-            if (ref) LAUNCH(x, k_update_p_ref, (dim3(1, 1, 1), 128, 0, s), (c->d));
-            else LAUNCH(x, k_update_p_ctr, (dim3(cdiv((int64_t)K * x->L, 256), 1, 1), 256, 0, s), (c->d));
+            if (ref) SL(c, k_update_p_ref, (1, 1, 1), (128), 0, 0);
+            else SL(c, k_update_p_ctr, (cdiv((int64_t)K * x->L, 256), 1, 1), (256), 0, 0);
             return VP_OK;
         case VP_STEP_LOGLIK: {
             int rc = launch_loglik(c, 1);
             if (rc) return rc;
-            LAUNCH(x, k_sample_noadmix, (dim3(c->h.nsampblk, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 1));
+            SL(c, k_sample_noadmix, (c->h.nsampblk, 1, 1), (SAMPLE_BLOCK), 0, 1, 1);
             return VP_OK;
         }
         case VP_STEP_UPDATEQ: {
@@ -369,55 +411,52 @@ int launch_step(vp_chain* c, int step, int force) {
             if (!P.admix) {
                 int rc = launch_loglik(c, force);
                 if (rc) return rc;
-                LAUNCH(x, k_sample_noadmix, (dim3(ref ? 1 : c->h.nsampblk, 1, 1), SAMPLE_BLOCK, 0, s), (c->d, 0));
-                if (c->h.nadmburnin > 0) LAUNCH(x, k_update_q_admix, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
+                SL(c, k_sample_noadmix, (ref ? 1 : c->h.nsampblk, 1, 1), (SAMPLE_BLOCK), 0, 1, 0);
+                if (c->h.nadmburnin > 0) SL(c, k_update_q_admix, (ref ? 1 : gi, 1, 1), (ref ? 32 : 256), 0, 1, 0);
             } else {
-                LAUNCH(x, k_update_q_admix, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
+                SL(c, k_update_q_admix, (ref ? 1 : gi, 1, 1), (ref ? 32 : 256), 0, 1, 0);
                 if (P.metrofreq > 0) {
-                    LAUNCH(x, k_metro_propose, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
+                    SL(c, k_metro_propose, (ref ? 1 : gi, 1, 1), (ref ? 32 : 256), 0, 1, 0);
                     if (int rc = launch_metro_ratio(c, 0)) return rc;
-                    LAUNCH(x, k_metro_accept, (dim3(ref ? 1 : gi, 1, 1), ref ? 32 : 256, 0, s), (c->d, 0));
+                    SL(c, k_metro_accept, (ref ? 1 : gi, 1, 1), (ref ? 32 : 256), 0, 1, 0);
                 }
             }
             return VP_OK;
         }
         case VP_STEP_LOCPRIORI:
-            if (P.locpriori) LAUNCH(x, k_update_locpriori, (dim3(1, 1, 1), 32, 0, s), (c->d));
+            if (P.locpriori) SL(c, k_update_locpriori, (1, 1, 1), (32), 0, 0);
             return VP_OK;
         case VP_STEP_UPDATEZ:
             if (!P.admix)
                 if (int rc = launch_count(c, 0)) return rc;
             if (P.admix || c->h.nadmburnin > 0) {
-                LAUNCH(x, k_zero_counts, (dim3(std::min<unsigned>(1024, cdiv((int64_t)K * x->KT, 256)), 1, 1), 256, 0, s), (c->d, 0));
-                if (ref)
-                    LAUNCH(x, k_update_z_admix_ref, (dim3(cdiv(x->L, 128), 1, 1), 128, 0, s), (c->d, 0));
-                else {
-                    int rc = launch_zadm_ctr(c, 0);
-                    if (rc) return rc;
-                }
+                SL(c, k_zero_counts, (std::min<unsigned>(1024, cdiv((int64_t)K * x->KT, 256)), 1, 1), (256), 0, 1, 0);
+                if (ref) SL(c, k_update_z_admix_ref, (cdiv(x->L, 128), 1, 1), (128), 0, 1, 0);
+                else if (int rc = launch_zadm_ctr(c, 0)) return rc;
             }
             return VP_OK;
         case VP_STEP_ALPHA:
             if ((P.inferalpha && (P.admix || c->h.nadmburnin > 0)) || (P.locpriori && P.admix)) {
-                LAUNCH(x, k_logprod_q, (dim3(ref ? std::max(1, (x->S * K + 255) / 256) : LPQ_BLOCKS, 1, 1), 256, 0, s), (c->d));
-                LAUNCH(x, k_update_alpha, (dim3(1, 1, 1), 128, 0, s), (c->d));
+                SL(c, k_logprod_q, (ref ? std::max(1, (x->S * K + 255) / 256) : LPQ_BLOCKS, 1, 1), (256), 0, 0);
+                SL(c, k_update_alpha, (1, 1, 1), (128), 0, 0);
             }
             return VP_OK;
         case VP_STEP_UPDATEA:
             if (P.fmodel) {
-                if (ref) LAUNCH(x, k_update_a, (dim3(1, 1, 1), 32, 0, s), (c->d));
-                else LAUNCH(x, k_update_a, (dim3(cdiv(x->L, 128), 1, 1), 128, 0, s), (c->d));
+                if (ref) SL(c, k_update_a, (1, 1, 1), (32), 0, 0);
+                else SL(c, k_update_a, (cdiv(x->L, 128), 1, 1), (128), 0, 0);
             }
             return VP_OK;
         case VP_STEP_UPDATEF:
-            if (P.fmodel) LAUNCH(x, k_update_f, (dim3(1, 1, 1), 256, 0, s), (c->d));
+            if (P.fmodel) SL(c, k_update_f, (1, 1, 1), (256), 0, 0);
             return VP_OK;
         case VP_STEP_RECORD:
-            LAUNCH(x, k_record, (dim3(1, 1, 1), 256, 0, s), (c->d));
-            LAUNCH(x, k_accumulate, (dim3(std::min<unsigned>(1024, cdiv((int64_t)K * x->KT, 256)), 1, 1), 256, 0, s), (c->d, 0));
+            // single steps (parity tests): Record alone, without the advance
+            LAUNCH(x, k_record, (dim3(1, 1, 1), 256, 0, x->stream), (c->d));
+            LAUNCH(x, k_accumulate, (dim3(std::min<unsigned>(1024, cdiv((int64_t)K * x->KT, 256)), 1, 1), 256, 0, x->stream), (c->d, 0));
             return VP_OK;
         case VP_STEP_NEXT:
-            LAUNCH(x, k_advance, (dim3(1, 1, 1), 32, 0, s), (c->d));
+            LAUNCH(x, k_advance, (dim3(1, 1, 1), 32, 0, x->stream), (c->d));
             return VP_OK;
     }
     vp_set_error("unknown step %d", step);
@@ -431,12 +470,11 @@ int launch_sweep(vp_chain* c) {
         int rc = launch_step(c, st, 0);
         if (rc) return rc;
     }
-    // Record and m += 1 as one launch
+    // Record and m += 1 as one launch; at most 128 blocks: the element-wise
+    // part only runs on recorded sweeps, and every block takes part in the
+    // last-block count
     vp_ctx* x = c->ctx;
-    // at most 128 blocks: the element-wise part only runs on recorded sweeps,
-    // and every block takes part in the last-block count
-    LAUNCH(x, k_record_sweep, (dim3(std::min<unsigned>(128, cdiv((int64_t)c->P.K * x->KT, 256)), 1, 1), 256, 0, x->stream),
-           (c->d, nullptr));
+    SL(c, k_record_sweep, (std::min<unsigned>(128, cdiv((int64_t)c->P.K * x->KT, 256)), 1, 1), (256), 0, -1);
     return VP_OK;
 }
 
