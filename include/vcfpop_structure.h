@@ -402,6 +402,33 @@ int vp_release(vp_server* s, int64_t id);
 /* Stop the scheduler (active runs are abandoned) and free everything. */
 int vp_server_close(vp_server* s);
 
+/* ---- cohorts: runs of different datasets in shared launches --------------
+ * Replaces, with the serving loop below, the reference's scheduling of one run
+ * per host thread and device slot (src/structure.cpp:2398-2413, 2467-2501;
+ * ManageCUDA 710-756). A cohort sweeps plain-form chains of any contexts on
+ * one device -- each with its own individuals, loci, clusters and model -- as
+ * one launch per kernel of the sweep (one per compiled variant in use) that
+ * covers every member's blocks, captured once into a CUDA graph and replayed.
+ * Each member's blocks do exactly the work of that chain's own launch, so its
+ * results are the same bit for bit. A member whose sweeps are all done idles
+ * (its blocks return at once) until it is removed.
+ * While a chain is in a cohort it advances only with the cohort (vp_run on it
+ * fails), and neither the chain nor its context can be destroyed: remove it
+ * first (vp_cohort_set without it). Operations on a member's own context
+ * stream (results, vp_finish's Arrange) are ordered after the cohort's
+ * queued sweeps. */
+typedef struct vp_cohort vp_cohort;
+int vp_cohort_open(int device, vp_cohort** out);
+/* The members (n = 0: none); the sweep graph is captured again. */
+int vp_cohort_set(vp_cohort* h, vp_chain** chains, int32_t n);
+/* Queue nsweeps sweeps of every member (each stops at its own end); asynchronous. */
+int vp_cohort_run(vp_cohort* h, int32_t nsweeps);
+int vp_cohort_sync(vp_cohort* h);
+void* vp_cohort_stream(vp_cohort* h);
+/* Kernel launches queued so far; *per_sweep (may be NULL) the launches of one sweep. */
+int64_t vp_cohort_launches(vp_cohort* h, int32_t* per_sweep);
+int vp_cohort_close(vp_cohort* h);
+
 /* Kernel launches issued by this library since the context was opened. */
 int64_t vp_launch_count(vp_ctx* ctx);
 

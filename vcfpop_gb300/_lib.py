@@ -100,7 +100,9 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_chain_set", "vp_launch_count", "vp_last_error", "vp_tc_status", "vp_debug_gemm_bf16", "vp_debug_gemm_e4m3", "vp_debug_gemm_time", "vp_stream", "vp_prof_enable", "vp_prof_read", "vp_loglik_packed2",
            "vp_loglik_packed2_noalloc", "vp_server_open", "vp_submit", "vp_poll", "vp_wait", "vp_request_chain",
            "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2", "vp_release_memory",
-           "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout", "vp_write_structure"]
+           "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout", "vp_write_structure",
+           "vp_cohort_open", "vp_cohort_set", "vp_cohort_run", "vp_cohort_sync", "vp_cohort_stream",
+           "vp_cohort_launches", "vp_cohort_close"]
 
 
 def lib():
@@ -163,6 +165,15 @@ def lib():
     L.vp_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int32, C.c_int, P, C.c_int64, P, P]
     L.vp_locus_filter_pack2.argtypes = [P, C.c_int64, C.c_int32, C.POINTER(VpLocusFilter), C.c_int, P, P]
     L.vp_write_structure.argtypes = [P, C.POINTER(VpWriteOpts)]
+    L.vp_cohort_open.argtypes = [C.c_int, C.POINTER(P)]
+    L.vp_cohort_set.argtypes = [P, C.POINTER(P), C.c_int32]
+    L.vp_cohort_run.argtypes = [P, C.c_int32]
+    L.vp_cohort_sync.argtypes = [P]
+    L.vp_cohort_stream.argtypes = [P]
+    L.vp_cohort_stream.restype = P
+    L.vp_cohort_launches.argtypes = [P, C.POINTER(C.c_int32)]
+    L.vp_cohort_launches.restype = C.c_int64
+    L.vp_cohort_close.argtypes = [P]
     _lib = L
     return L
 

@@ -63,3 +63,5 @@ void vp_chain_progress(const vp_chain* c, int64_t* issued, int64_t* total);
 // the dataset a chain's context holds, and the chain's parameters
 const vp_dataset* vp_chain_dataset(const vp_chain* c);
 void vp_chain_params(const vp_chain* c, vp_params* p);
+// vp_cohort_open with the cohort's stream at a CUDA stream priority
+int vp_cohort_open_ex(int device, int priority, vp_cohort** out);

@@ -89,6 +89,8 @@ struct vp_chain {
     // table and chunk partials (lt, LLp) only on its first plain-form use
     bool plain_lazy = false;
     void* plain_mem = nullptr;
+    // the cohort whose shared launches sweep this chain (vp_cohort_set)
+    struct vp_cohort* cohort = nullptr;
 };
 
 // launch configuration of a batch's two contractions: the likelihood
@@ -570,6 +572,8 @@ int vp_open_ex(const vp_dataset* ds, int device, int priority, vp_ctx** out) {
 
 extern "C" int vp_close(vp_ctx* x) {
     if (!x) return VP_OK;
+    for (vp_chain* c : x->chains)
+        if (c->cohort) { vp_set_error("a chain of this context belongs to a cohort: remove it (vp_cohort_set) first"); return VP_E_STATE; }
     cudaSetDevice(x->device);
     for (vp_chain* c : std::vector<vp_chain*>(x->chains)) vp_chain_destroy(c);
     if (x->stream) cudaStreamSynchronize(x->stream);
@@ -788,6 +792,7 @@ extern "C" int vp_chain_create(vp_ctx* x, const vp_params* P, vp_chain** out) {
 
 extern "C" int vp_chain_destroy(vp_chain* c) {
     if (!c) return VP_OK;
+    if (c->cohort) { vp_set_error("the chain belongs to a cohort: remove it (vp_cohort_set) first"); return VP_E_STATE; }
     cudaSetDevice(c->ctx->device);
     bool in_batch = false, in_pg = false;
     if (c->ctx->batch)
@@ -876,6 +881,11 @@ extern "C" int vp_run(vp_chain** cs, int32_t n, int32_t nsweeps) {
     for (int i = 0; i < n; ++i)
         if (!cs[i] || cs[i]->ctx != x) { vp_set_error("all chains of one vp_run must share a context"); return VP_E_ARG; }
     cudaSetDevice(x->device);
+    for (int i = 0; i < n; ++i)
+        if (cs[i]->cohort && nsweeps > 0 && cs[i]->issued < cs[i]->total) {
+            vp_set_error("a chain of a cohort advances with its cohort (vp_cohort_run)");
+            return VP_E_STATE;
+        }
     bool all_tc = true;
     for (int i = 0; i < n; ++i) all_tc &= cs[i]->P.form == VP_FORM_TC;
     if (!all_tc) return run_plain(x, cs, n, nsweeps);
@@ -1136,6 +1146,260 @@ extern "C" int vp_chain_step(vp_chain* c, int32_t step) {
     rc = launch_step(c, step, 0);
     if (rc) return rc;
     return vp_sync(c->ctx);
+}
+
+// ===================== cohorts: runs of different datasets in shared launches =====================
+// A cohort sweeps plain-form chains of any contexts on one device with one
+// launch per kernel of the sweep (one per compiled variant in use). Each
+// member's sweep is recorded (the launches launch_sweep would issue for it
+// alone); the recordings are merged in order -- the next launch of every
+// member that has the same kernel, block shape and scalar arguments go
+// together -- and every merged launch gets a block map listing, for each
+// member, every block of that member's own grid. The merged sequence is
+// captured once into a CUDA graph and replayed each sweep.
+struct vp_cohort {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev = nullptr;                 // after the last queued sweeps
+    std::vector<vp_chain*> chains;
+    void* mem = nullptr;                      // DevChain copies and block maps of the current graph
+    cudaGraphExec_t graph = nullptr;
+    int nodes = 0;
+    int64_t launches = 0;
+    // replaced graphs and their buffers, freed once an event after their last
+    // launch has completed
+    struct Old { cudaGraphExec_t g; cudaEvent_t e; };
+    std::vector<Old> old;
+};
+
+namespace {
+
+void cohort_reap(vp_cohort* h, bool wait) {
+    for (size_t i = 0; i < h->old.size();) {
+        if (wait) cudaEventSynchronize(h->old[i].e);
+        if (cudaEventQuery(h->old[i].e) == cudaSuccess) {
+            cudaGraphExecDestroy(h->old[i].g);
+            cudaEventDestroy(h->old[i].e);
+            h->old.erase(h->old.begin() + i);
+        } else {
+            ++i;
+        }
+    }
+}
+
+// the cohort stream waits for the work already queued on each member's own
+// stream (its upload, initialisation, earlier sweeps)
+int cohort_wait_members(vp_cohort* h, const std::vector<vp_chain*>& cs) {
+    for (vp_chain* c : cs) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        cudaEventRecord(e, c->ctx->stream);
+        cudaStreamWaitEvent(h->stream, e, 0);
+        cudaEventDestroy(e);
+    }
+    return VP_OK;
+}
+
+struct MergedLaunch {
+    const void* fn;
+    const char* name;
+    dim3 block;
+    size_t smem = 0;
+    int nint, i0, i1;
+    int64_t map0 = 0, nmap = 0;   // entries in the map buffer
+};
+
+int cohort_build(vp_cohort* h) {
+    const int n = (int)h->chains.size();
+    if (h->graph) {
+        // keep the old graph until its queued replays are done
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        cudaEventRecord(e, h->stream);
+        h->old.push_back({h->graph, e});
+        h->graph = nullptr;
+    }
+    if (h->mem) { dev_free(h->mem, h->stream); h->mem = nullptr; }
+    h->nodes = 0;
+    if (n == 0) return VP_OK;
+    // 1. each member's sweep, recorded
+    std::vector<std::vector<SweepRec>> rec(n);
+    for (int i = 0; i < n; ++i) {
+        vp_chain* c = h->chains[i];
+        c->ctx->rec = &rec[i];
+        int rc = launch_sweep(c);
+        c->ctx->rec = nullptr;
+        if (rc) return rc;
+    }
+    // 2. merge: repeatedly take the next launch of the first member with
+    // launches left, and the next launch of every other member that matches it
+    std::vector<size_t> pos(n, 0);
+    std::vector<MergedLaunch> ml;
+    std::vector<int4> maps;
+    auto same = [](const SweepRec& a, const SweepRec& b) {
+        return a.fn == b.fn && a.block.x == b.block.x && a.block.y == b.block.y && a.block.z == b.block.z &&
+               a.nint == b.nint && a.i0 == b.i0 && a.i1 == b.i1;
+    };
+    for (;;) {
+        int lead = -1;
+        for (int i = 0; i < n && lead < 0; ++i)
+            if (pos[i] < rec[i].size()) lead = i;
+        if (lead < 0) break;
+        const SweepRec head = rec[lead][pos[lead]];
+        MergedLaunch m{head.fn, head.name, head.block, 0, head.nint, head.i0, head.i1, (int64_t)maps.size(), 0};
+        for (int i = 0; i < n; ++i) {
+            if (pos[i] >= rec[i].size() || !same(rec[i][pos[i]], head)) continue;
+            const SweepRec& r = rec[i][pos[i]++];
+            m.smem = std::max(m.smem, r.smem);
+            for (unsigned z = 0; z < r.grid.z; ++z)
+                for (unsigned y = 0; y < r.grid.y; ++y)
+                    for (unsigned x = 0; x < r.grid.x; ++x)
+                        maps.push_back(make_int4((int)(i * r.grid.z + z), (int)x, (int)y, (int)r.grid.x));
+        }
+        m.nmap = (int64_t)maps.size() - m.map0;
+        ml.push_back(m);
+    }
+    // 3. the members' headers and the maps in one device buffer
+    const size_t hb = ((size_t)n * sizeof(DevChain) + 255) & ~(size_t)255;
+    const size_t bytes = hb + maps.size() * sizeof(int4);
+    cudaError_t e = dev_alloc(&h->mem, bytes, h->device, h->stream);
+    if (e != cudaSuccess) { h->mem = nullptr; vp_set_error("cohort buffer of %zu bytes: %s", bytes, cudaGetErrorString(e)); return VP_E_MEM; }
+    std::vector<DevChain> hc(n);
+    for (int i = 0; i < n; ++i) hc[i] = h->chains[i]->h;
+    DevChain* dchains = (DevChain*)h->mem;
+    int4* dmaps = (int4*)((char*)h->mem + hb);
+    CK(cudaMemcpyAsync(dchains, hc.data(), (size_t)n * sizeof(DevChain), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(dmaps, maps.data(), maps.size() * sizeof(int4), cudaMemcpyHostToDevice, h->stream));
+    // the host copies must not be released before the uploads have read them
+    CK(cudaStreamSynchronize(h->stream));
+    // 4. capture one sweep
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = cudaSuccess;
+    const char* bad = nullptr;
+    for (const MergedLaunch& m : ml) {
+        const DevChain* d = dchains;
+        const int4* map = dmaps + m.map0;
+        double* none = nullptr;
+        int i0 = m.i0, i1 = m.i1;
+        void* args[4];
+        int k = 0;
+        args[k++] = (void*)&d;
+        if (m.nint < 0) args[k++] = (void*)&none;
+        if (m.nint >= 1) args[k++] = (void*)&i0;
+        if (m.nint >= 2) args[k++] = (void*)&i1;
+        args[k++] = (void*)&map;
+        le = cudaLaunchKernel(m.fn, dim3((unsigned)m.nmap, 1, 1), m.block, args, m.smem, h->stream);
+        if (le != cudaSuccess) { bad = m.name; break; }
+    }
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+    if (le != cudaSuccess) {
+        if (ce == cudaSuccess) cudaGraphDestroy(g);
+        vp_set_error("cohort launch of %s: %s", bad, cudaGetErrorString(le));
+        return VP_E_CUDA;
+    }
+    if (ce != cudaSuccess) { vp_set_error("cohort capture: %s", cudaGetErrorString(ce)); return VP_E_CUDA; }
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { h->graph = nullptr; vp_set_error("cohort graph: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
+    h->nodes = (int)ml.size();
+    return VP_OK;
+}
+
+}  // namespace
+
+int vp_cohort_open_ex(int device, int priority, vp_cohort** out) {
+    if (!out) { vp_set_error("null argument"); return VP_E_ARG; }
+    if (cudaSetDevice(device) != cudaSuccess) { vp_set_error("cudaSetDevice(%d) failed", device); return VP_E_NODEV; }
+    auto* h = new vp_cohort();
+    h->device = device;
+    if (cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, priority) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev, cudaEventDisableTiming) != cudaSuccess) {
+        if (h->stream) cudaStreamDestroy(h->stream);
+        delete h;
+        vp_set_error("cohort stream: %s", cudaGetErrorString(cudaGetLastError()));
+        return VP_E_CUDA;
+    }
+    *out = h;
+    return VP_OK;
+}
+
+extern "C" int vp_cohort_open(int device, vp_cohort** out) { return vp_cohort_open_ex(device, 0, out); }
+
+extern "C" int vp_cohort_set(vp_cohort* h, vp_chain** cs, int32_t n) {
+    if (!h || n < 0 || (n > 0 && !cs)) { vp_set_error("bad arguments"); return VP_E_ARG; }
+    cudaSetDevice(h->device);
+    std::vector<vp_chain*> next(cs, cs + n);
+    for (int i = 0; i < n; ++i) {
+        vp_chain* c = cs[i];
+        if (!c) { vp_set_error("null chain"); return VP_E_ARG; }
+        if (c->ctx->device != h->device) { vp_set_error("chain on device %d, cohort on %d", c->ctx->device, h->device); return VP_E_ARG; }
+        if (c->cohort && c->cohort != h) { vp_set_error("the chain belongs to another cohort"); return VP_E_STATE; }
+        if (c->P.form == VP_FORM_TC) { vp_set_error("a cohort runs plain-form chains (the tensor-core form has its own batch)"); return VP_E_ARG; }
+        for (int j = 0; j < i; ++j)
+            if (cs[j] == c) { vp_set_error("chain listed twice"); return VP_E_ARG; }
+        if (int rc = ensure_counts(c)) return rc;
+        if (int rc = ensure_plain(c)) return rc;
+    }
+    if (int rc = cohort_wait_members(h, next)) return rc;
+    for (vp_chain* c : h->chains) c->cohort = nullptr;
+    h->chains = next;
+    for (vp_chain* c : h->chains) c->cohort = h;
+    cohort_reap(h, false);
+    int rc = cohort_build(h);
+    if (rc) {
+        for (vp_chain* c : h->chains) c->cohort = nullptr;
+        h->chains.clear();
+    }
+    return rc;
+}
+
+extern "C" int vp_cohort_run(vp_cohort* h, int32_t nsweeps) {
+    if (!h || nsweeps < 0) { vp_set_error("bad arguments"); return VP_E_ARG; }
+    if (h->chains.empty() || nsweeps == 0) return VP_OK;
+    cudaSetDevice(h->device);
+    for (int s = 0; s < nsweeps; ++s) CK(cudaGraphLaunch(h->graph, h->stream));
+    h->launches += (int64_t)h->nodes * nsweeps;
+    // members' own streams (results, Arrange, later single steps) follow
+    CK(cudaEventRecord(h->ev, h->stream));
+    for (vp_chain* c : h->chains) {
+        CK(cudaStreamWaitEvent(c->ctx->stream, h->ev, 0));
+        c->issued = (int)std::min<int64_t>(c->total, (int64_t)c->issued + nsweeps);
+    }
+    cohort_reap(h, false);
+    return VP_OK;
+}
+
+extern "C" int vp_cohort_sync(vp_cohort* h) {
+    if (!h) { vp_set_error("null argument"); return VP_E_ARG; }
+    cudaSetDevice(h->device);
+    CK(cudaStreamSynchronize(h->stream));
+    cohort_reap(h, true);
+    return VP_OK;
+}
+
+extern "C" void* vp_cohort_stream(vp_cohort* h) { return h ? (void*)h->stream : nullptr; }
+
+extern "C" int64_t vp_cohort_launches(vp_cohort* h, int32_t* per_sweep) {
+    if (!h) return -1;
+    if (per_sweep) *per_sweep = h->nodes;
+    return h->launches;
+}
+
+extern "C" int vp_cohort_close(vp_cohort* h) {
+    if (!h) return VP_OK;
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    for (vp_chain* c : h->chains) c->cohort = nullptr;
+    h->chains.clear();
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    cohort_reap(h, true);
+    dev_free(h->mem, h->stream);
+    cudaStreamSynchronize(h->stream);
+    cudaEventDestroy(h->ev);
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return VP_OK;
 }
 
 // ===================== tensor-core K-sweep =====================

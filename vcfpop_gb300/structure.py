@@ -348,6 +348,44 @@ def _chain_array(chains):
     return (C.c_void_p * len(chains))(*[c.h for c in chains])
 
 
+class Cohort:
+    """Chains of any contexts swept together in shared launches (vp_cohort_*)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        B.check(B.lib().vp_cohort_open(device, C.byref(h)))
+        self.h = h
+        self.members = []
+
+    def set(self, chains) -> None:
+        arr = (C.c_void_p * max(1, len(chains)))(*[c.h for c in chains])
+        B.check(B.lib().vp_cohort_set(self.h, arr, len(chains)))
+        self.members = list(chains)
+
+    def run(self, nsweeps: int) -> None:
+        B.check(B.lib().vp_cohort_run(self.h, nsweeps))
+
+    def sync(self) -> None:
+        B.check(B.lib().vp_cohort_sync(self.h))
+
+    def launches(self) -> tuple[int, int]:
+        """(launches queued so far, launches of one sweep)"""
+        per = C.c_int32()
+        n = B.lib().vp_cohort_launches(self.h, C.byref(per))
+        return int(n), int(per.value)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            B.check(B.lib().vp_cohort_close(self.h))
+            self.h = None
+            self.members = []
+
+    def __del__(self):
+        if getattr(self, "h", None) and not sys.is_finalizing():
+            B.lib().vp_cohort_close(self.h)
+            self.h = None
+
+
 def tune(chains: list[Chain], effort: int = 1) -> dict:
     """Autotune the batched sweep of these tensor-core chains (vp_tune): the
     chosen launch configuration and the device times before and after."""
