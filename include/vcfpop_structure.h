@@ -366,9 +366,12 @@ int vp_locus_filter_pack2(const uint32_t* packed, int64_t n_loc, int32_t n_ind, 
  * A server owns one scheduler thread on one device. Submitted runs queue in
  * arrival order and start when their device bytes (dataset upload plus chain
  * state) fit under mem_budget and fewer than max_active runs are active; each
- * active run has its own context and stream, and the scheduler keeps up to
- * two chunks of `chunk` sweeps queued per run, so runs of every size overlap
- * on the GPU. Results stay on the device until the run is released.
+ * active run has its own context. Small runs are batched: the runs of one
+ * size class sweep together in a cohort, one launch per kernel for all of
+ * them, joining and leaving it as they start and finish; larger runs keep
+ * their own streams. The scheduler keeps up to two chunks of `chunk` sweeps
+ * queued per cohort and per run, so runs of every size overlap on the GPU.
+ * Results stay on the device until the run is released.
  * The dataset passed to vp_submit must stay alive until the run is done. */
 typedef struct vp_server vp_server;
 #define VP_REQ_QUEUED 0
@@ -401,6 +404,13 @@ int vp_request_chain(vp_server* s, int64_t id, vp_chain** chain);
 int vp_release(vp_server* s, int64_t id);
 /* Stop the scheduler (active runs are abandoned) and free everything. */
 int vp_server_close(vp_server* s);
+/* on = 1 (the default): runs whose sweep is small (expected device time of a
+ * sweep below about 300 us) are swept in cohorts of their size class, one
+ * launch per kernel for all of them (vp_cohort_*); on = 0: every run on its
+ * own stream. Set before the first vp_submit. */
+int vp_server_set_batching(vp_server* s, int32_t on);
+/* Kernel launches the scheduler has queued, and the run-sweeps they carry. */
+int vp_server_stats(vp_server* s, int64_t* launches, int64_t* run_sweeps);
 
 /* ---- cohorts: runs of different datasets in shared launches --------------
  * Replaces, with the serving loop below, the reference's scheduling of one run

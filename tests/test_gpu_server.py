@@ -160,3 +160,22 @@ def test_context_closed_before_its_chains():
     ch.run(3)
     ch.close()
     ctx2.close()
+
+
+def test_batched_cohorts_give_the_same_results_with_fewer_launches():
+    """With batching (the default) the small runs of a mix sweep together in a
+    cohort, one launch per kernel of the sweep for all of them: the results
+    are those of every run on its own stream, bit for bit, with fewer kernel
+    launches per run-sweep."""
+    runs = _runs()
+    got = {}
+    for batching in (False, True):
+        srv = S.Server(max_active=8, chunk=6, batching=batching)
+        ids = [srv.submit(ds, p) for ds, p in runs]
+        got[batching] = [_collect(srv, rid)[0] for rid in ids]
+        st = srv.stats()
+        got[(batching, "lps")] = st["launches"] / st["run_sweeps"]
+        srv.close()
+    for a, b in zip(got[False], got[True]):
+        _same(a, b)
+    assert got[(True, "lps")] < 0.6 * got[(False, "lps")], (got[(True, "lps")], got[(False, "lps")])

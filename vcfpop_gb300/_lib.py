@@ -102,7 +102,7 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2", "vp_release_memory",
            "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout", "vp_write_structure",
            "vp_cohort_open", "vp_cohort_set", "vp_cohort_run", "vp_cohort_sync", "vp_cohort_stream",
-           "vp_cohort_launches", "vp_cohort_close"]
+           "vp_cohort_launches", "vp_cohort_close", "vp_server_set_batching", "vp_server_stats"]
 
 
 def lib():
@@ -174,6 +174,8 @@ def lib():
     L.vp_cohort_launches.argtypes = [P, C.POINTER(C.c_int32)]
     L.vp_cohort_launches.restype = C.c_int64
     L.vp_cohort_close.argtypes = [P]
+    L.vp_server_set_batching.argtypes = [P, C.c_int32]
+    L.vp_server_stats.argtypes = [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     _lib = L
     return L
 

@@ -3,9 +3,12 @@
 // The reference runs each (K, replicate) on its own host thread that claims a
 // device slot for the run's whole length (BayesianThread and ManageCUDA,
 // src/structure.cpp:2467-2501 and 710-756). Here one scheduler thread keeps
-// every admitted run's sweeps queued on that run's own stream, in chunks, so
-// small runs (launch- and latency-bound on their own) overlap each other and
-// large ones, and a run's results are ready the moment its last chunk lands.
+// the admitted runs' sweeps queued in chunks. Runs whose sweeps are small
+// (launch- and latency-bound on their own) are batched: the runs of one size
+// class form a cohort whose every sweep is one launch per kernel for all of
+// them (vp_cohort_*), and runs join and leave it as they are admitted and
+// finish. Larger runs fill the device alone and keep their own streams. A
+// run's results are ready the moment its last chunk lands.
 //
 // Admission is in arrival order, bounded by a device-memory budget (dataset
 // upload plus chain state, sized exactly as vp_open / vp_chain_create
@@ -49,9 +52,28 @@ struct Req {
     int head = 0;            // event slot of the oldest of them
     bool finishing = false;  // the last chunk (with Arrange) is queued
     int64_t issued = 0, total = 0;
+    int cls = -1;            // the cohort class it runs in, -1: its own stream
     // the request holds its own reference to the dataset until it is deleted
     ~Req() { if (ds) vp_dataset_free(const_cast<vp_dataset*>(ds)); }
 };
+
+// the runs of one size class swept together in one cohort: one launch per
+// kernel of the sweep for all of them (vp_cohort_*), chunks of sweeps queued
+// on the cohort's stream
+struct CohortSlot {
+    vp_cohort* h = nullptr;
+    std::vector<Req*> members;
+    std::vector<Req*> joining;     // started, waiting for the next membership change
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int inflight = 0, head = 0;
+};
+
+// Cohort classes by the expected device time of one sweep (updates per sweep,
+// admixture sweeps weighted 10x, at about 3e12 updates/s): below 3 us, 30 us
+// and 300 us. Runs in one class differ at most tenfold in sweep cost, so the
+// lockstep of a cohort holds none back for long; larger runs fill the device
+// alone and keep their own stream.
+constexpr int N_CLASSES = 3;
 
 }  // namespace
 
@@ -68,6 +90,11 @@ struct vp_server {
     std::map<int64_t, Req*> reqs;
     int64_t next_id = 1;
     bool stop = false;
+    bool batching = true;           // small runs in cohorts (else every run on its own stream)
+    CohortSlot cohorts[N_CLASSES];  // touched by the scheduler thread only
+    // kernel launches queued and run-sweeps they carry (a cohort sweep of n
+    // members carries n run-sweeps)
+    int64_t launches = 0, run_sweeps = 0;
     std::thread th;
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
@@ -117,6 +144,16 @@ int run_priority(const vp_server* s, const Req* r) {
     return s->prio_greatest + idx;
 }
 
+int run_class(const Req* r) {
+    vp_dataset_info di{};
+    vp_dataset_info_get(r->ds, &di);
+    const double w = (double)di.n_ind * (double)di.n_loc * r->P.K * (r->P.admix ? 10.0 : 1.0);
+    const double us = w / 3e6;
+    for (int c = 0; c < N_CLASSES; ++c)
+        if (us < 3.0 * std::pow(10.0, c)) return c;
+    return -1;
+}
+
 // upload the dataset, create the chain and the two completion events
 int start_run(vp_server* s, Req* r) {
     int rc = vp_open_ex(r->ds, s->device, run_priority(s, r), &r->ctx);
@@ -163,12 +200,15 @@ bool advance(vp_server* s, Req* r, bool* finished) {
     cudaStream_t st = (cudaStream_t)vp_stream(r->ctx);
     while (r->inflight < 2 && !r->finishing) {
         const int64_t left = r->total - r->issued;
+        const int64_t l0 = vp_launch_count(r->ctx);
         int rc;
         if (left > s->chunk) {
             rc = vp_run(&r->chain, 1, s->chunk);
             if (!rc) {
                 std::lock_guard<std::mutex> lk(s->mu);
                 r->issued += s->chunk;
+                s->launches += vp_launch_count(r->ctx) - l0;
+                s->run_sweeps += s->chunk;
             }
         } else {
             rc = vp_finish_issue(&r->chain, 1);
@@ -176,6 +216,8 @@ bool advance(vp_server* s, Req* r, bool* finished) {
                 std::lock_guard<std::mutex> lk(s->mu);
                 r->issued = r->total;
                 r->finishing = true;
+                s->launches += vp_launch_count(r->ctx) - l0;
+                s->run_sweeps += left;
             }
         }
         if (!rc && cudaEventRecord(r->ev[(r->head + r->inflight) & 1], st) != cudaSuccess) rc = VP_E_CUDA;
@@ -190,6 +232,97 @@ bool advance(vp_server* s, Req* r, bool* finished) {
     return moved;
 }
 
+// every member of slot k fails with the cohort
+void fail_cohort(vp_server* s, CohortSlot& k, int rc, const char* what) {
+    std::vector<Req*> all = k.members;
+    all.insert(all.end(), k.joining.begin(), k.joining.end());
+    if (k.h) vp_cohort_set(k.h, nullptr, 0);
+    k.members.clear();
+    k.joining.clear();
+    k.inflight = 0;
+    for (Req* r : all) fail(s, r, rc, what);
+}
+
+// runs that have had every sweep queued leave the cohort (its graph is
+// captured again without them, with the runs waiting to join) and queue
+// their Arrange on their own stream, which is ordered after the cohort's
+// sweeps; their completion is then watched like a run of its own stream
+bool cohort_membership(vp_server* s, CohortSlot& k, std::vector<Req*>& finishing) {
+    std::vector<Req*> stay;
+    bool changed = !k.joining.empty();
+    for (Req* r : k.members) {
+        int64_t issued = 0, total = 0;
+        vp_chain_progress(r->chain, &issued, &total);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            r->issued = issued;
+        }
+        if (issued >= total) { finishing.push_back(r); changed = true; }
+        else stay.push_back(r);
+    }
+    if (!changed) return false;
+    stay.insert(stay.end(), k.joining.begin(), k.joining.end());
+    std::vector<vp_chain*> cs;
+    for (Req* r : stay) cs.push_back(r->chain);
+    int rc = vp_cohort_set(k.h, cs.data(), (int32_t)cs.size());
+    k.members = stay;
+    k.joining.clear();
+    if (rc) {
+        fail_cohort(s, k, rc, "forming the cohort failed");
+        return true;
+    }
+    for (Req* r : finishing) {
+        cudaStream_t st = (cudaStream_t)vp_stream(r->ctx);
+        int rc2 = vp_finish_issue(&r->chain, 1);
+        if (!rc2 && cudaEventRecord(r->ev[0], st) != cudaSuccess) rc2 = VP_E_CUDA;
+        if (rc2) { fail(s, r, rc2, "finishing the run failed"); continue; }
+        r->finishing = true;
+        r->inflight = 1;
+        r->head = 0;
+        r->cls = -1;
+        std::lock_guard<std::mutex> lk(s->mu);
+        r->issued = r->total;
+    }
+    return true;
+}
+
+// retire the cohort's finished chunks, change its members, queue more chunks
+bool advance_cohort(vp_server* s, CohortSlot& k, std::vector<Req*>& finishing) {
+    bool moved = false;
+    while (k.inflight > 0) {
+        cudaError_t q = cudaEventQuery(k.ev[k.head]);
+        if (q == cudaErrorNotReady) break;
+        if (q != cudaSuccess) {
+            char buf[160];
+            snprintf(buf, sizeof buf, "cohort failed on the device: %s", cudaGetErrorString(q));
+            fail_cohort(s, k, VP_E_CUDA, buf);
+            return true;
+        }
+        k.head ^= 1;
+        k.inflight--;
+        moved = true;
+    }
+    if (cohort_membership(s, k, finishing)) moved = true;
+    cudaStream_t st = (cudaStream_t)vp_cohort_stream(k.h);
+    while (k.inflight < 2 && !k.members.empty()) {
+        int rc = vp_cohort_run(k.h, s->chunk);
+        if (!rc && cudaEventRecord(k.ev[(k.head + k.inflight) & 1], st) != cudaSuccess) rc = VP_E_CUDA;
+        if (rc) { fail_cohort(s, k, rc, "queueing the cohort's sweeps failed"); return true; }
+        k.inflight++;
+        int32_t per = 0;
+        vp_cohort_launches(k.h, &per);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->launches += (int64_t)per * s->chunk;
+            for (Req* r : k.members) s->run_sweeps += std::min<int64_t>(s->chunk, r->total - r->issued);
+        }
+        moved = true;
+        // members whose last sweep is now queued leave at once
+        if (cohort_membership(s, k, finishing)) moved = true;
+    }
+    return moved;
+}
+
 void scheduler(vp_server* s) {
     cudaSetDevice(s->device);
     for (;;) {
@@ -197,7 +330,9 @@ void scheduler(vp_server* s) {
         {
             std::unique_lock<std::mutex> lk(s->mu);
             if (s->stop) return;
-            if (s->active.empty() && s->queue.empty()) {
+            bool cohort_work = false;
+            for (const CohortSlot& k : s->cohorts) cohort_work |= !k.members.empty() || !k.joining.empty();
+            if (s->active.empty() && s->queue.empty() && !cohort_work) {
                 s->cv_work.wait_for(lk, std::chrono::milliseconds(20));
                 continue;
             }
@@ -215,10 +350,27 @@ void scheduler(vp_server* s) {
         }
         for (Req* r : admit) {
             int rc = start_run(s, r);
-            if (rc) fail(s, r, rc, "starting the run failed");
+            if (rc) { fail(s, r, rc, "starting the run failed"); continue; }
+            r->cls = s->batching ? run_class(r) : -1;
+            if (r->cls >= 0 && !s->cohorts[r->cls].h) {
+                CohortSlot& k = s->cohorts[r->cls];
+                // smaller classes at higher stream priority (lower numbers run first)
+                const int prio = std::min(s->prio_least, s->prio_greatest + r->cls);
+                if (vp_cohort_open_ex(s->device, prio, &k.h) ||
+                    cudaEventCreateWithFlags(&k.ev[0], cudaEventDisableTiming) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&k.ev[1], cudaEventDisableTiming) != cudaSuccess)
+                    r->cls = -1;
+            }
+            if (r->cls >= 0) s->cohorts[r->cls].joining.push_back(r);
             else s->active.push_back(r);
         }
         bool moved = !admit.empty();
+        for (CohortSlot& k : s->cohorts) {
+            if (!k.h) continue;
+            std::vector<Req*> finishing;
+            moved |= advance_cohort(s, k, finishing);
+            for (Req* r : finishing) s->active.push_back(r);
+        }
         for (size_t i = 0; i < s->active.size();) {
             bool finished = false;
             moved |= advance(s, s->active[i], &finished);
@@ -377,10 +529,32 @@ extern "C" int vp_server_close(vp_server* s) {
     s->cv_work.notify_all();
     if (s->th.joinable()) s->th.join();
     cudaSetDevice(s->device);
+    for (CohortSlot& k : s->cohorts) {
+        if (k.h) vp_cohort_close(k.h);   // waits for its sweeps and lets go of its members
+        for (cudaEvent_t& e : k.ev)
+            if (e) cudaEventDestroy(e);
+        k.h = nullptr;
+    }
     for (auto& kv : s->reqs) {
         free_run(kv.second);
         delete kv.second;
     }
     delete s;
+    return VP_OK;
+}
+
+extern "C" int vp_server_set_batching(vp_server* s, int32_t on) {
+    if (!s) { vp_set_error("null argument"); return VP_E_ARG; }
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->reqs.empty()) { vp_set_error("set batching before the first vp_submit"); return VP_E_STATE; }
+    s->batching = on != 0;
+    return VP_OK;
+}
+
+extern "C" int vp_server_stats(vp_server* s, int64_t* launches, int64_t* run_sweeps) {
+    if (!s) { vp_set_error("null argument"); return VP_E_ARG; }
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (launches) *launches = s->launches;
+    if (run_sweeps) *run_sweeps = s->run_sweeps;
     return VP_OK;
 }

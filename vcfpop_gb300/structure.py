@@ -289,9 +289,11 @@ class Server:
     runs by device-memory budget and overlaps them on per-run streams
     (vp_server_open / vp_submit / vp_poll / vp_wait / vp_release)."""
 
-    def __init__(self, device: int = 0, mem_budget: int = 0, max_active: int = 0, chunk: int = 0):
+    def __init__(self, device: int = 0, mem_budget: int = 0, max_active: int = 0, chunk: int = 0,
+                 batching: bool = True):
         h = C.c_void_p()
         B.check(B.lib().vp_server_open(device, mem_budget, max_active, chunk, C.byref(h)))
+        B.check(B.lib().vp_server_set_batching(h, int(batching)))
         self.h = h
 
     def submit(self, ds: Dataset, p: B.VpParams) -> int:
@@ -327,6 +329,12 @@ class Server:
 
     def release(self, rid: int) -> None:
         B.check(B.lib().vp_release(self.h, rid))
+
+    def stats(self) -> dict:
+        """Kernel launches the scheduler queued and the run-sweeps they carry."""
+        a, b = C.c_int64(), C.c_int64()
+        B.check(B.lib().vp_server_stats(self.h, C.byref(a), C.byref(b)))
+        return dict(launches=int(a.value), run_sweeps=int(b.value))
 
     def close(self):
         if getattr(self, "h", None):
