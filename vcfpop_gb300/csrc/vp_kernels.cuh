@@ -337,6 +337,20 @@ __global__ void k_update_p_ctr(const DevChain* chains, const int4* map = nullptr
 // takes the codes of four loci with one 16-byte load. FP32 sums over a slice
 // are folded into Kahan-compensated FP32 totals (FP64 adds are slow on this
 // part), converted to FP64 once per chunk.
+// asynchronous global -> shared copies (cp.async); with ok false nothing is
+// read and the destination is zero-filled
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 constexpr int LL_SL = 32;
 template <int KC>
 __device__ __forceinline__ void kahan_fold(float* acc, float* s, float* cmp) {
@@ -358,9 +372,9 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
     constexpr int TS = ll_stride<KC>();
     constexpr int GW = LL_BLOCK / 16;          // genotype words per CTA and locus
     constexpr int GS = LL_SL + 4;              // padded row of the transposed words
-    __shared__ __align__(16) float sT[LL_SL][4][TS];
+    __shared__ __align__(16) float sT[2][LL_SL][4][TS];       // two slices in flight
     __shared__ __align__(16) float sP[LL_SL / 2][16][TS];
-    __shared__ __align__(16) uint32_t sG[GW][GS];
+    __shared__ __align__(16) uint32_t sG[2][GW][GS];
     const VBlock vb = vblock(map);
     const DevChain& c = chains[vb.z / kgroups];
     if (map && run_over(c)) return;
@@ -380,28 +394,46 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
     if (D.packed2) {
         const int w0 = i0 >> 4;
         const int wsel = threadIdx.x >> 4, sh = (threadIdx.x & 15) * 2;
-        for (int64_t ls = l0; ls < l1; ls += LL_SL) {
+        // Each slice's table rows (16-byte chunks) and genotype words are
+        // copied to shared memory asynchronously (cp.async) one slice ahead, so
+        // their global latency is covered by the pair-table build and the adds
+        // of the slice before. Rows and words past the chunk or the data are
+        // zero-filled: a zero row adds nothing, whatever the code.
+        constexpr int Q4 = KC / 4;                          // 16-byte chunks per table row
+        auto issue = [&](int64_t ls, int buf) {
             const int nl = (int)min((int64_t)LL_SL, l1 - ls);
-            __syncthreads();
-            // single-locus rows (zero past the chunk: those loci add nothing)
-            for (int j = threadIdx.x; j < LL_SL * 4 * KC; j += LL_BLOCK) {
-                int kk = j % KC, code = (j / KC) & 3, ll = j / (4 * KC);
-                float v = 0.f;
-                if (ll < nl && kg0 + kk < K) v = __ldg(c.lt + ((ls + ll) * 4 + code) * c.kp + kg0 + kk);
-                sT[ll][code][kk] = v;
+            for (int j = threadIdx.x; j < LL_SL * 4 * Q4; j += LL_BLOCK) {
+                const int q = j % Q4, row = j / Q4;
+                const bool ok = (row >> 2) < nl && kg0 + 4 * q < c.kp;
+                const float* src = ok ? c.lt + ((ls << 2) + row) * c.kp + kg0 + 4 * q : c.lt;
+                cp_async16(&sT[buf][row >> 2][row & 3][4 * q], src, ok);
             }
             for (int j = threadIdx.x; j < LL_SL * GW; j += LL_BLOCK) {
-                int ll = j % LL_SL, w = j / LL_SL;
-                sG[w][ll] = (ll < nl && w0 + w < D.Nw) ? __ldg(D.g2 + (ls + ll) * D.Nw + w0 + w) : 0xFFFFFFFFu;
+                const int ll = j % LL_SL, w = j / LL_SL;
+                const bool ok = ll < nl && w0 + w < D.Nw;
+                cp_async4(&sG[buf][w][ll], ok ? D.g2 + (ls + ll) * D.Nw + w0 + w : D.g2, ok);
+            }
+            cp_async_commit();
+        };
+        issue(l0, 0);
+        int buf = 0;
+        for (int64_t ls = l0; ls < l1; ls += LL_SL, buf ^= 1) {
+            if (ls + LL_SL < l1) {
+                issue(ls + LL_SL, buf ^ 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
             }
             __syncthreads();
             // pair rows: sP[p][a | b << 2] = sT[2p][a] + sT[2p + 1][b]
-            for (int j = threadIdx.x; j < (LL_SL / 2) * 16 * KC; j += LL_BLOCK) {
-                int kk = j % KC, cp = (j / KC) & 15, p = j / (16 * KC);
-                sP[p][cp][kk] = sT[2 * p][cp & 3][kk] + sT[2 * p + 1][cp >> 2][kk];
+            for (int j = threadIdx.x; j < (LL_SL / 2) * 16 * Q4; j += LL_BLOCK) {
+                const int q = j % Q4, cp = (j / Q4) & 15, p = j / (16 * Q4);
+                const float4 x = *reinterpret_cast<const float4*>(&sT[buf][2 * p][cp & 3][4 * q]);
+                const float4 y = *reinterpret_cast<const float4*>(&sT[buf][2 * p + 1][cp >> 2][4 * q]);
+                *reinterpret_cast<float4*>(&sP[p][cp][4 * q]) = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
             }
             __syncthreads();
-            const uint4* gw = reinterpret_cast<const uint4*>(&sG[wsel][0]);
+            const uint4* gw = reinterpret_cast<const uint4*>(&sG[buf][wsel][0]);
 #pragma unroll 2
             for (int q = 0; q < LL_SL / 4; ++q) {
                 const uint4 g = gw[q];
@@ -417,6 +449,7 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
                 }
             }
             kahan_fold<KC>(acc, s, cmp);
+            __syncthreads();   // sP and this buffer are rewritten next
         }
     } else {
         int cnt = 0;
