@@ -558,8 +558,8 @@ def serve_stream(args, local, rank):
     upd = sum(ds.N * ds.L * q["K"] * (q["nburnin"] + q["nreps"]) for q, ds, p in runs)
     h2d = sum(ds.L * ((ds.N + 15) // 16) * 4 + ds.L * 12 + ds.N * 12 for q, ds, p in runs)
 
-    def serve(max_active):
-        srv = S.Server(device=local, max_active=max_active, chunk=16)
+    def serve(max_active, batching=True):
+        srv = S.Server(device=local, max_active=max_active, chunk=16, batching=batching)
         ids = [None] * len(runs)
         t0 = time.perf_counter()
 
@@ -580,14 +580,18 @@ def serve_stream(args, local, rank):
             lnl.append(srv.result(rid)["rout"][0])
             infos.append(inf)
             srv.release(rid)
+        st = srv.stats()
         srv.close()
         ttr = np.array([i["t_done"] - i["t_submit"] for i in infos])
         span = max(i["t_done"] for i in infos) - min(i["t_submit"] for i in infos)
         assert np.isfinite(lnl).all()
         return {"updates_per_s": upd / span, "makespan_s": span, "p50_s": float(np.percentile(ttr, 50)),
-                "p99_s": float(np.percentile(ttr, 99)), "max_active": max_active}
+                "p99_s": float(np.percentile(ttr, 99)), "max_active": max_active, "batching": batching,
+                "launches": st["launches"], "run_sweeps": st["run_sweeps"],
+                "launches_per_run_sweep": st["launches"] / max(1, st["run_sweeps"])}
 
     conc = serve(64)
+    conc["unbatched"] = serve(64, batching=False)
     alone = serve(1)
     return conc, alone, runs, upd, h2d
 

@@ -337,19 +337,22 @@ int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int device, uint
                  int64_t* line_start, int64_t* n_loc);
 
 /* Locus filter of the reference (-f_bmaf, -f_k, -f_n, -f_ptype, -f_he, -f_ho,
- * -f_pic, -f_ae, -f_I: MarkerDiversity, src/filter.cpp:485-507, on the
+ * -f_pic, -f_ae, -f_I, -f_pval: MarkerDiversity, src/filter.cpp:485-507, on the
  * statistics of DIVERSITY::CalcDiversity, src/diversity.cpp:144-311). Each
  * window is used when its flag is set; a locus fails when no call is typed
  * or any used statistic falls outside its window (a NaN statistic passes,
- * as in the reference). The HWE test filter (-f_pval) is not included. */
+ * as in the reference). -f_pval uses the HWE G-test's p-value: NaN (the
+ * locus passes) when an expected genotype count is below 5. */
 typedef struct {
     int32_t bmaf_b, k_b, n_b, ptype_b, he_b, ho_b, pic_b, ae_b, I_b;
     int32_t k_min, k_max, n_min, n_max;
     int32_t single;   /* statistics in float (the reference's REAL under -g_float=single), else double */
     double bmaf_min, bmaf_max, ptype_min, ptype_max, he_min, he_max, ho_min, ho_max;
     double pic_min, pic_max, ae_min, ae_max, I_min, I_max;
+    int32_t pval_b;   /* -f_pval: the p-value of the HWE G-test (CalcDiversity, src/diversity.cpp:337-492) */
+    double pval_min, pval_max;
 } vp_locus_filter;
-#define VP_LOCUS_STATS 9   /* n, k, ptype, bmaf, he, ho, pic, ae, I */
+#define VP_LOCUS_STATS 10  /* n, k, ptype, bmaf, he, ho, pic, ae, I, pval */
 /* The statistics and the pass flag of every locus of a packed biallelic
  * diploid matrix (packed[n_loc][ceil(n_ind/16)], as vp_input.packed2) on the
  * device: keep[n_loc] = 1 if the locus passes; stats[n_loc][VP_LOCUS_STATS]

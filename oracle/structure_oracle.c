@@ -1241,6 +1241,21 @@ int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packe
             }                                                                                            \
             if (b > 0.5) b = 1 - b;                                                                      \
             bmaf = b; he = 1 - a2; ae = 1 / a2; I = Iv; pic = picv;                                      \
+            /* HWE G-test (diversity.cpp:337-492): expected count of each observed genotype */          \
+            /* GFZ * n (HWECoef x product of frequencies, in double, stored in REAL); any   */          \
+            /* expectation below 5 collapses two alleles into one, which leaves no test     */          \
+            REAL G = 0;                                                                                  \
+            int ok = 1;                                                                                  \
+            for (int g = 0; g < 3 && ok; ++g) {                                                          \
+                if (!gcount[g]) continue;                                                                \
+                const double gf = g == 1 ? 2.0 * (double)fre[1] * (double)fre[0]                         \
+                                         : (double)fre[g >> 1] * (double)fre[g >> 1];                     \
+                const REAL obs = (REAL)gcount[g], ex = (REAL)(gf * n);                                   \
+                if (ex < 5) ok = 0;                                                                      \
+                else G += 2 * obs * LOG(obs / ex);                                                       \
+            }                                                                                            \
+            /* df = C(ploidy + k - 1, ploidy) - k = 1; 1 - the chi-square CDF */                        \
+            if (ok) pval = (REAL)(1.0 - erf(sqrt(0.5 * (double)G)));                                     \
         }                                                                                                \
     } while (0)
 
@@ -1252,7 +1267,7 @@ void orc_locus_filter_pack2(const uint32_t* packed, int64_t L, int n_ind, const 
         unsigned gcount[4] = {0, 0, 0, 0};
         for (int i = 0; i < n_ind; ++i) gcount[(packed[l * Nw + (i >> 4)] >> (2 * (i & 15))) & 3]++;
         int k = 0, nn = 0;
-        double ptype, bmaf = NANV, he = NANV, hoo = NANV, pic = NANV, ae = NANV, I = NANV;
+        double ptype, bmaf = NANV, he = NANV, hoo = NANV, pic = NANV, ae = NANV, I = NANV, pval = NANV;
         if (f->single) ORC_LOCUS_STATS(float, logf);
         else ORC_LOCUS_STATS(double, log);
 #define OUT(v, lo, hi) ((v) < (lo) || (v) > (hi))
@@ -1261,12 +1276,14 @@ void orc_locus_filter_pack2(const uint32_t* packed, int64_t L, int n_ind, const 
                          (f->ptype_b && OUT(ptype, f->ptype_min, f->ptype_max)) ||
                          (f->he_b && OUT(he, f->he_min, f->he_max)) || (f->ho_b && OUT(hoo, f->ho_min, f->ho_max)) ||
                          (f->pic_b && OUT(pic, f->pic_min, f->pic_max)) || (f->ae_b && OUT(ae, f->ae_min, f->ae_max)) ||
-                         (f->I_b && OUT(I, f->I_min, f->I_max));
+                         (f->I_b && OUT(I, f->I_min, f->I_max)) ||
+                         (f->pval_b && pval != -1 && OUT(pval, f->pval_min, f->pval_max));
 #undef OUT
         keep[l] = fail ? 0 : 1;
         if (stats) {
-            double* o = stats + l * 9;
+            double* o = stats + l * 10;
             o[0] = nn; o[1] = k; o[2] = ptype; o[3] = bmaf; o[4] = he; o[5] = hoo; o[6] = pic; o[7] = ae; o[8] = I;
+            o[9] = pval;
         }
     }
 }

@@ -143,14 +143,16 @@ int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packe
 
 /* The locus filter (filter.cpp MarkerDiversity over diversity.cpp
  * CalcDiversity) for a packed biallelic diploid matrix; f holds the flags
- * and windows in the layout of vp_locus_filter. keep[L], stats[L][9] (n, k,
- * ptype, bmaf, he, ho, pic, ae, I). */
+ * and windows in the layout of vp_locus_filter. keep[L], stats[L][10] (n, k,
+ * ptype, bmaf, he, ho, pic, ae, I, pval). */
 typedef struct {
     int32_t bmaf_b, k_b, n_b, ptype_b, he_b, ho_b, pic_b, ae_b, I_b;
     int32_t k_min, k_max, n_min, n_max;
     int32_t single;   /* statistics in float (the reference's REAL under -g_float=single), else double */
     double bmaf_min, bmaf_max, ptype_min, ptype_max, he_min, he_max, ho_min, ho_max;
     double pic_min, pic_max, ae_min, ae_max, I_min, I_max;
+    int32_t pval_b;
+    double pval_min, pval_max;
 } orc_locus_filter;
 void orc_locus_filter_pack2(const uint32_t* packed, int64_t L, int n_ind, const orc_locus_filter* f, uint8_t* keep,
                             double* stats);

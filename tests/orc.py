@@ -216,13 +216,14 @@ class LocusFilter(C.Structure):
                                          "k_min", "k_max", "n_min", "n_max", "single")] + \
                [(n, C.c_double) for n in ("bmaf_min", "bmaf_max", "ptype_min", "ptype_max", "he_min", "he_max",
                                           "ho_min", "ho_max", "pic_min", "pic_max", "ae_min", "ae_max", "I_min",
-                                          "I_max")]
+                                          "I_max")] + \
+               [("pval_b", C.c_int32), ("pval_min", C.c_double), ("pval_max", C.c_double)]
 
 
 def locus_filter_pack2(packed, n_ind, f):
     packed = np.ascontiguousarray(packed, np.uint32)
     L = packed.shape[0]
     keep = np.zeros(L, np.uint8)
-    stats = np.zeros((L, 9))
+    stats = np.zeros((L, 10))
     lib().orc_locus_filter_pack2(packed.ctypes.data, L, n_ind, C.byref(f), keep.ctypes.data, stats.ctypes.data)
     return keep, stats

@@ -10,7 +10,7 @@ import pytest
 from vcfpop_gb300.build import CLI
 
 
-@pytest.mark.parametrize("flag", ["-f_dp=[10,100]", "-f_gq=[20,99]", "-f_qual=[30,255]", "-f_pval=[0.001,1]",
+@pytest.mark.parametrize("flag", ["-f_dp=[10,100]", "-f_gq=[20,99]", "-f_qual=[30,255]",
                                   "-f_windowsize=1000", "-f_ploidy=[2,2]",
                                   "-f_type=snp", "-f_chrprefix=chr"])
 def test_unimplemented_filters_are_refused(flag, tmp_path):
@@ -27,7 +27,7 @@ def test_implemented_filters_are_accepted(tmp_path):
     r = subprocess.run([CLI, "-structure", f"-g_input={tmp_path}/none.vcf", f"-g_output={tmp_path}/out", "-f",
                         "-f_bmaf=[0.05,0.5]", "-f_ptype=[0.9,1]", "-f_k=[2,2]", "-f_n=[1,1000]", "-f_he=[0,1]",
                         "-f_ho=[0,1]", "-f_pic=[0,1]", "-f_ae=[1,2]", "-f_I=[0,2]", "-f_itype=[0.5,1]",
-                        "-f_iploidy=[2,2]"], capture_output=True, text=True)
+                        "-f_iploidy=[2,2]", "-f_pval=[0.001,1]"], capture_output=True, text=True)
     assert r.returncode == 2
     assert "not implemented" not in r.stderr and "cannot read" in r.stderr
 

@@ -28,6 +28,9 @@ def _compare(packed, N, f):
     assert np.array_equal(np.isnan(stats), np.isnan(ostats))
     assert np.array_equal(stats[:, :8][both[:, :8]], ostats[:, :8][both[:, :8]])
     assert np.allclose(stats[:, 8][both[:, 8]], ostats[:, 8][both[:, 8]], rtol=1e-6)
+    # the HWE p-value: logs of the G statistic and the device's erf may differ
+    # in the last place
+    assert np.allclose(stats[:, 9][both[:, 9]], ostats[:, 9][both[:, 9]], rtol=1e-5, atol=1e-12)
     return keep
 
 
@@ -48,7 +51,8 @@ def test_every_window_with_edge_loci(single):
     G[60:80, 5:] = -1               # almost nothing typed
     packed = S.pack2(G)
     windows = [dict(), dict(k=(2, 2)), dict(n=(300, 333)), dict(he=(0.1, 0.45)), dict(pic=(0.05, 0.3)),
-               dict(ae=(1.2, 1.9)), dict(I=(0.2, 0.6)), dict(bmaf=(0.05, 0.5), ptype=(0.9, 1.0), ho=(0.0, 0.5))]
+               dict(ae=(1.2, 1.9)), dict(I=(0.2, 0.6)), dict(pval=(0.05, 1.0)),
+               dict(bmaf=(0.05, 0.5), ptype=(0.9, 1.0), ho=(0.0, 0.5), pval=(1e-4, 1.0))]
     for w in windows:
         keep = _compare(packed, 333, S.locus_filter_spec(single=single, **w))
         assert not keep[:20].any()

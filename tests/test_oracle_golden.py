@@ -9,6 +9,7 @@ import os
 import shutil
 import subprocess
 
+import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -178,3 +179,52 @@ def test_oracle_driver_runs_clean_under_sanitizers(tmp_path):
         for f in c["files"]:
             if f != "out.structure.txt":
                 assert open(w / f, "rb").read() == open(os.path.join(GOLD, case, f), "rb").read(), f"{case}/{f}"
+
+
+def test_oracle_hwe_pvalue_is_the_g_test_upper_tail(oracle_build):
+    """-f_pval's statistic (CalcDiversity's HWE test, src/diversity.cpp:
+    337-492) for biallelic diploid loci: the G statistic of the observed
+    genotype counts against HWE expectations from the sample's allele
+    frequencies, and its chi-square upper tail with one degree of freedom;
+    NaN when an expected count is below 5. The reference's own chi-square
+    CDF comes from a library that is not in its tree, so the p-value is
+    checked here against scipy's chi-square survival function of the same G
+    (in double), over loci drawn with and without HWE deviations."""
+    from . import orc
+    scipy_stats = pytest.importorskip("scipy.stats")
+    rng = np.random.default_rng(8)
+    N, L = 300, 400
+    p = rng.uniform(0.02, 0.98, L)
+    F = rng.uniform(-0.2, 0.6, L)                     # inbreeding: departures from HWE
+    probs = np.stack([p * p + F * p * (1 - p), 2 * p * (1 - p) * (1 - F), (1 - p) ** 2 + F * p * (1 - p)], 1)
+    probs = np.clip(probs, 0, None)
+    probs /= probs.sum(1, keepdims=True)
+    codes = np.array([rng.choice(3, N, p=pr) for pr in probs])
+    codes[rng.random((L, N)) < 0.05] = 3
+    Nw = (N + 15) // 16
+    pad = np.full((L, Nw * 16), 3, np.uint32)
+    pad[:, :N] = codes
+    packed = np.bitwise_or.reduce(pad.reshape(L, Nw, 16) << (np.arange(16, dtype=np.uint32) * 2), axis=2).astype(np.uint32)
+    f = orc.LocusFilter(single=0)
+    keep, stats = orc.locus_filter_pack2(packed, N, f)
+    tested = 0
+    for l in range(L):
+        c = np.array([(codes[l] == g).sum() for g in range(3)], np.float64)
+        n = c.sum()
+        fr = np.array([2 * c[0] + c[1], c[1] + 2 * c[2]]) + 1e-10
+        fr /= fr.sum()
+        ex = np.array([fr[0] ** 2, 2 * fr[0] * fr[1], fr[1] ** 2]) * n
+        if (ex[c > 0] < 5).any():
+            assert np.isnan(stats[l, 9])
+            continue
+        G = float(np.sum(2 * c[c > 0] * np.log(c[c > 0] / ex[c > 0])))
+        want = scipy_stats.chi2.sf(G, 1)
+        assert abs(stats[l, 9] - want) <= 1e-12 + 1e-9 * want, (l, stats[l, 9], want)
+        tested += 1
+    assert tested > L // 2
+    # the window drops the loci whose p-value falls outside it; NaN passes
+    f2 = orc.LocusFilter(single=0, pval_b=1, pval_min=0.01, pval_max=1.0)
+    keep2, _ = orc.locus_filter_pack2(packed, N, f2)
+    pv = stats[:, 9]
+    assert np.array_equal(keep2.astype(bool), keep.astype(bool) & ~(pv < 0.01))
+    assert (pv < 0.01).sum() > 10

@@ -68,7 +68,8 @@ class VpLocusFilter(C.Structure):
                                          "k_min", "k_max", "n_min", "n_max", "single")] + \
                [(n, C.c_double) for n in ("bmaf_min", "bmaf_max", "ptype_min", "ptype_max", "he_min", "he_max",
                                           "ho_min", "ho_max", "pic_min", "pic_max", "ae_min", "ae_max", "I_min",
-                                          "I_max")]
+                                          "I_max")] + \
+               [("pval_b", C.c_int32), ("pval_min", C.c_double), ("pval_max", C.c_double)]
 
 
 class VpTcConfig(C.Structure):

@@ -113,6 +113,7 @@ bool parse(int argc, char** argv, Opts& o) {
         else if (k == "-f_pic") o.lf.pic_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.pic_min, &o.lf.pic_max) == 2;
         else if (k == "-f_ae") o.lf.ae_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.ae_min, &o.lf.ae_max) == 2;
         else if (k == "-f_I") o.lf.I_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.I_min, &o.lf.I_max) == 2;
+        else if (k == "-f_pval") o.lf.pval_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.pval_min, &o.lf.pval_max) == 2;
         else if (k == "-f_itype") o.itype_b = sscanf(v.c_str(), "[%lf,%lf]", &o.itype_min, &o.itype_max) == 2;
         else if (k == "-f_iploidy") o.iploidy_b = sscanf(v.c_str(), "[%d,%d]", &o.iploidy_min, &o.iploidy_max) == 2;
         else if (k.rfind("-f_", 0) == 0) unimplemented.push_back(k);
@@ -121,12 +122,12 @@ bool parse(int argc, char** argv, Opts& o) {
     }
     // the reference applies its -f_* windows only under -f
     // (src/parameters.cpp:1336-1343); every other filter of the reference
-    // (-f_pval, -f_qual, -f_dp, -f_gq, -f_windowsize, ...) would change which
+    // (-f_qual, -f_dp, -f_gq, -f_windowsize, ...) would change which
     // loci, calls or individuals the clustering sees: refuse it rather than
     // run on unfiltered data
     if (o.filter && !unimplemented.empty()) {
         fprintf(stderr, "vcfpop-gb300: the filter %s is not implemented (implemented: -f_bmaf -f_k -f_n -f_ptype "
-                        "-f_he -f_ho -f_pic -f_ae -f_I -f_itype -f_iploidy)\n", unimplemented[0].c_str());
+                        "-f_he -f_ho -f_pic -f_ae -f_I -f_pval -f_itype -f_iploidy)\n", unimplemented[0].c_str());
         return false;
     }
     if (!structure) { fprintf(stderr, "vcfpop-gb300: only -structure is implemented\n"); return false; }
@@ -488,7 +489,8 @@ int main(int argc, char** argv) {
     // the locus filter (-f with -f_* windows: src/filter.cpp MarkerDiversity)
     // on the packed matrix, on the device; loci that fail are dropped here
     const vp_locus_filter& lf = o.lf;
-    const bool windows = lf.bmaf_b || lf.k_b || lf.n_b || lf.ptype_b || lf.he_b || lf.ho_b || lf.pic_b || lf.ae_b || lf.I_b;
+    const bool windows = lf.bmaf_b || lf.k_b || lf.n_b || lf.ptype_b || lf.he_b || lf.ho_b || lf.pic_b || lf.ae_b ||
+                         lf.I_b || lf.pval_b;
     std::vector<uint32_t> kept_packed;
     if (o.filter && windows) {
         if (!in.packed2) { fprintf(stderr, "vcfpop-gb300: the locus filter needs biallelic diploid data\n"); return 1; }

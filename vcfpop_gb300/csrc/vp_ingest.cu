@@ -373,12 +373,12 @@ __device__ __forceinline__ double rlog(double x) { return log(x); }
 // Unify in double stored in REAL, CountK above 1e-10, then the statistics
 template <typename REAL>
 __device__ void locus_stats(int c0, int c1, int c2, int N, int& k, double& ptype, double& bmaf, double& he, double& ho,
-                            double& pic, double& ae, double& I) {
+                            double& pic, double& ae, double& I, double& pval) {
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
     const int n = c0 + c1 + c2;
     ptype = (double)((REAL)n / (REAL)N);
     k = 0;
-    bmaf = he = ho = pic = ae = I = nan;
+    bmaf = he = ho = pic = ae = I = pval = nan;
     if (n == 0) return;
     REAL fre[2] = {(REAL)(2 * c0 + c1), (REAL)(c1 + 2 * c2)};
     const double invsum = 1.0 / ((double)fre[0] + (double)fre[1] + 2 * 1e-10);
@@ -404,6 +404,21 @@ __device__ void locus_stats(int c0, int c1, int c2, int N, int& k, double& ptype
     pic = picv;
     ae = (REAL)(1 / a2);
     I = Iv;
+    // HWE G-test (src/diversity.cpp:337-492): the expected count of each
+    // observed genotype, GFZ x n (HWE coefficient x frequencies in double,
+    // stored in REAL); an expectation below 5 collapses the two alleles into
+    // one and leaves no test (NaN). With two alleles df = 1, and the p-value
+    // is 1 - the chi-square CDF, 1 - erf(sqrt(G / 2)).
+    const int gc[3] = {c0, c1, c2};
+    REAL G = 0;
+    for (int g = 0; g < 3; ++g) {
+        if (!gc[g]) continue;
+        const double gf = g == 1 ? 2.0 * (double)fre[1] * (double)fre[0] : (double)fre[g >> 1] * (double)fre[g >> 1];
+        const REAL obs = (REAL)gc[g], ex = (REAL)(gf * n);
+        if (ex < 5) return;
+        G += 2 * obs * rlog(obs / ex);
+    }
+    pval = (REAL)(1.0 - erf(sqrt(0.5 * (double)G)));
 }
 
 __device__ __forceinline__ bool outside(double v, double lo, double hi) { return v < lo || v > hi; }
@@ -430,20 +445,22 @@ __global__ void k_locus_filter(const uint32_t* packed, int64_t L, int N, int Nw,
     if (lane) return;
     const int c0 = Nw * 16 - c1 - c2 - c3;  // padding calls are coded missing (3)
     const int n = c0 + c1 + c2;
-    double ptype, bmaf, he, ho, pic, ae, I;
+    double ptype, bmaf, he, ho, pic, ae, I, pval;
     int k;
-    if (f.single) locus_stats<float>(c0, c1, c2, N, k, ptype, bmaf, he, ho, pic, ae, I);
-    else locus_stats<double>(c0, c1, c2, N, k, ptype, bmaf, he, ho, pic, ae, I);
+    if (f.single) locus_stats<float>(c0, c1, c2, N, k, ptype, bmaf, he, ho, pic, ae, I, pval);
+    else locus_stats<double>(c0, c1, c2, N, k, ptype, bmaf, he, ho, pic, ae, I, pval);
     const bool fail = k == 0 || (f.bmaf_b && k == 2 && outside(bmaf, f.bmaf_min, f.bmaf_max)) ||
                       (f.k_b && (k < f.k_min || k > f.k_max)) || (f.n_b && (n < f.n_min || n > f.n_max)) ||
                       (f.ptype_b && outside(ptype, f.ptype_min, f.ptype_max)) ||
                       (f.he_b && outside(he, f.he_min, f.he_max)) || (f.ho_b && outside(ho, f.ho_min, f.ho_max)) ||
                       (f.pic_b && outside(pic, f.pic_min, f.pic_max)) || (f.ae_b && outside(ae, f.ae_min, f.ae_max)) ||
-                      (f.I_b && outside(I, f.I_min, f.I_max));
+                      (f.I_b && outside(I, f.I_min, f.I_max)) ||
+                      (f.pval_b && pval != -1 && outside(pval, f.pval_min, f.pval_max));
     keep[l] = fail ? 0 : 1;
     if (stats) {
         double* o = stats + l * VP_LOCUS_STATS;
         o[0] = n; o[1] = k; o[2] = ptype; o[3] = bmaf; o[4] = he; o[5] = ho; o[6] = pic; o[7] = ae; o[8] = I;
+        o[9] = pval;
     }
 }
 }  // namespace

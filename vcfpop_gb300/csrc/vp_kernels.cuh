@@ -1084,25 +1084,23 @@ __global__ void __launch_bounds__(ZA_WARPS * 32) k_update_z_admix_ctr(const DevC
                 if (act) {
                     const int al = cp.a[a];
                     const float* f = sF + (ll * MK + al) * KPAD;
-                    float sx = 0.f, pq[KM];
+                    // prefix sums of the weights q_k p_k (fused multiply-adds)
+                    float sx = 0.f, pre[KM];
 #pragma unroll
                     for (int k = 0; k < KM; ++k) {
-                        pq[k] = (EXACT || k < K) ? q[k] * f[k] : 0.f;
-                        sx += pq[k];
+                        if (EXACT || k < K) sx = __fmaf_rn(q[k], f[k], sx);
+                        pre[k] = sx;
                     }
                     if (rec) lacc += logf(sx);
-                    // Poly (src/statistics.cpp:357-385) on the same float weights
-                    float t = u * (sx + (float)(VP_MIN_FREQ * K));
+                    // Poly (src/statistics.cpp:357-385): the first cluster whose
+                    // cumulative weight (each weight + 1e-10) exceeds the
+                    // uniform times the total; the comparisons are independent
+                    // of each other, the smallest passing cluster wins
+                    const float t = u * (sx + (float)(VP_MIN_FREQ * K));
                     int k2 = K - 1;
-                    bool found = false;
 #pragma unroll
-                    for (int k = 0; k < KM; ++k) {
-                        if ((EXACT || k < K) && !found) {
-                            const float w = pq[k] + (float)VP_MIN_FREQ;
-                            if (t < w) { k2 = k; found = true; }
-                            else t -= w;
-                        }
-                    }
+                    for (int k = KM - 1; k >= 0; --k)
+                        if ((EXACT || k < K) && t < __fmaf_rn((float)(k + 1), (float)VP_MIN_FREQ, pre[k])) k2 = k;
                     // this slice's label counts, 8 bits per cluster (at most
                     // ZA_LC x 10 copies per slice)
 #pragma unroll
@@ -1195,8 +1193,8 @@ __global__ void __launch_bounds__(256) k_metro_ratio(const DevChain* chains, int
 #pragma unroll
                 for (int k = 0; k < KM; ++k)
                     if (EXACT || k < K) {
-                        s1 += q1[k] * f[k];
-                        s2 += q0[k] * f[k];
+                        s1 = __fmaf_rn(q1[k], f[k], s1);
+                        s2 = __fmaf_rn(q0[k], f[k], s2);
                     }
                 acc += logf(s1 / s2);
             }

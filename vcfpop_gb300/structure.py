@@ -237,12 +237,12 @@ def vcf_pack2(text: bytes, n_ind: int, device: int = 0):
     return packed[:n.value], starts[:n.value + 1]
 
 
-LOCUS_STATS = ("n", "k", "ptype", "bmaf", "he", "ho", "pic", "ae", "I")
+LOCUS_STATS = ("n", "k", "ptype", "bmaf", "he", "ho", "pic", "ae", "I", "pval")
 
 
 def locus_filter_spec(single: bool = True, **windows) -> B.VpLocusFilter:
     """A locus filter from -f_* windows given as name=(min, max), names as in
-    LOCUS_STATS (bmaf, k, n, ptype, he, ho, pic, ae, I)."""
+    LOCUS_STATS (bmaf, k, n, ptype, he, ho, pic, ae, I, pval)."""
     f = B.VpLocusFilter()
     f.single = 1 if single else 0
     for name, (lo, hi) in windows.items():
@@ -256,7 +256,7 @@ def locus_filter_spec(single: bool = True, **windows) -> B.VpLocusFilter:
 
 def locus_filter(packed: np.ndarray, n_ind: int, f: B.VpLocusFilter, device: int = 0):
     """Per-locus statistics and the pass flags of the -f_* locus filter on the
-    device: (keep [L] uint8, stats [L][9])."""
+    device: (keep [L] uint8, stats [L][10])."""
     packed = np.ascontiguousarray(packed, np.uint32)
     L = packed.shape[0]
     keep = np.zeros(L, np.uint8)
