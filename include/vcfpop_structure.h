@@ -336,6 +336,18 @@ int vp_prof_read(vp_ctx* ctx, double* ms, int32_t* launches);
 int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int device, uint32_t* packed, int64_t max_loci,
                  int64_t* line_start, int64_t* n_loc);
 
+/* The same ingest for any ploidy and allele count (the general genotype
+ * store of vp_input.alleles): alleles[n_loc][n_ind][vmax] gets each call's
+ * allele indices in ascending order (unphased, as the reference's
+ * AddVCFGenotype), -1 for a missing call (any '.' copy) and for copies past
+ * the call's ploidy; copies past vmax are dropped, as the reference's reader
+ * keeps the ploidy of each individual's first call. n_alleles[n_loc] = REF +
+ * ALTs; ploidy[n_ind] = the copies of each sample's call on the first line.
+ * vmax is 1..16; allele indices above 127 and malformed lines fail with
+ * VP_E_ARG naming the line. With max_loci == 0 it only counts the lines. */
+int vp_vcf_parse(const char* text, size_t bytes, int32_t n_ind, int32_t vmax, int device, int8_t* alleles,
+                 int32_t* n_alleles, int32_t* ploidy, int64_t max_loci, int64_t* line_start, int64_t* n_loc);
+
 /* Locus filter of the reference (-f_bmaf, -f_k, -f_n, -f_ptype, -f_he, -f_ho,
  * -f_pic, -f_ae, -f_I, -f_pval: MarkerDiversity, src/filter.cpp:485-507, on the
  * statistics of DIVERSITY::CalcDiversity, src/diversity.cpp:144-311). Each

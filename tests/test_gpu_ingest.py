@@ -100,3 +100,72 @@ def test_packed_vcf_runs_a_chain():
     ch = S.Chain(ctx, S.params(3, 5, admix=0, nadmburnin=0, nburnin=5, nreps=5))
     S.finish([ch])
     assert np.isfinite(ch.result()["rout"]).all()
+
+
+def _general_vcf(d, phased_every=0, extra=False, crlf=False):
+    """A VCF of any ploidy and allele count; calls in a shuffled copy order
+    (and '|' every phased_every-th call), so the parser must sort them."""
+    G, ploidy, k = d["G"], d["ploidy"], d["k"]
+    L, N, _ = G.shape
+    rng = np.random.default_rng(3)
+    lines = []
+    for l in range(L):
+        calls = []
+        for i in range(N):
+            v = int(ploidy[i])
+            g = G[l, i, :v]
+            if g[0] < 0:
+                c = "/".join(["."] * v)
+            else:
+                sep = "|" if phased_every and (l * N + i) % phased_every == 0 else "/"
+                c = sep.join(str(int(x)) for x in rng.permutation(g))
+            calls.append(c + (":12,3" if extra else ""))
+        alt = ",".join(["G"] * (int(k[l]) - 1))
+        lines.append(f"2\t{l + 1}\tv{l}\tA\t{alt}\t.\tPASS\t.\t{'GT:AD' if extra else 'GT'}\t" + "\t".join(calls))
+    nl = "\r\n" if crlf else "\n"
+    return (nl.join(lines) + nl).encode()
+
+
+@pytest.mark.parametrize("case", ["poly", "poly_extra_crlf", "haploid_diploid"])
+def test_general_parse_matches_the_source_genotypes(case):
+    """vp_vcf_parse on polyploid multiallelic data (ploidy 2/4/6, 2-8
+    alleles), with phased and unphased calls in any copy order, extra FORMAT
+    keys and CRLF line ends: the allele copies the data were drawn with, in
+    ascending order, -1 for missing calls, bit for bit; the alleles per locus
+    and each sample's ploidy as the host reader sets them."""
+    rng = np.random.default_rng(11)
+    if case == "haploid_diploid":
+        d = synth.fmodel(12, 50, 120, 2, 0.1, 0.05, ploidy=np.array([1, 2] * 25), n_alleles=rng.integers(2, 5, 120),
+                         anc_alpha=1.0)
+    else:
+        d = synth.fmodel(13, 90, 300, 3, 0.08, 0.03, ploidy=np.array([2, 2, 4, 6] * 22 + [2, 2]),
+                         n_alleles=rng.integers(2, 9, 300), anc_alpha=1.0)
+    text = _general_vcf(d, phased_every=7, extra="extra" in case, crlf="crlf" in case)
+    vmax = int(d["ploidy"].max())
+    G, k, ploidy, starts = S.vcf_parse(text, d["G"].shape[1], vmax)
+    assert np.array_equal(G, d["G"])
+    assert np.array_equal(k, d["k"])
+    assert np.array_equal(ploidy, d["ploidy"])
+    assert starts[0] == 0 and starts[-1] == len(text)
+
+
+def test_general_parse_of_the_golden_polyploid_vcf():
+    raw = gzip.open(os.path.join(GOLD, "poly.vcf.gz")).read()
+    header = raw[raw.index(b"\n#CHROM") + 1:].split(b"\n", 1)[0].decode().split("\t")
+    N = len(header) - 9
+    G, k, ploidy, _ = S.vcf_parse(_data_section(raw), N, 6)
+    # the genotypes the golden file was written from (tests/golden/make_golden.py)
+    d = synth.fmodel(3, 120, 300, 3, 0.08, 0.03, ploidy=np.array([2, 2, 4, 6] * 30),
+                     n_alleles=np.random.default_rng(0).integers(2, 9, 300), anc_alpha=1.0,
+                     loc_ids=np.repeat(np.arange(4), 30), loc_alpha=1.0)
+    assert np.array_equal(G, d["G"]) and np.array_equal(k, d["k"]) and np.array_equal(ploidy, d["ploidy"])
+
+
+def test_general_parse_rejects_what_it_cannot_store():
+    d = synth.fmodel(14, 10, 5, 2, 0.1, 0.0)
+    text = _general_vcf(d).replace(b"\t0/", b"\t200/", 1)
+    with pytest.raises(B.VpError, match="line 1: an allele index above 127"):
+        S.vcf_parse(text, 10, 2)
+    bad = _general_vcf(d).replace(b"\tGT\t", b"\tDP:GT\t", 1)
+    with pytest.raises(B.VpError, match="GT is not the first"):
+        S.vcf_parse(bad, 10, 2)

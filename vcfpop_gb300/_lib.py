@@ -103,7 +103,8 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_release", "vp_server_close", "vp_vcf_pack2", "vp_locus_filter_pack2", "vp_release_memory",
            "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout", "vp_write_structure",
            "vp_cohort_open", "vp_cohort_set", "vp_cohort_run", "vp_cohort_sync", "vp_cohort_stream",
-           "vp_cohort_launches", "vp_cohort_close", "vp_server_set_batching", "vp_server_stats"]
+           "vp_cohort_launches", "vp_cohort_close", "vp_server_set_batching", "vp_server_stats",
+           "vp_vcf_parse"]
 
 
 def lib():
@@ -164,6 +165,7 @@ def lib():
     L.vp_release.argtypes = [P, C.c_int64]
     L.vp_server_close.argtypes = [P]
     L.vp_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int32, C.c_int, P, C.c_int64, P, P]
+    L.vp_vcf_parse.argtypes = [P, C.c_size_t, C.c_int32, C.c_int32, C.c_int, P, P, P, C.c_int64, P, P]
     L.vp_locus_filter_pack2.argtypes = [P, C.c_int64, C.c_int32, C.POINTER(VpLocusFilter), C.c_int, P, P]
     L.vp_write_structure.argtypes = [P, C.POINTER(VpWriteOpts)]
     L.vp_cohort_open.argtypes = [C.c_int, C.POINTER(P)]

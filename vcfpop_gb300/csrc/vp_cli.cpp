@@ -215,11 +215,12 @@ bool read_vcf(const std::string& path, Vcf& v) {
 }
 
 // The whole file in memory (gzip or plain), then its genotypes parsed on the
-// device into the 2-bit matrix (vp_vcf_pack2). Biallelic diploid data only:
-// returns false (the host reader takes over) for anything else.
-bool read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
+// device: into the 2-bit matrix (vp_vcf_pack2) for biallelic diploid data
+// (returns 1), else into allele copies per call (vp_vcf_parse, returns 2).
+// Returns 0 when the host reader has to take over.
+int read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
     gzFile f = gzopen(o.input.c_str(), "rb");
-    if (!f) return false;
+    if (!f) return 0;
     std::vector<char> text;
     size_t n = 0;
     text.resize(1 << 26);
@@ -234,12 +235,12 @@ bool read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
     size_t p = 0;
     while (p < n && text[p] == '#' && p + 1 < n && text[p + 1] == '#') {
         const char* e = (const char*)memchr(text.data() + p, '\n', n - p);
-        if (!e) return false;
+        if (!e) return 0;
         p = (size_t)(e - text.data()) + 1;
     }
-    if (p >= n || text[p] != '#') return false;
+    if (p >= n || text[p] != '#') return 0;
     const char* he = (const char*)memchr(text.data() + p, '\n', n - p);
-    if (!he) return false;
+    if (!he) return 0;
     std::string hdr(text.data() + p, he - (text.data() + p));
     while (!hdr.empty() && hdr.back() == '\r') hdr.pop_back();
     int col = 0;
@@ -252,22 +253,58 @@ bool read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
         s0 = t + 1;
     }
     const int N = (int)v.inds.size();
-    if (N == 0) return false;
+    if (N == 0) return 0;
     const char* data = he + 1;
     const size_t bytes = n - (size_t)(data - text.data());
     int64_t L = 0;
     for (const char* q = data; (q = (const char*)memchr(q, '\n', bytes - (q - data))); ++q) ++L;
     if (bytes && data[bytes - 1] != '\n') ++L;
-    if (L == 0) return false;
+    if (L == 0) return 0;
     const int Nw = (N + 15) / 16;
     packed.assign((size_t)L * Nw, 0);
     std::vector<int64_t> starts(L + 1);
     int64_t got = 0;
     if (vp_vcf_pack2(data, bytes, N, o.device, packed.data(), L, starts.data(), &got) || got != L) {
-        fprintf(stderr, "vcfpop-gb300: device ingest not used (%s); reading on the host\n", vp_last_error());
-        v.inds.clear();
+        // not biallelic diploid: the general parse on the device (any ploidy
+        // and allele count), with each sample's ploidy from its first call
+        fprintf(stderr, "vcfpop-gb300: packed ingest not used (%s)\n", vp_last_error());
         packed.clear();
-        return false;
+        int vmax = 1;
+        {
+            const char* le = (const char*)memchr(data, '\n', bytes);
+            std::string first(data, le ? le - data : bytes);
+            int field = 0, cur = 1;
+            bool gt = false;
+            for (char ch : first) {
+                if (ch == '\t') { if (field >= 9) vmax = std::max(vmax, cur); ++field; cur = 1; gt = field >= 9; continue; }
+                if (ch == ':') gt = false;
+                if (gt && (ch == '/' || ch == '|')) ++cur;
+            }
+            if (field >= 9) vmax = std::max(vmax, cur);
+        }
+        vmax = std::min(vmax, 16);
+        v.G.assign((size_t)L * N * vmax, -1);
+        v.k.assign(L, 0);
+        v.ploidy.assign(N, 0);
+        if (vp_vcf_parse(data, bytes, N, vmax, o.device, v.G.data(), v.k.data(), v.ploidy.data(), L, starts.data(),
+                         &got) || got != L) {
+            fprintf(stderr, "vcfpop-gb300: device ingest not used (%s); reading on the host\n", vp_last_error());
+            v = Vcf();
+            return 0;
+        }
+        v.vmax = vmax;
+        v.locs.resize(L);
+        for (int64_t l = 0; l < L; ++l) {
+            const char* a = data + starts[l];
+            const char* e = data + starts[l + 1];
+            const char* t1 = (const char*)memchr(a, '\t', e - a);
+            const char* t2 = t1 ? (const char*)memchr(t1 + 1, '\t', e - t1 - 1) : nullptr;
+            const char* t3 = t2 ? (const char*)memchr(t2 + 1, '\t', e - t2 - 1) : nullptr;
+            if (!t1 || !t2 || !t3) { v = Vcf(); return 0; }
+            std::string id(t2 + 1, t3 - t2 - 1);
+            v.locs[l] = std::string(a, t1 - a) + "_" + (id != "." ? id : std::string(t1 + 1, t2 - t1 - 1));
+        }
+        return 2;
     }
     v.vmax = 2;
     v.ploidy.assign(N, 2);
@@ -280,11 +317,11 @@ bool read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
         const char* t1 = (const char*)memchr(a, '\t', e - a);
         const char* t2 = t1 ? (const char*)memchr(t1 + 1, '\t', e - t1 - 1) : nullptr;
         const char* t3 = t2 ? (const char*)memchr(t2 + 1, '\t', e - t2 - 1) : nullptr;
-        if (!t1 || !t2 || !t3) return false;
+        if (!t1 || !t2 || !t3) { v = Vcf(); packed.clear(); return 0; }
         std::string id(t2 + 1, t3 - t2 - 1);
         v.locs[l] = std::string(a, t1 - a) + "_" + (id != "." ? id : std::string(t1 + 1, t2 - t1 - 1));
     }
-    return true;
+    return 1;
 }
 
 // -g_indtext="pop1:#1-#30,#40 pop2:#31-#39 ..." (1-based individual ranges)
@@ -413,8 +450,9 @@ int main(int argc, char** argv) {
     if (!parse(argc, argv, o)) return 2;
     Vcf v;
     std::vector<uint32_t> dev_packed;   // device-parsed 2-bit matrix, file order of individuals
-    const bool dev_ingest = read_vcf_device(o, v, dev_packed);
-    if (!dev_ingest && !read_vcf(o.input, v)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
+    const int ingest = read_vcf_device(o, v, dev_packed);
+    const bool dev_ingest = ingest == 1;   // the 2-bit matrix (else allele copies in v.G)
+    if (!ingest && !read_vcf(o.input, v)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
     const int N0 = (int)v.inds.size();
     const int64_t L0 = (int64_t)v.k.size();
     std::vector<int> pop;

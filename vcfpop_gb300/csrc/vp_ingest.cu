@@ -208,6 +208,107 @@ __global__ void __launch_bounds__(PB) k_parse_lines(const char* t, const int64_t
     }
 }
 
+// One CTA per line, any ploidy and allele count: the call of each sample
+// ("a/b/c/..." or with '|', alleles 0..127, '.' for a missing copy, ending at
+// ':', tab or end of line) becomes its allele indices in ascending order (the
+// reference's unphased genotype, AddVCFGenotype in src/load.cpp), the first
+// vmax of them stored, -1 for a missing call or an absent copy; ploidy0 gets
+// the copies of each call on the first line (which sets each individual's
+// ploidy) and nall[l] the alleles of the locus (REF plus the ALT commas + 1).
+__global__ void __launch_bounds__(PB) k_parse_general(const char* t, const int64_t* start, int64_t L, int N, int vmax,
+                                                      int8_t* G, int32_t* nall, int32_t* bad, int32_t* ploidy0,
+                                                      int64_t line0) {
+    __shared__ int warp_tabs[PB / 32];
+    __shared__ int err;
+    __shared__ int nall_s;
+    const int64_t l = blockIdx.x;
+    if (l >= L) return;
+    const int64_t s = start[l];
+    int64_t e = start[l + 1];
+    if (e > s && t[e - 1] == '\n') --e;
+    if (e > s && t[e - 1] == '\r') --e;
+    if (threadIdx.x == 0) { err = 0; nall_s = 0; }
+    const int64_t len = e - s;
+    const int64_t seg = (len + PB - 1) / PB;
+    const int64_t a = s + min(len, (int64_t)threadIdx.x * seg), b = s + min(len, (int64_t)(threadIdx.x + 1) * seg);
+    int mine = 0;
+    for (int64_t p = a; p < b; ++p) mine += t[p] == '\t';
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tabs[warp] = incl;
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < warp; ++w) before += warp_tabs[w];
+    for (int w = 0; w < PB / 32; ++w) total += warp_tabs[w];
+    int f = before + incl - mine;
+    if (threadIdx.x == 0 && total != 8 + N) err = 1;
+    for (int64_t p = a; p < b; ++p) {
+        if (t[p] != '\t') continue;
+        const int field = f + 1;
+        ++f;
+        const char* q = t + p + 1;
+        const int64_t room = e - (p + 1);
+        if (field == 4) {
+            int commas = 0;
+            for (int64_t r = 0; r < room && q[r] != '\t'; ++r) commas += q[r] == ',';
+            nall_s = commas + 2;
+        } else if (field == 8) {
+            if (!(room >= 2 && q[0] == 'G' && q[1] == 'T' && (room == 2 || q[2] == ':' || q[2] == '\t'))) err = 2;
+        } else if (field >= 9) {
+            const int i = field - 9;
+            if (i >= N) { err = 1; continue; }
+            int al[16];
+            int n = 0, cur = -1;
+            bool miss = false, any = false;
+            int64_t r = 0;
+            for (; r < room && q[r] != ':' && q[r] != '\t'; ++r) {
+                const char ch = q[r];
+                if (ch == '/' || ch == '|') {
+                    if (!any) miss = true;
+                    else if (n < 16) al[n] = cur;
+                    ++n;
+                    cur = -1;
+                    any = false;
+                } else if (ch == '.') {
+                    miss = true;
+                    any = true;
+                } else if (ch >= '0' && ch <= '9') {
+                    cur = (cur < 0 ? 0 : cur * 10) + (ch - '0');
+                    if (cur > 127) { err = 5; cur = 127; }
+                    any = true;
+                } else {
+                    err = 3;
+                }
+            }
+            if (!any) miss = true;
+            else if (n < 16) al[n] = cur;
+            ++n;
+            if (n > 16) { err = 6; n = 16; }
+            if (l == 0 && line0 == 0) ploidy0[i] = n;
+            int8_t* out = G + ((size_t)l * N + i) * vmax;
+            for (int c = 0; c < vmax; ++c) out[c] = -1;
+            if (miss) continue;
+            // ascending order (insertion sort of at most 16)
+            for (int x = 1; x < n; ++x) {
+                const int v = al[x];
+                int y = x - 1;
+                while (y >= 0 && al[y] > v) { al[y + 1] = al[y]; --y; }
+                al[y + 1] = v;
+            }
+            for (int c = 0; c < n && c < vmax; ++c) out[c] = (int8_t)al[c];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bad[l] = err;
+        nall[l] = nall_s;
+    }
+}
+
 // host text -> device through two pinned staging buffers: the host copy into
 // one overlaps the DMA out of the other
 int upload_staged(char* dst, const char* src, int64_t n, cudaStream_t st) {
@@ -248,8 +349,82 @@ const char* reason(int code) {
         case 2: return "GT is not the first FORMAT key";
         case 3: return "a call is not a diploid 0/1 genotype";
         case 4: return "the locus does not have exactly 2 alleles";
+        case 5: return "an allele index above 127";
+        case 6: return "a call with more than 16 copies";
     }
     return "unknown";
+}
+
+}  // namespace
+
+namespace {
+
+// the text on the device and the start offsets of its lines (L + 1 entries,
+// the last the end of the text); with max_loci <= 0 only *n_loc is set
+struct TextIndex {
+    char* dt = nullptr;
+    int64_t* cnt = nullptr;
+    int64_t* starts = nullptr;
+    int64_t L = 0;
+    void release(cudaStream_t st) {
+        if (starts) cudaFreeAsync(starts, st);
+        if (cnt) cudaFreeAsync(cnt, st);
+        if (dt) cudaFreeAsync(dt, st);
+        starts = cnt = nullptr;
+        dt = nullptr;
+    }
+};
+
+int index_text(const char* text, size_t bytes, int64_t max_loci, cudaStream_t st, TextIndex& ix, int64_t* n_loc) {
+    const int64_t n = (int64_t)bytes;
+    const int64_t nchunks = (n + CHUNK - 1) / CHUNK;
+    cudaError_t e;
+    if ((e = cudaMallocAsync((void**)&ix.dt, n + 1, st)) != cudaSuccess ||
+        (e = cudaMallocAsync((void**)&ix.cnt, (nchunks + 1) * 8, st)) != cudaSuccess) {
+        vp_set_error("device allocation for the text failed: %s", cudaGetErrorString(e));
+        return VP_E_MEM;
+    }
+    if (int rc = upload_staged(ix.dt, text, n, st)) return rc;
+    const unsigned g = (unsigned)((nchunks * 32 + 255) / 256);
+    k_count_lf<<<g, 256, 0, st>>>(ix.dt, n, nchunks, ix.cnt);
+    cudaMemsetAsync(ix.cnt + nchunks, 0, 8, st);
+    k_scan<<<1, 1024, 0, st>>>(ix.cnt, nchunks + 1);
+    int64_t nlf = 0;
+    if ((e = cudaMemcpyAsync(&nlf, ix.cnt + nchunks, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+        vp_set_error("line index failed: %s", cudaGetErrorString(e));
+        return VP_E_CUDA;
+    }
+    // a last line without a line feed counts too
+    const bool tail = n > 0 && text[n - 1] != '\n';
+    ix.L = nlf + (tail ? 1 : 0);
+    *n_loc = ix.L;
+    if (max_loci <= 0 || ix.L == 0) return VP_OK;
+    if (ix.L > max_loci) { vp_set_error("%lld loci, buffer holds %lld", (long long)ix.L, (long long)max_loci); return VP_E_ARG; }
+    if ((e = cudaMallocAsync((void**)&ix.starts, (nlf + 2) * 8, st)) != cudaSuccess) {
+        vp_set_error("device allocation failed: %s", cudaGetErrorString(e));
+        return VP_E_MEM;
+    }
+    cudaMemsetAsync(ix.starts, 0, 8, st);
+    k_line_starts<<<g, 256, 0, st>>>(ix.dt, n, nchunks, ix.cnt, ix.starts);
+    // the end of the last line (the host value must outlive the copy)
+    static thread_local int64_t endv;
+    endv = n;
+    if ((e = cudaMemcpyAsync(ix.starts + ix.L, &endv, 8, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+        vp_set_error("line index failed: %s", cudaGetErrorString(e));
+        return VP_E_CUDA;
+    }
+    return VP_OK;
+}
+
+int open_device(int device, cudaStream_t* st) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
+    if (device < 0 || device >= ndev) { vp_set_error("device %d out of range", device); return VP_E_ARG; }
+    CKI(cudaSetDevice(device));
+    CKI(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+    return VP_OK;
 }
 
 }  // namespace
@@ -257,56 +432,17 @@ const char* reason(int code) {
 extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int device, uint32_t* packed,
                             int64_t max_loci, int64_t* line_start, int64_t* n_loc) {
     if (!text || !n_loc || n_ind <= 0 || (max_loci > 0 && !packed)) { vp_set_error("bad arguments"); return VP_E_ARG; }
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
-    if (device < 0 || device >= ndev) { vp_set_error("device %d out of range", device); return VP_E_ARG; }
-    CKI(cudaSetDevice(device));
     const int Nw = (n_ind + 15) / 16;
     if ((size_t)Nw * 4 > 200 * 1024) { vp_set_error("too many samples for one line row in shared memory"); return VP_E_ARG; }
     cudaStream_t st;
-    CKI(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    const int64_t n = (int64_t)bytes;
-    const int64_t nchunks = (n + CHUNK - 1) / CHUNK;
-    char* dt = nullptr;
-    int64_t *cnt = nullptr, *starts = nullptr;
+    if (int rc0 = open_device(device, &st)) return rc0;
+    TextIndex ix;
     int rc = VP_OK;
     do {
+        if ((rc = index_text(text, bytes, max_loci, st, ix, n_loc))) break;
+        const int64_t L = ix.L;
+        if (max_loci <= 0 || L == 0) break;                       // size query
         cudaError_t e;
-        if ((e = cudaMallocAsync((void**)&dt, n + 1, st)) != cudaSuccess ||
-            (e = cudaMallocAsync((void**)&cnt, (nchunks + 1) * 8, st)) != cudaSuccess) {
-            vp_set_error("device allocation for the text failed: %s", cudaGetErrorString(e));
-            rc = VP_E_MEM;
-            break;
-        }
-        if ((rc = upload_staged(dt, text, n, st))) break;
-        const unsigned g = (unsigned)((nchunks * 32 + 255) / 256);
-        k_count_lf<<<g, 256, 0, st>>>(dt, n, nchunks, cnt);
-        cudaMemsetAsync(cnt + nchunks, 0, 8, st);
-        k_scan<<<1, 1024, 0, st>>>(cnt, nchunks + 1);
-        int64_t nlf = 0;
-        if ((e = cudaMemcpyAsync(&nlf, cnt + nchunks, 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-            (e = cudaStreamSynchronize(st)) != cudaSuccess) {
-            vp_set_error("line index failed: %s", cudaGetErrorString(e));
-            rc = VP_E_CUDA;
-            break;
-        }
-        // a last line without a line feed counts too
-        const bool tail = n > 0 && text[n - 1] != '\n';
-        const int64_t L = nlf + (tail ? 1 : 0);
-        *n_loc = L;
-        if (max_loci <= 0) break;                       // size query
-        if (L > max_loci) { vp_set_error("%lld loci, buffer holds %lld", (long long)L, (long long)max_loci); rc = VP_E_ARG; break; }
-        if (L == 0) break;
-        if ((e = cudaMallocAsync((void**)&starts, (nlf + 2) * 8, st)) != cudaSuccess) {
-            vp_set_error("device allocation failed: %s", cudaGetErrorString(e));
-            rc = VP_E_MEM;
-            break;
-        }
-        cudaMemsetAsync(starts, 0, 8, st);
-        k_line_starts<<<g, 256, 0, st>>>(dt, n, nchunks, cnt, starts);
-        // the end of the last line
-        int64_t endv = n;
-        cudaMemcpyAsync(starts + L, &endv, 8, cudaMemcpyHostToDevice, st);
         uint32_t* dp = nullptr;
         int32_t* flags = nullptr;
         if ((e = cudaMallocAsync((void**)&dp, (size_t)L * Nw * 4, st)) != cudaSuccess ||
@@ -318,7 +454,7 @@ extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int d
         }
         for (int64_t l0 = 0; l0 < L; l0 += 1 << 30) {
             const unsigned nb = (unsigned)std::min<int64_t>(L - l0, 1 << 30);
-            k_parse_lines<<<nb, PB, (size_t)Nw * 4, st>>>(dt, starts + l0, nb, n_ind, Nw, dp + l0 * Nw,
+            k_parse_lines<<<nb, PB, (size_t)Nw * 4, st>>>(ix.dt, ix.starts + l0, nb, n_ind, Nw, dp + l0 * Nw,
                                                           LineOut{flags + l0, flags + L + l0});
         }
         if ((e = cudaGetLastError()) != cudaSuccess) {
@@ -328,7 +464,7 @@ extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int d
         std::vector<int32_t> hb(L);
         if (!rc && ((e = cudaMemcpyAsync(packed, dp, (size_t)L * Nw * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
                     (e = cudaMemcpyAsync(hb.data(), flags, (size_t)L * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-                    (line_start && (e = cudaMemcpyAsync(line_start, starts, (size_t)(L + 1) * 8, cudaMemcpyDeviceToHost,
+                    (line_start && (e = cudaMemcpyAsync(line_start, ix.starts, (size_t)(L + 1) * 8, cudaMemcpyDeviceToHost,
                                                         st)) != cudaSuccess))) {
             vp_set_error("copy-out failed: %s", cudaGetErrorString(e));
             rc = VP_E_CUDA;
@@ -347,9 +483,72 @@ extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int d
                     break;
                 }
     } while (0);
-    if (starts) cudaFreeAsync(starts, st);
-    if (cnt) cudaFreeAsync(cnt, st);
-    if (dt) cudaFreeAsync(dt, st);
+    ix.release(st);
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    return rc;
+}
+
+extern "C" int vp_vcf_parse(const char* text, size_t bytes, int32_t n_ind, int32_t vmax, int device, int8_t* alleles,
+                            int32_t* n_alleles, int32_t* ploidy, int64_t max_loci, int64_t* line_start, int64_t* n_loc) {
+    if (!text || !n_loc || n_ind <= 0 || vmax < 1 || vmax > 16 ||
+        (max_loci > 0 && (!alleles || !n_alleles || !ploidy))) {
+        vp_set_error("bad arguments");
+        return VP_E_ARG;
+    }
+    cudaStream_t st;
+    if (int rc0 = open_device(device, &st)) return rc0;
+    TextIndex ix;
+    int rc = VP_OK;
+    int8_t* dG = nullptr;
+    int32_t* flags = nullptr;
+    do {
+        if ((rc = index_text(text, bytes, max_loci, st, ix, n_loc))) break;
+        const int64_t L = ix.L;
+        if (max_loci <= 0 || L == 0) break;
+        cudaError_t e;
+        const size_t gb = (size_t)L * n_ind * vmax;
+        if ((e = cudaMallocAsync((void**)&dG, gb, st)) != cudaSuccess ||
+            (e = cudaMallocAsync((void**)&flags, (size_t)L * 8 + (size_t)n_ind * 4, st)) != cudaSuccess) {
+            vp_set_error("device allocation failed: %s", cudaGetErrorString(e));
+            rc = VP_E_MEM;
+            break;
+        }
+        int32_t* dnall = flags + L;
+        int32_t* dploidy = flags + 2 * L;
+        cudaMemsetAsync(dploidy, 0, (size_t)n_ind * 4, st);
+        for (int64_t l0 = 0; l0 < L; l0 += 1 << 30) {
+            const unsigned nb = (unsigned)std::min<int64_t>(L - l0, 1 << 30);
+            k_parse_general<<<nb, PB, 0, st>>>(ix.dt, ix.starts + l0, nb, n_ind, vmax, dG + (size_t)l0 * n_ind * vmax,
+                                               dnall + l0, flags + l0, dploidy, l0);
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            vp_set_error("parse launch failed: %s", cudaGetErrorString(e));
+            rc = VP_E_CUDA;
+            break;
+        }
+        std::vector<int32_t> hb(L);
+        if ((e = cudaMemcpyAsync(alleles, dG, gb, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(n_alleles, dnall, (size_t)L * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(ploidy, dploidy, (size_t)n_ind * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(hb.data(), flags, (size_t)L * 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (line_start && (e = cudaMemcpyAsync(line_start, ix.starts, (size_t)(L + 1) * 8, cudaMemcpyDeviceToHost,
+                                                st)) != cudaSuccess) ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+            vp_set_error("parse failed: %s", cudaGetErrorString(e));
+            rc = VP_E_CUDA;
+            break;
+        }
+        for (int64_t l = 0; l < L; ++l)
+            if (hb[l]) {
+                vp_set_error("data line %lld: %s", (long long)(l + 1), reason(hb[l]));
+                rc = VP_E_ARG;
+                break;
+            }
+    } while (0);
+    if (dG) cudaFreeAsync(dG, st);
+    if (flags) cudaFreeAsync(flags, st);
+    ix.release(st);
     cudaStreamSynchronize(st);
     cudaStreamDestroy(st);
     return rc;

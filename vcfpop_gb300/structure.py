@@ -237,6 +237,25 @@ def vcf_pack2(text: bytes, n_ind: int, device: int = 0):
     return packed[:n.value], starts[:n.value + 1]
 
 
+def vcf_parse(text: bytes, n_ind: int, vmax: int, device: int = 0):
+    """Parse the data lines of a VCF of any ploidy and allele count on the
+    device: (alleles [L][N][vmax] int8, ascending, -1 missing; alleles per
+    locus [L]; ploidy of each sample's first call [N]; line offsets [L + 1])."""
+    buf = np.frombuffer(text, dtype=np.uint8)
+    n = C.c_int64()
+    B.check(B.lib().vp_vcf_parse(buf.ctypes.data, len(text), n_ind, vmax, device, None, None, None, 0, None,
+                                 C.byref(n)))
+    L = n.value
+    G = np.empty((L, n_ind, vmax), np.int8)
+    k = np.empty(L, np.int32)
+    ploidy = np.empty(n_ind, np.int32)
+    starts = np.empty(L + 1, np.int64)
+    if L:
+        B.check(B.lib().vp_vcf_parse(buf.ctypes.data, len(text), n_ind, vmax, device, G.ctypes.data, k.ctypes.data,
+                                     ploidy.ctypes.data, L, starts.ctypes.data, C.byref(n)))
+    return G, k, ploidy, starts
+
+
 LOCUS_STATS = ("n", "k", "ptype", "bmaf", "he", "ho", "pic", "ae", "I", "pval")
 
 
