@@ -164,10 +164,14 @@ def test_context_closed_before_its_chains():
 
 def test_batched_cohorts_give_the_same_results_with_fewer_launches():
     """With batching (the default) the small runs of a mix sweep together in a
-    cohort, one launch per kernel of the sweep for all of them: the results
-    are those of every run on its own stream, bit for bit, with fewer kernel
-    launches per run-sweep."""
+    cohort, one launch per kernel variant of the sweep for all of them: the
+    results are those of every run on its own stream, bit for bit, with fewer
+    kernel launches per run-sweep."""
     runs = _runs()
+    # replicates with other seeds: runs of one sweep signature that merge
+    runs += [(ds, S.params(p.K, p.seed + 17 * j, rng=p.rng, admix=p.admix, locpriori=p.locpriori, f=p.fmodel,
+                           nburnin=p.nburnin, nreps=p.nreps, nadmburnin=p.nadmburnin))
+             for j, (ds, p) in enumerate(runs[:1] * 3 + runs[2:3] * 3, start=1)]
     got = {}
     for batching in (False, True):
         srv = S.Server(max_active=8, chunk=6, batching=batching)
@@ -178,4 +182,6 @@ def test_batched_cohorts_give_the_same_results_with_fewer_launches():
         srv.close()
     for a, b in zip(got[False], got[True]):
         _same(a, b)
-    assert got[(True, "lps")] < 0.6 * got[(False, "lps")], (got[(True, "lps")], got[(False, "lps")])
+    # runs of one model and cluster count (replicates) share a cohort and
+    # merge every launch; the others sweep in cohorts of their own
+    assert got[(True, "lps")] < 0.8 * got[(False, "lps")], (got[(True, "lps")], got[(False, "lps")])

@@ -65,3 +65,6 @@ const vp_dataset* vp_chain_dataset(const vp_chain* c);
 void vp_chain_params(const vp_chain* c, vp_params* p);
 // vp_cohort_open with the cohort's stream at a CUDA stream priority
 int vp_cohort_open_ex(int device, int priority, vp_cohort** out);
+// a hash of the launches of one sweep of the chain (kernels, shapes, scalar
+// arguments): chains with equal signatures merge every launch of a cohort
+uint64_t vp_chain_sweep_signature(vp_chain* c);

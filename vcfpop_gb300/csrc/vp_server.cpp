@@ -57,9 +57,10 @@ struct Req {
     ~Req() { if (ds) vp_dataset_free(const_cast<vp_dataset*>(ds)); }
 };
 
-// the runs of one size class swept together in one cohort: one launch per
-// kernel of the sweep for all of them (vp_cohort_*), chunks of sweeps queued
-// on the cohort's stream
+// the runs of one size class and one sweep signature (the same kernels,
+// launch shapes and scalar arguments) swept together in one cohort: one
+// launch per kernel of the sweep for all of them (vp_cohort_*), chunks of
+// sweeps queued on the cohort's stream
 struct CohortSlot {
     vp_cohort* h = nullptr;
     std::vector<Req*> members;
@@ -70,9 +71,10 @@ struct CohortSlot {
 
 // Cohort classes by the expected device time of one sweep (updates per sweep,
 // admixture sweeps weighted 10x, at about 3e12 updates/s): below 3 us, 30 us
-// and 300 us. Runs in one class differ at most tenfold in sweep cost, so the
-// lockstep of a cohort holds none back for long; larger runs fill the device
-// alone and keep their own stream.
+// and 300 us. Runs in one cohort have one sweep signature and differ at most
+// tenfold in sweep cost, so a cohort sweep costs about one run's sweep and
+// its lockstep holds none back for long; larger runs fill the device alone
+// and keep their own stream.
 constexpr int N_CLASSES = 3;
 
 }  // namespace
@@ -91,7 +93,10 @@ struct vp_server {
     int64_t next_id = 1;
     bool stop = false;
     bool batching = true;           // small runs in cohorts (else every run on its own stream)
-    CohortSlot cohorts[N_CLASSES];  // touched by the scheduler thread only
+    // cohorts by (size class, sweep signature): the runs of one cohort merge
+    // every launch of a sweep; touched by the scheduler thread only
+    std::map<std::pair<int, uint64_t>, CohortSlot> cohorts;
+    int in_cohorts = 0;             // runs in cohorts (members and joining), under mu
     // kernel launches queued and run-sweeps they carry (a cohort sweep of n
     // members carries n run-sweeps)
     int64_t launches = 0, run_sweeps = 0;
@@ -240,6 +245,10 @@ void fail_cohort(vp_server* s, CohortSlot& k, int rc, const char* what) {
     k.members.clear();
     k.joining.clear();
     k.inflight = 0;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->in_cohorts -= (int)all.size();
+    }
     for (Req* r : all) fail(s, r, rc, what);
 }
 
@@ -270,6 +279,10 @@ bool cohort_membership(vp_server* s, CohortSlot& k, std::vector<Req*>& finishing
     if (rc) {
         fail_cohort(s, k, rc, "forming the cohort failed");
         return true;
+    }
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->in_cohorts -= (int)finishing.size();
     }
     for (Req* r : finishing) {
         cudaStream_t st = (cudaStream_t)vp_stream(r->ctx);
@@ -330,14 +343,12 @@ void scheduler(vp_server* s) {
         {
             std::unique_lock<std::mutex> lk(s->mu);
             if (s->stop) return;
-            bool cohort_work = false;
-            for (const CohortSlot& k : s->cohorts) cohort_work |= !k.members.empty() || !k.joining.empty();
-            if (s->active.empty() && s->queue.empty() && !cohort_work) {
+            if (s->active.empty() && s->queue.empty() && s->in_cohorts == 0) {
                 s->cv_work.wait_for(lk, std::chrono::milliseconds(20));
                 continue;
             }
             // arrival order: the head of the queue waits for room
-            while (!s->queue.empty() && (int)(s->active.size() + admit.size()) < s->max_active) {
+            while (!s->queue.empty() && (int)(s->active.size() + s->in_cohorts + admit.size()) < s->max_active) {
                 Req* r = s->queue.front();
                 if (s->used + r->bytes > s->budget) break;
                 s->queue.pop_front();
@@ -352,24 +363,47 @@ void scheduler(vp_server* s) {
             int rc = start_run(s, r);
             if (rc) { fail(s, r, rc, "starting the run failed"); continue; }
             r->cls = s->batching ? run_class(r) : -1;
-            if (r->cls >= 0 && !s->cohorts[r->cls].h) {
-                CohortSlot& k = s->cohorts[r->cls];
-                // smaller classes at higher stream priority (lower numbers run first)
-                const int prio = std::min(s->prio_least, s->prio_greatest + r->cls);
-                if (vp_cohort_open_ex(s->device, prio, &k.h) ||
-                    cudaEventCreateWithFlags(&k.ev[0], cudaEventDisableTiming) != cudaSuccess ||
-                    cudaEventCreateWithFlags(&k.ev[1], cudaEventDisableTiming) != cudaSuccess)
-                    r->cls = -1;
+            std::pair<int, uint64_t> key(r->cls, 0);
+            if (r->cls >= 0) {
+                key.second = vp_chain_sweep_signature(r->chain);
+                CohortSlot& k = s->cohorts[key];
+                if (!k.h) {
+                    // smaller classes at higher stream priority (lower numbers run first)
+                    const int prio = std::min(s->prio_least, s->prio_greatest + r->cls);
+                    if (vp_cohort_open_ex(s->device, prio, &k.h) ||
+                        cudaEventCreateWithFlags(&k.ev[0], cudaEventDisableTiming) != cudaSuccess ||
+                        cudaEventCreateWithFlags(&k.ev[1], cudaEventDisableTiming) != cudaSuccess) {
+                        if (k.h) vp_cohort_close(k.h);
+                        for (cudaEvent_t& e : k.ev)
+                            if (e) cudaEventDestroy(e);
+                        s->cohorts.erase(key);
+                        r->cls = -1;
+                    }
+                }
             }
-            if (r->cls >= 0) s->cohorts[r->cls].joining.push_back(r);
-            else s->active.push_back(r);
+            if (r->cls >= 0) {
+                s->cohorts[key].joining.push_back(r);
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->in_cohorts++;
+            } else {
+                s->active.push_back(r);
+            }
         }
         bool moved = !admit.empty();
-        for (CohortSlot& k : s->cohorts) {
-            if (!k.h) continue;
+        for (auto it = s->cohorts.begin(); it != s->cohorts.end();) {
+            CohortSlot& k = it->second;
             std::vector<Req*> finishing;
             moved |= advance_cohort(s, k, finishing);
             for (Req* r : finishing) s->active.push_back(r);
+            // a cohort left without runs and without sweeps in flight closes
+            if (k.members.empty() && k.joining.empty() && k.inflight == 0) {
+                vp_cohort_close(k.h);
+                for (cudaEvent_t& e : k.ev)
+                    if (e) cudaEventDestroy(e);
+                it = s->cohorts.erase(it);
+            } else {
+                ++it;
+            }
         }
         for (size_t i = 0; i < s->active.size();) {
             bool finished = false;
@@ -529,12 +563,14 @@ extern "C" int vp_server_close(vp_server* s) {
     s->cv_work.notify_all();
     if (s->th.joinable()) s->th.join();
     cudaSetDevice(s->device);
-    for (CohortSlot& k : s->cohorts) {
+    for (auto& kv : s->cohorts) {
+        CohortSlot& k = kv.second;
         if (k.h) vp_cohort_close(k.h);   // waits for its sweeps and lets go of its members
         for (cudaEvent_t& e : k.ev)
             if (e) cudaEventDestroy(e);
         k.h = nullptr;
     }
+    s->cohorts.clear();
     for (auto& kv : s->reqs) {
         free_run(kv.second);
         delete kv.second;

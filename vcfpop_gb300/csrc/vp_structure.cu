@@ -1268,10 +1268,9 @@ int cohort_build(vp_cohort* h) {
     for (int i = 0; i < n; ++i) hc[i] = h->chains[i]->h;
     DevChain* dchains = (DevChain*)h->mem;
     int4* dmaps = (int4*)((char*)h->mem + hb);
+    // (from pageable memory: the copies are staged before the calls return)
     CK(cudaMemcpyAsync(dchains, hc.data(), (size_t)n * sizeof(DevChain), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(dmaps, maps.data(), maps.size() * sizeof(int4), cudaMemcpyHostToDevice, h->stream));
-    // the host copies must not be released before the uploads have read them
-    CK(cudaStreamSynchronize(h->stream));
     // 4. capture one sweep
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -1325,6 +1324,24 @@ int vp_cohort_open_ex(int device, int priority, vp_cohort** out) {
 }
 
 extern "C" int vp_cohort_open(int device, vp_cohort** out) { return vp_cohort_open_ex(device, 0, out); }
+
+// a hash of the kernels, launch shapes and scalar arguments of one sweep of
+// the chain: chains with equal signatures merge every launch of a cohort
+uint64_t vp_chain_sweep_signature(vp_chain* c) {
+    std::vector<SweepRec> rec;
+    c->ctx->rec = &rec;
+    launch_sweep(c);
+    c->ctx->rec = nullptr;
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
+    for (const SweepRec& r : rec) {
+        mix((uint64_t)(uintptr_t)r.fn);
+        mix(((uint64_t)r.block.x << 32) | ((uint64_t)r.block.y << 16) | r.block.z);
+        mix(((uint64_t)(uint32_t)r.nint << 32) | (uint32_t)r.i0);
+        mix((uint64_t)(uint32_t)r.i1);
+    }
+    return h;
+}
 
 extern "C" int vp_cohort_set(vp_cohort* h, vp_chain** cs, int32_t n) {
     if (!h || n < 0 || (n > 0 && !cs)) { vp_set_error("bad arguments"); return VP_E_ARG; }
