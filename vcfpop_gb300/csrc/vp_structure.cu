@@ -999,6 +999,9 @@ extern "C" int vp_chain_sizes(vp_chain* c, vp_result* r) {
     r->K = c->P.K; r->N = c->ctx->N; r->S = c->ctx->S; r->KT = c->ctx->KT;
     r->nburnin = c->h.nburnin; r->nreps = c->h.nreps; r->nthinning = c->h.nthinning; r->rlen = c->h.rlen;
     r->seed = c->P.seed;
+    // after the sweeps queued on the chain's (non-blocking) stream
+    cudaSetDevice(c->ctx->device);
+    CK(cudaStreamSynchronize(c->ctx->stream));
     Ctl ctl;
     CK(cudaMemcpy(&ctl, c->h.ctl, sizeof ctl, cudaMemcpyDeviceToHost));
     r->nr = ctl.nr; r->nlnl = ctl.nlnl;
@@ -2128,6 +2131,10 @@ extern "C" int vp_tc_config_get(vp_chain** cs, int32_t n, vp_tc_config* out) {
 extern "C" int vp_tc_status(vp_ctx* x) {
     if (!x) { vp_set_error("null context"); return VP_E_ARG; }
     if (!x->tc.ready) return 0;
+    // the context's stream is non-blocking: a copy on the default stream
+    // would not wait for the kernels (or the initial clear) queued on it
+    cudaSetDevice(x->device);
+    CK(cudaStreamSynchronize(x->stream));
     int e = 0;
     CK(cudaMemcpy(&e, x->tc.err, sizeof(int), cudaMemcpyDeviceToHost));
     return e;
