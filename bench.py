@@ -897,8 +897,29 @@ def main():
     # the batched UpdateP of the same sweeps: Dirichlet draws per second, from
     # CUDA events around its launch inside the sweep graph (after the timed
     # steps; the chains run a few more of their sweeps)
-    updatep = None
+    updatep = pipeline = None
     if form == B.VP_FORM_TC:
+        # the same chains' next sweeps by allele ranges (UpdateP of one range
+        # beside the contraction of the range before it), for comparison
+        # with the timed one-pass sweeps
+        cfg = S.tc_config(chains)
+        ctx.tc_pipeline(2)
+        for _ in range(2):
+            B.check(lib.vp_run(arr, len(chains), 1))
+        ctx.sync()
+        n1 = 10
+        e0.record(stream)
+        for _ in range(n1):
+            B.check(lib.vp_run(arr, len(chains), 1))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ranges_ms = e0.elapsed_time(e1) / n1
+        ctx.tc_pipeline(0)
+        pipeline = {"ms_per_step": ms_step, "ms_per_step_by_ranges": ranges_ms, "ranges": cfg["splits"],
+                    "what": "timed sweeps in one pass (UpdateP of every locus, then the whole likelihood "
+                            "contraction) against the same chains' next sweeps by allele ranges (UpdateP of a "
+                            "range beside the contraction slice of the range before it, at most 2 UpdateP "
+                            "blocks beside a contraction CTA)"}
         lib.vp_prof_enable(ctx.h, 2)
         up_ms = []
         for it in range(4):
@@ -1039,7 +1060,7 @@ def main():
             "gpu_launches": launches, "clocks": clk.summary(), "tc_error_flag": tc_err, "lnp_rel_err": lnp_err,
             "plain_form": plain, "batched_over_plain": value / plain["value"] if plain else None,
             "labels": labels, "serving": serving, "single_chain": extra,
-            "tuning": tuning, "updatep": updatep,
+            "tuning": tuning, "updatep": updatep, "pipeline": pipeline,
             "outputs": outputs, "ingest": ingest, "locus_filter": lfilter}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -215,8 +215,8 @@ int vp_tc_status(vp_ctx* ctx);
  * split `splits` ways (0: the whole-wave rule), and with `group_major` the
  * column groups of one individual tile launch next to each other. The count
  * contraction has `count_stages` and `count_group_major`. Compiled tiles
- * (bk, row_tiles, cols, piece): (64, 2, 192, 192), (64, 1, 288, 144),
- * (32, 2, 192, 192). */
+ * (bk, row_tiles, cols, piece): (64, 2, 192, 192), (64, 2, 144, 144),
+ * (64, 1, 288, 144), (32, 2, 192, 192). */
 typedef struct vp_tc_config {
     int32_t bk, row_tiles, cols, piece, stages, splits, group_major;
     int32_t count_stages, count_group_major;
@@ -242,6 +242,18 @@ int vp_tune(vp_chain** chains, int32_t n, int32_t effort, vp_tc_config* out);
 int vp_tc_configure(vp_chain** chains, int32_t n, const vp_tc_config* cfg);
 /* The configuration the batch of these chains runs with. */
 int vp_tc_config_get(vp_chain** chains, int32_t n, vp_tc_config* out);
+
+/* share >= 1: the tensor-core sweep of this context runs by allele ranges,
+ * one per split-K slice of the likelihood contraction, UpdateP of a range
+ * beside the contraction of the range before it, with at most `share` (1-8)
+ * UpdateP blocks on an SM beside one contraction CTA; share = 0 (the
+ * default): UpdateP of every locus, then the whole contraction. All give the
+ * same values (no reference counterpart: the reference has no batched form).
+ * On GB300 the contraction slows by about UpdateP's own time when the two
+ * share SMs, so the ranges save nothing there. With profiling mode 1 the
+ * profiled span is the contraction's, from its first slice to its last;
+ * with mode 2 it is UpdateP's, from its first range to its last. */
+int vp_tc_pipeline(vp_ctx* ctx, int share);
 
 /* Diagnostic: D[s][m][n] = sum over this split's k of A[m,k] (B0[n,k] + B1[n,k])
  * through the tensor-core kernel. A [M][K], B0/B1 [N][K] bf16 bit patterns,

@@ -40,6 +40,7 @@ def gemm(A, B0, B1, BN, piece, splits=1, stages=2, mt=1, bk=64):
     (100, 192, 64, 192, 192, 1, 1, 3, 2, 64),
     (256, 576, 512, 288, 144, 2, 1, 2, 1, 64),
     (200, 576, 1024, 288, 144, 2, 3, 2, 1, 64),
+    (300, 432, 1024, 144, 144, 2, 2, 3, 2, 64),
     (128, 256, 64, 256, 256, 1, 1, 2, 1, 64),
     (384, 512, 640, 256, 256, 1, 1, 4, 1, 64),
     (300, 384, 800, 192, 192, 2, 3, 5, 2, 32),
@@ -177,7 +178,7 @@ def test_plain_steps_on_a_batch_chain_equal_plain_chain():
     ctx.close()
 
 
-TILES = [(64, 2, 192, 192), (64, 1, 288, 144), (32, 2, 192, 192)]
+TILES = [(64, 2, 192, 192), (64, 2, 144, 144), (64, 1, 288, 144), (32, 2, 192, 192)]
 
 
 def _tc_set(ctx, Ks, seed0):
@@ -238,6 +239,79 @@ def test_every_tc_configuration_gives_the_same_sweep():
                         for f in a:
                             assert np.array_equal(a[f], b[f]), (bk, cols, stages, gm, f)
     assert ran >= 12
+
+
+@pytest.mark.parametrize("bk,splits,share", [(64, 2, 2), (64, 3, 1), (64, 7, 8), (32, 5, 2), (64, 1, 2)])
+def test_sweep_by_allele_ranges_equals_one_pass(bk, splits, share):
+    """The sweep by allele ranges (UpdateP of one range beside the likelihood
+    contraction of the range before it) against UpdateP of every locus, then
+    the whole contraction: the same state bit for bit after every sweep,
+    including a last range shorter than the rest, an odd number of 32-allele
+    k-blocks per range (ranges that do not start on a 64-allele boundary), and
+    one split (no ranges), and caps of 1, 2 and 8 UpdateP blocks beside a
+    contraction CTA. Both profiling modes time one span per sweep."""
+    d = synth.fmodel(56, 300, 3103, 3, 0.05, 0.02)
+    ds = S.Dataset.from_synth(d)
+    if bk == 32:
+        # a split count (near the one asked) with an odd number of k-blocks per split
+        kblocks = (2 * ds.L + 63) // 64 * 2
+        splits = next(s for s in (splits, splits - 2, splits + 2, splits + 4, splits + 6)
+                      if (-(-kblocks // s)) % 2 == 1 and -(-kblocks // -(-kblocks // s)) == s)
+    states = []
+    for pipe in (share, 0):
+        ctx = S.Context(ds)
+        ctx.tc_pipeline(pipe)
+        chains = _tc_set(ctx, [2, 3, 5, 10], 700)
+        mt, cols, piece = next((m, c, p) for b, m, c, p in TILES if b == bk)
+        S.tc_configure(chains, bk=bk, row_tiles=mt, cols=cols, piece=piece, stages=2, splits=splits)
+        assert S.tc_config(chains)["splits"] == splits
+        seq = []
+        for mode in (1, 2, 0):
+            B.check(B.lib().vp_prof_enable(ctx.h, mode))
+            S.run_chains(chains, 1)
+            if mode:
+                ms, nl = C.c_double(), C.c_int32()
+                B.check(B.lib().vp_prof_read(ctx.h, C.byref(ms), C.byref(nl)))
+                assert nl.value == 1 and ms.value > 0
+            seq.append(_state(chains))
+        assert B.lib().vp_tc_status(ctx.h) == 0
+        states.append(seq)
+        for c in chains:
+            c.close()
+        ctx.close()
+    for a_sweep, b_sweep in zip(*states):
+        for a, b in zip(a_sweep, b_sweep):
+            for f in a:
+                assert np.array_equal(a[f], b[f]), (bk, splits, f)
+
+
+def test_label_draw_does_not_depend_on_the_batch_around_a_chain():
+    """The label draw runs by tiles of 32 individuals and groups of
+    consecutive chains (at most 160 cluster rows per group). 40 chains of
+    K = 10 alone (groups of 16 chains from the first) and behind 13 chains of
+    K = 3 (39 rows first: every group boundary moves), at the same split
+    count, reach the same labels, counts, frequencies and likelihoods bit for
+    bit, and the same per-sweep likelihood sums to 1e-12."""
+    d = synth.fmodel(57, 333, 1500, 4, 0.05, 0.02)
+    ds = S.Dataset.from_synth(d)
+    got = []
+    for extra in (0, 13):
+        ctx = S.Context(ds)
+        front = [S.Chain(ctx, S.params(3, 2000 + j, form=B.VP_FORM_TC, admix=0, nadmburnin=0, nburnin=20, nreps=20))
+                 for j in range(extra)]
+        chains = front + _tc_set(ctx, [10] * 40, 1300)
+        S.tc_configure(chains, splits=3)
+        S.run_chains(chains, 3)
+        assert B.lib().vp_tc_status(ctx.h) == 0
+        got.append((_state(chains[extra:]), [c.get("LNL")[0] for c in chains[extra:]]))
+        for c in chains:
+            c.close()
+        ctx.close()
+    (a, la), (b, lb) = got
+    for x, y in zip(a, b):
+        for f in ("Z", "NI", "FREQ", "LL"):
+            assert np.array_equal(x[f], y[f]), f
+    assert np.allclose(la, lb, rtol=1e-12, atol=0)
 
 
 def test_tune_keeps_chain_state_and_serves_later_batches(tmp_path, monkeypatch):

@@ -49,6 +49,31 @@ def test_noalloc_matches_allocating_call_twice():
         assert rel.max() < REL, rel.max()
 
 
+def test_noalloc_replays_from_a_captured_graph():
+    """After one uncaptured call, the call captured into a CUDA graph and
+    replayed twice gives what the uncaptured call gives, bit for bit: its
+    chain descriptor travels as a kernel parameter, so a replay reads nothing
+    of the capturing call's host frame."""
+    import ctypes as C
+    import torch
+    lib = B.lib()
+    N, L, K = 700, 3000, 5
+    g, f = _inputs(3, N, L, K)
+    want = _call(lib.vp_loglik_packed2_noalloc, g, f, N, L, K)
+    out = torch.full((N, K), float("nan"), dtype=torch.float64, device="cuda")
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.graph(graph, stream=side):
+        B.check(lib.vp_loglik_packed2_noalloc(g.data_ptr(), N, L, f.data_ptr(), K, out.data_ptr(),
+                                              C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    for _ in range(2):
+        out.fill_(float("nan"))
+        graph.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), want)
+
+
 def test_noalloc_rejects_oversized_problems():
     import torch
     N, L, K = 20000, 400000, 12  # table + partial sums far beyond the fixed array

@@ -104,7 +104,7 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout", "vp_write_structure",
            "vp_cohort_open", "vp_cohort_set", "vp_cohort_run", "vp_cohort_sync", "vp_cohort_stream",
            "vp_cohort_launches", "vp_cohort_close", "vp_server_set_batching", "vp_server_stats",
-           "vp_vcf_parse"]
+           "vp_vcf_parse", "vp_tc_pipeline"]
 
 
 def lib():
@@ -146,6 +146,7 @@ def lib():
     L.vp_tune.argtypes = [C.POINTER(P), C.c_int32, C.c_int32, C.POINTER(VpTcConfig)]
     L.vp_tc_configure.argtypes = [C.POINTER(P), C.c_int32, C.POINTER(VpTcConfig)]
     L.vp_tc_config_get.argtypes = [C.POINTER(P), C.c_int32, C.POINTER(VpTcConfig)]
+    L.vp_tc_pipeline.argtypes = [P, C.c_int]
     L.vp_debug_gemm_bf16.argtypes = [P, P, P] + [C.c_int32] * 9 + [P]
     L.vp_debug_gemm_time.argtypes = [C.c_int32] * 13 + [P]
     L.vp_debug_gemm_e4m3.argtypes = [P, P] + [C.c_int32] * 7 + [P]

@@ -65,6 +65,15 @@ struct vp_ctx {
     // or contraction), captured into the graphs when enabled
     int prof = 0, prof_next = 0, prof_used = 0;
     std::vector<cudaEvent_t> prof_ev;
+    // tensor-core sweep by allele ranges: UpdateP of one range beside the
+    // likelihood contraction of the range before it, at most this many
+    // UpdateP blocks on an SM beside a contraction CTA (0, the default: one
+    // pass; vp_tc_pipeline)
+    int tc_pipeline = 0;
+    // branch streams and events of a captured sweep's fork and join
+    std::vector<cudaStream_t> fork;
+    std::vector<cudaEvent_t> fork_ev;
+    const void* last_gemm = nullptr;    // kernel of the latest contraction launch
 };
 
 struct vp_chain {
@@ -125,6 +134,11 @@ struct TcBatch {
     CUtensorMap mapC1, mapWhi, mapWlo, mapOH;
     cudaGraphExec_t graph = nullptr;
     int graph_nodes = 0;
+    const void* gemm1_fn = nullptr;     // the likelihood contraction's kernel in the captured sweep
+    // groups of consecutive chains for the label draw: {first chain, end
+    // chain, first row, rows}, and the most rows of a group
+    int4* sgrp = nullptr;
+    int nsgrp = 0, sgrp_rows = 0;
 };
 
 namespace {
@@ -580,6 +594,8 @@ extern "C" int vp_close(vp_ctx* x) {
     if (x->batch) { cudaGraphExecDestroy(x->batch->graph); dev_free(x->batch->mem, x->stream); delete x->batch; x->batch = nullptr; }
     if (x->pg) cudaGraphExecDestroy(x->pg);
     for (cudaEvent_t e : x->prof_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : x->fork_ev) cudaEventDestroy(e);
+    for (cudaStream_t f : x->fork) cudaStreamDestroy(f);
     for (void* p : x->allocs) dev_free(p, x->stream);
     if (x->stream) {
         cudaStreamSynchronize(x->stream);
@@ -710,7 +726,7 @@ int chain_plan(const vp_ctx* x, const vp_params* P, vp_chain* c, size_t* bytes) 
         return VP_E_ARG;
     }
     h.nlnlp = (int32_t)std::max<int64_t>(std::max<int64_t>(cdiv(L, 128), (int64_t)cdiv(N, ZA_WARPS * 32) * cdiv(L, h.zadm_lc)),
-                                         h.nsampblk);
+                                         std::max<int64_t>(h.nsampblk, cdiv(N, tc::TS_TILE)));
     c->plain_lazy = tc_batchable(x, P, h);
     Carve probe{nullptr};
     chain_layout(probe, c, x);
@@ -1472,6 +1488,7 @@ int launch_gemm_t(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const 
     if (first_on_device(mu, seen, x->device))
         CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     kern<<<grid, tc::NTHREADS, sm, x->stream>>>(A, B0, B1, g);
+    x->last_gemm = (const void*)kern;
     return check_launch(x, "k_gemm_bf16");
 }
 
@@ -1479,6 +1496,7 @@ int launch_gemm_t(vp_ctx* x, const CUtensorMap& A, const CUtensorMap& B0, const 
 // bytes, 128-row A tiles per CTA, B operands, columns per CTA, columns per MMA)
 #define VP_GEMM_TILES(X)             \
     X(64, 2, 2, 2, 192, 192)         \
+    X(64, 2, 2, 2, 144, 144)         \
     X(64, 2, 2, 1, 192, 192)         \
     X(128, 1, 2, 1, 192, 192)        \
     X(64, 2, 1, 2, 288, 144)         \
@@ -1563,8 +1581,14 @@ int tc_splits(int64_t tiles, int nsm) {
 // the likelihood-contraction tiles compiled in with two B operands (hi, lo):
 // bf16 K elements per stage, 128-row tiles per CTA, cluster rows per CTA and
 // per MMA
-const int kTiles1[][4] = {{64, 2, 192, 192}, {64, 1, 288, 144}, {32, 2, 192, 192}};
+const int kTiles1[][4] = {{64, 2, 192, 192}, {64, 2, 144, 144}, {64, 1, 288, 144}, {32, 2, 192, 192}};
 constexpr int kMaxStages = 6, kMaxSplits = 64;
+
+// cluster rows of a chain group of the label draw (a chain of more rows is
+// a group of its own: K <= 64 keeps the shared-memory sums of a tile of 32
+// individuals within 48 KB)
+constexpr int kSampleGroupRows = 160;
+
 
 int64_t gemm1_tiles(const vp_ctx* x, int Rpad, const TcChoice& c) {
     return cdiv(x->tc.Npad, 128 * c.mt1) * (int64_t)(Rpad / c.bn1);
@@ -1655,8 +1679,10 @@ void tune_store(const vp_ctx* x, int R, const TcChoice& c) {
 }
 
 // the likelihood contraction of the current batch under choice c
+// the likelihood contraction in `splits` split-K slices: all of them, or the
+// `nz` slices from slice z0 on
 int launch_gemm1(vp_ctx* x, const TcChoice& c, const CUtensorMap& A, const CUtensorMap& W0, const CUtensorMap& W1,
-                 int splits, float* out) {
+                 int splits, float* out, int z0 = 0, int nz = -1) {
     const TcOperands& t = x->tc;
     const TcBatch* b = x->batch;
     tc::GemmArgs g{};
@@ -1665,8 +1691,10 @@ int launch_gemm1(vp_ctx* x, const TcChoice& c, const CUtensorMap& A, const CUten
     g.BN = c.bn1; g.piece = c.piece1; g.nb = 2; g.mt = c.mt1; g.stages = c.st1; g.bk = c.bk1; g.esz = 2; g.mode = 0;
     g.group_major = c.gm1;
     g.out_f = out; g.ldo = b->Rpad; g.err = t.err;
+    g.z0 = z0;
+    const unsigned nzs = nz < 0 ? (unsigned)splits : (unsigned)nz;
     const unsigned mtiles = cdiv(t.Npad, 128 * c.mt1), groups = (unsigned)(b->Rpad / c.bn1);
-    return launch_gemm(x, A, W0, W1, g, c.gm1 ? dim3(groups, mtiles, splits) : dim3(mtiles, groups, splits));
+    return launch_gemm(x, A, W0, W1, g, c.gm1 ? dim3(groups, mtiles, nzs) : dim3(mtiles, groups, nzs));
 }
 
 // copies each batch chain's header to the chain's own device header
@@ -1724,6 +1752,17 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n, const TcChoice* force) {
         for (int k = 0; k < cs[i]->P.K; ++k) { rowchain.push_back(i); rowk.push_back(k); }
     }
     b->R = (int)rowchain.size();
+    // chain groups of the label draw: consecutive chains, at most
+    // kSampleGroupRows cluster rows unless one chain has more
+    std::vector<int4> sgrp;
+    for (int i = 0; i < n; ++i) {
+        const int K = cs[i]->P.K;
+        if (sgrp.empty() || sgrp.back().w + K > kSampleGroupRows) sgrp.push_back(make_int4(i, i, row0[i], 0));
+        sgrp.back().y = i + 1;
+        sgrp.back().w += K;
+    }
+    b->nsgrp = (int)sgrp.size();
+    for (const int4& gr : sgrp) b->sgrp_rows = std::max(b->sgrp_rows, gr.w);
     b->G = (b->R + b->BN - 1) / b->BN;
     b->Rpad = b->G * b->BN;
     const TcOperands& t = x->tc;
@@ -1745,6 +1784,7 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n, const TcChoice* force) {
         b->rowchain = cv.take<int32_t>(b->R);
         b->rowk = cv.take<int32_t>(b->R);
         b->row0 = cv.take<int32_t>(n);
+        b->sgrp = cv.take<int4>(b->nsgrp);
         b->Whi = cv.take<__nv_bfloat16>((int64_t)b->Rpad * t.Apad);
         b->Wlo = cv.take<__nv_bfloat16>((int64_t)b->Rpad * t.Apad);
         b->OH = cv.take<uint8_t>((int64_t)b->Rpad * t.Npad);
@@ -1768,7 +1808,8 @@ int make_batch(vp_ctx* x, vp_chain** cs, int n, const TcChoice* force) {
     if ((e = cudaMemsetAsync(b->mem, 0, probe.off, x->stream)) != cudaSuccess ||
         (e = cudaMemcpyAsync(b->rowchain, rowchain.data(), rowchain.size() * 4, cudaMemcpyHostToDevice, x->stream)) != cudaSuccess ||
         (e = cudaMemcpyAsync(b->rowk, rowk.data(), rowk.size() * 4, cudaMemcpyHostToDevice, x->stream)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(b->row0, row0.data(), row0.size() * 4, cudaMemcpyHostToDevice, x->stream)) != cudaSuccess)
+        (e = cudaMemcpyAsync(b->row0, row0.data(), row0.size() * 4, cudaMemcpyHostToDevice, x->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b->sgrp, sgrp.data(), sgrp.size() * sizeof(int4), cudaMemcpyHostToDevice, x->stream)) != cudaSuccess)
         return undo("batch upload", e);
     // the batch's count contraction writes every chain's Ni inside NiAll
     // (counts still pending are computed there below); the chains' device
@@ -1822,51 +1863,184 @@ tc::BatchDev batch_dev(vp_ctx* x) {
     d.R = b->R; d.Rpad = b->Rpad; d.nchains = (int)b->chains.size(); d.splits = b->splits;
     d.Apad = x->tc.Apad; d.Npad = x->tc.Npad; d.Whi = b->Whi; d.Wlo = b->Wlo; d.OH = b->OH;
     d.logpbar = x->tc.logpbar; d.Bc = x->tc.Bc; d.LLpart = b->LLpart;
+    d.sgrp = b->sgrp; d.sgrp_ld = b->sgrp_rows | 1;
     return d;
+}
+
+// UpdateP blocks along the loci for `nloci` loci of R rows: between 2 and
+// 16 (at most one block per 256 loci), chosen so that the blocks fill whole
+// waves of the kernel's resident blocks
+unsigned updatep_blocks(const vp_ctx* x, int64_t nloci, int R) {
+    static const int per_sm = [] {
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, tc::k_update_p_tc, 256, 0) != cudaSuccess || v < 1) v = 4;
+        return v;
+    }();
+    const double slots = (double)x->nsm * std::max(1, per_sm);
+    const unsigned hi = std::max<unsigned>(1, std::min<unsigned>(16, cdiv(nloci, 256)));
+    unsigned upx = 1;
+    double best = -1;
+    for (unsigned u = std::min(2u, hi); u <= hi; ++u) {
+        const double w = (double)u * R / slots, eff = w / std::ceil(w);
+        if (eff > best + 0.01) { best = eff; upx = u; }
+    }
+    return upx;
+}
+
+// branch streams and events for a sweep's fork and join
+int fork_resources(vp_ctx* x, int nstreams, int nevents) {
+    while ((int)x->fork.size() < nstreams) {
+        cudaStream_t f;
+        CK(cudaStreamCreateWithFlags(&f, cudaStreamNonBlocking));
+        x->fork.push_back(f);
+    }
+    while ((int)x->fork_ev.size() < nevents) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        x->fork_ev.push_back(e);
+    }
+    return VP_OK;
+}
+
+// dynamic shared memory of an UpdateP block that lets at most `share` of
+// them sit on an SM beside one CTA of the likelihood contraction (the
+// contraction's issuing warps then share their schedulers with fewer ALU
+// warps); 0 when the contraction leaves no room to divide
+size_t updatep_share_smem(const vp_ctx* x, int share) {
+    const TcChoice& c = x->batch->cfg;
+    size_t g = tc::gemm_smem_bytes(c.bn1, 2, c.st1, c.mt1, c.bk1, 2);
+    if (c.mt1 * c.bn1 > 256) g = std::max<size_t>(g, 115 * 1024);     // launch_gemm's TMEM rule
+    int per_sm = 0, reserved = 0;
+    if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, x->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, x->device) != cudaSuccess)
+        return 0;
+    const int64_t room = (int64_t)per_sm - (int64_t)g - reserved;
+    if (room <= 0) return 0;
+    // a slot inside (room / (share + 1), room / share]: `share` slots fit, one more does not
+    const int64_t slot = (room / (share + 1) + room / share) / 2;
+    return (size_t)std::max<int64_t>(0, slot - reserved);
+}
+
+// launches go to another stream while in scope
+struct OnStream {
+    vp_ctx* x;
+    cudaStream_t saved;
+    OnStream(vp_ctx* x_, cudaStream_t f) : x(x_), saved(x_->stream) { x->stream = f; }
+    ~OnStream() { x->stream = saved; }
+};
+
+// split-K slices of the likelihood contraction that run as separate ranges
+int pipeline_ranges(const vp_ctx* x) {
+    const TcBatch* b = x->batch;
+    return x->tc_pipeline && b->splits > 1 ? b->splits : 1;
 }
 
 int launch_tc_sweep(vp_ctx* x) {
     TcBatch* b = x->batch;
-    const TcOperands& t = x->tc;
     const int n = (int)b->chains.size();
     tc::BatchDev bd = batch_dev(x);
     cudaStream_t s = x->stream;
-    // UpdateP for all chains, with the split-bf16 centred log-frequency rows:
-    // R rows x upx blocks, each thread walking many loci; upx between 2 and 16
-    // (at most one block per 256 loci) chosen so that the blocks fill whole
-    // waves of the kernel's resident blocks
-    unsigned upx = 1;
-    {
-        static const int per_sm = [] {
-            int v = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, tc::k_update_p_tc, 256, 0) != cudaSuccess || v < 1) v = 4;
-            return v;
-        }();
-        const double slots = (double)x->nsm * std::max(1, per_sm);
-        const unsigned hi = std::max<unsigned>(1, std::min<unsigned>(16, cdiv(x->L, 256)));
-        double best = -1;
-        for (unsigned u = std::min(2u, hi); u <= hi; ++u) {
-            const double w = (double)u * b->R / slots, eff = w / std::ceil(w);
-            if (eff > best + 0.01) { best = eff; upx = u; }
-        }
-    }
-    prof_mark(x, true, PROF_UPDATEP_TC);
-    LAUNCH(x, tc::k_update_p_tc, (dim3(upx, b->R, 1), 256, 0, s), (bd));
-    prof_mark(x, false, PROF_UPDATEP_TC);
-    // likelihood contraction: LL'[i, row] = sum_a C[i,a] (Whi + Wlo)[row, a]
-    {
+    const int nr = pipeline_ranges(x);
+    if (nr == 1) {
+        // UpdateP for all chains, with the split-bf16 centred log-frequency
+        // rows (R rows x upx blocks, each thread walking many loci), then
+        // the likelihood contraction
+        const unsigned upx = updatep_blocks(x, x->L, b->R);
+        prof_mark(x, true, PROF_UPDATEP_TC);
+        LAUNCH(x, tc::k_update_p_tc, (dim3(upx, b->R, 1), 256, 0, s), (bd, (int64_t)0, x->L));
+        prof_mark(x, false, PROF_UPDATEP_TC);
         prof_mark(x, true);
         int rc = launch_gemm1(x, b->cfg, b->mapC1, b->mapWhi, b->mapWlo, b->splits, b->LLpart);
         prof_mark(x, false);
         if (rc) return rc;
+        b->gemm1_fn = x->last_gemm;
+    } else {
+        // by allele ranges, one per split-K slice of the likelihood
+        // contraction: UpdateP of the ranges one after another on one
+        // branch, each range's slice on a branch of its own once the range's
+        // draws are written. The slices (tensor pipes, one CTA per SM) and
+        // the next range's draws (ALUs, in the registers the contraction
+        // leaves) share the SMs; the slices take precedence (graph node
+        // priority). The slices write disjoint split-K partials, so the
+        // labels are those of the single-launch order.
+        const int ng = std::min(nr, 8);
+        if (int rc = fork_resources(x, 1 + ng, 2 * nr + 3)) return rc;
+        const size_t psm = updatep_share_smem(x, x->tc_pipeline);
+        {
+            static std::mutex mu;
+            static std::vector<char> seen;
+            if (first_on_device(mu, seen, x->device))
+                CK(cudaFuncSetAttribute(tc::k_update_p_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        }
+        cudaEvent_t* ev = x->fork_ev.data();
+        cudaStream_t ps = x->fork[0];
+        CK(cudaEventRecord(ev[0], s));
+        CK(cudaStreamWaitEvent(ps, ev[0], 0));
+        const int64_t kbps = cdiv(x->tc.Apad / b->cfg.bk1, b->splits);
+        const int64_t loci = kbps * b->cfg.bk1 / 2;          // biallelic: two allele columns per locus
+        for (int r = 0; r < nr; ++r) {
+            const int64_t l0 = r * loci, l1 = std::min<int64_t>(x->L, l0 + loci);
+            {
+                OnStream on(x, ps);
+                if (r == 0) prof_mark(x, true, PROF_UPDATEP_TC);
+                if (l1 > l0) {
+                    // the first range runs alone: no cap
+                    const unsigned upx = updatep_blocks(x, l1 - l0, b->R);
+                    LAUNCH(x, tc::k_update_p_tc, (dim3(upx, b->R, 1), 256, r ? psm : 0, ps), (bd, l0, l1));
+                }
+                if (r == nr - 1) prof_mark(x, false, PROF_UPDATEP_TC);
+                CK(cudaEventRecord(ev[1 + r], ps));
+            }
+            cudaStream_t gs = x->fork[1 + r % ng];
+            CK(cudaStreamWaitEvent(gs, ev[1 + r], 0));
+            {
+                OnStream on(x, gs);
+                if (r == 0) prof_mark(x, true);
+                int rc = launch_gemm1(x, b->cfg, b->mapC1, b->mapWhi, b->mapWlo, b->splits, b->LLpart, r, 1);
+                if (rc) return rc;
+                CK(cudaEventRecord(ev[1 + nr + r], gs));
+            }
+        }
+        b->gemm1_fn = x->last_gemm;
+        for (int r = 0; r < nr; ++r) CK(cudaStreamWaitEvent(s, ev[1 + nr + r], 0));
+        CK(cudaEventRecord(ev[1 + 2 * nr], ps));        // the UpdateP branch rejoins too
+        CK(cudaStreamWaitEvent(s, ev[1 + 2 * nr], 0));
+        prof_mark(x, false);
     }
     // labels of every chain, one-hot rows for the count contraction
-    LAUNCH(x, tc::k_sample_tc, (dim3(cdiv(x->N, SAMPLE_BLOCK), n, 1), SAMPLE_BLOCK, 0, s), (bd));
+    const size_t tsm = (size_t)tc::TS_TILE * (b->sgrp_rows | 1) * sizeof(float);
+    LAUNCH(x, tc::k_sample_tc_tiles, (dim3(cdiv(x->N, tc::TS_TILE), b->nsgrp, 1), tc::TS_THREADS, tsm, s), (bd));
     // count contraction: Ni[row, a] = sum_i OH[row, i] C[i, a]
     if (int rc = launch_counts_gemm(x)) return rc;
     // Record for every chain, then m += 1
     unsigned ga = std::min<unsigned>(128, cdiv((int64_t)16 * x->KT, 256));
     LAUNCH(x, k_record_sweep, (dim3(ga, 1, n), 256, 0, s), (b->dchains, b->lnlrec));
+    return VP_OK;
+}
+
+// graph node priorities of a captured sweep: the likelihood contraction's
+// slices one level above the rest, which keep the context stream's priority
+int set_node_priorities(vp_ctx* x, cudaGraph_t g, const void* hi_fn) {
+    int least = 0, greatest = 0, base = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamGetPriority(x->stream, &base));
+    int hi = base, lo = base;
+    if (base > greatest) hi = base - 1;        // numerically lower is more urgent
+    else if (base < least) lo = base + 1;
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CK(cudaGraphGetNodes(g, nodes.data(), &nn));
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType ty;
+        CK(cudaGraphNodeGetType(nd, &ty));
+        if (ty != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp{};
+        CK(cudaGraphKernelNodeGetParams(nd, &kp));
+        cudaLaunchAttributeValue v{};
+        v.priority = kp.func == hi_fn ? hi : lo;
+        CK(cudaGraphKernelNodeSetAttribute(nd, cudaLaunchAttributePriority, &v));
+    }
     return VP_OK;
 }
 
@@ -1903,7 +2077,9 @@ int run_tc(vp_ctx* x, vp_chain** cs, int n, int nsweeps) {
         if (e != cudaSuccess) { vp_set_error("graph capture failed: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
         b->graph_nodes = (int)(x->launches - before);
         x->launches = before;
-        e = cudaGraphInstantiate(&b->graph, g, 0);
+        const bool forked = pipeline_ranges(x) > 1;
+        if (forked && (rc = set_node_priorities(x, g, b->gemm1_fn))) { cudaGraphDestroy(g); return rc; }
+        e = cudaGraphInstantiate(&b->graph, g, forked ? cudaGraphInstantiateFlagUseNodePriority : 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) { vp_set_error("graph instantiate failed: %s", cudaGetErrorString(e)); return VP_E_CUDA; }
     }
@@ -2399,6 +2575,18 @@ extern "C" int vp_prof_enable(vp_ctx* x, int on) {
     x->prof = on;
     // cached graphs were captured with or without the markers: re-capture
     if (x->pg) { cudaGraphExecDestroy(x->pg); x->pg = nullptr; x->pg_chains.clear(); }
+    if (x->batch && x->batch->graph) { cudaGraphExecDestroy(x->batch->graph); x->batch->graph = nullptr; }
+    return VP_OK;
+}
+
+extern "C" int vp_tc_pipeline(vp_ctx* x, int on) {
+    if (!x) { vp_set_error("null context"); return VP_E_ARG; }
+    if (on < 0 || on > 8) { vp_set_error("pipeline share %d: 0 (one pass) to 8", on); return VP_E_ARG; }
+    if (x->tc_pipeline == on) return VP_OK;
+    cudaSetDevice(x->device);
+    CK(cudaStreamSynchronize(x->stream));
+    x->tc_pipeline = on;
+    // the cached sweep graph has the other shape: re-capture
     if (x->batch && x->batch->graph) { cudaGraphExecDestroy(x->batch->graph); x->batch->graph = nullptr; }
     return VP_OK;
 }

@@ -32,6 +32,7 @@ struct GemmArgs {
     int M, N;               // rows of A / D, columns of D (= rows of B)
     int kblocks;            // K / bk of the whole problem
     int kb_per_split;       // k-blocks handled by one CTA (grid.z splits K)
+    int z0;                 // split index of grid.z = 0 (a launch of some of the splits)
     int BN;                 // columns per CTA (multiple of 16, <= 512)
     int piece;              // columns per MMA instruction (<= 256, multiple of 16)
     int nb;                 // 1 or 2 B operands
@@ -161,7 +162,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
     const int m0 = (g.group_major ? blockIdx.y : blockIdx.x) * BM * MT;
     const int n0 = (g.group_major ? blockIdx.x : blockIdx.y) * BNT;
-    const int kb0 = blockIdx.z * g.kb_per_split;
+    const int split = blockIdx.z + g.z0;
+    const int kb0 = split * g.kb_per_split;
     const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
     const int nk = kb1 - kb0;
 
@@ -267,7 +269,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (!valid) continue;
                 if (g.mode == 0) {
                     if (row < g.M) {
-                        float* o = g.out_f + ((int64_t)blockIdx.z * g.M + row) * g.ldo + n0 + c0;
+                        float* o = g.out_f + ((int64_t)split * g.M + row) * g.ldo + n0 + c0;
 #pragma unroll
                         for (int j = 0; j < 16; ++j)
                             if (n0 + c0 + j < g.N) o[j] = v[j];
@@ -471,6 +473,8 @@ struct BatchDev {
     const float* logpbar;
     const double* Bc;
     const float* LLpart;      // [splits][N][Rpad]
+    const int4* sgrp;         // chain groups of the label draw: {first chain, end chain, first row, rows}
+    int sgrp_ld;              // shared-memory words per individual of a group's row sums
 };
 
 // UpdateP for every chain of the batch (counter streams, the same Philox
@@ -478,8 +482,11 @@ struct BatchDev {
 // Freq and, centred and split into bf16 hi + lo, to the rows of W.
 // grid.y = cluster row; a thread walks loci with a stride of the grid's
 // width, so the chain's parameters are fetched once per thread, not per locus.
-// Biallelic data: allele offsets are 2l.
-__global__ void __launch_bounds__(256) k_update_p_tc(BatchDev b) {
+// Biallelic data: allele offsets are 2l. Loci [l0, l1): the sweep runs the
+// step over allele ranges, each range's draws ahead of that range's slice of
+// the likelihood contraction; every locus draws from its own counter, so the
+// ranges give the values of one launch over all loci.
+__global__ void __launch_bounds__(256) k_update_p_tc(BatchDev b, int64_t l0, int64_t l1) {
     const int r = blockIdx.y;
     const DevChain& c = b.chains[b.rowchain[r]];
     const int64_t L = c.D.L;
@@ -493,7 +500,8 @@ __global__ void __launch_bounds__(256) k_update_p_tc(BatchDev b) {
     const float2* lpb = reinterpret_cast<const float2*>(b.logpbar);
     const int2* Ni2 = reinterpret_cast<const int2*>(Ni);
     float2* F2 = reinterpret_cast<float2*>(Freq);
-    for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < L; l += (int64_t)gridDim.x * blockDim.x) {
+    l1 = min(l1, L);
+    for (int64_t l = l0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < l1; l += (int64_t)gridDim.x * blockDim.x) {
         const int64_t kl = (int64_t)k * L + l;
         Philox ph;
         ph.init(seed, ST_P | ((uint32_t)m << 4), (uint32_t)kl, (uint32_t)(kl >> 32));
@@ -520,26 +528,26 @@ __global__ void k_onehot_from_z(BatchDev b) {
     for (int k = 0; k < c.K; ++k) b.OH[(int64_t)(r0 + k) * b.Npad + i] = k == z ? E4M3_ONE : 0;
 }
 
-// One (chain, individual). The split-K partials sum, in FP32, to the centred
-// log-likelihood; the individual's constant B_i cancels from the label
-// weights exp(LL_k - max), so the draw runs in FP32 on the centred sums (the
-// GEMM accumulated them in FP32; a float uniform) and only LL itself, B_i +
-// the centred sum, is formed in FP64. K <= KM with the values in registers;
-// larger K goes through a separate (not inlined) copy with local arrays, so
-// it does not raise the kernel's registers.
+// One (chain, individual). The split-K partials sum (`sums`, the chain's K
+// values), in FP32, to the centred log-likelihood; the individual's constant
+// B_i cancels from the label weights exp(LL_k - max), so the draw runs in
+// FP32 on the centred sums (the GEMM accumulated them in FP32; a float
+// uniform) and only LL itself, B_i + the centred sum, is formed in FP64.
+// K <= KM with the values in registers; larger K goes through a separate
+// (not inlined) copy with local arrays, so it does not raise the kernel's
+// registers.
 template <int KM, bool WIDE>
-__device__ __forceinline__ double sample_tc_body(const BatchDev& b, const DevChain& c, int i, int m, int r0) {
+__device__ __forceinline__ double sample_tc_body(const BatchDev& b, const DevChain& c, int i, int m, int r0,
+                                                 const float* sums) {
     const DevData& D = c.D;
-    const int K = c.K, N = D.N;
+    const int K = c.K;
     constexpr int UNR = WIDE ? 1 : KM;   // the wide copy keeps its loops rolled (arrays in local memory)
     float sf[KM];
     const double bc = b.Bc[i];
 #pragma unroll UNR
     for (int k = 0; k < KM; ++k) {
         if (k >= K) break;
-        float v = 0.f;
-#pragma unroll 4
-        for (int s = 0; s < b.splits; ++s) v += b.LLpart[((int64_t)s * N + i) * b.Rpad + r0 + k];
+        const float v = sums[k];
         sf[k] = v;
         c.LL[(int64_t)i * K + k] = bc + (double)v;
     }
@@ -585,28 +593,73 @@ __device__ __forceinline__ double sample_tc_body(const BatchDev& b, const DevCha
     return lnl;
 }
 
-__device__ __noinline__ double sample_tc_wide(const BatchDev& b, const DevChain& c, int i, int m, int r0) {
-    return sample_tc_body<64, true>(b, c, i, m, r0);
+__device__ __noinline__ double sample_tc_wide(const BatchDev& b, const DevChain& c, int i, int m, int r0,
+                                              const float* sums) {
+    return sample_tc_body<64, true>(b, c, i, m, r0, sums);
 }
 
-// label draw for every (chain, individual) from the tensor-core likelihoods;
-// also writes the one-hot label rows OH that the count contraction reads
-__global__ void __launch_bounds__(SAMPLE_BLOCK) k_sample_tc(BatchDev b) {
-    const int ci = blockIdx.y;
-    const DevChain& c = b.chains[ci];
-    const int K = c.K, N = c.D.N, m = c.ctl->m;
-    const int r0 = b.row0[ci];
-    __shared__ double sh[32];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double lnl = 0;
-    if (i < N) lnl = K <= 16 ? sample_tc_body<16, false>(b, c, i, m, r0) : sample_tc_wide(b, c, i, m, r0);
-    double t = block_sum(lnl, sh);
-    if (threadIdx.x == 0) c.lnlp[blockIdx.x] = t;
-    if (!last_block_done(c.ctl, gridDim.x)) return;
-    const double tot = block_sum_partials(c.lnlp, gridDim.x, sh);
-    if (threadIdx.x == 0) {
-        c.ctl->lnl = tot;
-        c.ctl->done = 0;
+// Label draw for every (chain, individual) from the tensor-core likelihoods;
+// also writes the one-hot label rows OH that the count contraction reads.
+// A block takes TS_TILE individuals and one group of consecutive chains (grid.y; at most a few hundred cluster rows), so a
+// c3 batch of 10,000 individuals and 100 chains runs about 1,250 blocks.
+// The split-K partials of the group's rows are read as row segments
+// (consecutive threads, consecutive rows; two in flight per thread) and
+// summed in split order into shared memory, [individual][sgrp_ld] words (an
+// odd stride: no bank conflicts); then warp w draws the labels of the
+// group's chains w, w + 8, ... with lane = individual. Each chain's lnL
+// partial of the tile goes to lnlp[tile]; the warp that writes a chain's
+// last partial folds that chain's partials.
+constexpr int TS_TILE = 32, TS_THREADS = 256;
+__global__ void __launch_bounds__(TS_THREADS) k_sample_tc_tiles(BatchDev b) {
+    extern __shared__ float rs[];
+    const int4 gr = b.sgrp[blockIdx.y];
+    const int N = b.chains[0].D.N;
+    const int i0 = blockIdx.x * TS_TILE, ni = min(TS_TILE, N - i0);
+    const int nr = gr.w, ld = b.sgrp_ld, tot = ni * nr;
+    const int64_t plane = (int64_t)N * b.Rpad;
+    const float* base = b.LLpart + (int64_t)i0 * b.Rpad + gr.z;
+    for (int j = threadIdx.x; j < tot; j += 2 * TS_THREADS) {
+        const int j2 = min(j + TS_THREADS, tot - 1);    // the last element again when past the end
+        const int ia = j / nr, ra = j - ia * nr, ib = j2 / nr, rb = j2 - ib * nr;
+        const float* pa = base + (int64_t)ia * b.Rpad + ra;
+        const float* pb = base + (int64_t)ib * b.Rpad + rb;
+        float va = 0.f, vb = 0.f;
+#pragma unroll 4
+        for (int s = 0; s < b.splits; ++s) {
+            va += pa[s * plane];
+            vb += pb[s * plane];
+        }
+        rs[ia * ld + ra] = va;
+        rs[ib * ld + rb] = vb;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int ci = gr.x + warp; ci < gr.y; ci += TS_THREADS / 32) {
+        const DevChain& c = b.chains[ci];
+        const int r0 = b.row0[ci], m = c.ctl->m;
+        double lnl = 0;
+        if (lane < ni) {
+            const float* sums = rs + lane * ld + (r0 - gr.z);
+            lnl = c.K <= 16 ? sample_tc_body<16, false>(b, c, i0 + lane, m, r0, sums)
+                            : sample_tc_wide(b, c, i0 + lane, m, r0, sums);
+        }
+        for (int o = 16; o > 0; o >>= 1) lnl += __shfl_xor_sync(0xffffffffu, lnl, o);
+        int last = 0;
+        if (lane == 0) {
+            c.lnlp[blockIdx.x] = lnl;
+            __threadfence();
+            last = atomicAdd(&c.ctl->done, 1) == (int)gridDim.x - 1;
+        }
+        if (__shfl_sync(0xffffffffu, last, 0)) {
+            __threadfence();
+            double t = 0;
+            for (int j = lane; j < (int)gridDim.x; j += 32) t += __ldcg(c.lnlp + j);
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) {
+                c.ctl->lnl = t;
+                c.ctl->done = 0;
+            }
+        }
     }
 }
 

@@ -135,6 +135,13 @@ class Context:
     def launches(self) -> int:
         return int(B.lib().vp_launch_count(self.h))
 
+    def tc_pipeline(self, share: int) -> None:
+        """Tensor-core sweeps by allele ranges, UpdateP of one range beside
+        the likelihood contraction of the range before it with at most
+        `share` UpdateP blocks beside a contraction CTA (1-8), or in one pass
+        (0)."""
+        B.check(B.lib().vp_tc_pipeline(self.h, int(share)))
+
     def close(self):
         if getattr(self, "h", None):
             B.lib().vp_close(self.h)
