@@ -52,6 +52,17 @@ typedef struct {
     const int32_t* n_alleles; /* [L] alleles per locus (REF + ALTs) */
     const int32_t* popid;   /* [N] population index, individuals grouped by population */
     int32_t n_pop;          /* S */
+    /* optional, per input locus: the facts of the loader's genotype table,
+     * which registers every call of a line before the genotype filter
+     * (-f_dp, -f_gq, -f_ploidy) turns calls into missing ones
+     * (src/load.cpp:2145-2230 and 3545-3566): whether the locus is
+     * polymorphic (a genotype with two alleles, or two different ones:
+     * ApplyFilter, src/filter.cpp:102-133) and how many genotype ids it has
+     * (their bit width orders the loci, src/structure.cpp:2202-2295). From
+     * vp_genotype_table on the calls before that filter; NULL: taken from
+     * the calls above. */
+    const uint8_t* table_poly;
+    const int32_t* table_ngeno;
 } vp_input;
 
 typedef struct vp_dataset vp_dataset;
@@ -61,6 +72,10 @@ typedef struct vp_dataset vp_dataset;
  * bit width (src/structure.cpp:2202-2295), allele offsets (2374-2381).
  * Host-only; no GPU needed. */
 int vp_dataset_prepare(const vp_input* in, vp_dataset** out);
+/* The genotype-table facts of each input locus of `in` (its calls, packed2 or
+ * alleles): poly[n_loc] and ngeno[n_loc] as vp_input.table_poly and
+ * table_ngeno take them. Host-only. */
+int vp_genotype_table(const vp_input* in, uint8_t* poly, int32_t* ngeno);
 
 typedef struct {
     int32_t n_ind, n_pop, maxploidy, max_alleles, packed2;
@@ -359,6 +374,29 @@ int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int device, uint
  * VP_E_ARG naming the line. With max_loci == 0 it only counts the lines. */
 int vp_vcf_parse(const char* text, size_t bytes, int32_t n_ind, int32_t vmax, int device, int8_t* alleles,
                  int32_t* n_alleles, int32_t* ploidy, int64_t max_loci, int64_t* line_start, int64_t* n_loc);
+
+/* The reference's genotype filter (-f with -f_dp, -f_gq, -f_ploidy;
+ * AddVCFGenotype, src/load.cpp:3545-3566, flags src/parameters.cpp:743-748):
+ * a typed call becomes missing when its number of copies is outside
+ * [ploidy_min, ploidy_max], or when the FORMAT column has a DP (GQ) key, the
+ * call has at least that many keys, and its value read as the reference's
+ * ReadIntegerKeep reads it (characters up to the first digit or '-' are
+ * skipped, so a '.' value takes the next number on the line; here the scan
+ * stops at the end of the line, with 0) is outside the window: DP compared as
+ * unsigned (-1 never filters), GQ as signed (-1 never filters). FORMAT keys
+ * are matched ignoring case. A window is used when its flag is non-zero. */
+typedef struct {
+    int32_t dp_b, dp_min, dp_max;
+    int32_t gq_b, gq_min, gq_max;
+    int32_t ploidy_b, ploidy_min, ploidy_max;
+} vp_call_filter;
+/* vp_vcf_pack2 and vp_vcf_parse with the genotype filter applied to every
+ * call as it is decoded (cf may be null: no filter). */
+int vp_vcf_pack2_ex(const char* text, size_t bytes, int32_t n_ind, int device, uint32_t* packed, int64_t max_loci,
+                    int64_t* line_start, int64_t* n_loc, const vp_call_filter* cf);
+int vp_vcf_parse_ex(const char* text, size_t bytes, int32_t n_ind, int32_t vmax, int device, int8_t* alleles,
+                    int32_t* n_alleles, int32_t* ploidy, int64_t max_loci, int64_t* line_start, int64_t* n_loc,
+                    const vp_call_filter* cf);
 
 /* Locus filter of the reference (-f_bmaf, -f_k, -f_n, -f_ptype, -f_he, -f_ho,
  * -f_pic, -f_ae, -f_I, -f_pval: MarkerDiversity, src/filter.cpp:485-507, on the

@@ -20,9 +20,10 @@ static int yesno(const char* v) { return strcmp(v, "yes") == 0 ? 1 : 0; }
 
 typedef struct { char** names; int n; } strlist;
 
-/* Read a plain VCF: sample names, per-locus allele counts and GT calls. */
+/* Read a plain VCF: sample names, per-locus allele counts and GT calls; a
+ * typed call that fails the genotype filter (cf, may be null) is missing. */
 static int read_vcf(const char* path, int* N, int64_t* L, int* vmax, int8_t** G, int32_t** ploidy,
-                    int32_t** k, strlist* inds, strlist* locs) {
+                    int32_t** k, strlist* inds, strlist* locs, const orc_call_filter* cf) {
     FILE* f = fopen(path, "r");
     if (!f) return -1;
     size_t cap = 1 << 20;
@@ -47,8 +48,22 @@ static int read_vcf(const char* path, int* N, int64_t* L, int* vmax, int8_t** G,
             continue;
         }
         if (nl == lcap) { lcap *= 2; kk = realloc(kk, lcap * sizeof(int32_t)); lnames = realloc(lnames, lcap * sizeof(char*)); }
+        /* the calls of the line, kept whole (with their keys) for the filter */
+        const int filter = cf && (cf->dp_b || cf->gq_b || cf->ploidy_b);
+        char* calls = NULL;
         char* fields[10]; char* p = line;
         for (int c = 0; c < 9; ++c) { fields[c] = p; p = strchr(p, '\t'); *p++ = 0; }
+        /* the loader's rewritten calls (orc_rewrite_calls) for the filter */
+        int dpid = -1, gqid = -1;
+        size_t* call_at = NULL;
+        size_t rw_len = 0;
+        if (filter) {
+            const size_t plen = strlen(p);
+            calls = malloc(plen + 1);
+            call_at = malloc(sizeof(size_t) * (size_t)n);
+            rw_len = orc_rewrite_calls(fields[8], fields[8] + strlen(fields[8]), p, p + plen, n, calls, call_at,
+                                       &dpid, &gqid);
+        }
         int nalt = 1;
         for (char* q = fields[4]; *q; ++q) if (*q == ',') nalt++;
         kk[nl] = 1 + nalt;
@@ -81,6 +96,8 @@ static int read_vcf(const char* path, int* N, int64_t* L, int* vmax, int8_t** G,
             while (*q && *q != '\t') q++;
             if (*q) q++;
             for (int c = 0; c < vm; ++c) row[i * vm + c] = -1;
+            if (!miss && filter && orc_call_filtered(calls + call_at[i], rw_len - call_at[i], dpid, gqid, v, cf))
+                miss = 1;
             if (!miss) {
                 for (int a = 0; a < v; ++a)
                     for (int b = a + 1; b < v; ++b)
@@ -88,6 +105,8 @@ static int read_vcf(const char* path, int* N, int64_t* L, int* vmax, int8_t** G,
                 for (int c = 0; c < v; ++c) row[i * vm + c] = al[c];
             }
         }
+        free(calls);
+        free(call_at);
         nl++;
     }
     free(line);
@@ -132,7 +151,9 @@ int main(int argc, char** argv) {
     P.uniformalpha = 1; P.alphapriora = 0.05; P.alphapriorb = 0.001; P.metrofreq = 10;
     P.r = 1; P.maxr = 20; P.epsr = 0.1; P.epseta = 0.025; P.epsgamma = 0.025;
     P.pmeanf = 0.01; P.pstdf = 0.05; P.stdf = 0.05; P.fsame = 0;
-    int diversity = 0;
+    int diversity = 0, ffilter = 0;
+    orc_call_filter cf;
+    memset(&cf, 0, sizeof cf);
     for (int i = 1; i < argc; ++i) {
         char* a = argv[i];
         char* eq = strchr(a, '=');
@@ -174,15 +195,29 @@ int main(int argc, char** argv) {
         else if (IS("-structure_pstdf")) P.pstdf = atof(v);
         else if (IS("-structure_stdf")) P.stdf = atof(v);
         else if (IS("-structure_singlef")) P.fsame = yesno(v);
+        else if (IS("-f")) ffilter = 1;
+        else if (IS("-f_dp")) cf.dp_b = sscanf(v, "[%d,%d]", &cf.dp_min, &cf.dp_max) == 2;
+        else if (IS("-f_gq")) cf.gq_b = sscanf(v, "[%d,%d]", &cf.gq_min, &cf.gq_max) == 2;
+        else if (IS("-f_ploidy")) cf.ploidy_b = sscanf(v, "[%d,%d]", &cf.ploidy_min, &cf.ploidy_max) == 2;
 #undef IS
     }
     if (!g_input) { fprintf(stderr, "missing -g_input\n"); return 2; }
     int N, vmax; int64_t L; int8_t* G; int32_t *ploidy, *k;
     strlist inds, locs, pops;
-    if (read_vcf(g_input, &N, &L, &vmax, &G, &ploidy, &k, &inds, &locs)) { fprintf(stderr, "cannot read %s\n", g_input); return 2; }
+    /* the genotype filter applies only under -f (parameters.cpp:1338-1339) */
+    if (read_vcf(g_input, &N, &L, &vmax, &G, &ploidy, &k, &inds, &locs, ffilter ? &cf : NULL)) { fprintf(stderr, "cannot read %s\n", g_input); return 2; }
+    /* with the genotype filter, the calls before it (the loader's genotype
+     * table, load.cpp:2145-2230) decide the polymorphic loci and their order */
+    int8_t* Gt = NULL;
+    if (ffilter && (cf.dp_b || cf.gq_b || cf.ploidy_b)) {
+        int N2, vmax2; int64_t L2; int32_t *ploidy2, *k2;
+        strlist inds2, locs2;
+        if (read_vcf(g_input, &N2, &L2, &vmax2, &Gt, &ploidy2, &k2, &inds2, &locs2, NULL) || N2 != N || L2 != L ||
+            vmax2 != vmax) { fprintf(stderr, "cannot read %s\n", g_input); return 2; }
+    }
     int32_t* popid = malloc(sizeof(int32_t) * N);
     parse_indtext(g_indtext, N, popid, &pops);
-    orc_owned_data* od = orc_data_build(N, L, vmax, G, ploidy, k, popid, pops.n);
+    orc_owned_data* od = orc_data_build_ex(N, L, vmax, G, ploidy, k, popid, pops.n, Gt);
     const orc_data* D = orc_data_view(od);
     const int64_t* order = orc_data_order(od);
     /* order[] has one entry per locus kept by the monomorphic filter:

@@ -50,9 +50,18 @@ static int cmp_u64(const void* a, const void* b) {
 orc_owned_data* orc_data_build(int32_t N, int64_t L, int32_t vmax, const int8_t* G,
                                const int32_t* ploidy, const int32_t* k,
                                const int32_t* popid, int32_t S) {
+    return orc_data_build_ex(N, L, vmax, G, ploidy, k, popid, S, NULL);
+}
+
+orc_owned_data* orc_data_build_ex(int32_t N, int64_t L, int32_t vmax, const int8_t* G,
+                                  const int32_t* ploidy, const int32_t* k,
+                                  const int32_t* popid, int32_t S, const int8_t* Gtable) {
     orc_owned_data* d = NEW(orc_owned_data, 1);
-    /* 0. keep loci that are polymorphic among typed calls: a heterozygote or
-     *    two different homozygotes (filter.cpp:102-131); k < 2 never passes */
+    /* the loader's genotype table holds the calls before the genotype filter
+     * (load.cpp:2145-2230): the polymorphism test and the id widths read it */
+    const int8_t* T = Gtable ? Gtable : G;
+    /* 0. keep loci that are polymorphic in the genotype table: a heterozygote
+     *    or two different homozygotes (filter.cpp:102-131); k < 2 never passes */
     int64_t* keep = NEW(int64_t, L);
     int64_t L0 = L;
     L = 0;
@@ -60,7 +69,7 @@ orc_owned_data* orc_data_build(int32_t N, int64_t L, int32_t vmax, const int8_t*
         int pass = 0, first = -1;
         if (k[l] >= 2)
             for (int32_t i = 0; i < N && !pass; ++i) {
-                const int8_t* g = G + ((size_t)l * N + i) * vmax;
+                const int8_t* g = T + ((size_t)l * N + i) * vmax;
                 if (g[0] < 0) continue;
                 for (int c = 1; c < ploidy[i]; ++c) if (g[c] != g[0]) pass = 1;
                 if (first < 0) first = g[0];
@@ -76,7 +85,7 @@ orc_owned_data* orc_data_build(int32_t N, int64_t L, int32_t vmax, const int8_t*
         int used[16] = {0};
         int ng = 0, n = 0;
         for (int32_t i = 0; i < N; ++i) {
-            const int8_t* g = G + ((size_t)keep[l] * N + i) * vmax;
+            const int8_t* g = T + ((size_t)keep[l] * N + i) * vmax;
             int v = ploidy[i];
             if (!used[v]) { used[v] = 1; ng++; }
             if (g[0] < 0) continue;
@@ -1149,7 +1158,116 @@ void orc_divergence(const float* freqm, const int32_t* k, int64_t L, int64_t KT,
 
 /* load.cpp AddVCFGenotype for biallelic diploid calls: one line at a time,
  * fields split at tabs, the GT part of each sample field split at '/' or '|' */
+/* ReadIntegerKeep (string2.cpp:711-727): characters up to the first digit
+ * or '-' are skipped, then digits are read (int arithmetic, wrapping). The
+ * reference's scan has no end; this one stops at `end` with what it read. */
+static int read_integer_keep(const char* p, const char* end) {
+    int c, sign = 0;
+    unsigned x = 0;
+    for (c = p < end ? *p : 0, ++p; c < '0' || c > '9'; c = p < end ? *p : 0, ++p) {
+        if (p > end) return 0;
+        if (c == '-') {
+            sign = 1;
+            c = p < end ? *p : 0;
+            ++p;
+            break;
+        }
+    }
+    for (; c >= '0' && c <= '9'; c = p < end ? *p : 0, ++p) x = (x << 1) + (x << 3) + (unsigned)(c - '0');
+    return sign ? -(int)x : (int)x;
+}
+
+int orc_call_filtered(char* call, size_t room, int dpid, int gqid, int v, const orc_call_filter* cf) {
+    char* end = call + room;
+    /* AddVCFGenotype: count this call's keys, splitting them into '\0' */
+    int fmtc = 0;
+    for (char* q = call;;) {
+        fmtc++;
+        while (q < end && *q != ':' && *q != '\t' && *q != '\n' && *q != 0) q++;
+        if (q < end && *q == ':') *q++ = 0;
+        else {
+            if (q < end) *q = 0;
+            break;
+        }
+    }
+    /* GetTagValue (load.cpp:3596-3602): past `id` terminators */
+#define TAG(id, out)                                        \
+    do {                                                    \
+        char* r_ = call;                                    \
+        for (int i_ = 0; i_ < (id); ++i_) while (*r_++) {}  \
+        (out) = r_;                                         \
+    } while (0)
+    if (cf->dp_b && dpid >= 0 && dpid < fmtc) {
+        char* t;
+        TAG(dpid, t);
+        const unsigned dp = (unsigned)read_integer_keep(t, end);
+        if (dp != (unsigned)-1 && (dp < (unsigned)cf->dp_min || dp > (unsigned)cf->dp_max)) return 1;
+    }
+    if (cf->gq_b && gqid >= 0 && gqid < fmtc) {
+        char* t;
+        TAG(gqid, t);
+        const int gq = read_integer_keep(t, end);
+        if (gq != -1 && (gq < cf->gq_min || gq > cf->gq_max)) return 1;
+    }
+#undef TAG
+    if (cf->ploidy_b && (v < cf->ploidy_min || v > cf->ploidy_max)) return 1;
+    return 0;
+}
+
+size_t orc_rewrite_calls(const char* fmt, const char* fmt_end, const char* calls, const char* end, int n,
+                         char* out, size_t* call_at, int* dpid, int* gqid) {
+    /* FORMAT keys: kept when two bytes GT, DP or GQ then ':' or the tab */
+    int kept[1024], nk = 0, nkept = 0;
+    *dpid = *gqid = -1;
+    for (const char* k = fmt; k <= fmt_end && nk < 1024;) {
+        const char* ke = k;
+        while (ke < fmt_end && *ke != ':') ++ke;
+        const int two = ke - k == 2;
+        const int gt = two && k[0] == 'G' && k[1] == 'T', dp = two && k[0] == 'D' && k[1] == 'P',
+                  gq = two && k[0] == 'G' && k[1] == 'Q';
+        kept[nk++] = gt || dp || gq;
+        /* LOCUS::GetFormatId on the rewritten keys: the first DP, the first GQ */
+        if (dp && *dpid < 0) *dpid = nkept;
+        if (gq && *gqid < 0) *gqid = nkept;
+        nkept += gt || dp || gq;
+        if (ke >= fmt_end) break;
+        k = ke + 1;
+    }
+    /* each call: the values of the kept keys, joined by ':'; calls by tabs */
+    size_t o = 0;
+    const char* c = calls;
+    for (int i = 0; i < n && c <= end; ++i) {
+        call_at[i] = o;
+        int writed = 0;
+        for (int j = 0; j < nk; ++j) {
+            const char* v = c;
+            while (c < end && *c != ':' && *c != '\t') ++c;
+            if (kept[j]) {
+                if (writed) out[o++] = ':';
+                memcpy(out + o, v, (size_t)(c - v));
+                o += (size_t)(c - v);
+            }
+            if (c >= end || *c == '\t') break;
+            ++c;
+            if (kept[j]) writed = 1;
+        }
+        while (c < end && *c != '\t') ++c;      /* keys beyond FORMAT */
+        ++c;
+        if (i + 1 < n) out[o++] = '\t';
+    }
+    out[o] = 0;
+    return o;
+}
+
 int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packed, int64_t max_loci) {
+    return orc_vcf_pack2_ex(text, bytes, n_ind, packed, max_loci, NULL);
+}
+
+int64_t orc_vcf_pack2_ex(const char* text, size_t bytes, int n_ind, uint32_t* packed, int64_t max_loci,
+                         const orc_call_filter* cf) {
+    const int filter = cf && (cf->dp_b || cf->gq_b || cf->ploidy_b);
+    char* copy = NULL;
+    size_t copy_cap = 0;
     const int Nw = (n_ind + 15) / 16;
     const char* p = text;
     const char* end = text + bytes;
@@ -1158,10 +1276,22 @@ int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packe
         const char* e = memchr(p, '\n', (size_t)(end - p));
         const char* le = e ? e : end;
         if (le > p && le[-1] == '\r') --le;
-        if (l >= max_loci) return -(l + 1);
+        if (l >= max_loci) { free(copy); return -(l + 1); }
         uint32_t* row = packed + l * Nw;
         memset(row, 0, (size_t)Nw * 4);
-        int field = 0, nalt = 0;
+        int field = 0, nalt = 0, dpid = -1, gqid = -1;
+        size_t* call_at = NULL;
+        size_t rw_len = 0;
+        if (filter) {   /* the loader's rewritten calls, for the in-place key split and the value scans */
+            const char* fmt = p;
+            for (int c = 0; c < 8 && fmt < le; ++c) { fmt = memchr(fmt, '\t', (size_t)(le - fmt)); if (!fmt) break; ++fmt; }
+            const char* fe = fmt ? memchr(fmt, '\t', (size_t)(le - fmt)) : NULL;
+            if (!fmt || !fe) { free(copy); return -(l + 1); }
+            const size_t n = (size_t)(le - p);
+            if (n + 1 > copy_cap) { copy_cap = 2 * (n + 1); copy = realloc(copy, copy_cap); }
+            call_at = malloc(sizeof(size_t) * (size_t)n_ind);
+            rw_len = orc_rewrite_calls(fmt, fe, fe + 1, le, n_ind, copy, call_at, &dpid, &gqid);
+        }
         const char* f = p;
         while (f <= le) {
             const char* t = memchr(f, '\t', (size_t)(le - f));
@@ -1170,32 +1300,35 @@ int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packe
                 nalt = 2;
                 for (const char* c = f; c < fe; ++c) nalt += *c == ',';
             } else if (field == 8) {
-                if (!(fe - f >= 2 && f[0] == 'G' && f[1] == 'T' && (fe - f == 2 || f[2] == ':'))) return -(l + 1);
+                if (!(fe - f >= 2 && f[0] == 'G' && f[1] == 'T' && (fe - f == 2 || f[2] == ':'))) { free(copy); return -(l + 1); }
             } else if (field >= 9) {
                 const int i = field - 9;
-                if (i >= n_ind) return -(l + 1);
+                if (i >= n_ind) { free(copy); return -(l + 1); }
                 const char* g = f;
                 const char* ge = memchr(f, ':', (size_t)(fe - f));
                 if (!ge) ge = fe;
-                if (ge - g != 3 || (g[1] != '/' && g[1] != '|')) return -(l + 1);
+                if (ge - g != 3 || (g[1] != '/' && g[1] != '|')) { free(copy); return -(l + 1); }
                 int miss = 0, sum = 0;
                 for (int c = 0; c < 3; c += 2) {
                     if (g[c] == '.') miss = 1;
                     else if (g[c] == '0' || g[c] == '1') sum += g[c] - '0';
-                    else return -(l + 1);
+                    else { free(copy); return -(l + 1); }
                 }
+                if (!miss && filter && orc_call_filtered(copy + call_at[i], rw_len - call_at[i], dpid, gqid, 2, cf)) miss = 1;
                 row[i >> 4] |= (uint32_t)(miss ? 3 : sum) << (2 * (i & 15));
             }
             ++field;
             if (!t) break;
             f = t + 1;
         }
-        if (field != 9 + n_ind || nalt != 2) return -(l + 1);
+        free(call_at);
+        if (field != 9 + n_ind || nalt != 2) { free(copy); return -(l + 1); }
         for (int i = n_ind; i < Nw * 16; ++i) row[i >> 4] |= 3u << (2 * (i & 15));
         ++l;
         if (!e) break;
         p = e + 1;
     }
+    free(copy);
     return l;
 }
 

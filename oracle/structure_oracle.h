@@ -96,6 +96,12 @@ typedef struct orc_owned_data orc_owned_data;
 orc_owned_data* orc_data_build(int32_t N, int64_t L, int32_t vmax, const int8_t* G,
                                const int32_t* ploidy, const int32_t* k,
                                const int32_t* popid, int32_t S);
+/* orc_data_build with the calls before the genotype filter (Gtable, same
+ * layout; NULL: G): the loader's genotype table holds those, so they decide
+ * which loci are polymorphic and the loci's id widths. */
+orc_owned_data* orc_data_build_ex(int32_t N, int64_t L, int32_t vmax, const int8_t* G,
+                                  const int32_t* ploidy, const int32_t* k,
+                                  const int32_t* popid, int32_t S, const int8_t* Gtable);
 const orc_data* orc_data_view(const orc_owned_data* d);
 const int64_t* orc_data_order(const orc_owned_data* d); /* sorted -> input locus */
 void orc_data_free(orc_owned_data* d);
@@ -140,6 +146,32 @@ void orc_sweep_many(orc_chain** cs, int n, int nsweeps, int nthreads, int init);
  * case). Returns the number of lines, or -(line number) of the first line
  * that is not biallelic diploid 0/1 data. */
 int64_t orc_vcf_pack2(const char* text, size_t bytes, int n_ind, uint32_t* packed, int64_t max_loci);
+
+/* The genotype filter of -f_dp, -f_gq, -f_ploidy (AddVCFGenotype,
+ * load.cpp:3495-3566; windows parameters.cpp:743-748): a window is used when
+ * its flag is non-zero. */
+typedef struct {
+    int32_t dp_b, dp_min, dp_max, gq_b, gq_min, gq_max, ploidy_b, ploidy_min, ploidy_max;
+} orc_call_filter;
+/* One typed call of v copies under the genotype filter. `call` is the call's
+ * first byte in the line's rewritten calls (orc_rewrite_calls: this call's
+ * kept keys up to its tab, the later calls, end at call + room), with dpid
+ * and gqid among the kept keys; the call's keys are split at ':' into '\0'
+ * as the reference splits them (AddVCFGenotype). Returns 1 when the call
+ * becomes missing. */
+int orc_call_filtered(char* call, size_t room, int dpid, int gqid, int v, const orc_call_filter* cf);
+/* The loader's rewrite of a line's calls (load.cpp:2130-2257): of the FORMAT
+ * keys [fmt, fmt_end) it keeps GT, DP and GQ (two bytes, then ':' or the
+ * tab), each of the n calls [calls, end) keeps the values of those keys
+ * joined by ':', calls joined by tabs. out (room for end - calls + 1 bytes)
+ * gets the text, call_at[i] the offset of call i; dpid and gqid the indices
+ * of DP and GQ among the kept keys (-1: absent). Returns the length. */
+size_t orc_rewrite_calls(const char* fmt, const char* fmt_end, const char* calls, const char* end, int n,
+                         char* out, size_t* call_at, int* dpid, int* gqid);
+/* orc_vcf_pack2 with the genotype filter applied to each typed call
+ * (cf may be null). */
+int64_t orc_vcf_pack2_ex(const char* text, size_t bytes, int n_ind, uint32_t* packed, int64_t max_loci,
+                         const orc_call_filter* cf);
 
 /* The locus filter (filter.cpp MarkerDiversity over diversity.cpp
  * CalcDiversity) for a packed biallelic diploid matrix; f holds the flags

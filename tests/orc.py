@@ -75,6 +75,8 @@ def lib():
         L.orc_divergence.argtypes = [P, P, C.c_int64, C.c_int64, C.c_int, P, P, P]
         L.orc_divergence.restype = None
         L.orc_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int, P, C.c_int64]
+        L.orc_vcf_pack2_ex.argtypes = [P, C.c_size_t, C.c_int, P, C.c_int64, C.POINTER(CallFilter)]
+        L.orc_vcf_pack2_ex.restype = C.c_int64
         L.orc_locus_filter_pack2.argtypes = [P, C.c_int64, C.c_int, P, P, P]
         L.orc_locus_filter_pack2.restype = None
         L.orc_vcf_pack2.restype = C.c_int64
@@ -199,12 +201,30 @@ def divergence(freqm, k, K, per_locus=False):
     return dict(H=H, D=D, Hl=Hl)
 
 
-def vcf_pack2(text: bytes, n_ind: int, max_loci: int):
+class CallFilter(C.Structure):
+    """The layout of orc_call_filter (and of vp_call_filter)."""
+    _fields_ = [(n, C.c_int32) for n in ("dp_b", "dp_min", "dp_max", "gq_b", "gq_min", "gq_max", "ploidy_b",
+                                         "ploidy_min", "ploidy_max")]
+
+
+def call_filter(dp=None, gq=None, ploidy=None):
+    cf = CallFilter()
+    for name, w in (("dp", dp), ("gq", gq), ("ploidy", ploidy)):
+        if w is not None:
+            setattr(cf, name + "_b", 1)
+            setattr(cf, name + "_min", int(w[0]))
+            setattr(cf, name + "_max", int(w[1]))
+    return cf
+
+
+def vcf_pack2(text: bytes, n_ind: int, max_loci: int, calls=None):
     """The oracle's biallelic diploid VCF genotype parse: (packed, lines) or
-    raises naming the first unsupported line."""
+    raises naming the first unsupported line. calls: a genotype filter
+    (call_filter)."""
     packed = np.zeros((max_loci, (n_ind + 15) // 16), np.uint32)
     buf = np.frombuffer(text, dtype=np.uint8)
-    n = lib().orc_vcf_pack2(buf.ctypes.data, len(text), n_ind, packed.ctypes.data, max_loci)
+    n = lib().orc_vcf_pack2_ex(buf.ctypes.data, len(text), n_ind, packed.ctypes.data, max_loci,
+                               C.byref(calls) if calls is not None else None)
     if n < 0:
         raise ValueError(f"data line {-n} is not biallelic diploid 0/1 data")
     return packed[:n]

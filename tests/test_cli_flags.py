@@ -1,6 +1,6 @@
-"""Flag handling of the drop-in driver that needs no GPU: the reference's
-filters that the driver does not implement are refused before any data is
-read, so no run ever clusters data the caller asked to have filtered. The
+"""Flag handling of the drop-in driver that needs no GPU: a filter of the
+reference that the driver does not implement (-f_pop) is refused before any
+data is read, so no run ever clusters data the caller asked to have filtered. The
 reference applies its -f_* windows only under -f (src/parameters.cpp:
 1336-1343), so without -f they are accepted and have no effect, as there."""
 import subprocess
@@ -10,9 +10,7 @@ import pytest
 from vcfpop_gb300.build import CLI
 
 
-@pytest.mark.parametrize("flag", ["-f_dp=[10,100]", "-f_gq=[20,99]", "-f_qual=[30,255]",
-                                  "-f_windowsize=1000", "-f_ploidy=[2,2]",
-                                  "-f_type=snp", "-f_chrprefix=chr"])
+@pytest.mark.parametrize("flag", ["-f_pop=pop1"])
 def test_unimplemented_filters_are_refused(flag, tmp_path):
     r = subprocess.run([CLI, "-structure", f"-g_input={tmp_path}/none.vcf", f"-g_output={tmp_path}/out", "-f", flag],
                        capture_output=True, text=True)
@@ -27,9 +25,26 @@ def test_implemented_filters_are_accepted(tmp_path):
     r = subprocess.run([CLI, "-structure", f"-g_input={tmp_path}/none.vcf", f"-g_output={tmp_path}/out", "-f",
                         "-f_bmaf=[0.05,0.5]", "-f_ptype=[0.9,1]", "-f_k=[2,2]", "-f_n=[1,1000]", "-f_he=[0,1]",
                         "-f_ho=[0,1]", "-f_pic=[0,1]", "-f_ae=[1,2]", "-f_I=[0,2]", "-f_itype=[0.5,1]",
-                        "-f_iploidy=[2,2]", "-f_pval=[0.001,1]"], capture_output=True, text=True)
+                        "-f_iploidy=[2,2]", "-f_pval=[0.001,1]", "-f_dp=[10,100]", "-f_gq=[20,99]",
+                        "-f_ploidy=[2,4]", "-f_qual=[30,255]", "-f_model=prcs", "-f_type=snp", "-f_original=yes",
+                        "-f_chrprefix=chr1,chr2", "-f_chrname=chr3", "-f_windowsize=1000", "-f_windowstat=pic"],
+                       capture_output=True, text=True)
     assert r.returncode == 2
     assert "not implemented" not in r.stderr and "cannot read" in r.stderr
+
+
+@pytest.mark.parametrize("flag", ["-f_qual=[20,1000]", "-f_gq=[20,101]", "-f_ploidy=[0,4]", "-f_dp=[30,10]",
+                                  "-f_type=snv", "-f_original=maybe", "-f_windowsize=0", "-f_windowstat=I",
+                                  "-f_model=hwe"])
+def test_filter_values_outside_the_reference_ranges_are_refused(flag, tmp_path):
+    """The reference's parameter ranges (src/parameters.cpp:695-756: -f_qual
+    0..255, -f_gq 0..100, -f_ploidy 1..10, -f_windowsize 1..10^9, choices of
+    -f_type, -f_original, -f_windowstat, -f_model) stop the driver before it
+    reads any data."""
+    r = subprocess.run([CLI, "-structure", f"-g_input={tmp_path}/none.vcf", f"-g_output={tmp_path}/out", "-f", flag],
+                       capture_output=True, text=True)
+    assert r.returncode == 2
+    assert flag.split("=")[0] in r.stderr and "cannot read" not in r.stderr
 
 
 def test_filters_without_f_are_ignored_as_in_the_reference(tmp_path):

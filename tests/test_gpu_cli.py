@@ -51,7 +51,10 @@ def test_cli_files_have_reference_layout(case, tmp_path):
         assert got.count("\r\n") == want.count("\r\n")
 
 
-@pytest.mark.parametrize("case", ["c1_noadmix", "adm_admix"])
+# the genotype filter cases pin the device parse's DP/GQ/ploidy windows and
+# the loci the loader's genotype table keeps: a call filtered differently, or
+# a locus kept or ordered differently, changes the reference streams' trace
+@pytest.mark.parametrize("case", ["c1_noadmix", "adm_admix", "fmt_dpgq", "polyfmt_dpgq_ploidy"])
 def test_cli_reference_streams_follow_golden_trace(case, tmp_path):
     c = _run(case, str(tmp_path), "reference")
     f = [x for x in c["files"] if x.endswith(".lnl.txt")][0]
@@ -62,10 +65,14 @@ def test_cli_reference_streams_follow_golden_trace(case, tmp_path):
         assert abs(g - w) <= 1e-5 * abs(w), (g, w)
 
 
-def test_cli_locus_filter_keeps_the_reference_loci(tmp_path):
-    """-f with -f_* windows: the diversity table lists the loci the reference
-    program kept, by name, in its order."""
-    c = _run("c1_filter", str(tmp_path), "counter")
+@pytest.mark.parametrize("case", ["c1_filter", "fmt_window", "fmt_window_stat", "fmt_window_all"])
+def test_cli_locus_filter_keeps_the_reference_loci(case, tmp_path):
+    """-f with locus filters: the diversity table lists the loci the reference
+    program kept, by name, in its order. The cases cover the diversity
+    windows, the loader's tests on the fixed columns (-f_type, -f_original,
+    -f_chrprefix, -f_chrname, -f_qual), the genotype filter, and the window
+    filter with three statistics."""
+    c = _run(case, str(tmp_path), "counter")
     f = [x for x in c["files"] if x.endswith("_id=1.txt")][0]
 
     def loci(path):
@@ -73,7 +80,8 @@ def test_cli_locus_filter_keeps_the_reference_loci(tmp_path):
         i = next(j for j, ln in enumerate(lines) if ln.startswith("Estimated genetic diversity in each cluster"))
         return [ln.split("\t")[0] for ln in lines[i + 2:] if ln.split("\t")[0] not in ("", "Average")]
 
-    assert loci(tmp_path / f) == loci(os.path.join(GOLD, "c1_filter", f))
+    got, want = loci(tmp_path / f), loci(os.path.join(GOLD, case, f))
+    assert 0 < len(want) and got == want
 
 
 def test_cli_tensor_core_form_writes_the_reference_files(tmp_path):

@@ -169,3 +169,32 @@ def test_general_parse_rejects_what_it_cannot_store():
     bad = _general_vcf(d).replace(b"\tGT\t", b"\tDP:GT\t", 1)
     with pytest.raises(B.VpError, match="GT is not the first"):
         S.vcf_parse(bad, 10, 2)
+
+
+# The genotype filter of the device parses against the oracle's parse, which
+# restates the loader's line rewrite (GT, DP and GQ kept, case as written) and
+# AddVCFGenotype literally and is pinned on the reference program by the
+# fmt_dpgq and polyfmt_dpgq_ploidy golden cases. The golden fmt VCF has DP,
+# GQ and AD keys in several orders, lowercase keys (which the loader drops),
+# '.' and -1 values, and calls with fewer keys than FORMAT.
+@pytest.mark.parametrize("windows", [dict(dp=(10, 60)), dict(gq=(25, 99)), dict(dp=(10, 60), gq=(25, 99)),
+                                     dict(ploidy=(3, 4)), dict(dp=(0, 0x7FFFFFFF), gq=(0, 100))])
+def test_genotype_filter_of_the_device_parses_matches_the_oracle(windows):
+    raw = gzip.open(os.path.join(GOLD, "fmt.vcf.gz")).read()
+    header = raw[raw.index(b"\n#CHROM") + 1:].split(b"\n", 1)[0].decode().split("\t")
+    N = len(header) - 9
+    text = _data_section(raw)
+    L = text.count(b"\n")
+    want = orc.vcf_pack2(text, N, L, calls=orc.call_filter(**windows))
+    unfiltered = orc.vcf_pack2(text, N, L)
+    got, _ = S.vcf_pack2(text, N, calls=S.call_filter(**windows))
+    assert np.array_equal(got, want)
+    codes = (want[:, np.arange(N) // 16] >> (2 * (np.arange(N) % 16))) & 3
+    before = (unfiltered[:, np.arange(N) // 16] >> (2 * (np.arange(N) % 16))) & 3
+    if windows.get("dp", (0, 0x7FFFFFFF)) != (0, 0x7FFFFFFF):
+        assert (codes == 3).sum() > (before == 3).sum()      # the windows took calls away
+    # the general parse of the same text gives the same calls
+    G, k, ploidy, _ = S.vcf_parse(text, N, 2, calls=S.call_filter(**windows))
+    typed = G[:, :, 0] >= 0
+    assert np.array_equal(typed, codes != 3)
+    assert np.array_equal(np.where(typed, G.sum(axis=2), 3), codes)

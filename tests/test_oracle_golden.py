@@ -23,9 +23,11 @@ def _summary_table(path):
     return [ln for ln in lines[i:] if ln.strip()]
 
 
-# cases whose flags the oracle's driver does not take (the locus filter) are
-# checked by their own tests
-WHOLE = sorted(c for c in CASES if "-f" not in CASES[c]["flags"])
+# the oracle's driver takes the genotype filter (-f with -f_dp, -f_gq,
+# -f_ploidy); cases with locus filters are checked by their own tests
+CALL_FILTERS = ("-f_dp=", "-f_gq=", "-f_ploidy=")
+WHOLE = sorted(c for c in CASES
+               if all(not x.startswith("-f_") or x.startswith(CALL_FILTERS) for x in CASES[c]["flags"]))
 
 
 @pytest.mark.parametrize("case", WHOLE)

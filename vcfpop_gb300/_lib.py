@@ -22,7 +22,8 @@ FIELD = dict(FREQ=1, Q=2, Z=3, NI=4, MI=5, LL=6, ALPHA=7, M=8, LNL=9, FREQA=10, 
 class VpInput(C.Structure):
     _fields_ = [("n_ind", C.c_int32), ("n_loc", C.c_int64), ("vmax", C.c_int32),
                 ("alleles", C.c_void_p), ("packed2", C.c_void_p), ("ploidy", C.c_void_p),
-                ("n_alleles", C.c_void_p), ("popid", C.c_void_p), ("n_pop", C.c_int32)]
+                ("n_alleles", C.c_void_p), ("popid", C.c_void_p), ("n_pop", C.c_int32),
+                ("table_poly", C.c_void_p), ("table_ngeno", C.c_void_p)]
 
 
 class VpDatasetInfo(C.Structure):
@@ -72,6 +73,11 @@ class VpLocusFilter(C.Structure):
                [("pval_b", C.c_int32), ("pval_min", C.c_double), ("pval_max", C.c_double)]
 
 
+class VpCallFilter(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("dp_b", "dp_min", "dp_max", "gq_b", "gq_min", "gq_max", "ploidy_b",
+                                         "ploidy_min", "ploidy_max")]
+
+
 class VpTcConfig(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("bk", "row_tiles", "cols", "piece", "stages", "splits", "group_major",
                                          "count_stages", "count_group_major", "candidates")] + \
@@ -104,7 +110,8 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_tune", "vp_tc_configure", "vp_tc_config_get", "vp_debug_gemm_wait_timeout", "vp_write_structure",
            "vp_cohort_open", "vp_cohort_set", "vp_cohort_run", "vp_cohort_sync", "vp_cohort_stream",
            "vp_cohort_launches", "vp_cohort_close", "vp_server_set_batching", "vp_server_stats",
-           "vp_vcf_parse", "vp_tc_pipeline"]
+           "vp_vcf_parse", "vp_tc_pipeline", "vp_vcf_pack2_ex", "vp_vcf_parse_ex",
+           "vp_genotype_table"]
 
 
 def lib():
@@ -118,6 +125,7 @@ def lib():
     L = C.CDLL(LIB)
     P = C.c_void_p
     L.vp_dataset_prepare.argtypes = [C.POINTER(VpInput), C.POINTER(P)]
+    L.vp_genotype_table.argtypes = [C.POINTER(VpInput), P, P]
     L.vp_dataset_info_get.argtypes = [P, C.POINTER(VpDatasetInfo)]
     L.vp_dataset_order.argtypes = [P, P]
     L.vp_dataset_free.argtypes = [P]
@@ -167,6 +175,9 @@ def lib():
     L.vp_server_close.argtypes = [P]
     L.vp_vcf_pack2.argtypes = [P, C.c_size_t, C.c_int32, C.c_int, P, C.c_int64, P, P]
     L.vp_vcf_parse.argtypes = [P, C.c_size_t, C.c_int32, C.c_int32, C.c_int, P, P, P, C.c_int64, P, P]
+    L.vp_vcf_pack2_ex.argtypes = [P, C.c_size_t, C.c_int32, C.c_int, P, C.c_int64, P, P, C.POINTER(VpCallFilter)]
+    L.vp_vcf_parse_ex.argtypes = [P, C.c_size_t, C.c_int32, C.c_int32, C.c_int, P, P, P, C.c_int64, P, P,
+                                  C.POINTER(VpCallFilter)]
     L.vp_locus_filter_pack2.argtypes = [P, C.c_int64, C.c_int32, C.POINTER(VpLocusFilter), C.c_int, P, P]
     L.vp_write_structure.argtypes = [P, C.POINTER(VpWriteOpts)]
     L.vp_cohort_open.argtypes = [C.c_int, C.POINTER(P)]

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../../include/vcfpop_structure.h"
+#include "vp_callfilter.h"
 
 namespace {
 
@@ -42,11 +43,50 @@ struct Opts {
     bool itype_b = false, iploidy_b = false;
     double itype_min = 0, itype_max = 0;
     int iploidy_min = 0, iploidy_max = 0;
+    // the genotype filter (-f_dp, -f_gq, -f_ploidy), applied as the calls are read
+    vp_call_filter cf{};
+    // the locus filters on the VCF's fixed columns (-f_type, -f_original,
+    // -f_chrprefix, -f_chrname; -f_qual is accepted and, as in the
+    // reference, removes nothing) and the window filter (-f_windowsize,
+    // -f_windowstat)
+    int type_val = 0;                  // 1 snp, 2 indel, 3 both
+    bool original_b = false;           // -f_original=yes
+    bool chrprefix_b = false, chrname_b = false;
+    std::vector<std::string> chrprefix, chrname;
+    int64_t windowsize = 0;            // 0: no window filter
+    int windowstat = 5;                // 1 bmaf, 2 k, 3 n, 4 ptype, 5 he, 6 ho, 7 pic, 8 ae
     vp_params p;
     std::vector<std::string> argv;
 };
 
 int yesno(const std::string& v) { return v == "yes" ? 1 : 0; }
+
+// a comma-separated list (SplitStr of TrimParQuote, src/parameters.cpp:703-714)
+std::vector<std::string> split_list(const std::string& v) {
+    std::vector<std::string> out;
+    size_t q = 0;
+    for (;;) {
+        size_t c = v.find(',', q);
+        out.push_back(v.substr(q, c == std::string::npos ? std::string::npos : c - q));
+        if (c == std::string::npos) break;
+        q = c + 1;
+    }
+    return out;
+}
+
+// the 1-based index of v in a '|' list of choices (GetParString), 0 if absent
+int choice(const std::string& v, const char* list) {
+    int idx = 1;
+    std::string l(list);
+    size_t q = 0;
+    for (;;) {
+        size_t c = l.find('|', q);
+        if (l.substr(q, c == std::string::npos ? std::string::npos : c - q) == v) return idx;
+        if (c == std::string::npos) return 0;
+        q = c + 1;
+        ++idx;
+    }
+}
 
 bool parse(int argc, char** argv, Opts& o) {
     vp_params_default(&o.p);
@@ -116,20 +156,58 @@ bool parse(int argc, char** argv, Opts& o) {
         else if (k == "-f_pval") o.lf.pval_b = sscanf(v.c_str(), "[%lf,%lf]", &o.lf.pval_min, &o.lf.pval_max) == 2;
         else if (k == "-f_itype") o.itype_b = sscanf(v.c_str(), "[%lf,%lf]", &o.itype_min, &o.itype_max) == 2;
         else if (k == "-f_iploidy") o.iploidy_b = sscanf(v.c_str(), "[%d,%d]", &o.iploidy_min, &o.iploidy_max) == 2;
-        else if (k.rfind("-f_", 0) == 0) unimplemented.push_back(k);
+        else if (k == "-f_dp" || k == "-f_gq" || k == "-f_ploidy") {
+            // windows and ranges of GetRangeParInteger (src/parameters.cpp:743-748)
+            int lo = 0, hi = 0;
+            const int bound = k == "-f_dp" ? 0x7FFFFFFF : k == "-f_gq" ? 100 : 10, floor_ = k == "-f_ploidy" ? 1 : 0;
+            if (sscanf(v.c_str(), "[%d,%d]", &lo, &hi) != 2 || lo < floor_ || hi > bound || lo > hi) {
+                fprintf(stderr, "vcfpop-gb300: parameter %s out of range (%d to %d)\n", a.c_str(), floor_, bound);
+                return false;
+            }
+            int32_t* w = k == "-f_dp" ? &o.cf.dp_b : k == "-f_gq" ? &o.cf.gq_b : &o.cf.ploidy_b;
+            w[0] = 1; w[1] = lo; w[2] = hi;
+        } else if (k == "-f_qual") {
+            // the reference's test (qual < min && qual > max, src/load.cpp
+            // :1916, 2420) never fails a locus for min <= max: only the
+            // window is checked
+            double lo = 0, hi = 0;
+            if (sscanf(v.c_str(), "[%lf,%lf]", &lo, &hi) != 2 || lo < 0 || hi > 255 || lo > hi) {
+                fprintf(stderr, "vcfpop-gb300: parameter %s out of range (0 to 255)\n", a.c_str());
+                return false;
+            }
+        } else if (k == "-f_model") {
+            // the genotype model of the HWE test, the same for every model
+            // at ploidy 2 (the locus statistics here are for diploid data)
+            if (!choice(v, "rcs|prcs|ces|pes")) { fprintf(stderr, "vcfpop-gb300: bad %s\n", a.c_str()); return false; }
+        } else if (k == "-f_type") {
+            if (!(o.type_val = choice(v, "snp|indel|both"))) { fprintf(stderr, "vcfpop-gb300: bad %s\n", a.c_str()); return false; }
+        } else if (k == "-f_original") {
+            const int c = choice(v, "yes|no");
+            if (!c) { fprintf(stderr, "vcfpop-gb300: bad %s\n", a.c_str()); return false; }
+            o.original_b = c == 1;
+        } else if (k == "-f_chrprefix") { o.chrprefix_b = true; o.chrprefix = split_list(v); }
+        else if (k == "-f_chrname") { o.chrname_b = true; o.chrname = split_list(v); }
+        else if (k == "-f_windowsize") {
+            o.windowsize = atoll(v.c_str());
+            if (o.windowsize < 1 || o.windowsize > 1000000000) { fprintf(stderr, "vcfpop-gb300: bad %s\n", a.c_str()); return false; }
+        } else if (k == "-f_windowstat") {
+            if (!(o.windowstat = choice(v, "bmaf|k|n|ptype|he|ho|pic|ae"))) { fprintf(stderr, "vcfpop-gb300: bad %s\n", a.c_str()); return false; }
+        } else if (k.rfind("-f_", 0) == 0) unimplemented.push_back(k);
         // other -g_* and -structure_* flags (threads, SIMD, plots, streams) do
         // not apply to the GPU path and are accepted silently
     }
-    // the reference applies its -f_* windows only under -f
-    // (src/parameters.cpp:1336-1343); every other filter of the reference
-    // (-f_qual, -f_dp, -f_gq, -f_windowsize, ...) would change which
-    // loci, calls or individuals the clustering sees: refuse it rather than
-    // run on unfiltered data
+    // the reference applies its -f_* filters only under -f
+    // (src/parameters.cpp:1336-1343); a filter of the reference that is not
+    // implemented here (-f_pop) would change which loci the clustering sees:
+    // refuse it rather than run on unfiltered data
     if (o.filter && !unimplemented.empty()) {
         fprintf(stderr, "vcfpop-gb300: the filter %s is not implemented (implemented: -f_bmaf -f_k -f_n -f_ptype "
-                        "-f_he -f_ho -f_pic -f_ae -f_I -f_pval -f_itype -f_iploidy)\n", unimplemented[0].c_str());
+                        "-f_he -f_ho -f_pic -f_ae -f_I -f_pval -f_itype -f_iploidy -f_dp -f_gq -f_ploidy -f_qual "
+                        "-f_model -f_type -f_original -f_chrprefix -f_chrname -f_windowsize -f_windowstat)\n",
+                unimplemented[0].c_str());
         return false;
     }
+    if (!o.filter) o.cf = vp_call_filter{};
     if (!structure) { fprintf(stderr, "vcfpop-gb300: only -structure is implemented\n"); return false; }
     if (o.input.empty()) { fprintf(stderr, "vcfpop-gb300: -g_input is required\n"); return false; }
     return true;
@@ -140,9 +218,45 @@ struct Vcf {
     std::vector<int32_t> ploidy, k;
     std::vector<int8_t> G;  // [L][N][vmax]
     int vmax = 0;
+    // per locus: CHROM, POS, whether REF and the ALT alleles differ in
+    // length (an indel, LOCUS::LOCUS src/function.cpp:3244-3253), whether
+    // FILTER starts with "pass" in any case (src/load.cpp:2429-2434)
+    std::vector<std::string> chrom;
+    std::vector<int64_t> pos;
+    std::vector<uint8_t> indel, pass;
 };
 
-bool read_vcf(const std::string& path, Vcf& v) {
+// the fixed fields of one data line [a, e) into v's per-locus vectors;
+// false when the line has fewer than 8 of them
+bool line_info(const char* a, const char* e, Vcf& v) {
+    const char* f[9];
+    int n = 0;
+    f[n++] = a;
+    for (const char* q = a; q < e && n < 9; ++q)
+        if (*q == '\t') f[n++] = q + 1;
+    if (n < 8) return false;
+    v.chrom.emplace_back(f[0], f[1] - 1 - f[0]);
+    v.pos.push_back(strtoll(f[1], nullptr, 10));
+    // allele string lengths: REF, then each comma-separated ALT
+    int64_t mn = f[4] - 1 - f[3], mx = mn, cur = 0;
+    for (const char* q = f[4]; q < f[5] - 1; ++q) {
+        if (*q == ',') { mn = std::min(mn, cur); mx = std::max(mx, cur); cur = 0; }
+        else ++cur;
+    }
+    mn = std::min(mn, cur);
+    mx = std::max(mx, cur);
+    v.indel.push_back(mn != mx);
+    static const char kPass[] = "pass";
+    bool pass = true;
+    for (int j = 0; j < 4; ++j) {
+        const char c = f[6] + j < e ? f[6][j] : '\0';
+        if ((c >= 'A' && c <= 'Z' ? c + 32 : c) != kPass[j]) { pass = false; break; }
+    }
+    v.pass.push_back(pass);
+    return true;
+}
+
+bool read_vcf(const std::string& path, const vp_call_filter& cf, Vcf& v) {
     gzFile f = gzopen(path.c_str(), "rb");
     if (!f) return false;
     std::vector<char> buf(1 << 24);
@@ -172,9 +286,16 @@ bool read_vcf(const std::string& path, Vcf& v) {
             continue;
         }
         const int N = (int)v.inds.size();
+        if (cols.size() < 9 || !line_info(line.data(), line.data() + line.size(), v)) return false;
         int nalt = 1;
         for (char ch : cols[4]) nalt += ch == ',';
         v.k.push_back(1 + nalt);
+        // FORMAT keys of the genotype filter, and each call's offset in the line
+        int dpid = -1, gqid = -1;
+        uint64_t kept = 0;
+        vp::parse_format(cols[8].data(), (int64_t)cols[8].size(), &dpid, &gqid, &kept);
+        std::vector<size_t> at(cols.size());
+        for (size_t c = 1, off = 0; c < cols.size(); ++c) { off += cols[c - 1].size() + 1; at[c] = off; }
         // the reference's default locus name: CHROM_ID (CHROM_POS without an ID)
         v.locs.push_back(cols[0] + "_" + (cols[2] != "." ? cols[2] : cols[1]));
         if (nl == 0) {
@@ -205,6 +326,7 @@ bool read_vcf(const std::string& path, Vcf& v) {
                 q = e + 1;
             }
             if (miss) continue;
+            if (vp::call_filtered(cf, line.data(), (int64_t)at[9 + i], (int64_t)line.size(), dpid, gqid, kept, n)) continue;
             std::sort(al, al + n);
             for (int c = 0; c < n && c < v.vmax; ++c) v.G[base + (size_t)i * v.vmax + c] = al[c];
         }
@@ -264,7 +386,7 @@ int read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
     packed.assign((size_t)L * Nw, 0);
     std::vector<int64_t> starts(L + 1);
     int64_t got = 0;
-    if (vp_vcf_pack2(data, bytes, N, o.device, packed.data(), L, starts.data(), &got) || got != L) {
+    if (vp_vcf_pack2_ex(data, bytes, N, o.device, packed.data(), L, starts.data(), &got, &o.cf) || got != L) {
         // not biallelic diploid: the general parse on the device (any ploidy
         // and allele count), with each sample's ploidy from its first call
         fprintf(stderr, "vcfpop-gb300: packed ingest not used (%s)\n", vp_last_error());
@@ -286,8 +408,8 @@ int read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
         v.G.assign((size_t)L * N * vmax, -1);
         v.k.assign(L, 0);
         v.ploidy.assign(N, 0);
-        if (vp_vcf_parse(data, bytes, N, vmax, o.device, v.G.data(), v.k.data(), v.ploidy.data(), L, starts.data(),
-                         &got) || got != L) {
+        if (vp_vcf_parse_ex(data, bytes, N, vmax, o.device, v.G.data(), v.k.data(), v.ploidy.data(), L,
+                            starts.data(), &got, &o.cf) || got != L) {
             fprintf(stderr, "vcfpop-gb300: device ingest not used (%s); reading on the host\n", vp_last_error());
             v = Vcf();
             return 0;
@@ -300,7 +422,7 @@ int read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
             const char* t1 = (const char*)memchr(a, '\t', e - a);
             const char* t2 = t1 ? (const char*)memchr(t1 + 1, '\t', e - t1 - 1) : nullptr;
             const char* t3 = t2 ? (const char*)memchr(t2 + 1, '\t', e - t2 - 1) : nullptr;
-            if (!t1 || !t2 || !t3) { v = Vcf(); return 0; }
+            if (!t1 || !t2 || !t3 || !line_info(a, e, v)) { v = Vcf(); return 0; }
             std::string id(t2 + 1, t3 - t2 - 1);
             v.locs[l] = std::string(a, t1 - a) + "_" + (id != "." ? id : std::string(t1 + 1, t2 - t1 - 1));
         }
@@ -317,7 +439,7 @@ int read_vcf_device(const Opts& o, Vcf& v, std::vector<uint32_t>& packed) {
         const char* t1 = (const char*)memchr(a, '\t', e - a);
         const char* t2 = t1 ? (const char*)memchr(t1 + 1, '\t', e - t1 - 1) : nullptr;
         const char* t3 = t2 ? (const char*)memchr(t2 + 1, '\t', e - t2 - 1) : nullptr;
-        if (!t1 || !t2 || !t3) { v = Vcf(); packed.clear(); return 0; }
+        if (!t1 || !t2 || !t3 || !line_info(a, e, v)) { v = Vcf(); packed.clear(); return 0; }
         std::string id(t2 + 1, t3 - t2 - 1);
         v.locs[l] = std::string(a, t1 - a) + "_" + (id != "." ? id : std::string(t1 + 1, t2 - t1 - 1));
     }
@@ -443,6 +565,52 @@ bool individual_filter(const Opts& o, Vcf& v, bool dev_ingest, std::vector<uint3
     return true;
 }
 
+// The loader's locus tests on the fixed columns (LOCUS::LOCUS, src/function.cpp
+// :3258-3290): -f_type=snp drops indels and =indel drops the other loci;
+// -f_original=yes drops loci whose FILTER does not start with "pass";
+// -f_chrprefix keeps chromosomes that start with one of its prefixes (LineCmp,
+// src/string2.cpp:222-231), -f_chrname those equal to one of its names.
+void info_filter(const Opts& o, const Vcf& v, std::vector<uint8_t>& keep) {
+    for (size_t l = 0; l < keep.size(); ++l) {
+        bool pass = keep[l];
+        if (pass && o.type_val == 1 && v.indel[l]) pass = false;
+        if (pass && o.type_val == 2 && !v.indel[l]) pass = false;
+        if (pass && o.original_b && !v.pass[l]) pass = false;
+        if (pass && o.chrprefix_b) {
+            pass = false;
+            for (const auto& pr : o.chrprefix) pass |= v.chrom[l].compare(0, pr.size(), pr) == 0 && v.chrom[l].size() >= pr.size();
+        }
+        if (pass && o.chrname_b) {
+            pass = false;
+            for (const auto& nm : o.chrname) pass |= v.chrom[l] == nm;
+        }
+        keep[l] = pass;
+    }
+}
+
+// The window filter (MarkerDiversity, src/filter.cpp:509-555, then 74-90):
+// of the loci that pass, each window (CHROM, (POS - 1) / -f_windowsize)
+// keeps one, the first in file order with the largest -f_windowstat
+// statistic (a later locus replaces it only with a strictly larger value:
+// the reference's order with one thread); every other locus fails. st holds
+// the device statistics, VP_LOCUS_STATS per locus.
+void window_filter(const Opts& o, const Vcf& v, const std::vector<double>& st, std::vector<uint8_t>& keep) {
+    // -f_windowstat 1..8 (bmaf, k, n, ptype, he, ho, pic, ae) -> statistic column (n, k, ptype, bmaf, he, ho, pic, ae, ...)
+    static const int col[9] = {4, 3, 1, 0, 2, 4, 5, 6, 7};
+    const int c = col[o.windowstat];
+    std::map<std::pair<std::string, int64_t>, std::pair<int64_t, double>> best;
+    for (size_t l = 0; l < keep.size(); ++l) {
+        if (!keep[l]) continue;
+        const double div = st[l * VP_LOCUS_STATS + c];
+        const auto key = std::make_pair(v.chrom[l], (v.pos[l] - 1) / o.windowsize);
+        auto it = best.find(key);
+        if (it == best.end()) best.emplace(key, std::make_pair((int64_t)l, div));
+        else if (it->second.second < div) it->second = std::make_pair((int64_t)l, div);
+    }
+    std::fill(keep.begin(), keep.end(), 0);
+    for (const auto& w : best) keep[w.second.first] = 1;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -452,9 +620,31 @@ int main(int argc, char** argv) {
     std::vector<uint32_t> dev_packed;   // device-parsed 2-bit matrix, file order of individuals
     const int ingest = read_vcf_device(o, v, dev_packed);
     const bool dev_ingest = ingest == 1;   // the 2-bit matrix (else allele copies in v.G)
-    if (!ingest && !read_vcf(o.input, v)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
+    if (!ingest && !read_vcf(o.input, o.cf, v)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
     const int N0 = (int)v.inds.size();
     const int64_t L0 = (int64_t)v.k.size();
+    // with the genotype filter, the loader's genotype table still holds
+    // every call of the file (src/load.cpp:2145-2230): which loci are
+    // polymorphic and how the loci are ordered follow the calls before the
+    // filter, read here a second time without it
+    std::vector<uint8_t> tpoly;
+    std::vector<int32_t> tngeno;
+    if (o.filter && (o.cf.dp_b || o.cf.gq_b || o.cf.ploidy_b)) {
+        Opts o0 = o;
+        o0.cf = vp_call_filter{};
+        Vcf v0;
+        std::vector<uint32_t> p0;
+        const int k0 = read_vcf_device(o0, v0, p0);
+        if (!k0 && !read_vcf(o.input, o0.cf, v0)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
+        if ((int64_t)v0.k.size() != L0 || (int)v0.inds.size() != N0) { fprintf(stderr, "vcfpop-gb300: the second read differs\n"); return 1; }
+        vp_input t{};
+        t.n_ind = N0; t.n_loc = L0; t.vmax = v0.vmax; t.ploidy = v0.ploidy.data(); t.n_alleles = v0.k.data();
+        if (k0 == 1) t.packed2 = p0.data();
+        else t.alleles = v0.G.data();
+        tpoly.resize(L0);
+        tngeno.resize(L0);
+        if (vp_genotype_table(&t, tpoly.data(), tngeno.data())) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+    }
     std::vector<int> pop;
     std::vector<std::string> pnames;
     populations(o.indtext, N0, pop, pnames);
@@ -524,38 +714,62 @@ int main(int argc, char** argv) {
     } else {
         in.alleles = G.data();
     }
-    // the locus filter (-f with -f_* windows: src/filter.cpp MarkerDiversity)
-    // on the packed matrix, on the device; loci that fail are dropped here
+    // the locus filters (src/filter.cpp ApplyFilter), over the loci of the
+    // file: the loader's tests on the fixed columns (-f_type, -f_original,
+    // -f_chrprefix, -f_chrname), then, on the device for the packed matrix,
+    // the diversity windows (MarkerDiversity) and the window filter over the
+    // loci that passed; the loci that fail are dropped here
     const vp_locus_filter& lf = o.lf;
     const bool windows = lf.bmaf_b || lf.k_b || lf.n_b || lf.ptype_b || lf.he_b || lf.ho_b || lf.pic_b || lf.ae_b ||
                          lf.I_b || lf.pval_b;
+    const bool info_tests = o.type_val == 1 || o.type_val == 2 || o.original_b || o.chrprefix_b || o.chrname_b;
     std::vector<uint32_t> kept_packed;
-    if (o.filter && windows) {
-        if (!in.packed2) { fprintf(stderr, "vcfpop-gb300: the locus filter needs biallelic diploid data\n"); return 1; }
-        const int Nw = (N + 15) / 16;
-        std::vector<uint8_t> keep(L0);
-        if (vp_locus_filter_pack2(in.packed2, L0, N, &lf, o.device, keep.data(), nullptr)) {
-            fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error());
-            return 1;
+    std::vector<int8_t> kept_G;
+    if (o.filter && (windows || info_tests || o.windowsize)) {
+        std::vector<uint8_t> keep(L0, 1);
+        if (info_tests) info_filter(o, v, keep);
+        if (windows || o.windowsize) {
+            if (!in.packed2) { fprintf(stderr, "vcfpop-gb300: the locus filter needs biallelic diploid data\n"); return 1; }
+            std::vector<uint8_t> kd(L0);
+            std::vector<double> st(o.windowsize ? (size_t)L0 * VP_LOCUS_STATS : 0);
+            if (vp_locus_filter_pack2(in.packed2, L0, N, &lf, o.device, kd.data(), o.windowsize ? st.data() : nullptr)) {
+                fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error());
+                return 1;
+            }
+            for (int64_t l = 0; l < L0; ++l) keep[l] &= kd[l];
+            if (o.windowsize) window_filter(o, v, st, keep);
         }
         int64_t nk = 0;
         for (int64_t l = 0; l < L0; ++l) nk += keep[l];
-        kept_packed.resize((size_t)nk * Nw);
+        if (nk == 0) { fprintf(stderr, "vcfpop-gb300: all %lld loci are excluded by the filters\n", (long long)L0); return 1; }
         std::vector<int32_t> k2;
         std::vector<std::string> locs2;
+        if (in.packed2) {
+            const int Nw = (N + 15) / 16;
+            kept_packed.resize((size_t)nk * Nw);
+            for (int64_t l = 0, j = 0; l < L0; ++l)
+                if (keep[l]) memcpy(&kept_packed[(size_t)j++ * Nw], in.packed2 + (size_t)l * Nw, (size_t)Nw * 4);
+            in.packed2 = kept_packed.data();
+        } else {
+            const size_t row = (size_t)N * v.vmax;
+            kept_G.resize((size_t)nk * row);
+            for (int64_t l = 0, j = 0; l < L0; ++l)
+                if (keep[l]) memcpy(&kept_G[(size_t)j++ * row], in.alleles + (size_t)l * row, row);
+            in.alleles = kept_G.data();
+        }
         for (int64_t l = 0, j = 0; l < L0; ++l)
             if (keep[l]) {
-                memcpy(&kept_packed[(size_t)j++ * Nw], in.packed2 + (size_t)l * Nw, (size_t)Nw * 4);
                 k2.push_back(v.k[l]);
                 locs2.push_back(v.locs[l]);
+                if (!tpoly.empty()) { tpoly[j] = tpoly[l]; tngeno[j] = tngeno[l]; ++j; }
             }
         v.k.swap(k2);
         v.locs.swap(locs2);
-        in.packed2 = kept_packed.data();
         in.n_loc = nk;
         in.n_alleles = v.k.data();
-        fprintf(stderr, "vcfpop-gb300: locus filter kept %lld of %lld loci\n", (long long)nk, (long long)L0);
+        fprintf(stderr, "vcfpop-gb300: locus filters kept %lld of %lld loci\n", (long long)nk, (long long)L0);
     }
+    if (!tpoly.empty()) { in.table_poly = tpoly.data(); in.table_ngeno = tngeno.data(); }
     vp_dataset* ds = nullptr;
     if (vp_dataset_prepare(&in, &ds)) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
     vp_dataset_info info;

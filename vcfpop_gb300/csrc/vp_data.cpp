@@ -70,6 +70,56 @@ bool is_coprime(int64_t x, int64_t y) {
 
 inline int code_at(const uint32_t* row, int i) { return (row[i >> 4] >> ((i & 15) * 2)) & 3; }
 
+// Per input locus, from its calls: whether the locus is polymorphic (a
+// typed genotype with two alleles, or two different typed genotypes:
+// ApplyFilter, src/filter.cpp:102-133; fewer than 2 alleles never) and how
+// many genotype ids the loader gives it (one per distinct typed genotype
+// plus one missing id per ploidy level of the individuals,
+// src/load.cpp:2180-2230)
+void table_facts(const vp_input* in, bool p2, int vmax, uint8_t* pass, int32_t* ngeno) {
+    const int32_t N = in->n_ind;
+    const int Nw = (N + 15) / 16;
+    parallel_for(in->n_loc, [&](int64_t l) {
+        pass[l] = 0;
+        ngeno[l] = 1;
+        if (in->n_alleles[l] < 2) return;
+        if (p2) {
+            const uint32_t* row = in->packed2 + (size_t)l * Nw;
+            int seen = 0;  // bit c set when code c observed
+            for (int i = 0; i < N; ++i) seen |= 1 << code_at(row, i);
+            int typed = seen & 7;
+            pass[l] = (typed & 2) || ((typed & 5) == 5);
+            ngeno[l] = 1 + ((typed & 1) != 0) + ((typed & 2) != 0) + ((typed & 4) != 0);
+            return;
+        }
+        const int8_t* G = in->alleles + (size_t)l * N * vmax;
+        int first = -1, ok = 0;
+        std::vector<uint64_t> keys;
+        keys.reserve(N);
+        uint32_t used = 0;
+        for (int i = 0; i < N; ++i) {
+            const int8_t* g = G + (size_t)i * vmax;
+            int v = in->ploidy[i];
+            used |= 1u << v;
+            if (g[0] < 0) continue;
+            uint64_t h = (uint64_t)v;
+            for (int c = 0; c < v; ++c) {
+                h = h * 64 + (uint64_t)(g[c] + 1);
+                if (g[c] != g[0]) ok = 1;
+            }
+            if (first < 0) first = g[0];
+            else if (g[0] != first) ok = 1;
+            keys.push_back(h);
+        }
+        std::sort(keys.begin(), keys.end());
+        int64_t ng = __builtin_popcount(used);
+        for (size_t j = 0; j < keys.size(); ++j)
+            if (j == 0 || keys[j] != keys[j - 1]) ng++;
+        pass[l] = (uint8_t)ok;
+        ngeno[l] = (int32_t)ng;
+    });
+}
+
 }  // namespace
 
 void vp_set_error(const char* fmt, ...) {
@@ -80,6 +130,17 @@ void vp_set_error(const char* fmt, ...) {
 }
 
 extern "C" const char* vp_last_error(void) { return g_err; }
+
+extern "C" int vp_genotype_table(const vp_input* in, uint8_t* poly, int32_t* ngeno) {
+    if (!in || !poly || !ngeno || in->n_ind <= 0 || in->n_loc <= 0 || !in->ploidy || !in->n_alleles ||
+        (!in->alleles && !in->packed2) || (!in->packed2 && (in->vmax <= 0 || in->vmax > 10))) {
+        vp_set_error("vp_genotype_table: missing or empty input");
+        return VP_E_ARG;
+    }
+    const bool p2 = in->packed2 != nullptr;
+    table_facts(in, p2, p2 ? 2 : in->vmax, poly, ngeno);
+    return VP_OK;
+}
 
 extern "C" int vp_dataset_prepare(const vp_input* in, vp_dataset** out) {
     if (!in || !out || in->n_ind <= 0 || in->n_loc <= 0 || !in->ploidy || !in->n_alleles || !in->popid ||
@@ -109,46 +170,19 @@ extern "C" int vp_dataset_prepare(const vp_input* in, vp_dataset** out) {
     auto* d = new vp_dataset();
     d->N = N; d->S = in->n_pop; d->vmax = vmax; d->Nw = Nw; d->packed2 = p2;
 
-    // 1. per input locus: pass flag (polymorphic among typed calls) and id width
+    // 1. per input locus: pass flag (polymorphic in the loader's genotype
+    //    table) and genotype-id width, from the table facts when given
     std::vector<uint8_t> pass(L0, 0), width(L0, 0);
-    parallel_for(L0, [&](int64_t l) {
-        if (in->n_alleles[l] < 2) return;
-        if (p2) {
-            const uint32_t* row = in->packed2 + (size_t)l * Nw;
-            int seen = 0;  // bit c set when code c observed
-            for (int i = 0; i < N; ++i) seen |= 1 << code_at(row, i);
-            int typed = seen & 7;
-            pass[l] = (typed & 2) || ((typed & 5) == 5);
-            int ng = 1 + ((typed & 1) != 0) + ((typed & 2) != 0) + ((typed & 4) != 0);
-            width[l] = (uint8_t)ceil_log2(ng);
-            return;
+    if (in->table_poly && in->table_ngeno) {
+        for (int64_t l = 0; l < L0; ++l) {
+            pass[l] = in->n_alleles[l] >= 2 && in->table_poly[l];
+            width[l] = (uint8_t)ceil_log2(std::max<int32_t>(1, in->table_ngeno[l]));
         }
-        const int8_t* G = in->alleles + (size_t)l * N * vmax;
-        int first = -1, ok = 0;
-        std::vector<uint64_t> keys;
-        keys.reserve(N);
-        uint32_t used = 0;
-        for (int i = 0; i < N; ++i) {
-            const int8_t* g = G + (size_t)i * vmax;
-            int v = in->ploidy[i];
-            used |= 1u << v;
-            if (g[0] < 0) continue;
-            uint64_t h = (uint64_t)v;
-            for (int c = 0; c < v; ++c) {
-                h = h * 64 + (uint64_t)(g[c] + 1);
-                if (g[c] != g[0]) ok = 1;
-            }
-            if (first < 0) first = g[0];
-            else if (g[0] != first) ok = 1;
-            keys.push_back(h);
-        }
-        std::sort(keys.begin(), keys.end());
-        int64_t ng = __builtin_popcount(used);
-        for (size_t j = 0; j < keys.size(); ++j)
-            if (j == 0 || keys[j] != keys[j - 1]) ng++;
-        pass[l] = (uint8_t)ok;
-        width[l] = (uint8_t)ceil_log2(ng);
-    });
+    } else {
+        std::vector<int32_t> ng(L0, 1);
+        table_facts(in, p2, vmax, pass.data(), ng.data());
+        for (int64_t l = 0; l < L0; ++l) width[l] = (uint8_t)ceil_log2(ng[l]);
+    }
     std::vector<int64_t> keep;
     for (int64_t l = 0; l < L0; ++l)
         if (pass[l]) keep.push_back(l);

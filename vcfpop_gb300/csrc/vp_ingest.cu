@@ -25,6 +25,7 @@
 #include <cstring>
 #include <vector>
 
+#include "vp_callfilter.h"
 #include "vp_internal.h"
 
 namespace {
@@ -133,11 +134,12 @@ struct LineOut {
 
 // one CTA per line
 __global__ void __launch_bounds__(PB) k_parse_lines(const char* t, const int64_t* start, int64_t L, int N, int Nw,
-                                                    uint32_t* packed, LineOut out) {
+                                                    uint32_t* packed, LineOut out, vp_call_filter cf) {
     extern __shared__ uint32_t row[];   // [Nw]
     __shared__ int warp_tabs[PB / 32];
     __shared__ int err;
-    __shared__ int nalt_s;
+    __shared__ int nalt_s, dpid_s, gqid_s;
+    __shared__ unsigned long long kept_s;
     const int64_t l = blockIdx.x;
     if (l >= L) return;
     const int64_t s = start[l];
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(PB) k_parse_lines(const char* t, const int64_t
     if (e > s && t[e - 1] == '\n') --e;
     if (e > s && t[e - 1] == '\r') --e;
     for (int w = threadIdx.x; w < Nw; w += PB) row[w] = 0;
-    if (threadIdx.x == 0) { err = 0; nalt_s = 0; }
+    if (threadIdx.x == 0) { err = 0; nalt_s = 0; dpid_s = -1; gqid_s = -1; kept_s = 0; }
     const int64_t len = e - s;
     const int64_t seg = (len + PB - 1) / PB;
     const int64_t a = s + min(len, (int64_t)threadIdx.x * seg), b = s + min(len, (int64_t)(threadIdx.x + 1) * seg);
@@ -165,8 +167,10 @@ __global__ void __launch_bounds__(PB) k_parse_lines(const char* t, const int64_t
     for (int w = 0; w < warp; ++w) before += warp_tabs[w];
     int total = 0;
     for (int w = 0; w < PB / 32; ++w) total += warp_tabs[w];
-    int f = before + incl - mine;   // index of the next tab this thread meets
+    const int f0 = before + incl - mine;   // index of the next tab this thread meets
     if (threadIdx.x == 0 && total != 8 + N) err = 1;   // 9 fixed fields + N samples
+    // the fixed fields first (ALT, FORMAT), then the calls
+    int f = f0;
     for (int64_t p = a; p < b; ++p) {
         if (t[p] != '\t') continue;
         const int field = f + 1;    // the field that starts after this tab
@@ -178,8 +182,25 @@ __global__ void __launch_bounds__(PB) k_parse_lines(const char* t, const int64_t
             for (int64_t r = 0; r < room && q[r] != '\t'; ++r) commas += q[r] == ',';
             nalt_s = commas + 1;
         } else if (field == 8) {   // FORMAT must start with GT
-            if (!(room >= 2 && q[0] == 'G' && q[1] == 'T' && (room == 2 || q[2] == ':' || q[2] == '\t'))) err = 2;
-        } else if (field >= 9) {
+            int dp, gq;
+            uint64_t kept;
+            if (!vp::parse_format(q, room, &dp, &gq, &kept)) err = 2;
+            dpid_s = dp;
+            gqid_s = gq;
+            kept_s = kept;
+        }
+    }
+    __syncthreads();
+    const int dpid = dpid_s, gqid = gqid_s;
+    const uint64_t kept = kept_s;
+    f = f0;
+    for (int64_t p = a; p < b; ++p) {
+        if (t[p] != '\t') continue;
+        const int field = f + 1;
+        ++f;
+        const char* q = t + p + 1;
+        const int64_t room = e - (p + 1);
+        if (field >= 9) {
             const int i = field - 9;
             if (i >= N) { err = 1; continue; }
             // "x/y" or "x|y", x, y in {0, 1, .}, then ':' or tab or end of line
@@ -187,7 +208,8 @@ __global__ void __launch_bounds__(PB) k_parse_lines(const char* t, const int64_t
             const char x = q[0], y = q[2];
             const bool mx = x == '.', my = y == '.';
             if ((!mx && x != '0' && x != '1') || (!my && y != '0' && y != '1')) { err = 3; continue; }
-            const uint32_t code = (mx || my) ? 3u : (uint32_t)((x - '0') + (y - '0'));
+            uint32_t code = (mx || my) ? 3u : (uint32_t)((x - '0') + (y - '0'));
+            if (code != 3u && vp::call_filtered(cf, t, p + 1, e, dpid, gqid, kept, 2)) code = 3u;
             atomicOr(&row[i >> 4], code << (2 * (i & 15)));
         }
     }
@@ -217,17 +239,18 @@ __global__ void __launch_bounds__(PB) k_parse_lines(const char* t, const int64_t
 // ploidy) and nall[l] the alleles of the locus (REF plus the ALT commas + 1).
 __global__ void __launch_bounds__(PB) k_parse_general(const char* t, const int64_t* start, int64_t L, int N, int vmax,
                                                       int8_t* G, int32_t* nall, int32_t* bad, int32_t* ploidy0,
-                                                      int64_t line0) {
+                                                      int64_t line0, vp_call_filter cf) {
     __shared__ int warp_tabs[PB / 32];
     __shared__ int err;
-    __shared__ int nall_s;
+    __shared__ int nall_s, dpid_s, gqid_s;
+    __shared__ unsigned long long kept_s;
     const int64_t l = blockIdx.x;
     if (l >= L) return;
     const int64_t s = start[l];
     int64_t e = start[l + 1];
     if (e > s && t[e - 1] == '\n') --e;
     if (e > s && t[e - 1] == '\r') --e;
-    if (threadIdx.x == 0) { err = 0; nall_s = 0; }
+    if (threadIdx.x == 0) { err = 0; nall_s = 0; dpid_s = -1; gqid_s = -1; kept_s = 0; }
     const int64_t len = e - s;
     const int64_t seg = (len + PB - 1) / PB;
     const int64_t a = s + min(len, (int64_t)threadIdx.x * seg), b = s + min(len, (int64_t)(threadIdx.x + 1) * seg);
@@ -244,8 +267,10 @@ __global__ void __launch_bounds__(PB) k_parse_general(const char* t, const int64
     int before = 0, total = 0;
     for (int w = 0; w < warp; ++w) before += warp_tabs[w];
     for (int w = 0; w < PB / 32; ++w) total += warp_tabs[w];
-    int f = before + incl - mine;
+    const int f0 = before + incl - mine;
     if (threadIdx.x == 0 && total != 8 + N) err = 1;
+    // the fixed fields first (ALT, FORMAT), then the calls
+    int f = f0;
     for (int64_t p = a; p < b; ++p) {
         if (t[p] != '\t') continue;
         const int field = f + 1;
@@ -257,8 +282,25 @@ __global__ void __launch_bounds__(PB) k_parse_general(const char* t, const int64
             for (int64_t r = 0; r < room && q[r] != '\t'; ++r) commas += q[r] == ',';
             nall_s = commas + 2;
         } else if (field == 8) {
-            if (!(room >= 2 && q[0] == 'G' && q[1] == 'T' && (room == 2 || q[2] == ':' || q[2] == '\t'))) err = 2;
-        } else if (field >= 9) {
+            int dp, gq;
+            uint64_t kept;
+            if (!vp::parse_format(q, room, &dp, &gq, &kept)) err = 2;
+            dpid_s = dp;
+            gqid_s = gq;
+            kept_s = kept;
+        }
+    }
+    __syncthreads();
+    const int dpid = dpid_s, gqid = gqid_s;
+    const uint64_t kept = kept_s;
+    f = f0;
+    for (int64_t p = a; p < b; ++p) {
+        if (t[p] != '\t') continue;
+        const int field = f + 1;
+        ++f;
+        const char* q = t + p + 1;
+        const int64_t room = e - (p + 1);
+        if (field >= 9) {
             const int i = field - 9;
             if (i >= N) { err = 1; continue; }
             int al[16];
@@ -291,7 +333,7 @@ __global__ void __launch_bounds__(PB) k_parse_general(const char* t, const int64
             if (l == 0 && line0 == 0) ploidy0[i] = n;
             int8_t* out = G + ((size_t)l * N + i) * vmax;
             for (int c = 0; c < vmax; ++c) out[c] = -1;
-            if (miss) continue;
+            if (miss || vp::call_filtered(cf, t, p + 1, e, dpid, gqid, kept, n)) continue;
             // ascending order (insertion sort of at most 16)
             for (int x = 1; x < n; ++x) {
                 const int v = al[x];
@@ -431,6 +473,13 @@ int open_device(int device, cudaStream_t* st) {
 
 extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int device, uint32_t* packed,
                             int64_t max_loci, int64_t* line_start, int64_t* n_loc) {
+    return vp_vcf_pack2_ex(text, bytes, n_ind, device, packed, max_loci, line_start, n_loc, nullptr);
+}
+
+extern "C" int vp_vcf_pack2_ex(const char* text, size_t bytes, int32_t n_ind, int device, uint32_t* packed,
+                               int64_t max_loci, int64_t* line_start, int64_t* n_loc, const vp_call_filter* cf) {
+    const vp_call_filter none{};
+    if (!cf) cf = &none;
     if (!text || !n_loc || n_ind <= 0 || (max_loci > 0 && !packed)) { vp_set_error("bad arguments"); return VP_E_ARG; }
     const int Nw = (n_ind + 15) / 16;
     if ((size_t)Nw * 4 > 200 * 1024) { vp_set_error("too many samples for one line row in shared memory"); return VP_E_ARG; }
@@ -455,7 +504,7 @@ extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int d
         for (int64_t l0 = 0; l0 < L; l0 += 1 << 30) {
             const unsigned nb = (unsigned)std::min<int64_t>(L - l0, 1 << 30);
             k_parse_lines<<<nb, PB, (size_t)Nw * 4, st>>>(ix.dt, ix.starts + l0, nb, n_ind, Nw, dp + l0 * Nw,
-                                                          LineOut{flags + l0, flags + L + l0});
+                                                          LineOut{flags + l0, flags + L + l0}, *cf);
         }
         if ((e = cudaGetLastError()) != cudaSuccess) {
             vp_set_error("parse launch failed: %s", cudaGetErrorString(e));
@@ -491,6 +540,15 @@ extern "C" int vp_vcf_pack2(const char* text, size_t bytes, int32_t n_ind, int d
 
 extern "C" int vp_vcf_parse(const char* text, size_t bytes, int32_t n_ind, int32_t vmax, int device, int8_t* alleles,
                             int32_t* n_alleles, int32_t* ploidy, int64_t max_loci, int64_t* line_start, int64_t* n_loc) {
+    return vp_vcf_parse_ex(text, bytes, n_ind, vmax, device, alleles, n_alleles, ploidy, max_loci, line_start, n_loc,
+                           nullptr);
+}
+
+extern "C" int vp_vcf_parse_ex(const char* text, size_t bytes, int32_t n_ind, int32_t vmax, int device, int8_t* alleles,
+                               int32_t* n_alleles, int32_t* ploidy, int64_t max_loci, int64_t* line_start,
+                               int64_t* n_loc, const vp_call_filter* cf) {
+    const vp_call_filter none{};
+    if (!cf) cf = &none;
     if (!text || !n_loc || n_ind <= 0 || vmax < 1 || vmax > 16 ||
         (max_loci > 0 && (!alleles || !n_alleles || !ploidy))) {
         vp_set_error("bad arguments");
@@ -520,7 +578,7 @@ extern "C" int vp_vcf_parse(const char* text, size_t bytes, int32_t n_ind, int32
         for (int64_t l0 = 0; l0 < L; l0 += 1 << 30) {
             const unsigned nb = (unsigned)std::min<int64_t>(L - l0, 1 << 30);
             k_parse_general<<<nb, PB, 0, st>>>(ix.dt, ix.starts + l0, nb, n_ind, vmax, dG + (size_t)l0 * n_ind * vmax,
-                                               dnall + l0, flags + l0, dploidy, l0);
+                                               dnall + l0, flags + l0, dploidy, l0, *cf);
         }
         if ((e = cudaGetLastError()) != cudaSuccess) {
             vp_set_error("parse launch failed: %s", cudaGetErrorString(e));

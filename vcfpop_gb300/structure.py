@@ -230,24 +230,40 @@ class Chain:
             self.close()
 
 
-def vcf_pack2(text: bytes, n_ind: int, device: int = 0):
+def call_filter(dp=None, gq=None, ploidy=None):
+    """The genotype filter of -f_dp, -f_gq, -f_ploidy: each window a (min,
+    max) pair or None (not used). None when no window is used."""
+    if dp is None and gq is None and ploidy is None:
+        return None
+    cf = B.VpCallFilter()
+    for name, w in (("dp", dp), ("gq", gq), ("ploidy", ploidy)):
+        if w is not None:
+            setattr(cf, name + "_b", 1)
+            setattr(cf, name + "_min", int(w[0]))
+            setattr(cf, name + "_max", int(w[1]))
+    return cf
+
+
+def vcf_pack2(text: bytes, n_ind: int, device: int = 0, calls=None):
     """Parse the data lines of a biallelic diploid VCF on the device: returns
-    (packed [L][ceil(N/16)] uint32 2-bit codes, line offsets [L + 1])."""
+    (packed [L][ceil(N/16)] uint32 2-bit codes, line offsets [L + 1]). calls:
+    a genotype filter (call_filter) applied as the calls are decoded."""
     buf = np.frombuffer(text, dtype=np.uint8)
     # a well-formed line holds 9 fields and n_ind calls of 3 bytes, each after a tab
     L = len(text) // (4 * n_ind + 17) + 1
     packed = np.empty((L, (n_ind + 15) // 16), np.uint32)
     starts = np.empty(L + 1, np.int64)
     n = C.c_int64()
-    B.check(B.lib().vp_vcf_pack2(buf.ctypes.data, len(text), n_ind, device, packed.ctypes.data, max(L, 1),
-                                 starts.ctypes.data, C.byref(n)))
+    B.check(B.lib().vp_vcf_pack2_ex(buf.ctypes.data, len(text), n_ind, device, packed.ctypes.data, max(L, 1),
+                                    starts.ctypes.data, C.byref(n), C.byref(calls) if calls is not None else None))
     return packed[:n.value], starts[:n.value + 1]
 
 
-def vcf_parse(text: bytes, n_ind: int, vmax: int, device: int = 0):
+def vcf_parse(text: bytes, n_ind: int, vmax: int, device: int = 0, calls=None):
     """Parse the data lines of a VCF of any ploidy and allele count on the
     device: (alleles [L][N][vmax] int8, ascending, -1 missing; alleles per
-    locus [L]; ploidy of each sample's first call [N]; line offsets [L + 1])."""
+    locus [L]; ploidy of each sample's first call [N]; line offsets [L + 1]).
+    calls: a genotype filter (call_filter)."""
     buf = np.frombuffer(text, dtype=np.uint8)
     n = C.c_int64()
     B.check(B.lib().vp_vcf_parse(buf.ctypes.data, len(text), n_ind, vmax, device, None, None, None, 0, None,
@@ -258,8 +274,9 @@ def vcf_parse(text: bytes, n_ind: int, vmax: int, device: int = 0):
     ploidy = np.empty(n_ind, np.int32)
     starts = np.empty(L + 1, np.int64)
     if L:
-        B.check(B.lib().vp_vcf_parse(buf.ctypes.data, len(text), n_ind, vmax, device, G.ctypes.data, k.ctypes.data,
-                                     ploidy.ctypes.data, L, starts.ctypes.data, C.byref(n)))
+        B.check(B.lib().vp_vcf_parse_ex(buf.ctypes.data, len(text), n_ind, vmax, device, G.ctypes.data,
+                                        k.ctypes.data, ploidy.ctypes.data, L, starts.ctypes.data, C.byref(n),
+                                        C.byref(calls) if calls is not None else None))
     return G, k, ploidy, starts
 
 
