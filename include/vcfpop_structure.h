@@ -422,6 +422,19 @@ typedef struct {
  * undefined (fewer than 2 alleles). Host buffers; synchronous. */
 int vp_locus_filter_pack2(const uint32_t* packed, int64_t n_loc, int32_t n_ind, const vp_locus_filter* f, int device,
                           uint8_t* keep, double* stats);
+/* The same for the general genotype layout (vp_input.alleles: [n_loc][n_ind]
+ * [vmax] allele indices, -1 missing; any ploidy up to 10, n_alleles[l] up to
+ * 64). The statistics are CalcDiversity's over the locus' genotype table in
+ * order of first appearance (the REAL sums run in that order) among the
+ * calls of alleles_table (the calls before the genotype filter, same layout;
+ * NULL: alleles), counted over alleles; the HWE p-value comes from the test
+ * with allele collapsing (src/diversity.cpp:337-492) for the default
+ * genotype model (no -f_model), NaN with mixed ploidy at the locus, and the
+ * chi-square upper tail by the regularized incomplete gamma function. A
+ * locus with more than 512 distinct genotypes fails with VP_E_ARG. */
+int vp_locus_filter_general(const int8_t* alleles, const int8_t* alleles_table, int64_t n_loc, int32_t n_ind,
+                            int32_t vmax, const int32_t* n_alleles, const vp_locus_filter* f, int device,
+                            uint8_t* keep, double* stats);
 
 /* ---- serving: many independent runs on one device ------------------------
  * Replaces the reference's run scheduling (BAYESIAN<REAL>::CalcBayesian and

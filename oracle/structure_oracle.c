@@ -1420,3 +1420,291 @@ void orc_locus_filter_pack2(const uint32_t* packed, int64_t L, int n_ind, const 
         }
     }
 }
+
+/* ---- locus statistics of any ploidy and allele count ---------------------
+ * DIVERSITY::CalcDiversity (diversity.cpp:144-492) for the general genotype
+ * layout, and MarkerDiversity's windows (filter.cpp:494-507). The locus'
+ * genotype table lists its typed genotypes in order of first appearance
+ * (the loader's table, load.cpp:2180-2230): the sums over genotypes run in
+ * that order, in the reference's REAL. */
+
+/* one genotype: ploidy, sorted alleles, its count, and its dosage pattern:
+ * distinct alleles by descending copy count, ties by the larger allele first
+ * (GENOTYPE::GENOTYPE, function.cpp:259-337) */
+typedef struct {
+    int v, na;
+    int al[16], key[16], cnt[16];
+    unsigned count;
+} orc_gtype;
+
+static void orc_gtype_pattern(orc_gtype* g) {
+    g->na = 0;
+    for (int i = 0; i < g->v; ++i) {
+        int isnew = 1;
+        for (int j = i - 1; j >= 0; --j) if (g->al[i] == g->al[j]) { isnew = 0; break; }
+        if (!isnew) continue;
+        int ac = 1;
+        for (int j = i + 1; j < g->v; ++j) ac += g->al[j] == g->al[i];
+        g->key[g->na] = g->al[i];
+        g->cnt[g->na++] = ac;
+    }
+    for (int i = 0; i < g->na; ++i)
+        for (int j = i + 1; j < g->na; ++j)
+            if (g->cnt[i] < g->cnt[j] || (g->cnt[i] == g->cnt[j] && g->key[i] < g->key[j])) {
+                int t = g->cnt[i]; g->cnt[i] = g->cnt[j]; g->cnt[j] = t;
+                t = g->key[i]; g->key[i] = g->key[j]; g->key[j] = t;
+            }
+}
+
+/* GENOTYPE::HIndex: the share of ordered pairs of copies that differ, as
+ * the reference's table holds it, a literal of 15 decimals: the double
+ * nearest to round(p / q x 10^15) / 10^15 (0 for one copy) */
+static double orc_hindex(const orc_gtype* g) {
+    const long long q = (long long)g->v * (g->v - 1);
+    if (q == 0) return 0;
+    long long same = 0;
+    for (int i = 0; i < g->na; ++i) same += (long long)g->cnt[i] * (g->cnt[i] - 1);
+    const long long p = q - same;
+    const long long n15 = (2 * p * 1000000000000000LL + q) / (2 * q);
+    return (double)n15 / 1e15;
+}
+
+/* GENOTYPE::HWECoef: the multinomial coefficient v! / prod cnt! */
+static double orc_hwecoef(const orc_gtype* g) {
+    double f = 1;
+    for (int i = 2; i <= g->v; ++i) f *= i;
+    for (int a = 0; a < g->na; ++a)
+        for (int i = 2; i <= g->cnt[a]; ++i) f /= i;
+    return f;
+}
+
+/* IntegerPower (math2.h:307-350) in double */
+static double orc_ipow(double x, int n) {
+    switch (n) {
+        case 0: return 1;
+        case 1: return x;
+        case 2: return x * x;
+        case 3: return x * x * x;
+        case 4: { double x2 = x * x; return x2 * x2; }
+        case 5: { double x2 = x * x; return x2 * x2 * x; }
+        case 6: { double x3 = x * x * x; return x3 * x3; }
+        case 7: { double x3 = x * x * x; return x3 * x3 * x; }
+        case 8: { double x2 = x * x, x4 = x2 * x2; return x4 * x4; }
+        case 9: { double x3 = x * x * x; return x3 * x3 * x3; }
+        case 10: { double x2 = x * x, x4 = x2 * x2; return x4 * x4 * x2; }
+        default: return pow(x, (double)n);
+    }
+}
+
+/* the upper tail of the chi-square distribution with df degrees of freedom:
+ * erfc for df = 1 (as the biallelic kernel), else 1 - P(df/2, x/2), the
+ * regularized lower incomplete gamma function by its series (x < a + 1) or
+ * its continued fraction (Numerical Recipes, 6.2) */
+static double orc_chi2_upper(double x, int df) {
+    if (df == 1) return 1.0 - erf(sqrt(0.5 * x));
+    const double a = 0.5 * df, z = 0.5 * x;
+    if (z <= 0) return 1;
+    const double lg = lgamma(a);
+    if (z < a + 1) {
+        double ap = a, sum = 1.0 / a, del = sum;
+        for (int n = 0; n < 1000; ++n) { ap += 1; del *= z / ap; sum += del; if (fabs(del) < fabs(sum) * 1e-16) break; }
+        return 1.0 - sum * exp(-z + a * log(z) - lg);
+    }
+    double b = z + 1 - a, c = 1.0 / 1e-300, d = 1.0 / b, h = d;
+    for (int i = 1; i < 1000; ++i) {
+        const double an = -i * (i - a);
+        b += 2;
+        d = an * d + b; if (fabs(d) < 1e-300) d = 1e-300;
+        c = b + an / c; if (fabs(c) < 1e-300) c = 1e-300;
+        d = 1.0 / d;
+        const double del = d * c;
+        h *= del;
+        if (fabs(del - 1) < 1e-16) break;
+    }
+    return exp(-z + a * log(z) - lg) * h;
+}
+
+#define ORC_GENERAL_STATS(NAME, REAL, LOG)                                                                      \
+static void NAME(orc_gtype* tab, int ng, int k2, int ni, double* out) {                                        \
+    const double MINF = 1e-10, NANV = 0.0 / 0.0;                                                               \
+    REAL fre[64], ho = 0, how = 0;                                                                             \
+    for (int a = 0; a < k2; ++a) fre[a] = 0;                                                                   \
+    int n = 0, nhaplo = 0, minp = 100, maxp = 0, varploidy = 0;                                                \
+    for (int gi = 0; gi < ng; ++gi) {                                                                          \
+        const orc_gtype* g = tab + gi;                                                                         \
+        if (!g->count) continue;                                                                               \
+        const unsigned c = g->count;                                                                           \
+        const int v = g->v;                                                                                    \
+        nhaplo += v * c;                                                                                       \
+        if (v > maxp) maxp = v;                                                                                \
+        if (v < minp) minp = v;                                                                                \
+        if (maxp != minp) varploidy = 1;                                                                       \
+        ho += orc_hindex(g) * c * v * (v - 1);                                                                 \
+        how += c * v * (v - 1);                                                                                \
+        n += c;                                                                                                \
+        for (int i = 0; i < v; ++i) fre[g->al[i]] += c;                                                        \
+    }                                                                                                          \
+    const REAL ptype = n / (REAL)ni;                                                                           \
+    {   /* Unify (math2.cpp:2268-2304) */                                                                      \
+        double s = 0;                                                                                          \
+        for (int a = 0; a < k2; ++a) s += fre[a];                                                              \
+        const double invsum = 1.0 / (s + k2 * MINF);                                                           \
+        for (int a = 0; a < k2; ++a) fre[a] = (REAL)(((double)fre[a] + MINF) * invsum);                       \
+    }                                                                                                          \
+    int k = 0;                                                                                                 \
+    if (n) for (int a = 0; a < k2; ++a) k += fre[a] > MINF;                                                    \
+    double bmaf = NANV, he = NANV, hoo = NANV, pic = NANV, ae = NANV, I = NANV, pval = NANV;                   \
+    if (k >= 2) {                                                                                              \
+        hoo = ho / how;                                                                                        \
+        REAL b = 1, a2 = 0, picv = 0, Iv = 0;                                                                  \
+        const int nh = (int)(nhaplo + 0.5);                                                                    \
+        for (int a = 0; a < k2; ++a) {                                                                         \
+            const REAL af = fre[a];                                                                            \
+            if (af * nh < 1e-5) continue;                                                                      \
+            if (af > 1e-5) Iv += -af * LOG(af);                                                                \
+            if (b > af) b = af;                                                                                \
+            a2 += af * af;                                                                                     \
+            for (int c = a + 1; c < k2; ++c)                                                                   \
+                if (fre[c] > 0) picv += 2 * af * fre[c] * (1 - af * fre[c]);                                  \
+        }                                                                                                      \
+        if (b > 0.5) b = 1 - b;                                                                                \
+        bmaf = b; he = (REAL)(1 - a2); ae = (REAL)(1 / a2); I = Iv; pic = picv;                               \
+        if (!varploidy) {                                                                                      \
+            /* HWE G-test with allele collapsing (diversity.cpp:337-492), genotype model 0 */                  \
+            const int ploidy = maxp;                                                                           \
+            orc_gtype* t1 = malloc(sizeof(orc_gtype) * (size_t)(ng + 1));                                      \
+            orc_gtype* t2 = malloc(sizeof(orc_gtype) * (size_t)(ng + 1));                                      \
+            int n1 = 0;                                                                                        \
+            for (int gi = 0; gi < ng; ++gi) t1[n1++] = tab[gi];                                                \
+            REAL f1[64], f2[64];                                                                               \
+            int amap[64];                                                                                      \
+            for (int a = 0; a < k2; ++a) f1[a] = fre[a];                                                       \
+            REAL G = 0;                                                                                        \
+            int flag = 0;                                                                                      \
+            for (int kk = k2; kk >= 1 && !flag; kk = (kk <= k ? kk - 1 : k)) {                                 \
+                if (kk == 1) break;                                                                            \
+                for (int a = 0; a < kk; ++a) f2[a] = 0;                                                        \
+                if (kk <= k) {                                                                                 \
+                    flag = 1;                                                                                  \
+                    G = 0;                                                                                     \
+                    for (int gi = 0; gi < n1; ++gi) {                                                          \
+                        const orc_gtype* g = t1 + gi;                                                          \
+                        if (!g->count) continue;                                                               \
+                        double gfz = orc_hwecoef(g);                                                           \
+                        for (int ai = g->na - 1; ai >= 0; --ai) gfz *= orc_ipow((double)f1[g->key[ai]], g->cnt[ai]); \
+                        const REAL obs = (REAL)g->count, ex = (REAL)(gfz * n);                                  \
+                        if (ex < 5) { flag = 0; break; }                                                       \
+                        G += 2 * obs * LOG(obs / ex);                                                          \
+                    }                                                                                          \
+                }                                                                                              \
+                if (flag) {                                                                                    \
+                    /* df = C(ploidy + kk - 1, ploidy) - kk (Binomial via factorials) */                       \
+                    double bin = 1;                                                                            \
+                    for (int i = 2; i <= ploidy + kk - 1; ++i) bin *= i;                                       \
+                    for (int i = 2; i <= ploidy; ++i) bin /= i;                                                \
+                    for (int i = 2; i <= kk - 1; ++i) bin /= i;                                                \
+                    const int df = (int)(bin - kk + 0.5);                                                      \
+                    pval = (REAL)orc_chi2_upper((double)G, df);                                                \
+                    break;                                                                                     \
+                }                                                                                              \
+                if (kk <= k) {                                                                                 \
+                    /* merge the two rarest alleles (GetMinID: the first minimum) */                           \
+                    int m1 = 0;                                                                                \
+                    for (int a = 1; a < kk; ++a) if (f1[m1] > f1[a]) m1 = a;                                   \
+                    f1[m1]++;                                                                                  \
+                    int m2 = 0;                                                                                \
+                    for (int a = 1; a < kk; ++a) if (f1[m2] > f1[a]) m2 = a;                                   \
+                    f1[m1]--;                                                                                  \
+                    if (m1 > m2) { int t = m1; m1 = m2; m2 = t; }                                              \
+                    for (int j = 0, p = 0; j < kk; ++j) {                                                      \
+                        if (j == m2) { amap[j] = m1; f2[m1] = f1[m1] + f1[m2]; }                               \
+                        else { amap[j] = p; f2[p++] = f1[j]; }                                                 \
+                    }                                                                                          \
+                } else {                                                                                       \
+                    /* drop absent alleles onto the most frequent one (GetMaxID: the first maximum) */          \
+                    int m1 = 0;                                                                                \
+                    for (int a = 1; a < kk; ++a) if (f1[m1] < f1[a]) m1 = a;                                   \
+                    for (int j = 0, p = 0; j < kk; ++j) amap[j] = f1[j] < MINF ? -1 : p++;                     \
+                    for (int j = 0; j < kk; ++j) amap[j] = amap[j] == -1 ? amap[m1] : amap[j];                 \
+                }                                                                                              \
+                /* the collapsed genotype table, in order of first mapping */                                  \
+                int n2 = 0;                                                                                    \
+                for (int gi = 0; gi < n1; ++gi) {                                                              \
+                    const orc_gtype* g = t1 + gi;                                                              \
+                    if (!g->count) continue;                                                                   \
+                    orc_gtype h;                                                                               \
+                    h.v = ploidy;                                                                              \
+                    for (int ai = 0; ai < ploidy; ++ai) h.al[ai] = amap[g->al[ai]];                            \
+                    for (int x = 1; x < ploidy; ++x) {                                                         \
+                        const int y0 = h.al[x]; int y = x - 1;                                                 \
+                        while (y >= 0 && h.al[y] > y0) { h.al[y + 1] = h.al[y]; --y; }                         \
+                        h.al[y + 1] = y0;                                                                      \
+                    }                                                                                          \
+                    for (int j = 0; j < ploidy; ++j) f2[h.al[j]] += g->count;                                  \
+                    int found = -1;                                                                            \
+                    for (int x = 0; x < n2 && found < 0; ++x)                                                  \
+                        if (!memcmp(t2[x].al, h.al, sizeof(int) * (size_t)ploidy)) found = x;                  \
+                    if (found < 0) { h.count = g->count; orc_gtype_pattern(&h); t2[n2++] = h; }                \
+                    else t2[found].count += g->count;                                                          \
+                }                                                                                              \
+                {   double s = 0;                                                                              \
+                    for (int a = 0; a < kk; ++a) s += f2[a];                                                   \
+                    const double invsum = 1.0 / (s + kk * MINF);                                               \
+                    for (int a = 0; a < kk; ++a) f2[a] = (REAL)(((double)f2[a] + MINF) * invsum);             \
+                }                                                                                              \
+                orc_gtype* tt = t1; t1 = t2; t2 = tt; n1 = n2;                                                 \
+                for (int a = 0; a < kk; ++a) f1[a] = f2[a];                                                    \
+            }                                                                                                  \
+            free(t1); free(t2);                                                                                \
+        }                                                                                                      \
+    }                                                                                                          \
+    out[0] = n; out[1] = k; out[2] = ptype; out[3] = bmaf; out[4] = he; out[5] = hoo; out[6] = pic;           \
+    out[7] = ae; out[8] = I; out[9] = pval;                                                                    \
+}
+ORC_GENERAL_STATS(orc_general_stats_f, float, logf)
+ORC_GENERAL_STATS(orc_general_stats_d, double, log)
+
+void orc_locus_filter_general(const int8_t* G, const int8_t* Gtable, int64_t L, int n_ind, int vmax,
+                              const int32_t* k, const orc_locus_filter* f, uint8_t* keep, double* stats) {
+    orc_gtype* tab = malloc(sizeof(orc_gtype) * (size_t)(n_ind + 1));
+    for (int64_t l = 0; l < L; ++l) {
+        /* the table's order: first appearance among the calls the loader saw
+         * (Gtable, before the genotype filter); its counts: the calls kept */
+        int ng = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+            const int8_t* src = pass == 0 ? (Gtable ? Gtable : G) : G;
+            for (int i = 0; i < n_ind; ++i) {
+                const int8_t* g = src + ((size_t)l * n_ind + i) * vmax;
+                if (g[0] < 0) continue;
+                orc_gtype h;
+                memset(&h, 0, sizeof h);
+                h.v = 0;
+                int bad = 0;
+                while (h.v < vmax && g[h.v] >= 0) { bad |= g[h.v] >= k[l]; h.al[h.v] = g[h.v]; h.v++; }
+                if (bad) continue;   /* an allele outside the locus' alleles: missing */
+                int found = -1;
+                for (int x = 0; x < ng && found < 0; ++x)
+                    if (tab[x].v == h.v && !memcmp(tab[x].al, h.al, sizeof(int) * (size_t)h.v)) found = x;
+                if (pass == 0) {
+                    if (found < 0) { orc_gtype_pattern(&h); h.count = 0; tab[ng++] = h; }
+                } else if (found >= 0) tab[found].count++;
+            }
+        }
+        double o[10];
+        if (f->single) orc_general_stats_f(tab, ng, k[l], n_ind, o);
+        else orc_general_stats_d(tab, ng, k[l], n_ind, o);
+        const int kk = (int)o[1], nn = (int)o[0];
+#define OUT(v, lo, hi) ((v) < (lo) || (v) > (hi))
+        const int fail = kk == 0 || (f->bmaf_b && kk == 2 && OUT(o[3], f->bmaf_min, f->bmaf_max)) ||
+                         (f->k_b && (kk < f->k_min || kk > f->k_max)) || (f->n_b && (nn < f->n_min || nn > f->n_max)) ||
+                         (f->ptype_b && OUT(o[2], f->ptype_min, f->ptype_max)) ||
+                         (f->he_b && OUT(o[4], f->he_min, f->he_max)) || (f->ho_b && OUT(o[5], f->ho_min, f->ho_max)) ||
+                         (f->pic_b && OUT(o[6], f->pic_min, f->pic_max)) || (f->ae_b && OUT(o[7], f->ae_min, f->ae_max)) ||
+                         (f->I_b && OUT(o[8], f->I_min, f->I_max)) ||
+                         (f->pval_b && o[9] != -1 && OUT(o[9], f->pval_min, f->pval_max));
+#undef OUT
+        keep[l] = fail ? 0 : 1;
+        if (stats) memcpy(stats + l * 10, o, sizeof o);
+    }
+    free(tab);
+}

@@ -188,6 +188,14 @@ typedef struct {
 } orc_locus_filter;
 void orc_locus_filter_pack2(const uint32_t* packed, int64_t L, int n_ind, const orc_locus_filter* f, uint8_t* keep,
                             double* stats);
+/* The same windows for the general genotype layout G[L][n_ind][vmax] (any
+ * ploidy, k[l] alleles per locus, up to 64): the statistics of
+ * CalcDiversity over the locus' genotype table in order of first appearance
+ * among the calls of Gtable (the calls before the genotype filter; NULL: G),
+ * counted over G, and the HWE test with allele collapsing for genotype model
+ * 0 (diversity.cpp:337-492; no test with mixed ploidy at the locus). */
+void orc_locus_filter_general(const int8_t* G, const int8_t* Gtable, int64_t L, int n_ind, int vmax,
+                              const int32_t* k, const orc_locus_filter* f, uint8_t* keep, double* stats);
 
 /* WriteStructure's heterozygosity and net nucleotide distance
  * (structure.cpp:293-324) on mean frequencies freqm[K][KT] of L loci with

@@ -177,6 +177,14 @@ CASES = {
                                     "-f_windowstat=ptype", "-f_dp=[10,60]", "-structure_krange=[2,2]",
                                     "-structure_nburnin=10", "-structure_nreps=20", "-structure_nadmburnin=0",
                                     "-structure_admix=no", "-structure_diversity=yes"]),
+    # the locus windows and the window filter on polyploid multiallelic data
+    "poly_filter": ("poly", 26, ["-f", "-f_k=[3,8]", "-f_he=[0.4,0.78]", "-f_ho=[0.3,0.76]", "-f_ae=[1.6,4.6]",
+                                 "-f_ptype=[0.96,1]", "-f_pic=[0.3,0.75]", "-f_I=[0.6,1.68]", "-f_n=[110,120]",
+                                 "-structure_admix=no", "-structure_krange=[2,2]", "-structure_nburnin=10",
+                                 "-structure_nreps=20", "-structure_nadmburnin=5", "-structure_diversity=yes"]),
+    "polyfmt_window": ("polyfmt", 27, ["-f", "-f_windowsize=2000", "-f_windowstat=pic", "-f_he=[0.3,0.9]",
+                                       "-f_dp=[5,70]", "-structure_admix=yes", "-structure_krange=[2,2]",
+                                       "-structure_nburnin=10", "-structure_nreps=20", "-structure_diversity=yes"]),
     "fmt_window_all": ("fmt", 25, ["-f", "-f_windowsize=3000", "-f_windowstat=ho", "-structure_krange=[2,2]",
                                    "-structure_nburnin=10", "-structure_nreps=20", "-structure_nadmburnin=0",
                                    "-structure_admix=no", "-structure_diversity=yes"]),

@@ -78,6 +78,8 @@ def lib():
         L.orc_vcf_pack2_ex.argtypes = [P, C.c_size_t, C.c_int, P, C.c_int64, C.POINTER(CallFilter)]
         L.orc_vcf_pack2_ex.restype = C.c_int64
         L.orc_locus_filter_pack2.argtypes = [P, C.c_int64, C.c_int, P, P, P]
+        L.orc_locus_filter_general.argtypes = [P, P, C.c_int64, C.c_int, C.c_int, P, P, P, P]
+        L.orc_locus_filter_general.restype = None
         L.orc_locus_filter_pack2.restype = None
         L.orc_vcf_pack2.restype = C.c_int64
         L.orc_hash_ulong_c.restype = C.c_uint32
@@ -246,4 +248,17 @@ def locus_filter_pack2(packed, n_ind, f):
     keep = np.zeros(L, np.uint8)
     stats = np.zeros((L, 10))
     lib().orc_locus_filter_pack2(packed.ctypes.data, L, n_ind, C.byref(f), keep.ctypes.data, stats.ctypes.data)
+    return keep, stats
+
+
+def locus_filter_general(G, n_alleles, f, table=None):
+    """The oracle's locus filter for the general genotype layout G[L][N][vmax]."""
+    G = np.ascontiguousarray(G, np.int8)
+    L, N, vmax = G.shape
+    k = np.ascontiguousarray(n_alleles, np.int32)
+    T = None if table is None else np.ascontiguousarray(table, np.int8)
+    keep = np.zeros(L, np.uint8)
+    stats = np.zeros((L, 10))
+    lib().orc_locus_filter_general(G.ctypes.data, None if T is None else T.ctypes.data, L, N, vmax, k.ctypes.data,
+                                   C.byref(f), keep.ctypes.data, stats.ctypes.data)
     return keep, stats

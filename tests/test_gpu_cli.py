@@ -65,7 +65,8 @@ def test_cli_reference_streams_follow_golden_trace(case, tmp_path):
         assert abs(g - w) <= 1e-5 * abs(w), (g, w)
 
 
-@pytest.mark.parametrize("case", ["c1_filter", "fmt_window", "fmt_window_stat", "fmt_window_all"])
+@pytest.mark.parametrize("case", ["c1_filter", "fmt_window", "fmt_window_stat", "fmt_window_all", "poly_filter",
+                                  "polyfmt_window"])
 def test_cli_locus_filter_keeps_the_reference_loci(case, tmp_path):
     """-f with locus filters: the diversity table lists the loci the reference
     program kept, by name, in its order. The cases cover the diversity

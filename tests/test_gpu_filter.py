@@ -56,3 +56,48 @@ def test_every_window_with_edge_loci(single):
     for w in windows:
         keep = _compare(packed, 333, S.locus_filter_spec(single=single, **w))
         assert not keep[:20].any()
+
+
+def _compare_general(G, k, f, table=None):
+    keep, stats = S.locus_filter_general(G, k, f, table=table)
+    okeep, ostats = orc.locus_filter_general(G, k, _orc_filter(f), table=table)
+    assert np.array_equal(keep, okeep)
+    both = ~np.isnan(ostats)
+    assert np.array_equal(np.isnan(stats), np.isnan(ostats))
+    assert np.array_equal(stats[:, :8][both[:, :8]], ostats[:, :8][both[:, :8]])
+    assert np.allclose(stats[:, 8][both[:, 8]], ostats[:, 8][both[:, 8]], rtol=1e-6)
+    # the HWE p-value: its G statistic's logs and the tail function may differ
+    # in the last places between the device and the host
+    assert np.allclose(stats[:, 9][both[:, 9]], ostats[:, 9][both[:, 9]], rtol=1e-5, atol=1e-12)
+    return keep, stats
+
+
+@pytest.mark.parametrize("single", [1, 0])
+def test_general_statistics_on_device_equal_the_oracle(single):
+    """vp_locus_filter_general against the oracle, which is pinned to the
+    loci the reference program kept (test_oracle_general_locus_filter_matches_
+    reference): ploidy 2/4/6 with 2-8 alleles (mixed ploidy: no HWE test),
+    diploid data with 2-6 alleles (the HWE test with allele collapsing and
+    the chi-square tail of 1 to 15 degrees of freedom), tetraploid data, a
+    table order taken from other calls, and every window at once."""
+    rng = np.random.default_rng(20 + single)
+    poly = synth.fmodel(8, 160, 400, 3, 0.08, 0.03, ploidy=np.array([2, 2, 4, 6] * 40),
+                        n_alleles=rng.integers(2, 9, 400), anc_alpha=1.0)
+    dip = synth.fmodel(9, 300, 400, 3, 0.05, 0.03, n_alleles=rng.integers(2, 7, 400), anc_alpha=1.0)
+    tet = synth.fmodel(10, 200, 300, 2, 0.05, 0.02, ploidy=np.full(200, 4), n_alleles=rng.integers(2, 5, 300),
+                       anc_alpha=1.0)
+    for d in (poly, dip, tet):
+        f = S.locus_filter_spec(single=bool(single))
+        _, st = _compare_general(d["G"], d["k"], f)
+    # the diploid set has defined p-values over several degrees of freedom
+    _, st = _compare_general(dip["G"], dip["k"], S.locus_filter_spec(single=bool(single)))
+    assert np.isfinite(st[:, 9]).sum() > 100
+    # windows on every statistic
+    f = S.locus_filter_spec(single=bool(single), k=(3, 7), he=(0.3, 0.8), ho=(0.2, 0.9), pic=(0.2, 0.8),
+                            ae=(1.5, 5), I=(0.5, 2), ptype=(0.9, 1), n=(100, 300), bmaf=(0.05, 0.5), pval=(0.01, 1))
+    keep, _ = _compare_general(dip["G"], dip["k"], f)
+    assert 0 < keep.sum() < len(keep)
+    # the genotype tables ordered by other calls (as the calls before a genotype filter)
+    G2 = dip["G"].copy()
+    G2[rng.random(G2.shape[:2]) < 0.2] = -1
+    _compare_general(G2, dip["k"], S.locus_filter_spec(single=bool(single)), table=dip["G"])

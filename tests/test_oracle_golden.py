@@ -130,6 +130,79 @@ def test_oracle_locus_filter_matches_reference(oracle_build):
     assert kept == want
 
 
+def test_oracle_general_locus_filter_matches_reference(oracle_build):
+    """The oracle's locus filter for the general genotype layout (ploidy
+    2/4/6, 2-8 alleles: CalcDiversity over each locus' genotype table in order
+    of first appearance) keeps exactly the loci the reference program kept
+    under every diversity window at once (poly_filter), in float."""
+    import numpy as np
+    from . import orc
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLD, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    d = mg.datasets()["poly"][0]
+    f = orc.LocusFilter(single=1, k_b=1, k_min=3, k_max=8, he_b=1, he_min=0.4, he_max=0.78, ho_b=1, ho_min=0.3,
+                        ho_max=0.76, ae_b=1, ae_min=1.6, ae_max=4.6, ptype_b=1, ptype_min=0.96, ptype_max=1.0,
+                        pic_b=1, pic_min=0.3, pic_max=0.75, I_b=1, I_min=0.6, I_max=1.68, n_b=1, n_min=110, n_max=120)
+    keep, stats = orc.locus_filter_general(d["G"], d["k"], f)
+    kept = {f"1_snp{l + 1}" for l in range(len(keep)) if keep[l] and stats[l, 1] >= 2}
+    want = set(_diversity_loci(os.path.join(GOLD, "poly_filter", "out.structure.k=2_rep=1_id=1.txt")))
+    assert 0 < len(want) < 300
+    assert kept == want
+
+
+def test_oracle_general_statistics_equal_the_biallelic_ones():
+    """On biallelic diploid data the general statistics are the packed
+    kernel's: n, k, ptype, bmaf, he, ho, pic, ae and I equal, in float and in
+    double; the p-value to 1e-5 (the G statistic sums the genotypes in table
+    order there, in a fixed order here)."""
+    import numpy as np
+    from vcfpop_gb300 import structure as S
+    from vcfpop_gb300 import synth
+    from . import orc
+    d = synth.fmodel(3, 200, 500, 3, 0.1, 0.05)
+    for single in (1, 0):
+        f = orc.LocusFilter(single=single)
+        kp, sp = orc.locus_filter_pack2(S.pack2(d["G"]), 200, f)
+        kg, sg = orc.locus_filter_general(d["G"], d["k"], f)
+        assert np.array_equal(kp, kg)
+        assert np.array_equal(np.isnan(sp), np.isnan(sg))
+        both = ~np.isnan(sp)
+        assert np.array_equal(sp[:, :9][both[:, :9]], sg[:, :9][both[:, :9]])
+        assert np.allclose(sp[:, 9][both[:, 9]], sg[:, 9][both[:, 9]], rtol=1e-5, atol=0)
+
+
+def test_oracle_chi_square_tail_by_the_incomplete_gamma_function():
+    """The HWE p-value of the general test: 1 - P(df/2, G/2) by the
+    regularized incomplete gamma function, against scipy's chi-square
+    survival function over the degrees of freedom the test meets."""
+    import ctypes as C
+    import numpy as np
+    from scipy import stats
+    from . import orc
+    # a diploid triallelic locus of 400 individuals in HWE proportions: df = 3
+    rng = np.random.default_rng(4)
+    p = np.array([0.5, 0.3, 0.2])
+    a = rng.choice(3, size=(1, 400, 2), p=p)
+    G = np.sort(a, axis=2).astype(np.int8)
+    f = orc.LocusFilter(single=0)
+    _, st = orc.locus_filter_general(G, [3], f)
+    pval = st[0, 9]
+    # the G statistic from the same table: observed and expected counts
+    n = 400
+    cnt = np.bincount(G[0].ravel(), minlength=3) + 0.0
+    fr = (cnt + 1e-10) / (cnt.sum() + 3e-10)
+    obs = {}
+    for g in map(tuple, G[0]):
+        obs[g] = obs.get(g, 0) + 1
+    Gs = 0.0
+    for (x, y), o in obs.items():
+        e = (fr[x] * fr[y] * (2 if x != y else 1)) * n
+        Gs += 2 * o * np.log(o / e)
+    assert abs(pval - stats.chi2.sf(Gs, 3)) <= 1e-9 * max(1.0, stats.chi2.sf(Gs, 3))
+
+
 def test_oracle_record_lnl_is_counts_times_log_frequencies(oracle_build):
     """Without admixture, Record's lnP(D) (structure.cpp:1902-1938) is the sum
     over clusters, loci and alleles of Ni x ln p at the state it is recorded

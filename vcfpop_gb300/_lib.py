@@ -111,7 +111,7 @@ EXPORTS = ["vp_dataset_prepare", "vp_dataset_info_get", "vp_dataset_order", "vp_
            "vp_cohort_open", "vp_cohort_set", "vp_cohort_run", "vp_cohort_sync", "vp_cohort_stream",
            "vp_cohort_launches", "vp_cohort_close", "vp_server_set_batching", "vp_server_stats",
            "vp_vcf_parse", "vp_tc_pipeline", "vp_vcf_pack2_ex", "vp_vcf_parse_ex",
-           "vp_genotype_table"]
+           "vp_genotype_table", "vp_locus_filter_general"]
 
 
 def lib():
@@ -126,6 +126,8 @@ def lib():
     P = C.c_void_p
     L.vp_dataset_prepare.argtypes = [C.POINTER(VpInput), C.POINTER(P)]
     L.vp_genotype_table.argtypes = [C.POINTER(VpInput), P, P]
+    L.vp_locus_filter_general.argtypes = [P, P, C.c_int64, C.c_int32, C.c_int32, P, C.POINTER(VpLocusFilter), C.c_int,
+                                          P, P]
     L.vp_dataset_info_get.argtypes = [P, C.POINTER(VpDatasetInfo)]
     L.vp_dataset_order.argtypes = [P, P]
     L.vp_dataset_free.argtypes = [P]

@@ -54,6 +54,7 @@ struct Opts {
     bool chrprefix_b = false, chrname_b = false;
     std::vector<std::string> chrprefix, chrname;
     int64_t windowsize = 0;            // 0: no window filter
+    int model_val = 0;                 // -f_model: 0 not given, 1 rcs, 2 prcs, 3 ces, 4 pes
     int windowstat = 5;                // 1 bmaf, 2 k, 3 n, 4 ptype, 5 he, 6 ho, 7 pic, 8 ae
     vp_params p;
     std::vector<std::string> argv;
@@ -178,7 +179,7 @@ bool parse(int argc, char** argv, Opts& o) {
         } else if (k == "-f_model") {
             // the genotype model of the HWE test, the same for every model
             // at ploidy 2 (the locus statistics here are for diploid data)
-            if (!choice(v, "rcs|prcs|ces|pes")) { fprintf(stderr, "vcfpop-gb300: bad %s\n", a.c_str()); return false; }
+            if (!(o.model_val = choice(v, "rcs|prcs|ces|pes"))) { fprintf(stderr, "vcfpop-gb300: bad %s\n", a.c_str()); return false; }
         } else if (k == "-f_type") {
             if (!(o.type_val = choice(v, "snp|indel|both"))) { fprintf(stderr, "vcfpop-gb300: bad %s\n", a.c_str()); return false; }
         } else if (k == "-f_original") {
@@ -501,7 +502,8 @@ struct Writer {
 // an individual without any typed call counts as ploidy 0), not with each
 // individual's own, so either every individual passes or every one is
 // removed, which the reference reports as an error; that is reproduced.
-bool individual_filter(const Opts& o, Vcf& v, bool dev_ingest, std::vector<uint32_t>& packed, std::vector<int>& pop) {
+bool individual_filter(const Opts& o, Vcf& v, bool dev_ingest, std::vector<uint32_t>& packed, std::vector<int>& pop,
+                       std::vector<int>& kept) {
     const int N = (int)v.inds.size();
     const int64_t L = (int64_t)v.k.size();
     const int Nw = (N + 15) / 16;
@@ -537,6 +539,7 @@ bool individual_filter(const Opts& o, Vcf& v, bool dev_ingest, std::vector<uint3
         return false;
     }
     fprintf(stderr, "vcfpop-gb300: individual filter kept %d of %d individuals\n", (int)keep.size(), N);
+    kept = keep;
     if ((int)keep.size() == N) return true;
     const int M = (int)keep.size(), Mw = (M + 15) / 16;
     std::vector<std::string> inds(M);
@@ -629,10 +632,10 @@ int main(int argc, char** argv) {
     // filter, read here a second time without it
     std::vector<uint8_t> tpoly;
     std::vector<int32_t> tngeno;
+    Vcf v0;    // the calls before the genotype filter, file order (general layout)
     if (o.filter && (o.cf.dp_b || o.cf.gq_b || o.cf.ploidy_b)) {
         Opts o0 = o;
         o0.cf = vp_call_filter{};
-        Vcf v0;
         std::vector<uint32_t> p0;
         const int k0 = read_vcf_device(o0, v0, p0);
         if (!k0 && !read_vcf(o.input, o0.cf, v0)) { fprintf(stderr, "vcfpop-gb300: cannot read %s\n", o.input.c_str()); return 2; }
@@ -644,12 +647,14 @@ int main(int argc, char** argv) {
         tpoly.resize(L0);
         tngeno.resize(L0);
         if (vp_genotype_table(&t, tpoly.data(), tngeno.data())) { fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error()); return 1; }
+        if (k0 == 1) v0.G.clear();
     }
     std::vector<int> pop;
     std::vector<std::string> pnames;
     populations(o.indtext, N0, pop, pnames);
+    std::vector<int> kept_inds;
     if (o.filter && (o.itype_b || o.iploidy_b)) {
-        if (!individual_filter(o, v, dev_ingest, dev_packed, pop)) return 1;
+        if (!individual_filter(o, v, dev_ingest, dev_packed, pop, kept_inds)) return 1;
     }
     const int N = (int)v.inds.size();
     // group individuals by population in the populations' order (stable)
@@ -729,10 +734,39 @@ int main(int argc, char** argv) {
         std::vector<uint8_t> keep(L0, 1);
         if (info_tests) info_filter(o, v, keep);
         if (windows || o.windowsize) {
-            if (!in.packed2) { fprintf(stderr, "vcfpop-gb300: the locus filter needs biallelic diploid data\n"); return 1; }
             std::vector<uint8_t> kd(L0);
             std::vector<double> st(o.windowsize ? (size_t)L0 * VP_LOCUS_STATS : 0);
-            if (vp_locus_filter_pack2(in.packed2, L0, N, &lf, o.device, kd.data(), o.windowsize ? st.data() : nullptr)) {
+            int frc;
+            if (in.packed2) {
+                frc = vp_locus_filter_pack2(in.packed2, L0, N, &lf, o.device, kd.data(), o.windowsize ? st.data() : nullptr);
+            } else {
+                // the general layout, in the file's order of individuals (the
+                // order in which the loader met each genotype); with the
+                // genotype filter, the calls before it order the tables
+                int maxp = 0;
+                for (int i = 0; i < N; ++i) maxp = std::max(maxp, (int)v.ploidy[i]);
+                if (lf.pval_b && o.model_val && maxp >= 4) {
+                    fprintf(stderr, "vcfpop-gb300: -f_model with -f_pval on data of ploidy 4 or more is not implemented "
+                                    "(the double-reduction genotype frequencies)\n");
+                    return 1;
+                }
+                std::vector<int8_t> tsub;
+                const int8_t* table = nullptr;
+                if (!v0.G.empty()) {
+                    if (kept_inds.empty()) table = v0.G.data();
+                    else {
+                        tsub.resize(v.G.size());
+                        for (int64_t l = 0; l < L0; ++l)
+                            for (size_t j = 0; j < kept_inds.size(); ++j)
+                                memcpy(&tsub[((size_t)l * N + j) * v.vmax], &v0.G[((size_t)l * N0 + kept_inds[j]) * v.vmax],
+                                       v.vmax);
+                        table = tsub.data();
+                    }
+                }
+                frc = vp_locus_filter_general(v.G.data(), table, L0, N, v.vmax, v.k.data(), &lf, o.device, kd.data(),
+                                              o.windowsize ? st.data() : nullptr);
+            }
+            if (frc) {
                 fprintf(stderr, "vcfpop-gb300: %s\n", vp_last_error());
                 return 1;
             }

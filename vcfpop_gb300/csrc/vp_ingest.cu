@@ -759,3 +759,449 @@ extern "C" int vp_locus_filter_pack2(const uint32_t* packed, int64_t n_loc, int3
     cudaStreamDestroy(st);
     return rc;
 }
+
+// ---------------------------------------------------------------------------
+// Locus statistics of any ploidy and allele count (the general genotype
+// layout G[L][N][vmax], allele indices 0..63, up to 10 copies). The
+// reference computes them over the locus' genotype table (DIVERSITY::
+// CalcDiversity, src/diversity.cpp:144-492), whose genotypes appear in the
+// order the loader first met them (src/load.cpp:2180-2230); its REAL sums run
+// in that order. One warp per locus builds the table in shared memory:
+// 32 calls at a time, each lane looks its call's key up, the lanes with a new
+// key group by key (__match_any_sync) and the first lane of each group
+// inserts it, in lane order, so the table keeps the order of first
+// appearance; the counts are shared-memory atomics. Lane 0 then derives the
+// statistics and runs the HWE test with the reference's allele collapsing.
+namespace {
+
+constexpr int GT_CAP = 512;   // distinct typed genotypes a locus may hold
+
+// a call's key: copies in bits 0-3, allele j in bits 4 + 6j (0: missing;
+// a call with an allele index outside the locus' kall alleles counts as
+// missing)
+__device__ __forceinline__ uint64_t call_key(const int8_t* g, int vmax, int kall) {
+    if (g[0] < 0) return 0;
+    uint64_t k = 0;
+    int v = 0;
+    for (; v < vmax && g[v] >= 0; ++v) {
+        if (g[v] >= kall) return 0;
+        k |= (uint64_t)g[v] << (4 + 6 * v);
+    }
+    return k | (uint64_t)v;
+}
+
+// one pass of the warp over the calls of a locus: with INSERT new keys join
+// the table in order of first appearance, with COUNT every call adds 1 to
+// its key's count
+template <bool INSERT, bool COUNT>
+__device__ void table_pass(const int8_t* G, int N, int vmax, int kall, uint64_t* tk, uint32_t* tc, int& T,
+                           int* overflow) {
+    const int lane = threadIdx.x & 31;
+    for (int i0 = 0; i0 < N; i0 += 32) {
+        const int i = i0 + lane;
+        const uint64_t k = i < N ? call_key(G + (size_t)i * vmax, vmax, kall) : 0;
+        int slot = -1;
+        if (k)
+            for (int s = 0; s < T; ++s)
+                if (tk[s] == k) { slot = s; break; }
+        if (INSERT) {
+            const bool isnew = k && slot < 0;
+            const unsigned peers = __match_any_sync(0xffffffffu, isnew ? k : ~0ull);
+            const bool leader = isnew && (__ffs(peers) - 1) == lane;
+            const unsigned leaders = __ballot_sync(0xffffffffu, leader);
+            if (leaders) {
+                if (leader) {
+                    const int s = T + __popc(leaders & ((1u << lane) - 1u));
+                    if (s < GT_CAP) { tk[s] = k; tc[s] = 0; }
+                    else *overflow = 1;
+                }
+                __syncwarp();
+                const int Tn = min(T + __popc(leaders), GT_CAP);
+                if (isnew)
+                    for (int s = T; s < Tn; ++s)
+                        if (tk[s] == k) { slot = s; break; }
+                T = Tn;
+            }
+        }
+        if (COUNT && slot >= 0) atomicAdd(&tc[slot], 1u);
+        __syncwarp();
+    }
+}
+
+// the dosage pattern of a key: distinct alleles by descending copy count,
+// ties by the larger allele first (GENOTYPE::GENOTYPE, src/function.cpp
+// :259-337)
+struct GtPattern {
+    int v, na;
+    int al[10], key[10], cnt[10];
+};
+__device__ void gt_pattern(uint64_t k, GtPattern& p) {
+    p.v = (int)(k & 15);
+    for (int j = 0; j < p.v; ++j) p.al[j] = (int)((k >> (4 + 6 * j)) & 63);
+    p.na = 0;
+    for (int i = 0; i < p.v; ++i) {
+        bool isnew = true;
+        for (int j = i - 1; j >= 0; --j)
+            if (p.al[i] == p.al[j]) { isnew = false; break; }
+        if (!isnew) continue;
+        int ac = 1;
+        for (int j = i + 1; j < p.v; ++j) ac += p.al[j] == p.al[i];
+        p.key[p.na] = p.al[i];
+        p.cnt[p.na++] = ac;
+    }
+    for (int i = 0; i < p.na; ++i)
+        for (int j = i + 1; j < p.na; ++j)
+            if (p.cnt[i] < p.cnt[j] || (p.cnt[i] == p.cnt[j] && p.key[i] < p.key[j])) {
+                int t = p.cnt[i]; p.cnt[i] = p.cnt[j]; p.cnt[j] = t;
+                t = p.key[i]; p.key[i] = p.key[j]; p.key[j] = t;
+            }
+}
+// GENOTYPE::HIndex as the reference's table holds it: a 15-decimal literal,
+// the double nearest round(p / q x 10^15) / 10^15 (0 for one copy)
+__device__ double gt_hindex(const GtPattern& p) {
+    const long long q = (long long)p.v * (p.v - 1);
+    if (q == 0) return 0;
+    long long same = 0;
+    for (int i = 0; i < p.na; ++i) same += (long long)p.cnt[i] * (p.cnt[i] - 1);
+    const long long n15 = (2 * (q - same) * 1000000000000000LL + q) / (2 * q);
+    return (double)n15 / 1e15;
+}
+// GENOTYPE::HWECoef: v! / prod cnt!
+__device__ double gt_hwecoef(const GtPattern& p) {
+    double f = 1;
+    for (int i = 2; i <= p.v; ++i) f *= i;
+    for (int a = 0; a < p.na; ++a)
+        for (int i = 2; i <= p.cnt[a]; ++i) f /= i;
+    return f;
+}
+// IntegerPower (src/math2.h:307-350) in double
+__device__ double ipow(double x, int n) {
+    switch (n) {
+        case 0: return 1;
+        case 1: return x;
+        case 2: return x * x;
+        case 3: return x * x * x;
+        case 4: { const double x2 = x * x; return x2 * x2; }
+        case 5: { const double x2 = x * x; return x2 * x2 * x; }
+        case 6: { const double x3 = x * x * x; return x3 * x3; }
+        case 7: { const double x3 = x * x * x; return x3 * x3 * x; }
+        case 8: { const double x2 = x * x, x4 = x2 * x2; return x4 * x4; }
+        case 9: { const double x3 = x * x * x; return x3 * x3 * x3; }
+        case 10: { const double x2 = x * x, x4 = x2 * x2; return x4 * x4 * x2; }
+        default: return pow(x, (double)n);
+    }
+}
+// the chi-square upper tail: 1 - erf(sqrt(x / 2)) for df = 1 (as the
+// biallelic kernel), else 1 - P(df / 2, x / 2), the regularized lower
+// incomplete gamma function by its series below a + 1 and its continued
+// fraction above (Numerical Recipes, 6.2)
+__device__ double chi2_upper(double x, int df) {
+    if (df == 1) return 1.0 - erf(sqrt(0.5 * x));
+    const double a = 0.5 * df, z = 0.5 * x;
+    if (z <= 0) return 1;
+    const double lg = lgamma(a);
+    if (z < a + 1) {
+        double ap = a, sum = 1.0 / a, del = sum;
+        for (int n = 0; n < 1000; ++n) {
+            ap += 1;
+            del *= z / ap;
+            sum += del;
+            if (fabs(del) < fabs(sum) * 1e-16) break;
+        }
+        return 1.0 - sum * exp(-z + a * log(z) - lg);
+    }
+    double b = z + 1 - a, c = 1.0 / 1e-300, d = 1.0 / b, h = d;
+    for (int i = 1; i < 1000; ++i) {
+        const double an = -i * (i - a);
+        b += 2;
+        d = an * d + b;
+        if (fabs(d) < 1e-300) d = 1e-300;
+        c = b + an / c;
+        if (fabs(c) < 1e-300) c = 1e-300;
+        d = 1.0 / d;
+        const double del = d * c;
+        h *= del;
+        if (fabs(del - 1) < 1e-16) break;
+    }
+    return exp(-z + a * log(z) - lg) * h;
+}
+
+// CalcDiversity over a genotype table (keys tk, counts tc, T entries), k2
+// alleles, ni individuals; t1/t2 (keys and counts, GT_CAP each) hold the
+// collapsed tables of the HWE test. out: n, k, ptype, bmaf, he, ho, pic, ae,
+// I, pval (NaN where the reference leaves them undefined).
+template <typename REAL>
+__device__ void general_stats(const uint64_t* tk, const uint32_t* tc, int T, uint64_t* k1, uint32_t* c1,
+                              uint64_t* k2b, uint32_t* c2, int k2, int ni, double* out) {
+    const double MINF = 1e-10, NANV = __longlong_as_double(0x7ff8000000000000ll);
+    REAL fre[64], ho = 0, how = 0;
+    for (int a = 0; a < k2; ++a) fre[a] = 0;
+    int n = 0, nhaplo = 0, minp = 100, maxp = 0;
+    bool varploidy = false;
+    GtPattern p;
+    for (int gi = 0; gi < T; ++gi) {
+        const unsigned c = tc[gi];
+        if (!c) continue;
+        gt_pattern(tk[gi], p);
+        const int v = p.v;
+        nhaplo += v * c;
+        maxp = max(maxp, v);
+        minp = min(minp, v);
+        if (maxp != minp) varploidy = true;
+        ho += gt_hindex(p) * c * v * (v - 1);
+        how += c * v * (v - 1);
+        n += c;
+        for (int i = 0; i < v; ++i) fre[p.al[i]] += c;
+    }
+    const REAL ptype = n / (REAL)ni;
+    {   // Unify (src/math2.cpp:2268-2304)
+        double s = 0;
+        for (int a = 0; a < k2; ++a) s += fre[a];
+        const double invsum = 1.0 / (s + k2 * MINF);
+        for (int a = 0; a < k2; ++a) fre[a] = (REAL)(((double)fre[a] + MINF) * invsum);
+    }
+    int k = 0;
+    if (n)
+        for (int a = 0; a < k2; ++a) k += fre[a] > MINF;
+    double bmaf = NANV, he = NANV, hoo = NANV, pic = NANV, ae = NANV, I = NANV, pval = NANV;
+    if (k >= 2) {
+        hoo = ho / how;
+        REAL b = 1, a2 = 0, picv = 0, Iv = 0;
+        const int nh = (int)(nhaplo + 0.5);
+        for (int a = 0; a < k2; ++a) {
+            const REAL af = fre[a];
+            if (af * nh < 1e-5) continue;
+            if (af > 1e-5) Iv += -af * rlog(af);
+            if (b > af) b = af;
+            a2 += af * af;
+            for (int c = a + 1; c < k2; ++c)
+                if (fre[c] > 0) picv += 2 * af * fre[c] * (1 - af * fre[c]);
+        }
+        if (b > 0.5) b = 1 - b;
+        bmaf = b;
+        he = (REAL)(1 - a2);
+        ae = (REAL)(1 / a2);
+        I = Iv;
+        pic = picv;
+        if (!varploidy) {
+            // the HWE G-test with allele collapsing (src/diversity.cpp:337-492),
+            // genotype model 0: expected counts HWECoef x prod f^count x n
+            const int ploidy = maxp;
+            const uint64_t* ck = tk;
+            const uint32_t* cc = tc;
+            int n1 = T;
+            REAL f1[64], f2[64];
+            int amap[64];
+            for (int a = 0; a < k2; ++a) f1[a] = fre[a];
+            uint64_t* dk = k1;
+            uint32_t* dc = c1;
+            REAL G = 0;
+            bool flag = false;
+            for (int kk = k2; kk >= 1 && !flag; kk = (kk <= k ? kk - 1 : k)) {
+                if (kk == 1) break;
+                for (int a = 0; a < kk; ++a) f2[a] = 0;
+                if (kk <= k) {
+                    flag = true;
+                    G = 0;
+                    for (int gi = 0; gi < n1; ++gi) {
+                        if (!cc[gi]) continue;
+                        gt_pattern(ck[gi], p);
+                        double gfz = gt_hwecoef(p);
+                        for (int ai = p.na - 1; ai >= 0; --ai) gfz *= ipow((double)f1[p.key[ai]], p.cnt[ai]);
+                        const REAL obs = (REAL)cc[gi], ex = (REAL)(gfz * n);
+                        if (ex < 5) { flag = false; break; }
+                        G += 2 * obs * rlog(obs / ex);
+                    }
+                }
+                if (flag) {
+                    double bin = 1;   // Binomial(ploidy + kk - 1, ploidy) by factorials
+                    for (int i = 2; i <= ploidy + kk - 1; ++i) bin *= i;
+                    for (int i = 2; i <= ploidy; ++i) bin /= i;
+                    for (int i = 2; i <= kk - 1; ++i) bin /= i;
+                    pval = (REAL)chi2_upper((double)G, (int)(bin - kk + 0.5));
+                    break;
+                }
+                if (kk <= k) {
+                    // merge the two rarest alleles (GetMinID: the first minimum)
+                    int m1 = 0;
+                    for (int a = 1; a < kk; ++a) if (f1[m1] > f1[a]) m1 = a;
+                    f1[m1]++;
+                    int m2 = 0;
+                    for (int a = 1; a < kk; ++a) if (f1[m2] > f1[a]) m2 = a;
+                    f1[m1]--;
+                    if (m1 > m2) { const int t = m1; m1 = m2; m2 = t; }
+                    for (int j = 0, q = 0; j < kk; ++j) {
+                        if (j == m2) { amap[j] = m1; f2[m1] = f1[m1] + f1[m2]; }
+                        else { amap[j] = q; f2[q++] = f1[j]; }
+                    }
+                } else {
+                    // absent alleles onto the most frequent one (GetMaxID: the first maximum)
+                    int m1 = 0;
+                    for (int a = 1; a < kk; ++a) if (f1[m1] < f1[a]) m1 = a;
+                    for (int j = 0, q = 0; j < kk; ++j) amap[j] = f1[j] < MINF ? -1 : q++;
+                    for (int j = 0; j < kk; ++j) amap[j] = amap[j] == -1 ? amap[m1] : amap[j];
+                }
+                // the collapsed table, in order of first mapping
+                int n2 = 0;
+                for (int gi = 0; gi < n1; ++gi) {
+                    if (!cc[gi]) continue;
+                    gt_pattern(ck[gi], p);
+                    int al[10];
+                    for (int ai = 0; ai < ploidy; ++ai) al[ai] = amap[p.al[ai]];
+                    for (int x = 1; x < ploidy; ++x) {
+                        const int y0 = al[x];
+                        int y = x - 1;
+                        while (y >= 0 && al[y] > y0) { al[y + 1] = al[y]; --y; }
+                        al[y + 1] = y0;
+                    }
+                    uint64_t nk = (uint64_t)ploidy;
+                    for (int j = 0; j < ploidy; ++j) {
+                        f2[al[j]] += cc[gi];
+                        nk |= (uint64_t)(al[j] & 63) << (4 + 6 * j);
+                    }
+                    int found = -1;
+                    for (int x = 0; x < n2 && found < 0; ++x)
+                        if (dk[x] == nk) found = x;
+                    if (found < 0) { dk[n2] = nk; dc[n2] = cc[gi]; ++n2; }
+                    else dc[found] += cc[gi];
+                }
+                {
+                    double s = 0;
+                    for (int a = 0; a < kk; ++a) s += f2[a];
+                    const double invsum = 1.0 / (s + kk * MINF);
+                    for (int a = 0; a < kk; ++a) f2[a] = (REAL)(((double)f2[a] + MINF) * invsum);
+                }
+                for (int a = 0; a < kk; ++a) f1[a] = f2[a];
+                // the new table becomes the current one; the other buffer is next
+                ck = dk;
+                cc = dc;
+                n1 = n2;
+                if (dk == k1) { dk = k2b; dc = c2; } else { dk = k1; dc = c1; }
+            }
+        }
+    }
+    out[0] = n; out[1] = k; out[2] = ptype; out[3] = bmaf; out[4] = he; out[5] = hoo; out[6] = pic;
+    out[7] = ae; out[8] = I; out[9] = pval;
+}
+
+// one warp (= block) per locus
+__global__ void __launch_bounds__(32) k_locus_filter_general(const int8_t* G, const int8_t* Gt, int64_t L, int N,
+                                                             int vmax, const int32_t* nall, vp_locus_filter f,
+                                                             uint8_t* keep, double* stats) {
+    extern __shared__ __align__(16) unsigned char sraw[];
+    uint64_t* tk = reinterpret_cast<uint64_t*>(sraw);
+    uint64_t* k1 = tk + GT_CAP;
+    uint64_t* k2 = k1 + GT_CAP;
+    uint32_t* tc = reinterpret_cast<uint32_t*>(k2 + GT_CAP);
+    uint32_t* c1 = tc + GT_CAP;
+    uint32_t* c2 = c1 + GT_CAP;
+    __shared__ int overflow;
+    const int lane = threadIdx.x;
+    for (int64_t l = blockIdx.x; l < L; l += gridDim.x) {
+        if (lane == 0) overflow = 0;
+        __syncwarp();
+        const int8_t* g = G + (size_t)l * N * vmax;
+        int T = 0;
+        const int kall = nall[l];
+        if (Gt) {
+            table_pass<true, false>(Gt + (size_t)l * N * vmax, N, vmax, kall, tk, tc, T, &overflow);
+            table_pass<false, true>(g, N, vmax, kall, tk, tc, T, &overflow);
+        } else {
+            table_pass<true, true>(g, N, vmax, kall, tk, tc, T, &overflow);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            if (overflow) {
+                keep[l] = 2;
+            } else {
+                double o[VP_LOCUS_STATS];
+                if (f.single) general_stats<float>(tk, tc, T, k1, c1, k2, c2, nall[l], N, o);
+                else general_stats<double>(tk, tc, T, k1, c1, k2, c2, nall[l], N, o);
+                const int k = (int)o[1], n = (int)o[0];
+                const bool fail = k == 0 || (f.bmaf_b && k == 2 && outside(o[3], f.bmaf_min, f.bmaf_max)) ||
+                                  (f.k_b && (k < f.k_min || k > f.k_max)) || (f.n_b && (n < f.n_min || n > f.n_max)) ||
+                                  (f.ptype_b && outside(o[2], f.ptype_min, f.ptype_max)) ||
+                                  (f.he_b && outside(o[4], f.he_min, f.he_max)) ||
+                                  (f.ho_b && outside(o[5], f.ho_min, f.ho_max)) ||
+                                  (f.pic_b && outside(o[6], f.pic_min, f.pic_max)) ||
+                                  (f.ae_b && outside(o[7], f.ae_min, f.ae_max)) ||
+                                  (f.I_b && outside(o[8], f.I_min, f.I_max)) ||
+                                  (f.pval_b && o[9] != -1 && outside(o[9], f.pval_min, f.pval_max));
+                keep[l] = fail ? 0 : 1;
+                if (stats)
+                    for (int j = 0; j < VP_LOCUS_STATS; ++j) stats[l * VP_LOCUS_STATS + j] = o[j];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+extern "C" int vp_locus_filter_general(const int8_t* alleles, const int8_t* alleles_table, int64_t n_loc,
+                                       int32_t n_ind, int32_t vmax, const int32_t* n_alleles,
+                                       const vp_locus_filter* f, int device, uint8_t* keep, double* stats) {
+    if (!alleles || !n_alleles || !f || !keep || n_loc < 0 || n_ind <= 0 || vmax < 1 || vmax > 10) {
+        vp_set_error("bad arguments");
+        return VP_E_ARG;
+    }
+    for (int64_t l = 0; l < n_loc; ++l)
+        if (n_alleles[l] < 1 || n_alleles[l] > 64) {
+            vp_set_error("locus %lld has %d alleles (1 to 64)", (long long)(l + 1), n_alleles[l]);
+            return VP_E_ARG;
+        }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { vp_set_error("no CUDA device"); return VP_E_NODEV; }
+    if (device < 0 || device >= ndev) { vp_set_error("device %d out of range", device); return VP_E_ARG; }
+    if (n_loc == 0) return VP_OK;
+    CKI(cudaSetDevice(device));
+    cudaStream_t st;
+    CKI(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const size_t gb = (size_t)n_loc * n_ind * vmax, tb = alleles_table ? gb : 0, kb = (size_t)n_loc * 4,
+                 sb = stats ? (size_t)n_loc * VP_LOCUS_STATS * 8 : 0;
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    char* buf = nullptr;
+    int rc = VP_OK;
+    cudaError_t e = cudaMallocAsync((void**)&buf, up(gb) + up(tb) + up(kb) + up((size_t)n_loc) + sb, st);
+    if (e != cudaSuccess) { vp_set_error("device allocation failed: %s", cudaGetErrorString(e)); rc = VP_E_MEM; }
+    std::vector<uint8_t> hk;
+    if (!rc) {
+        int8_t* dg = (int8_t*)buf;
+        int8_t* dt = alleles_table ? (int8_t*)(buf + up(gb)) : nullptr;
+        int32_t* dn = (int32_t*)(buf + up(gb) + up(tb));
+        uint8_t* dk = (uint8_t*)(buf + up(gb) + up(tb) + up(kb));
+        double* ds = stats ? (double*)(buf + up(gb) + up(tb) + up(kb) + up((size_t)n_loc)) : nullptr;
+        rc = upload_staged((char*)dg, (const char*)alleles, (int64_t)gb, st);
+        if (!rc && dt) rc = upload_staged((char*)dt, (const char*)alleles_table, (int64_t)tb, st);
+        if (!rc) {
+            const size_t smem = (size_t)GT_CAP * 3 * (8 + 4);
+            const unsigned grid = (unsigned)std::min<int64_t>(n_loc, 152 * 32);
+            hk.resize(n_loc);
+            if ((e = cudaMemcpyAsync(dn, n_alleles, kb, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+                vp_set_error("upload failed: %s", cudaGetErrorString(e));
+                rc = VP_E_CUDA;
+            } else {
+                k_locus_filter_general<<<grid, 32, smem, st>>>(dg, dt, n_loc, n_ind, vmax, dn, *f, dk, ds);
+                if ((e = cudaGetLastError()) != cudaSuccess ||
+                    (e = cudaMemcpyAsync(hk.data(), dk, (size_t)n_loc, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                    (ds && (e = cudaMemcpyAsync(stats, ds, sb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) ||
+                    (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+                    vp_set_error("locus filter failed: %s", cudaGetErrorString(e));
+                    rc = VP_E_CUDA;
+                }
+            }
+        }
+        cudaFreeAsync(buf, st);
+    }
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (!rc)
+        for (int64_t l = 0; l < n_loc; ++l) {
+            if (hk[l] == 2) {
+                vp_set_error("locus %lld has more than %d distinct genotypes", (long long)(l + 1), GT_CAP);
+                return VP_E_ARG;
+            }
+            keep[l] = hk[l];
+        }
+    return rc;
+}

@@ -309,6 +309,22 @@ def locus_filter(packed: np.ndarray, n_ind: int, f: B.VpLocusFilter, device: int
     return keep, stats
 
 
+def locus_filter_general(G: np.ndarray, n_alleles, f: B.VpLocusFilter, table=None, device: int = 0):
+    """The -f_* locus filter on the device for the general genotype layout
+    G[L][N][vmax] (any ploidy, up to 64 alleles per locus): (keep [L] uint8,
+    stats [L][10]). table: the calls before the genotype filter (same
+    layout), whose first appearances order each locus' genotype table."""
+    G = np.ascontiguousarray(G, np.int8)
+    L, N, vmax = G.shape
+    k = np.ascontiguousarray(n_alleles, np.int32)
+    T = None if table is None else np.ascontiguousarray(table, np.int8)
+    keep = np.zeros(L, np.uint8)
+    stats = np.zeros((L, len(LOCUS_STATS)))
+    B.check(B.lib().vp_locus_filter_general(G.ctypes.data, None if T is None else T.ctypes.data, L, N, vmax,
+                                            k.ctypes.data, C.byref(f), device, keep.ctypes.data, stats.ctypes.data))
+    return keep, stats
+
+
 def chain_result(h, final: bool = False) -> dict:
     r = B.VpResult()
     B.check(B.lib().vp_chain_sizes(h, C.byref(r)))
