@@ -268,6 +268,40 @@ def locus_filter_leg(packed, N, args, rank, sample=20000):
     return out
 
 
+def locus_filter_general_leg(d, with_cpu, sample=2000):
+    """The -f_* locus filter for the general genotype layout
+    (vp_locus_filter_general: each locus' genotype table in order of first
+    appearance, its statistics and the HWE test, copies included) on a
+    polyploid multiallelic dataset, and as its CPU baseline the oracle on one
+    core over a sample of loci, scaled to the same count."""
+    from vcfpop_gb300 import structure as S
+    f = S.locus_filter_spec(single=False, k=(3, 8), he=(0.3, 0.9), ptype=(0.9, 1.0), pval=(0.001, 1.0))
+    G, k = d["G"], d["k"]
+    S.locus_filter_general(G[:200], k[:200], f)        # warm-up
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        keep, _ = S.locus_filter_general(G, k, f)
+    dev = (time.perf_counter() - t0) / reps
+    L, N, vmax = G.shape
+    out = {"what": f"{L} loci x {N} individuals (ploidy {sorted(set(int(x) for x in d['ploidy']))}, "
+                   f"{int(k.min())}-{int(k.max())} alleles; {G.nbytes / 1e9:.2f} GB of allele copies), "
+                   f"-f_k=[3,8] -f_he=[0.3,0.9] -f_ptype=[0.9,1] -f_pval=[0.001,1]",
+           "device_ms": dev * 1e3, "device_gbs": G.nbytes / dev / 1e9, "kept": int(keep.sum())}
+    if with_cpu:
+        from tests import orc
+        o = orc.LocusFilter()
+        for name, _ in orc.LocusFilter._fields_:
+            setattr(o, name, getattr(f, name))
+        n = min(sample, L)
+        t0 = time.perf_counter()
+        okeep, _ = orc.locus_filter_general(G[:n], k[:n], o)
+        cpu = (time.perf_counter() - t0) * L / n
+        out.update({"cpu_baseline_ms": cpu * 1e3, "cpu_baseline_kind": f"port (the oracle on one core, {n} loci, scaled)",
+                    "cpu_equal_on_sample": bool(np.array_equal(okeep, keep[:n]))})
+    return out
+
+
 # ---------------------------------------------------------------- output reductions
 def output_reductions(ctx, ds, args, rank):
     """WriteStructure's heterozygosity / net-distance / per-locus diversity
@@ -520,6 +554,8 @@ def single_compact(name, local, peaks, cpu_budget_s=0.0):
         v, ns, dt = cpu_sample_single(d, K, run, budget_s=cpu_budget_s)
         out["cpu_baseline"] = {"value": v, "unit": "updates/s", "cores": 1, "kind": "port",
                                "sample": f"the same dataset, one chain on one host core, {ns} sweeps in {dt:.1f} s"}
+    if name == "c4":
+        out["locus_filter_general"] = locus_filter_general_leg(d, cpu_budget_s > 0)
     return out
 
 

@@ -430,8 +430,9 @@ int vp_locus_filter_pack2(const uint32_t* packed, int64_t n_loc, int32_t n_ind, 
  * NULL: alleles), counted over alleles; the HWE p-value comes from the test
  * with allele collapsing (src/diversity.cpp:337-492) for the default
  * genotype model (no -f_model), NaN with mixed ploidy at the locus, and the
- * chi-square upper tail by the regularized incomplete gamma function. A
- * locus with more than 512 distinct genotypes fails with VP_E_ARG. */
+ * chi-square upper tail by the regularized incomplete gamma function. The
+ * tables live in device scratch sized for n_ind distinct genotypes, so any
+ * number of distinct genotypes at a locus is accepted. */
 int vp_locus_filter_general(const int8_t* alleles, const int8_t* alleles_table, int64_t n_loc, int32_t n_ind,
                             int32_t vmax, const int32_t* n_alleles, const vp_locus_filter* f, int device,
                             uint8_t* keep, double* stats);

@@ -101,3 +101,18 @@ def test_general_statistics_on_device_equal_the_oracle(single):
     G2 = dip["G"].copy()
     G2[rng.random(G2.shape[:2]) < 0.2] = -1
     _compare_general(G2, dip["k"], S.locus_filter_spec(single=bool(single)), table=dip["G"])
+
+
+@pytest.mark.parametrize("single", [1, 0])
+def test_general_statistics_with_thousands_of_distinct_genotypes(single):
+    """Loci whose genotype tables hold thousands of entries (tetraploid with
+    30 alleles, diploid with 60): the tables and the HWE test's collapsed
+    tables grow with the sample, in the order of first appearance."""
+    tet = synth.fmodel(11, 3000, 12, 2, 0.01, 0.02, ploidy=np.full(3000, 4), n_alleles=np.full(12, 30),
+                       anc_alpha=5.0)
+    dip = synth.fmodel(12, 4000, 12, 2, 0.01, 0.02, n_alleles=np.full(12, 60), anc_alpha=5.0)
+    for d, least in ((tet, 1500), (dip, 700)):
+        G = d["G"]
+        ndist = [len({tuple(sorted(c)) for c in G[l].tolist() if min(c) >= 0}) for l in range(G.shape[0])]
+        assert min(ndist) > least
+        _compare_general(G, d["k"], S.locus_filter_spec(single=bool(single)))

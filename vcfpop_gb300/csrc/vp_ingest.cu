@@ -766,15 +766,16 @@ extern "C" int vp_locus_filter_pack2(const uint32_t* packed, int64_t n_loc, int3
 // reference computes them over the locus' genotype table (DIVERSITY::
 // CalcDiversity, src/diversity.cpp:144-492), whose genotypes appear in the
 // order the loader first met them (src/load.cpp:2180-2230); its REAL sums run
-// in that order. One warp per locus builds the table in shared memory:
-// 32 calls at a time, each lane looks its call's key up, the lanes with a new
-// key group by key (__match_any_sync) and the first lane of each group
-// inserts it, in lane order, so the table keeps the order of first
-// appearance; the counts are shared-memory atomics. Lane 0 then derives the
+// in that order. One warp per locus builds the table: 32 calls at a time,
+// each lane looks its call's key up, the lanes with a new key group by key
+// (__match_any_sync) and the first lane of each group appends it, in lane
+// order, so the table keeps the order of first appearance; the counts are
+// atomics. A locus holds at most N distinct genotypes, so each block's table
+// lives in global scratch of N entries, with an open-addressing map from key
+// to slot; a map entry carries the stamp of the locus (or collapse round)
+// that wrote it, so nothing is cleared between loci. Lane 0 then derives the
 // statistics and runs the HWE test with the reference's allele collapsing.
 namespace {
-
-constexpr int GT_CAP = 512;   // distinct typed genotypes a locus may hold
 
 // a call's key: copies in bits 0-3, allele j in bits 4 + 6j (0: missing;
 // a call with an allele index outside the locus' kall alleles counts as
@@ -790,20 +791,59 @@ __device__ __forceinline__ uint64_t call_key(const int8_t* g, int vmax, int kall
     return k | (uint64_t)v;
 }
 
+// key -> slot map: entries (stamp << 32 | slot), empty unless the stamp is
+// the current one; read past L1 (__ldcg), written by atomics
+struct SlotMap {
+    unsigned long long* e;
+    uint32_t mask;
+    uint32_t stamp;
+};
+// the 64-bit finalizer of MurmurHash3 (Appleby)
+__device__ __forceinline__ uint32_t key_hash(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return (uint32_t)k;
+}
+// the slot of key k among keys[], or -1
+__device__ int map_find(const SlotMap& m, const uint64_t* keys, uint64_t k) {
+    uint32_t h = key_hash(k) & m.mask;
+    for (uint32_t n = 0; n <= m.mask; ++n, h = (h + 1) & m.mask) {
+        const unsigned long long e = __ldcg(m.e + h);
+        if ((uint32_t)(e >> 32) != m.stamp) return -1;
+        const int s = (int)(uint32_t)e;
+        if (__ldcg(keys + s) == k) return s;
+    }
+    return -1;
+}
+// key k (absent from the map) -> slot; lanes of one warp may insert
+// distinct keys at once
+__device__ void map_insert(const SlotMap& m, uint64_t k, int slot) {
+    const unsigned long long v = ((unsigned long long)m.stamp << 32) | (uint32_t)slot;
+    uint32_t h = key_hash(k) & m.mask;
+    for (uint32_t n = 0; n <= m.mask; ++n, h = (h + 1) & m.mask) {
+        unsigned long long e = __ldcg(m.e + h);
+        while ((uint32_t)(e >> 32) != m.stamp) {
+            const unsigned long long old = atomicCAS(m.e + h, e, v);
+            if (old == e) return;
+            e = old;
+        }
+    }
+}
+
 // one pass of the warp over the calls of a locus: with INSERT new keys join
-// the table in order of first appearance, with COUNT every call adds 1 to
-// its key's count
+// the table (tk, tc: T entries) in order of first appearance, with COUNT
+// every call adds 1 to its key's count
 template <bool INSERT, bool COUNT>
 __device__ void table_pass(const int8_t* G, int N, int vmax, int kall, uint64_t* tk, uint32_t* tc, int& T,
-                           int* overflow) {
+                           const SlotMap& m) {
     const int lane = threadIdx.x & 31;
     for (int i0 = 0; i0 < N; i0 += 32) {
         const int i = i0 + lane;
         const uint64_t k = i < N ? call_key(G + (size_t)i * vmax, vmax, kall) : 0;
-        int slot = -1;
-        if (k)
-            for (int s = 0; s < T; ++s)
-                if (tk[s] == k) { slot = s; break; }
+        int slot = k ? map_find(m, tk, k) : -1;
         if (INSERT) {
             const bool isnew = k && slot < 0;
             const unsigned peers = __match_any_sync(0xffffffffu, isnew ? k : ~0ull);
@@ -812,20 +852,22 @@ __device__ void table_pass(const int8_t* G, int N, int vmax, int kall, uint64_t*
             if (leaders) {
                 if (leader) {
                     const int s = T + __popc(leaders & ((1u << lane) - 1u));
-                    if (s < GT_CAP) { tk[s] = k; tc[s] = 0; }
-                    else *overflow = 1;
+                    __stcg(tk + s, k);
+                    __stcg(tc + s, 0u);
+                    __threadfence_block();
+                    map_insert(m, k, s);
                 }
+                __threadfence_block();
                 __syncwarp();
-                const int Tn = min(T + __popc(leaders), GT_CAP);
-                if (isnew)
-                    for (int s = T; s < Tn; ++s)
-                        if (tk[s] == k) { slot = s; break; }
-                T = Tn;
+                if (isnew) slot = map_find(m, tk, k);
+                T += __popc(leaders);
             }
         }
-        if (COUNT && slot >= 0) atomicAdd(&tc[slot], 1u);
+        if (COUNT && slot >= 0) atomicAdd(tc + slot, 1u);
         __syncwarp();
     }
+    __threadfence_block();
+    __syncwarp();
 }
 
 // the dosage pattern of a key: distinct alleles by descending copy count,
@@ -927,12 +969,13 @@ __device__ double chi2_upper(double x, int df) {
 }
 
 // CalcDiversity over a genotype table (keys tk, counts tc, T entries), k2
-// alleles, ni individuals; t1/t2 (keys and counts, GT_CAP each) hold the
-// collapsed tables of the HWE test. out: n, k, ptype, bmaf, he, ho, pic, ae,
-// I, pval (NaN where the reference leaves them undefined).
+// alleles, ni individuals; k1/c1 and k2b/c2 (T entries each) hold the
+// collapsed tables of the HWE test, cm maps their keys (a new stamp per
+// round). out: n, k, ptype, bmaf, he, ho, pic, ae, I, pval (NaN where the
+// reference leaves them undefined).
 template <typename REAL>
 __device__ void general_stats(const uint64_t* tk, const uint32_t* tc, int T, uint64_t* k1, uint32_t* c1,
-                              uint64_t* k2b, uint32_t* c2, int k2, int ni, double* out) {
+                              uint64_t* k2b, uint32_t* c2, SlotMap& cm, int k2, int ni, double* out) {
     const double MINF = 1e-10, NANV = __longlong_as_double(0x7ff8000000000000ll);
     REAL fre[64], ho = 0, how = 0;
     for (int a = 0; a < k2; ++a) fre[a] = 0;
@@ -940,9 +983,9 @@ __device__ void general_stats(const uint64_t* tk, const uint32_t* tc, int T, uin
     bool varploidy = false;
     GtPattern p;
     for (int gi = 0; gi < T; ++gi) {
-        const unsigned c = tc[gi];
+        const unsigned c = __ldcg(tc + gi);
         if (!c) continue;
-        gt_pattern(tk[gi], p);
+        gt_pattern(__ldcg(tk + gi), p);
         const int v = p.v;
         nhaplo += v * c;
         maxp = max(maxp, v);
@@ -1004,11 +1047,12 @@ __device__ void general_stats(const uint64_t* tk, const uint32_t* tc, int T, uin
                     flag = true;
                     G = 0;
                     for (int gi = 0; gi < n1; ++gi) {
-                        if (!cc[gi]) continue;
-                        gt_pattern(ck[gi], p);
+                        const uint32_t cgi = __ldcg(cc + gi);
+                        if (!cgi) continue;
+                        gt_pattern(__ldcg(ck + gi), p);
                         double gfz = gt_hwecoef(p);
                         for (int ai = p.na - 1; ai >= 0; --ai) gfz *= ipow((double)f1[p.key[ai]], p.cnt[ai]);
-                        const REAL obs = (REAL)cc[gi], ex = (REAL)(gfz * n);
+                        const REAL obs = (REAL)cgi, ex = (REAL)(gfz * n);
                         if (ex < 5) { flag = false; break; }
                         G += 2 * obs * rlog(obs / ex);
                     }
@@ -1043,9 +1087,11 @@ __device__ void general_stats(const uint64_t* tk, const uint32_t* tc, int T, uin
                 }
                 // the collapsed table, in order of first mapping
                 int n2 = 0;
+                ++cm.stamp;
                 for (int gi = 0; gi < n1; ++gi) {
-                    if (!cc[gi]) continue;
-                    gt_pattern(ck[gi], p);
+                    const uint32_t cgi = __ldcg(cc + gi);
+                    if (!cgi) continue;
+                    gt_pattern(__ldcg(ck + gi), p);
                     int al[10];
                     for (int ai = 0; ai < ploidy; ++ai) al[ai] = amap[p.al[ai]];
                     for (int x = 1; x < ploidy; ++x) {
@@ -1056,14 +1102,18 @@ __device__ void general_stats(const uint64_t* tk, const uint32_t* tc, int T, uin
                     }
                     uint64_t nk = (uint64_t)ploidy;
                     for (int j = 0; j < ploidy; ++j) {
-                        f2[al[j]] += cc[gi];
+                        f2[al[j]] += cgi;
                         nk |= (uint64_t)(al[j] & 63) << (4 + 6 * j);
                     }
-                    int found = -1;
-                    for (int x = 0; x < n2 && found < 0; ++x)
-                        if (dk[x] == nk) found = x;
-                    if (found < 0) { dk[n2] = nk; dc[n2] = cc[gi]; ++n2; }
-                    else dc[found] += cc[gi];
+                    const int found = map_find(cm, dk, nk);
+                    if (found < 0) {
+                        __stcg(dk + n2, nk);
+                        __stcg(dc + n2, cgi);
+                        map_insert(cm, nk, n2);
+                        ++n2;
+                    } else {
+                        __stcg(dc + found, __ldcg(dc + found) + cgi);
+                    }
                 }
                 {
                     double s = 0;
@@ -1084,53 +1134,51 @@ __device__ void general_stats(const uint64_t* tk, const uint32_t* tc, int T, uin
     out[7] = ae; out[8] = I; out[9] = pval;
 }
 
-// one warp (= block) per locus
+// one warp (= block) per locus, grid-stride; scratch per block: three
+// tables of N keys and N counts, two maps of H entries (H a power of two,
+// at least 2N; zeroed once: stamp 0 is never current)
 __global__ void __launch_bounds__(32) k_locus_filter_general(const int8_t* G, const int8_t* Gt, int64_t L, int N,
                                                              int vmax, const int32_t* nall, vp_locus_filter f,
-                                                             uint8_t* keep, double* stats) {
-    extern __shared__ __align__(16) unsigned char sraw[];
-    uint64_t* tk = reinterpret_cast<uint64_t*>(sraw);
-    uint64_t* k1 = tk + GT_CAP;
-    uint64_t* k2 = k1 + GT_CAP;
-    uint32_t* tc = reinterpret_cast<uint32_t*>(k2 + GT_CAP);
-    uint32_t* c1 = tc + GT_CAP;
-    uint32_t* c2 = c1 + GT_CAP;
-    __shared__ int overflow;
+                                                             uint64_t* keys, uint32_t* counts,
+                                                             unsigned long long* maps, uint32_t H, uint8_t* keep,
+                                                             double* stats) {
     const int lane = threadIdx.x;
+    uint64_t* tk = keys + (size_t)blockIdx.x * 3 * N;
+    uint64_t* k1 = tk + N;
+    uint64_t* k2 = k1 + N;
+    uint32_t* tc = counts + (size_t)blockIdx.x * 3 * N;
+    uint32_t* c1 = tc + N;
+    uint32_t* c2 = c1 + N;
+    SlotMap tm{maps + (size_t)blockIdx.x * 2 * H, H - 1, 0};
+    SlotMap cm{tm.e + H, H - 1, 0};
     for (int64_t l = blockIdx.x; l < L; l += gridDim.x) {
-        if (lane == 0) overflow = 0;
-        __syncwarp();
+        tm.stamp = (uint32_t)(l / gridDim.x) + 1;    // a new stamp for each locus of this block
         const int8_t* g = G + (size_t)l * N * vmax;
-        int T = 0;
         const int kall = nall[l];
+        int T = 0;
         if (Gt) {
-            table_pass<true, false>(Gt + (size_t)l * N * vmax, N, vmax, kall, tk, tc, T, &overflow);
-            table_pass<false, true>(g, N, vmax, kall, tk, tc, T, &overflow);
+            table_pass<true, false>(Gt + (size_t)l * N * vmax, N, vmax, kall, tk, tc, T, tm);
+            table_pass<false, true>(g, N, vmax, kall, tk, tc, T, tm);
         } else {
-            table_pass<true, true>(g, N, vmax, kall, tk, tc, T, &overflow);
+            table_pass<true, true>(g, N, vmax, kall, tk, tc, T, tm);
         }
-        __syncwarp();
         if (lane == 0) {
-            if (overflow) {
-                keep[l] = 2;
-            } else {
-                double o[VP_LOCUS_STATS];
-                if (f.single) general_stats<float>(tk, tc, T, k1, c1, k2, c2, nall[l], N, o);
-                else general_stats<double>(tk, tc, T, k1, c1, k2, c2, nall[l], N, o);
-                const int k = (int)o[1], n = (int)o[0];
-                const bool fail = k == 0 || (f.bmaf_b && k == 2 && outside(o[3], f.bmaf_min, f.bmaf_max)) ||
-                                  (f.k_b && (k < f.k_min || k > f.k_max)) || (f.n_b && (n < f.n_min || n > f.n_max)) ||
-                                  (f.ptype_b && outside(o[2], f.ptype_min, f.ptype_max)) ||
-                                  (f.he_b && outside(o[4], f.he_min, f.he_max)) ||
-                                  (f.ho_b && outside(o[5], f.ho_min, f.ho_max)) ||
-                                  (f.pic_b && outside(o[6], f.pic_min, f.pic_max)) ||
-                                  (f.ae_b && outside(o[7], f.ae_min, f.ae_max)) ||
-                                  (f.I_b && outside(o[8], f.I_min, f.I_max)) ||
-                                  (f.pval_b && o[9] != -1 && outside(o[9], f.pval_min, f.pval_max));
-                keep[l] = fail ? 0 : 1;
-                if (stats)
-                    for (int j = 0; j < VP_LOCUS_STATS; ++j) stats[l * VP_LOCUS_STATS + j] = o[j];
-            }
+            double o[VP_LOCUS_STATS];
+            if (f.single) general_stats<float>(tk, tc, T, k1, c1, k2, c2, cm, nall[l], N, o);
+            else general_stats<double>(tk, tc, T, k1, c1, k2, c2, cm, nall[l], N, o);
+            const int k = (int)o[1], n = (int)o[0];
+            const bool fail = k == 0 || (f.bmaf_b && k == 2 && outside(o[3], f.bmaf_min, f.bmaf_max)) ||
+                              (f.k_b && (k < f.k_min || k > f.k_max)) || (f.n_b && (n < f.n_min || n > f.n_max)) ||
+                              (f.ptype_b && outside(o[2], f.ptype_min, f.ptype_max)) ||
+                              (f.he_b && outside(o[4], f.he_min, f.he_max)) ||
+                              (f.ho_b && outside(o[5], f.ho_min, f.ho_max)) ||
+                              (f.pic_b && outside(o[6], f.pic_min, f.pic_max)) ||
+                              (f.ae_b && outside(o[7], f.ae_min, f.ae_max)) ||
+                              (f.I_b && outside(o[8], f.I_min, f.I_max)) ||
+                              (f.pval_b && o[9] != -1 && outside(o[9], f.pval_min, f.pval_max));
+            keep[l] = fail ? 0 : 1;
+            if (stats)
+                for (int j = 0; j < VP_LOCUS_STATS; ++j) stats[l * VP_LOCUS_STATS + j] = o[j];
         }
         __syncwarp();
     }
@@ -1159,29 +1207,42 @@ extern "C" int vp_locus_filter_general(const int8_t* alleles, const int8_t* alle
     CKI(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     const size_t gb = (size_t)n_loc * n_ind * vmax, tb = alleles_table ? gb : 0, kb = (size_t)n_loc * 4,
                  sb = stats ? (size_t)n_loc * VP_LOCUS_STATS * 8 : 0;
+    uint32_t H = 64;
+    while (H < 2u * (uint32_t)n_ind) H <<= 1;
+    int nsm = 132;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    // a warp per block, 16 blocks per SM, scratch held under 2 GiB
+    const int64_t per_block = (int64_t)n_ind * 3 * 12 + (int64_t)H * 16;
+    const unsigned grid = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>({n_loc, (int64_t)nsm * 16, std::max<int64_t>(nsm, (2ll << 30) / per_block)}));
+    const size_t xb = (size_t)grid * 3 * n_ind * 8, cb = (size_t)grid * 3 * n_ind * 4, mb = (size_t)grid * 2 * H * 8;
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     char* buf = nullptr;
     int rc = VP_OK;
-    cudaError_t e = cudaMallocAsync((void**)&buf, up(gb) + up(tb) + up(kb) + up((size_t)n_loc) + sb, st);
+    cudaError_t e = cudaMallocAsync((void**)&buf, up(gb) + up(tb) + up(kb) + up((size_t)n_loc) + up(sb) + up(xb) +
+                                                      up(cb) + mb, st);
     if (e != cudaSuccess) { vp_set_error("device allocation failed: %s", cudaGetErrorString(e)); rc = VP_E_MEM; }
     std::vector<uint8_t> hk;
     if (!rc) {
-        int8_t* dg = (int8_t*)buf;
-        int8_t* dt = alleles_table ? (int8_t*)(buf + up(gb)) : nullptr;
-        int32_t* dn = (int32_t*)(buf + up(gb) + up(tb));
-        uint8_t* dk = (uint8_t*)(buf + up(gb) + up(tb) + up(kb));
-        double* ds = stats ? (double*)(buf + up(gb) + up(tb) + up(kb) + up((size_t)n_loc)) : nullptr;
+        char* q = buf;
+        int8_t* dg = (int8_t*)q; q += up(gb);
+        int8_t* dt = alleles_table ? (int8_t*)q : nullptr; q += up(tb);
+        int32_t* dn = (int32_t*)q; q += up(kb);
+        uint8_t* dk = (uint8_t*)q; q += up((size_t)n_loc);
+        double* ds = stats ? (double*)q : nullptr; q += up(sb);
+        uint64_t* xk = (uint64_t*)q; q += up(xb);
+        uint32_t* xc = (uint32_t*)q; q += up(cb);
+        unsigned long long* xm = (unsigned long long*)q;
         rc = upload_staged((char*)dg, (const char*)alleles, (int64_t)gb, st);
         if (!rc && dt) rc = upload_staged((char*)dt, (const char*)alleles_table, (int64_t)tb, st);
         if (!rc) {
-            const size_t smem = (size_t)GT_CAP * 3 * (8 + 4);
-            const unsigned grid = (unsigned)std::min<int64_t>(n_loc, 152 * 32);
             hk.resize(n_loc);
-            if ((e = cudaMemcpyAsync(dn, n_alleles, kb, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+            if ((e = cudaMemcpyAsync(dn, n_alleles, kb, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+                (e = cudaMemsetAsync(xm, 0, mb, st)) != cudaSuccess) {
                 vp_set_error("upload failed: %s", cudaGetErrorString(e));
                 rc = VP_E_CUDA;
             } else {
-                k_locus_filter_general<<<grid, 32, smem, st>>>(dg, dt, n_loc, n_ind, vmax, dn, *f, dk, ds);
+                k_locus_filter_general<<<grid, 32, 0, st>>>(dg, dt, n_loc, n_ind, vmax, dn, *f, xk, xc, xm, H, dk, ds);
                 if ((e = cudaGetLastError()) != cudaSuccess ||
                     (e = cudaMemcpyAsync(hk.data(), dk, (size_t)n_loc, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
                     (ds && (e = cudaMemcpyAsync(stats, ds, sb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) ||
@@ -1195,13 +1256,6 @@ extern "C" int vp_locus_filter_general(const int8_t* alleles, const int8_t* alle
     }
     cudaStreamSynchronize(st);
     cudaStreamDestroy(st);
-    if (!rc)
-        for (int64_t l = 0; l < n_loc; ++l) {
-            if (hk[l] == 2) {
-                vp_set_error("locus %lld has more than %d distinct genotypes", (long long)(l + 1), GT_CAP);
-                return VP_E_ARG;
-            }
-            keep[l] = hk[l];
-        }
+    if (!rc) memcpy(keep, hk.data(), (size_t)n_loc);
     return rc;
 }
