@@ -442,7 +442,7 @@ def bench_single(args):
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = byts / (dom_ms / 1e3) / 1e9
     l2 = byts < 120e6
-    roof = {"bound": "hbm", "kernel": "k_update_z_admix_ctr (per-copy labels)" if admix else "k_loglik (likelihood stream)",
+    roof = {"bound": "hbm", "kernel": "k_update_z_admix_ctr (per-copy labels)" if admix else "k_loglik / k_loglik_fma (likelihood stream)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback", "traffic": None,
             "avg_launch_ms": dom_ms, "bytes_per_launch": byts,
@@ -547,7 +547,7 @@ def single_compact(name, local, peaks, cpu_budget_s=0.0):
     out = {"workload": f"{name}: {SINGLE_DESC[name]}; one step = one sweep", "value": upd / (ms / 1e3),
            "unit": "updates/s", "ms_per_step": ms, "steps": n, "warmup": 3, "gpu_launches": launches,
            "roofline": {"bound": "hbm", "kernel": "k_update_z_admix_ctr (per-copy labels)" if admix else
-                        "k_loglik (likelihood stream)", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "k_loglik / k_loglik_fma (likelihood stream)", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "avg_launch_ms": dom_ms, "bytes_per_launch": byts},
            "data_seconds": t_data}
     if cpu_budget_s > 0:
@@ -806,7 +806,7 @@ def plain_form_leg(ctx, lib, upd_step, world, peaks, packed=None, steps=3):
     byts = sum(N_IND * L / 4 + 4 * K * 2 * L + 8 * N_IND * K for K in KS) / len(KS)
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = byts / (dom_ms / 1e3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_loglik (likelihood stream)", "achieved": achieved, "peak": peak,
+    roof = {"bound": "hbm", "kernel": "k_loglik / k_loglik_fma (likelihood stream)", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "avg_launch_ms": dom_ms, "bytes_per_launch": byts,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback",
             "bytes_what": "packed genotypes N*L/4 + frequencies 4*K*2L + per-individual output 8*N*K, per chain"}
@@ -926,7 +926,7 @@ def main():
         byts = [N_IND * ds.L / 4 + 4 * K * 2 * ds.L + 8 * N_IND * K for K in KS]
         achieved = sum(byts) / len(byts) / (dom_avg_ms / 1e3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
-        roof = {"bound": "hbm", "kernel": "k_loglik (likelihood stream)", "achieved": achieved, "peak": peak,
+        roof = {"bound": "hbm", "kernel": "k_loglik / k_loglik_fma (likelihood stream)", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback", "traffic": None}
     roof["avg_launch_ms"] = dom_avg_ms

@@ -473,6 +473,143 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
         if (kg0 + k < K) out[kg0 + k] = (double)s[k] - (double)cmp[k];
 }
 
+// Likelihood stream for 2-bit biallelic diploid data as two FP32 FMAs per
+// (individual, locus, cluster). The table's rows are T0 = 2 ln p0, T1 = ln p0 +
+// ln p1, T2 = 2 ln p1 and 0 for a missing call, so a call of c copies adds
+// typed * (a + c * b) with a = T0 and b = (T2 - T0) / 2 (the halving is
+// exact). Each thread holds M individuals of one genotype word and KC
+// clusters. A call's decode takes one logic op and two FMA-pipe ops: its two
+// code bits, masked in place into the mantissa of 2^23, give c exactly after
+// one FMA that rescales by 2^-2j and subtracts 2^(23-2j), and typed =
+// saturate(3 - c) (the missing code 3 gives typed 0, so the finite a + 3b it
+// meets adds nothing). The decode serves 2 KC FMAs; the slice's (a, b) pairs
+// are shared-memory broadcasts. The slice's table rows and genotype
+// words are copied to shared memory by cp.async one slice ahead. Sums over 32
+// loci are folded into Kahan-compensated FP32 totals, converted to FP64 once
+// per chunk, as in the table form.
+template <int KC>
+struct LfShape {
+    static constexpr int M = KC <= 2 ? 16 : KC <= 6 ? 4 : 2;                 // individuals per thread
+    static constexpr int SL = M >= 8 ? 32 : 64;                               // loci per staged slice
+    static constexpr int GW = LL_BLOCK * M / 16;                              // genotype words per CTA and locus
+    static constexpr int KQ = (KC + 3) / 4;                                   // 16-byte chunks of a staged row
+};
+// The FMA form runs where the table form's groups of four cluster columns
+// would be padded most: K = 1, 2 and K mod 4 = 1 or 2 up to 14 (measured at
+// N = 10,000 over 58,027 loci: K = 1, 2, 5, 6, 9, 10 take 0.24, 0.32, 0.49,
+// 0.49, 0.74, 0.74 ms against the table form's 0.38, 0.38, 0.61, 0.61, 0.79,
+// 0.79; at K = 3, 4, 7, 8 the table form is ahead, 0.38 and 0.61 against
+// 0.40 and 0.65). Its columns: K itself for K <= 2, else 6, 10 or 14.
+__host__ __device__ constexpr bool lf_form(int K) { return K <= 14 && (K % 4 == 1 || K % 4 == 2); }
+__host__ __device__ constexpr int lf_kc(int K) { return K <= 2 ? K : K <= 6 ? 6 : K <= 10 ? 10 : 14; }
+__host__ __device__ constexpr int lf_individuals(int kc) { return LL_BLOCK * (kc <= 2 ? 16 : kc <= 6 ? 4 : 2); }
+template <int KC>
+__global__ void __launch_bounds__(LL_BLOCK) k_loglik_fma(const DevChain* chains, int kgroups, int force,
+                                                         const int4* map = nullptr) {
+    using S = LfShape<KC>;
+    constexpr int M = S::M, SL = S::SL, GW = S::GW, KQ = S::KQ, GS = SL + 4;
+    __shared__ __align__(16) float sT[2][SL][2][4 * KQ];   // rows T0 and T2 of the slice's loci
+    __shared__ __align__(16) float2 sAB[SL][KC];            // (a, b)
+    __shared__ __align__(16) uint32_t sG[2][GW][GS];        // genotype words, transposed
+    const VBlock vb = vblock(map);
+    const DevChain& c = chains[vb.z / kgroups];
+    if (map && run_over(c)) return;
+    const int kg0 = (vb.z % kgroups) * KC;
+    const DevData& D = c.D;
+    const int K = c.K;
+    if (!force && !binaryq_at(c, c.ctl->m)) return;
+    const int64_t l0 = (int64_t)vb.y * c.lchunk;
+    const int64_t l1 = min(D.L, l0 + c.lchunk);
+    if (l0 >= D.L) return;
+    const int i0 = vb.x * LL_BLOCK * M;
+    const int ib = i0 + threadIdx.x * M;
+    const int w0 = i0 >> 4;
+    const int wsel = (threadIdx.x * M) >> 4, sh = (ib & 15) * 2;
+    float acc[M * KC], s[M * KC], cmp[M * KC];
+#pragma unroll
+    for (int j = 0; j < M * KC; ++j) { acc[j] = 0.f; s[j] = 0.f; cmp[j] = 0.f; }
+    // rows and words past the chunk or the data are zero-filled; table columns
+    // past kp are never read (their clusters' sums are not written)
+    auto issue = [&](int64_t ls, int buf) {
+        const int nl = (int)min((int64_t)SL, l1 - ls);
+        for (int j = threadIdx.x; j < SL * 2 * KQ; j += LL_BLOCK) {
+            const int q = j % KQ, r = (j / KQ) & 1, ll = j / (2 * KQ);
+            const bool ok = ll < nl && kg0 + 4 * q < c.kp;
+            const float* src = ok ? c.lt + (((ls + ll) << 2) + 2 * r) * c.kp + kg0 + 4 * q : c.lt;
+            cp_async16(&sT[buf][ll][r][4 * q], src, ok);
+        }
+        for (int j = threadIdx.x; j < SL * GW; j += LL_BLOCK) {
+            const int w = j % GW, ll = j / GW;
+            const bool ok = ll < nl && w0 + w < D.Nw;
+            cp_async4(&sG[buf][w][ll], ok ? D.g2 + (ls + ll) * D.Nw + w0 + w : D.g2, ok);
+        }
+        cp_async_commit();
+    };
+    issue(l0, 0);
+    int buf = 0;
+    for (int64_t ls = l0; ls < l1; ls += SL, buf ^= 1) {
+        if (ls + SL < l1) {
+            issue(ls + SL, buf ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < SL * KC; j += LL_BLOCK) {
+            const int k = j % KC, ll = j / KC;
+            const float t0 = sT[buf][ll][0][k], t2 = sT[buf][ll][1][k];
+            sAB[ll][k] = make_float2(t0, 0.5f * (t2 - t0));
+        }
+        __syncthreads();
+        const uint32_t* gw = &sG[buf][wsel][0];
+        // one locus a step, two in flight: the (a, b) registers of two loci
+        // stay live, not of four
+#pragma unroll 2
+        for (int ll = 0; ll < SL; ++ll) {
+            const uint32_t wd = gw[ll];
+            float a[KC], b[KC];
+            if constexpr (KC == 1) {
+                const float2 v = sAB[ll][0];
+                a[0] = v.x; b[0] = v.y;
+            } else {
+                const float4* ab = reinterpret_cast<const float4*>(&sAB[ll][0]);
+#pragma unroll
+                for (int k = 0; k < KC / 2; ++k) {
+                    const float4 v = ab[k];
+                    a[2 * k] = v.x; b[2 * k] = v.y; a[2 * k + 1] = v.z; b[2 * k + 1] = v.w;
+                }
+            }
+            // this thread's codes from bit 0 (M = 16: individuals 8..15 from
+            // the upper half word)
+            const uint32_t ws = wd >> sh, wh = ws >> 16;
+#pragma unroll
+            for (int j = 0; j < M; ++j) {
+                const int jj = j & 7;
+                const uint32_t src = j < 8 ? ws : wh;
+                const float x = __uint_as_float((src & (3u << (2 * jj))) | 0x4B000000u);
+                const float gf = fmaf(x, 1.0f / (float)(1u << (2 * jj)), -(float)(1u << (23 - 2 * jj)));
+                float tf;   // saturate(3 - c), the clamp folded into the subtraction
+                asm("sub.sat.f32 %0, 0f40400000, %1;" : "=f"(tf) : "f"(gf));
+#pragma unroll
+                for (int k = 0; k < KC; ++k)
+                    acc[j * KC + k] = fmaf(tf, fmaf(gf, b[k], a[k]), acc[j * KC + k]);
+            }
+            if ((ll & 31) == 31) kahan_fold<M * KC>(acc, s, cmp);
+        }
+        __syncthreads();   // sAB and this buffer are rewritten next
+    }
+    kahan_fold<M * KC>(acc, s, cmp);
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        const int i = ib + j;
+        if (i >= D.N) break;
+        double* out = c.LLp + ((int64_t)vb.y * D.N + i) * K;
+#pragma unroll
+        for (int k = 0; k < KC; ++k)
+            if (kg0 + k < K) out[kg0 + k] = (double)s[j * KC + k] - (double)cmp[j * KC + k];
+    }
+}
+
 // PolyLog (src/statistics.cpp:116-155): draw k with probability proportional
 // to exp(LL_k - max); overwrites ll with the weights.
 __device__ __forceinline__ int polylog(double* ll, int K, double u01, bool ref, Rng64* r) {
@@ -727,46 +864,50 @@ __global__ void __launch_bounds__(COUNT_WARPS * 32) k_count_noadmix(const DevCha
 }
 
 // UpdateZNoAdmix counts (src/structure.cpp:1257-1348) for 2-bit packed data,
-// from bit planes. A CTA first writes, for each cluster k of its group and
-// each word w of 16 individuals, the mask with bit 2j set when individual
-// 16w + j has label k (shared memory, KC x Nw words), then walks loci with one
-// warp per locus and the lanes over the locus's words: with lo/hi the two bit
-// planes of the codes (1 = one copy of allele 1, 2 = two, 3 = missing),
-//   allele-1 copies in cluster k = popc(lo & m) + 2 popc(hi & m) - 3 popc(lo & hi & m)
-//   typed calls in cluster k     = n_k - popc(lo & hi & m)
+// from bit planes, two genotype words (32 individuals) per 32-bit plane. With
+// lo/hi the two bit planes of a word's codes (1 = one copy of allele 1, 2 =
+// two, 3 = missing), each at the even bit positions, the planes of words 2p
+// and 2p + 1 merge into one word (the second on the odd positions): LO, HI and
+// MS = LO & HI. A CTA first writes, for each cluster k of its group and each
+// word pair p, the mask with the bits of the pair's individuals labelled k
+// (shared memory, KC x Np words), then walks loci with one warp per locus and
+// the lanes over the locus's word pairs:
+//   allele-1 copies in cluster k = popc(LO & m) + 2 popc(HI & m) - 3 popc(MS & m)
+//   typed calls in cluster k     = n_k - popc(MS & m)
 // and allele-0 copies = 2 x typed - allele-1 copies. Integer and exact; the
 // same Ni as k_count_noadmix. grid.z = cluster groups of KC.
 template <int KC>
 __global__ void __launch_bounds__(256) k_count_packed(const DevChain* chains, int kgroups, int force, const int4* map = nullptr) {
-    extern __shared__ uint32_t smask[];   // [KC][Nw] masks, then [KC] cluster sizes
+    extern __shared__ uint32_t smask[];   // [KC][Np] masks, then [KC] cluster sizes
     const VBlock vb = vblock(map);
     const DevChain& c = chains[vb.z / kgroups];
     if (map && run_over(c)) return;
     const int kg0 = (vb.z % kgroups) * KC;
     const DevData& D = c.D;
-    const int K = c.K, Nw = D.Nw;
+    const int K = c.K, Nw = D.Nw, Np = (D.Nw + 1) >> 1;
     if (!force && !binaryq_at(c, c.ctl->m)) return;
     const int kn = min(KC, K - kg0);
-    int32_t* nk = reinterpret_cast<int32_t*>(smask + (size_t)KC * Nw);
+    int32_t* nk = reinterpret_cast<int32_t*>(smask + (size_t)KC * Np);
     if (threadIdx.x < KC) nk[threadIdx.x] = 0;
     __syncthreads();
     int cnt[KC];
 #pragma unroll
     for (int k = 0; k < KC; ++k) cnt[k] = 0;
-    for (int w = threadIdx.x; w < Nw; w += blockDim.x) {
+    for (int p = threadIdx.x; p < Np; p += blockDim.x) {
         uint32_t mk[KC];
 #pragma unroll
         for (int k = 0; k < KC; ++k) mk[k] = 0;
-        for (int j = 0; j < 16; ++j) {
-            const int i = 16 * w + j;
+        for (int j = 0; j < 32; ++j) {
+            const int i = 32 * p + j;   // word 2p + (j >> 4), position j & 15
             const int z = i < D.N ? (int)c.Z[i] - kg0 : -1;
+            const uint32_t bit = 1u << (2 * (j & 15) + (j >> 4));
 #pragma unroll
             for (int k = 0; k < KC; ++k)
-                if (z == k) mk[k] |= 1u << (2 * j);
+                if (z == k) mk[k] |= bit;
         }
 #pragma unroll
         for (int k = 0; k < KC; ++k) {
-            smask[(size_t)k * Nw + w] = mk[k];
+            smask[(size_t)k * Np + p] = mk[k];
             cnt[k] += __popc(mk[k]);
         }
     }
@@ -780,24 +921,20 @@ __global__ void __launch_bounds__(256) k_count_packed(const DevChain* chains, in
         int a1[KC], n3[KC];
 #pragma unroll
         for (int k = 0; k < KC; ++k) { a1[k] = 0; n3[k] = 0; }
-        // two words per lane in flight
-        for (int w0 = lane; w0 < Nw; w0 += 64) {
-            const int w1 = w0 + 32;
-            const uint32_t g0 = __ldg(row + w0), g1 = w1 < Nw ? __ldg(row + w1) : 0xFFFFFFFFu;
+        for (int p = lane; p < Np; p += 32) {
+            // a missing word past the row's end: its masks are 0
+            const uint32_t g0 = __ldg(row + 2 * p), g1 = 2 * p + 1 < Nw ? __ldg(row + 2 * p + 1) : 0xFFFFFFFFu;
+            // bit select: even positions from the first operand, odd from the second
+            const uint32_t LO = (g0 & 0x55555555u) | ((g1 << 1) & 0xAAAAAAAAu);
+            const uint32_t HI = ((g0 >> 1) & 0x55555555u) | (g1 & 0xAAAAAAAAu);
+            const uint32_t MS = LO & HI;
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int w = h ? w1 : w0;
-                if (w >= Nw) break;
-                const uint32_t g = h ? g1 : g0;
-                const uint32_t lo = g & 0x55555555u, hi = (g >> 1) & 0x55555555u, ms = lo & hi;
-#pragma unroll
-                for (int k = 0; k < KC; ++k) {
-                    if (k < kn) {
-                        const uint32_t m = smask[(size_t)k * Nw + w];
-                        const int p3 = __popc(ms & m);
-                        a1[k] += __popc(lo & m) + 2 * __popc(hi & m) - 3 * p3;
-                        n3[k] += p3;
-                    }
+            for (int k = 0; k < KC; ++k) {
+                if (k < kn) {
+                    const uint32_t m = smask[(size_t)k * Np + p];
+                    const int p3 = __popc(MS & m);
+                    a1[k] += __popc(LO & m) + 2 * __popc(HI & m) - 3 * p3;
+                    n3[k] += p3;
                 }
             }
         }

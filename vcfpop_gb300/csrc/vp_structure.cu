@@ -85,6 +85,7 @@ struct vp_chain {
     int total = 0;        // sweeps of the run: nburnin (+ admixture burn-in) + nreps
     int issued = 0;       // sweeps launched so far
     int kc = 16, kgroups = 1;
+    bool ll_fma = false;   // likelihood stream in the FMA form (else the table form)
     bool arranged = false;
     double* ancestry = nullptr;
     cudaGraphExec_t graph = nullptr;
@@ -285,11 +286,68 @@ struct Carve {
 
 int kc_for(int K) { return K <= 4 ? 4 : K <= 8 ? 8 : K <= 12 ? 12 : 16; }
 
+// likelihood-stream columns and individuals per CTA: the FMA form (2-bit
+// data and the cluster counts lf_form picks) or the table form
+int ll_kc(bool fma, int K) { return fma ? lf_kc(K) : kc_for(K); }
+int ll_individuals(bool fma, int kc) { return fma ? lf_individuals(kc) : LL_BLOCK; }
+
+// resident CTAs per SM of the FMA form's instantiation for kc columns (its
+// registers and shared memory), looked up once per process
+int lf_resident(int kc) {
+    static std::mutex mu;
+    static int occ[17] = {0};
+    std::lock_guard<std::mutex> lk(mu);
+    if (kc < 1 || kc > 16) return 1;
+    if (!occ[kc]) {
+        const void* fn = nullptr;
+        switch (kc) {
+            case 1: fn = (const void*)k_loglik_fma<1>; break;
+            case 2: fn = (const void*)k_loglik_fma<2>; break;
+            case 6: fn = (const void*)k_loglik_fma<6>; break;
+            case 10: fn = (const void*)k_loglik_fma<10>; break;
+            default: fn = (const void*)k_loglik_fma<14>; break;
+        }
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, LL_BLOCK, 0) != cudaSuccess || n < 1) {
+            cudaGetLastError();
+            n = 1;
+        }
+        occ[kc] = n;
+    }
+    return occ[kc];
+}
+
+// locus chunks of the likelihood stream. The FMA form fills whole waves of
+// its resident CTAs (one wave when the chunks stay long enough: no tail, and
+// few chunk partials for the label draw to sum); the table form runs about 12
+// of its small CTAs per SM, enough warps to cover the genotype stream's
+// latency. Chunks hold at least 64 loci.
+int64_t ll_chunks(bool fma, int kc, int kgroups, int32_t N, int64_t L, int nsm) {
+    const int64_t nbi = cdiv(N, ll_individuals(fma, kc)) * (int64_t)kgroups;
+    const int64_t maxc = std::max<int64_t>(1, L / 64);
+    if (!fma) return std::min(std::max<int64_t>(1, (int64_t)nsm * 12 / std::max<int64_t>(nbi, 1)), maxc);
+    const int64_t slots = (int64_t)nsm * lf_resident(kc);
+    int64_t nch = std::max<int64_t>(1, slots / nbi);
+    if (nch > maxc) nch = maxc;
+    return nch;
+}
+
 int launch_loglik(vp_chain* c, int force) {
     vp_ctx* x = c->ctx;
-    dim3 g(cdiv(x->N, LL_BLOCK), c->h.nchunk, c->kgroups);
     prof_mark(x, true);
     struct End { vp_ctx* x; ~End() { prof_mark(x, false); } } end_{x};
+    if (c->ll_fma) {
+        const dim3 g(cdiv(x->N, lf_individuals(c->kc)), c->h.nchunk, c->kgroups);
+        switch (c->kc) {
+            case 1: SL(c, k_loglik_fma<1>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+            case 2: SL(c, k_loglik_fma<2>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+            case 6: SL(c, k_loglik_fma<6>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+            case 10: SL(c, k_loglik_fma<10>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+            default: SL(c, k_loglik_fma<14>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+        }
+        return VP_OK;
+    }
+    dim3 g(cdiv(x->N, LL_BLOCK), c->h.nchunk, c->kgroups);
     switch (c->kc) {
         case 4: SL(c, k_loglik<4>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
         case 8: SL(c, k_loglik<8>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
@@ -391,7 +449,7 @@ int launch_count(vp_chain* c, int force) {
     if (x->packed2) {
         const int kc = K <= 4 ? 4 : K <= 8 ? 8 : 16;
         const int kgroups = (K + kc - 1) / kc;
-        const size_t sm = (size_t)kc * x->D.Nw * 4 + kc * 4;
+        const size_t sm = (size_t)kc * ((x->D.Nw + 1) / 2) * 4 + kc * 4;   // masks per word pair, sizes
         if (sm <= 200 * 1024 && x->D.Nw >= 32) {
             const dim3 g((unsigned)std::min<int64_t>(cdiv(x->L, 8), (int64_t)x->nsm * 8), 1, (unsigned)kgroups);
             switch (kc) {
@@ -694,15 +752,11 @@ int chain_plan(const vp_ctx* x, const vp_params* P, vp_chain* c, size_t* bytes) 
     // lnL trace records: ceil(nburnin / t) + ceil(nreps / t), plus slack;
     // Record never writes more than this many
     h.ntrace = (int32_t)(h.nburnin / h.nthinning + h.nreps / h.nthinning + 2);
-    c->kc = kc_for(K);
+    c->ll_fma = x->packed2 && lf_form(K);
+    c->kc = ll_kc(c->ll_fma, K);
     c->kgroups = (K + c->kc - 1) / c->kc;
-    // locus chunks for the likelihood passes: about 12 CTAs per SM, so that
-    // enough warps are resident to cover the genotype stream's latency
     {
-        int64_t nbi = cdiv(N, LL_BLOCK) * (int64_t)c->kgroups;
-        int64_t want = std::max<int64_t>(1, (int64_t)x->nsm * 12 / std::max<int64_t>(nbi, 1));
-        int64_t maxc = std::max<int64_t>(1, L / 64);
-        int64_t nch = std::min(want, maxc);
+        const int64_t nch = ll_chunks(c->ll_fma, c->kc, c->kgroups, N, L, x->nsm);
         h.lchunk = (int32_t)((L + nch - 1) / nch);
         h.nchunk = (int32_t)((L + h.lchunk - 1) / h.lchunk);
     }
@@ -2637,6 +2691,7 @@ struct LLPlan {
     DevChain h{};
     size_t scratch = 0;   // bytes: descriptor, table, partials
     int kc = 16, kgroups = 1;
+    bool fma = false;
 };
 
 int ll_plan(int32_t N, int64_t L, int32_t K, int nsm, LLPlan* pl) {
@@ -2645,10 +2700,10 @@ int ll_plan(int32_t N, int64_t L, int32_t K, int nsm, LLPlan* pl) {
     h.D.N = N; h.D.L = L; h.D.KT = 2 * L; h.D.Nw = (N + 15) / 16; h.D.packed2 = 1; h.D.vmax = 2; h.D.maxK = 2;
     h.K = K;
     h.kp = (K + 3) & ~3;
-    pl->kc = kc_for(K);
+    pl->fma = lf_form(K);
+    pl->kc = ll_kc(pl->fma, K);
     pl->kgroups = (K + pl->kc - 1) / pl->kc;
-    int64_t nbi = cdiv(N, LL_BLOCK) * (int64_t)pl->kgroups;
-    int64_t nch = std::min<int64_t>(std::max<int64_t>(1, (int64_t)nsm * 4 / nbi), std::max<int64_t>(1, L / 64));
+    const int64_t nch = ll_chunks(pl->fma, pl->kc, pl->kgroups, N, L, nsm);
     h.lchunk = (int32_t)((L + nch - 1) / nch);
     h.nchunk = (int32_t)((L + h.lchunk - 1) / h.lchunk);
     Carve cv{nullptr};
@@ -2671,12 +2726,22 @@ int ll_run(LLPlan& pl, const uint32_t* geno, const float* freq, double* ll, void
     // to outlive the call
     k_set_chain<<<1, 128, 0, s>>>(d, h);
     k_lt_from_freq<<<cdiv((int64_t)h.K * h.D.L, 256), 256, 0, s>>>(freq, h.K, h.D.L, h.kp, h.lt);
-    dim3 g(cdiv(h.D.N, LL_BLOCK), h.nchunk, pl.kgroups);
-    switch (pl.kc) {
-        case 4: k_loglik<4><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
-        case 8: k_loglik<8><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
-        case 12: k_loglik<12><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
-        default: k_loglik<16><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+    const dim3 g(cdiv(h.D.N, ll_individuals(pl.fma, pl.kc)), h.nchunk, pl.kgroups);
+    if (pl.fma) {
+        switch (pl.kc) {
+            case 1: k_loglik_fma<1><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            case 2: k_loglik_fma<2><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            case 6: k_loglik_fma<6><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            case 10: k_loglik_fma<10><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            default: k_loglik_fma<14><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+        }
+    } else {
+        switch (pl.kc) {
+            case 4: k_loglik<4><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            case 8: k_loglik<8><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            case 12: k_loglik<12><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            default: k_loglik<16><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+        }
     }
     k_ll_reduce<<<std::min<unsigned>(1024, cdiv((int64_t)h.D.N * h.K, 256)), 256, 0, s>>>(d, ll);
     CK(cudaGetLastError());
