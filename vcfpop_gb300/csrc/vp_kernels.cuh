@@ -921,20 +921,32 @@ __global__ void __launch_bounds__(256) k_count_packed(const DevChain* chains, in
         int a1[KC], n3[KC];
 #pragma unroll
         for (int k = 0; k < KC; ++k) { a1[k] = 0; n3[k] = 0; }
-        for (int p = lane; p < Np; p += 32) {
-            // a missing word past the row's end: its masks are 0
-            const uint32_t g0 = __ldg(row + 2 * p), g1 = 2 * p + 1 < Nw ? __ldg(row + 2 * p + 1) : 0xFFFFFFFFu;
-            // bit select: even positions from the first operand, odd from the second
-            const uint32_t LO = (g0 & 0x55555555u) | ((g1 << 1) & 0xAAAAAAAAu);
-            const uint32_t HI = ((g0 >> 1) & 0x55555555u) | (g1 & 0xAAAAAAAAu);
-            const uint32_t MS = LO & HI;
+        // four word pairs per lane in flight: their eight loads first
+        for (int p0 = lane; p0 < Np; p0 += 128) {
+            uint32_t g0[4], g1[4];
 #pragma unroll
-            for (int k = 0; k < KC; ++k) {
-                if (k < kn) {
-                    const uint32_t m = smask[(size_t)k * Np + p];
-                    const int p3 = __popc(MS & m);
-                    a1[k] += __popc(LO & m) + 2 * __popc(HI & m) - 3 * p3;
-                    n3[k] += p3;
+            for (int u = 0; u < 4; ++u) {
+                const int p = p0 + 32 * u;
+                // a missing word past the row's end: its masks are 0
+                g0[u] = p < Np ? __ldg(row + 2 * p) : 0xFFFFFFFFu;
+                g1[u] = p < Np && 2 * p + 1 < Nw ? __ldg(row + 2 * p + 1) : 0xFFFFFFFFu;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int p = p0 + 32 * u;
+                if (p >= Np) break;
+                // bit select: even positions from the first operand, odd from the second
+                const uint32_t LO = (g0[u] & 0x55555555u) | ((g1[u] << 1) & 0xAAAAAAAAu);
+                const uint32_t HI = ((g0[u] >> 1) & 0x55555555u) | (g1[u] & 0xAAAAAAAAu);
+                const uint32_t MS = LO & HI;
+#pragma unroll
+                for (int k = 0; k < KC; ++k) {
+                    if (k < kn) {
+                        const uint32_t m = smask[(size_t)k * Np + p];
+                        const int p3 = __popc(MS & m);
+                        a1[k] += __popc(LO & m) + 2 * __popc(HI & m) - 3 * p3;
+                        n3[k] += p3;
+                    }
                 }
             }
         }
