@@ -40,3 +40,37 @@ def test_loglik_packed2_matches_float64(N, L, K):
     ref = loglik_ref(d["G"], freq)
     rel = np.abs(out.cpu().numpy() - ref) / np.abs(ref)
     assert rel.max() < 1e-5, rel.max()
+
+
+def _loglik_device(G, freq, N, L, K):
+    import torch
+    packed = S.pack2(G)
+    g = torch.from_numpy(packed.view(np.int32)).cuda()
+    f = torch.from_numpy(freq).cuda()
+    out = torch.full((N, K), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    B.check(B.lib().vp_loglik_packed2(g.data_ptr(), N, L, f.data_ptr(), K, out.data_ptr(), None))
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("N", [5, 701, 5003])
+def test_loglik_packed2_every_cluster_count(N):
+    """Every K from 1 to 17 against float64: the FMA form (K = 1, 2, 5, 6, 9,
+    10, 13, 14: 1, 2, 6, 10 or 14 columns, 16, 4 or 2 individuals per thread)
+    and the table form (the other K, 4 to 16 columns, two groups at K = 17);
+    N below one genotype word, N with a partial last word, and N spanning
+    several CTA columns of every instantiation."""
+    L = 900 if N > 1000 else 1500
+    d = synth.fmodel(N + 17, N, L, 3, 0.1, 0.05)
+    rng = np.random.default_rng(N)
+    for K in range(1, 18):
+        p = rng.dirichlet([0.7, 0.7], size=(K, L)).astype(np.float32)
+        p = np.maximum(p, 1e-6)
+        p /= p.sum(axis=2, keepdims=True)
+        freq = np.ascontiguousarray(p.reshape(K, 2 * L))
+        got = _loglik_device(d["G"], freq, N, L, K)
+        ref = loglik_ref(d["G"], freq)
+        assert np.isfinite(got).all(), K
+        rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)
+        assert rel.max() < 1e-5, (K, rel.max())

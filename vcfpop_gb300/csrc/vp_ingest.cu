@@ -1211,10 +1211,11 @@ extern "C" int vp_locus_filter_general(const int8_t* alleles, const int8_t* alle
     while (H < 2u * (uint32_t)n_ind) H <<= 1;
     int nsm = 132;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
-    // a warp per block, 16 blocks per SM, scratch held under 2 GiB
+    // a warp per block, 16 blocks per SM, scratch held under 2 GiB (fewer
+    // blocks than SMs for very large samples)
     const int64_t per_block = (int64_t)n_ind * 3 * 12 + (int64_t)H * 16;
     const unsigned grid = (unsigned)std::max<int64_t>(
-        1, std::min<int64_t>({n_loc, (int64_t)nsm * 16, std::max<int64_t>(nsm, (2ll << 30) / per_block)}));
+        1, std::min<int64_t>({n_loc, (int64_t)nsm * 16, (2ll << 30) / per_block}));
     const size_t xb = (size_t)grid * 3 * n_ind * 8, cb = (size_t)grid * 3 * n_ind * 4, mb = (size_t)grid * 2 * H * 8;
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     char* buf = nullptr;
