@@ -1604,16 +1604,24 @@ int tc_operands(vp_ctx* x) {
     t.Bc = (double*)q; q += t.Npad * 8;
     t.err = (int*)q; q += 256;
     float* part = (float*)q;
-    tc::k_allele_center<<<cdiv(x->L * 32, 256), 256, 0, x->stream>>>(x->D, t.logpbar);
-    int rc = check_launch(x, "k_allele_center");
-    if (rc) return rc;
-    tc::k_build_counts<<<dim3((unsigned)(t.Npad / 128), groups, 1), 256, 0, x->stream>>>(x->D, t.C, t.CT, t.Apad, t.Npad,
-                                                                                      t.logpbar, part);
-    if ((rc = check_launch(x, "k_build_counts"))) return rc;
-    tc::k_center_sum<<<cdiv(x->N, 256), 256, 0, x->stream>>>(x->D, part, (int)groups, t.Npad, t.Bc);
-    if ((rc = check_launch(x, "k_center_sum"))) return rc;
-    if ((rc = make_map(&t.mapC, t.C, t.Npad, t.Apad, t.Apad, 128, t.bk))) return rc;
-    if ((rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128, t.bk8, 1))) return rc;
+    int rc = VP_OK;
+    do {
+        tc::k_allele_center<<<cdiv(x->L * 32, 256), 256, 0, x->stream>>>(x->D, t.logpbar);
+        if ((rc = check_launch(x, "k_allele_center"))) break;
+        tc::k_build_counts<<<dim3((unsigned)(t.Npad / 128), groups, 1), 256, 0, x->stream>>>(
+            x->D, t.C, t.CT, t.Apad, t.Npad, t.logpbar, part);
+        if ((rc = check_launch(x, "k_build_counts"))) break;
+        tc::k_center_sum<<<cdiv(x->N, 256), 256, 0, x->stream>>>(x->D, part, (int)groups, t.Npad, t.Bc);
+        if ((rc = check_launch(x, "k_center_sum"))) break;
+        if ((rc = make_map(&t.mapC, t.C, t.Npad, t.Apad, t.Apad, 128, t.bk))) break;
+        rc = make_map(&t.mapCT, t.CT, t.Apad, t.Npad, t.Npad, 128, t.bk8, 1);
+    } while (0);
+    if (rc) {
+        // nothing keeps the operands: a later call starts over
+        x->allocs.pop_back();
+        dev_free(p, x->stream);
+        return rc;
+    }
     t.ready = true;
     return VP_OK;
 }
