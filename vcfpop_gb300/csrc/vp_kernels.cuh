@@ -10,7 +10,7 @@
 namespace vp {
 
 constexpr int KG = 16;          // clusters per thread in the likelihood kernels
-constexpr int LL_BLOCK = 128;   // individuals per likelihood CTA
+constexpr int LL_BLOCK = 128;   // threads per likelihood CTA (the table form: one individual each)
 constexpr int SUB = 32;         // loci per FP32 sub-sum before folding into FP64
 
 struct DevData {
