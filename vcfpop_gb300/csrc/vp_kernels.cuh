@@ -10,7 +10,8 @@
 namespace vp {
 
 constexpr int KG = 16;          // clusters per thread in the likelihood kernels
-constexpr int LL_BLOCK = 128;   // threads per likelihood CTA (the table form: one individual each)
+constexpr int LL_BLOCK = 128;   // threads per CTA of the likelihood stream's FMA form
+constexpr int LT_BLOCK = 256;   // threads (= individuals) per CTA of its table form
 constexpr int SUB = 32;         // loci per FP32 sub-sum before folding into FP64
 
 struct DevData {
@@ -327,7 +328,7 @@ __global__ void k_update_p_ctr(const DevChain* chains, const int4* map = nullptr
 // ---------------------------------------------------------------------------
 // Log-likelihood of every individual under every cluster (the locus loop of
 // UpdateQNoAdmix, src/structure.cpp:902-932): LL[i,k] = sum over loci and
-// copies of ln p_{k,l,allele}. One thread per individual, 128 per CTA; grid.y
+// copies of ln p_{k,l,allele}. One thread per individual, 256 per CTA; grid.y
 // splits the loci into chunks whose FP64 partials are summed in a fixed order
 // by the sampling kernel. Biallelic diploid data: each 32-locus slice of the
 // per-genotype log-probability table is staged in shared memory and folded
@@ -368,9 +369,9 @@ __device__ __forceinline__ void kahan_fold(float* acc, float* s, float* cmp) {
 template <int KC>
 __host__ __device__ constexpr int ll_stride() { return (KC / 4) % 2 ? KC : KC + 4; }
 template <int KC>
-__global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int kgroups, int force, const int4* map = nullptr) {
+__global__ void __launch_bounds__(LT_BLOCK, 3) k_loglik(const DevChain* chains, int kgroups, int force, const int4* map = nullptr) {
     constexpr int TS = ll_stride<KC>();
-    constexpr int GW = LL_BLOCK / 16;          // genotype words per CTA and locus
+    constexpr int GW = LT_BLOCK / 16;          // genotype words per CTA and locus
     constexpr int GS = LL_SL + 4;              // padded row of the transposed words
     __shared__ __align__(16) float sT[2][LL_SL][4][TS];       // two slices in flight
     __shared__ __align__(16) float sP[LL_SL / 2][16][TS];
@@ -382,7 +383,7 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
     const DevData& D = c.D;
     const int K = c.K;
     if (!force && !binaryq_at(c, c.ctl->m)) return;
-    const int i0 = vb.x * LL_BLOCK;
+    const int i0 = vb.x * LT_BLOCK;
     const int i = i0 + threadIdx.x;
     const int64_t l0 = (int64_t)vb.y * c.lchunk;
     const int64_t l1 = min(D.L, l0 + c.lchunk);
@@ -402,13 +403,13 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
         constexpr int Q4 = KC / 4;                          // 16-byte chunks per table row
         auto issue = [&](int64_t ls, int buf) {
             const int nl = (int)min((int64_t)LL_SL, l1 - ls);
-            for (int j = threadIdx.x; j < LL_SL * 4 * Q4; j += LL_BLOCK) {
+            for (int j = threadIdx.x; j < LL_SL * 4 * Q4; j += LT_BLOCK) {
                 const int q = j % Q4, row = j / Q4;
                 const bool ok = (row >> 2) < nl && kg0 + 4 * q < c.kp;
                 const float* src = ok ? c.lt + ((ls << 2) + row) * c.kp + kg0 + 4 * q : c.lt;
                 cp_async16(&sT[buf][row >> 2][row & 3][4 * q], src, ok);
             }
-            for (int j = threadIdx.x; j < LL_SL * GW; j += LL_BLOCK) {
+            for (int j = threadIdx.x; j < LL_SL * GW; j += LT_BLOCK) {
                 const int ll = j % LL_SL, w = j / LL_SL;
                 const bool ok = ll < nl && w0 + w < D.Nw;
                 cp_async4(&sG[buf][w][ll], ok ? D.g2 + (ls + ll) * D.Nw + w0 + w : D.g2, ok);
@@ -426,7 +427,7 @@ __global__ void __launch_bounds__(LL_BLOCK) k_loglik(const DevChain* chains, int
             }
             __syncthreads();
             // pair rows: sP[p][a | b << 2] = sT[2p][a] + sT[2p + 1][b]
-            for (int j = threadIdx.x; j < (LL_SL / 2) * 16 * Q4; j += LL_BLOCK) {
+            for (int j = threadIdx.x; j < (LL_SL / 2) * 16 * Q4; j += LT_BLOCK) {
                 const int q = j % Q4, cp = (j / Q4) & 15, p = j / (16 * Q4);
                 const float4 x = *reinterpret_cast<const float4*>(&sT[buf][2 * p][cp & 3][4 * q]);
                 const float4 y = *reinterpret_cast<const float4*>(&sT[buf][2 * p + 1][cp >> 2][4 * q]);
@@ -498,8 +499,9 @@ struct LfShape {
 // would be padded most: K = 1, 2 and K mod 4 = 1 or 2 up to 14 (measured at
 // N = 10,000 over 58,027 loci: K = 1, 2, 5, 6, 9, 10 take 0.24, 0.32, 0.49,
 // 0.49, 0.74, 0.74 ms against the table form's 0.38, 0.38, 0.61, 0.61, 0.79,
-// 0.79; at K = 3, 4, 7, 8 the table form is ahead, 0.38 and 0.61 against
-// 0.40 and 0.65). Its columns: K itself for K <= 2, else 6, 10 or 14.
+// 0.79 with 128-thread table CTAs; at K = 3, 4, 7, 8 the table form is ahead,
+// 0.34 and 0.57 with 256-thread CTAs against 0.40 and 0.65). Its columns: K
+// itself for K <= 2, else 6, 10 or 14.
 __host__ __device__ constexpr bool lf_form(int K) { return K <= 14 && (K % 4 == 1 || K % 4 == 2); }
 __host__ __device__ constexpr int lf_kc(int K) { return K <= 2 ? K : K <= 6 ? 6 : K <= 10 ? 10 : 14; }
 __host__ __device__ constexpr int lf_individuals(int kc) { return LL_BLOCK * (kc <= 2 ? 16 : kc <= 6 ? 4 : 2); }

@@ -289,7 +289,7 @@ int kc_for(int K) { return K <= 4 ? 4 : K <= 8 ? 8 : K <= 12 ? 12 : 16; }
 // likelihood-stream columns and individuals per CTA: the FMA form (2-bit
 // data and the cluster counts lf_form picks) or the table form
 int ll_kc(bool fma, int K) { return fma ? lf_kc(K) : kc_for(K); }
-int ll_individuals(bool fma, int kc) { return fma ? lf_individuals(kc) : LL_BLOCK; }
+int ll_individuals(bool fma, int kc) { return fma ? lf_individuals(kc) : LT_BLOCK; }
 
 // resident CTAs per SM of the FMA form's instantiation for kc columns (its
 // registers and shared memory), looked up once per process
@@ -325,7 +325,7 @@ int lf_resident(int kc) {
 int64_t ll_chunks(bool fma, int kc, int kgroups, int32_t N, int64_t L, int nsm) {
     const int64_t nbi = cdiv(N, ll_individuals(fma, kc)) * (int64_t)kgroups;
     const int64_t maxc = std::max<int64_t>(1, L / 64);
-    if (!fma) return std::min(std::max<int64_t>(1, (int64_t)nsm * 12 / std::max<int64_t>(nbi, 1)), maxc);
+    if (!fma) return std::min(std::max<int64_t>(1, (int64_t)nsm * 12 * LL_BLOCK / LT_BLOCK / std::max<int64_t>(nbi, 1)), maxc);
     const int64_t slots = (int64_t)nsm * lf_resident(kc);
     int64_t nch = std::max<int64_t>(1, slots / nbi);
     if (nch > maxc) nch = maxc;
@@ -347,12 +347,12 @@ int launch_loglik(vp_chain* c, int force) {
         }
         return VP_OK;
     }
-    dim3 g(cdiv(x->N, LL_BLOCK), c->h.nchunk, c->kgroups);
+    dim3 g(cdiv(x->N, LT_BLOCK), c->h.nchunk, c->kgroups);
     switch (c->kc) {
-        case 4: SL(c, k_loglik<4>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
-        case 8: SL(c, k_loglik<8>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
-        case 12: SL(c, k_loglik<12>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
-        default: SL(c, k_loglik<16>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
+        case 4: SL(c, k_loglik<4>, (g), (LT_BLOCK), 0, 2, c->kgroups, force); break;
+        case 8: SL(c, k_loglik<8>, (g), (LT_BLOCK), 0, 2, c->kgroups, force); break;
+        case 12: SL(c, k_loglik<12>, (g), (LT_BLOCK), 0, 2, c->kgroups, force); break;
+        default: SL(c, k_loglik<16>, (g), (LT_BLOCK), 0, 2, c->kgroups, force); break;
     }
     return VP_OK;
 }
@@ -2745,10 +2745,10 @@ int ll_run(LLPlan& pl, const uint32_t* geno, const float* freq, double* ll, void
         }
     } else {
         switch (pl.kc) {
-            case 4: k_loglik<4><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
-            case 8: k_loglik<8><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
-            case 12: k_loglik<12><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
-            default: k_loglik<16><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            case 4: k_loglik<4><<<g, LT_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            case 8: k_loglik<8><<<g, LT_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            case 12: k_loglik<12><<<g, LT_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
+            default: k_loglik<16><<<g, LT_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
         }
     }
     k_ll_reduce<<<std::min<unsigned>(1024, cdiv((int64_t)h.D.N * h.K, 256)), 256, 0, s>>>(d, ll);
