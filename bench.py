@@ -1009,7 +1009,7 @@ def main():
 
     # ---- end to end through the C ABI: upload from pinned host memory, create
     # the chains, sweep, read every chain's likelihood back, close
-    e2e_steps, e2e_ms = 5, []   # the median of five (host allocation times vary by several ms between steps)
+    e2e_steps, e2e_ms = 5, []   # the median of five: single steps vary by several ms
     h2d = ds.L * ((N_IND + 15) // 16) * 4 + ds.L * (4 + 8) + N_IND * (8 + 4)
     d2h = 8 * len(KS)
     for it in range(0 if args.no_e2e else e2e_steps + 1):
