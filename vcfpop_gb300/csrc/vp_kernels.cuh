@@ -496,12 +496,13 @@ struct LfShape {
     static constexpr int KQ = (KC + 3) / 4;                                   // 16-byte chunks of a staged row
 };
 // The FMA form runs where the table form's groups of four cluster columns
-// would be padded most: K = 1, 2 and K mod 4 = 1 or 2 up to 14 (measured at
-// N = 10,000 over 58,027 loci: K = 1, 2, 5, 6, 9, 10 take 0.24, 0.32, 0.49,
-// 0.49, 0.74, 0.74 ms against the table form's 0.38, 0.38, 0.61, 0.61, 0.79,
-// 0.79 with 128-thread table CTAs; at K = 3, 4, 7, 8 the table form is ahead,
-// 0.34 and 0.57 with 256-thread CTAs against 0.40 and 0.65). Its columns: K
-// itself for K <= 2, else 6, 10 or 14.
+// would be padded most: K = 1, 2 and K mod 4 = 1 or 2 up to 14. Measured at
+// N = 10,000 over 58,027 loci (ms, FMA form / table form with 256-individual
+// CTAs): K = 1 0.24 / 0.34, K = 2 0.32 / 0.34, K = 5, 6 0.49 / 0.56, K = 9, 10
+// 0.74 / 0.74, K = 13, 14 0.98 / 1.00; at K = 3, 4, 7, 8 the table form is
+// ahead (0.34 and 0.57 against 0.40 and 0.65 for the FMA form's 4- and
+// 8-column kernels, which are not kept). Its columns: K itself for K <= 2,
+// else 6, 10 or 14.
 __host__ __device__ constexpr bool lf_form(int K) { return K <= 14 && (K % 4 == 1 || K % 4 == 2); }
 __host__ __device__ constexpr int lf_kc(int K) { return K <= 2 ? K : K <= 6 ? 6 : K <= 10 ? 10 : 14; }
 __host__ __device__ constexpr int lf_individuals(int kc) { return LL_BLOCK * (kc <= 2 ? 16 : kc <= 6 ? 4 : 2); }
