@@ -56,9 +56,9 @@ def _loglik_device(G, freq, N, L, K):
 
 @pytest.mark.parametrize("N", [5, 701, 5003])
 def test_loglik_packed2_every_cluster_count(N):
-    """Every K from 1 to 17 against float64: the FMA form (K = 1, 2, 5, 6, 9,
-    10, 13, 14: 1, 2, 6, 10 or 14 columns, 16, 4 or 2 individuals per thread)
-    and the table form (the other K, 4 to 16 columns, two groups at K = 17);
+    """Every K from 1 to 17 against float64: the FMA form (K = 1, 2, 5, 6, 13,
+    14: 1, 2, 6 or 14 columns, 16, 4 or 2 individuals per thread) and the
+    table form (the other K, 4 to 16 columns, two groups at K = 17);
     N below one genotype word, N with a partial last word, and N spanning
     several CTA columns of every instantiation."""
     L = 900 if N > 1000 else 1500

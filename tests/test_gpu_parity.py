@@ -102,9 +102,9 @@ def test_update_p(data):
         assert (u == 0).mean() > 0.99
 
 
-# Packed data: K = 1, 2, 6, 10 and 13 take the FMA form's 1-, 2-, 6-, 10- and
-# 14-column kernels, K = 3 the table form's 4 columns, K = 20 two table
-# groups of 16; general data: the table form's 4 and 12 columns
+# Packed data: K = 1, 2, 6 and 13 take the FMA form's 1-, 2-, 6- and
+# 14-column kernels, K = 3 and 10 the table form's 4 and 12 columns, K = 20
+# two table groups of 16; general data: the table form's 4 and 12 columns
 @pytest.mark.parametrize("packed,K", [(True, 1), (True, 2), (True, 3), (False, 3), (True, 6), (True, 10), (False, 10),
                                       (True, 13), (True, 20)])
 def test_loglik_and_labels_noadmix(packed, K):

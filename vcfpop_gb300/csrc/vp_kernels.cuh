@@ -333,8 +333,8 @@ __global__ void k_update_p_ctr(const DevChain* chains, const int4* map = nullptr
 // by the sampling kernel. Biallelic diploid data: each 32-locus slice of the
 // per-genotype log-probability table is staged in shared memory and folded
 // into a table per locus pair (16 code pairs: the sum of the two loci's
-// entries), so one 16-byte shared load and four adds serve two loci and four
-// clusters; the slice's genotype words are staged transposed, so a thread
+// entries, rows placed by ll_pair_mul), so one 16-byte shared load and four
+// adds serve two loci and four clusters; the slice's genotype words are staged transposed, so a thread
 // takes the codes of four loci with one 16-byte load. FP32 sums over a slice
 // are folded into Kahan-compensated FP32 totals (FP64 adds are slow on this
 // part), converted to FP64 once per chunk.
@@ -368,13 +368,24 @@ __device__ __forceinline__ void kahan_fold(float* acc, float* s, float* cmp) {
 // so rows that differ by fewer than 8 land on different banks
 template <int KC>
 __host__ __device__ constexpr int ll_stride() { return (KC / 4) % 2 ? KC : KC + 4; }
+// Row of code pair (a, b) in a locus pair's table: a + PB b. With PB = 11 the
+// eight pairs without a missing code and other than (2, 2), the common ones,
+// sit in eight different bank groups (each row an odd number of 16-byte
+// chunks), so a quarter warp's gathers conflict only on rare pairs; the table
+// spans 37 rows instead of 16, which static shared memory holds up to 12
+// columns (16 columns keep a + 4b).
+template <int KC>
+__host__ __device__ constexpr int ll_pair_mul() { return KC <= 12 ? 11 : 4; }
+template <int KC>
+__host__ __device__ constexpr int ll_pair_rows() { return 3 + 3 * ll_pair_mul<KC>() + 1; }
 template <int KC>
 __global__ void __launch_bounds__(LT_BLOCK, 3) k_loglik(const DevChain* chains, int kgroups, int force, const int4* map = nullptr) {
     constexpr int TS = ll_stride<KC>();
     constexpr int GW = LT_BLOCK / 16;          // genotype words per CTA and locus
     constexpr int GS = LL_SL + 4;              // padded row of the transposed words
     __shared__ __align__(16) float sT[2][LL_SL][4][TS];       // two slices in flight
-    __shared__ __align__(16) float sP[LL_SL / 2][16][TS];
+    constexpr int PB = ll_pair_mul<KC>();
+    __shared__ __align__(16) float sP[LL_SL / 2][ll_pair_rows<KC>()][TS];
     __shared__ __align__(16) uint32_t sG[2][GW][GS];
     const VBlock vb = vblock(map);
     const DevChain& c = chains[vb.z / kgroups];
@@ -426,20 +437,21 @@ __global__ void __launch_bounds__(LT_BLOCK, 3) k_loglik(const DevChain* chains, 
                 cp_async_wait<0>();
             }
             __syncthreads();
-            // pair rows: sP[p][a | b << 2] = sT[2p][a] + sT[2p + 1][b]
+            // pair rows: sP[p][a + PB b] = sT[2p][a] + sT[2p + 1][b]
             for (int j = threadIdx.x; j < (LL_SL / 2) * 16 * Q4; j += LT_BLOCK) {
                 const int q = j % Q4, cp = (j / Q4) & 15, p = j / (16 * Q4);
                 const float4 x = *reinterpret_cast<const float4*>(&sT[buf][2 * p][cp & 3][4 * q]);
                 const float4 y = *reinterpret_cast<const float4*>(&sT[buf][2 * p + 1][cp >> 2][4 * q]);
-                *reinterpret_cast<float4*>(&sP[p][cp][4 * q]) = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+                *reinterpret_cast<float4*>(&sP[p][(cp & 3) + PB * (cp >> 2)][4 * q]) =
+                    make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
             }
             __syncthreads();
             const uint4* gw = reinterpret_cast<const uint4*>(&sG[buf][wsel][0]);
 #pragma unroll 2
             for (int q = 0; q < LL_SL / 4; ++q) {
                 const uint4 g = gw[q];
-                const int ca = ((g.x >> sh) & 3) | (((g.y >> sh) & 3) << 2);
-                const int cb = ((g.z >> sh) & 3) | (((g.w >> sh) & 3) << 2);
+                const int ca = ((g.x >> sh) & 3) + PB * ((g.y >> sh) & 3);
+                const int cb = ((g.z >> sh) & 3) + PB * ((g.w >> sh) & 3);
                 const float4* ta = reinterpret_cast<const float4*>(&sP[2 * q][ca][0]);
                 const float4* tb = reinterpret_cast<const float4*>(&sP[2 * q + 1][cb][0]);
 #pragma unroll
@@ -495,16 +507,15 @@ struct LfShape {
     static constexpr int GW = LL_BLOCK * M / 16;                              // genotype words per CTA and locus
     static constexpr int KQ = (KC + 3) / 4;                                   // 16-byte chunks of a staged row
 };
-// The FMA form runs where the table form's groups of four cluster columns
-// would be padded most: K = 1, 2 and K mod 4 = 1 or 2 up to 14. Measured at
-// N = 10,000 over 58,027 loci (ms, FMA form / table form with 256-individual
-// CTAs): K = 1 0.24 / 0.34, K = 2 0.32 / 0.34, K = 5, 6 0.49 / 0.56, K = 9, 10
-// 0.74 / 0.74, K = 13, 14 0.98 / 1.00; at K = 3, 4, 7, 8 the table form is
-// ahead (0.34 and 0.57 against 0.40 and 0.65 for the FMA form's 4- and
-// 8-column kernels, which are not kept). Its columns: K itself for K <= 2,
-// else 6, 10 or 14.
-__host__ __device__ constexpr bool lf_form(int K) { return K <= 14 && (K % 4 == 1 || K % 4 == 2); }
-__host__ __device__ constexpr int lf_kc(int K) { return K <= 2 ? K : K <= 6 ? 6 : K <= 10 ? 10 : 14; }
+// The FMA form runs where it measured ahead of the table form (N = 10,000
+// over 58,027 loci, ms, FMA form / table form with 256-individual CTAs and
+// the spread pair rows): K = 1 0.24 / 0.34, K = 2 0.32 / 0.33, K = 5, 6
+// 0.49 / 0.52, K = 13, 14 0.98 / 1.00. The table form takes the rest: K = 3,
+// 4, 7, 8 in 0.33 and 0.52 (the FMA form's 4- and 8-column kernels took 0.40
+// and 0.65), K = 9..12 in 0.67 (its 10-column kernel 0.74), K = 15, 16 and
+// K > 16. Its columns: K itself for K <= 2, else 6 or 14.
+__host__ __device__ constexpr bool lf_form(int K) { return K <= 2 || K == 5 || K == 6 || K == 13 || K == 14; }
+__host__ __device__ constexpr int lf_kc(int K) { return K <= 2 ? K : K <= 6 ? 6 : 14; }
 __host__ __device__ constexpr int lf_individuals(int kc) { return LL_BLOCK * (kc <= 2 ? 16 : kc <= 6 ? 4 : 2); }
 template <int KC>
 __global__ void __launch_bounds__(LL_BLOCK) k_loglik_fma(const DevChain* chains, int kgroups, int force,

@@ -304,7 +304,6 @@ int lf_resident(int kc) {
             case 1: fn = (const void*)k_loglik_fma<1>; break;
             case 2: fn = (const void*)k_loglik_fma<2>; break;
             case 6: fn = (const void*)k_loglik_fma<6>; break;
-            case 10: fn = (const void*)k_loglik_fma<10>; break;
             default: fn = (const void*)k_loglik_fma<14>; break;
         }
         int n = 0;
@@ -342,7 +341,6 @@ int launch_loglik(vp_chain* c, int force) {
             case 1: SL(c, k_loglik_fma<1>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
             case 2: SL(c, k_loglik_fma<2>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
             case 6: SL(c, k_loglik_fma<6>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
-            case 10: SL(c, k_loglik_fma<10>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
             default: SL(c, k_loglik_fma<14>, (g), (LL_BLOCK), 0, 2, c->kgroups, force); break;
         }
         return VP_OK;
@@ -2740,7 +2738,6 @@ int ll_run(LLPlan& pl, const uint32_t* geno, const float* freq, double* ll, void
             case 1: k_loglik_fma<1><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
             case 2: k_loglik_fma<2><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
             case 6: k_loglik_fma<6><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
-            case 10: k_loglik_fma<10><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
             default: k_loglik_fma<14><<<g, LL_BLOCK, 0, s>>>(d, pl.kgroups, 1); break;
         }
     } else {
