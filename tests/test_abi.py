@@ -206,3 +206,23 @@ def test_collected_reference_cycle_never_destroys_after_close(monkeypatch):
     assert names.count("close") == 1
     closed_at = names.index("close")
     assert "destroy" not in names[closed_at:]
+
+
+def test_general_locus_filter_rejects_bad_arguments():
+    """vp_locus_filter_general checks its sizes before any device call: a
+    ploidy outside 1..10, more individuals than its genotype tables' hash
+    maps index (2^28), an allele count outside 1..64."""
+    import numpy as np
+    L = B.lib()
+    f = S.locus_filter_spec()
+    G = np.zeros(16, dtype=np.int8)
+    k = np.array([2], dtype=np.int32)
+    bad_k = np.array([65], dtype=np.int32)
+    keep = np.zeros(1, dtype=np.uint8)
+    call = lambda n_ind, vmax, kk: L.vp_locus_filter_general(G.ctypes.data, None, 1, n_ind, vmax, kk.ctypes.data,
+                                                             ctypes.byref(f), 0, keep.ctypes.data, None)
+    assert call(4, 11, k) == B.VP_E_ARG
+    assert call((1 << 28) + 1, 2, k) == B.VP_E_ARG
+    assert "2^28" in L.vp_last_error().decode()
+    assert call(4, 2, bad_k) == B.VP_E_ARG
+    assert "alleles" in L.vp_last_error().decode()

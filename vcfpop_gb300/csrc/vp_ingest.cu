@@ -1193,6 +1193,11 @@ extern "C" int vp_locus_filter_general(const int8_t* alleles, const int8_t* alle
         vp_set_error("bad arguments");
         return VP_E_ARG;
     }
+    // the genotype tables' hash maps index their entries with 32-bit masks
+    if (n_ind > (1 << 28)) {
+        vp_set_error("%d individuals: at most 2^28 for the genotype tables", n_ind);
+        return VP_E_ARG;
+    }
     for (int64_t l = 0; l < n_loc; ++l)
         if (n_alleles[l] < 1 || n_alleles[l] > 64) {
             vp_set_error("locus %lld has %d alleles (1 to 64)", (long long)(l + 1), n_alleles[l]);
@@ -1207,8 +1212,9 @@ extern "C" int vp_locus_filter_general(const int8_t* alleles, const int8_t* alle
     CKI(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     const size_t gb = (size_t)n_loc * n_ind * vmax, tb = alleles_table ? gb : 0, kb = (size_t)n_loc * 4,
                  sb = stats ? (size_t)n_loc * VP_LOCUS_STATS * 8 : 0;
+    // hash entries: a power of two, at least twice the individuals
     uint32_t H = 64;
-    while (H < 2u * (uint32_t)n_ind) H <<= 1;
+    while ((uint64_t)H < 2ull * (uint64_t)n_ind) H <<= 1;
     int nsm = 132;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
     // a warp per block, 16 blocks per SM, scratch held under 2 GiB (fewer
